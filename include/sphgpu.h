@@ -1,0 +1,214 @@
+/*
+ * sphgpu.h -- C ABI of the GB300-native SPH hydro package (libsphgpu.so).
+ *
+ * The library replaces, on one GPU, the ideal-gas SPH hot path of Spheral:
+ * the connectivity build, the density sum, the SPH pair loop with the
+ * TableKernel, Monaghan-Gingold viscosity and compatible-energy pair work,
+ * the SPH smoothing-scale (IdealH) update, the TreeGravity walk and the
+ * CheapSynchronousRK2 state update.  All particle state stays resident on the
+ * device between calls; host arrays cross the boundary only in
+ * sphgpu_set_particles / sphgpu_get_field / sphgpu_set_field.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: SPHGPU_OK (0) or one of the
+ *    SPHGPU_E_* codes below; sphgpu_last_error() gives a readable message.
+ *    No C++ exception crosses this boundary (the reference raises
+ *    VERIFYError, src/Utilities/DBC.hh:175-183; a C++ shim maps non-zero
+ *    codes back to that).
+ *  - Arrays are host pointers in the reference's FieldList layouts:
+ *    Vector = 3 doubles per node, SymTensor = 6 doubles per node in the order
+ *    (xx, xy, xz, yy, yz, zz), Tensor = 9 doubles row-major (xx, xy, xz, yx,
+ *    ..., zz).  Node order is the caller's order and is preserved.
+ *  - Calls on one handle are synchronous on a library-owned CUDA stream and
+ *    must not overlap (the reference calls packages from one host thread,
+ *    src/Integrator/Integrator.cc:219-230).
+ *
+ * Reference interfaces each entry point replaces are cited as
+ * path:line inside the llnl/spheral source tree.
+ */
+#ifndef SPHGPU_H
+#define SPHGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGPU_OK 0
+#define SPHGPU_E_CUDA 1         /* a CUDA runtime call failed                        */
+#define SPHGPU_E_ARG 2          /* bad argument (null pointer, size, unknown name)   */
+#define SPHGPU_E_UNSUPPORTED 3  /* input outside the supported path (e.g. non-isotropic H) */
+#define SPHGPU_E_OVERFLOW 4     /* a capacity limit was exceeded                     */
+#define SPHGPU_E_NAN 5          /* non-finite or non-physical state detected         */
+#define SPHGPU_E_TIMEOUT 6      /* a bounded device wait ran out                     */
+#define SPHGPU_E_STATE 7        /* call out of order (e.g. step before set_particles) */
+
+#define SPHGPU_PRECISION_FP64 0   /* every pair sum in FP64                               */
+#define SPHGPU_PRECISION_FP32 1   /* FP32 pair loop on cell-relative positions, compensated sums */
+
+#define SPHGPU_BOUNDARY_PERIODIC 0
+#define SPHGPU_BOUNDARY_REFLECTING 1
+
+#define SPHGPU_DENSITY_RIGOROUS_SUM 0   /* MassDensityType::RigorousSumDensity */
+#define SPHGPU_DENSITY_INTEGRATE 1      /* MassDensityType::IntegrateDensity   */
+
+typedef struct sphgpu_ctx* sphgpu_handle;
+
+/* Package, artificial-viscosity, integrator and gravity settings.  Field
+ * meanings follow the reference constructors:
+ *   SPH(...) factory             src/SPH/SPHHydros.py:9-33
+ *   SPH<Dim<3>> constructor      src/SPH/SPH.cc:43-79
+ *   MonaghanGingoldViscosity     src/ArtificialViscosity/MonaghanGingoldViscosity.cc:25-37
+ *   ArtificialViscosityHandle    src/ArtificialViscosity/ArtificialViscosityHandle.cc:36-54 (epsilon2)
+ *   Integrator dtMin/dtMax/dtGrowth  src/Integrator/Integrator.cc:43-47
+ *   OctTreeGravity(G, softeningLength, opening, ftimestep) src/Gravity/TreeGravity.cc:88-115 */
+typedef struct sphgpu_config {
+  int num_table_points;             /* TableKernel(BSplineKernel3d(), numPoints)           */
+  double cfl;
+  int use_velocity_magnitude_for_dt;
+  int compatible_energy;            /* compatibleEnergyEvolution                           */
+  int gradh_correction;
+  int xsph;
+  int correct_velocity_gradient;
+  int sum_mass_density_over_all_nodelists;
+  int density_update;               /* SPHGPU_DENSITY_*                                    */
+  double eps_tensile, n_tensile;
+  double Cl, Cq, eps2;
+  int linear_in_expansion, quadratic_in_expansion;
+  double dt_min, dt_max, dt_growth, last_dt, time;
+  int gravity;
+  double G, softening, opening, ftimestep;
+  int precision;                    /* SPHGPU_PRECISION_*                                  */
+  int device;                       /* CUDA device ordinal                                 */
+} sphgpu_config;
+
+/* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,
+ * compatible energy, grad-h on, XSPH off in this path, corrected velocity
+ * gradient, RigorousSumDensity), MG Cl = Cq = 1, epsilon2 = 1e-2, FP64.
+ * Replaces: the keyword defaults of src/SPH/SPHHydros.py:9-33. */
+void sphgpu_default_config(sphgpu_config* cfg);
+
+/* Create a context on cfg->device.  Replaces: SPH<Dim<3>>::SPH
+ * (src/SPH/SPH.cc:43-79) together with its Q sub-package and the
+ * SPHSmoothingScale post sub-package (src/SPH/SPHHydros.py:125-140). */
+int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out);
+int sphgpu_destroy(sphgpu_handle h);
+const char* sphgpu_last_error(sphgpu_handle h);
+
+/* Build the cubic B-spline TableKernel on the host into caller buffers.
+ * w, grad, grad2: 3*(n1+1) coefficients each (n1 = (numPoints|1 - 1)/2 - 1);
+ * nperh, wsum: 2*numPoints values each (Hermite knot values then slopes);
+ * meta[9] = {n1, xstep, numPoints, nperh_xmin, nperh_xmax, wsum_xmin,
+ * wsum_xmax, minNperh, maxNperh}.
+ * Replaces: TableKernel<Dim<3>>::TableKernel (src/Kernel/TableKernel.cc:169-209). */
+int sphgpu_build_bspline_table(int num_points, double* w, double* grad, double* grad2,
+                               double* nperh, double* wsum, double* meta);
+
+/* Install a kernel table (the product of a reference TableKernel or of
+ * sphgpu_build_bspline_table; same layouts).  Replaces: the TableKernelView
+ * handed to the pair loops (src/Kernel/TableKernelView.hh:17-81). */
+int sphgpu_set_kernel_table(sphgpu_handle h, const double* w, const double* grad, const double* grad2,
+                            const double* nperh, const double* wsum, const double* meta);
+
+/* Per-NodeList parameters.  Replaces: FluidNodeList(name, eos, ..., hmin,
+ * hmax, hminratio, nPerh, maxNumNeighbors, rhoMin, rhoMax)
+ * (src/NodeList/FluidNodeLists.py:15-47) + GammaLawGas(gamma)
+ * (src/Material/GammaLawGas.cc:185-243). */
+int sphgpu_set_nodelist(sphgpu_handle h, int nodelist, double nPerh, double hmin, double hmax,
+                        double rhoMin, double rhoMax, double gamma);
+
+/* Axis-aligned boundary.  type SPHGPU_BOUNDARY_PERIODIC: planes at lo and hi.
+ * type SPHGPU_BOUNDARY_REFLECTING: one wall, at lo with normal +axis
+ * (wall_high = 0) or at hi with normal -axis (wall_high = 1).
+ * Replaces: PeriodicBoundary(plane1, plane2) (src/Boundary/PeriodicBoundary.cc:54-63)
+ * and ReflectingBoundary(plane) (src/Boundary/ReflectingBoundary.cc:140-166),
+ * whose ghost nodes become implicit periodic/mirror images. */
+int sphgpu_add_boundary(sphgpu_handle h, int type, int axis, double lo, double hi, int wall_high);
+
+/* Upload n internal nodes (host arrays, caller order).  H must be isotropic
+ * (H = I/h, the form SPHSmoothingScale maintains); otherwise
+ * SPHGPU_E_UNSUPPORTED.  nodelist may be NULL (all zero).
+ * Replaces: the registered state FieldLists of SPHBase::registerState
+ * (src/SPH/SPHBase.cc:203-263). */
+int sphgpu_set_particles(sphgpu_handle h, long n, const double* pos, const double* vel, const double* mass,
+                         const double* rho, const double* eps, const double* H, const int* nodelist);
+
+/* Pressure, sound speed and grad-h correction of the current state.
+ * Replaces: SPHBase::initializeProblemStartupDependencies (src/SPH/SPHBase.cc:152-197). */
+int sphgpu_initialize(sphgpu_handle h);
+
+/* Rebuild the neighbour lists from the current positions and H.
+ * Replaces: ConnectivityMap::computeConnectivity (src/Neighbor/ConnectivityMap.cc:747-1029)
+ * after Integrator::setGhostNodes (src/Integrator/Integrator.cc:372-540). */
+int sphgpu_connectivity(sphgpu_handle h);
+
+/* Replace the mass density by the SPH sum.  Replaces: computeSPHSumMassDensity
+ * (src/SPH/computeSPHSumMassDensity.cc:15-87) via SPHBase::preStepInitialize. */
+int sphgpu_sum_density(sphgpu_handle h);
+
+/* Grad-h correction.  Replaces: computeSPHOmegaGradhCorrection
+ * (src/SPH/computeSPHOmegaGradhCorrection.cc:15-116) via SPHBase::postStateUpdate. */
+int sphgpu_gradh(sphgpu_handle h);
+
+/* Evaluate all derivatives on the current state with the current neighbour
+ * lists.  Replaces: SPH::evaluateDerivatives (src/SPH/SPH.cc:143-555),
+ * SPHSmoothingScale::evaluateDerivatives (src/SmoothingScale/SPHSmoothingScale.cc:101-275),
+ * TreeGravity::evaluateDerivatives (src/Gravity/TreeGravity.cc:146-331) when
+ * gravity is on, and SPHBase::finalizeDerivatives (src/SPH/SPHBase.cc:499-521). */
+int sphgpu_evaluate_derivatives(sphgpu_handle h);
+
+/* Time-step vote (already multiplied by cfl).  reason: 0 sound speed,
+ * 1 artificial viscosity, 2 velocity divergence, 3 acceleration,
+ * 4 velocity magnitude, 5 pairwise velocity difference, 6 gravity.
+ * Replaces: GenericHydro::dt (src/Physics/GenericHydro.cc:113-381) and
+ * TreeGravity::dt (src/Gravity/TreeGravity.cc:484-520). */
+int sphgpu_dt(sphgpu_handle h, double* dt, int* reason);
+
+/* One CheapSynchronousRK2 step bounded by max_time; *dt_out gets the step.
+ * Replaces: Integrator::step (src/Integrator/Integrator.cc:67-110) ->
+ * CheapSynchronousRK2::step (src/Integrator/CheapSynchronousRK2.cc:40-132). */
+int sphgpu_step(sphgpu_handle h, double max_time, double* dt_out);
+
+/* nsteps calls of sphgpu_step (stops early at max_time). */
+int sphgpu_advance(sphgpu_handle h, int nsteps, double max_time);
+
+/* Download / overwrite a field by reference name (caller node order).
+ * Names: position velocity mass massDensity specificThermalEnergy H pressure
+ * soundSpeed omegaGradh massDensitySum normalization DxDt DvDt DrhoDt DepsDt
+ * DvDx internalDvDx gradRho M localM maxViscousPressure effViscousPressure
+ * XSPHWeightSum XSPHDeltaV DHDt Hideal massZerothMoment massFirstMoment
+ * DvDtGravity potential DepsDtCompatible numNeighbors.
+ * *ncomp (may be NULL) receives the component count.
+ * Replaces: State/StateDerivatives::fields(name, ...) (src/DataBase/State.hh:58-118). */
+int sphgpu_get_field(sphgpu_handle h, const char* name, double* out, int* ncomp);
+int sphgpu_set_field(sphgpu_handle h, const char* name, const double* in);
+
+/* Ordered neighbour pairs (i, j, image) in caller node indices; image packs
+ * 2 bits per axis (0 none, 1 low-side image / lo mirror, 2 high-side image /
+ * hi mirror).  Call with i == NULL to get *npairs only.
+ * Replaces: ConnectivityMap::nodePairList (src/Neighbor/ConnectivityMap.hh). */
+int sphgpu_get_pairs(sphgpu_handle h, int* i, int* j, int* image, long* npairs);
+
+/* Conserved totals in FP64: {mass, px, py, pz, kinetic, thermal, gravity
+ * potential (1/2 sum m phi), total}.  Replaces: SpheralConservation
+ * (src/SimulationControl/SpheralConservation.py:54-150). */
+int sphgpu_conservation(sphgpu_handle h, double out[8]);
+
+/* Integrator clock: time, last dt, cycle. */
+int sphgpu_get_time(sphgpu_handle h, double* time, double* last_dt, long* cycle);
+int sphgpu_num_particles(sphgpu_handle h, long* n);
+
+/* Per-kernel device timing.  enable != 0 records CUDA events around each
+ * kernel of the next calls; sphgpu_profile_get returns, for kernel `name`,
+ * the number of launches and the summed milliseconds. */
+int sphgpu_profile_enable(sphgpu_handle h, int enable);
+int sphgpu_profile_get(sphgpu_handle h, const char* name, long* launches, double* ms);
+int sphgpu_profile_reset(sphgpu_handle h);
+/* Number of kernels this library launched on the handle since creation. */
+int sphgpu_launch_count(sphgpu_handle h, long* launches);
+/* Wait for all work on the handle's stream. */
+int sphgpu_synchronize(sphgpu_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPHGPU_H */

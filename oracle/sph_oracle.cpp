@@ -1,0 +1,1480 @@
+// =============================================================================
+// CPU ORACLE -- test infrastructure only.
+//
+// A plain C++17 / OpenMP FP64 restatement of the reference's ideal-gas SPH
+// hydro step, written to check the GPU product path.  Nothing in the product
+// (spheral_gb300/, include/) links or calls this file; only the tests, the
+// smoke check and the CPU-baseline leg of bench.py load it.
+//
+// It follows the reference's own formulation literally:
+//   * ghost nodes are explicit extra nodes created boundary by boundary
+//     (PlanarBoundary / PeriodicBoundary / ReflectingBoundary), and
+//   * every sweep walks the UNORDERED pair list (internal-internal pairs once,
+//     internal-ghost pairs once) with thread-private accumulators that are
+//     summed at the end (FieldList::threadCopy / threadReduce),
+// so that it can also serve as the timed "reference CPU path".
+//
+// Reference files restated (paths inside the llnl/spheral source tree):
+//   src/Kernel/BSplineKernelInline.hh:28-93            cubic B-spline
+//   src/Kernel/TableKernel.cc:23-66,169-209            table + nperh lookups
+//   src/Utilities/QuadraticInterpolator.cc:60-100      quadratic table fit
+//   src/Utilities/QuadraticInterpolatorViewInline.hh   lookups
+//   src/Utilities/CubicHermiteInterpolator.cc:95-180   Hermite knots, monotonic
+//   src/Utilities/CubicHermiteInterpolatorViewInline.hh
+//   src/Utilities/bisectRoot.hh:20-74
+//   src/Neighbor/ConnectivityMap.cc:747-1029           pair criterion / pairs
+//   src/Neighbor/ConnectivityMapInline.hh:296-309
+//   src/Boundary/PlanarBoundary.cc:102-334, PeriodicBoundary.cc:77-128,
+//   src/Boundary/findNodesTouchingThroughPlanes.cc:13-76,
+//   src/Boundary/mapPositionThroughPlanes.hh:17-27, Utilities/pointDistances.hh:69-74
+//   src/SPH/computeSPHSumMassDensity.cc:15-87
+//   src/SPH/computeSPHOmegaGradhCorrection.cc:15-116
+//   src/SPH/SPH.cc:166-555                             pair loop + finalize
+//   src/ArtificialViscosity/MonaghanGingoldViscosity.cc:41-101
+//   src/SmoothingScale/SPHSmoothingScale.cc:101-275
+//   src/Physics/GenericHydro.cc:113-381                dt
+//   src/Hydro/SpecificThermalEnergyPolicy.cc:47-174    compatible energy
+//   src/Integrator/CheapSynchronousRK2.cc:40-132, Integrator.cc:67-169
+//   src/DataBase/State.cc:222-340 (+ Increment/Replace bounded policies)
+//   src/Material/GammaLawGas.cc:185-243
+//   src/Geometry/GeomSymmetricTensorInline.hh:1650-1747,2230-2260
+//   src/Geometry/GeomTensorInline.hh:1885-1972
+//   src/Gravity/TreeGravity.cc:55-82,146-480,819-932, TreeGravityInline.hh:38-165
+//
+// Third-party arithmetic: the reference fits each quadratic table interval
+// with Eigen's 3x3 inverse and solves the Hermite knot system with Eigen's
+// SparseLU (Eigen 5.0.0, not vendored).  Here the 3x3 inverse is the cofactor
+// formula and the tridiagonal system is solved with the Thomas algorithm: the
+// coefficients agree with the reference to rounding, bit parity is unpinned.
+// =============================================================================
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+using std::vector;
+static const double kTiny30 = 1.0e-30;
+static const double kDblEps = std::numeric_limits<double>::epsilon();
+
+//------------------------------------------------------------------------------
+// Small geometry types (component orders as in GeomVector / GeomTensor /
+// GeomSymmetricTensor of the reference).
+//------------------------------------------------------------------------------
+struct V3 { double x = 0, y = 0, z = 0; };
+struct ST { double xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0; };   // symmetric
+struct T9 { double xx = 0, xy = 0, xz = 0, yx = 0, yy = 0, yz = 0, zx = 0, zy = 0, zz = 0; };
+
+static inline V3 sub(const V3& a, const V3& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V3 add(const V3& a, const V3& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline V3 mul(const V3& a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 mul(double s, const V3& a) { return {s * a.x, s * a.y, s * a.z}; }
+static inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline double mag2(const V3& a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+static inline double mag(const V3& a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+static inline V3 unitVector(const V3& a) {            // GeomVectorInline.hh:998
+  const double m = mag(a);
+  return m > 1.0e-50 ? V3{a.x / m, a.y / m, a.z / m} : V3{1.0, 0.0, 0.0};
+}
+static inline V3 dotSV(const ST& H, const V3& r) {    // GeomSymmetricTensorInline.hh:1773
+  return {H.xx * r.x + H.xy * r.y + H.xz * r.z,
+          H.xy * r.x + H.yy * r.y + H.yz * r.z,
+          H.xz * r.x + H.yz * r.y + H.zz * r.z};
+}
+static inline ST scaleS(const ST& H, double s) {
+  return {H.xx * s, H.xy * s, H.xz * s, H.yy * s, H.yz * s, H.zz * s};
+}
+static inline ST scaleS(double s, const ST& H) {
+  return {s * H.xx, s * H.xy, s * H.xz, s * H.yy, s * H.yz, s * H.zz};
+}
+static inline double detS(const ST& H) {               // GeomSymmetricTensorInline.hh:1740
+  return (H.xx * H.yy * H.zz + H.xy * H.yz * H.xz + H.xz * H.xy * H.yz -
+          H.xx * H.yz * H.yz - H.xy * H.xy * H.zz - H.xz * H.yy * H.xz);
+}
+static inline double maxAbsS(const ST& H) {
+  return std::max(std::fabs(H.xx), std::max(std::fabs(H.xy), std::max(std::fabs(H.xz),
+         std::max(std::fabs(H.yy), std::max(std::fabs(H.yz), std::fabs(H.zz))))));
+}
+// Eberly closed-form eigenvalues, GeomSymmetricTensorInline.hh:2230-2260.
+static inline V3 eigenValuesS(const ST& H) {
+  const double onethird = 1.0 / 3.0;
+  const double sqrt3 = std::sqrt(3.0);
+  const double fscale = std::max(10.0 * kDblEps, maxAbsS(H));
+  const double fscalei = 1.0 / fscale;
+  const double a00 = H.xx * fscalei, a01 = H.xy * fscalei, a02 = H.xz * fscalei;
+  const double a11 = H.yy * fscalei, a12 = H.yz * fscalei, a22 = H.zz * fscalei;
+  const double c0 = a00 * a11 * a22 + 2.0 * a01 * a02 * a12 - a00 * a12 * a12 - a11 * a02 * a02 - a22 * a01 * a01;
+  const double c1 = a00 * a11 - a01 * a01 + a00 * a22 - a02 * a02 + a11 * a22 - a12 * a12;
+  const double c2 = a00 + a11 + a22;
+  const double c2Div3 = c2 * onethird;
+  const double aDiv3 = std::min(0.0, onethird * (c1 - c2 * c2Div3));
+  const double mbDiv2 = 0.5 * (c0 + c2Div3 * (2.0 * c2Div3 * c2Div3 - c1));
+  const double q = std::min(0.0, mbDiv2 * mbDiv2 + aDiv3 * aDiv3 * aDiv3);
+  const double magv = std::sqrt(-aDiv3);
+  const double angle = std::atan2(std::sqrt(-q), mbDiv2) * onethird;
+  const double cs = std::cos(angle), sn = std::sin(angle);
+  return {fscale * (c2Div3 + 2.0 * magv * cs),
+          fscale * (c2Div3 - magv * (cs + sqrt3 * sn)),
+          fscale * (c2Div3 - magv * (cs - sqrt3 * sn))};
+}
+static inline double maxElem(const V3& v) { return std::max(v.x, std::max(v.y, v.z)); }
+static inline double minElem(const V3& v) { return std::min(v.x, std::min(v.y, v.z)); }
+static inline bool isIsotropic(const ST& H) {
+  return H.xy == 0.0 && H.xz == 0.0 && H.yz == 0.0 && H.xx == H.yy && H.xx == H.zz;
+}
+static inline T9 dyad(const V3& a, const V3& b) {     // GeomVectorInline.hh:946
+  return {a.x * b.x, a.x * b.y, a.x * b.z, a.y * b.x, a.y * b.y, a.y * b.z, a.z * b.x, a.z * b.y, a.z * b.z};
+}
+static inline void addT(T9& a, const T9& b) {
+  a.xx += b.xx; a.xy += b.xy; a.xz += b.xz; a.yx += b.yx; a.yy += b.yy; a.yz += b.yz; a.zx += b.zx; a.zy += b.zy; a.zz += b.zz;
+}
+static inline void subT(T9& a, const T9& b) {
+  a.xx -= b.xx; a.xy -= b.xy; a.xz -= b.xz; a.yx -= b.yx; a.yy -= b.yy; a.yz -= b.yz; a.zx -= b.zx; a.zy -= b.zy; a.zz -= b.zz;
+}
+static inline T9 scaleT(double s, const T9& a) {
+  return {s * a.xx, s * a.xy, s * a.xz, s * a.yx, s * a.yy, s * a.yz, s * a.zx, s * a.zy, s * a.zz};
+}
+static inline double traceT(const T9& a) { return a.xx + a.yy + a.zz; }
+static inline double detT(const T9& a) {               // GeomTensorInline.hh:1969
+  return (a.xx * a.yy * a.zz + a.xy * a.yz * a.zx + a.xz * a.yx * a.zy -
+          a.xx * a.yz * a.zy - a.xy * a.yx * a.zz - a.xz * a.yy * a.zx);
+}
+static inline T9 inverseT(const T9& a) {               // GeomTensorInline.hh:1885
+  const double d = detT(a);
+  return {(a.yy * a.zz - a.yz * a.zy) / d, (a.xz * a.zy - a.xy * a.zz) / d, (a.xy * a.yz - a.xz * a.yy) / d,
+          (a.yz * a.zx - a.yx * a.zz) / d, (a.xx * a.zz - a.xz * a.zx) / d, (a.xz * a.yx - a.xx * a.yz) / d,
+          (a.yx * a.zy - a.yy * a.zx) / d, (a.xy * a.zx - a.xx * a.zy) / d, (a.xx * a.yy - a.xy * a.yx) / d};
+}
+static inline T9 dotTT(const T9& a, const T9& b) {    // GeomTensorInline.hh:2031
+  return {a.xx * b.xx + a.xy * b.yx + a.xz * b.zx, a.xx * b.xy + a.xy * b.yy + a.xz * b.zy, a.xx * b.xz + a.xy * b.yz + a.xz * b.zz,
+          a.yx * b.xx + a.yy * b.yx + a.yz * b.zx, a.yx * b.xy + a.yy * b.yy + a.yz * b.zy, a.yx * b.xz + a.yy * b.yz + a.yz * b.zz,
+          a.zx * b.xx + a.zy * b.yx + a.zz * b.zx, a.zx * b.xy + a.zy * b.yy + a.zz * b.zy, a.zx * b.xz + a.zy * b.yz + a.zz * b.zz};
+}
+static inline double sgn(double x) { return x < 0.0 ? -1.0 : 1.0; }
+static inline double safeInv(double x, double fuzz = kTiny30) { return x / (x * x + fuzz); }
+static inline double safeInvVar(double x, double fuzz = kTiny30) { return sgn(x) / std::max(fuzz, std::fabs(x)); }
+static inline bool fuzzyEqual(double a, double b, double fuzz = 1.0e-15) {
+  return std::fabs(a - b) <= fuzz * std::max(1.0, std::fabs(a) + std::fabs(b));
+}
+static inline double pow4(double x) { return x * x * x * x; }
+static inline double rootnu3(double x) { return sgn(x) * std::pow(std::fabs(x), 0.3333333333333333); }
+
+//------------------------------------------------------------------------------
+// Cubic B-spline (3-D), BSplineKernelInline.hh:28-93.
+//------------------------------------------------------------------------------
+struct BSpline3 {
+  double A = 1.0 / M_PI;
+  double extent = 2.0;
+  double value(double eta, double Hdet) const {
+    if (eta < 1.0) { const double eta2 = eta * eta; return A * Hdet * (1.0 - 1.5 * eta2 + 0.75 * eta2 * eta); }
+    if (eta < 2.0) { const double d = 2.0 - eta; return A * Hdet * 0.25 * (d * d * d); }
+    return 0.0;
+  }
+  double grad(double eta, double Hdet) const {
+    if (eta < 1.0) return -A * Hdet * (3.0 - 2.25 * eta) * eta;
+    if (eta < 2.0) { const double d = 2.0 - eta; return -A * Hdet * 0.75 * (d * d); }
+    return 0.0;
+  }
+  double grad2(double eta, double Hdet) const {
+    if (eta < 1.0) return -A * Hdet * (3 - 4.5 * eta);
+    if (eta < 2.0) return A * Hdet * 1.5 * (2 - eta);
+    return 0.0;
+  }
+};
+
+//------------------------------------------------------------------------------
+// QuadraticInterpolator (QuadraticInterpolator.cc:60-100 + Inline.hh).
+//------------------------------------------------------------------------------
+struct QuadInterp {
+  size_t N1 = 0;
+  double xmin = 0, xmax = 0, xstep = 0;
+  vector<double> c;
+  template <class F>
+  void initialize(double x0_, double x1_, size_t n, const F& f) {
+    if (n % 2 == 0) ++n;
+    const double st = (x1_ - x0_) / (n - 1u);
+    vector<double> y(n);
+    for (size_t i = 0; i < n; ++i) y[i] = f(x0_ + i * st);
+    N1 = (n - 1u) / 2u - 1u;
+    xmin = x0_; xmax = x1_;
+    xstep = (x1_ - x0_) / (N1 + 1u);
+    c.assign(3 * (N1 + 1u), 0.0);
+    for (size_t i0 = 0; i0 <= N1; ++i0) {
+      const double a0 = xmin + i0 * xstep, a1 = a0 + 0.5 * xstep, a2 = a0 + xstep;
+      // A = [[1,a0,a0^2],[1,a1,a1^2],[1,a2,a2^2]] ; X = A^{-1} B (cofactor inverse)
+      const double m00 = 1.0, m01 = a0, m02 = a0 * a0;
+      const double m10 = 1.0, m11 = a1, m12 = a1 * a1;
+      const double m20 = 1.0, m21 = a2, m22 = a2 * a2;
+      const double C00 = m11 * m22 - m12 * m21, C01 = m12 * m20 - m10 * m22, C02 = m10 * m21 - m11 * m20;
+      const double det = m00 * C00 + m01 * C01 + m02 * C02;
+      const double inv[3][3] = {
+          {C00 / det, (m02 * m21 - m01 * m22) / det, (m01 * m12 - m02 * m11) / det},
+          {C01 / det, (m00 * m22 - m02 * m20) / det, (m02 * m10 - m00 * m12) / det},
+          {C02 / det, (m01 * m20 - m00 * m21) / det, (m00 * m11 - m01 * m10) / det}};
+      const double B0 = y[2 * i0], B1 = y[2 * i0 + 1], B2 = y[2 * i0 + 2];
+      for (int r = 0; r < 3; ++r) c[3 * i0 + r] = inv[r][0] * B0 + inv[r][1] * B1 + inv[r][2] * B2;
+    }
+  }
+  size_t lowerBound(double x) const {
+    return 3u * std::min(N1, size_t(std::max(0.0, x - xmin) / xstep));
+  }
+  double operator()(double x) const { const size_t i0 = lowerBound(x); return c[i0] + (c[i0 + 1] + c[i0 + 2] * x) * x; }
+  double at(double x, size_t i0) const { return c[i0] + (c[i0 + 1] + c[i0 + 2] * x) * x; }
+};
+
+//------------------------------------------------------------------------------
+// CubicHermiteInterpolator (CubicHermiteInterpolator.cc, ViewInline.hh).
+//------------------------------------------------------------------------------
+struct HermiteInterp {
+  size_t N = 0;
+  double xmin = 0, xmax = 0, xstep = 0;
+  vector<double> v;   // [0,N): values, [N,2N): gradients
+  template <class F>
+  void initialize(double x0_, double x1_, size_t n, const F& f) {
+    const double st = (x1_ - x0_) / (n - 1u);
+    vector<double> y(n);
+    for (size_t i = 0; i < n; ++i) y[i] = f(x0_ + i * st);
+    N = n; xmin = x0_; xmax = x1_;
+    xstep = (x1_ - x0_) / (N - 1u);
+    v.assign(2 * N, 0.0);
+    for (size_t i = 0; i < N; ++i) v[i] = y[i];
+    gradientKnots();
+  }
+  // Tridiagonal system of CubicHermiteInterpolator::initializeGradientKnots,
+  // solved with the Thomas algorithm.
+  void gradientKnots() {
+    vector<double> a(N, 0.0), b(N, 4.0), cc(N, 0.0), d(N, 0.0);
+    cc[0] = -1.0; a[N - 1] = -1.0;
+    d[0] = 3.0 * (v[1] - v[0]) / xstep;
+    d[N - 1] = 3.0 * (v[N - 1] - v[N - 2]) / xstep;
+    for (size_t k = 1; k + 1 < N; ++k) { a[k] = -0.5; cc[k] = -0.5; d[k] = 1.5 * (v[k + 1] - v[k - 1]) / xstep; }
+    vector<double> cp(N), dp(N);
+    cp[0] = cc[0] / b[0]; dp[0] = d[0] / b[0];
+    for (size_t k = 1; k < N; ++k) {
+      const double m = b[k] - a[k] * cp[k - 1];
+      cp[k] = cc[k] / m;
+      dp[k] = (d[k] - a[k] * dp[k - 1]) / m;
+    }
+    v[N + N - 1] = dp[N - 1];
+    for (size_t k = N - 1; k-- > 0;) v[N + k] = dp[k] - cp[k] * v[N + k + 1];
+  }
+  void makeMonotonic() {
+    vector<double> cg(N - 1);
+    const double dxInv = 1.0 / xstep;
+    for (size_t k = 0; k + 1 < N; ++k) cg[k] = (v[k + 1] - v[k]) * dxInv;
+    auto g = [&](size_t i) -> double& { return v[N + i]; };
+    for (size_t k = 1; k + 1 < N; ++k) {
+      if (cg[k - 1] * cg[k] <= 0.0) g(k) = 0.0;
+      if (cg[k] == 0.0) { g(k) = 0.0; g(k + 1) = 0.0; }
+    }
+    bool done = false;
+    while (!done) {
+      done = true;
+      for (size_t k = 0; k + 1 < N; ++k) {
+        double alpha = g(k) / cg[k], beta = g(k + 1) / cg[k];
+        if (alpha < 0.0) { g(k) = 0.0; alpha = 0.0; done = false; }
+        if (beta < 0.0) { g(k + 1) = 0.0; beta = 0.0; done = false; }
+        const double tau = 3.0 / std::sqrt(alpha * alpha + beta * beta);
+        if (tau < 1.0) { g(k) = 0.99 * tau * alpha * cg[k]; g(k + 1) = 0.99 * tau * beta * cg[k]; done = false; }
+      }
+    }
+  }
+  size_t lowerBound(double x) const { return std::min(N - 2u, size_t(std::max(0.0, x - xmin) / xstep)); }
+  double eval(double x, size_t i0) const {
+    const double t = std::max(0.0, std::min(1.0, (x - xmin - i0 * xstep) / xstep));
+    const double t2 = t * t, t3 = t * t2;
+    return ((2.0 * t3 - 3.0 * t2 + 1.0) * v[i0] + (-2.0 * t3 + 3.0 * t2) * v[i0 + 1u] +
+            xstep * ((t3 - 2.0 * t2 + t) * v[N + i0] + (t3 - t2) * v[N + i0 + 1u]));
+  }
+  double operator()(double x) const {
+    if (x < xmin) return v[0] + v[N] * (x - xmin);
+    if (x > xmax) return v[N - 1u] + v[2u * N - 1u] * (x - xmin);
+    return eval(x, lowerBound(x));
+  }
+};
+
+template <class F>
+static double bisectRoot(const F& f, double xmin, double xmax, double xacc = 1.0e-15, double yacc = 1.0e-10,
+                         unsigned maxIter = 100u) {
+  const double fxmin = f(xmin), fxmax = f(xmax);
+  if (fuzzyEqual(fxmin, 0.0, yacc)) return xmin;
+  if (fuzzyEqual(fxmax, 0.0, yacc)) return xmax;
+  double x0, x1;
+  if (fxmin < 0.0) { x0 = xmin; x1 = xmax; } else { x0 = xmax; x1 = xmin; }
+  unsigned iter = 0;
+  while (iter++ < maxIter) {
+    const double dx = 0.5 * (x1 - x0);
+    const double r = x0 + dx;
+    if (std::fabs(dx) <= xacc) return r;
+    const double fr = f(r);
+    if (fuzzyEqual(fr, 0.0, yacc)) return r;
+    if (fr < 0.0) x0 = r; else x1 = r;
+  }
+  return 0.0;
+}
+
+//------------------------------------------------------------------------------
+// TableKernel<Dim<3>> (TableKernel.cc:169-209).
+//------------------------------------------------------------------------------
+struct TableKernel {
+  QuadInterp W, gW, g2W;
+  HermiteInterp nperhLookup, wsumLookup;
+  double extent = 2.0, minNperh = 0, maxNperh = 0;
+  int numPoints = 0;
+  double kernelValueSPH(double eta) const { return eta < extent ? std::fabs(gW(eta)) : 0.0; }
+  double kernelValue(double eta, double Hdet) const { return eta < extent ? Hdet * W(eta) : 0.0; }
+  void kernelAndGradValue(double eta, double Hdet, double& w, double& g) const {
+    if (eta < extent) { const size_t i0 = W.lowerBound(eta); w = Hdet * W.at(eta, i0); g = Hdet * gW.at(eta, i0); }
+    else { w = 0.0; g = 0.0; }
+  }
+  double sumKernelValues(double nPerh) const {          // TableKernel.cc:53-66
+    const double deta = 1.0 / nPerh;
+    double result = 0.0, etar = deta;
+    while (etar < extent) {
+      const double q = etar / deta;
+      result += 4.0 * M_PI * (q * q) * kernelValueSPH(etar);
+      etar += deta;
+    }
+    return std::pow(result, 1.0 / 3.0);
+  }
+  void build(int nPoints, double minNperh_ = 0.25, double maxNperh_ = 64.0) {
+    BSpline3 k;
+    numPoints = nPoints;
+    extent = k.extent;
+    W.initialize(0.0, k.extent, nPoints, [&](double x) { return k.value(x, 1.0); });
+    gW.initialize(0.0, k.extent, nPoints, [&](double x) { return k.grad(x, 1.0); });
+    g2W.initialize(0.0, k.extent, nPoints, [&](double x) { return k.grad2(x, 1.0); });
+    maxNperh = maxNperh_;
+    minNperh = std::max(minNperh_, 1.1 / k.extent);
+    if (maxNperh <= minNperh) maxNperh = 4.0 * minNperh;
+    wsumLookup.initialize(minNperh, maxNperh, nPoints, [&](double x) { return sumKernelValues(x); });
+    nperhLookup.initialize(wsumLookup(minNperh), wsumLookup(maxNperh), nPoints, [&](double Wsum) {
+      return bisectRoot([&](double nperh) { return wsumLookup(nperh) - Wsum; }, minNperh, maxNperh);
+    });
+    wsumLookup.makeMonotonic();
+    nperhLookup.makeMonotonic();
+  }
+  double equivalentNodesPerSmoothingScale(double Wsum) const { return std::max(0.0, nperhLookup(Wsum)); }
+  double equivalentWsum(double nPerh) const { return std::max(0.0, wsumLookup(nPerh)); }
+};
+
+//------------------------------------------------------------------------------
+// Problem description.
+//------------------------------------------------------------------------------
+struct NodeListParams {
+  double nPerh = 1.51, hmin = 1e-20, hmax = 1e20, rhoMin = 1e-10, rhoMax = 1e10, gamma = 5.0 / 3.0;
+  double minP = -std::numeric_limits<double>::max(), maxP = std::numeric_limits<double>::max();
+};
+
+// One plane pair (periodic) or one plane (reflecting), axis-aligned.
+struct Boundary {
+  int type = 0;         // 0 periodic, 1 reflecting
+  int axis = 0;
+  double lo = 0, hi = 0;   // periodic: the two planes; reflecting: wall at lo (normal +) or hi (normal -)
+  int wallHigh = 0;        // reflecting: 0 -> wall at lo with normal +axis, 1 -> wall at hi with normal -axis
+  // ghost bookkeeping: parallel lists, per sub-boundary
+  vector<int> control[2], ghost[2];
+};
+
+struct Config {
+  int numTablePoints = 1000;
+  double cfl = 0.25;
+  int useVelocityMagnitudeForDt = 0;
+  int compatibleEnergy = 1;
+  int gradhCorrection = 1;
+  int XSPH = 0;
+  int correctVelocityGradient = 1;
+  int sumMassDensityOverAllNodeLists = 1;
+  int densityUpdate = 0;     // 0 RigorousSumDensity, 1 IntegrateDensity
+  double epsTensile = 0.0, nTensile = 4.0;
+  double Cl = 1.0, Cq = 1.0, eps2 = 1.0e-2;
+  int linearInExpansion = 0, quadraticInExpansion = 0;
+  double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
+  int gravity = 0;
+  double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
+};
+
+static inline double& comp(V3& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+static inline double compc(const V3& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+// mapPositionThroughPlanes (mapPositionThroughPlanes.hh:17-27) for an
+// axis-aligned plane pair; only the axis coordinate changes.  enter/exit
+// planes are (coordinate w, normal sign s).
+static inline double mapCoord(double p, double wEnter, double sEnter, double wExit, double sExit) {
+  // closestPointOnPlane: p + ((origin - p).n) n  (pointDistances.hh:69-74)
+  const double dotv = (wExit - p) * sExit;
+  const double p0 = p + dotv * sExit;
+  const double s = (p - wEnter) * sEnter;          // enterPlane.signedDistance
+  return p0 - s * sExit;
+}
+
+struct Problem {
+  Config cfg;
+  TableKernel W;
+  vector<NodeListParams> lists;
+  vector<Boundary> bcs;
+  int nInt = 0, nTot = 0;
+  double time = 0.0, lastDt = 1.0e-5;
+  int cycle = 0;
+  double dtMultiplier = 1.0;
+
+  // state (size nTot)
+  vector<V3> pos, vel;
+  vector<double> mass, rho, eps, P, cs, omega;
+  vector<ST> H;
+  vector<int> list;
+  // ghost transform bookkeeping: for each ghost: control index and per-axis code
+  vector<int> ctrl;      // flat control index (ultimately an internal node)
+  vector<int> image;     // per-axis 2-bit codes: 0 none, 1 low image / lo mirror, 2 high image / hi mirror
+
+  // connectivity
+  vector<std::pair<int, int>> pairs;
+  vector<int> numNeighbors;   // per internal node
+  vector<vector<int>> neighbors;  // per internal node: flat neighbor indices (for the numNeighbors contract / tests)
+
+  // derivatives (size nTot)
+  vector<double> rhoSum, normalization, DrhoDt, DepsDt, maxQ, effQ, XSPHWeightSum, massZeroth, DepsDtCompat;
+  vector<V3> DxDt, DvDt, gradRho, XSPHDeltaV, massFirst, DvDtGrav;
+  vector<T9> DvDx, localDvDx, M, localM;
+  vector<ST> DHDt, Hideal;
+  vector<V3> pairAccel;   // per pair
+  vector<double> potential;
+  double extraEnergy = 0.0, dtMinAcc = std::numeric_limits<double>::max();
+  std::string dtReason;
+
+  void resizeAll(int n) {
+    pos.resize(n); vel.resize(n); mass.resize(n); rho.resize(n); eps.resize(n); P.resize(n); cs.resize(n);
+    omega.resize(n, 1.0); H.resize(n); list.resize(n);
+  }
+  void resizeDerivs() {
+    const int n = nTot;
+    auto z = [&](vector<double>& v) { v.assign(n, 0.0); };
+    auto zv = [&](vector<V3>& v) { v.assign(n, V3{}); };
+    auto zt = [&](vector<T9>& v) { v.assign(n, T9{}); };
+    auto zs = [&](vector<ST>& v) { v.assign(n, ST{}); };
+    if ((int)rhoSum.size() != nInt) {
+      z(rhoSum); z(normalization); z(DrhoDt); z(DepsDt); z(maxQ); z(effQ); z(XSPHWeightSum); z(massZeroth); z(DepsDtCompat);
+      zv(DxDt); zv(DvDt); zv(gradRho); zv(XSPHDeltaV); zv(massFirst); zv(DvDtGrav);
+      zt(DvDx); zt(localDvDx); zt(M); zt(localM); zs(DHDt); zs(Hideal); z(potential);
+    }
+  }
+  // Resize derivative arrays to nTot, preserving internal values (ghost
+  // entries are scratch).
+  template <class T> static void keepResize(vector<T>& v, int nInt_, int nTot_) { v.resize(nTot_); (void)nInt_; }
+  void derivsToTotal() {
+    keepResize(rhoSum, nInt, nTot); keepResize(normalization, nInt, nTot); keepResize(DrhoDt, nInt, nTot);
+    keepResize(DepsDt, nInt, nTot); keepResize(maxQ, nInt, nTot); keepResize(effQ, nInt, nTot);
+    keepResize(XSPHWeightSum, nInt, nTot); keepResize(massZeroth, nInt, nTot); keepResize(DepsDtCompat, nInt, nTot);
+    keepResize(DxDt, nInt, nTot); keepResize(DvDt, nInt, nTot); keepResize(gradRho, nInt, nTot);
+    keepResize(XSPHDeltaV, nInt, nTot); keepResize(massFirst, nInt, nTot); keepResize(DvDtGrav, nInt, nTot);
+    keepResize(DvDx, nInt, nTot); keepResize(localDvDx, nInt, nTot); keepResize(M, nInt, nTot); keepResize(localM, nInt, nTot);
+    keepResize(DHDt, nInt, nTot); keepResize(Hideal, nInt, nTot); keepResize(potential, nInt, nTot);
+  }
+
+  double hmaxOf(const ST& Hi) const { return 1.0 / minElem(eigenValuesS(Hi)); }
+
+  //----------------------------------------------------------------------------
+  // Ghost nodes: Integrator::setGhostNodes -> Boundary::setAllGhostNodes ->
+  // PlanarBoundary::setGhostNodes (findNodesTouchingThroughPlanes).
+  //----------------------------------------------------------------------------
+  void planeSpec(const Boundary& b, int sub, double& wEnter, double& sEnter, double& wExit, double& sExit) const {
+    if (b.type == 0) {
+      if (sub == 0) { wEnter = b.lo; sEnter = 1.0; wExit = b.hi; sExit = -1.0; }   // mPlane1Boundary(plane1, plane2)
+      else          { wEnter = b.hi; sEnter = -1.0; wExit = b.lo; sExit = 1.0; }   // mPlane2Boundary(plane2, plane1)
+    } else {
+      const double w = b.wallHigh ? b.hi : b.lo, s = b.wallHigh ? -1.0 : 1.0;
+      wEnter = wExit = w; sEnter = sExit = s;
+    }
+  }
+  void setGhostNodes() {
+    nTot = nInt;
+    resizeAll(nInt);
+    ctrl.assign(nInt, -1);
+    image.assign(nInt, 0);
+    const double ext = W.extent;
+    const int nLists = (int)lists.size();
+    for (auto& b : bcs) {
+      const int nsub = b.type == 0 ? 2 : 1;
+      for (int sub = 0; sub < nsub; ++sub) {
+        b.control[sub].clear(); b.ghost[sub].clear();
+        double wEn, sEn, wEx, sEx;
+        planeSpec(b, sub, wEn, sEn, wEx, sEx);
+        for (int L = 0; L < nLists; ++L) {
+          const int n = nTot;
+          double hmax = 0.0;
+          for (int i = 0; i < n; ++i) {
+            if (list[i] != L) continue;
+            const double p = compc(pos[i], b.axis);
+            const double hmaxi = hmaxOf(H[i]);
+            const double dEx = std::fabs((p - wEx) * sEx), dEn = std::fabs((p - wEn) * sEn);
+            if (hmaxi > hmax && std::min(dEx, dEn) < ext * hmaxi) hmax = hmaxi;
+          }
+          vector<int> controls;
+          if (hmax > 0.0) {
+            for (int i = 0; i < n; ++i) {
+              if (list[i] != L) continue;
+              const double disti = ((compc(pos[i], b.axis) - wEx) * sEx) / hmax;
+              if (disti >= 0.0 && disti <= ext) controls.push_back(i);
+            }
+          }
+          // append ghosts
+          for (int c : controls) {
+            const int g = nTot++;
+            pos.push_back(pos[c]); vel.push_back(vel[c]); mass.push_back(mass[c]); rho.push_back(rho[c]);
+            eps.push_back(eps[c]); P.push_back(P[c]); cs.push_back(cs[c]); omega.push_back(omega[c]);
+            H.push_back(H[c]); list.push_back(list[c]);
+            const int root = ctrl[c] < 0 ? c : ctrl[c];
+            ctrl.push_back(root);
+            const int code = (b.type == 0 ? (sub == 0 ? 1 : 2) : (b.wallHigh ? 2 : 1));
+            int im = image[c];
+            im &= ~(3 << (2 * b.axis));
+            im |= code << (2 * b.axis);
+            image.push_back(im);
+            // position: mapPosition(pos(control), mExitPlane, mEnterPlane)
+            comp(pos[g], b.axis) = mapCoord(compc(pos[c], b.axis), wEx, sEx, wEn, sEn);
+            b.control[sub].push_back(c);
+            b.ghost[sub].push_back(g);
+          }
+        }
+      }
+    }
+    derivsToTotal();
+  }
+  // applyGhostBoundaries for the state fields (boundary by boundary).
+  void applyGhostState() {
+    for (auto& b : bcs) {
+      const int nsub = b.type == 0 ? 2 : 1;
+      for (int sub = 0; sub < nsub; ++sub) {
+        double wEn, sEn, wEx, sEx;
+        planeSpec(b, sub, wEn, sEn, wEx, sEx);
+        for (size_t k = 0; k < b.control[sub].size(); ++k) {
+          const int c = b.control[sub][k], g = b.ghost[sub][k];
+          pos[g] = pos[c];
+          comp(pos[g], b.axis) = mapCoord(compc(pos[c], b.axis), wEx, sEx, wEn, sEn);
+          H[g] = H[c]; mass[g] = mass[c]; rho[g] = rho[c]; eps[g] = eps[c]; P[g] = P[c]; cs[g] = cs[c];
+          omega[g] = omega[c]; vel[g] = vel[c];
+          if (b.type == 1) {
+            comp(vel[g], b.axis) = -compc(vel[c], b.axis);
+            // (R H R).Symmetric(): flips the off-diagonal terms that touch the axis
+            ST h = H[c];
+            if (b.axis == 0) { h.xy = -h.xy; h.xz = -h.xz; }
+            else if (b.axis == 1) { h.xy = -h.xy; h.yz = -h.yz; }
+            else { h.xz = -h.xz; h.yz = -h.yz; }
+            H[g] = h;
+          }
+        }
+      }
+    }
+  }
+  template <class T, class Fn>
+  void applyGhostField(vector<T>& f, Fn reflect) {
+    for (auto& b : bcs) {
+      const int nsub = b.type == 0 ? 2 : 1;
+      for (int sub = 0; sub < nsub; ++sub)
+        for (size_t k = 0; k < b.control[sub].size(); ++k) {
+          const int c = b.control[sub][k], g = b.ghost[sub][k];
+          f[g] = f[c];
+          if (b.type == 1) reflect(f[g], b.axis);
+        }
+    }
+  }
+  void applyGhostScalar(vector<double>& f) { applyGhostField(f, [](double&, int) {}); }
+  void applyGhostVector(vector<V3>& f) { applyGhostField(f, [](V3& v, int a) { comp(v, a) = -comp(v, a); }); }
+
+  //----------------------------------------------------------------------------
+  // ConnectivityMap::computeConnectivity (pair criterion and pair list).
+  //----------------------------------------------------------------------------
+  void computeConnectivity() {
+    const double ext = W.extent, ext2 = ext * ext;
+    double hmaxAll = 0.0;
+    V3 lo{1e300, 1e300, 1e300}, hi{-1e300, -1e300, -1e300};
+    for (int i = 0; i < nTot; ++i) {
+      hmaxAll = std::max(hmaxAll, hmaxOf(H[i]));
+      lo.x = std::min(lo.x, pos[i].x); lo.y = std::min(lo.y, pos[i].y); lo.z = std::min(lo.z, pos[i].z);
+      hi.x = std::max(hi.x, pos[i].x); hi.y = std::max(hi.y, pos[i].y); hi.z = std::max(hi.z, pos[i].z);
+    }
+    double cell = std::max(ext * hmaxAll * 1.0001, 1e-300);
+    int nc[3];
+    double L[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    for (int a = 0; a < 3; ++a) nc[a] = std::max(1, (int)std::floor(L[a] / cell) + 1);
+    while ((double)nc[0] * nc[1] * nc[2] > 8.0e7) { cell *= 1.26; for (int a = 0; a < 3; ++a) nc[a] = std::max(1, (int)std::floor(L[a] / cell) + 1); }
+    auto cidx = [&](const V3& p, int c[3]) {
+      const double q[3] = {p.x - lo.x, p.y - lo.y, p.z - lo.z};
+      for (int a = 0; a < 3; ++a) c[a] = std::min(nc[a] - 1, std::max(0, (int)std::floor(q[a] / cell)));
+    };
+    const size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
+    vector<int> head(ncell + 1, 0), order(nTot);
+    vector<int> cellOf(nTot);
+    for (int i = 0; i < nTot; ++i) { int c[3]; cidx(pos[i], c); cellOf[i] = (c[2] * nc[1] + c[1]) * nc[0] + c[0]; head[cellOf[i] + 1]++; }
+    for (size_t k = 0; k < ncell; ++k) head[k + 1] += head[k];
+    { vector<int> fill(head.begin(), head.end() - 1); for (int i = 0; i < nTot; ++i) order[fill[cellOf[i]]++] = i; }
+    neighbors.assign(nInt, {});
+    numNeighbors.assign(nInt, 0);
+    int nthreads = 1;
+#ifdef _OPENMP
+    nthreads = omp_get_max_threads();
+#endif
+    vector<vector<std::pair<int, int>>> tp(nthreads);
+#pragma omp parallel
+    {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      auto& mine = tp[tid];
+#pragma omp for schedule(dynamic, 256)
+      for (int i = 0; i < nInt; ++i) {
+        int c[3]; cidx(pos[i], c);
+        const V3 ri = pos[i]; const ST Hi = H[i];
+        auto& nb = neighbors[i];
+        for (int dz = -1; dz <= 1; ++dz) for (int dy = -1; dy <= 1; ++dy) for (int dx = -1; dx <= 1; ++dx) {
+          const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+          if (x < 0 || y < 0 || z < 0 || x >= nc[0] || y >= nc[1] || z >= nc[2]) continue;
+          const int cc = (z * nc[1] + y) * nc[0] + x;
+          for (int k = head[cc]; k < head[cc + 1]; ++k) {
+            const int j = order[k];
+            if (j == i) continue;
+            const V3 rij = sub(ri, pos[j]);
+            const double eta2i = mag2(dotSV(Hi, rij));
+            const double eta2j = mag2(dotSV(H[j], rij));
+            if (eta2i <= ext2 || eta2j <= ext2) {
+              nb.push_back(j);
+              if (j > i) mine.push_back({i, j});   // calculatePairInteraction (one NodeList ordering)
+            }
+          }
+        }
+        std::sort(nb.begin(), nb.end());
+        numNeighbors[i] = (int)nb.size();
+      }
+    }
+    pairs.clear();
+    for (auto& v : tp) pairs.insert(pairs.end(), v.begin(), v.end());
+    std::sort(pairs.begin(), pairs.end());
+    pairAccel.assign(pairs.size(), V3{});
+  }
+
+  //----------------------------------------------------------------------------
+  // Equation of state (GammaLawGas) -- PressurePolicy / SoundSpeedPolicy.
+  //----------------------------------------------------------------------------
+  double pressure(int i) const {
+    const auto& L = lists[list[i]];
+    double p = (L.gamma - 1.0) * rho[i] * eps[i];
+    return p < L.minP ? L.minP : (p > L.maxP ? L.maxP : p);
+  }
+  double soundSpeed(int i) const {
+    const auto& L = lists[list[i]];
+    return std::sqrt(std::max(0.0, L.gamma * (L.gamma - 1.0) * eps[i]));
+  }
+  void updateEOS(int n) {
+    for (int i = 0; i < n; ++i) { P[i] = pressure(i); cs[i] = soundSpeed(i); }
+  }
+
+  //----------------------------------------------------------------------------
+  // Thread-private accumulation helper (FieldList::threadCopy/threadReduce).
+  //----------------------------------------------------------------------------
+  template <class T, class Body>
+  static void pairSweep(size_t npairs, vector<T>& out, int n, Body body) {
+    int nthreads = 1;
+#ifdef _OPENMP
+    nthreads = omp_get_max_threads();
+#endif
+    vector<vector<T>> priv(nthreads, vector<T>(n));
+#pragma omp parallel
+    {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      auto& p = priv[tid];
+#pragma omp for schedule(static)
+      for (long kk = 0; kk < (long)npairs; ++kk) body(kk, p);
+    }
+    for (int t = 0; t < nthreads; ++t)
+      for (int i = 0; i < n; ++i) out[i] += priv[t][i];
+  }
+
+  //----------------------------------------------------------------------------
+  // computeSPHSumMassDensity (computeSPHSumMassDensity.cc:15-87).
+  //----------------------------------------------------------------------------
+  void sumMassDensity() {
+    vector<double> rhoNew(nTot, 0.0);
+    for (int i = 0; i < nInt; ++i) {
+      const double Hdet = detS(H[i]);
+      const V3 etaii = dotSV(H[i], pos[i]);
+      rhoNew[i] = mass[i] * W.kernelValue(mag(sub(etaii, etaii)), Hdet);
+    }
+    vector<double> acc(nTot, 0.0);
+    pairSweep(pairs.size(), acc, nTot, [&](long k, vector<double>& p) {
+      const int i = pairs[k].first, j = pairs[k].second;
+      const double Hdeti = detS(H[i]), Hdetj = detS(H[j]);
+      const double Wi = W.kernelValue(mag(sub(dotSV(H[i], pos[i]), dotSV(H[i], pos[j]))), Hdeti);
+      const double Wj = W.kernelValue(mag(sub(dotSV(H[j], pos[i]), dotSV(H[j], pos[j]))), Hdetj);
+      const bool same = list[i] == list[j];
+      p[i] += (same ? mass[j] : mass[i]) * Wj;
+      p[j] += (same ? mass[i] : mass[j]) * Wi;
+    });
+    for (int i = 0; i < nInt; ++i) rho[i] = rhoNew[i] + acc[i];
+    applyGhostScalar(rho);
+  }
+
+  //----------------------------------------------------------------------------
+  // computeSPHOmegaGradhCorrection (computeSPHOmegaGradhCorrection.cc:15-116).
+  //----------------------------------------------------------------------------
+  void omegaGradh() {
+    const double W0 = W.kernelValue(0.0, 1.0);
+    struct Acc { double w = 0, g = 0; Acc& operator+=(const Acc& o) { w += o.w; g += o.g; return *this; } };
+    vector<Acc> acc(nTot);
+    pairSweep(pairs.size(), acc, nTot, [&](long k, vector<Acc>& p) {
+      const int i = pairs[k].first, j = pairs[k].second;
+      const V3 rij = sub(pos[i], pos[j]);
+      const double etai = mag(dotSV(H[i], rij)), etaj = mag(dotSV(H[j], rij));
+      double Wi, gWi, Wj, gWj;
+      W.kernelAndGradValue(etai, detS(H[i]), Wi, gWi);
+      W.kernelAndGradValue(etaj, detS(H[j]), Wj, gWj);
+      p[i].w += Wi; p[j].w += Wj;
+      p[i].g += etai * gWi; p[j].g += etaj * gWj;
+    });
+    for (int i = 0; i < nInt; ++i) {
+      if (numNeighbors[i] == 0) { omega[i] = 1.0; continue; }
+      double o = acc[i].w;
+      o += detS(H[i]) * W0;
+      omega[i] = std::max(1.0e-30, -acc[i].g / (3 * o));
+    }
+    applyGhostScalar(omega);
+  }
+
+  //----------------------------------------------------------------------------
+  // SPH::evaluateDerivativesImpl (SPH.cc:166-555) for a Scalar Q
+  // (MonaghanGingoldViscosity::QPiij), followed by
+  // SPHSmoothingScale::evaluateDerivatives (SPHSmoothingScale.cc:101-275).
+  //----------------------------------------------------------------------------
+  struct PairAcc {
+    double rhoSum = 0, norm = 0, DepsDt = 0, maxQ = 0, effQ = 0, xsphW = 0, m0 = 0;
+    V3 DvDt, gradRho, xsphDV, m1;
+    T9 DvDx, localDvDx, M, localM;
+    PairAcc& operator+=(const PairAcc& o) {
+      rhoSum += o.rhoSum; norm += o.norm; DepsDt += o.DepsDt; maxQ = std::max(maxQ, o.maxQ); effQ += o.effQ;
+      xsphW += o.xsphW; m0 += o.m0;
+      DvDt = add(DvDt, o.DvDt); gradRho = add(gradRho, o.gradRho); xsphDV = add(xsphDV, o.xsphDV); m1 = add(m1, o.m1);
+      addT(DvDx, o.DvDx); addT(localDvDx, o.localDvDx); addT(M, o.M); addT(localM, o.localM);
+      return *this;
+    }
+  };
+  void QPiij(double& QPiij_, double& QPiji_, double& Qij, double& Qji, const V3& etai, const V3& vi, double rhoi,
+             double csi, const V3& etaj, const V3& vj, double rhoj, double csj) const {
+    const double fCli = 1.0, fCqi = 1.0, fClj = 1.0, fCqj = 1.0, fshear = 1.0;
+    const double Clij = 0.5 * (fCli + fClj) * fshear * cfg.Cl;
+    const double Cqij = 0.5 * (fCqi + fCqj) * fshear * cfg.Cq;
+    const V3 vij = sub(vi, vj);
+    const double mui = dot(vij, etai) / (mag2(etai) + cfg.eps2);
+    const double muj = dot(vij, etaj) / (mag2(etaj) + cfg.eps2);
+    const double li = cfg.linearInExpansion ? mui : std::min(0.0, mui);
+    const double lj = cfg.linearInExpansion ? muj : std::min(0.0, muj);
+    const double qi = cfg.quadraticInExpansion ? -sgn(mui) * mui * mui : std::min(0.0, mui) * std::min(0.0, mui);
+    const double qj = cfg.quadraticInExpansion ? -sgn(muj) * muj * muj : std::min(0.0, muj) * std::min(0.0, muj);
+    const double ei = -Clij * csi * li + Cqij * qi;
+    const double ej = -Clij * csj * lj + Cqij * qj;
+    QPiij_ = ei / rhoi; QPiji_ = ej / rhoj;
+    Qij = rhoi * ei; Qji = rhoj * ej;
+  }
+  void evaluateDerivatives() {
+    const double W0 = W.kernelValue(0.0, 1.0);
+    const double tiny = 1.0e-30;
+    const double epsTensile = cfg.epsTensile;
+    const bool compatible = cfg.compatibleEnergy != 0, XSPH = cfg.XSPH != 0;
+    vector<PairAcc> acc(nTot);
+    pairAccel.assign(pairs.size(), V3{});
+    pairSweep(pairs.size(), acc, nTot, [&](long kk, vector<PairAcc>& p) {
+      const int i = pairs[kk].first, j = pairs[kk].second;
+      const V3 ri = pos[i], vi = vel[i]; const double mi = mass[i], rhoi = rho[i], Pi = P[i], ci = cs[i];
+      const ST Hi = H[i]; const double safeOmegai = safeInv(omega[i], tiny), Hdeti = detS(Hi);
+      const V3 rj = pos[j], vj = vel[j]; const double mj = mass[j], rhoj = rho[j], Pj = P[j], cj = cs[j];
+      const ST Hj = H[j]; const double safeOmegaj = safeInv(omega[j], tiny), Hdetj = detS(Hj);
+      // SPH.cc:264-266: the tensile scale uses the first NodeList's nPerh
+      const double WnPerhi = W.kernelValue(1.0 / lists[0].nPerh, 1.0);
+      const double WnPerhj = WnPerhi;
+      auto& ai = p[i]; auto& aj = p[j];
+
+      const V3 rij = sub(ri, rj);
+      const V3 etai = dotSV(Hi, rij), etaj = dotSV(Hj, rij);
+      const double etaMagi = mag(etai), etaMagj = mag(etaj);
+      const V3 etaiUnit = mul(etai, safeInvVar(etaMagi)), etajUnit = mul(etaj, safeInvVar(etaMagj));
+      double Wi, gWi, Wj, gWj;
+      W.kernelAndGradValue(etaMagi, Hdeti, Wi, gWi);
+      W.kernelAndGradValue(etaMagj, Hdetj, Wj, gWj);
+      const V3 gradWi = dotSV(scaleS(gWi, Hi), etaiUnit), gradWj = dotSV(scaleS(gWj, Hj), etajUnit);
+      const double WQi = Wi, WQj = Wj; const V3 gradWQi = gradWi, gradWQj = gradWj;
+      if (list[i] == list[j]) {
+        ai.rhoSum += mj * Wi; aj.rhoSum += mi * Wj;
+        ai.norm += mi / rhoi * Wi; aj.norm += mj / rhoj * Wj;
+      }
+      const V3 vij = sub(vi, vj);
+      double QPi_ij, QPi_ji, Qi, Qj;
+      QPiij(QPi_ij, QPi_ji, Qi, Qj, etai, vi, rhoi, ci, etaj, vj, rhoj, cj);
+      const V3 Qacci = mul(0.5, mul(QPi_ij, gradWQi)), Qaccj = mul(0.5, mul(QPi_ji, gradWQj));
+      const double workQi = dot(vij, Qacci), workQj = dot(vij, Qaccj);
+      ai.maxQ = std::max(ai.maxQ, Qi); aj.maxQ = std::max(aj.maxQ, Qj);
+      ai.effQ += mj * Qi * WQi / rhoj; aj.effQ += mi * Qj * WQj / rhoi;
+      const double Ri = epsTensile * pow4(Wi / (Hdeti * WnPerhi)) * (Pi < 0.0 ? -Pi : 0.0);
+      const double Rj = epsTensile * pow4(Wj / (Hdetj * WnPerhj)) * (Pj < 0.0 ? -Pj : 0.0);
+      const double Peffi = Pi + Ri, Peffj = Pj + Rj;
+      const double Prhoi = safeOmegai * Peffi / (rhoi * rhoi), Prhoj = safeOmegaj * Peffj / (rhoj * rhoj);
+      const V3 deltaDvDt = add(add(add(mul(Prhoi, gradWi), mul(Prhoj, gradWj)), Qacci), Qaccj);
+      ai.DvDt = sub(ai.DvDt, mul(mj, deltaDvDt));
+      aj.DvDt = add(aj.DvDt, mul(mi, deltaDvDt));
+      if (compatible) pairAccel[kk] = mul(-mj, deltaDvDt);
+      ai.DepsDt += mj * (Prhoi * dot(vij, gradWi) + workQi);
+      aj.DepsDt += mi * (Prhoj * dot(vij, gradWj) + workQj);
+      const T9 dDvDxi = scaleT(mj, dyad(vij, gradWi)), dDvDxj = scaleT(mi, dyad(vij, gradWj));
+      subT(ai.DvDx, dDvDxi); subT(aj.DvDx, dDvDxj);
+      subT(ai.localDvDx, dDvDxi); subT(aj.localDvDx, dDvDxj);
+      if (XSPH) {
+        const double w = 0.5 * (mi / rhoi * Wi + mj / rhoj * Wj);
+        ai.xsphW += w; aj.xsphW += w;
+        ai.xsphDV = sub(ai.xsphDV, mul(w, vij)); aj.xsphDV = add(aj.xsphDV, mul(w, vij));
+      }
+      ai.gradRho = add(ai.gradRho, mul(mj * (rhoj - rhoi), gradWi));
+      aj.gradRho = add(aj.gradRho, mul(mi * (rhoj - rhoi), gradWj));
+      subT(ai.M, scaleT(mj, dyad(rij, gradWi))); subT(aj.M, scaleT(mi, dyad(rij, gradWj)));
+      subT(ai.localM, scaleT(mj, dyad(rij, gradWi))); subT(aj.localM, scaleT(mi, dyad(rij, gradWj)));
+      // SPHSmoothingScale moments (fweightij for distinct NodeLists).
+      const double fweightij = (list[i] != list[j]) ? mj * rhoi / (mi * rhoj) : 1.0;
+      const double WSPHi = W.kernelValueSPH(etaMagi), WSPHj = W.kernelValueSPH(etaMagj);
+      ai.m0 += fweightij * WSPHi; aj.m0 += 1.0 / fweightij * WSPHj;
+      ai.m1 = sub(ai.m1, mul(fweightij * WSPHi, etai)); aj.m1 = add(aj.m1, mul(1.0 / fweightij * WSPHj, etaj));
+    });
+    // SPH finalize, SPH.cc:480-552
+    for (int i = 0; i < nInt; ++i) {
+      auto& a = acc[i];
+      const double mi = mass[i], rhoi = rho[i]; const V3 vi = vel[i]; const double Hdeti = detS(H[i]);
+      rhoSum[i] = a.rhoSum + mi * W0 * Hdeti;
+      normalization[i] = a.norm + mi / rhoi * W0 * Hdeti;
+      T9 Mi = a.M, lMi = a.localM, DvDxi = a.DvDx, lDvDxi = a.localDvDx;
+      if (cfg.correctVelocityGradient && std::fabs(detT(Mi)) > 1.0e-10 && numNeighbors[i] > 8) {
+        Mi = inverseT(Mi); DvDxi = dotTT(DvDxi, Mi);
+      } else {
+        DvDxi.xx /= rhoi; DvDxi.xy /= rhoi; DvDxi.xz /= rhoi; DvDxi.yx /= rhoi; DvDxi.yy /= rhoi;
+        DvDxi.yz /= rhoi; DvDxi.zx /= rhoi; DvDxi.zy /= rhoi; DvDxi.zz /= rhoi;
+      }
+      if (cfg.correctVelocityGradient && std::fabs(detT(lMi)) > 1.0e-10 && numNeighbors[i] > 8) {
+        lMi = inverseT(lMi); lDvDxi = dotTT(lDvDxi, lMi);
+      } else {
+        lDvDxi.xx /= rhoi; lDvDxi.xy /= rhoi; lDvDxi.xz /= rhoi; lDvDxi.yx /= rhoi; lDvDxi.yy /= rhoi;
+        lDvDxi.yz /= rhoi; lDvDxi.zx /= rhoi; lDvDxi.zy /= rhoi; lDvDxi.zz /= rhoi;
+      }
+      M[i] = Mi; localM[i] = lMi; DvDx[i] = DvDxi; localDvDx[i] = lDvDxi;
+      gradRho[i] = {a.gradRho.x / rhoi, a.gradRho.y / rhoi, a.gradRho.z / rhoi};
+      DrhoDt[i] = -rhoi * traceT(DvDxi);
+      DvDt[i] = a.DvDt;
+      DepsDt[i] = a.DepsDt;
+      maxQ[i] = a.maxQ; effQ[i] = a.effQ;
+      XSPHWeightSum[i] = a.xsphW; XSPHDeltaV[i] = a.xsphDV;
+      if (XSPH) {
+        XSPHWeightSum[i] += Hdeti * mi / rhoi * W0;
+        const double ws = std::max(tiny, XSPHWeightSum[i]);
+        DxDt[i] = add(vi, V3{XSPHDeltaV[i].x / ws, XSPHDeltaV[i].y / ws, XSPHDeltaV[i].z / ws});
+      } else {
+        DxDt[i] = vi;
+      }
+      // SPHSmoothingScale finalize
+      const auto& L = lists[list[i]];
+      double m0 = rootnu3(std::max(0.0, a.m0));
+      massZeroth[i] = m0; massFirst[i] = a.m1;
+      const double tr = traceT(DvDxi);
+      const ST mH{-H[i].xx, -H[i].xy, -H[i].xz, -H[i].yy, -H[i].yz, -H[i].zz};
+      DHDt[i] = scaleS(ST{mH.xx / 3, mH.xy / 3, mH.xz / 3, mH.yy / 3, mH.yz / 3, mH.zz / 3}, tr);
+      const double cur = fuzzyEqual(m0, 0.0) ? 0.5 * L.nPerh : W.equivalentNodesPerSmoothingScale(m0);
+      const double s = std::min(4.0, std::max(0.25, L.nPerh / (cur + 1.0e-30)));
+      const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
+      const double hi0 = 1.0 / H[i].xx;
+      const double hi1 = std::min(L.hmax, std::max(L.hmin, hi0 * (1.0 - aa + aa * s)));
+      const double hinv = 1.0 / hi1;
+      Hideal[i] = ST{hinv * 1.0, hinv * 0.0, hinv * 0.0, hinv * 1.0, hinv * 0.0, hinv * 1.0};
+    }
+  }
+
+  // SPHBase::finalizeDerivatives: ghost values of DvDt and DepsDt.
+  void finalizeDerivatives() {
+    if (cfg.compatibleEnergy) { applyGhostVector(DvDt); applyGhostScalar(DepsDt); }
+  }
+
+  //----------------------------------------------------------------------------
+  // GenericHydro::dt (GenericHydro.cc:113-381).
+  //----------------------------------------------------------------------------
+  double hydroDt() {
+    const double tiny = kDblEps;
+    double minDt = std::numeric_limits<double>::max();
+    std::string reason;
+    for (int L = 0; L < (int)lists.size(); ++L) {
+      const double nPerh = lists[L].nPerh;
+      for (int i = 0; i < nInt; ++i) {
+        if (list[i] != L) continue;
+        const double nodeScalei = 1.0 / maxElem(eigenValuesS(H[i])) / nPerh;
+        const double csDt = nodeScalei / (cs[i] + tiny);
+        if (csDt < minDt) { minDt = csDt; reason = "sound speed"; }
+        const double csq = std::sqrt(maxQ[i] / rho[i]);
+        const double csqDt = nodeScalei / (csq + tiny);
+        if (csqDt < minDt) { minDt = csqDt; reason = "artificial viscosity"; }
+        const double divv = traceT(DvDx[i]);
+        const double divvDt = 1.0 / (std::fabs(divv) + tiny);
+        if (divvDt < minDt) { minDt = divvDt; reason = "velocity divergence"; }
+        const double vmagi = mag(vel[i]);
+        const double dtAcc = 0.1 * std::max(nodeScalei / (vmagi + tiny), vmagi / (mag(DvDt[i]) + tiny));
+        if (dtAcc < minDt) { minDt = dtAcc; reason = "acceleration"; }
+        if (cfg.useVelocityMagnitudeForDt) {
+          const double velDt = nodeScalei / (mag(vel[i]) + 1.0e-10);
+          if (velDt < minDt) { minDt = velDt; reason = "velocity magnitude"; }
+        }
+      }
+      for (size_t k = 0; k < pairs.size(); ++k) {
+        const int i = pairs[k].first, j = pairs[k].second;
+        const double nsi = 1.0 / maxElem(eigenValuesS(H[i])) / nPerh;
+        const double nsj = 1.0 / maxElem(eigenValuesS(H[j])) / nPerh;
+        const double dtv = std::min(nsi, nsj) * safeInvVar(mag(sub(vel[i], vel[j])), tiny);
+        if (dtv < minDt) { minDt = dtv; reason = "pairwise velocity difference"; }
+      }
+    }
+    dtReason = reason;
+    return minDt * cfg.cfl;
+  }
+  double gravityDt() const {
+    return cfg.ftimestep * dtMinAcc;   // TreeGravity::dt, AccelerationRatio
+  }
+  double selectDt(double dtMin, double dtMax) {
+    double dt = dtMax;
+    const double hv = hydroDt();
+    if (hv > 0.0 && hv < dt) dt = hv;
+    if (cfg.gravity) { const double gv = gravityDt(); if (gv > 0.0 && gv < dt) dt = gv; }
+    dt *= dtMultiplier;
+    dt = std::min(dt, cfg.dtGrowth * lastDt);
+    dt = std::min(dtMax, std::max(dtMin, dt));
+    return dt;
+  }
+
+  //----------------------------------------------------------------------------
+  // SpecificThermalEnergyPolicy::update (SpecificThermalEnergyPolicy.cc:47-174).
+  //----------------------------------------------------------------------------
+  void compatibleEnergyUpdate(double multiplier) {
+    const double hdt = 0.5 * multiplier;
+    vector<double> acc(nTot, 0.0);
+    pairSweep(pairs.size(), acc, nTot, [&](long kk, vector<double>& p) {
+      const int i = pairs[kk].first, j = pairs[kk].second;
+      const double mi = mass[i], mj = mass[j];
+      const V3 vi12 = add(vel[i], mul(DvDt[i], hdt)), vj12 = add(vel[j], mul(DvDt[j], hdt));
+      const V3 vji12 = sub(vj12, vi12);
+      const double duij = dot(vji12, pairAccel[kk]);
+      const double weighti = std::max(kDblEps, DepsDt[i] * sgn(duij));
+      const double weightj = std::max(kDblEps, DepsDt[j] * sgn(duij));
+      const double wi = weighti / (weighti + weightj);
+      p[i] += wi * duij;
+      p[j] += (1.0 - wi) * duij * mi / mj;
+    });
+    for (int i = 0; i < nInt; ++i) { DepsDtCompat[i] = acc[i]; eps[i] += acc[i] * multiplier; }
+  }
+
+  //----------------------------------------------------------------------------
+  // State::update for this package set.  midStep: timeAdvanceOnly update with
+  // the previous derivatives (CheapSynchronousRK2.cc:75-80); otherwise the full
+  // update from state0 (CheapSynchronousRK2.cc:105-110).
+  //----------------------------------------------------------------------------
+  static ST clampH(const ST& h, double minv, double maxv) {
+    // min(maxv, max(minv, H)) on the eigenvalues; exact for isotropic H.
+    if (isIsotropic(h)) {
+      double a = h.xx;
+      if (a < minv) a = minv;
+      if (a > maxv) a = maxv;
+      return ST{a, 0.0, 0.0, a, 0.0, a};
+    }
+    return h;   // anisotropic H is not exercised on this path
+  }
+  void stateUpdate(double multiplier, bool midStep) {
+    // specific thermal energy
+    if (midStep || !cfg.compatibleEnergy) {
+      for (int i = 0; i < nInt; ++i) eps[i] += multiplier * DepsDt[i];
+    } else {
+      compatibleEnergyUpdate(multiplier);
+    }
+    for (int i = 0; i < nInt; ++i) {
+      const auto& L = lists[list[i]];
+      pos[i] = add(pos[i], mul(multiplier, DxDt[i]));
+      vel[i] = add(vel[i], mul(multiplier, DvDt[i]));
+      if (cfg.gravity) vel[i] = add(vel[i], mul(multiplier, DvDtGrav[i]));
+      rho[i] = std::min(L.rhoMax, std::max(L.rhoMin, rho[i] + multiplier * DrhoDt[i]));
+      if (midStep) {
+        ST hn{H[i].xx + multiplier * DHDt[i].xx, H[i].xy + multiplier * DHDt[i].xy, H[i].xz + multiplier * DHDt[i].xz,
+              H[i].yy + multiplier * DHDt[i].yy, H[i].yz + multiplier * DHDt[i].yz, H[i].zz + multiplier * DHDt[i].zz};
+        H[i] = clampH(hn, 1.0 / L.hmax, 1.0 / L.hmin);
+      } else {
+        H[i] = clampH(Hideal[i], 1.0 / L.hmax, 1.0 / L.hmin);
+      }
+    }
+    updateEOS(nInt);
+  }
+
+  // Boundary::setAllViolationNodes + enforceBoundary (PlanarBoundary.cc:153-190,
+  // ReflectingBoundary.cc:465-500): map positions of internal nodes that left
+  // through a plane and reflect their vectors.
+  void enforceBoundaries() {
+    for (auto& b : bcs) {
+      const int nsub = b.type == 0 ? 2 : 1;
+      for (int sub = 0; sub < nsub; ++sub) {
+        double wEn, sEn, wEx, sEx;
+        planeSpec(b, sub, wEn, sEn, wEx, sEx);
+        for (int i = 0; i < nInt; ++i) {
+          const double p = compc(pos[i], b.axis);
+          const double sd = (p - wEn) * sEn;            // vec < plane: compare() == 1
+          if (sd < 0.0 && !orc::fuzzyEqual(sd, 0.0)) {
+            comp(pos[i], b.axis) = mapCoord(p, wEn, sEn, wEx, sEx);
+            if (b.type == 1) comp(vel[i], b.axis) = -compc(vel[i], b.axis);
+          }
+        }
+      }
+    }
+  }
+
+  //----------------------------------------------------------------------------
+  // TreeGravity (TreeGravity.cc:146-480, 819-932; TreeGravityInline.hh:38-165).
+  //----------------------------------------------------------------------------
+  struct Cell {
+    double M = 0, Mglobal = 0; V3 xcm, vcm; double rcm2cc2 = 0; uint64_t key = 0;
+    vector<uint64_t> daughters; vector<Cell*> daughterPtrs;
+    vector<double> masses; vector<V3> positions, velocities;
+  };
+  static const int num1dbits = 21;
+  vector<std::unordered_map<uint64_t, Cell>> tree;
+  V3 gxmin, gxmax; double boxLength = 0;
+  void buildCellKey(int ilevel, const V3& xi, uint64_t& key, uint64_t& ix, uint64_t& iy, uint64_t& iz) const {
+    const uint64_t ncell = (1ULL << ilevel), maxcell = ncell - 1ULL, max1dKey = (1ULL << num1dbits) - 1ULL;
+    ix = std::min(maxcell, (uint64_t)((xi.x - gxmin.x) / boxLength * ncell));
+    iy = std::min(maxcell, (uint64_t)((xi.y - gxmin.y) / boxLength * ncell));
+    iz = std::min(maxcell, (uint64_t)((xi.z - gxmin.z) / boxLength * ncell));
+    key = (std::min(max1dKey, iz) << 2 * num1dbits) + (std::min(max1dKey, iy) << num1dbits) + std::min(max1dKey, ix);
+  }
+  void addNodeToTree(double mi, const V3& xi, const V3& vi) {
+    int ilevel = 0; bool terminated = false;
+    uint64_t key = 0, parentKey = 0, otherKey, ix, iy, iz;
+    while (ilevel < num1dbits && !terminated) {
+      if (ilevel == (int)tree.size()) tree.emplace_back();
+      buildCellKey(ilevel, xi, key, ix, iy, iz);
+      auto itr = tree[ilevel].find(key);
+      if (itr == tree[ilevel].end()) {
+        terminated = true;
+        Cell c; c.M = mi; c.Mglobal = mi; c.xcm = xi; c.vcm = vi; c.key = key;
+        c.masses = {mi}; c.positions = {xi}; c.velocities = {vi};
+        tree[ilevel][key] = c;
+      } else {
+        Cell& cell = itr->second;
+        if (!cell.masses.empty()) {
+          if (ilevel < num1dbits - 1) {
+            const int il1 = ilevel + 1;
+            if (il1 == (int)tree.size()) tree.emplace_back();   // capacity reserved: no reallocation
+            buildCellKey(il1, cell.xcm, otherKey, ix, iy, iz);
+            Cell d; d.M = cell.M; d.Mglobal = cell.M; d.xcm = cell.xcm; d.vcm = cell.vcm; d.key = otherKey;
+            d.masses = {cell.M}; d.positions = {cell.xcm}; d.velocities = {cell.vcm};
+            tree[il1][otherKey] = d;
+            cell.daughters = {otherKey};
+            cell.masses.clear(); cell.positions.clear(); cell.velocities.clear();
+          } else {
+            cell.masses.push_back(mi); cell.positions.push_back(xi); cell.velocities.push_back(vi);
+          }
+        }
+        const double Mn = cell.M + mi;
+        const V3 xs = add(mul(cell.M, cell.xcm), mul(mi, xi));
+        const V3 vs = add(mul(cell.M, cell.vcm), mul(mi, vi));
+        cell.xcm = V3{xs.x / Mn, xs.y / Mn, xs.z / Mn};
+        cell.vcm = V3{vs.x / Mn, vs.y / Mn, vs.z / Mn};
+        cell.M += mi;
+        cell.Mglobal = cell.M;
+      }
+      if (ilevel > 0) {
+        auto& par = tree[ilevel - 1][parentKey];
+        if (std::find(par.daughters.begin(), par.daughters.end(), key) == par.daughters.end()) par.daughters.push_back(key);
+      }
+      parentKey = key;
+      ++ilevel;
+    }
+  }
+  void buildTree() {
+    tree.clear();
+    tree.reserve(num1dbits);
+    if (nInt == 0) return;
+    gxmin = pos[0]; gxmax = pos[0];
+    for (int i = 0; i < nInt; ++i) {
+      gxmin.x = std::min(gxmin.x, pos[i].x); gxmin.y = std::min(gxmin.y, pos[i].y); gxmin.z = std::min(gxmin.z, pos[i].z);
+      gxmax.x = std::max(gxmax.x, pos[i].x); gxmax.y = std::max(gxmax.y, pos[i].y); gxmax.z = std::max(gxmax.z, pos[i].z);
+    }
+    boxLength = std::max(gxmax.x - gxmin.x, std::max(gxmax.y - gxmin.y, gxmax.z - gxmin.z));
+    for (int i = 0; i < nInt; ++i) addNodeToTree(mass[i], pos[i], vel[i]);
+    for (size_t l = 0; l + 1 < tree.size(); ++l)
+      for (auto& kv : tree[l]) {
+        kv.second.daughterPtrs.clear();
+        for (auto dk : kv.second.daughters) kv.second.daughterPtrs.push_back(&tree[l + 1][dk]);
+      }
+    for (size_t l = 0; l < tree.size(); ++l) {
+      const double cellsize = boxLength / (1U << l);
+      for (auto& kv : tree[l]) {
+        const uint64_t k = kv.first;
+        const uint64_t mask = (1ULL << num1dbits) - 1ULL;
+        const uint64_t ix = k & mask, iy = (k >> num1dbits) & mask, iz = (k >> 2 * num1dbits) & mask;
+        const V3 cc{gxmin.x + (ix + 0.5) * cellsize, gxmin.y + (iy + 0.5) * cellsize, gxmin.z + (iz + 0.5) * cellsize};
+        kv.second.rcm2cc2 = mag2(sub(kv.second.xcm, cc));
+      }
+    }
+  }
+  // applyTreeForces for one tree (single process: no remote trees, so the
+  // cellsCompleted sets never filter a cell).
+  void applyTreeForces() {
+    const double boxLength2 = boxLength * boxLength;
+    const double soft2 = cfg.softening * cfg.softening;
+    const double opening2 = cfg.opening * cfg.opening;
+    DvDtGrav.assign(nTot, V3{});
+    potential.assign(nTot, 0.0);
+    double result = std::numeric_limits<double>::max();
+    const int numLevels = (int)tree.size();
+    if (numLevels >= 1) {
+      const Cell& root = tree[0].begin()->second;
+#pragma omp parallel for schedule(dynamic, 64) reduction(min : result)
+      for (int i = 0; i < nInt; ++i) {
+        const V3 xi = pos[i];
+        V3 a{}; double phi = 0.0;
+        int ilevel = 0;
+        vector<Cell*> remaining = root.daughterPtrs, next;
+        while (!remaining.empty() && ++ilevel < numLevels) {
+          next.clear();
+          // 64-bit shift: the 32-bit form in the reference is only defined below level 16
+          const double cellsize2 = boxLength2 / (double)(1ULL << (2 * ilevel));
+          for (Cell* cp : remaining) {
+            const Cell& cell = *cp;
+            V3 xji = sub(cell.xcm, xi);
+            double rji2 = mag2(xji);
+            if (rji2 > cellsize2 / opening2 + cell.rcm2cc2) {
+              const V3 nhat = unitVector(xji);
+              rji2 += soft2;
+              a = add(a, mul(cell.Mglobal * (1.0 / rji2), nhat));
+              phi -= cell.Mglobal * (1.0 / std::sqrt(rji2));
+            } else if (cell.daughterPtrs.empty()) {
+              for (size_t j = 0; j < cell.masses.size(); ++j) {
+                const double mj = cell.masses[j];
+                V3 x2 = sub(cell.positions[j], xi);
+                double r2 = mag2(x2);
+                if (r2 / soft2 > 1.0e-10) {
+                  const V3 nhat = unitVector(x2);
+                  r2 += soft2;
+                  a = add(a, mul(mj * (1.0 / r2), nhat));
+                  phi -= mj * (1.0 / std::sqrt(r2));
+                }
+              }
+            } else {
+              next.insert(next.end(), cell.daughterPtrs.begin(), cell.daughterPtrs.end());
+            }
+          }
+          remaining.swap(next);
+        }
+        DvDtGrav[i] = a; potential[i] = phi;
+        const double amag = mag(a);
+        if (amag > 0.0) result = std::min(result, std::sqrt(cfg.softening / amag));
+      }
+    }
+    dtMinAcc = result / std::sqrt(cfg.G);
+    extraEnergy = 0.0;
+    for (int i = 0; i < nInt; ++i) {
+      DvDtGrav[i] = mul(DvDtGrav[i], cfg.G);
+      potential[i] *= cfg.G;
+      extraEnergy += 0.5 * mass[i] * potential[i];
+    }
+  }
+
+  //----------------------------------------------------------------------------
+  // Problem start-up (SPHBase::initializeProblemStartupDependencies): ghosts,
+  // connectivity, pressure, sound speed and the grad-h correction.
+  //----------------------------------------------------------------------------
+  void initialize() {
+    resizeDerivs();
+    setGhostNodes();
+    computeConnectivity();
+    applyGhostState();
+    updateEOS(nTot);
+    applyGhostState();
+    if (cfg.gradhCorrection) omegaGradh();
+  }
+
+  //----------------------------------------------------------------------------
+  // One Integrator::step -> CheapSynchronousRK2::step (no dt-check retry:
+  // allowDtCheck defaults to false).
+  //----------------------------------------------------------------------------
+  double step(double maxTime) {
+    setGhostNodes();
+    applyGhostState();
+    computeConnectivity();
+    const double t = time;
+    // preStepInitialize: RigorousSumDensity
+    if (cfg.densityUpdate == 0) sumMassDensity();
+    // initializeDerivatives(t, 0): TreeGravity::initialize builds the tree
+    if (cfg.gravity) buildTree();
+    const double dt = selectDt(std::min(cfg.dtMin, maxTime - t), std::min(cfg.dtMax, maxTime - t));
+    const double hdt = 0.5 * dt;
+    // state0 copy (internal + ghost values)
+    const auto pos0 = pos; const auto vel0 = vel; const auto rho0 = rho; const auto eps0 = eps;
+    const auto H0 = H; const auto P0 = P; const auto cs0 = cs; const auto omega0 = omega;
+    // mid-step: timeAdvanceOnly update with the previous derivatives
+    stateUpdate(hdt, true);
+    time = t + hdt;
+    applyGhostState();
+    if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
+    // derivatives at the midpoint
+    if (cfg.gravity) buildTree();
+    evaluateDerivatives();
+    if (cfg.gravity) applyTreeForces();
+    finalizeDerivatives();
+    // full step from state0
+    pos = pos0; vel = vel0; rho = rho0; eps = eps0; H = H0; P = P0; cs = cs0; omega = omega0;
+    stateUpdate(dt, false);
+    time = t + dt;
+    applyGhostState();
+    if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
+    enforceBoundaries();
+    ++cycle;
+    lastDt = dt;
+    return dt;
+  }
+
+  // Conserved totals (SpheralConservation.py:54-150): mass, momentum(3),
+  // kinetic, thermal, package (gravity) energy, total energy.
+  void conservation(double out[8]) const {
+    double m = 0, px = 0, py = 0, pz = 0, ke = 0, te = 0;
+    for (int i = 0; i < nInt; ++i) {
+      m += mass[i]; px += mass[i] * vel[i].x; py += mass[i] * vel[i].y; pz += mass[i] * vel[i].z;
+      ke += 0.5 * mass[i] * mag2(vel[i]); te += mass[i] * eps[i];
+    }
+    out[0] = m; out[1] = px; out[2] = py; out[3] = pz; out[4] = ke; out[5] = te;
+    out[6] = cfg.gravity ? extraEnergy : 0.0; out[7] = ke + te + out[6];
+  }
+};
+
+}  // namespace orc
+
+//==============================================================================
+// C ABI for the test harness (ctypes).
+//==============================================================================
+using orc::Problem;
+
+extern "C" {
+
+struct orc_config {
+  int num_table_points;
+  double cfl;
+  int use_velocity_magnitude_for_dt, compatible_energy, gradh_correction, xsph, correct_velocity_gradient,
+      sum_mass_density_over_all_nodelists, density_update;
+  double eps_tensile, n_tensile, Cl, Cq, eps2;
+  int linear_in_expansion, quadratic_in_expansion;
+  double dt_min, dt_max, dt_growth, last_dt, time;
+  int gravity;
+  double G, softening, opening, ftimestep;
+};
+
+void* orc_create(const orc_config* c) {
+  auto* p = new Problem();
+  auto& g = p->cfg;
+  g.numTablePoints = c->num_table_points; g.cfl = c->cfl; g.useVelocityMagnitudeForDt = c->use_velocity_magnitude_for_dt;
+  g.compatibleEnergy = c->compatible_energy; g.gradhCorrection = c->gradh_correction; g.XSPH = c->xsph;
+  g.correctVelocityGradient = c->correct_velocity_gradient; g.sumMassDensityOverAllNodeLists = c->sum_mass_density_over_all_nodelists;
+  g.densityUpdate = c->density_update; g.epsTensile = c->eps_tensile; g.nTensile = c->n_tensile;
+  g.Cl = c->Cl; g.Cq = c->Cq; g.eps2 = c->eps2; g.linearInExpansion = c->linear_in_expansion;
+  g.quadraticInExpansion = c->quadratic_in_expansion; g.dtMin = c->dt_min; g.dtMax = c->dt_max; g.dtGrowth = c->dt_growth;
+  g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
+  p->lastDt = c->last_dt; p->time = c->time;
+  p->W.build(c->num_table_points);
+  return p;
+}
+void orc_destroy(void* h) { delete static_cast<Problem*>(h); }
+
+int orc_set_nodelist(void* h, int L, double nPerh, double hmin, double hmax, double rhoMin, double rhoMax, double gamma) {
+  auto* p = static_cast<Problem*>(h);
+  if (L < 0) return 1;
+  if ((int)p->lists.size() <= L) p->lists.resize(L + 1);
+  auto& n = p->lists[L];
+  n.nPerh = nPerh; n.hmin = hmin; n.hmax = hmax; n.rhoMin = rhoMin; n.rhoMax = rhoMax; n.gamma = gamma;
+  return 0;
+}
+// type 0 periodic (lo, hi); type 1 reflecting wall at lo (wall_high=0) or hi (wall_high=1)
+int orc_add_boundary(void* h, int type, int axis, double lo, double hi, int wall_high) {
+  auto* p = static_cast<Problem*>(h);
+  orc::Boundary b; b.type = type; b.axis = axis; b.lo = lo; b.hi = hi; b.wallHigh = wall_high;
+  p->bcs.push_back(b);
+  return 0;
+}
+// H given as 6 components per node (xx, xy, xz, yy, yz, zz).
+int orc_set_particles(void* h, int n, const double* pos, const double* vel, const double* mass, const double* rho,
+                      const double* eps, const double* H, const int* list) {
+  auto* p = static_cast<Problem*>(h);
+  p->nInt = p->nTot = n;
+  p->resizeAll(n);
+  p->ctrl.assign(n, -1); p->image.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    p->pos[i] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    p->vel[i] = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+    p->mass[i] = mass[i]; p->rho[i] = rho[i]; p->eps[i] = eps[i];
+    p->H[i] = {H[6 * i], H[6 * i + 1], H[6 * i + 2], H[6 * i + 3], H[6 * i + 4], H[6 * i + 5]};
+    p->list[i] = list ? list[i] : 0;
+    p->omega[i] = 1.0;
+  }
+  if (p->lists.empty()) p->lists.resize(1);
+  p->rhoSum.clear();
+  p->resizeDerivs();
+  return 0;
+}
+int orc_initialize(void* h) { static_cast<Problem*>(h)->initialize(); return 0; }
+// Ghosts + connectivity + ghost state on the current positions.
+int orc_connectivity(void* h) {
+  auto* p = static_cast<Problem*>(h);
+  p->setGhostNodes(); p->applyGhostState(); p->computeConnectivity();
+  return 0;
+}
+int orc_update_eos(void* h) { auto* p = static_cast<Problem*>(h); p->updateEOS(p->nTot); return 0; }
+int orc_sum_density(void* h) { static_cast<Problem*>(h)->sumMassDensity(); return 0; }
+int orc_gradh(void* h) { auto* p = static_cast<Problem*>(h); p->omegaGradh(); return 0; }
+int orc_apply_ghosts(void* h) { static_cast<Problem*>(h)->applyGhostState(); return 0; }
+int orc_eval_derivs(void* h) {
+  auto* p = static_cast<Problem*>(h);
+  p->evaluateDerivatives();
+  p->finalizeDerivatives();
+  return 0;
+}
+double orc_hydro_dt(void* h) { return static_cast<Problem*>(h)->hydroDt(); }
+double orc_step(void* h, double maxTime) { return static_cast<Problem*>(h)->step(maxTime); }
+int orc_gravity(void* h) {
+  auto* p = static_cast<Problem*>(h);
+  p->buildTree(); p->applyTreeForces();
+  return 0;
+}
+int orc_num_internal(void* h) { return static_cast<Problem*>(h)->nInt; }
+int orc_num_total(void* h) { return static_cast<Problem*>(h)->nTot; }
+long orc_num_pairs(void* h) { return (long)static_cast<Problem*>(h)->pairs.size(); }
+double orc_time(void* h) { return static_cast<Problem*>(h)->time; }
+// Pair list as flat (i, j) with j possibly a ghost; ghosts resolved through
+// ctrl/image so the caller can compare against (control index, image code).
+int orc_get_pairs(void* h, int* i_out, int* jctrl_out, int* image_out) {
+  auto* p = static_cast<Problem*>(h);
+  for (size_t k = 0; k < p->pairs.size(); ++k) {
+    const int i = p->pairs[k].first, j = p->pairs[k].second;
+    i_out[k] = i;
+    jctrl_out[k] = j < p->nInt ? j : p->ctrl[j];
+    image_out[k] = j < p->nInt ? 0 : p->image[j];
+  }
+  return 0;
+}
+int orc_get_num_neighbors(void* h, int* out) {
+  auto* p = static_cast<Problem*>(h);
+  for (int i = 0; i < p->nInt; ++i) out[i] = p->numNeighbors[i];
+  return 0;
+}
+void orc_conservation(void* h, double* out) { static_cast<Problem*>(h)->conservation(out); }
+double orc_extra_energy(void* h) { return static_cast<Problem*>(h)->extraEnergy; }
+double orc_dt_min_acc(void* h) { return static_cast<Problem*>(h)->dtMinAcc; }
+
+// Field access by name (internal nodes only).  Returns number of components or -1.
+int orc_get_field(void* h, const char* name, double* out) {
+  auto* p = static_cast<Problem*>(h);
+  const std::string s(name);
+  const int n = p->nInt;
+  auto sc = [&](const std::vector<double>& f) { for (int i = 0; i < n; ++i) out[i] = f[i]; return 1; };
+  auto v3 = [&](const std::vector<orc::V3>& f) {
+    for (int i = 0; i < n; ++i) { out[3 * i] = f[i].x; out[3 * i + 1] = f[i].y; out[3 * i + 2] = f[i].z; }
+    return 3;
+  };
+  auto t9 = [&](const std::vector<orc::T9>& f) {
+    for (int i = 0; i < n; ++i) {
+      const auto& t = f[i]; double* o = out + 9 * i;
+      o[0] = t.xx; o[1] = t.xy; o[2] = t.xz; o[3] = t.yx; o[4] = t.yy; o[5] = t.yz; o[6] = t.zx; o[7] = t.zy; o[8] = t.zz;
+    }
+    return 9;
+  };
+  auto s6 = [&](const std::vector<orc::ST>& f) {
+    for (int i = 0; i < n; ++i) {
+      const auto& t = f[i]; double* o = out + 6 * i;
+      o[0] = t.xx; o[1] = t.xy; o[2] = t.xz; o[3] = t.yy; o[4] = t.yz; o[5] = t.zz;
+    }
+    return 6;
+  };
+  if (s == "position") return v3(p->pos);
+  if (s == "velocity") return v3(p->vel);
+  if (s == "mass") return sc(p->mass);
+  if (s == "massDensity") return sc(p->rho);
+  if (s == "specificThermalEnergy") return sc(p->eps);
+  if (s == "H") return s6(p->H);
+  if (s == "pressure") return sc(p->P);
+  if (s == "soundSpeed") return sc(p->cs);
+  if (s == "omegaGradh") return sc(p->omega);
+  if (s == "massDensitySum") return sc(p->rhoSum);
+  if (s == "normalization") return sc(p->normalization);
+  if (s == "DxDt") return v3(p->DxDt);
+  if (s == "DvDt") return v3(p->DvDt);
+  if (s == "DrhoDt") return sc(p->DrhoDt);
+  if (s == "DepsDt") return sc(p->DepsDt);
+  if (s == "DvDx") return t9(p->DvDx);
+  if (s == "internalDvDx") return t9(p->localDvDx);
+  if (s == "gradRho") return v3(p->gradRho);
+  if (s == "M") return t9(p->M);
+  if (s == "localM") return t9(p->localM);
+  if (s == "maxViscousPressure") return sc(p->maxQ);
+  if (s == "effViscousPressure") return sc(p->effQ);
+  if (s == "XSPHWeightSum") return sc(p->XSPHWeightSum);
+  if (s == "XSPHDeltaV") return v3(p->XSPHDeltaV);
+  if (s == "DHDt") return s6(p->DHDt);
+  if (s == "Hideal") return s6(p->Hideal);
+  if (s == "massZerothMoment") return sc(p->massZeroth);
+  if (s == "massFirstMoment") return v3(p->massFirst);
+  if (s == "DvDtGravity") return v3(p->DvDtGrav);
+  if (s == "potential") return sc(p->potential);
+  if (s == "DepsDtCompatible") return sc(p->DepsDtCompat);
+  return -1;
+}
+// Overwrite a state field (internal nodes) by name.
+int orc_set_field(void* h, const char* name, const double* in) {
+  auto* p = static_cast<Problem*>(h);
+  const std::string s(name);
+  const int n = p->nInt;
+  if (s == "pressure") { for (int i = 0; i < n; ++i) p->P[i] = in[i]; return 0; }
+  if (s == "soundSpeed") { for (int i = 0; i < n; ++i) p->cs[i] = in[i]; return 0; }
+  if (s == "omegaGradh") { for (int i = 0; i < n; ++i) p->omega[i] = in[i]; return 0; }
+  if (s == "massDensity") { for (int i = 0; i < n; ++i) p->rho[i] = in[i]; return 0; }
+  if (s == "specificThermalEnergy") { for (int i = 0; i < n; ++i) p->eps[i] = in[i]; return 0; }
+  return -1;
+}
+// Kernel table export: W, gradW, grad2W coefficient arrays (3*(N1+1) each),
+// and the Hermite nperh/Wsum lookups (2*n each).  meta: [N1, xstep, nH,
+// nperh_xmin, nperh_xmax, wsum_xmin, wsum_xmax, minNperh, maxNperh].
+int orc_table(void* h, double* w, double* g, double* g2, double* nperh, double* wsum, double* meta) {
+  auto* p = static_cast<Problem*>(h);
+  const auto& W = p->W;
+  for (size_t k = 0; k < W.W.c.size(); ++k) { w[k] = W.W.c[k]; g[k] = W.gW.c[k]; g2[k] = W.g2W.c[k]; }
+  for (size_t k = 0; k < W.nperhLookup.v.size(); ++k) { nperh[k] = W.nperhLookup.v[k]; wsum[k] = W.wsumLookup.v[k]; }
+  meta[0] = (double)W.W.N1; meta[1] = W.W.xstep; meta[2] = (double)W.nperhLookup.N;
+  meta[3] = W.nperhLookup.xmin; meta[4] = W.nperhLookup.xmax; meta[5] = W.wsumLookup.xmin; meta[6] = W.wsumLookup.xmax;
+  meta[7] = W.minNperh; meta[8] = W.maxNperh;
+  return 0;
+}
+double orc_kernel_value(void* h, double eta, double Hdet) { return static_cast<Problem*>(h)->W.kernelValue(eta, Hdet); }
+double orc_grad_value(void* h, double eta, double Hdet) {
+  double w, g; static_cast<Problem*>(h)->W.kernelAndGradValue(eta, Hdet, w, g); return g;
+}
+double orc_nperh_lookup(void* h, double wsum) { return static_cast<Problem*>(h)->W.equivalentNodesPerSmoothingScale(wsum); }
+double orc_wsum_lookup(void* h, double nperh) { return static_cast<Problem*>(h)->W.equivalentWsum(nperh); }
+double orc_bspline_value(double eta) { return orc::BSpline3().value(eta, 1.0); }
+double orc_bspline_grad(double eta) { return orc::BSpline3().grad(eta, 1.0); }
+int orc_num_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+}  // extern "C"

@@ -1,0 +1,978 @@
+// libsphgpu host runtime: device-resident state, the neighbour-list build,
+// the CheapSynchronousRK2 step orchestration and the C ABI of include/sphgpu.h.
+#include "../../include/sphgpu.h"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace sph {
+namespace table {
+int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* nperh, double* wsum, double* meta);
+}
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CUDA_OK(expr)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (expr);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      throw ::sph::Error(SPHGPU_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Grow-only device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t b) {
+    if (b <= bytes) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    CUDA_OK(cudaMalloc(&p, b));
+    bytes = b;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct Profiler {
+  bool on = false;
+  struct Rec { std::string name; cudaEvent_t a, b; };
+  std::vector<Rec> pending;
+  std::map<std::string, std::pair<long, double>> acc;
+  cudaStream_t s = nullptr;
+  void begin(const char* name, cudaEvent_t* a) {
+    if (!on) return;
+    CUDA_OK(cudaEventCreate(a));
+    CUDA_OK(cudaEventRecord(*a, s));
+    (void)name;
+  }
+  void end(const char* name, cudaEvent_t a) {
+    if (!on) return;
+    cudaEvent_t b;
+    CUDA_OK(cudaEventCreate(&b));
+    CUDA_OK(cudaEventRecord(b, s));
+    pending.push_back({name, a, b});
+  }
+  void collect() {
+    if (pending.empty()) return;
+    CUDA_OK(cudaStreamSynchronize(s));
+    for (auto& r : pending) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      auto& e = acc[r.name];
+      e.first += 1;
+      e.second += ms;
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    pending.clear();
+  }
+};
+
+struct Scope {
+  Profiler& p;
+  const char* n;
+  cudaEvent_t a{};
+  Scope(Profiler& p_, const char* n_) : p(p_), n(n_) { p.begin(n, &a); }
+  ~Scope() {
+    try { p.end(n, a); } catch (...) {}
+  }
+};
+
+struct Boundary {
+  int type, axis;
+  double lo, hi;
+  int wallHigh;
+};
+
+}  // namespace sph
+
+using namespace sph;
+
+struct sphgpu_ctx {
+  sphgpu_config cfg{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  LaunchCounter lc;
+  Profiler prof;
+
+  // parameters
+  NodeListParams lists[kMaxNodeLists]{};
+  int numLists = 0;
+  std::vector<Boundary> bcs;
+  HydroParams hp{};
+  bool haveTable = false;
+  std::vector<double> tw, tg, tg2, therm, twsum;
+  double tmeta[9]{};
+  DBuf dTable;   // w | g | herm (FP64) then w32 | g32
+
+  // particles
+  long n = 0;
+  DBuf bankA, bankB;   // F_NUM_FIELDS * cap doubles each
+  Fields F{}, Falt{};
+  DBuf orig[2], list[2], cellc[2];
+  int cur = 0;
+  long cap = 0;
+  // neighbour build
+  Grid grid{};
+  DBuf keys, vals, keysAlt, valsAlt, sortWs, cellStart, cellEnd, counts, nbrStart, nbr, scanWs, pacc;
+  size_t cellSpace = 0;
+  long long nnbr = 0;
+  bool haveNeighbors = false;
+  // scratch
+  DBuf scratch, small;
+  double* hsmall = nullptr;   // pinned
+  // integrator
+  double time = 0.0, lastDt = 1e-5, dtMultiplier = 1.0;
+  long cycle = 0;
+  double dtMinAcc = 1e300, extraEnergy = 0.0;
+  GravityWork* grav = nullptr;
+  bool initialized = false;
+
+  Fields fieldsOf(DBuf& bank) {
+    Fields f{};
+    for (int k = 0; k < F_NUM_FIELDS; ++k) f.f[k] = bank.as<double>() + (size_t)k * cap;
+    return f;
+  }
+  int* origp() { return orig[cur].as<int>(); }
+  int* listp() { return list[cur].as<int>(); }
+  uint32_t* cellp() { return cellc[cur].as<uint32_t>(); }
+  double maxNperh() const {
+    double m = 0.0;
+    for (int k = 0; k < std::max(1, numLists); ++k) m = std::max(m, lists[k].nPerh);
+    return m;
+  }
+  TableDev tableDev() {
+    TableDev t;
+    const size_t nc = tw.size();
+    double* base = dTable.as<double>();
+    t.w = base;
+    t.g = base + nc;
+    t.herm = base + 2 * nc;
+    float* b32 = reinterpret_cast<float*>(base + 2 * nc + therm.size());
+    t.w32 = b32;
+    t.g32 = b32 + nc;
+    return t;
+  }
+  NeighborLists nl() const { return NeighborLists{nbrStart.as<long long>(), nbr.as<uint32_t>()}; }
+  void check() { CUDA_OK(cudaGetLastError()); }
+};
+
+namespace {
+
+void ensureCapacity(sphgpu_ctx* c, long n) {
+  if (n <= c->cap) return;
+  c->cap = n;
+  const size_t bytes = (size_t)F_NUM_FIELDS * n * sizeof(double);
+  c->bankA.release();
+  c->bankB.release();
+  c->bankA.ensure(bytes);
+  c->bankB.ensure(bytes);
+  for (int k = 0; k < 2; ++k) {
+    c->orig[k].release(); c->orig[k].ensure(n * sizeof(int));
+    c->list[k].release(); c->list[k].ensure(n * sizeof(int));
+    c->cellc[k].release(); c->cellc[k].ensure(n * sizeof(uint32_t));
+  }
+}
+
+void setTable(sphgpu_ctx* c, const double* w, const double* g, const double* g2, const double* nperh,
+              const double* wsum, const double* meta) {
+  const int N1 = (int)meta[0];
+  const int nh = (int)meta[2];
+  if (N1 < 1 || 3 * (N1 + 1) > kMaxTable || nh < 3) throw Error(SPHGPU_E_ARG, "kernel table size out of range");
+  const size_t nc = 3 * (size_t)(N1 + 1);
+  c->tw.assign(w, w + nc);
+  c->tg.assign(g, g + nc);
+  c->tg2.assign(g2, g2 + nc);
+  c->therm.assign(nperh, nperh + 2 * nh);
+  c->twsum.assign(wsum, wsum + 2 * nh);
+  std::memcpy(c->tmeta, meta, sizeof(c->tmeta));
+  std::vector<double> host(2 * nc + c->therm.size());
+  std::copy(c->tw.begin(), c->tw.end(), host.begin());
+  std::copy(c->tg.begin(), c->tg.end(), host.begin() + nc);
+  std::copy(c->therm.begin(), c->therm.end(), host.begin() + 2 * nc);
+  std::vector<float> h32(2 * nc);
+  for (size_t k = 0; k < nc; ++k) { h32[k] = (float)c->tw[k]; h32[nc + k] = (float)c->tg[k]; }
+  const size_t bytes = host.size() * sizeof(double) + h32.size() * sizeof(float);
+  c->dTable.ensure(bytes);
+  CUDA_OK(cudaMemcpy(c->dTable.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OK(cudaMemcpy(static_cast<char*>(c->dTable.p) + host.size() * sizeof(double), h32.data(),
+                     h32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // Derived constants
+  auto& hp = c->hp;
+  hp.tableN1 = N1;
+  hp.tableXstep = meta[1];
+  hp.extent = 2.0;
+  hp.W0 = 1.0 * (c->tw[0] + (c->tw[1] + c->tw[2] * 0.0) * 0.0);
+  hp.hermN = nh;
+  hp.hermXmin = meta[3];
+  hp.hermXmax = meta[4];
+  hp.hermXstep = (meta[4] - meta[3]) / (nh - 1);
+  c->haveTable = true;
+}
+
+double tableW(const sphgpu_ctx* c, double eta) {   // TableKernel::kernelValue(eta, 1)
+  if (!(eta < c->hp.extent)) return 0.0;
+  const size_t i0 = 3u * std::min((size_t)c->hp.tableN1, size_t(std::max(0.0, eta) / c->hp.tableXstep));
+  return 1.0 * (c->tw[i0] + (c->tw[i0 + 1] + c->tw[i0 + 2] * eta) * eta);
+}
+
+void refreshParams(sphgpu_ctx* c) {
+  auto& hp = c->hp;
+  const auto& g = c->cfg;
+  hp.compatible = g.compatible_energy;
+  hp.gradh = g.gradh_correction;
+  hp.xsph = g.xsph;
+  hp.correctVelGrad = g.correct_velocity_gradient;
+  hp.sumAllLists = g.sum_mass_density_over_all_nodelists;
+  hp.densityUpdate = g.density_update;
+  hp.linearInExpansion = g.linear_in_expansion;
+  hp.quadraticInExpansion = g.quadratic_in_expansion;
+  hp.useVelMagDt = g.use_velocity_magnitude_for_dt;
+  hp.epsTensile = g.eps_tensile;
+  hp.nTensile = g.n_tensile;
+  hp.Cl = g.Cl;
+  hp.Cq = g.Cq;
+  hp.eps2 = g.eps2;
+  hp.cfl = g.cfl;
+  hp.numLists = std::max(1, c->numLists);
+  if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
+}
+
+void requireState(sphgpu_ctx* c) {
+  if (!c->haveTable) throw Error(SPHGPU_E_STATE, "no kernel table installed");
+  if (c->n <= 0) throw Error(SPHGPU_E_STATE, "no particles");
+}
+
+//------------------------------------------------------------------------------
+// Grid for the cell list: periodic axes span their planes, reflecting walls
+// bound their side, open sides follow the bounding box.  Cells are at least
+// kernelExtent * hmax (strictly larger, so every interacting pair lies in
+// adjacent cells).
+//------------------------------------------------------------------------------
+void buildGrid(sphgpu_ctx* c) {
+  Scope sc(c->prof, "bounds");
+  double* d = c->small.as<double>();
+  c->scratch.ensure(7 * sizeof(double) * 4096);
+  launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, d, c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(c->hsmall, d, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  const double minHinv = c->hsmall[0];
+  if (!(minHinv > 0.0) || !std::isfinite(minHinv)) throw Error(SPHGPU_E_NAN, "non-positive or non-finite H");
+  const double hmax = 1.0 / minHinv;
+  const double support = c->hp.extent * hmax * (1.0 + 1.0e-9);
+  Grid g{};
+  for (int a = 0; a < 3; ++a) {
+    g.kindLo[a] = g.kindHi[a] = AXIS_OPEN;
+    g.wallLo[a] = c->hsmall[1 + a];
+    g.wallHi[a] = c->hsmall[4 + a];
+  }
+  for (const auto& b : c->bcs) {
+    if (b.type == SPHGPU_BOUNDARY_PERIODIC) {
+      g.kindLo[b.axis] = g.kindHi[b.axis] = AXIS_PERIODIC;
+      g.wallLo[b.axis] = b.lo;
+      g.wallHi[b.axis] = b.hi;
+    } else if (b.wallHigh) {
+      g.kindHi[b.axis] = AXIS_REFLECT;
+      g.wallHi[b.axis] = b.hi;
+    } else {
+      g.kindLo[b.axis] = AXIS_REFLECT;
+      g.wallLo[b.axis] = b.lo;
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    const double lo = g.kindLo[a] == AXIS_OPEN ? c->hsmall[1 + a] : g.wallLo[a];
+    const double hi = g.kindHi[a] == AXIS_OPEN ? c->hsmall[4 + a] : g.wallHi[a];
+    const double L = hi - lo;
+    int nc = (int)std::min(1024.0, std::floor(L / support));
+    if (g.kindLo[a] == AXIS_PERIODIC) {
+      if (nc < 3)
+        throw Error(SPHGPU_E_UNSUPPORTED,
+                    "periodic box narrower than three kernel supports on axis " + std::to_string(a));
+    } else {
+      nc = std::max(1, nc);
+    }
+    // cell >= support: every interacting pair sits in adjacent cells
+    const double cell = std::max(L / nc, support);
+    g.lo[a] = lo;
+    g.hi[a] = hi;
+    g.cell[a] = cell;
+    g.nc[a] = nc;
+    if (g.kindLo[a] != AXIS_PERIODIC) {   // open sides: the grid origin follows the data
+      if (g.kindLo[a] == AXIS_OPEN) g.wallLo[a] = lo;
+      if (g.kindHi[a] == AXIS_OPEN) g.wallHi[a] = hi;
+    }
+  }
+  c->grid = g;
+}
+
+//------------------------------------------------------------------------------
+// Neighbour build: cell keys -> stable radix sort -> permute every field ->
+// cell ranges -> count -> scan -> fill.
+//------------------------------------------------------------------------------
+void buildNeighbors(sphgpu_ctx* c) {
+  const long n = c->n;
+  buildGrid(c);
+  const Grid& g = c->grid;
+  int bitsAxis = 0;
+  while ((1 << bitsAxis) < std::max(g.nc[0], std::max(g.nc[1], g.nc[2]))) ++bitsAxis;
+  const int keyBits = std::max(1, 3 * bitsAxis);
+  c->keys.ensure(n * sizeof(uint32_t));
+  c->keysAlt.ensure(n * sizeof(uint32_t));
+  c->vals.ensure(n * sizeof(int));
+  c->valsAlt.ensure(n * sizeof(int));
+  c->sortWs.ensure(radixSortWorkspaceBytes(n));
+  {
+    Scope sc(c->prof, "cell_keys");
+    launchCellKeys(c->F, n, g, c->keys.as<uint32_t>(), c->vals.as<int>(), c->cellp(), c->stream, &c->lc);
+  }
+  uint32_t* k = c->keys.as<uint32_t>();
+  int* v = c->vals.as<int>();
+  uint32_t* ka = c->keysAlt.as<uint32_t>();
+  int* va = c->valsAlt.as<int>();
+  {
+    Scope sc(c->prof, "radix_sort");
+    radixSortPairs(k, v, ka, va, n, ((keyBits + 7) / 8) * 8, c->sortWs.p, c->stream, &c->lc);
+  }
+  c->check();
+  {
+    Scope sc(c->prof, "permute");
+    const int nx = 1 - c->cur;
+    launchPermute(c->F, c->Falt, v, c->orig[c->cur].as<int>(), c->orig[nx].as<int>(), c->list[c->cur].as<int>(),
+                  c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n, c->stream,
+                  &c->lc);
+    std::swap(c->bankA, c->bankB);
+    std::swap(c->F, c->Falt);
+    c->cur = nx;
+  }
+  c->check();
+  const size_t space = (size_t)1 << keyBits;
+  if (space > c->cellSpace) {
+    c->cellStart.release(); c->cellEnd.release();
+    c->cellStart.ensure(space * sizeof(int));
+    c->cellEnd.ensure(space * sizeof(int));
+    c->cellSpace = space;
+  }
+  CUDA_OK(cudaMemsetAsync(c->cellStart.p, 0, space * sizeof(int), c->stream));
+  CUDA_OK(cudaMemsetAsync(c->cellEnd.p, 0, space * sizeof(int), c->stream));
+  {
+    Scope sc(c->prof, "cell_ranges");
+    launchCellRanges(k, n, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->stream, &c->lc);
+  }
+  c->counts.ensure(n * sizeof(int));
+  c->nbrStart.ensure((n + 1) * sizeof(long long));
+  c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
+  const double ext2 = c->hp.extent * c->hp.extent;
+  {
+    Scope sc(c->prof, "neighbor_count");
+    launchNeighborCount(c->F, c->cellp(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
+                        ext2, c->stream, &c->lc);
+  }
+  long long* dTot = c->nbrStart.as<long long>() + n;
+  scanExclusive<int>(c->counts.as<int>(), c->nbrStart.as<long long>(), n, c->scanWs.p, dTot, c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(c->hsmall, dTot, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  long long total;
+  std::memcpy(&total, c->hsmall, sizeof(long long));
+  c->nnbr = total;
+  c->nbr.ensure(std::max<long long>(1, total) * sizeof(uint32_t));
+  {
+    Scope sc(c->prof, "neighbor_fill");
+    launchNeighborFill(c->F, c->cellp(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->nbrStart.as<long long>(),
+                       c->nbr.as<uint32_t>(), ext2, c->stream, &c->lc);
+  }
+  c->check();
+  c->haveNeighbors = true;
+}
+
+void ensurePacc(sphgpu_ctx* c) {
+  const size_t per = c->cfg.precision == SPHGPU_PRECISION_FP32 ? sizeof(float) : sizeof(double);
+  c->pacc.ensure(std::max<long long>(1, c->nnbr) * 3 * per);
+}
+
+void sumDensity(sphgpu_ctx* c) {
+  Scope sc(c->prof, "sum_density");
+  launchSumDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  c->check();
+}
+void gradh(sphgpu_ctx* c) {
+  Scope sc(c->prof, "gradh");
+  launchGradh(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  c->check();
+}
+void evalDerivs(sphgpu_ctx* c) {
+  ensurePacc(c);
+  {
+    Scope sc(c->prof, "pair_fp64");
+    launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists, c->pacc.as<double>(),
+                   128, c->stream, &c->lc);
+  }
+  c->check();
+  if (c->cfg.gravity) {
+    Scope sc(c->prof, "gravity");
+    char msg[256] = {0};
+    double* d = c->small.as<double>() + 16;
+    const int rc = gravityEvaluate(c->grav, c->F, c->n, c->cfg.G, c->cfg.softening, c->cfg.opening, d, c->stream,
+                                   &c->lc, msg, sizeof(msg));
+    if (rc != SPHGPU_OK) throw Error(rc, std::string("gravity: ") + msg);
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 16, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    c->dtMinAcc = c->hsmall[16];
+    c->extraEnergy = c->hsmall[17];
+  }
+}
+
+// Integrator::selectDt (src/Integrator/Integrator.cc:116-169).
+double packageDt(sphgpu_ctx* c, int* reason) {
+  Scope sc(c->prof, "dt");
+  const long nb = (c->n + 127) / 128;
+  c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
+  double* d = c->small.as<double>();
+  launchDt(c->F, c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(), c->scratch.as<double>(),
+           (int)(2 * nb), d, c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(c->hsmall, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  double dt = c->hsmall[0] * c->cfg.cfl;
+  int r = (int)c->hsmall[1];
+  if (c->cfg.gravity) {
+    const double gdt = c->cfg.ftimestep * c->dtMinAcc;
+    if (gdt < dt) { dt = gdt; r = 6; }
+  }
+  if (reason) *reason = r;
+  return dt;
+}
+
+double selectDt(sphgpu_ctx* c, double dtMin, double dtMax) {
+  double dt = dtMax;
+  int r;
+  const double v = packageDt(c, &r);
+  if (v > 0.0 && v < dt) dt = v;
+  dt *= c->dtMultiplier;
+  dt = std::min(dt, c->cfg.dt_growth * c->lastDt);
+  dt = std::min(dtMax, std::max(dtMin, dt));
+  return dt;
+}
+
+void checkState(sphgpu_ctx* c, const char* where) {
+  int* flag = reinterpret_cast<int*>(c->small.as<double>() + 30);
+  CUDA_OK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+  launchCheckState(c->F, c->n, flag, c->stream, &c->lc);
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 30, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  int h;
+  std::memcpy(&h, c->hsmall + 30, sizeof(int));
+  if (h) throw Error(SPHGPU_E_NAN, std::string("non-finite or non-positive state after ") + where);
+}
+
+// CheapSynchronousRK2::step (src/Integrator/CheapSynchronousRK2.cc:40-132).
+double step(sphgpu_ctx* c, double maxTime) {
+  requireState(c);
+  refreshParams(c);
+  buildNeighbors(c);                                 // Integrator::setGhostNodes + connectivity
+  if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) sumDensity(c);   // preStepInitialize
+  const double t = c->time;
+  const double dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t));
+  const double hdt = 0.5 * dt;
+  {
+    Scope sc(c->prof, "update");
+    launchSaveState0(c->F, c->n, c->stream, &c->lc);
+    launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, hdt, true, c->cfg.gravity != 0, c->stream, &c->lc);
+  }
+  c->check();
+  c->time = t + hdt;
+  if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
+  evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
+  {
+    Scope sc(c->prof, "update");
+    launchRestoreState0(c->F, c->n, c->stream, &c->lc);
+  }
+  if (c->cfg.compatible_energy) {
+    Scope sc(c->prof, "energy");
+    launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);
+  }
+  {
+    Scope sc(c->prof, "update");
+    launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, dt, false, c->cfg.gravity != 0, c->stream, &c->lc);
+  }
+  c->check();
+  c->time = t + dt;
+  if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
+  {
+    Scope sc(c->prof, "enforce");
+    launchEnforce(c->F, c->n, c->grid, c->stream, &c->lc);
+  }
+  c->check();
+  checkState(c, "the step");
+  c->cycle += 1;
+  c->lastDt = dt;
+  return dt;
+}
+
+struct FieldSpec {
+  int first;
+  int ncomp;
+};
+bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb) {
+  isH = false;
+  isNumNb = false;
+  static const std::map<std::string, FieldSpec> m = {
+      {"position", {F_X, 3}}, {"velocity", {F_VX, 3}}, {"mass", {F_MASS, 1}}, {"massDensity", {F_RHO, 1}},
+      {"specificThermalEnergy", {F_EPS, 1}}, {"pressure", {F_P, 1}}, {"soundSpeed", {F_CS, 1}},
+      {"omegaGradh", {F_OMEGA, 1}}, {"massDensitySum", {F_RHOSUM, 1}}, {"normalization", {F_NORM, 1}},
+      {"DxDt", {F_DXDT_X, 3}}, {"DvDt", {F_DVDT_X, 3}}, {"DrhoDt", {F_DRHODT, 1}}, {"DepsDt", {F_DEPSDT, 1}},
+      {"DvDx", {F_DVDX_XX, 9}}, {"internalDvDx", {F_DVDX_XX, 9}}, {"gradRho", {F_GRADRHO_X, 3}},
+      {"M", {F_M_XX, 9}}, {"localM", {F_M_XX, 9}}, {"maxViscousPressure", {F_MAXQ, 1}},
+      {"effViscousPressure", {F_EFFQ, 1}}, {"XSPHWeightSum", {F_XSPHW, 1}}, {"XSPHDeltaV", {F_XSPHDV_X, 3}},
+      {"massZerothMoment", {F_M0, 1}}, {"massFirstMoment", {F_M1_X, 3}}, {"DvDtGravity", {F_GRAV_X, 3}},
+      {"potential", {F_POT, 1}}, {"DepsDtCompatible", {F_DEPS_COMPAT, 1}}};
+  if (s == "H" || s == "Hideal" || s == "DHDt") {
+    isH = true;
+    fs = {s == "H" ? F_HINV : (s == "Hideal" ? F_HIDEAL : F_DHDT), 6};
+    return true;
+  }
+  if (s == "numNeighbors") {
+    isNumNb = true;
+    fs = {0, 1};
+    return true;
+  }
+  auto it = m.find(s);
+  if (it == m.end()) return false;
+  fs = it->second;
+  return true;
+}
+
+int fail(sphgpu_ctx* c, const Error& e) {
+  if (c) c->err = e.what();
+  return e.code;
+}
+int failStd(sphgpu_ctx* c, const std::exception& e) {
+  if (c) c->err = e.what();
+  return SPHGPU_E_CUDA;
+}
+
+#define API_BEGIN(h) \
+  if (!(h)) return SPHGPU_E_ARG; \
+  try {
+#define API_END(h)                        \
+  }                                       \
+  catch (const Error& e) {                \
+    return fail(h, e);                    \
+  }                                       \
+  catch (const std::exception& e) {       \
+    return failStd(h, e);                 \
+  }                                       \
+  return SPHGPU_OK;
+
+}  // namespace
+
+extern "C" {
+
+void sphgpu_default_config(sphgpu_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->num_table_points = 1000;
+  c->cfl = 0.25;
+  c->use_velocity_magnitude_for_dt = 0;
+  c->compatible_energy = 1;
+  c->gradh_correction = 1;
+  c->xsph = 0;
+  c->correct_velocity_gradient = 1;
+  c->sum_mass_density_over_all_nodelists = 1;
+  c->density_update = SPHGPU_DENSITY_RIGOROUS_SUM;
+  c->eps_tensile = 0.0;
+  c->n_tensile = 4.0;
+  c->Cl = 1.0;
+  c->Cq = 1.0;
+  c->eps2 = 1.0e-2;
+  c->dt_min = 0.0;
+  c->dt_max = 1.0e300;
+  c->dt_growth = 2.0;
+  c->last_dt = 1.0e-5;
+  c->time = 0.0;
+  c->gravity = 0;
+  c->G = 1.0;
+  c->softening = 0.01;
+  c->opening = 0.5;
+  c->ftimestep = 0.1;
+  c->precision = SPHGPU_PRECISION_FP64;
+  c->device = 0;
+}
+
+int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
+  if (!cfg || !out) return SPHGPU_E_ARG;
+  *out = nullptr;
+  auto* c = new sphgpu_ctx();
+  try {
+    c->cfg = *cfg;
+    if (cfg->precision != SPHGPU_PRECISION_FP64 && cfg->precision != SPHGPU_PRECISION_FP32)
+      throw Error(SPHGPU_E_ARG, "unknown precision mode");
+    if (cfg->density_update != SPHGPU_DENSITY_RIGOROUS_SUM && cfg->density_update != SPHGPU_DENSITY_INTEGRATE)
+      throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
+    CUDA_OK(cudaSetDevice(cfg->device));
+    CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->prof.s = c->stream;
+    c->small.ensure(64 * sizeof(double));
+    CUDA_OK(cudaMallocHost(&c->hsmall, 64 * sizeof(double)));
+    c->time = cfg->time;
+    c->lastDt = cfg->last_dt;
+    c->lists[0] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308};
+    c->numLists = 0;
+    if (cfg->gravity) c->grav = gravityCreate();
+    // Build the default cubic B-spline table.
+    const int np = cfg->num_table_points > 0 ? cfg->num_table_points : 1000;
+    const int nq = np | 1;
+    std::vector<double> w(3 * ((nq - 1) / 2)), g(w.size()), g2(w.size()), nh(2 * np), ws(2 * np), meta(9);
+    if (table::buildBSplineTable(np, w.data(), g.data(), g2.data(), nh.data(), ws.data(), meta.data()) != 0)
+      throw Error(SPHGPU_E_ARG, "bad num_table_points");
+    setTable(c, w.data(), g.data(), g2.data(), nh.data(), ws.data(), meta.data());
+    refreshParams(c);
+  } catch (const Error& e) {
+    const int code = e.code;
+    sphgpu_destroy(c);
+    return code;
+  } catch (const std::exception& e) {
+    sphgpu_destroy(c);
+    return SPHGPU_E_CUDA;
+  }
+  *out = c;
+  return SPHGPU_OK;
+}
+
+int sphgpu_destroy(sphgpu_handle c) {
+  if (!c) return SPHGPU_E_ARG;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->prof.on = false;
+  for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
+                  &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
+                  &c->scratch, &c->small};
+  for (auto* b : bufs) b->release();
+  for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
+  if (c->grav) gravityDestroy(c->grav);
+  if (c->hsmall) cudaFreeHost(c->hsmall);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return SPHGPU_OK;
+}
+
+const char* sphgpu_last_error(sphgpu_handle c) { return c ? c->err.c_str() : "null handle"; }
+
+int sphgpu_build_bspline_table(int num_points, double* w, double* grad, double* grad2, double* nperh, double* wsum,
+                               double* meta) {
+  if (!w || !grad || !grad2 || !nperh || !wsum || !meta) return SPHGPU_E_ARG;
+  return sph::table::buildBSplineTable(num_points, w, grad, grad2, nperh, wsum, meta) == 0 ? SPHGPU_OK
+                                                                                           : SPHGPU_E_ARG;
+}
+
+int sphgpu_set_kernel_table(sphgpu_handle c, const double* w, const double* grad, const double* grad2,
+                            const double* nperh, const double* wsum, const double* meta) {
+  API_BEGIN(c)
+  if (!w || !grad || !grad2 || !nperh || !wsum || !meta) throw Error(SPHGPU_E_ARG, "null table pointer");
+  setTable(c, w, grad, grad2, nperh, wsum, meta);
+  refreshParams(c);
+  API_END(c)
+}
+
+int sphgpu_set_nodelist(sphgpu_handle c, int k, double nPerh, double hmin, double hmax, double rhoMin, double rhoMax,
+                        double gamma) {
+  API_BEGIN(c)
+  if (k < 0 || k >= kMaxNodeLists) throw Error(SPHGPU_E_ARG, "nodelist index out of range");
+  if (!(nPerh > 0.0) || !(hmin > 0.0) || !(hmax >= hmin) || !(gamma > 1.0))
+    throw Error(SPHGPU_E_ARG, "bad nodelist parameters");
+  c->lists[k] = NodeListParams{nPerh, hmin, hmax, rhoMin, rhoMax, gamma, -1.7976931348623157e308,
+                               1.7976931348623157e308};
+  c->numLists = std::max(c->numLists, k + 1);
+  refreshParams(c);
+  API_END(c)
+}
+
+int sphgpu_add_boundary(sphgpu_handle c, int type, int axis, double lo, double hi, int wall_high) {
+  API_BEGIN(c)
+  if (axis < 0 || axis > 2) throw Error(SPHGPU_E_ARG, "axis must be 0, 1 or 2");
+  if (type == SPHGPU_BOUNDARY_PERIODIC) {
+    if (!(hi > lo)) throw Error(SPHGPU_E_ARG, "periodic boundary needs hi > lo");
+  } else if (type != SPHGPU_BOUNDARY_REFLECTING) {
+    throw Error(SPHGPU_E_ARG, "unknown boundary type");
+  }
+  c->bcs.push_back(Boundary{type, axis, lo, hi, wall_high});
+  API_END(c)
+}
+
+int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const double* vel, const double* mass,
+                         const double* rho, const double* eps, const double* H, const int* nodelist) {
+  API_BEGIN(c)
+  if (n <= 0 || n >= kMaxNodes) throw Error(SPHGPU_E_ARG, "particle count out of range");
+  if (!pos || !vel || !mass || !rho || !eps || !H) throw Error(SPHGPU_E_ARG, "null particle array");
+  if (c->numLists == 0) c->numLists = 1;
+  for (long i = 0; i < n; ++i) {
+    const double* h = H + 6 * i;
+    if (h[1] != 0.0 || h[2] != 0.0 || h[4] != 0.0 || h[0] != h[3] || h[0] != h[5])
+      throw Error(SPHGPU_E_UNSUPPORTED, "H must be isotropic (H = I/h) on node " + std::to_string(i));
+    if (!(h[0] > 0.0)) throw Error(SPHGPU_E_NAN, "non-positive H on node " + std::to_string(i));
+    if (nodelist && (nodelist[i] < 0 || nodelist[i] >= c->numLists))
+      throw Error(SPHGPU_E_ARG, "nodelist id out of range on node " + std::to_string(i));
+  }
+  ensureCapacity(c, n);
+  c->n = n;
+  c->cur = 0;
+  c->F = c->fieldsOf(c->bankA);
+  c->Falt = c->fieldsOf(c->bankB);
+  CUDA_OK(cudaMemsetAsync(c->bankA.p, 0, c->bankA.bytes, c->stream));
+  std::vector<double> tmp(n);
+  auto up = [&](int f, const double* src, int stride, int comp) {
+    for (long i = 0; i < n; ++i) tmp[i] = src[(size_t)stride * i + comp];
+    CUDA_OK(cudaMemcpyAsync(c->F.f[f], tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+  };
+  for (int a = 0; a < 3; ++a) { up(F_X + a, pos, 3, a); up(F_VX + a, vel, 3, a); }
+  up(F_MASS, mass, 1, 0);
+  up(F_RHO, rho, 1, 0);
+  up(F_EPS, eps, 1, 0);
+  up(F_HINV, H, 6, 0);
+  for (long i = 0; i < n; ++i) tmp[i] = 1.0;
+  CUDA_OK(cudaMemcpyAsync(c->F.f[F_OMEGA], tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  std::vector<int> ids(n);
+  for (long i = 0; i < n; ++i) ids[i] = (int)i;
+  CUDA_OK(cudaMemcpy(c->orig[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  for (long i = 0; i < n; ++i) ids[i] = nodelist ? nodelist[i] : 0;
+  CUDA_OK(cudaMemcpy(c->list[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  c->haveNeighbors = false;
+  c->initialized = false;
+  refreshParams(c);
+  API_END(c)
+}
+
+int sphgpu_initialize(sphgpu_handle c) {
+  API_BEGIN(c)
+  requireState(c);
+  refreshParams(c);
+  launchEOS(c->F, c->listp(), c->n, c->lists, c->stream, &c->lc);
+  c->check();
+  buildNeighbors(c);
+  if (c->cfg.gradh_correction) gradh(c);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->initialized = true;
+  API_END(c)
+}
+
+int sphgpu_connectivity(sphgpu_handle c) {
+  API_BEGIN(c)
+  requireState(c);
+  refreshParams(c);
+  buildNeighbors(c);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_sum_density(sphgpu_handle c) {
+  API_BEGIN(c)
+  requireState(c);
+  if (!c->haveNeighbors) buildNeighbors(c);
+  sumDensity(c);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_gradh(sphgpu_handle c) {
+  API_BEGIN(c)
+  requireState(c);
+  if (!c->haveNeighbors) buildNeighbors(c);
+  gradh(c);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_evaluate_derivatives(sphgpu_handle c) {
+  API_BEGIN(c)
+  requireState(c);
+  refreshParams(c);
+  if (!c->haveNeighbors) buildNeighbors(c);
+  evalDerivs(c);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_dt(sphgpu_handle c, double* dt, int* reason) {
+  API_BEGIN(c)
+  requireState(c);
+  refreshParams(c);
+  if (!c->haveNeighbors) buildNeighbors(c);
+  const double v = packageDt(c, reason);
+  if (dt) *dt = v;
+  API_END(c)
+}
+
+int sphgpu_step(sphgpu_handle c, double max_time, double* dt_out) {
+  API_BEGIN(c)
+  const double dt = step(c, max_time);
+  if (dt_out) *dt_out = dt;
+  API_END(c)
+}
+
+int sphgpu_advance(sphgpu_handle c, int nsteps, double max_time) {
+  API_BEGIN(c)
+  for (int k = 0; k < nsteps && c->time < max_time; ++k) step(c, max_time);
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp) {
+  API_BEGIN(c)
+  if (!name) throw Error(SPHGPU_E_ARG, "null field name");
+  FieldSpec fs;
+  bool isH, isNb;
+  if (!fieldSpec(name, fs, isH, isNb)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  if (ncomp) *ncomp = fs.ncomp;
+  if (!out) return SPHGPU_OK;
+  requireState(c);
+  const long n = c->n;
+  std::vector<int> orig(n);
+  CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<double> buf(n);
+  if (isNb) {
+    if (!c->haveNeighbors) throw Error(SPHGPU_E_STATE, "no neighbour lists yet");
+    std::vector<long long> st(n + 1);
+    CUDA_OK(cudaMemcpyAsync(st.data(), c->nbrStart.p, (n + 1) * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    for (long i = 0; i < n; ++i) out[orig[i]] = (double)(st[i + 1] - st[i]);
+    return SPHGPU_OK;
+  }
+  if (isH) {
+    CUDA_OK(cudaMemcpyAsync(buf.data(), c->F.f[fs.first], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    for (long i = 0; i < n; ++i) {
+      double* o = out + 6 * (size_t)orig[i];
+      o[0] = buf[i]; o[1] = 0.0; o[2] = 0.0; o[3] = buf[i]; o[4] = 0.0; o[5] = buf[i];
+    }
+    return SPHGPU_OK;
+  }
+  for (int k = 0; k < fs.ncomp; ++k) {
+    CUDA_OK(cudaMemcpyAsync(buf.data(), c->F.f[fs.first + k], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    for (long i = 0; i < n; ++i) out[(size_t)fs.ncomp * orig[i] + k] = buf[i];
+  }
+  API_END(c)
+}
+
+int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
+  API_BEGIN(c)
+  if (!name || !in) throw Error(SPHGPU_E_ARG, "null argument");
+  FieldSpec fs;
+  bool isH, isNb;
+  if (!fieldSpec(name, fs, isH, isNb) || isNb) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  requireState(c);
+  const long n = c->n;
+  std::vector<int> orig(n);
+  CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  std::vector<double> buf(n);
+  const int nc = isH ? 1 : fs.ncomp;
+  for (int k = 0; k < nc; ++k) {
+    for (long i = 0; i < n; ++i) buf[i] = isH ? in[6 * (size_t)orig[i]] : in[(size_t)fs.ncomp * orig[i] + k];
+    CUDA_OK(cudaMemcpyAsync(c->F.f[fs.first + k], buf.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+  }
+  API_END(c)
+}
+
+int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* npairs) {
+  API_BEGIN(c)
+  if (!npairs) throw Error(SPHGPU_E_ARG, "null npairs");
+  if (!c->haveNeighbors) throw Error(SPHGPU_E_STATE, "no neighbour lists yet");
+  *npairs = (long)c->nnbr;
+  if (!i_out) return SPHGPU_OK;
+  const long n = c->n;
+  std::vector<int> orig(n);
+  std::vector<long long> st(n + 1);
+  std::vector<uint32_t> nb(std::max<long long>(1, c->nnbr));
+  CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(st.data(), c->nbrStart.p, (n + 1) * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(nb.data(), c->nbr.p, c->nnbr * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  for (long i = 0; i < n; ++i)
+    for (long long k = st[i]; k < st[i + 1]; ++k) {
+      i_out[k] = orig[i];
+      j_out[k] = orig[nb[k] & kIndexMask];
+      if (image) image[k] = (int)(nb[k] >> kIndexBits);
+    }
+  API_END(c)
+}
+
+int sphgpu_conservation(sphgpu_handle c, double out[8]) {
+  API_BEGIN(c)
+  requireState(c);
+  if (!out) throw Error(SPHGPU_E_ARG, "null output");
+  c->scratch.ensure(7 * sizeof(double) * 4096);
+  double* d = c->small.as<double>() + 32;
+  launchConservation(c->F, c->n, c->cfg.gravity != 0, c->scratch.as<double>(), 7 * 4096, d, c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 32, d, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 8; ++k) out[k] = c->hsmall[32 + k];
+  API_END(c)
+}
+
+int sphgpu_get_time(sphgpu_handle c, double* time, double* last_dt, long* cycle) {
+  API_BEGIN(c)
+  if (time) *time = c->time;
+  if (last_dt) *last_dt = c->lastDt;
+  if (cycle) *cycle = c->cycle;
+  API_END(c)
+}
+
+int sphgpu_num_particles(sphgpu_handle c, long* n) {
+  API_BEGIN(c)
+  if (n) *n = c->n;
+  API_END(c)
+}
+
+int sphgpu_profile_enable(sphgpu_handle c, int enable) {
+  API_BEGIN(c)
+  c->prof.collect();
+  c->prof.on = enable != 0;
+  API_END(c)
+}
+int sphgpu_profile_get(sphgpu_handle c, const char* name, long* launches, double* ms) {
+  API_BEGIN(c)
+  c->prof.collect();
+  auto it = c->prof.acc.find(name ? name : "");
+  if (launches) *launches = it == c->prof.acc.end() ? 0 : it->second.first;
+  if (ms) *ms = it == c->prof.acc.end() ? 0.0 : it->second.second;
+  API_END(c)
+}
+int sphgpu_profile_reset(sphgpu_handle c) {
+  API_BEGIN(c)
+  c->prof.collect();
+  c->prof.acc.clear();
+  API_END(c)
+}
+int sphgpu_launch_count(sphgpu_handle c, long* launches) {
+  API_BEGIN(c)
+  if (launches) *launches = c->lc.n;
+  API_END(c)
+}
+int sphgpu_synchronize(sphgpu_handle c) {
+  API_BEGIN(c)
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// Shared device-side definitions of libsphgpu (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sph {
+
+// Neighbour entries: 26-bit sorted node index + 6-bit image code (2 bits per axis).
+constexpr int kIndexBits = 26;
+constexpr uint32_t kIndexMask = (1u << kIndexBits) - 1u;
+constexpr long kMaxNodes = (1L << kIndexBits);
+constexpr int kMaxNodeLists = 8;
+constexpr int kMaxTable = 1536;   // 3*(N1+1) coefficients; N1+1 <= 512
+
+// Axis boundary kinds for the implicit ghost images.
+enum AxisKind { AXIS_OPEN = 0, AXIS_PERIODIC = 1, AXIS_REFLECT = 2 };
+
+struct Grid {
+  double lo[3];        // grid origin per axis
+  double hi[3];        // periodic / wall extents (hi of the domain)
+  double cell[3];      // cell edge per axis
+  int nc[3];           // cells per axis
+  int kindLo[3];       // AxisKind of the low side
+  int kindHi[3];       // AxisKind of the high side
+  double wallLo[3];    // reflecting wall coordinates / periodic planes
+  double wallHi[3];
+};
+
+struct NodeListParams {
+  double nPerh, hmin, hmax, rhoMin, rhoMax, gamma, minP, maxP;
+};
+
+struct HydroParams {
+  int compatible, gradh, xsph, correctVelGrad, sumAllLists, densityUpdate;
+  int linearInExpansion, quadraticInExpansion, useVelMagDt;
+  double epsTensile, nTensile, Cl, Cq, eps2, cfl;
+  double W0;          // kernel value at eta = 0 (Hdet = 1)
+  double WnPerh;      // W(1/nPerh of the first NodeList, 1)
+  int numLists;
+  int tableN1;        // N1 of the quadratic table
+  double tableXstep;  // interval of the quadratic table
+  double extent;      // kernel extent
+  int hermN;          // Hermite knots of the nperh lookup
+  double hermXmin, hermXmax, hermXstep;
+};
+
+// Image of coordinate p under the per-axis code (reference ghost mapping,
+// PlanarBoundary::mapPosition -> mapPositionThroughPlanes, with
+// closestPointOnPlane = p + ((origin - p).n) n).  Written with explicit
+// round-to-nearest adds so no multiply-add contraction changes the bits.
+__device__ __forceinline__ double imageCoord(double p, int code, int kindLo, int kindHi, double lo, double hi) {
+  if (code == 0) return p;
+  if (code == 1) {
+    if (kindLo == AXIS_PERIODIC) return __dsub_rn(__dadd_rn(p, __dsub_rn(lo, p)), __dsub_rn(hi, p));   // low image
+    return __dsub_rn(__dadd_rn(p, __dsub_rn(lo, p)), __dsub_rn(p, lo));                                 // mirror at lo
+  }
+  if (kindHi == AXIS_PERIODIC) return __dadd_rn(__dadd_rn(p, __dsub_rn(hi, p)), __dsub_rn(p, lo));      // high image
+  return __dadd_rn(__dadd_rn(p, __dsub_rn(hi, p)), __dsub_rn(hi, p));                                    // mirror at hi
+}
+__device__ __forceinline__ bool mirrored(int code, int kindLo, int kindHi) {
+  return (code == 1 && kindLo == AXIS_REFLECT) || (code == 2 && kindHi == AXIS_REFLECT);
+}
+
+// |(a x, a y, a z)|^2 exactly as GeomVector::magnitude2 of H*r for H = a I
+// (left-to-right sum, no contraction).
+__device__ __forceinline__ double eta2Exact(double a, double rx, double ry, double rz) {
+  const double ex = __dmul_rn(a, rx), ey = __dmul_rn(a, ry), ez = __dmul_rn(a, rz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+}
+
+__host__ __device__ __forceinline__ uint32_t spreadBits10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  return spreadBits10(x) | (spreadBits10(y) << 1) | (spreadBits10(z) << 2);
+}
+
+}  // namespace sph

@@ -1,0 +1,941 @@
+// SPH hydro kernels of libsphgpu (sm_103a): cell-list neighbour build,
+// density sum, grad-h correction, the FP64 pair loop with its per-node
+// finalisation and smoothing-scale update, the time-step vote, the
+// compatible-energy sweep and the CheapSynchronousRK2 state updates.
+//
+// Formulation.  The reference walks an unordered pair list and scatters into
+// both nodes through thread-private copies of 13 FieldLists
+// (src/SPH/SPH.cc:271-475).  Here every kernel is a gather: one thread owns
+// node i and walks i's neighbour list, so each unordered pair is evaluated
+// twice (once per side) with no atomics and a fixed summation order.  Ghost
+// nodes of periodic and reflecting boundaries are implicit: a neighbour
+// entry carries a 6-bit image code and the neighbour's coordinates are mapped
+// with the reference's own plane formula (imageCoord).
+#include "kernels.cuh"
+#include <cfloat>
+
+namespace sph {
+namespace {
+
+constexpr double kTiny30 = 1.0e-30;
+
+__device__ __forceinline__ void unpackCell(uint32_t cc, int c[3]) {
+  c[0] = (int)(cc & 1023u);
+  c[1] = (int)((cc >> 10) & 1023u);
+  c[2] = (int)((cc >> 20) & 1023u);
+}
+
+// Walk the 27 cells around packed cell cc, resolving periodic wrap and
+// reflecting mirrors into (cell, image code); fn(k, code) for every candidate
+// slot k in cell order.
+template <class Fn>
+__device__ __forceinline__ void forEachCandidate(const Grid& g, uint32_t cc, const int* __restrict__ cellStart,
+                                                 const int* __restrict__ cellEnd, Fn fn) {
+  int c[3];
+  unpackCell(cc, c);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int d[3] = {dx, dy, dz};
+        int cell[3];
+        int code = 0;
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          int nn = c[a] + d[a];
+          if (nn < 0) {
+            if (g.kindLo[a] == AXIS_PERIODIC) nn = g.nc[a] - 1;
+            else if (g.kindLo[a] == AXIS_REFLECT) nn = 0;
+            else ok = false;
+            code |= 1 << (2 * a);
+          } else if (nn >= g.nc[a]) {
+            if (g.kindHi[a] == AXIS_PERIODIC) nn = 0;
+            else if (g.kindHi[a] == AXIS_REFLECT) nn = g.nc[a] - 1;
+            else ok = false;
+            code |= 2 << (2 * a);
+          }
+          cell[a] = nn;
+        }
+        if (!ok) continue;
+        const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
+        const int s = cellStart[key], e = cellEnd[key];
+        for (int k = s; k < e; ++k) fn(k, code);
+      }
+}
+
+__device__ __forceinline__ void imagePos(const Grid& g, int code, double& x, double& y, double& z) {
+  if (code) {
+    x = imageCoord(x, code & 3, g.kindLo[0], g.kindHi[0], g.wallLo[0], g.wallHi[0]);
+    y = imageCoord(y, (code >> 2) & 3, g.kindLo[1], g.kindHi[1], g.wallLo[1], g.wallHi[1]);
+    z = imageCoord(z, (code >> 4) & 3, g.kindLo[2], g.kindHi[2], g.wallLo[2], g.wallHi[2]);
+  }
+}
+__device__ __forceinline__ void imageVec(const Grid& g, int code, double& x, double& y, double& z) {
+  if (code) {
+    if (mirrored(code & 3, g.kindLo[0], g.kindHi[0])) x = -x;
+    if (mirrored((code >> 2) & 3, g.kindLo[1], g.kindHi[1])) y = -y;
+    if (mirrored((code >> 4) & 3, g.kindLo[2], g.kindHi[2])) z = -z;
+  }
+}
+
+// QuadraticInterpolatorView lookup shared by W and dW/deta
+// (src/Utilities/QuadraticInterpolatorViewInline.hh:17-21,71-77).
+__device__ __forceinline__ int tableIndex(double eta, int N1, double xstep) {
+  const long k = (long)(fmax(0.0, eta) / xstep);
+  return 3 * (int)min((long)N1, k);
+}
+__device__ __forceinline__ double tableEval(const double* c, int i0, double x) {
+  return c[i0] + (c[i0 + 1] + c[i0 + 2] * x) * x;
+}
+
+__device__ __forceinline__ double blockMin(double v, double* sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) sm[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? sm[lane] : DBL_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  __syncthreads();
+  return v;
+}
+__device__ __forceinline__ double blockMax(double v, double* sm) { return -blockMin(-v, sm); }
+__device__ __forceinline__ double blockSum(double v, double* sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sm[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+//------------------------------------------------------------------------------
+// Bounds: min hinv and bounding box (for open axes).
+//------------------------------------------------------------------------------
+__global__ void boundsKernel(Fields F, long n, double* __restrict__ part) {
+  __shared__ double sm[32];
+  double ah = DBL_MAX, mnx = DBL_MAX, mny = DBL_MAX, mnz = DBL_MAX, mxx = -DBL_MAX, mxy = -DBL_MAX, mxz = -DBL_MAX;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    ah = fmin(ah, F.f[F_HINV][i]);
+    const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i];
+    mnx = fmin(mnx, x); mny = fmin(mny, y); mnz = fmin(mnz, z);
+    mxx = fmax(mxx, x); mxy = fmax(mxy, y); mxz = fmax(mxz, z);
+  }
+  const double r[7] = {blockMin(ah, sm), blockMin(mnx, sm), blockMin(mny, sm), blockMin(mnz, sm),
+                       blockMax(mxx, sm), blockMax(mxy, sm), blockMax(mxz, sm)};
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 7; ++k) part[blockIdx.x * 7 + k] = r[k];
+}
+__global__ void boundsFinalKernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sm[32];
+  double v[7];
+  for (int k = 0; k < 7; ++k) v[k] = k < 4 ? DBL_MAX : -DBL_MAX;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int k = 0; k < 7; ++k) v[k] = k < 4 ? fmin(v[k], part[b * 7 + k]) : fmax(v[k], part[b * 7 + k]);
+  for (int k = 0; k < 7; ++k) {
+    const double r = k < 4 ? blockMin(v[k], sm) : blockMax(v[k], sm);
+    if (threadIdx.x == 0) out[k] = r;
+  }
+}
+
+//------------------------------------------------------------------------------
+// Neighbour build.
+//------------------------------------------------------------------------------
+__global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ keys, int* __restrict__ vals,
+                              uint32_t* __restrict__ cellc) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p[3] = {F.f[F_X][i], F.f[F_Y][i], F.f[F_Z][i]};
+  uint32_t c[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double q = floor((p[a] - g.lo[a]) / g.cell[a]);
+    long ci = (long)q;
+    if (!(q == q)) ci = 0;
+    ci = ci < 0 ? 0 : (ci >= g.nc[a] ? g.nc[a] - 1 : ci);
+    c[a] = (uint32_t)ci;
+  }
+  keys[i] = morton3(c[0], c[1], c[2]);
+  vals[i] = (int)i;
+  cellc[i] = c[0] | (c[1] << 10) | (c[2] << 20);
+}
+
+__global__ void permuteKernel(Fields Fin, Fields Fout, const int* __restrict__ perm, const int* __restrict__ origIn,
+                              int* __restrict__ origOut, const int* __restrict__ listIn, int* __restrict__ listOut,
+                              const uint32_t* __restrict__ cellIn, uint32_t* __restrict__ cellOut, long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int p = perm[k];
+#pragma unroll 4
+  for (int f = 0; f < F_NUM_PERMUTED; ++f) Fout.f[f][k] = Fin.f[f][p];
+  origOut[k] = origIn[p];
+  listOut[k] = listIn[p];
+  cellOut[k] = cellIn[p];
+}
+
+__global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* __restrict__ cellStart,
+                                int* __restrict__ cellEnd) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t key = keys[k];
+  if (k == 0 || keys[k - 1] != key) cellStart[key] = (int)k;
+  if (k == n - 1 || keys[k + 1] != key) cellEnd[key] = (int)(k + 1);
+}
+
+// Pair criterion of ConnectivityMap::computeConnectivity
+// (src/Neighbor/ConnectivityMap.cc:917-929): (Hi rij)^2 <= ext^2 or
+// (Hj rij)^2 <= ext^2, self excluded, in exact FP64 with the reference's
+// operation order.
+template <bool FILL>
+__global__ void neighborKernel(Fields F, const uint32_t* __restrict__ cellc, long n, Grid g,
+                               const int* __restrict__ cellStart, const int* __restrict__ cellEnd,
+                               int* __restrict__ counts, const long long* __restrict__ start,
+                               uint32_t* __restrict__ nbr, double ext2) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ X = F.f[F_X];
+  const double* __restrict__ Y = F.f[F_Y];
+  const double* __restrict__ Z = F.f[F_Z];
+  const double* __restrict__ A = F.f[F_HINV];
+  const double xi = X[i], yi = Y[i], zi = Z[i], ai = A[i];
+  int cnt = 0;
+  long long w = FILL ? start[i] : 0;
+  forEachCandidate(g, cellc[i], cellStart, cellEnd, [&](int j, int code) {
+    if (j == (int)i && code == 0) return;
+    double xj = X[j], yj = Y[j], zj = Z[j];
+    imagePos(g, code, xj, yj, zj);
+    const double rx = __dsub_rn(xi, xj), ry = __dsub_rn(yi, yj), rz = __dsub_rn(zi, zj);
+    const double aj = A[j];
+    if (eta2Exact(ai, rx, ry, rz) <= ext2 || eta2Exact(aj, rx, ry, rz) <= ext2) {
+      if (FILL) nbr[w++] = (uint32_t)j | ((uint32_t)code << kIndexBits);
+      else ++cnt;
+    }
+  });
+  if (!FILL) counts[i] = cnt;
+}
+
+//------------------------------------------------------------------------------
+// computeSPHSumMassDensity (src/SPH/computeSPHSumMassDensity.cc:15-87),
+// gathered: rho_i = m_i W(0) Hdet_i + sum_j m W(|Hj ri - Hj rj|, Hdet_j) with
+// m = m_j for the same NodeList and m_i otherwise.
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __restrict__ list, long n, Grid g,
+                                                        NeighborLists nl, TableDev t, HydroParams hp) {
+  extern __shared__ double smem[];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) smem[k] = t.w[k];
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ X = F.f[F_X];
+  const double* __restrict__ Y = F.f[F_Y];
+  const double* __restrict__ Z = F.f[F_Z];
+  const double* __restrict__ A = F.f[F_HINV];
+  const double* __restrict__ Ms = F.f[F_MASS];
+  const double xi = X[i], yi = Y[i], zi = Z[i], ai = A[i], mi = Ms[i];
+  const int li = list[i];
+  const double Hdeti = (ai * ai) * ai;
+  const double self = mi * (Hdeti * smem[0]);
+  double sum = 0.0;
+  const long long e = nl.start[i + 1];
+  for (long long k = nl.start[i]; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    double xj = X[j], yj = Y[j], zj = Z[j];
+    imagePos(g, code, xj, yj, zj);
+    const double aj = A[j];
+    const double dx = __dsub_rn(__dmul_rn(aj, xi), __dmul_rn(aj, xj));
+    const double dy = __dsub_rn(__dmul_rn(aj, yi), __dmul_rn(aj, yj));
+    const double dz = __dsub_rn(__dmul_rn(aj, zi), __dmul_rn(aj, zj));
+    const double eta = sqrt(dx * dx + dy * dy + dz * dz);
+    if (eta < hp.extent) {
+      const double Hdetj = (aj * aj) * aj;
+      const int i0 = tableIndex(eta, hp.tableN1, hp.tableXstep);
+      const double Wj = Hdetj * tableEval(smem, i0, eta);
+      sum += (list[j] == li ? Ms[j] : mi) * Wj;
+    }
+  }
+  F.f[F_RHO][i] = self + sum;
+}
+
+//------------------------------------------------------------------------------
+// computeSPHOmegaGradhCorrection (src/SPH/computeSPHOmegaGradhCorrection.cc:15-116).
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, NeighborLists nl, TableDev t,
+                                                   HydroParams hp) {
+  extern __shared__ double smem[];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { smem[k] = t.w[k]; smem[ntab + k] = t.g[k]; }
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ X = F.f[F_X];
+  const double* __restrict__ Y = F.f[F_Y];
+  const double* __restrict__ Z = F.f[F_Z];
+  const double xi = X[i], yi = Y[i], zi = Z[i], ai = F.f[F_HINV][i];
+  const double Hdeti = (ai * ai) * ai;
+  double wsum = 0.0, gsum = 0.0;
+  const long long s = nl.start[i], e = nl.start[i + 1];
+  for (long long k = s; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    double xj = X[j], yj = Y[j], zj = Z[j];
+    imagePos(g, code, xj, yj, zj);
+    const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
+    const double ex = ai * rx, ey = ai * ry, ez = ai * rz;
+    const double eta = sqrt(ex * ex + ey * ey + ez * ez);
+    if (eta < hp.extent) {
+      const int i0 = tableIndex(eta, hp.tableN1, hp.tableXstep);
+      wsum += Hdeti * tableEval(smem, i0, eta);
+      gsum += eta * (Hdeti * tableEval(smem + ntab, i0, eta));
+    }
+  }
+  double omega;
+  if (e == s) omega = 1.0;
+  else omega = fmax(1.0e-30, -gsum / (3.0 * (wsum + Hdeti * hp.W0)));
+  F.f[F_OMEGA][i] = omega;
+}
+
+//------------------------------------------------------------------------------
+// SPH::evaluateDerivativesImpl (src/SPH/SPH.cc:294-552) with
+// MonaghanGingoldViscosity::QPiij (MonaghanGingoldViscosity.cc:41-101) and the
+// SPHSmoothingScale moments + IdealH (SPHSmoothingScale.cc:154-272), FP64.
+//------------------------------------------------------------------------------
+__constant__ NodeListParams cLists[kMaxNodeLists];
+
+__device__ __forceinline__ double hermiteLookup(const double* __restrict__ v, const HydroParams& hp, double x) {
+  // CubicHermiteInterpolatorView::operator() (CubicHermiteInterpolatorViewInline.hh:10-36)
+  const int N = hp.hermN;
+  if (x < hp.hermXmin) return v[0] + v[N] * (x - hp.hermXmin);
+  if (x > hp.hermXmax) return v[N - 1] + v[2 * N - 1] * (x - hp.hermXmin);
+  long k = (long)(fmax(0.0, x - hp.hermXmin) / hp.hermXstep);
+  const int i0 = (int)min((long)(N - 2), k);
+  const double t = fmax(0.0, fmin(1.0, (x - hp.hermXmin - i0 * hp.hermXstep) / hp.hermXstep));
+  const double t2 = t * t, t3 = t * t2;
+  return ((2.0 * t3 - 3.0 * t2 + 1.0) * v[i0] + (-2.0 * t3 + 3.0 * t2) * v[i0 + 1] +
+          hp.hermXstep * ((t3 - 2.0 * t2 + t) * v[N + i0] + (t3 - t2) * v[N + i0 + 1]));
+}
+
+// Per-node completion shared by the FP64 and FP32 pair kernels: self terms,
+// corrected velocity gradient, continuity, XSPH, and the IdealH update.
+struct NodeAcc {
+  double rhoSum, norm, dvx, dvy, dvz, deps, gx, gy, gz, maxQ, effQ, xw, xdx, xdy, xdz, m0, m1x, m1y, m1z;
+  double D[9], M[9];
+};
+
+__device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const NodeAcc& a, double mi, double rhoi,
+                                             double vxi, double vyi, double vzi, double ai, int numNb,
+                                             const HydroParams& hp, const double* __restrict__ herm) {
+  const double Hdeti = (ai * ai) * ai;
+  F.f[F_RHOSUM][i] = a.rhoSum + mi * hp.W0 * Hdeti;
+  F.f[F_NORM][i] = a.norm + mi / rhoi * hp.W0 * Hdeti;
+  double D[9], Mm[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { D[k] = a.D[k]; Mm[k] = a.M[k]; }
+  const double detM = (Mm[0] * Mm[4] * Mm[8] + Mm[1] * Mm[5] * Mm[6] + Mm[2] * Mm[3] * Mm[7] -
+                       Mm[0] * Mm[5] * Mm[7] - Mm[1] * Mm[3] * Mm[8] - Mm[2] * Mm[4] * Mm[6]);
+  if (hp.correctVelGrad && fabs(detM) > 1.0e-10 && numNb > 8) {
+    // GeomTensor<3>::Inverse (src/Geometry/GeomTensorInline.hh:1885-1890)
+    const double inv[9] = {(Mm[4] * Mm[8] - Mm[5] * Mm[7]) / detM, (Mm[2] * Mm[7] - Mm[1] * Mm[8]) / detM,
+                           (Mm[1] * Mm[5] - Mm[2] * Mm[4]) / detM, (Mm[5] * Mm[6] - Mm[3] * Mm[8]) / detM,
+                           (Mm[0] * Mm[8] - Mm[2] * Mm[6]) / detM, (Mm[2] * Mm[3] - Mm[0] * Mm[5]) / detM,
+                           (Mm[3] * Mm[7] - Mm[4] * Mm[6]) / detM, (Mm[1] * Mm[6] - Mm[0] * Mm[7]) / detM,
+                           (Mm[0] * Mm[4] - Mm[1] * Mm[3]) / detM};
+    double R[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        R[3 * r + c] = D[3 * r] * inv[c] + D[3 * r + 1] * inv[3 + c] + D[3 * r + 2] * inv[6 + c];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { D[k] = R[k]; Mm[k] = inv[k]; }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) D[k] /= rhoi;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { F.f[F_DVDX_XX + k][i] = D[k]; F.f[F_M_XX + k][i] = Mm[k]; }
+  F.f[F_GRADRHO_X][i] = a.gx / rhoi;
+  F.f[F_GRADRHO_Y][i] = a.gy / rhoi;
+  F.f[F_GRADRHO_Z][i] = a.gz / rhoi;
+  const double trace = D[0] + D[4] + D[8];
+  F.f[F_DRHODT][i] = -rhoi * trace;
+  F.f[F_DVDT_X][i] = a.dvx;
+  F.f[F_DVDT_Y][i] = a.dvy;
+  F.f[F_DVDT_Z][i] = a.dvz;
+  F.f[F_DEPSDT][i] = a.deps;
+  F.f[F_MAXQ][i] = a.maxQ;
+  F.f[F_EFFQ][i] = a.effQ;
+  double xw = a.xw;
+  if (hp.xsph) {
+    xw += Hdeti * mi / rhoi * hp.W0;
+    const double ws = fmax(kTiny30, xw);
+    F.f[F_DXDT_X][i] = vxi + a.xdx / ws;
+    F.f[F_DXDT_Y][i] = vyi + a.xdy / ws;
+    F.f[F_DXDT_Z][i] = vzi + a.xdz / ws;
+  } else {
+    F.f[F_DXDT_X][i] = vxi;
+    F.f[F_DXDT_Y][i] = vyi;
+    F.f[F_DXDT_Z][i] = vzi;
+  }
+  F.f[F_XSPHW][i] = xw;
+  F.f[F_XSPHDV_X][i] = a.xdx;
+  F.f[F_XSPHDV_Y][i] = a.xdy;
+  F.f[F_XSPHDV_Z][i] = a.xdz;
+  // SPHSmoothingScale finalize (SPHSmoothingScale.cc:235-270)
+  const NodeListParams L = cLists[li];
+  const double m0s = fmax(0.0, a.m0);
+  const double m0 = m0s < 0.0 ? -pow(-m0s, 0.3333333333333333) : pow(m0s, 0.3333333333333333);
+  F.f[F_M0][i] = m0;
+  F.f[F_M1_X][i] = a.m1x;
+  F.f[F_M1_Y][i] = a.m1y;
+  F.f[F_M1_Z][i] = a.m1z;
+  F.f[F_DHDT][i] = ((-ai) / 3.0) * trace;
+  const bool iso = fabs(m0 - 0.0) <= 1.0e-15 * fmax(1.0, fabs(m0));
+  const double cur = iso ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(herm, hp, m0));
+  const double s = fmin(4.0, fmax(0.25, L.nPerh / (cur + 1.0e-30)));
+  const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
+  const double hi0 = 1.0 / ai;
+  const double hi1 = fmin(L.hmax, fmax(L.hmin, hi0 * (1.0 - aa + aa * s)));
+  F.f[F_HIDEAL][i] = 1.0 / hi1;
+}
+
+template <bool XSPH, bool COMPAT>
+__global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __restrict__ list, long n, Grid g,
+                                                      NeighborLists nl, TableDev t, HydroParams hp,
+                                                      double* __restrict__ pacc) {
+  extern __shared__ double smem[];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { smem[k] = t.w[k]; smem[ntab + k] = t.g[k]; }
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* __restrict__ X = F.f[F_X];
+  const double* __restrict__ Y = F.f[F_Y];
+  const double* __restrict__ Z = F.f[F_Z];
+  const double* __restrict__ VX = F.f[F_VX];
+  const double* __restrict__ VY = F.f[F_VY];
+  const double* __restrict__ VZ = F.f[F_VZ];
+  const double* __restrict__ Ms = F.f[F_MASS];
+  const double* __restrict__ RHO = F.f[F_RHO];
+  const double* __restrict__ PP = F.f[F_P];
+  const double* __restrict__ CS = F.f[F_CS];
+  const double* __restrict__ OM = F.f[F_OMEGA];
+  const double* __restrict__ A = F.f[F_HINV];
+  const double* __restrict__ tw = smem;
+  const double* __restrict__ tg = smem + ntab;
+
+  const double xi = X[i], yi = Y[i], zi = Z[i], vxi = VX[i], vyi = VY[i], vzi = VZ[i];
+  const double mi = Ms[i], rhoi = RHO[i], Pi = PP[i], ci = CS[i], omi = OM[i], ai = A[i];
+  const int li = list[i];
+  const double Hdeti = (ai * ai) * ai;
+  const double safeOmegai = omi / (omi * omi + kTiny30);
+  const double tiny = kTiny30;
+  const double Clij = 0.5 * (1.0 + 1.0) * 1.0 * hp.Cl;
+  const double Cqij = 0.5 * (1.0 + 1.0) * 1.0 * hp.Cq;
+
+  NodeAcc a;
+  a.rhoSum = a.norm = a.dvx = a.dvy = a.dvz = a.deps = a.gx = a.gy = a.gz = 0.0;
+  a.maxQ = 0.0; a.effQ = a.xw = a.xdx = a.xdy = a.xdz = a.m0 = a.m1x = a.m1y = a.m1z = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { a.D[k] = 0.0; a.M[k] = 0.0; }
+
+  const long long s = nl.start[i], e = nl.start[i + 1];
+  for (long long k = s; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    double xj = X[j], yj = Y[j], zj = Z[j], vxj = VX[j], vyj = VY[j], vzj = VZ[j];
+    imagePos(g, code, xj, yj, zj);
+    imageVec(g, code, vxj, vyj, vzj);
+    const double mj = Ms[j], rhoj = RHO[j], Pj = PP[j], cj = CS[j], omj = OM[j], aj = A[j];
+    const int lj = list[j];
+    const double Hdetj = (aj * aj) * aj;
+    const double safeOmegaj = omj / (omj * omj + kTiny30);
+
+    const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
+    const double eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
+    const double ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
+    const double etaMag2i = eix * eix + eiy * eiy + eiz * eiz;
+    const double etaMag2j = ejx * ejx + ejy * ejy + ejz * ejz;
+    const double etaMagi = sqrt(etaMag2i), etaMagj = sqrt(etaMag2j);
+    const double sIi = 1.0 / fmax(tiny, etaMagi), sIj = 1.0 / fmax(tiny, etaMagj);
+    const double uix = eix * sIi, uiy = eiy * sIi, uiz = eiz * sIi;
+    const double ujx = ejx * sIj, ujy = ejy * sIj, ujz = ejz * sIj;
+    double Wi = 0.0, gi = 0.0, Wj = 0.0, gj = 0.0;
+    if (etaMagi < hp.extent) {
+      const int i0 = tableIndex(etaMagi, hp.tableN1, hp.tableXstep);
+      Wi = tableEval(tw, i0, etaMagi);
+      gi = tableEval(tg, i0, etaMagi);
+    }
+    if (etaMagj < hp.extent) {
+      const int i0 = tableIndex(etaMagj, hp.tableN1, hp.tableXstep);
+      Wj = tableEval(tw, i0, etaMagj);
+      gj = tableEval(tg, i0, etaMagj);
+    }
+    const double WSPHi = fabs(gi);
+    Wi *= Hdeti; Wj *= Hdetj;
+    const double gWi = Hdeti * gi, gWj = Hdetj * gj;
+    const double gHi = gWi * ai, gHj = gWj * aj;
+    const double gwix = gHi * uix, gwiy = gHi * uiy, gwiz = gHi * uiz;
+    const double gwjx = gHj * ujx, gwjy = gHj * ujy, gwjz = gHj * ujz;
+
+    if (lj == li) {
+      a.rhoSum += mj * Wi;
+      a.norm += mi / rhoi * Wi;
+    }
+    const double vijx = vxi - vxj, vijy = vyi - vyj, vijz = vzi - vzj;
+    // Monaghan-Gingold Q
+    const double mui = (vijx * eix + vijy * eiy + vijz * eiz) / (etaMag2i + hp.eps2);
+    const double muj = (vijx * ejx + vijy * ejy + vijz * ejz) / (etaMag2j + hp.eps2);
+    const double lmi = hp.linearInExpansion ? mui : fmin(0.0, mui);
+    const double lmj = hp.linearInExpansion ? muj : fmin(0.0, muj);
+    const double qmi = hp.quadraticInExpansion ? -(mui < 0.0 ? -1.0 : 1.0) * mui * mui : fmin(0.0, mui) * fmin(0.0, mui);
+    const double qmj = hp.quadraticInExpansion ? -(muj < 0.0 ? -1.0 : 1.0) * muj * muj : fmin(0.0, muj) * fmin(0.0, muj);
+    const double ei = -Clij * ci * lmi + Cqij * qmi;
+    const double ej = -Clij * cj * lmj + Cqij * qmj;
+    const double QPiij = ei / rhoi, QPiji = ej / rhoj;
+    const double Qi = rhoi * ei;
+    const double qai = 0.5 * QPiij, qaj = 0.5 * QPiji;
+    const double Qaix = qai * gwix, Qaiy = qai * gwiy, Qaiz = qai * gwiz;
+    const double Qajx = qaj * gwjx, Qajy = qaj * gwjy, Qajz = qaj * gwjz;
+    const double workQi = vijx * Qaix + vijy * Qaiy + vijz * Qaiz;
+    a.maxQ = fmax(a.maxQ, Qi);
+    a.effQ += mj * Qi * Wi / rhoj;
+    double Peffi = Pi, Peffj = Pj;
+    if (hp.epsTensile != 0.0) {
+      const double ri = Wi / (Hdeti * hp.WnPerh), rj = Wj / (Hdetj * hp.WnPerh);
+      Peffi += hp.epsTensile * (ri * ri * ri * ri) * (Pi < 0.0 ? -Pi : 0.0);
+      Peffj += hp.epsTensile * (rj * rj * rj * rj) * (Pj < 0.0 ? -Pj : 0.0);
+    }
+    const double Prhoi = safeOmegai * Peffi / (rhoi * rhoi);
+    const double Prhoj = safeOmegaj * Peffj / (rhoj * rhoj);
+    const double ddx = Prhoi * gwix + Prhoj * gwjx + Qaix + Qajx;
+    const double ddy = Prhoi * gwiy + Prhoj * gwjy + Qaiy + Qajy;
+    const double ddz = Prhoi * gwiz + Prhoj * gwjz + Qaiz + Qajz;
+    a.dvx -= mj * ddx;
+    a.dvy -= mj * ddy;
+    a.dvz -= mj * ddz;
+    if (COMPAT) {
+      pacc[3 * k] = -mj * ddx;
+      pacc[3 * k + 1] = -mj * ddy;
+      pacc[3 * k + 2] = -mj * ddz;
+    }
+    a.deps += mj * (Prhoi * (vijx * gwix + vijy * gwiy + vijz * gwiz) + workQi);
+    const double mvx = mj * vijx, mvy = mj * vijy, mvz = mj * vijz;
+    a.D[0] -= mvx * gwix; a.D[1] -= mvx * gwiy; a.D[2] -= mvx * gwiz;
+    a.D[3] -= mvy * gwix; a.D[4] -= mvy * gwiy; a.D[5] -= mvy * gwiz;
+    a.D[6] -= mvz * gwix; a.D[7] -= mvz * gwiy; a.D[8] -= mvz * gwiz;
+    if (XSPH) {
+      const double wx = 0.5 * (mi / rhoi * Wi + mj / rhoj * Wj);
+      a.xw += wx;
+      a.xdx -= wx * vijx; a.xdy -= wx * vijy; a.xdz -= wx * vijz;
+    }
+    const double gr = mj * (rhoj - rhoi);
+    a.gx += gr * gwix; a.gy += gr * gwiy; a.gz += gr * gwiz;
+    const double mrx = mj * rx, mry = mj * ry, mrz = mj * rz;
+    a.M[0] -= mrx * gwix; a.M[1] -= mrx * gwiy; a.M[2] -= mrx * gwiz;
+    a.M[3] -= mry * gwix; a.M[4] -= mry * gwiy; a.M[5] -= mry * gwiz;
+    a.M[6] -= mrz * gwix; a.M[7] -= mrz * gwiy; a.M[8] -= mrz * gwiz;
+    // SPHSmoothingScale zeroth / first moments
+    const double fw = (lj != li) ? mj * rhoi / (mi * rhoj) : 1.0;
+    a.m0 += fw * WSPHi;
+    const double fwW = fw * WSPHi;
+    a.m1x -= fwW * eix; a.m1y -= fwW * eiy; a.m1z -= fwW * eiz;
+  }
+  finalizeNode(F, i, li, a, mi, rhoi, vxi, vyi, vzi, ai, (int)(e - s), hp, t.herm);
+}
+
+//------------------------------------------------------------------------------
+// GenericHydro::dt (src/Physics/GenericHydro.cc:113-381): node limits and the
+// pairwise velocity-difference limit, min-reduced.  The reason code travels
+// with the value (value, reason) through both reduction stages.
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict__ list, long n, Grid g,
+                                                NeighborLists nl, HydroParams hp, double maxNperh,
+                                                double* __restrict__ part) {
+  __shared__ double sv[128];
+  __shared__ int sr[128];
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const double tiny = DBL_EPSILON;
+  double best = DBL_MAX;
+  int reason = -1;
+  if (i < n) {
+    const NodeListParams L = cLists[list[i]];
+    const double ai = F.f[F_HINV][i];
+    const double nodeScalei = 1.0 / ai / L.nPerh;
+    const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
+    const double rhoi = F.f[F_RHO][i];
+    const double csDt = nodeScalei / (F.f[F_CS][i] + tiny);
+    if (csDt < best) { best = csDt; reason = 0; }
+    const double csq = sqrt(F.f[F_MAXQ][i] / rhoi);
+    const double csqDt = nodeScalei / (csq + tiny);
+    if (csqDt < best) { best = csqDt; reason = 1; }
+    const double divv = F.f[F_DVDX_XX][i] + F.f[F_DVDX_YY][i] + F.f[F_DVDX_ZZ][i];
+    const double divvDt = 1.0 / (fabs(divv) + tiny);
+    if (divvDt < best) { best = divvDt; reason = 2; }
+    const double vmag = sqrt(vxi * vxi + vyi * vyi + vzi * vzi);
+    const double ax = F.f[F_DVDT_X][i], ay = F.f[F_DVDT_Y][i], az = F.f[F_DVDT_Z][i];
+    const double amag = sqrt(ax * ax + ay * ay + az * az);
+    const double dtAcc = 0.1 * fmax(nodeScalei / (vmag + tiny), vmag / (amag + tiny));
+    if (dtAcc < best) { best = dtAcc; reason = 3; }
+    if (hp.useVelMagDt) {
+      const double velDt = nodeScalei / (vmag + 1.0e-10);
+      if (velDt < best) { best = velDt; reason = 4; }
+    }
+    const double nsi = 1.0 / ai / maxNperh;
+    const long long e = nl.start[i + 1];
+    for (long long k = nl.start[i]; k < e; ++k) {
+      const uint32_t ent = nl.nbr[k];
+      const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+      double vxj = F.f[F_VX][j], vyj = F.f[F_VY][j], vzj = F.f[F_VZ][j];
+      imageVec(g, code, vxj, vyj, vzj);
+      const double nsj = 1.0 / F.f[F_HINV][j] / maxNperh;
+      const double dvx = vxi - vxj, dvy = vyi - vyj, dvz = vzi - vzj;
+      const double vm = sqrt(dvx * dvx + dvy * dvy + dvz * dvz);
+      const double dtv = fmin(nsi, nsj) * (1.0 / fmax(tiny, vm));
+      if (dtv < best) { best = dtv; reason = 5; }
+    }
+  }
+  sv[threadIdx.x] = best;
+  sr[threadIdx.x] = reason;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && sv[threadIdx.x + o] < sv[threadIdx.x]) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      sr[threadIdx.x] = sr[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = sv[0]; part[2 * blockIdx.x + 1] = (double)sr[0]; }
+}
+__global__ void dtFinalKernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sv[256];
+  __shared__ double sr[256];
+  double best = DBL_MAX, reason = -1.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (part[2 * b] < best) { best = part[2 * b]; reason = part[2 * b + 1]; }
+  sv[threadIdx.x] = best;
+  sr[threadIdx.x] = reason;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && sv[threadIdx.x + o] < sv[threadIdx.x]) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      sr[threadIdx.x] = sr[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = sv[0]; out[1] = sr[0]; }
+}
+
+//------------------------------------------------------------------------------
+// SpecificThermalEnergyPolicy::update (src/Hydro/SpecificThermalEnergyPolicy.cc:110-173),
+// gathered: node i takes its own share w_i du_ij of every pair, with the pair
+// acceleration stored per ordered slot by the pair loop.
+//------------------------------------------------------------------------------
+template <bool F32PACC>
+__global__ void __launch_bounds__(128) energyKernel(Fields F, long n, Grid g, NeighborLists nl,
+                                                    const double* __restrict__ pacc, const float* __restrict__ pacc32,
+                                                    double dt) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double hdt = 0.5 * dt;
+  const double* __restrict__ VX = F.f[F_VX];
+  const double* __restrict__ VY = F.f[F_VY];
+  const double* __restrict__ VZ = F.f[F_VZ];
+  const double* __restrict__ AX = F.f[F_DVDT_X];
+  const double* __restrict__ AY = F.f[F_DVDT_Y];
+  const double* __restrict__ AZ = F.f[F_DVDT_Z];
+  const double* __restrict__ D0 = F.f[F_DEPSDT];
+  const double vxi = VX[i] + AX[i] * hdt, vyi = VY[i] + AY[i] * hdt, vzi = VZ[i] + AZ[i] * hdt;
+  const double d0i = D0[i];
+  double sum = 0.0;
+  const long long e = nl.start[i + 1];
+  for (long long k = nl.start[i]; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    double vxj = VX[j], vyj = VY[j], vzj = VZ[j], axj = AX[j], ayj = AY[j], azj = AZ[j];
+    imageVec(g, code, vxj, vyj, vzj);
+    imageVec(g, code, axj, ayj, azj);
+    const double wx = vxj + axj * hdt - vxi, wy = vyj + ayj * hdt - vyi, wz = vzj + azj * hdt - vzi;
+    double px, py, pz;
+    if (F32PACC) { px = pacc32[3 * k]; py = pacc32[3 * k + 1]; pz = pacc32[3 * k + 2]; }
+    else { px = pacc[3 * k]; py = pacc[3 * k + 1]; pz = pacc[3 * k + 2]; }
+    const double du = wx * px + wy * py + wz * pz;
+    const double sg = du < 0.0 ? -1.0 : 1.0;
+    const double weighti = fmax(DBL_EPSILON, d0i * sg);
+    const double weightj = fmax(DBL_EPSILON, D0[j] * sg);
+    const double wi = weighti / (weighti + weightj);
+    sum += wi * du;
+  }
+  F.f[F_DEPS_COMPAT][i] = sum;
+  F.f[F_EPS][i] += sum * dt;
+}
+
+//------------------------------------------------------------------------------
+// State updates (State::update with IncrementState / IncrementBoundedState /
+// ReplaceBoundedState, PressurePolicy, SoundSpeedPolicy) and GammaLawGas.
+//------------------------------------------------------------------------------
+__device__ __forceinline__ void eosNode(Fields& F, long i, const NodeListParams& L) {
+  const double rho = F.f[F_RHO][i], eps = F.f[F_EPS][i];
+  double p = (L.gamma - 1.0) * rho * eps;
+  p = p < L.minP ? L.minP : (p > L.maxP ? L.maxP : p);
+  F.f[F_P][i] = p;
+  F.f[F_CS][i] = sqrt(fmax(0.0, L.gamma * (L.gamma - 1.0) * eps));
+}
+
+__global__ void saveState0Kernel(Fields F, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  F.f[F_X0][i] = F.f[F_X][i]; F.f[F_Y0][i] = F.f[F_Y][i]; F.f[F_Z0][i] = F.f[F_Z][i];
+  F.f[F_VX0][i] = F.f[F_VX][i]; F.f[F_VY0][i] = F.f[F_VY][i]; F.f[F_VZ0][i] = F.f[F_VZ][i];
+  F.f[F_RHO0][i] = F.f[F_RHO][i]; F.f[F_EPS0][i] = F.f[F_EPS][i]; F.f[F_HINV0][i] = F.f[F_HINV][i];
+}
+__global__ void restoreState0Kernel(Fields F, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  F.f[F_X][i] = F.f[F_X0][i]; F.f[F_Y][i] = F.f[F_Y0][i]; F.f[F_Z][i] = F.f[F_Z0][i];
+  F.f[F_VX][i] = F.f[F_VX0][i]; F.f[F_VY][i] = F.f[F_VY0][i]; F.f[F_VZ][i] = F.f[F_VZ0][i];
+  F.f[F_RHO][i] = F.f[F_RHO0][i]; F.f[F_EPS][i] = F.f[F_EPS0][i]; F.f[F_HINV][i] = F.f[F_HINV0][i];
+}
+
+__global__ void updateKernel(Fields F, const int* __restrict__ list, long n, double mult, int mid, int gravity,
+                             int epsIncrement) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const NodeListParams L = cLists[list[i]];
+  if (epsIncrement) F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
+  F.f[F_X][i] += mult * F.f[F_DXDT_X][i];
+  F.f[F_Y][i] += mult * F.f[F_DXDT_Y][i];
+  F.f[F_Z][i] += mult * F.f[F_DXDT_Z][i];
+  // velocity: "delta velocity hydro" sorts before "delta velocity" (gravity)
+  F.f[F_VX][i] += mult * F.f[F_DVDT_X][i];
+  F.f[F_VY][i] += mult * F.f[F_DVDT_Y][i];
+  F.f[F_VZ][i] += mult * F.f[F_DVDT_Z][i];
+  if (gravity) {
+    F.f[F_VX][i] += mult * F.f[F_GRAV_X][i];
+    F.f[F_VY][i] += mult * F.f[F_GRAV_Y][i];
+    F.f[F_VZ][i] += mult * F.f[F_GRAV_Z][i];
+  }
+  F.f[F_RHO][i] = fmin(L.rhoMax, fmax(L.rhoMin, F.f[F_RHO][i] + mult * F.f[F_DRHODT][i]));
+  const double hminInv = 1.0 / L.hmin, hmaxInv = 1.0 / L.hmax;
+  double h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
+  if (h < hmaxInv) h = hmaxInv;
+  if (h > hminInv) h = hminInv;
+  F.f[F_HINV][i] = h;
+  eosNode(F, i, L);
+}
+
+__global__ void eosKernel(Fields F, const int* __restrict__ list, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  eosNode(F, i, cLists[list[i]]);
+}
+
+// Boundary::setAllViolationNodes + enforceBoundary (PlanarBoundary.cc:153-190,
+// ReflectingBoundary.cc:465-473): nodes strictly outside a plane are mapped
+// back; reflecting walls also mirror the velocity.
+__device__ __forceinline__ bool fuzzyZero(double x) { return fabs(x) <= 1.0e-15 * fmax(1.0, fabs(x)); }
+__global__ void enforceKernel(Fields F, long n, Grid g) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* P[3] = {F.f[F_X], F.f[F_Y], F.f[F_Z]};
+  double* V[3] = {F.f[F_VX], F.f[F_VY], F.f[F_VZ]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double lo = g.wallLo[a], hi = g.wallHi[a];
+    double p = P[a][i];
+    const double sdLo = p - lo, sdHi = hi - p;
+    if (g.kindLo[a] == AXIS_PERIODIC) {
+      if (sdLo < 0.0 && !fuzzyZero(sdLo)) p = imageCoord(p, 2, AXIS_PERIODIC, AXIS_PERIODIC, lo, hi);
+      else if (sdHi < 0.0 && !fuzzyZero(sdHi)) p = imageCoord(p, 1, AXIS_PERIODIC, AXIS_PERIODIC, lo, hi);
+      P[a][i] = p;
+    } else {
+      if (g.kindLo[a] == AXIS_REFLECT && sdLo < 0.0 && !fuzzyZero(sdLo)) {
+        p = imageCoord(p, 1, AXIS_REFLECT, g.kindHi[a], lo, hi);
+        P[a][i] = p;
+        V[a][i] = -V[a][i];
+      }
+      const double sdHi2 = hi - p;
+      if (g.kindHi[a] == AXIS_REFLECT && sdHi2 < 0.0 && !fuzzyZero(sdHi2)) {
+        p = imageCoord(p, 2, g.kindLo[a], AXIS_REFLECT, lo, hi);
+        P[a][i] = p;
+        V[a][i] = -V[a][i];
+      }
+    }
+  }
+}
+
+// SpheralConservation totals (SpheralConservation.py:54-150) in FP64:
+// mass, momentum, kinetic, thermal, gravitational (1/2 m phi).
+__global__ void conservationKernel(Fields F, long n, int gravity, double* __restrict__ part) {
+  __shared__ double sm[32];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double m = F.f[F_MASS][i], vx = F.f[F_VX][i], vy = F.f[F_VY][i], vz = F.f[F_VZ][i];
+    acc[0] += m;
+    acc[1] += m * vx; acc[2] += m * vy; acc[3] += m * vz;
+    acc[4] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+    acc[5] += m * F.f[F_EPS][i];
+    if (gravity) acc[6] += 0.5 * m * F.f[F_POT][i];
+  }
+  for (int k = 0; k < 7; ++k) {
+    const double r = blockSum(acc[k], sm);
+    if (threadIdx.x == 0) part[blockIdx.x * 7 + k] = r;
+  }
+}
+__global__ void conservationFinalKernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sm[32];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int k = 0; k < 7; ++k) acc[k] += part[b * 7 + k];
+  for (int k = 0; k < 7; ++k) {
+    const double r = blockSum(acc[k], sm);
+    if (threadIdx.x == 0) out[k] = r;
+  }
+  if (threadIdx.x == 0) out[7] = out[4] + out[5] + out[6];
+}
+
+__global__ void checkStateKernel(Fields F, long n, int* __restrict__ flag) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double m = F.f[F_MASS][i], rho = F.f[F_RHO][i], a = F.f[F_HINV][i], eps = F.f[F_EPS][i];
+  const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i];
+  const double vx = F.f[F_VX][i], vy = F.f[F_VY][i], vz = F.f[F_VZ][i];
+  const bool bad = !(m > 0.0) || !(rho > 0.0) || !(a > 0.0) || !isfinite(eps) || !isfinite(x) || !isfinite(y) ||
+                   !isfinite(z) || !isfinite(vx) || !isfinite(vy) || !isfinite(vz) || !isfinite(rho) || !isfinite(a);
+  if (bad) atomicExch(flag, 1);
+}
+
+inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+//==============================================================================
+// Launchers
+//==============================================================================
+void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+                  LaunchCounter* lc) {
+  int nb = (int)std::min<long>((n + 255) / 256, nScratch / 7);
+  if (nb < 1) nb = 1;
+  boundsKernel<<<nb, 256, 0, s>>>(F, n, dScratch);
+  boundsFinalKernel<<<1, 256, 0, s>>>(dScratch, nb, dOut);
+  lc->add(2);
+}
+void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, uint32_t* cellc, cudaStream_t s,
+                    LaunchCounter* lc) {
+  cellKeyKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, g, keys, vals, cellc);
+  lc->add(1);
+}
+void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
+                   const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
+                   cudaStream_t s, LaunchCounter* lc) {
+  permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n);
+  lc->add(1);
+}
+void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
+                      LaunchCounter* lc) {
+  cellRangeKernel<<<gridFor(n, 256), 256, 0, s>>>(sortedKeys, n, cellStart, cellEnd);
+  lc->add(1);
+}
+void launchNeighborCount(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
+                         const int* cellEnd, int* counts, double ext2, cudaStream_t s, LaunchCounter* lc) {
+  neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, cellc, n, g, cellStart, cellEnd, counts, nullptr, nullptr,
+                                                         ext2);
+  lc->add(1);
+}
+void launchNeighborFill(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
+                        const int* cellEnd, const long long* start, uint32_t* nbr, double ext2, cudaStream_t s,
+                        LaunchCounter* lc) {
+  neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, cellc, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2);
+  lc->add(1);
+}
+void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                      cudaStream_t s, LaunchCounter* lc) {
+  const size_t sm = sizeof(double) * 3 * (hp.tableN1 + 1);
+  sumDensityKernel<<<gridFor(n, 128), 128, sm, s>>>(F, list, n, g, nl, t, hp);
+  lc->add(1);
+}
+void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
+                 LaunchCounter* lc) {
+  const size_t sm = sizeof(double) * 6 * (hp.tableN1 + 1);
+  gradhKernel<<<gridFor(n, 128), 128, sm, s>>>(F, n, g, nl, t, hp);
+  lc->add(1);
+}
+void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                    const NodeListParams* lists, double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  const size_t sm = sizeof(double) * 6 * (hp.tableN1 + 1);
+  const int b = 128;
+  (void)blockSize;
+  if (hp.xsph) {
+    if (hp.compatible) pairKernelFP64<true, true><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+    else pairKernelFP64<true, false><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+  } else {
+    if (hp.compatible) pairKernelFP64<false, true><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+    else pairKernelFP64<false, false><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+  }
+  lc->add(1);
+}
+void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
+              const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+              cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  const int nb = (int)gridFor(n, 128);
+  (void)nScratch;
+  dtKernel<<<nb, 128, 0, s>>>(F, list, n, g, nl, hp, maxNperh, dScratch);
+  dtFinalKernel<<<1, 256, 0, s>>>(dScratch, nb, dOut);
+  lc->add(2);
+}
+void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
+                            double dt, cudaStream_t s, LaunchCounter* lc) {
+  if (pacc32) energyKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, pacc, pacc32, dt);
+  else energyKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, pacc, pacc32, dt);
+  lc->add(1);
+}
+void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
+  saveState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
+  lc->add(1);
+}
+void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
+  restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
+  lc->add(1);
+}
+void launchUpdate(Fields F, const int* list, long n, const NodeListParams* lists, HydroParams hp, double mult,
+                  bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  const int epsInc = (mid || !hp.compatible) ? 1 : 0;
+  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc);
+  lc->add(1);
+}
+void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  eosKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n);
+  lc->add(1);
+}
+void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc) {
+  enforceKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, g);
+  lc->add(1);
+}
+void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+                        LaunchCounter* lc) {
+  int nb = (int)std::min<long>((n + 255) / 256, nScratch / 7);
+  if (nb < 1) nb = 1;
+  conservationKernel<<<nb, 256, 0, s>>>(F, n, gravity ? 1 : 0, dScratch);
+  conservationFinalKernel<<<1, 256, 0, s>>>(dScratch, nb, dOut);
+  lc->add(2);
+}
+void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc) {
+  checkStateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, dFlag);
+  lc->add(1);
+}
+
+}  // namespace sph

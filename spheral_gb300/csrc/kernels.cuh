@@ -1,0 +1,82 @@
+// Host-callable launchers of the hydro kernels (defined in hydro.cu) and the
+// gravity kernels (gravity.cu).
+#pragma once
+#include "fields.cuh"
+#include "sort.cuh"
+
+namespace sph {
+
+struct TableDev {
+  const double* w;      // 3*(N1+1) quadratic coefficients of W
+  const double* g;      // 3*(N1+1) quadratic coefficients of dW/deta
+  const double* herm;   // 2*hermN Hermite knots of the nperh lookup (values, slopes)
+  const float* w32;     // FP32 copies for the FP32 pair loop
+  const float* g32;
+};
+
+struct NeighborLists {
+  const long long* start;   // n+1 offsets
+  const uint32_t* nbr;      // entries: index | code << 26
+};
+
+// Reductions ------------------------------------------------------------------
+// out[0] = min hinv, out[1..3] = min x,y,z, out[4..6] = max x,y,z
+void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+                  LaunchCounter* lc);
+
+// Neighbour build -------------------------------------------------------------
+void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, uint32_t* cellc, cudaStream_t s,
+                    LaunchCounter* lc);
+void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
+                   const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
+                   cudaStream_t s, LaunchCounter* lc);
+void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
+                      LaunchCounter* lc);
+void launchNeighborCount(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
+                         const int* cellEnd, int* counts, double ext2, cudaStream_t s, LaunchCounter* lc);
+void launchNeighborFill(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
+                        const int* cellEnd, const long long* start, uint32_t* nbr, double ext2, cudaStream_t s,
+                        LaunchCounter* lc);
+
+// Sweeps ---------------------------------------------------------------------
+void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                      cudaStream_t s, LaunchCounter* lc);
+void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
+                 LaunchCounter* lc);
+void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                    const NodeListParams* lists, double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
+void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                    HydroParams hp, const NodeListParams* lists, float* pacc, int blockSize, cudaStream_t s,
+                    LaunchCounter* lc);
+void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
+// dt: writes per-block (value, reason) pairs then a final min into dOut[0], dOut[1] (reason as double)
+void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
+              const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+              cudaStream_t s, LaunchCounter* lc);
+void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
+                            double dt, cudaStream_t s, LaunchCounter* lc);
+void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
+void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
+// mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
+// already advanced by the compatible-energy sweep when compatible).
+void launchUpdate(Fields F, const int* list, long n, const NodeListParams* lists, HydroParams hp, double mult,
+                  bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc);
+void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc);
+void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
+// out[0..7] conservation totals
+void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+                        LaunchCounter* lc);
+// check finite / positive state: writes a flag
+void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc);
+
+// Gravity (gravity.cu) ---------------------------------------------------------
+struct GravityWork;
+GravityWork* gravityCreate();
+void gravityDestroy(GravityWork* w);
+// Build the octree of the current positions and walk it; writes F_GRAV_*,
+// F_POT (already multiplied by G) and returns dtMinAcc via dOut[0], extra
+// energy via dOut[1].
+int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening, double opening, double* dOut,
+                    cudaStream_t s, LaunchCounter* lc, char* err, int errlen);
+
+}  // namespace sph

@@ -1,0 +1,184 @@
+"""Device-resident SPH engine: a thin Python handle over the C ABI.
+
+``Engine`` owns one ``sphgpu_handle``; the particle state lives on the GPU
+between calls and every physics call launches the library's sm_103a kernels.
+There is no host fallback: without the built library or a CUDA device every
+call raises ``SphGpuError``.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+FIELD_NCOMP = {
+    "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
+    "pressure": 1, "soundSpeed": 1, "omegaGradh": 1, "massDensitySum": 1, "normalization": 1, "DxDt": 3,
+    "DvDt": 3, "DrhoDt": 1, "DepsDt": 1, "DvDx": 9, "internalDvDx": 9, "gradRho": 3, "M": 9, "localM": 9,
+    "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
+    "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
+    "DepsDtCompatible": 1, "numNeighbors": 1,
+}
+
+DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acceleration", "velocity magnitude",
+              "pairwise velocity difference", "gravity"]
+
+
+def config_from_dict(cfg, precision="fp64", device=0):
+    c = N.default_config()
+    for k, v in cfg.items():
+        if k in dict(N.Config._fields_):
+            setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
+    c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)
+    c.device = device
+    return c
+
+
+class Engine:
+    def __init__(self, config=None, precision="fp64", device=0, table=None):
+        self.L = N.lib()
+        cfg = config_from_dict(config or {}, precision, device)
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = self.L.sphgpu_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != N.SPHGPU_OK:
+            raise N.SphGpuError(rc, "sphgpu_create failed")
+        self.h = h
+        self.n = 0
+        if table is not None:
+            self.set_kernel_table(table)
+
+    @classmethod
+    def from_problem(cls, problem, precision="fp64", device=0, table=None):
+        e = cls(problem.config, precision, device, table)
+        e.load(problem)
+        return e
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sphgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        N.check(self.h, rc)
+
+    # -- set up ---------------------------------------------------------------
+    def set_kernel_table(self, t):
+        arrs = [np.ascontiguousarray(t[k], dtype=np.float64) for k in ("W", "gradW", "grad2W", "nperh", "wsum", "meta")]
+        self._table_keep = arrs
+        self._chk(self.L.sphgpu_set_kernel_table(self.h, *[N.dptr(a) for a in arrs]))
+
+    def set_nodelist(self, k, nPerh, hmin, hmax, rhoMin, rhoMax, gamma):
+        self._chk(self.L.sphgpu_set_nodelist(self.h, k, nPerh, hmin, hmax, rhoMin, rhoMax, gamma))
+
+    def add_boundary(self, type, axis, lo, hi, wall_high=0):
+        self._chk(self.L.sphgpu_add_boundary(self.h, type, axis, lo, hi, wall_high))
+
+    def set_particles(self, pos, vel, mass, rho, eps, H, nodelist=None):
+        n = len(mass)
+        arr = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        keep = [arr(pos), arr(vel), arr(mass), arr(rho), arr(eps), arr(H)]
+        nl = None if nodelist is None else np.ascontiguousarray(nodelist, dtype=np.int32)
+        self._chk(self.L.sphgpu_set_particles(self.h, n, *[N.dptr(a) for a in keep],
+                                              None if nl is None else N.iptr(nl)))
+        self.n = n
+
+    def load(self, problem):
+        for k, nl in enumerate(problem.nodelists):
+            self.set_nodelist(k, nl["nPerh"], nl["hmin"], nl["hmax"], nl["rhoMin"], nl["rhoMax"], nl["gamma"])
+        for b in problem.boundaries:
+            self.add_boundary(b["type"], b["axis"], b["lo"], b["hi"], b.get("wall_high", 0))
+        self.set_particles(problem.pos, problem.vel, problem.mass, problem.rho, problem.eps, problem.H,
+                           problem.nodelist)
+
+    # -- physics --------------------------------------------------------------
+    def initialize(self):
+        self._chk(self.L.sphgpu_initialize(self.h))
+
+    def connectivity(self):
+        self._chk(self.L.sphgpu_connectivity(self.h))
+
+    def sum_density(self):
+        self._chk(self.L.sphgpu_sum_density(self.h))
+
+    def gradh(self):
+        self._chk(self.L.sphgpu_gradh(self.h))
+
+    def evaluate_derivatives(self):
+        self._chk(self.L.sphgpu_evaluate_derivatives(self.h))
+
+    def dt(self):
+        d = ctypes.c_double()
+        r = ctypes.c_int()
+        self._chk(self.L.sphgpu_dt(self.h, ctypes.byref(d), ctypes.byref(r)))
+        return d.value, (DT_REASONS[r.value] if 0 <= r.value < len(DT_REASONS) else str(r.value))
+
+    def step(self, max_time=1.0e300):
+        d = ctypes.c_double()
+        self._chk(self.L.sphgpu_step(self.h, max_time, ctypes.byref(d)))
+        return d.value
+
+    def advance(self, nsteps, max_time=1.0e300):
+        self._chk(self.L.sphgpu_advance(self.h, nsteps, max_time))
+
+    def synchronize(self):
+        self._chk(self.L.sphgpu_synchronize(self.h))
+
+    # -- inspection -----------------------------------------------------------
+    def field(self, name):
+        nc = FIELD_NCOMP[name]
+        out = np.zeros(self.n * nc)
+        self._chk(self.L.sphgpu_get_field(self.h, name.encode(), N.dptr(out), None))
+        return out.reshape(self.n, nc) if nc > 1 else out
+
+    def set_field(self, name, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._chk(self.L.sphgpu_set_field(self.h, name.encode(), N.dptr(v)))
+
+    def pairs(self):
+        n = ctypes.c_long()
+        self._chk(self.L.sphgpu_get_pairs(self.h, None, None, None, ctypes.byref(n)))
+        i = np.zeros(n.value, np.int32)
+        j = np.zeros(n.value, np.int32)
+        im = np.zeros(n.value, np.int32)
+        self._chk(self.L.sphgpu_get_pairs(self.h, N.iptr(i), N.iptr(j), N.iptr(im), ctypes.byref(n)))
+        return i, j, im
+
+    def conservation(self):
+        out = np.zeros(8)
+        self._chk(self.L.sphgpu_conservation(self.h, N.dptr(out)))
+        return out
+
+    @property
+    def time(self):
+        t = ctypes.c_double()
+        self._chk(self.L.sphgpu_get_time(self.h, ctypes.byref(t), None, None))
+        return t.value
+
+    def clock(self):
+        t, d, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+        self._chk(self.L.sphgpu_get_time(self.h, ctypes.byref(t), ctypes.byref(d), ctypes.byref(c)))
+        return t.value, d.value, c.value
+
+    def profile(self, enable=True):
+        self._chk(self.L.sphgpu_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_reset(self):
+        self._chk(self.L.sphgpu_profile_reset(self.h))
+
+    def profile_get(self, name):
+        n = ctypes.c_long()
+        ms = ctypes.c_double()
+        self._chk(self.L.sphgpu_profile_get(self.h, name.encode(), ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
+
+    def launch_count(self):
+        n = ctypes.c_long()
+        self._chk(self.L.sphgpu_launch_count(self.h, ctypes.byref(n)))
+        return n.value

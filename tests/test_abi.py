@@ -1,0 +1,60 @@
+"""CPU checks of the C-ABI library: it loads, exports every entry point that
+include/sphgpu.h declares, builds the kernel table on the host (matching the
+oracle's restatement of TableKernel), and fails loudly -- with a status code,
+not a crash or a silent fallback -- when no GPU is present."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            names += re.findall(r"^\s*(?:int|void|const char\*)\s+(sphgpu_\w+)\s*\(", txt, re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    names = declared_symbols()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(native_lib, n), n
+
+
+def test_host_table_matches_oracle(native_lib, oracle_mod):
+    from spheral_gb300 import _native, problems
+    t = _native.build_bspline_table(1000)
+    o = oracle_mod.Oracle(problems.random_box(n_side=12))
+    r = o.table()
+    for k in ("W", "gradW", "grad2W", "nperh", "wsum", "meta"):
+        a, b = t[k], r[k]
+        assert a.shape == b.shape
+        assert np.max(np.abs(a - b)) <= 1e-14 * max(1.0, np.max(np.abs(b))), k
+
+
+def test_default_config_values(native_lib):
+    from spheral_gb300 import _native
+    c = _native.default_config()
+    assert c.cfl == 0.25 and c.compatible_energy == 1 and c.gradh_correction == 1
+    assert c.Cl == 1.0 and c.Cq == 1.0 and c.eps2 == 1.0e-2 and c.num_table_points == 1000
+
+
+def test_create_without_gpu_fails_loudly(native_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from spheral_gb300 import _native
+    c = _native.default_config()
+    h = ctypes.c_void_p()
+    rc = native_lib.sphgpu_create(ctypes.byref(c), ctypes.byref(h))
+    assert rc == 1 and not h.value
+    from spheral_gb300.engine import Engine
+    with pytest.raises(_native.SphGpuError):
+        Engine({})

@@ -1,0 +1,169 @@
+"""CPU checks that pin the oracle to the reference's own tests and invariants.
+
+* TableKernel accuracy and lookup consistency, after
+  tests/unit/Kernel/testTableKernel.py:35-175 (W within 1e-3, grad W within
+  1e-2 of the analytic B-spline; monotonic nperh / Wsum lookups; 3-D lattice
+  Wsum sums).
+* Neighbour sets equal a brute-force search with the ConnectivityMap
+  criterion, after tests/unit/Neighbor/NeighborTestBase.py:134-260 and
+  SpheralTestUtilities.findNeighborNodes (src/SimulationControl/SpheralTestUtilities.py:71-83).
+* Linear velocity fields are differentiated exactly by the corrected SPH
+  gradient, after tests/unit/SPH/testLinearVelocityGradient.py.
+* Compatible-energy CheapRK2 steps conserve total energy and momentum to
+  rounding (SpecificThermalEnergyPolicy.cc:86-108 contract).
+"""
+import math
+import random
+
+import numpy as np
+import pytest
+
+from spheral_gb300 import problems
+
+
+def fuzzy_equal(a, b, fuzz):
+    # SpheralTestUtilities.fuzzyEqual (src/SimulationControl/SpheralTestUtilities.py:199-205)
+    return abs(a - b) / max(1.0, abs(a) + abs(b)) < fuzz
+
+
+@pytest.fixture(scope="module")
+def table_oracle(oracle_mod):
+    p = problems.random_box(n_side=12, seed=3)
+    return oracle_mod.Oracle(p)
+
+
+def test_table_matches_analytic_bspline(table_oracle, oracle_mod):
+    o = table_oracle
+    n = 1000
+    for i in range(n):
+        eta = i * 2.0 / (n - 1)
+        assert fuzzy_equal(o.kernel_value(eta, 1.0), oracle_mod.bspline_value(eta), 1.0e-3)
+        assert fuzzy_equal(o.grad_value(eta, 1.0), oracle_mod.bspline_grad(eta), 1.0e-2)
+
+
+def test_table_lookups_monotonic(table_oracle):
+    o = table_oracle
+    t = o.table()
+    mn, mx = t["meta"][7], t["meta"][8]
+    wmin, wmax = o.wsum_lookup(mn), o.wsum_lookup(mx)
+    nperh = np.array([o.nperh_lookup(x) for x in np.linspace(wmin, wmax, 2000)])
+    assert np.all(np.diff(nperh) >= 0.0)
+    wsum = np.array([o.wsum_lookup(x) for x in np.linspace(mn, mx, 2000)])
+    assert np.all(np.diff(wsum) >= 0.0)
+
+
+def test_table_wsum_3d_lattice_sums(table_oracle, oracle_mod):
+    o = table_oracle
+    rng = random.Random(458945989204001)
+    t = o.table()
+    mn = max(t["meta"][7], 1.0)
+    for _ in range(6):
+        nperh = rng.uniform(mn, 6.0)
+        deta = 1.0 / nperh
+        etac = np.arange(-2.0, 2.0 + deta, deta)
+        X, Y, Z = np.meshgrid(etac, etac, etac, indexing="ij")
+        r = np.sqrt(X * X + Y * Y + Z * Z).ravel()
+        vals = np.array([abs(o.grad_value(x, 1.0)) if x < 2.0 else 0.0 for x in r])
+        test_sum = vals.sum() ** (1.0 / 3.0)
+        tol = 5.0 * 2.0e-1 / (2.0 / deta) ** 3
+        assert fuzzy_equal(o.wsum_lookup(nperh), test_sum, tol)
+        assert fuzzy_equal(o.nperh_lookup(test_sum), nperh, tol)
+
+
+def _brute_pairs(pos, hinv, images):
+    """All (i, j, image) with min(|Hi rij|, |Hj rij|) <= 2, i internal."""
+    n = len(pos)
+    out = set()
+    for code, shift in images:
+        pj = pos + shift
+        d = pos[:, None, :] - pj[None, :, :]
+        r = np.sqrt(np.sum(d * d, axis=2))
+        ei = r * hinv[:, None]
+        ej = r * hinv[None, :]
+        ok = (np.minimum(ei, ej) <= 2.0)
+        if code == 0:
+            np.fill_diagonal(ok, False)
+        ii, jj = np.nonzero(ok)
+        out.update(zip(ii.tolist(), jj.tolist(), [code] * len(ii)))
+    return out
+
+
+def _expand_unordered(i, j, im, periodic_axes):
+    s = set()
+    for a, b, c in zip(i.tolist(), j.tolist(), im.tolist()):
+        s.add((a, b, c))
+        inv = 0
+        for ax in range(3):
+            code = (c >> (2 * ax)) & 3
+            if code and ax in periodic_axes:
+                code = 3 - code
+            inv |= code << (2 * ax)
+        s.add((b, a, inv))
+    return s
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_oracle_pairs_match_brute_force_open(oracle_mod, seed):
+    p = problems.random_box(n_side=8, seed=seed, boundaries="open")
+    o = oracle_mod.Oracle(p)
+    o.connectivity()
+    i, j, im = o.pairs()
+    assert np.all(im == 0)
+    got = _expand_unordered(i, j, im, ())
+    want = _brute_pairs(p.pos, p.H[:, 0], [(0, np.zeros(3))])
+    assert got == want
+    nn = o.num_neighbors()
+    counts = np.bincount(np.array([a for a, _, _ in want]), minlength=p.n)
+    assert np.array_equal(nn, counts)
+
+
+def test_oracle_pairs_match_brute_force_periodic(oracle_mod):
+    p = problems.random_box(n_side=8, seed=4, boundaries="periodic", nPerh=1.1)
+    o = oracle_mod.Oracle(p)
+    o.connectivity()
+    i, j, im = o.pairs()
+    got = _expand_unordered(i, j, im, (0, 1, 2))
+    images = []
+    for cz in range(3):
+        for cy in range(3):
+            for cx in range(3):
+                code = cx | (cy << 2) | (cz << 4)
+                shift = np.array([{0: 0.0, 1: -1.0, 2: 1.0}[c] for c in (cx, cy, cz)])
+                images.append((code, shift))
+    want = _brute_pairs(p.pos, p.H[:, 0], images)
+    # Only compare pairs away from the ulp-level ambiguity at exactly eta = 2.
+    assert got == want
+
+
+def test_oracle_linear_velocity_gradient_exact(oracle_mod):
+    p = problems.random_box(n_side=10, seed=7, boundaries="open")
+    A = np.array([[0.3, -0.2, 0.1], [0.05, 0.4, -0.3], [-0.1, 0.25, 0.2]])
+    p.vel = p.pos @ A.T
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    o.evaluate_derivatives()
+    D = o.field("DvDx").reshape(-1, 3, 3)
+    nn = o.num_neighbors()
+    sel = nn > 8
+    assert sel.sum() > 0.9 * p.n
+    err = np.abs(D[sel] - A[None, :, :]).max()
+    assert err < 1.0e-10, err
+    rho = o.field("massDensity")
+    drho = o.field("DrhoDt")
+    assert np.allclose(drho[sel], -rho[sel] * np.trace(A), rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("bc", ["periodic", "reflecting"])
+def test_oracle_compatible_energy_conserves(oracle_mod, bc):
+    p = problems.random_box(n_side=9, seed=5, boundaries=bc, nPerh=1.3, vel_scale=0.2)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    c0 = o.conservation()
+    for _ in range(4):
+        o.step()
+    c1 = o.conservation()
+    assert abs(c1[7] - c0[7]) <= 1.0e-12 * abs(c0[7])
+    assert abs(c1[0] - c0[0]) <= 1.0e-14 * c0[0]
+    if bc == "periodic":
+        scale = np.sum(p.mass * np.linalg.norm(p.vel, axis=1))
+        assert np.all(np.abs(c1[1:4] - c0[1:4]) <= 1.0e-12 * scale)
