@@ -1,0 +1,346 @@
+"""Benchmark: SPH pair-interactions/s of the CheapSynchronousRK2 hydro step.
+
+Workload (default): 3-D Kelvin-Helmholtz in a periodic unit cube, two
+lattices of 112 and 140 nodes per unit length (2,074,464 nodes, the nearest
+two-lattice set to 128^3 with a 2^(-1/3) spacing ratio), nPerh 1.51, Monaghan-
+Gingold Q (Cl = Cq = 1), compatible energy, RigorousSumDensity, CFL 0.5.  One
+step = one full CheapSynchronousRK2 step (neighbour build, density sum, dt,
+half-step update, mid-point pair loop + smoothing scale, compatible-energy
+sweep, full update, boundary enforcement).
+
+value  = unordered neighbour pairs per step x steps / device time of the timed
+         steps (state resident in HBM; CUDA events on the library stream).
+e2e    = the same metric through the C ABI with host buffers: every step
+         uploads the state from pinned host memory (sphgpu_upload_state), runs
+         the step, and downloads the new state (sphgpu_download_state).
+
+--impl reference times the CPU implementation of the same step (the oracle's
+FP64/OpenMP restatement of the reference loops, all host threads) on a
+bounded sample of the workload.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np
+
+METRIC = "SPH pair-interactions/sec at stated energy error: mixed vs FP64 GPU vs CPU"
+UNIT = "pair-interactions/s"
+FLOP_PER_PAIR = 456        # algorithmic FLOPs of the reference pair body per unordered pair
+VALUES_PER_NODE = 63       # per-node state read + derivatives written by the pair loop
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured", d
+    return 6800.0, "fallback", {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+    return ws, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_workload(args):
+    from spheral_gb300 import problems
+    if args.workload == "kh":
+        return problems.kelvin_helmholtz(n1=args.n1), "kelvin_helmholtz_3d"
+    if args.workload == "sweep":
+        return problems.sweep_box(n_side=args.n1, neighbors=args.neighbors), "sweep_box"
+    if args.workload == "sod":
+        return problems.sod(nx1=args.n1), "sod_planar_3d"
+    raise SystemExit("unknown workload")
+
+
+def cpu_baseline(args, threads=None):
+    """Oracle CheapRK2 steps on a bounded sample of the workload (same
+    generator, smaller lattice); returns pairs/s and the sample description."""
+    from oracle import oracle as orc
+    from spheral_gb300 import problems
+    orc.build()
+    if args.workload == "kh":
+        p = problems.kelvin_helmholtz(n1=args.cpu_n1)
+    elif args.workload == "sweep":
+        p = problems.sweep_box(n_side=args.cpu_n1, neighbors=args.neighbors)
+    else:
+        p = problems.sod(nx1=args.cpu_n1)
+    o = orc.Oracle(p)
+    o.initialize()
+    o.step()   # warm-up step (first step allocates)
+    steps = args.cpu_steps
+    t0 = time.perf_counter()
+    pairs = 0
+    for _ in range(steps):
+        o.step()
+        pairs += o.L.orc_num_pairs(o.h)
+    dt = time.perf_counter() - t0
+    return pairs / dt, dict(n=p.n, steps=steps, seconds=dt, pairs_per_step=pairs / steps,
+                            cores=orc.num_threads(), kind="port")
+
+
+def run_reference(args, ws, rank, dist):
+    if rank != 0:
+        return
+    val, info = cpu_baseline(args)
+    sample = (f"{info['steps']} CheapSynchronousRK2 steps of the same generator at n1={args.cpu_n1} "
+              f"({info['n']} nodes, {info['pairs_per_step']:.0f} pairs/step), {info['seconds']:.1f} s")
+    line = {
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": info["steps"], "warmup": 1,
+        "ms_per_step": 1e3 * info["seconds"] / info["steps"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "impl": "reference",
+        "config": {"workload": "kelvin_helmholtz_3d" if args.workload == "kh" else args.workload,
+                   "sample_n": info["n"]},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(eng, steps, prof_names=()):
+    eng.profile_reset()
+    l0 = eng.launch_count()
+    eng.synchronize()
+    pairs = 0
+    eng.timer_start()
+    for _ in range(steps):
+        eng.step()
+        pairs += eng.neighbor_entries() // 2
+    ms = eng.timer_stop()
+    launches = eng.launch_count() - l0
+    prof = {n: eng.profile_get(n) for n in prof_names}
+    return ms, pairs, launches, prof
+
+
+def run_ours(args, ws, rank, local, dist):
+    from spheral_gb300.engine import Engine
+    prob, wname = make_workload(args)
+    n = prob.n
+    eng = Engine.from_problem(prob, precision=args.precision, device=local)
+    eng.initialize()
+    for _ in range(args.warmup):
+        eng.step()
+    e0 = eng.conservation()
+    pair_kernel = "pair_fp32" if args.precision == "fp32" else "pair_fp64"
+    names = [pair_kernel, "neighbor_count", "neighbor_fill", "sum_density", "dt", "energy", "gradh", "radix_sort",
+             "permute", "update", "prepare_fp32", "enforce", "cell_keys", "bounds", "cell_ranges"]
+    eng.profile(True)
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        ms, pairs, launches, prof = time_steps(eng, args.steps, names)
+    eng.profile(False)
+    ms = max_over_ranks(dist, ms)
+    e1 = eng.conservation()
+    energy_err = abs(e1[7] - e0[7]) / abs(e0[7])
+    value = ws * pairs / (ms / 1e3)
+    k_mean = 2.0 * pairs / args.steps / n
+
+    # e2e through the C ABI with host buffers
+    import torch
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hp, hv, hr, he, hH = pin((n, 3)), pin((n, 3)), pin(n), pin(n), pin((n, 6))
+    hm = pin(n)
+    hm[:] = prob.mass
+    eng.download_state(hp, hv, hr, he, hH)
+    barrier(dist)
+    eng.synchronize()
+    e2e_pairs = 0
+    eng.timer_start()
+    for _ in range(args.e2e_steps):
+        eng.upload_state(hp, hv, hm, hr, he, hH)
+        eng.step()
+        e2e_pairs += eng.neighbor_entries() // 2
+        eng.download_state(hp, hv, hr, he, hH)
+    e2e_ms = max_over_ranks(dist, eng.timer_stop())
+    e2e_value = ws * e2e_pairs / (e2e_ms / 1e3)
+    h2d = n * (3 + 3 + 1 + 1 + 1 + 6) * 8
+    d2h = n * (3 + 3 + 1 + 1 + 6) * 8
+
+    # FP64 GPU comparison (same workload, same step) for the mixed-vs-FP64 ratio
+    fp64 = None
+    if args.precision == "fp32" and args.fp64_steps > 0:
+        e64 = Engine.from_problem(prob, precision="fp64", device=local)
+        e64.initialize()
+        e64.step()
+        ms64, pairs64, _, _ = time_steps(e64, args.fp64_steps)
+        fp64 = {"value": pairs64 / (ms64 / 1e3), "unit": UNIT, "steps": args.fp64_steps,
+                "ms_per_step": ms64 / args.fp64_steps}
+        e64.close()
+
+    if rank != 0:
+        return
+    hbm, peak_kind, pk = peaks()
+    nl, tl = prof.get(pair_kernel, (0, 0.0))
+    avg_ms = tl / max(1, nl)
+    pairs_per_launch = pairs / max(1, args.steps)
+    elem = 4 if args.precision == "fp32" else 8
+    b_pair = elem * VALUES_PER_NODE / (k_mean / 2.0) + 6 * elem
+    achieved_gbs = b_pair * pairs_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
+    tflops = FLOP_PER_PAIR * pairs_per_launch / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else None
+    clocks = clk.summary()
+    fp32_peak = 152 * 128 * 2 * (clocks["sm_max_mhz"] or 2070.0) * 1e6 / 1e12
+    cpu = None
+    if args.cpu_steps > 0:
+        cval, cinfo = cpu_baseline(args)
+        cpu = {"value": cval, "unit": UNIT, "cores": cinfo["cores"], "kind": "port",
+               "sample": (f"{cinfo['steps']} steps of the same generator at n1={args.cpu_n1} ({cinfo['n']} nodes), "
+                          f"{cinfo['seconds']:.1f} s, FP64 oracle, OpenMP")}
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32" if args.precision == "fp32" else "f64",
+        "precision": ("FP32 pair sweeps on cell-relative positions with compensated sums; FP64 neighbour "
+                      "criterion, integration, compatible energy and tallies") if args.precision == "fp32"
+        else "FP64 throughout",
+        "data": "synthetic (seeded generator, no external data)",
+        "energy_error": energy_err,
+        "energy_error_steps": args.steps,
+        "config": {"workload": wname, "n": n, "n1": prob.meta.get("n1"), "n2": prob.meta.get("n2"),
+                   "mean_neighbors": k_mean, "pairs_per_step": pairs / args.steps,
+                   "cache": "inputs larger than L2 (state + neighbour lists > 1 GB)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": args.e2e_steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved_gbs / hbm) if achieved_gbs else None, "traffic": None,
+                     "peak_kind": peak_kind, "kernel": pair_kernel,
+                     "algorithmic_bytes_per_pair": b_pair, "pairs_per_launch": pairs_per_launch,
+                     "avg_launch_ms": avg_ms},
+        "roofline_pipe": {"unit": "TFLOP/s", "achieved": tflops, "flop_per_pair": FLOP_PER_PAIR,
+                          "peak": fp32_peak if args.precision == "fp32" else None,
+                          "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)",
+                          "frac": (tflops / fp32_peak) if (tflops and args.precision == "fp32") else None},
+        "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items() if v[0] > 0},
+        "fp64_gpu": fp64,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--n1", type=int, default=112)
+    ap.add_argument("--neighbors", type=int, default=64)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-n1", type=int, default=40)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    args = ap.parse_args()
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, dist)
+    else:
+        from spheral_gb300 import build
+        build.build()
+        run_ours(args, ws, rank, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

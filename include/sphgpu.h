@@ -182,6 +182,19 @@ int sphgpu_advance(sphgpu_handle h, int nsteps, double max_time);
 int sphgpu_get_field(sphgpu_handle h, const char* name, double* out, int* ncomp);
 int sphgpu_set_field(sphgpu_handle h, const char* name, const double* in);
 
+/* Overwrite the evolved state of all nodes from host arrays in caller order
+ * (any pointer may be NULL to keep that field).  The package's derivative
+ * fields stay on the device, as SPHBase owns its derivative FieldLists
+ * (src/SPH/SPHBase.hh:223-253) while the NodeLists own the state.
+ * Replaces: the State field references handed to Physics::evaluateDerivatives
+ * (src/Physics/Physics.hh:49-60) when the host owns the FieldLists. */
+int sphgpu_upload_state(sphgpu_handle h, const double* pos, const double* vel, const double* mass, const double* rho,
+                        const double* eps, const double* H);
+
+/* Copy the evolved state back to host arrays in caller order (NULL skips a
+ * field).  Replaces: reading the NodeList FieldLists after Integrator::step. */
+int sphgpu_download_state(sphgpu_handle h, double* pos, double* vel, double* rho, double* eps, double* H);
+
 /* Ordered neighbour pairs (i, j, image) in caller node indices; image packs
  * 2 bits per axis (0 none, 1 low-side image / lo mirror, 2 high-side image /
  * hi mirror).  Call with i == NULL to get *npairs only.
@@ -205,6 +218,12 @@ int sphgpu_profile_get(sphgpu_handle h, const char* name, long* launches, double
 int sphgpu_profile_reset(sphgpu_handle h);
 /* Number of kernels this library launched on the handle since creation. */
 int sphgpu_launch_count(sphgpu_handle h, long* launches);
+/* Device timing of everything issued on the handle's stream between the two
+ * calls (CUDA events on that stream); stop waits for the stop event. */
+int sphgpu_timer_start(sphgpu_handle h);
+int sphgpu_timer_stop(sphgpu_handle h, double* ms);
+/* Ordered neighbour entries of the current lists (2x the unordered pairs). */
+int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
 /* Wait for all work on the handle's stream. */
 int sphgpu_synchronize(sphgpu_handle h);
 

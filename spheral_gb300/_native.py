@@ -91,6 +91,8 @@ SIGNATURES = {
     "sphgpu_get_field": (_i, [_vp, _cp, _dp, _ip]),
     "sphgpu_set_field": (_i, [_vp, _cp, _dp]),
     "sphgpu_get_pairs": (_i, [_vp, _ip, _ip, _ip, _lp]),
+    "sphgpu_upload_state": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "sphgpu_download_state": (_i, [_vp, _dp, _dp, _dp, _dp, _dp]),
     "sphgpu_conservation": (_i, [_vp, _dp]),
     "sphgpu_get_time": (_i, [_vp, _dp, _dp, _lp]),
     "sphgpu_num_particles": (_i, [_vp, _lp]),
@@ -99,6 +101,9 @@ SIGNATURES = {
     "sphgpu_profile_reset": (_i, [_vp]),
     "sphgpu_launch_count": (_i, [_vp, _lp]),
     "sphgpu_synchronize": (_i, [_vp]),
+    "sphgpu_timer_start": (_i, [_vp]),
+    "sphgpu_timer_stop": (_i, [_vp, _dp]),
+    "sphgpu_neighbor_count": (_i, [_vp, _lp]),
 }
 
 

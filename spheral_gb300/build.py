@@ -18,7 +18,8 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 CUDA_SOURCES = ["sort.cu", "hydro.cu", "hydro32.cu", "gravity.cu", "api.cu"]
 HOST_SOURCES = ["table.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "-I" + CSRC, "-I" + INCLUDE]
+# -ffp-contract=off: host arithmetic (kernel-table build) is identical on x86-64 and aarch64
+COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-lineinfo", "-I" + CSRC, "-I" + INCLUDE]
 
 
 def _nvcc():

@@ -125,6 +125,8 @@ struct sphgpu_ctx {
   DBuf bankA, bankB;   // F_NUM_FIELDS * cap doubles each
   Fields F{}, Falt{};
   DBuf orig[2], list[2], cellc[2];
+  DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
+  DBuf stage;                // host <-> device staging for caller-order transfers
   int cur = 0;
   long cap = 0;
   // neighbour build
@@ -142,6 +144,7 @@ struct sphgpu_ctx {
   double dtMinAcc = 1e300, extraEnergy = 0.0;
   GravityWork* grav = nullptr;
   bool initialized = false;
+  cudaEvent_t tA = nullptr, tB = nullptr;
 
   Fields fieldsOf(DBuf& bank) {
     Fields f{};
@@ -168,7 +171,16 @@ struct sphgpu_ctx {
     t.g32 = b32 + nc;
     return t;
   }
-  NeighborLists nl() const { return NeighborLists{nbrStart.as<long long>(), nbr.as<uint32_t>()}; }
+  NeighborLists nl() { return NeighborLists{nbrStart.as<long long>(), nbr.as<uint32_t>(), cellp()}; }
+  Fields32 f32() {
+    Fields32 p;
+    p.posh = posh.as<float4>();
+    p.velm = velm.as<float4>();
+    p.thermo = thermo.as<float4>();
+    p.cell = cellp();
+    return p;
+  }
+  bool fp32() const { return cfg.precision == SPHGPU_PRECISION_FP32; }
   void check() { CUDA_OK(cudaGetLastError()); }
 };
 
@@ -182,6 +194,9 @@ void ensureCapacity(sphgpu_ctx* c, long n) {
   c->bankB.release();
   c->bankA.ensure(bytes);
   c->bankB.ensure(bytes);
+  c->posh.release(); c->posh.ensure(n * sizeof(float4));
+  c->velm.release(); c->velm.ensure(n * sizeof(float4));
+  c->thermo.release(); c->thermo.ensure(n * sizeof(float4));
   for (int k = 0; k < 2; ++k) {
     c->orig[k].release(); c->orig[k].ensure(n * sizeof(int));
     c->list[k].release(); c->list[k].ensure(n * sizeof(int));
@@ -374,13 +389,17 @@ void buildNeighbors(sphgpu_ctx* c) {
     Scope sc(c->prof, "cell_ranges");
     launchCellRanges(k, n, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->stream, &c->lc);
   }
+  {
+    Scope sc(c->prof, "prepare_fp32");
+    launchPrepareFP32(c->F, c->f32(), n, g, c->stream, &c->lc);
+  }
   c->counts.ensure(n * sizeof(int));
   c->nbrStart.ensure((n + 1) * sizeof(long long));
   c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
   const double ext2 = c->hp.extent * c->hp.extent;
   {
     Scope sc(c->prof, "neighbor_count");
-    launchNeighborCount(c->F, c->cellp(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
+    launchNeighborCount(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
                         ext2, c->stream, &c->lc);
   }
   long long* dTot = c->nbrStart.as<long long>() + n;
@@ -394,7 +413,7 @@ void buildNeighbors(sphgpu_ctx* c) {
   c->nbr.ensure(std::max<long long>(1, total) * sizeof(uint32_t));
   {
     Scope sc(c->prof, "neighbor_fill");
-    launchNeighborFill(c->F, c->cellp(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->nbrStart.as<long long>(),
+    launchNeighborFill(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->nbrStart.as<long long>(),
                        c->nbr.as<uint32_t>(), ext2, c->stream, &c->lc);
   }
   c->check();
@@ -406,19 +425,35 @@ void ensurePacc(sphgpu_ctx* c) {
   c->pacc.ensure(std::max<long long>(1, c->nnbr) * 3 * per);
 }
 
+void prepare32(sphgpu_ctx* c) {
+  if (!c->fp32()) return;
+  Scope sc(c->prof, "prepare_fp32");
+  launchPrepareFP32(c->F, c->f32(), c->n, c->grid, c->stream, &c->lc);
+  c->check();
+}
 void sumDensity(sphgpu_ctx* c) {
   Scope sc(c->prof, "sum_density");
-  launchSumDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  if (c->fp32())
+    launchSumDensityFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  else
+    launchSumDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
   c->check();
 }
 void gradh(sphgpu_ctx* c) {
   Scope sc(c->prof, "gradh");
-  launchGradh(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  if (c->fp32())
+    launchGradhFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  else
+    launchGradh(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
   c->check();
 }
 void evalDerivs(sphgpu_ctx* c) {
   ensurePacc(c);
-  {
+  if (c->fp32()) {
+    Scope sc(c->prof, "pair_fp32");
+    launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+                   c->pacc.as<float>(), 128, c->stream, &c->lc);
+  } else {
     Scope sc(c->prof, "pair_fp64");
     launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists, c->pacc.as<double>(),
                    128, c->stream, &c->lc);
@@ -444,8 +479,12 @@ double packageDt(sphgpu_ctx* c, int* reason) {
   const long nb = (c->n + 127) / 128;
   c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
   double* d = c->small.as<double>();
-  launchDt(c->F, c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(), c->scratch.as<double>(),
-           (int)(2 * nb), d, c->stream, &c->lc);
+  if (c->fp32())
+    launchDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(),
+                 c->scratch.as<double>(), (int)(2 * nb), d, c->stream, &c->lc);
+  else
+    launchDt(c->F, c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(), c->scratch.as<double>(),
+             (int)(2 * nb), d, c->stream, &c->lc);
   c->check();
   CUDA_OK(cudaMemcpyAsync(c->hsmall, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
@@ -496,6 +535,7 @@ double step(sphgpu_ctx* c, double maxTime) {
     launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, hdt, true, c->cfg.gravity != 0, c->stream, &c->lc);
   }
   c->check();
+  prepare32(c);
   c->time = t + hdt;
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
@@ -505,13 +545,17 @@ double step(sphgpu_ctx* c, double maxTime) {
   }
   if (c->cfg.compatible_energy) {
     Scope sc(c->prof, "energy");
-    launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);
+    if (c->fp32())
+      launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), nullptr, c->pacc.as<float>(), dt, c->stream, &c->lc);
+    else
+      launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);
   }
   {
     Scope sc(c->prof, "update");
     launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, dt, false, c->cfg.gravity != 0, c->stream, &c->lc);
   }
   c->check();
+  prepare32(c);
   c->time = t + dt;
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
   {
@@ -662,10 +706,12 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small};
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);
+  if (c->tA) cudaEventDestroy(c->tA);
+  if (c->tB) cudaEventDestroy(c->tB);
   if (c->hsmall) cudaFreeHost(c->hsmall);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -786,6 +832,7 @@ int sphgpu_sum_density(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
   if (!c->haveNeighbors) buildNeighbors(c);
+  prepare32(c);
   sumDensity(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -795,6 +842,7 @@ int sphgpu_gradh(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
   if (!c->haveNeighbors) buildNeighbors(c);
+  prepare32(c);
   gradh(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -805,6 +853,7 @@ int sphgpu_evaluate_derivatives(sphgpu_handle c) {
   requireState(c);
   refreshParams(c);
   if (!c->haveNeighbors) buildNeighbors(c);
+  prepare32(c);
   evalDerivs(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -815,6 +864,7 @@ int sphgpu_dt(sphgpu_handle c, double* dt, int* reason) {
   requireState(c);
   refreshParams(c);
   if (!c->haveNeighbors) buildNeighbors(c);
+  prepare32(c);
   const double v = packageDt(c, reason);
   if (dt) *dt = v;
   API_END(c)
@@ -844,31 +894,19 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   if (!out) return SPHGPU_OK;
   requireState(c);
   const long n = c->n;
-  std::vector<int> orig(n);
-  CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  std::vector<double> buf(n);
+  c->stage.ensure((size_t)n * fs.ncomp * sizeof(double));
+  double* st = c->stage.as<double>();
   if (isNb) {
     if (!c->haveNeighbors) throw Error(SPHGPU_E_STATE, "no neighbour lists yet");
-    std::vector<long long> st(n + 1);
-    CUDA_OK(cudaMemcpyAsync(st.data(), c->nbrStart.p, (n + 1) * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
-    for (long i = 0; i < n; ++i) out[orig[i]] = (double)(st[i + 1] - st[i]);
-    return SPHGPU_OK;
+    launchCountsOut(c->nbrStart.as<long long>(), c->origp(), st, n, c->stream, &c->lc);
+  } else if (isH) {
+    launchGatherOutH(c->F, c->origp(), st, fs.first, n, c->stream, &c->lc);
+  } else {
+    launchGatherOut(c->F, c->origp(), st, fs.first, fs.ncomp, fs.ncomp, n, c->stream, &c->lc);
   }
-  if (isH) {
-    CUDA_OK(cudaMemcpyAsync(buf.data(), c->F.f[fs.first], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
-    for (long i = 0; i < n; ++i) {
-      double* o = out + 6 * (size_t)orig[i];
-      o[0] = buf[i]; o[1] = 0.0; o[2] = 0.0; o[3] = buf[i]; o[4] = 0.0; o[5] = buf[i];
-    }
-    return SPHGPU_OK;
-  }
-  for (int k = 0; k < fs.ncomp; ++k) {
-    CUDA_OK(cudaMemcpyAsync(buf.data(), c->F.f[fs.first + k], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
-    for (long i = 0; i < n; ++i) out[(size_t)fs.ncomp * orig[i] + k] = buf[i];
-  }
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(out, st, (size_t)n * fs.ncomp * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
 }
 
@@ -880,16 +918,60 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   if (!fieldSpec(name, fs, isH, isNb) || isNb) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
   requireState(c);
   const long n = c->n;
-  std::vector<int> orig(n);
-  CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  c->stage.ensure((size_t)n * fs.ncomp * sizeof(double));
+  double* st = c->stage.as<double>();
+  CUDA_OK(cudaMemcpyAsync(st, in, (size_t)n * fs.ncomp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (isH) launchScatterIn(c->F, c->origp(), st, fs.first, 1, 6, n, c->stream, &c->lc);
+  else launchScatterIn(c->F, c->origp(), st, fs.first, fs.ncomp, fs.ncomp, n, c->stream, &c->lc);
+  c->check();
+  if (c->haveNeighbors) prepare32(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
-  std::vector<double> buf(n);
-  const int nc = isH ? 1 : fs.ncomp;
-  for (int k = 0; k < nc; ++k) {
-    for (long i = 0; i < n; ++i) buf[i] = isH ? in[6 * (size_t)orig[i]] : in[(size_t)fs.ncomp * orig[i] + k];
-    CUDA_OK(cudaMemcpyAsync(c->F.f[fs.first + k], buf.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, const double* mass, const double* rho,
+                        const double* eps, const double* H) {
+  API_BEGIN(c)
+  requireState(c);
+  const long n = c->n;
+  c->stage.ensure((size_t)n * 15 * sizeof(double));
+  double* st = c->stage.as<double>();
+  struct Item { const double* p; int first, ncomp, stride; };
+  const Item items[] = {{pos, F_X, 3, 3}, {vel, F_VX, 3, 3}, {mass, F_MASS, 1, 1}, {rho, F_RHO, 1, 1},
+                        {eps, F_EPS, 1, 1}, {H, F_HINV, 1, 6}};
+  size_t off = 0;
+  for (const auto& it : items) {
+    if (!it.p) continue;
+    CUDA_OK(cudaMemcpyAsync(st + off, it.p, (size_t)n * it.stride * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    launchScatterIn(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
+    off += (size_t)n * it.stride;
   }
+  c->check();
+  if (c->haveNeighbors) prepare32(c);
+  API_END(c)
+}
+
+int sphgpu_download_state(sphgpu_handle c, double* pos, double* vel, double* rho, double* eps, double* H) {
+  API_BEGIN(c)
+  requireState(c);
+  const long n = c->n;
+  c->stage.ensure((size_t)n * 14 * sizeof(double));
+  double* st = c->stage.as<double>();
+  struct Item { double* p; int first, ncomp, stride; };
+  const Item items[] = {{pos, F_X, 3, 3}, {vel, F_VX, 3, 3}, {rho, F_RHO, 1, 1}, {eps, F_EPS, 1, 1},
+                        {H, F_HINV, 1, 6}};
+  size_t off = 0;
+  for (const auto& it : items) {
+    if (!it.p) continue;
+    if (it.first == F_HINV) launchGatherOutH(c->F, c->origp(), st + off, F_HINV, n, c->stream, &c->lc);
+    else launchGatherOut(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
+    CUDA_OK(cudaMemcpyAsync(it.p, st + off, (size_t)n * it.stride * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+    off += (size_t)n * it.stride;
+  }
+  c->check();
+  CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
 }
 
@@ -902,7 +984,8 @@ int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* 
   const long n = c->n;
   std::vector<int> orig(n);
   std::vector<long long> st(n + 1);
-  std::vector<uint32_t> nb(std::max<long long>(1, c->nnbr));
+  std::vector<uint32_t> nb(std::max<long long>(1, c->nnbr)), cells(n);
+  CUDA_OK(cudaMemcpyAsync(cells.data(), c->cellp(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(st.data(), c->nbrStart.p, (n + 1) * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(nb.data(), c->nbr.p, c->nnbr * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
@@ -911,7 +994,17 @@ int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* 
     for (long long k = st[i]; k < st[i + 1]; ++k) {
       i_out[k] = orig[i];
       j_out[k] = orig[nb[k] & kIndexMask];
-      if (image) image[k] = (int)(nb[k] >> kIndexBits);
+      if (image) {
+        const int d = (int)(nb[k] >> kIndexBits);
+        int code = 0;
+        for (int a = 0; a < 3; ++a) {
+          const int ca = (int)((cells[i] >> (10 * a)) & 1023u);
+          const int da = (d >> (2 * a)) & 3;
+          if (da == 1 && ca == 0) code |= 1 << (2 * a);
+          else if (da == 2 && ca == c->grid.nc[a] - 1) code |= 2 << (2 * a);
+        }
+        image[k] = code;
+      }
     }
   API_END(c)
 }
@@ -967,6 +1060,28 @@ int sphgpu_profile_reset(sphgpu_handle c) {
 int sphgpu_launch_count(sphgpu_handle c, long* launches) {
   API_BEGIN(c)
   if (launches) *launches = c->lc.n;
+  API_END(c)
+}
+int sphgpu_timer_start(sphgpu_handle c) {
+  API_BEGIN(c)
+  if (!c->tA) CUDA_OK(cudaEventCreate(&c->tA));
+  if (!c->tB) CUDA_OK(cudaEventCreate(&c->tB));
+  CUDA_OK(cudaEventRecord(c->tA, c->stream));
+  API_END(c)
+}
+int sphgpu_timer_stop(sphgpu_handle c, double* ms) {
+  API_BEGIN(c)
+  if (!c->tA || !c->tB) throw Error(SPHGPU_E_STATE, "timer not started");
+  CUDA_OK(cudaEventRecord(c->tB, c->stream));
+  CUDA_OK(cudaEventSynchronize(c->tB));
+  float f = 0.f;
+  CUDA_OK(cudaEventElapsedTime(&f, c->tA, c->tB));
+  if (ms) *ms = f;
+  API_END(c)
+}
+int sphgpu_neighbor_count(sphgpu_handle c, long* entries) {
+  API_BEGIN(c)
+  if (entries) *entries = (long)c->nnbr;
   API_END(c)
 }
 int sphgpu_synchronize(sphgpu_handle c) {

@@ -11,112 +11,11 @@
 // nodes of periodic and reflecting boundaries are implicit: a neighbour
 // entry carries a 6-bit image code and the neighbour's coordinates are mapped
 // with the reference's own plane formula (imageCoord).
-#include "kernels.cuh"
-#include <cfloat>
+#include "device.cuh"
 
 namespace sph {
 namespace {
-
-constexpr double kTiny30 = 1.0e-30;
-
-__device__ __forceinline__ void unpackCell(uint32_t cc, int c[3]) {
-  c[0] = (int)(cc & 1023u);
-  c[1] = (int)((cc >> 10) & 1023u);
-  c[2] = (int)((cc >> 20) & 1023u);
-}
-
-// Walk the 27 cells around packed cell cc, resolving periodic wrap and
-// reflecting mirrors into (cell, image code); fn(k, code) for every candidate
-// slot k in cell order.
-template <class Fn>
-__device__ __forceinline__ void forEachCandidate(const Grid& g, uint32_t cc, const int* __restrict__ cellStart,
-                                                 const int* __restrict__ cellEnd, Fn fn) {
-  int c[3];
-  unpackCell(cc, c);
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int d[3] = {dx, dy, dz};
-        int cell[3];
-        int code = 0;
-        bool ok = true;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          int nn = c[a] + d[a];
-          if (nn < 0) {
-            if (g.kindLo[a] == AXIS_PERIODIC) nn = g.nc[a] - 1;
-            else if (g.kindLo[a] == AXIS_REFLECT) nn = 0;
-            else ok = false;
-            code |= 1 << (2 * a);
-          } else if (nn >= g.nc[a]) {
-            if (g.kindHi[a] == AXIS_PERIODIC) nn = 0;
-            else if (g.kindHi[a] == AXIS_REFLECT) nn = g.nc[a] - 1;
-            else ok = false;
-            code |= 2 << (2 * a);
-          }
-          cell[a] = nn;
-        }
-        if (!ok) continue;
-        const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
-        const int s = cellStart[key], e = cellEnd[key];
-        for (int k = s; k < e; ++k) fn(k, code);
-      }
-}
-
-__device__ __forceinline__ void imagePos(const Grid& g, int code, double& x, double& y, double& z) {
-  if (code) {
-    x = imageCoord(x, code & 3, g.kindLo[0], g.kindHi[0], g.wallLo[0], g.wallHi[0]);
-    y = imageCoord(y, (code >> 2) & 3, g.kindLo[1], g.kindHi[1], g.wallLo[1], g.wallHi[1]);
-    z = imageCoord(z, (code >> 4) & 3, g.kindLo[2], g.kindHi[2], g.wallLo[2], g.wallHi[2]);
-  }
-}
-__device__ __forceinline__ void imageVec(const Grid& g, int code, double& x, double& y, double& z) {
-  if (code) {
-    if (mirrored(code & 3, g.kindLo[0], g.kindHi[0])) x = -x;
-    if (mirrored((code >> 2) & 3, g.kindLo[1], g.kindHi[1])) y = -y;
-    if (mirrored((code >> 4) & 3, g.kindLo[2], g.kindHi[2])) z = -z;
-  }
-}
-
-// QuadraticInterpolatorView lookup shared by W and dW/deta
-// (src/Utilities/QuadraticInterpolatorViewInline.hh:17-21,71-77).
-__device__ __forceinline__ int tableIndex(double eta, int N1, double xstep) {
-  const long k = (long)(fmax(0.0, eta) / xstep);
-  return 3 * (int)min((long)N1, k);
-}
-__device__ __forceinline__ double tableEval(const double* c, int i0, double x) {
-  return c[i0] + (c[i0 + 1] + c[i0 + 2] * x) * x;
-}
-
-__device__ __forceinline__ double blockMin(double v, double* sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if (lane == 0) sm[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sm[lane] : DBL_MAX;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  }
-  __syncthreads();
-  return v;
-}
-__device__ __forceinline__ double blockMax(double v, double* sm) { return -blockMin(-v, sm); }
-__device__ __forceinline__ double blockSum(double v, double* sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if (lane == 0) sm[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  }
-  __syncthreads();
-  return v;
-}
+using namespace dev;
 
 //------------------------------------------------------------------------------
 // Bounds: min hinv and bounding box (for open axes).
@@ -193,30 +92,50 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 
 // Pair criterion of ConnectivityMap::computeConnectivity
 // (src/Neighbor/ConnectivityMap.cc:917-929): (Hi rij)^2 <= ext^2 or
-// (Hj rij)^2 <= ext^2, self excluded, in exact FP64 with the reference's
-// operation order.
+// (Hj rij)^2 <= ext^2, self excluded.  An FP32 test on cell-relative
+// positions settles every candidate outside a narrow band around the
+// threshold; candidates inside the band get the exact FP64 test with the
+// reference's operation order, so the neighbour sets are exact.
 template <bool FILL>
-__global__ void neighborKernel(Fields F, const uint32_t* __restrict__ cellc, long n, Grid g,
-                               const int* __restrict__ cellStart, const int* __restrict__ cellEnd,
-                               int* __restrict__ counts, const long long* __restrict__ start,
-                               uint32_t* __restrict__ nbr, double ext2) {
+__global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long n, Grid g,
+                                                      const int* __restrict__ cellStart,
+                                                      const int* __restrict__ cellEnd, int* __restrict__ counts,
+                                                      const long long* __restrict__ start, uint32_t* __restrict__ nbr,
+                                                      double ext2, float bandLo, float bandHi) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* __restrict__ X = F.f[F_X];
   const double* __restrict__ Y = F.f[F_Y];
   const double* __restrict__ Z = F.f[F_Z];
   const double* __restrict__ A = F.f[F_HINV];
-  const double xi = X[i], yi = Y[i], zi = Z[i], ai = A[i];
+  const uint32_t cc = P.cell[i];
+  int ci[3];
+  unpackCell(cc, ci);
+  const float4 pi = P.posh[i];
+  const float cellx = (float)g.cell[0], celly = (float)g.cell[1], cellz = (float)g.cell[2];
+  const uint32_t mm = mirrorMask(g, ci);
   int cnt = 0;
   long long w = FILL ? start[i] : 0;
-  forEachCandidate(g, cellc[i], cellStart, cellEnd, [&](int j, int code) {
-    if (j == (int)i && code == 0) return;
-    double xj = X[j], yj = Y[j], zj = Z[j];
-    imagePos(g, code, xj, yj, zj);
-    const double rx = __dsub_rn(xi, xj), ry = __dsub_rn(yi, yj), rz = __dsub_rn(zi, zj);
-    const double aj = A[j];
-    if (eta2Exact(ai, rx, ry, rz) <= ext2 || eta2Exact(aj, rx, ry, rz) <= ext2) {
-      if (FILL) nbr[w++] = (uint32_t)j | ((uint32_t)code << kIndexBits);
+  forEachCandidate(g, cc, cellStart, cellEnd, [&](int j, int dcode) {
+    if (j == (int)i && dcode == 0) return;
+    const float4 pj = P.posh[j];
+    float rx, ry, rz;
+    relSep(pi, pj, dcode, mm, cellx, celly, cellz, rx, ry, rz);
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    const float e2i = pi.w * pi.w * r2, e2j = pj.w * pj.w * r2;
+    const float e2 = fminf(e2i, e2j);
+    bool inside;
+    if (e2 < bandLo) inside = true;
+    else if (e2 > bandHi) inside = false;
+    else {
+      const double xi = X[i], yi = Y[i], zi = Z[i];
+      double xj = X[j], yj = Y[j], zj = Z[j];
+      imagePos(g, imageCode(g, ci, dcode), xj, yj, zj);
+      const double qx = __dsub_rn(xi, xj), qy = __dsub_rn(yi, yj), qz = __dsub_rn(zi, zj);
+      inside = eta2Exact(A[i], qx, qy, qz) <= ext2 || eta2Exact(A[j], qx, qy, qz) <= ext2;
+    }
+    if (inside) {
+      if (FILL) nbr[w++] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
       else ++cnt;
     }
   });
@@ -236,6 +155,8 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int hc[3];
+  unpackCell(nl.cell[i], hc);
   const double* __restrict__ X = F.f[F_X];
   const double* __restrict__ Y = F.f[F_Y];
   const double* __restrict__ Z = F.f[F_Z];
@@ -249,7 +170,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
   const long long e = nl.start[i + 1];
   for (long long k = nl.start[i]; k < e; ++k) {
     const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j];
     imagePos(g, code, xj, yj, zj);
     const double aj = A[j];
@@ -278,6 +199,8 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int hc[3];
+  unpackCell(nl.cell[i], hc);
   const double* __restrict__ X = F.f[F_X];
   const double* __restrict__ Y = F.f[F_Y];
   const double* __restrict__ Z = F.f[F_Z];
@@ -287,7 +210,7 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
   const long long s = nl.start[i], e = nl.start[i + 1];
   for (long long k = s; k < e; ++k) {
     const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j];
     imagePos(g, code, xj, yj, zj);
     const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
@@ -310,105 +233,6 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
 // MonaghanGingoldViscosity::QPiij (MonaghanGingoldViscosity.cc:41-101) and the
 // SPHSmoothingScale moments + IdealH (SPHSmoothingScale.cc:154-272), FP64.
 //------------------------------------------------------------------------------
-__constant__ NodeListParams cLists[kMaxNodeLists];
-
-__device__ __forceinline__ double hermiteLookup(const double* __restrict__ v, const HydroParams& hp, double x) {
-  // CubicHermiteInterpolatorView::operator() (CubicHermiteInterpolatorViewInline.hh:10-36)
-  const int N = hp.hermN;
-  if (x < hp.hermXmin) return v[0] + v[N] * (x - hp.hermXmin);
-  if (x > hp.hermXmax) return v[N - 1] + v[2 * N - 1] * (x - hp.hermXmin);
-  long k = (long)(fmax(0.0, x - hp.hermXmin) / hp.hermXstep);
-  const int i0 = (int)min((long)(N - 2), k);
-  const double t = fmax(0.0, fmin(1.0, (x - hp.hermXmin - i0 * hp.hermXstep) / hp.hermXstep));
-  const double t2 = t * t, t3 = t * t2;
-  return ((2.0 * t3 - 3.0 * t2 + 1.0) * v[i0] + (-2.0 * t3 + 3.0 * t2) * v[i0 + 1] +
-          hp.hermXstep * ((t3 - 2.0 * t2 + t) * v[N + i0] + (t3 - t2) * v[N + i0 + 1]));
-}
-
-// Per-node completion shared by the FP64 and FP32 pair kernels: self terms,
-// corrected velocity gradient, continuity, XSPH, and the IdealH update.
-struct NodeAcc {
-  double rhoSum, norm, dvx, dvy, dvz, deps, gx, gy, gz, maxQ, effQ, xw, xdx, xdy, xdz, m0, m1x, m1y, m1z;
-  double D[9], M[9];
-};
-
-__device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const NodeAcc& a, double mi, double rhoi,
-                                             double vxi, double vyi, double vzi, double ai, int numNb,
-                                             const HydroParams& hp, const double* __restrict__ herm) {
-  const double Hdeti = (ai * ai) * ai;
-  F.f[F_RHOSUM][i] = a.rhoSum + mi * hp.W0 * Hdeti;
-  F.f[F_NORM][i] = a.norm + mi / rhoi * hp.W0 * Hdeti;
-  double D[9], Mm[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) { D[k] = a.D[k]; Mm[k] = a.M[k]; }
-  const double detM = (Mm[0] * Mm[4] * Mm[8] + Mm[1] * Mm[5] * Mm[6] + Mm[2] * Mm[3] * Mm[7] -
-                       Mm[0] * Mm[5] * Mm[7] - Mm[1] * Mm[3] * Mm[8] - Mm[2] * Mm[4] * Mm[6]);
-  if (hp.correctVelGrad && fabs(detM) > 1.0e-10 && numNb > 8) {
-    // GeomTensor<3>::Inverse (src/Geometry/GeomTensorInline.hh:1885-1890)
-    const double inv[9] = {(Mm[4] * Mm[8] - Mm[5] * Mm[7]) / detM, (Mm[2] * Mm[7] - Mm[1] * Mm[8]) / detM,
-                           (Mm[1] * Mm[5] - Mm[2] * Mm[4]) / detM, (Mm[5] * Mm[6] - Mm[3] * Mm[8]) / detM,
-                           (Mm[0] * Mm[8] - Mm[2] * Mm[6]) / detM, (Mm[2] * Mm[3] - Mm[0] * Mm[5]) / detM,
-                           (Mm[3] * Mm[7] - Mm[4] * Mm[6]) / detM, (Mm[1] * Mm[6] - Mm[0] * Mm[7]) / detM,
-                           (Mm[0] * Mm[4] - Mm[1] * Mm[3]) / detM};
-    double R[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        R[3 * r + c] = D[3 * r] * inv[c] + D[3 * r + 1] * inv[3 + c] + D[3 * r + 2] * inv[6 + c];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) { D[k] = R[k]; Mm[k] = inv[k]; }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 9; ++k) D[k] /= rhoi;
-  }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) { F.f[F_DVDX_XX + k][i] = D[k]; F.f[F_M_XX + k][i] = Mm[k]; }
-  F.f[F_GRADRHO_X][i] = a.gx / rhoi;
-  F.f[F_GRADRHO_Y][i] = a.gy / rhoi;
-  F.f[F_GRADRHO_Z][i] = a.gz / rhoi;
-  const double trace = D[0] + D[4] + D[8];
-  F.f[F_DRHODT][i] = -rhoi * trace;
-  F.f[F_DVDT_X][i] = a.dvx;
-  F.f[F_DVDT_Y][i] = a.dvy;
-  F.f[F_DVDT_Z][i] = a.dvz;
-  F.f[F_DEPSDT][i] = a.deps;
-  F.f[F_MAXQ][i] = a.maxQ;
-  F.f[F_EFFQ][i] = a.effQ;
-  double xw = a.xw;
-  if (hp.xsph) {
-    xw += Hdeti * mi / rhoi * hp.W0;
-    const double ws = fmax(kTiny30, xw);
-    F.f[F_DXDT_X][i] = vxi + a.xdx / ws;
-    F.f[F_DXDT_Y][i] = vyi + a.xdy / ws;
-    F.f[F_DXDT_Z][i] = vzi + a.xdz / ws;
-  } else {
-    F.f[F_DXDT_X][i] = vxi;
-    F.f[F_DXDT_Y][i] = vyi;
-    F.f[F_DXDT_Z][i] = vzi;
-  }
-  F.f[F_XSPHW][i] = xw;
-  F.f[F_XSPHDV_X][i] = a.xdx;
-  F.f[F_XSPHDV_Y][i] = a.xdy;
-  F.f[F_XSPHDV_Z][i] = a.xdz;
-  // SPHSmoothingScale finalize (SPHSmoothingScale.cc:235-270)
-  const NodeListParams L = cLists[li];
-  const double m0s = fmax(0.0, a.m0);
-  const double m0 = m0s < 0.0 ? -pow(-m0s, 0.3333333333333333) : pow(m0s, 0.3333333333333333);
-  F.f[F_M0][i] = m0;
-  F.f[F_M1_X][i] = a.m1x;
-  F.f[F_M1_Y][i] = a.m1y;
-  F.f[F_M1_Z][i] = a.m1z;
-  F.f[F_DHDT][i] = ((-ai) / 3.0) * trace;
-  const bool iso = fabs(m0 - 0.0) <= 1.0e-15 * fmax(1.0, fabs(m0));
-  const double cur = iso ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(herm, hp, m0));
-  const double s = fmin(4.0, fmax(0.25, L.nPerh / (cur + 1.0e-30)));
-  const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
-  const double hi0 = 1.0 / ai;
-  const double hi1 = fmin(L.hmax, fmax(L.hmin, hi0 * (1.0 - aa + aa * s)));
-  F.f[F_HIDEAL][i] = 1.0 / hi1;
-}
-
 template <bool XSPH, bool COMPAT>
 __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __restrict__ list, long n, Grid g,
                                                       NeighborLists nl, TableDev t, HydroParams hp,
@@ -419,6 +243,8 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int hc[3];
+  unpackCell(nl.cell[i], hc);
   const double* __restrict__ X = F.f[F_X];
   const double* __restrict__ Y = F.f[F_Y];
   const double* __restrict__ Z = F.f[F_Z];
@@ -452,7 +278,7 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
   const long long s = nl.start[i], e = nl.start[i + 1];
   for (long long k = s; k < e; ++k) {
     const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j], vxj = VX[j], vyj = VY[j], vzj = VZ[j];
     imagePos(g, code, xj, yj, zj);
     imageVec(g, code, vxj, vyj, vzj);
@@ -569,6 +395,8 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
   double best = DBL_MAX;
   int reason = -1;
   if (i < n) {
+    int hc[3];
+    unpackCell(nl.cell[i], hc);
     const NodeListParams L = cLists[list[i]];
     const double ai = F.f[F_HINV][i];
     const double nodeScalei = 1.0 / ai / L.nPerh;
@@ -595,7 +423,7 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
     const long long e = nl.start[i + 1];
     for (long long k = nl.start[i]; k < e; ++k) {
       const uint32_t ent = nl.nbr[k];
-      const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+      const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
       double vxj = F.f[F_VX][j], vyj = F.f[F_VY][j], vzj = F.f[F_VZ][j];
       imageVec(g, code, vxj, vyj, vzj);
       const double nsj = 1.0 / F.f[F_HINV][j] / maxNperh;
@@ -647,6 +475,8 @@ __global__ void __launch_bounds__(128) energyKernel(Fields F, long n, Grid g, Ne
                                                     double dt) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int hc[3];
+  unpackCell(nl.cell[i], hc);
   const double hdt = 0.5 * dt;
   const double* __restrict__ VX = F.f[F_VX];
   const double* __restrict__ VY = F.f[F_VY];
@@ -661,7 +491,7 @@ __global__ void __launch_bounds__(128) energyKernel(Fields F, long n, Grid g, Ne
   const long long e = nl.start[i + 1];
   for (long long k = nl.start[i]; k < e; ++k) {
     const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), code = (int)(ent >> kIndexBits);
+    const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double vxj = VX[j], vyj = VY[j], vzj = VZ[j], axj = AX[j], ayj = AY[j], azj = AZ[j];
     imageVec(g, code, vxj, vyj, vzj);
     imageVec(g, code, axj, ayj, azj);
@@ -815,6 +645,37 @@ __global__ void checkStateKernel(Fields F, long n, int* __restrict__ flag) {
   if (bad) atomicExch(flag, 1);
 }
 
+// Caller-order transfers: stage[orig[k] * stride + c] <-> F[first + c][k].
+__global__ void gatherOutKernel(Fields F, const int* __restrict__ orig, double* __restrict__ stage, int first,
+                                int ncomp, int stride, long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long o = (long)orig[k] * stride;
+  for (int c = 0; c < ncomp; ++c) stage[o + c] = F.f[first + c][k];
+}
+__global__ void scatterInKernel(Fields F, const int* __restrict__ orig, const double* __restrict__ stage, int first,
+                                int ncomp, int stride, long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long o = (long)orig[k] * stride;
+  for (int c = 0; c < ncomp; ++c) F.f[first + c][k] = stage[o + c];
+}
+// H as SymTensor (xx, xy, xz, yy, yz, zz) <-> isotropic hinv.
+__global__ void gatherOutHKernel(Fields F, const int* __restrict__ orig, double* __restrict__ stage, int field,
+                                 long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double* o = stage + (long)orig[k] * 6;
+  const double a = F.f[field][k];
+  o[0] = a; o[1] = 0.0; o[2] = 0.0; o[3] = a; o[4] = 0.0; o[5] = a;
+}
+__global__ void countsOutKernel(const long long* __restrict__ start, const int* __restrict__ orig,
+                                double* __restrict__ stage, long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  stage[orig[k]] = (double)(start[k + 1] - start[k]);
+}
+
 inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 }  // namespace
@@ -846,16 +707,27 @@ void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* c
   cellRangeKernel<<<gridFor(n, 256), 256, 0, s>>>(sortedKeys, n, cellStart, cellEnd);
   lc->add(1);
 }
-void launchNeighborCount(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
-                         const int* cellEnd, int* counts, double ext2, cudaStream_t s, LaunchCounter* lc) {
-  neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, cellc, n, g, cellStart, cellEnd, counts, nullptr, nullptr,
-                                                         ext2);
+// Band of the FP32 pre-filter on (H r)^2 around ext^2 = 4: wide enough for
+// the FP32 rounding of cell-relative separations (<= ~4e-7 of a cell).
+static void neighborBand(const Grid& g, double ext2, float& lo, float& hi) {
+  (void)g;
+  lo = (float)(ext2 * (1.0 - 2.0e-3));
+  hi = (float)(ext2 * (1.0 + 2.0e-3));
+}
+void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                         int* counts, double ext2, cudaStream_t s, LaunchCounter* lc) {
+  float lo, hi;
+  neighborBand(g, ext2, lo, hi);
+  neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, nullptr, ext2,
+                                                         lo, hi);
   lc->add(1);
 }
-void launchNeighborFill(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
-                        const int* cellEnd, const long long* start, uint32_t* nbr, double ext2, cudaStream_t s,
-                        LaunchCounter* lc) {
-  neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, cellc, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2);
+void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                        const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc) {
+  float lo, hi;
+  neighborBand(g, ext2, lo, hi);
+  neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2, lo,
+                                                        hi);
   lc->add(1);
 }
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -935,6 +807,26 @@ void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nS
 }
 void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc) {
   checkStateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, dFlag);
+  lc->add(1);
+}
+
+void launchGatherOut(Fields F, const int* orig, double* stage, int first, int ncomp, int stride, long n,
+                     cudaStream_t s, LaunchCounter* lc) {
+  gatherOutKernel<<<gridFor(n, 256), 256, 0, s>>>(F, orig, stage, first, ncomp, stride, n);
+  lc->add(1);
+}
+void launchScatterIn(Fields F, const int* orig, const double* stage, int first, int ncomp, int stride, long n,
+                     cudaStream_t s, LaunchCounter* lc) {
+  scatterInKernel<<<gridFor(n, 256), 256, 0, s>>>(F, orig, stage, first, ncomp, stride, n);
+  lc->add(1);
+}
+void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long n, cudaStream_t s, LaunchCounter* lc) {
+  gatherOutHKernel<<<gridFor(n, 256), 256, 0, s>>>(F, orig, stage, field, n);
+  lc->add(1);
+}
+void launchCountsOut(const long long* start, const int* orig, double* stage, long n, cudaStream_t s,
+                     LaunchCounter* lc) {
+  countsOutKernel<<<gridFor(n, 256), 256, 0, s>>>(start, orig, stage, n);
   lc->add(1);
 }
 

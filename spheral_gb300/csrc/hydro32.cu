@@ -1,0 +1,425 @@
+// Mixed-precision sweeps of libsphgpu (sm_103a): the SPH pair loop, density
+// sum, grad-h correction and pairwise dt limit in FP32 on cell-relative
+// positions.  Time integration, the compatible-energy update, the per-node
+// finalisation and all conserved tallies stay in FP64.
+//
+// Precision design.
+//  * Positions are stored relative to the origin of each node's cell
+//    (|x_rel| < one cell), so a pair separation is
+//    (x_i,rel - x_j,rel) - d cell with d in {-1, 0, 1}: it keeps FP32 digits
+//    relative to h instead of relative to the box size.
+//  * The pair force Delta_ij is evaluated in a symmetric order,
+//    (Prho_i gradW_i + Qacc_i) + (Prho_j gradW_j + Qacc_j), so the two ordered
+//    slots (i, j) and (j, i) hold bitwise opposite values: momentum and the
+//    compatible-energy split stay exactly antisymmetric despite FP32.
+//  * The acceleration and energy-rate sums are Kahan compensated and leave
+//    the kernel as the FP64 value s - c of the compensated pair (s, c).
+#include "device.cuh"
+
+namespace sph {
+namespace {
+using namespace dev;
+
+__device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+__device__ __forceinline__ double kahanValue(float s, float c) { return (double)s - (double)c; }
+
+__device__ __forceinline__ void mirrorVel(uint32_t mir, float& vx, float& vy, float& vz) {
+  if (mir) {
+    if (mir & 3u) vx = -vx;
+    if (mir & 12u) vy = -vy;
+    if (mir & 48u) vz = -vz;
+  }
+}
+
+__global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[3];
+  unpackCell(P.cell[i], c);
+  const double ox = g.lo[0] + c[0] * g.cell[0];
+  const double oy = g.lo[1] + c[1] * g.cell[1];
+  const double oz = g.lo[2] + c[2] * g.cell[2];
+  P.posh[i] = make_float4((float)(F.f[F_X][i] - ox), (float)(F.f[F_Y][i] - oy), (float)(F.f[F_Z][i] - oz),
+                          (float)F.f[F_HINV][i]);
+  P.velm[i] = make_float4((float)F.f[F_VX][i], (float)F.f[F_VY][i], (float)F.f[F_VZ][i], (float)F.f[F_MASS][i]);
+  const double om = F.f[F_OMEGA][i];
+  P.thermo[i] = make_float4((float)F.f[F_RHO][i], (float)F.f[F_P][i], (float)F.f[F_CS][i],
+                            (float)(om / (om * om + 1.0e-30)));
+}
+
+__device__ __forceinline__ void lookup32(const float* __restrict__ tw, const float* __restrict__ tg, int N1,
+                                         float invStep, float eta, float extent, float& w, float& gr) {
+  if (eta < extent) {
+    const int k = min(N1, (int)(fmaxf(0.0f, eta) * invStep));
+    const int i0 = 3 * k;
+    w = __fmaf_rn(__fmaf_rn(tw[i0 + 2], eta, tw[i0 + 1]), eta, tw[i0]);
+    gr = __fmaf_rn(__fmaf_rn(tg[i0 + 2], eta, tg[i0 + 1]), eta, tg[i0]);
+  } else {
+    w = 0.0f;
+    gr = 0.0f;
+  }
+}
+
+//------------------------------------------------------------------------------
+// SPH pair loop (src/SPH/SPH.cc:294-470) + SPHSmoothingScale moments, FP32.
+//------------------------------------------------------------------------------
+template <bool XSPH, bool COMPAT>
+__global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
+                                                      Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                                                      float* __restrict__ pacc) {
+  __shared__ float tw[kMaxTable];
+  __shared__ float tg[kMaxTable];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { tw[k] = t.w32[k]; tg[k] = t.g32[k]; }
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ci[3];
+  unpackCell(P.cell[i], ci);
+  const uint32_t mm = mirrorMask(g, ci);
+  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float4 pi = P.posh[i], vi = P.velm[i], thi = P.thermo[i];
+  const int li = list[i];
+  const float ai = pi.w, mi = vi.w, rhoi = thi.x, Pi = thi.y, csi = thi.z, sOi = thi.w;
+  const float Hdeti = ai * ai * ai;
+  const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
+  const int N1 = hp.tableN1;
+  const float Cl = (float)hp.Cl, Cq = (float)hp.Cq, eps2 = (float)hp.eps2;
+  const float epsT = (float)hp.epsTensile, WnPerh = (float)hp.WnPerh;
+  const float tiny = 1.0e-30f;
+  const float mrhoi = mi / rhoi;
+  const float Prhoi0 = sOi * Pi / (rhoi * rhoi);
+
+  float rhoSum = 0.f, norm = 0.f, maxQ = 0.f, effQ = 0.f, xw = 0.f, xdx = 0.f, xdy = 0.f, xdz = 0.f;
+  float sdx = 0.f, cdx = 0.f, sdy = 0.f, cdy = 0.f, sdz = 0.f, cdz = 0.f, se = 0.f, ce = 0.f;
+  float gx = 0.f, gy = 0.f, gz = 0.f, m0 = 0.f, m1x = 0.f, m1y = 0.f, m1z = 0.f;
+  float D[9], M[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { D[k] = 0.f; M[k] = 0.f; }
+
+  const long long s = nl.start[i], e = nl.start[i + 1];
+  for (long long k = s; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+    const float4 pj = P.posh[j], vj4 = P.velm[j], thj = P.thermo[j];
+    float rx, ry, rz;
+    relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
+    float vxj = vj4.x, vyj = vj4.y, vzj = vj4.z;
+    mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
+    const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z, sOj = thj.w;
+    const int lj = list[j];
+    const float Hdetj = aj * aj * aj;
+
+    const float eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
+    const float ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
+    // explicit fused forms: node j evaluates this pair with bitwise the same arithmetic
+    const float e2i = __fmaf_rn(eiz, eiz, __fmaf_rn(eiy, eiy, __fmul_rn(eix, eix)));
+    const float e2j = __fmaf_rn(ejz, ejz, __fmaf_rn(ejy, ejy, __fmul_rn(ejx, ejx)));
+    const float etai = sqrtf(e2i), etaj = sqrtf(e2j);
+    float Wi, gi, Wj, gj;
+    lookup32(tw, tg, N1, invStep, etai, extent, Wi, gi);
+    lookup32(tw, tg, N1, invStep, etaj, extent, Wj, gj);
+    const float WSPHi = fabsf(gi);
+    Wi *= Hdeti;
+    Wj *= Hdetj;
+    // gradW = gW H eta/|eta| = (Hdet g a / |eta|) eta
+    const float fi = __fmul_rn(__fmul_rn(Hdeti, gi), ai) / fmaxf(tiny, etai);
+    const float fj = __fmul_rn(__fmul_rn(Hdetj, gj), aj) / fmaxf(tiny, etaj);
+    const float gwix = fi * eix, gwiy = fi * eiy, gwiz = fi * eiz;
+    const float gwjx = fj * ejx, gwjy = fj * ejy, gwjz = fj * ejz;
+
+    if (lj == li) {
+      rhoSum += mj * Wi;
+      norm += mrhoi * Wi;
+    }
+    const float vx = vi.x - vxj, vy = vi.y - vyj, vz = vi.z - vzj;
+    const float mui = __fmaf_rn(vz, eiz, __fmaf_rn(vy, eiy, __fmul_rn(vx, eix))) / __fadd_rn(e2i, eps2);
+    const float muj = __fmaf_rn(vz, ejz, __fmaf_rn(vy, ejy, __fmul_rn(vx, ejx))) / __fadd_rn(e2j, eps2);
+    float li_ = hp.linearInExpansion ? mui : fminf(0.f, mui);
+    float lj_ = hp.linearInExpansion ? muj : fminf(0.f, muj);
+    float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : fminf(0.f, mui) * fminf(0.f, mui);
+    float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : fminf(0.f, muj) * fminf(0.f, muj);
+    const float ei = __fmaf_rn(Cq, qi_, __fmul_rn(__fmul_rn(-Cl, csi), li_));
+    const float ej = __fmaf_rn(Cq, qj_, __fmul_rn(__fmul_rn(-Cl, csj), lj_));
+    const float qai = __fmul_rn(0.5f, ei / rhoi), qaj = __fmul_rn(0.5f, ej / rhoj);
+    const float Qi = rhoi * ei;
+    maxQ = fmaxf(maxQ, Qi);
+    effQ += mj * Qi * Wi / rhoj;
+    float Prhoi = Prhoi0, Prhoj = sOj * Pj / (rhoj * rhoj);
+    if (epsT != 0.f) {
+      const float ri = Wi / (Hdeti * WnPerh), rj = Wj / (Hdetj * WnPerh);
+      Prhoi = sOi * (Pi + epsT * (ri * ri * ri * ri) * (Pi < 0.f ? -Pi : 0.f)) / (rhoi * rhoi);
+      Prhoj = sOj * (Pj + epsT * (rj * rj * rj * rj) * (Pj < 0.f ? -Pj : 0.f)) / (rhoj * rhoj);
+    }
+    // symmetric-order pair force: (Prho_i + Q_i/2) gradW_i + (Prho_j + Q_j/2) gradW_j
+    const float ci_ = __fadd_rn(Prhoi, qai), cj_ = __fadd_rn(Prhoj, qaj);
+    const float ddx = __fadd_rn(__fmul_rn(ci_, gwix), __fmul_rn(cj_, gwjx));
+    const float ddy = __fadd_rn(__fmul_rn(ci_, gwiy), __fmul_rn(cj_, gwjy));
+    const float ddz = __fadd_rn(__fmul_rn(ci_, gwiz), __fmul_rn(cj_, gwjz));
+    const float pax = __fmul_rn(-mj, ddx), pay = __fmul_rn(-mj, ddy), paz = __fmul_rn(-mj, ddz);
+    kahanAdd(sdx, cdx, pax);
+    kahanAdd(sdy, cdy, pay);
+    kahanAdd(sdz, cdz, paz);
+    if (COMPAT) {
+      pacc[3 * k] = pax;
+      pacc[3 * k + 1] = pay;
+      pacc[3 * k + 2] = paz;
+    }
+    const float vg = vx * gwix + vy * gwiy + vz * gwiz;
+    kahanAdd(se, ce, mj * (Prhoi * vg + qai * vg));
+    const float mvx = mj * vx, mvy = mj * vy, mvz = mj * vz;
+    D[0] -= mvx * gwix; D[1] -= mvx * gwiy; D[2] -= mvx * gwiz;
+    D[3] -= mvy * gwix; D[4] -= mvy * gwiy; D[5] -= mvy * gwiz;
+    D[6] -= mvz * gwix; D[7] -= mvz * gwiy; D[8] -= mvz * gwiz;
+    if (XSPH) {
+      const float wx = 0.5f * (mrhoi * Wi + mj / rhoj * Wj);
+      xw += wx;
+      xdx -= wx * vx; xdy -= wx * vy; xdz -= wx * vz;
+    }
+    const float gr = mj * (rhoj - rhoi);
+    gx += gr * gwix; gy += gr * gwiy; gz += gr * gwiz;
+    const float mrx = mj * rx, mry = mj * ry, mrz = mj * rz;
+    M[0] -= mrx * gwix; M[1] -= mrx * gwiy; M[2] -= mrx * gwiz;
+    M[3] -= mry * gwix; M[4] -= mry * gwiy; M[5] -= mry * gwiz;
+    M[6] -= mrz * gwix; M[7] -= mrz * gwiy; M[8] -= mrz * gwiz;
+    const float fw = (lj != li) ? mj * rhoi / (mi * rhoj) : 1.0f;
+    const float fwW = fw * WSPHi;
+    m0 += fwW;
+    m1x -= fwW * eix; m1y -= fwW * eiy; m1z -= fwW * eiz;
+  }
+  NodeAcc a;
+  a.rhoSum = rhoSum; a.norm = norm;
+  a.dvx = kahanValue(sdx, cdx); a.dvy = kahanValue(sdy, cdy); a.dvz = kahanValue(sdz, cdz);
+  a.deps = kahanValue(se, ce);
+  a.gx = gx; a.gy = gy; a.gz = gz; a.maxQ = maxQ; a.effQ = effQ;
+  a.xw = xw; a.xdx = xdx; a.xdy = xdy; a.xdz = xdz;
+  a.m0 = m0; a.m1x = m1x; a.m1y = m1y; a.m1z = m1z;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { a.D[k] = D[k]; a.M[k] = M[k]; }
+  finalizeNode(F, i, li, a, F.f[F_MASS][i], F.f[F_RHO][i], F.f[F_VX][i], F.f[F_VY][i], F.f[F_VZ][i],
+               F.f[F_HINV][i], (int)(e - s), hp, t.herm);
+}
+
+//------------------------------------------------------------------------------
+// Density sum, FP32 (computeSPHSumMassDensity.cc:15-87, gathered).
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n,
+                                                          Grid g, NeighborLists nl, TableDev t, HydroParams hp) {
+  __shared__ float tw[kMaxTable];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) tw[k] = t.w32[k];
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ci[3];
+  unpackCell(P.cell[i], ci);
+  const uint32_t mm = mirrorMask(g, ci);
+  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float4 pi = P.posh[i];
+  const float mi = P.velm[i].w;
+  const int li = list[i];
+  const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
+  const int N1 = hp.tableN1;
+  float s = 0.f, c = 0.f;
+  const long long e = nl.start[i + 1];
+  for (long long k = nl.start[i]; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+    const float4 pj = P.posh[j];
+    float rx, ry, rz;
+    relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
+    const float aj = pj.w;
+    const float eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+    if (eta < extent) {
+      const int i0 = 3 * min(N1, (int)(eta * invStep));
+      const float w = (aj * aj * aj) * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
+      kahanAdd(s, c, (list[j] == li ? P.velm[j].w : mi) * w);
+    }
+  }
+  const double a = F.f[F_HINV][i];
+  const double self = F.f[F_MASS][i] * (((a * a) * a) * hp.W0);
+  const double rho = self + kahanValue(s, c);
+  F.f[F_RHO][i] = rho;
+  P.thermo[i].x = (float)rho;
+}
+
+//------------------------------------------------------------------------------
+// Grad-h correction, FP32 sums (computeSPHOmegaGradhCorrection.cc:15-116).
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl,
+                                                     TableDev t, HydroParams hp) {
+  __shared__ float tw[kMaxTable];
+  __shared__ float tg[kMaxTable];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { tw[k] = t.w32[k]; tg[k] = t.g32[k]; }
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ci[3];
+  unpackCell(P.cell[i], ci);
+  const uint32_t mm = mirrorMask(g, ci);
+  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float4 pi = P.posh[i];
+  const float ai = pi.w;
+  const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
+  const int N1 = hp.tableN1;
+  float ws = 0.f, wc = 0.f, gs = 0.f, gc = 0.f;
+  const long long s = nl.start[i], e = nl.start[i + 1];
+  for (long long k = s; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+    float rx, ry, rz;
+    relSep(pi, P.posh[j], dcode, mm, cx, cy, cz, rx, ry, rz);
+    const float eta = ai * sqrtf(rx * rx + ry * ry + rz * rz);
+    float w, gr;
+    lookup32(tw, tg, N1, invStep, eta, extent, w, gr);
+    kahanAdd(ws, wc, w);
+    kahanAdd(gs, gc, eta * gr);
+  }
+  const double a = F.f[F_HINV][i];
+  const double Hdet = (a * a) * a;
+  double omega;
+  if (e == s) omega = 1.0;
+  else omega = fmax(1.0e-30, -(Hdet * kahanValue(gs, gc)) / (3.0 * (Hdet * kahanValue(ws, wc) + Hdet * hp.W0)));
+  F.f[F_OMEGA][i] = omega;
+  P.thermo[i].w = (float)(omega / (omega * omega + 1.0e-30));
+}
+
+//------------------------------------------------------------------------------
+// GenericHydro::dt with the pairwise velocity limit in FP32.
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n, Grid g,
+                                                  NeighborLists nl, HydroParams hp, double maxNperh,
+                                                  double* __restrict__ part) {
+  __shared__ double sv[128];
+  __shared__ int sr[128];
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const double tiny = DBL_EPSILON;
+  double best = DBL_MAX;
+  int reason = -1;
+  if (i < n) {
+    int ci[3];
+    unpackCell(P.cell[i], ci);
+    const uint32_t mm = mirrorMask(g, ci);
+    const NodeListParams L = cLists[list[i]];
+    const double ai = F.f[F_HINV][i];
+    const double nodeScalei = 1.0 / ai / L.nPerh;
+    const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
+    const double rhoi = F.f[F_RHO][i];
+    const double csDt = nodeScalei / (F.f[F_CS][i] + tiny);
+    if (csDt < best) { best = csDt; reason = 0; }
+    const double csqDt = nodeScalei / (sqrt(F.f[F_MAXQ][i] / rhoi) + tiny);
+    if (csqDt < best) { best = csqDt; reason = 1; }
+    const double divvDt = 1.0 / (fabs(F.f[F_DVDX_XX][i] + F.f[F_DVDX_YY][i] + F.f[F_DVDX_ZZ][i]) + tiny);
+    if (divvDt < best) { best = divvDt; reason = 2; }
+    const double vmag = sqrt(vxi * vxi + vyi * vyi + vzi * vzi);
+    const double ax = F.f[F_DVDT_X][i], ay = F.f[F_DVDT_Y][i], az = F.f[F_DVDT_Z][i];
+    const double dtAcc = 0.1 * fmax(nodeScalei / (vmag + tiny), vmag / (sqrt(ax * ax + ay * ay + az * az) + tiny));
+    if (dtAcc < best) { best = dtAcc; reason = 3; }
+    if (hp.useVelMagDt) {
+      const double velDt = nodeScalei / (vmag + 1.0e-10);
+      if (velDt < best) { best = velDt; reason = 4; }
+    }
+    const float4 vi = P.velm[i];
+    const float hi = 1.0f / P.posh[i].w;
+    float bestPair = 3.0e38f;
+    const long long e = nl.start[i + 1];
+    for (long long k = nl.start[i]; k < e; ++k) {
+      const uint32_t ent = nl.nbr[k];
+      const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+      const float4 vj = P.velm[j];
+      float vxj = vj.x, vyj = vj.y, vzj = vj.z;
+      mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
+      const float dx = vi.x - vxj, dy = vi.y - vyj, dz = vi.z - vzj;
+      const float hmin = fminf(hi, 1.0f / P.posh[j].w);
+      const float dtv = hmin / fmaxf(1.0e-30f, sqrtf(dx * dx + dy * dy + dz * dz));
+      bestPair = fminf(bestPair, dtv);
+    }
+    const double pairDt = (double)bestPair / maxNperh;
+    if (pairDt < best) { best = pairDt; reason = 5; }
+  }
+  sv[threadIdx.x] = best;
+  sr[threadIdx.x] = reason;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && sv[threadIdx.x + o] < sv[threadIdx.x]) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      sr[threadIdx.x] = sr[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = sv[0]; part[2 * blockIdx.x + 1] = (double)sr[0]; }
+}
+__global__ void dtFinalKernel32(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sv[256];
+  __shared__ double sr[256];
+  double best = DBL_MAX, reason = -1.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (part[2 * b] < best) { best = part[2 * b]; reason = part[2 * b + 1]; }
+  sv[threadIdx.x] = best;
+  sr[threadIdx.x] = reason;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && sv[threadIdx.x + o] < sv[threadIdx.x]) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      sr[threadIdx.x] = sr[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = sv[0]; out[1] = sr[0]; }
+}
+
+inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, LaunchCounter* lc) {
+  prepareKernel<<<gridFor(n, 256), 256, 0, s>>>(F, F32, n, g);
+  lc->add(1);
+}
+
+void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                    HydroParams hp, const NodeListParams* lists, float* pacc, int blockSize, cudaStream_t s,
+                    LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  (void)blockSize;
+  const int b = 128;
+  if (hp.xsph) {
+    if (hp.compatible) pairKernelFP32<true, true><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+    else pairKernelFP32<true, false><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+  } else {
+    if (hp.compatible) pairKernelFP32<false, true><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+    else pairKernelFP32<false, false><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+  }
+  lc->add(1);
+}
+
+void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                          HydroParams hp, cudaStream_t s, LaunchCounter* lc) {
+  sumDensityKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, F32, list, n, g, nl, t, hp);
+  lc->add(1);
+}
+
+void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                     cudaStream_t s, LaunchCounter* lc) {
+  gradhKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  lc->add(1);
+}
+
+void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
+                  const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+                  cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  (void)nScratch;
+  const int nb = (int)gridFor(n, 128);
+  dtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
+  dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
+  lc->add(2);
+}
+
+}  // namespace sph

@@ -16,7 +16,8 @@ struct TableDev {
 
 struct NeighborLists {
   const long long* start;   // n+1 offsets
-  const uint32_t* nbr;      // entries: index | code << 26
+  const uint32_t* nbr;      // entries: index | cell-offset code << 26
+  const uint32_t* cell;     // home cell of every node (packed, 10 bits per axis)
 };
 
 // Reductions ------------------------------------------------------------------
@@ -32,11 +33,10 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
                    cudaStream_t s, LaunchCounter* lc);
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
-void launchNeighborCount(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
-                         const int* cellEnd, int* counts, double ext2, cudaStream_t s, LaunchCounter* lc);
-void launchNeighborFill(const Fields& F, const uint32_t* cellc, long n, Grid g, const int* cellStart,
-                        const int* cellEnd, const long long* start, uint32_t* nbr, double ext2, cudaStream_t s,
-                        LaunchCounter* lc);
+void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                         int* counts, double ext2, cudaStream_t s, LaunchCounter* lc);
+void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                        const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -49,6 +49,13 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
                     HydroParams hp, const NodeListParams* lists, float* pacc, int blockSize, cudaStream_t s,
                     LaunchCounter* lc);
 void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
+void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                          HydroParams hp, cudaStream_t s, LaunchCounter* lc);
+void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                     cudaStream_t s, LaunchCounter* lc);
+void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
+                  const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+                  cudaStream_t s, LaunchCounter* lc);
 // dt: writes per-block (value, reason) pairs then a final min into dOut[0], dOut[1] (reason as double)
 void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
               const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
@@ -66,6 +73,14 @@ void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
 // out[0..7] conservation totals
 void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
                         LaunchCounter* lc);
+// caller-order transfers through a device staging buffer (stride doubles per node)
+void launchGatherOut(Fields F, const int* orig, double* stage, int first, int ncomp, int stride, long n,
+                     cudaStream_t s, LaunchCounter* lc);
+void launchScatterIn(Fields F, const int* orig, const double* stage, int first, int ncomp, int stride, long n,
+                     cudaStream_t s, LaunchCounter* lc);
+void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long n, cudaStream_t s, LaunchCounter* lc);
+void launchCountsOut(const long long* start, const int* orig, double* stage, long n, cudaStream_t s,
+                     LaunchCounter* lc);
 // check finite / positive state: writes a flag
 void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc);
 

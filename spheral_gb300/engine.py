@@ -178,6 +178,27 @@ class Engine:
         self._chk(self.L.sphgpu_profile_get(self.h, name.encode(), ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
 
+    def timer_start(self):
+        self._chk(self.L.sphgpu_timer_start(self.h))
+
+    def timer_stop(self):
+        ms = ctypes.c_double()
+        self._chk(self.L.sphgpu_timer_stop(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def neighbor_entries(self):
+        n = ctypes.c_long()
+        self._chk(self.L.sphgpu_neighbor_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def upload_state(self, pos=None, vel=None, mass=None, rho=None, eps=None, H=None):
+        ptr = lambda a: None if a is None else N.dptr(a)
+        self._chk(self.L.sphgpu_upload_state(self.h, ptr(pos), ptr(vel), ptr(mass), ptr(rho), ptr(eps), ptr(H)))
+
+    def download_state(self, pos=None, vel=None, rho=None, eps=None, H=None):
+        ptr = lambda a: None if a is None else N.dptr(a)
+        self._chk(self.L.sphgpu_download_state(self.h, ptr(pos), ptr(vel), ptr(rho), ptr(eps), ptr(H)))
+
     def launch_count(self):
         n = ctypes.c_long()
         self._chk(self.L.sphgpu_launch_count(self.h, ctypes.byref(n)))

@@ -36,7 +36,8 @@ def test_host_table_matches_oracle(native_lib, oracle_mod):
     for k in ("W", "gradW", "grad2W", "nperh", "wsum", "meta"):
         a, b = t[k], r[k]
         assert a.shape == b.shape
-        assert np.max(np.abs(a - b)) <= 1e-14 * max(1.0, np.max(np.abs(b))), k
+        # bitwise: the quadratic fit amplifies last-bit differences near the kernel edge
+        assert np.array_equal(a, b), (k, float(np.max(np.abs(a - b))))
 
 
 def test_default_config_values(native_lib):
