@@ -127,6 +127,7 @@ struct sphgpu_ctx {
   DBuf orig[2], list[2], cellc[2];
   DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
   DBuf stage;                // host <-> device staging for caller-order transfers
+  DBuf v12;                  // half-step velocities + DepsDt0 of the mixed-mode energy sweep
   int cur = 0;
   long cap = 0;
   // neighbour build
@@ -134,6 +135,8 @@ struct sphgpu_ctx {
   DBuf keys, vals, keysAlt, valsAlt, sortWs, cellStart, cellEnd, counts, nbrStart, nbr, scanWs, pacc;
   size_t cellSpace = 0;
   long long nnbr = 0;
+  int nbCap = 0;             // per-node capacity of the single-pass neighbour buffer (0: two passes)
+  DBuf nbTmp;
   bool haveNeighbors = false;
   // scratch
   DBuf scratch, small;
@@ -397,25 +400,38 @@ void buildNeighbors(sphgpu_ctx* c) {
   c->nbrStart.ensure((n + 1) * sizeof(long long));
   c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
   const double ext2 = c->hp.extent * c->hp.extent;
+  int* dMax = reinterpret_cast<int*>(c->small.as<double>() + 40);
+  CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
+  const int cap = c->nbCap;
+  if (cap > 0) c->nbTmp.ensure((size_t)n * cap * sizeof(uint32_t));
   {
     Scope sc(c->prof, "neighbor_count");
-    launchNeighborCount(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
-                        ext2, c->stream, &c->lc);
+    launchNeighborCount(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
+                        cap > 0 ? c->nbTmp.as<uint32_t>() : nullptr, cap, ext2, c->stream, &c->lc);
   }
   long long* dTot = c->nbrStart.as<long long>() + n;
   scanExclusive<int>(c->counts.as<int>(), c->nbrStart.as<long long>(), n, c->scanWs.p, dTot, c->stream, &c->lc);
   c->check();
   CUDA_OK(cudaMemcpyAsync(c->hsmall, dTot, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, dMax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
   long long total;
+  int maxCount;
   std::memcpy(&total, c->hsmall, sizeof(long long));
+  std::memcpy(&maxCount, c->hsmall + 40, sizeof(int));
   c->nnbr = total;
   c->nbr.ensure(std::max<long long>(1, total) * sizeof(uint32_t));
-  {
+  if (cap > 0 && maxCount <= cap) {
+    Scope sc(c->prof, "neighbor_compact");
+    launchNeighborCompact(c->nbTmp.as<uint32_t>(), cap, c->nbrStart.as<long long>(), n, c->nbr.as<uint32_t>(),
+                          c->stream, &c->lc);
+  } else {
     Scope sc(c->prof, "neighbor_fill");
     launchNeighborFill(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->nbrStart.as<long long>(),
                        c->nbr.as<uint32_t>(), ext2, c->stream, &c->lc);
   }
+  // capacity for the next build: the largest count with a margin, in steps of 32
+  c->nbCap = ((maxCount + maxCount / 8 + 16 + 31) / 32) * 32;
   c->check();
   c->haveNeighbors = true;
 }
@@ -545,8 +561,11 @@ double step(sphgpu_ctx* c, double maxTime) {
   }
   if (c->cfg.compatible_energy) {
     Scope sc(c->prof, "energy");
-    if (c->fp32())
-      launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), nullptr, c->pacc.as<float>(), dt, c->stream, &c->lc);
+    if (c->fp32()) {
+      c->v12.ensure(c->n * sizeof(double4));
+      launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<double4>(), dt,
+                                 c->stream, &c->lc);
+    }
     else
       launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);
   }
@@ -706,7 +725,7 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage};
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->nbTmp};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);

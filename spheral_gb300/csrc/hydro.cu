@@ -96,12 +96,16 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 // positions settles every candidate outside a narrow band around the
 // threshold; candidates inside the band get the exact FP64 test with the
 // reference's operation order, so the neighbour sets are exact.
-template <bool FILL>
+// MODE 0: count only; 1: fill the CSR lists; 2: count and write into a
+// per-node buffer of capacity cap (entries beyond cap are counted, not written).
+template <int MODE>
 __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long n, Grid g,
                                                       const int* __restrict__ cellStart,
                                                       const int* __restrict__ cellEnd, int* __restrict__ counts,
                                                       const long long* __restrict__ start, uint32_t* __restrict__ nbr,
-                                                      double ext2, float bandLo, float bandHi) {
+                                                      double ext2, float bandLo, float bandHi, int cap,
+                                                      int* __restrict__ maxCount) {
+  constexpr bool FILL = MODE == 1;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* __restrict__ X = F.f[F_X];
@@ -116,6 +120,7 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
   const uint32_t mm = mirrorMask(g, ci);
   int cnt = 0;
   long long w = FILL ? start[i] : 0;
+  uint32_t* __restrict__ tmp = MODE == 2 ? nbr + (long long)i * cap : nullptr;
   forEachCandidate(g, cc, cellStart, cellEnd, [&](int j, int dcode) {
     if (j == (int)i && dcode == 0) return;
     const float4 pj = P.posh[j];
@@ -135,11 +140,29 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
       inside = eta2Exact(A[i], qx, qy, qz) <= ext2 || eta2Exact(A[j], qx, qy, qz) <= ext2;
     }
     if (inside) {
-      if (FILL) nbr[w++] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-      else ++cnt;
+      const uint32_t entry = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
+      if (FILL) nbr[w++] = entry;
+      else {
+        if (MODE == 2 && cnt < cap) tmp[cnt] = entry;
+        ++cnt;
+      }
     }
   });
-  if (!FILL) counts[i] = cnt;
+  if (!FILL) {
+    counts[i] = cnt;
+    atomicMax(maxCount, cnt);
+  }
+}
+
+// Copy per-node capacity buffers into the CSR lists (one warp per node).
+__global__ void compactKernel(const uint32_t* __restrict__ tmp, int cap, const long long* __restrict__ start, long n,
+                              uint32_t* __restrict__ nbr) {
+  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const long long s0 = start[w], cnt = start[w + 1] - s0;
+  const uint32_t* src = tmp + w * (long long)cap;
+  for (long long c = lane; c < cnt; c += 32) nbr[s0 + c] = src[c];
 }
 
 //------------------------------------------------------------------------------
@@ -715,19 +738,30 @@ static void neighborBand(const Grid& g, double ext2, float& lo, float& hi) {
   hi = (float)(ext2 * (1.0 + 2.0e-3));
 }
 void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                         int* counts, double ext2, cudaStream_t s, LaunchCounter* lc) {
+                         int* counts, int* maxCount, uint32_t* tmp, int cap, double ext2, cudaStream_t s,
+                         LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
-  neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, nullptr, ext2,
-                                                         lo, hi);
+  if (tmp)
+    neighborKernel<2><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, tmp, ext2, lo,
+                                                       hi, cap, maxCount);
+  else
+    neighborKernel<0><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, nullptr, ext2,
+                                                       lo, hi, 0, maxCount);
   lc->add(1);
 }
 void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
                         const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
-  neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2, lo,
-                                                        hi);
+  neighborKernel<1><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2, lo, hi,
+                                                     0, nullptr);
+  lc->add(1);
+}
+void launchNeighborCompact(const uint32_t* tmp, int cap, const long long* start, long n, uint32_t* nbr,
+                           cudaStream_t s, LaunchCounter* lc) {
+  const long threads = n * 32;
+  compactKernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(tmp, cap, start, n, nbr);
   lc->add(1);
 }
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,

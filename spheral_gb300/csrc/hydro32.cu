@@ -374,6 +374,55 @@ __global__ void dtFinalKernel32(const double* __restrict__ part, int nb, double*
   if (threadIdx.x == 0) { out[0] = sv[0]; out[1] = sr[0]; }
 }
 
+//------------------------------------------------------------------------------
+// Compatible-energy sweep of the mixed mode (SpecificThermalEnergyPolicy.cc:110-173).
+// v12 = v + a dt/2 is formed once per node in FP64; the per-pair work
+// du_ij = (v12_j - v12_i) . pacc_ij uses the FP64 velocity difference rounded
+// to FP32 and the FP32 pair acceleration; the weighted shares are summed and
+// applied to the specific energy in FP64.
+//------------------------------------------------------------------------------
+__global__ void halfStepVelocityKernel(Fields F, long n, double hdt, double4* __restrict__ v12) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  v12[i] = make_double4(F.f[F_VX][i] + F.f[F_DVDT_X][i] * hdt, F.f[F_VY][i] + F.f[F_DVDT_Y][i] * hdt,
+                        F.f[F_VZ][i] + F.f[F_DVDT_Z][i] * hdt, F.f[F_DEPSDT][i]);
+}
+
+__global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, NeighborLists nl,
+                                                      const double4* __restrict__ v12, const float* __restrict__ pacc,
+                                                      double dt) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ci[3];
+  unpackCell(nl.cell[i], ci);
+  const uint32_t mm = mirrorMask(g, ci);
+  const double4 vi = v12[i];
+  const float d0i = (float)vi.w;
+  const float feps = (float)DBL_EPSILON;
+  double sum = 0.0;
+  const long long e = nl.start[i + 1];
+  for (long long k = nl.start[i]; k < e; ++k) {
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+    const double4 vj = v12[j];
+    double vxj = vj.x, vyj = vj.y, vzj = vj.z;
+    const uint32_t mir = (uint32_t)dcode & mm;
+    if (mir) {
+      if (mir & 3u) vxj = -vxj;
+      if (mir & 12u) vyj = -vyj;
+      if (mir & 48u) vzj = -vzj;
+    }
+    const float wx = (float)(vxj - vi.x), wy = (float)(vyj - vi.y), wz = (float)(vzj - vi.z);
+    const float du = __fmaf_rn(wz, pacc[3 * k + 2], __fmaf_rn(wy, pacc[3 * k + 1], __fmul_rn(wx, pacc[3 * k])));
+    const float sg = du < 0.0f ? -1.0f : 1.0f;
+    const float weighti = fmaxf(feps, d0i * sg);
+    const float weightj = fmaxf(feps, (float)vj.w * sg);
+    sum += (double)(weighti / (weighti + weightj) * du);
+  }
+  F.f[F_DEPS_COMPAT][i] = sum;
+  F.f[F_EPS][i] += sum * dt;
+}
+
 inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 }  // namespace
@@ -419,6 +468,13 @@ void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Neigh
   const int nb = (int)gridFor(n, 128);
   dtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
+  lc->add(2);
+}
+
+void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, double4* v12,
+                                double dt, cudaStream_t s, LaunchCounter* lc) {
+  halfStepVelocityKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, 0.5 * dt, v12);
+  energyKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, v12, pacc, dt);
   lc->add(2);
 }
 

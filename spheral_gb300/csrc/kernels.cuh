@@ -33,8 +33,13 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
                    cudaStream_t s, LaunchCounter* lc);
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
+// Counts neighbours (and, with tmp != nullptr, writes them into a per-node
+// buffer of capacity cap); *maxCount (device) receives the largest count.
 void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                         int* counts, double ext2, cudaStream_t s, LaunchCounter* lc);
+                         int* counts, int* maxCount, uint32_t* tmp, int cap, double ext2, cudaStream_t s,
+                         LaunchCounter* lc);
+void launchNeighborCompact(const uint32_t* tmp, int cap, const long long* start, long n, uint32_t* nbr,
+                           cudaStream_t s, LaunchCounter* lc);
 void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
                         const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc);
 
@@ -62,6 +67,8 @@ void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, Hydro
               cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
                             double dt, cudaStream_t s, LaunchCounter* lc);
+void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, double4* v12,
+                                double dt, cudaStream_t s, LaunchCounter* lc);
 void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
