@@ -135,8 +135,7 @@ struct sphgpu_ctx {
   DBuf keys, vals, keysAlt, valsAlt, sortWs, cellStart, cellEnd, counts, nbrStart, nbr, scanWs, pacc;
   size_t cellSpace = 0;
   long long nnbr = 0;
-  int nbCap = 0;             // per-node capacity of the single-pass neighbour buffer (0: two passes)
-  DBuf nbTmp;
+  int nbCap = 0;             // slots per node of the warp-interleaved neighbour lists (0: not sized yet)
   bool haveNeighbors = false;
   // scratch
   DBuf scratch, small;
@@ -148,6 +147,8 @@ struct sphgpu_ctx {
   GravityWork* grav = nullptr;
   bool initialized = false;
   cudaEvent_t tA = nullptr, tB = nullptr;
+  int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
+  long tunedN = 0;
 
   Fields fieldsOf(DBuf& bank) {
     Fields f{};
@@ -172,9 +173,12 @@ struct sphgpu_ctx {
     float* b32 = reinterpret_cast<float*>(base + 2 * nc + therm.size());
     t.w32 = b32;
     t.g32 = b32 + nc;
+    t.p32a = reinterpret_cast<const float4*>(b32 + 2 * nc);
+    t.p32b = reinterpret_cast<const float2*>(b32 + 2 * nc + 4 * (nc / 3));
     return t;
   }
-  NeighborLists nl() { return NeighborLists{nbrStart.as<long long>(), nbr.as<uint32_t>(), cellp()}; }
+  NeighborLists nl() { return NeighborLists{nbr.as<uint32_t>(), counts.as<int>(), nbCap, cellp()}; }
+  size_t nbSlots() const { return (size_t)((n + 31) / 32) * 32 * (size_t)nbCap; }
   Fields32 f32() {
     Fields32 p;
     p.posh = posh.as<float4>();
@@ -223,8 +227,17 @@ void setTable(sphgpu_ctx* c, const double* w, const double* g, const double* g2,
   std::copy(c->tw.begin(), c->tw.end(), host.begin());
   std::copy(c->tg.begin(), c->tg.end(), host.begin() + nc);
   std::copy(c->therm.begin(), c->therm.end(), host.begin() + 2 * nc);
-  std::vector<float> h32(2 * nc);
+  // FP32: plain copies (2 nc floats), then packed intervals (N1+1) x (w0 w1 w2 g0) and (N1+1) x (g1 g2)
+  const size_t nint = (size_t)(N1 + 1);
+  std::vector<float> h32(2 * nc + 4 * nint + 2 * nint);
   for (size_t k = 0; k < nc; ++k) { h32[k] = (float)c->tw[k]; h32[nc + k] = (float)c->tg[k]; }
+  for (size_t k = 0; k < nint; ++k) {
+    float* A = &h32[2 * nc + 4 * k];
+    A[0] = (float)c->tw[3 * k]; A[1] = (float)c->tw[3 * k + 1]; A[2] = (float)c->tw[3 * k + 2];
+    A[3] = (float)c->tg[3 * k];
+    float* B = &h32[2 * nc + 4 * nint + 2 * k];
+    B[0] = (float)c->tg[3 * k + 1]; B[1] = (float)c->tg[3 * k + 2];
+  }
   const size_t bytes = host.size() * sizeof(double) + h32.size() * sizeof(float);
   c->dTable.ensure(bytes);
   CUDA_OK(cudaMemcpy(c->dTable.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -401,44 +414,53 @@ void buildNeighbors(sphgpu_ctx* c) {
   c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
   const double ext2 = c->hp.extent * c->hp.extent;
   int* dMax = reinterpret_cast<int*>(c->small.as<double>() + 40);
-  CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
-  const int cap = c->nbCap;
-  if (cap > 0) c->nbTmp.ensure((size_t)n * cap * sizeof(uint32_t));
-  {
+  auto readMax = [&]() {
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, dMax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    int m;
+    std::memcpy(&m, c->hsmall + 40, sizeof(int));
+    return m;
+  };
+  auto capFor = [](int m) { return std::max(32, ((m + m / 8 + 16 + 31) / 32) * 32); };
+  if (c->nbCap == 0) {   // first build: size the lists with a counting pass
+    CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     Scope sc(c->prof, "neighbor_count");
-    launchNeighborCount(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
-                        cap > 0 ? c->nbTmp.as<uint32_t>() : nullptr, cap, ext2, c->stream, &c->lc);
+    launchNeighbors(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
+                    nullptr, 0, ext2, c->stream, &c->lc);
+    c->check();
+    c->nbCap = capFor(readMax());
+  }
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    c->nbr.ensure(std::max<size_t>(1, c->nbSlots()) * sizeof(uint32_t));
+    CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
+    {
+      Scope sc(c->prof, "neighbors");
+      launchNeighbors(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
+                      c->nbr.as<uint32_t>(), c->nbCap, ext2, c->stream, &c->lc);
+    }
+    c->check();
+    const int m = readMax();
+    if (m <= c->nbCap) {
+      if (capFor(m) * 2 < c->nbCap) c->nbCap = capFor(m);   // shrink on the next build
+      break;
+    }
+    c->nbCap = capFor(m);   // overflow: enlarge and rebuild
   }
   long long* dTot = c->nbrStart.as<long long>() + n;
   scanExclusive<int>(c->counts.as<int>(), c->nbrStart.as<long long>(), n, c->scanWs.p, dTot, c->stream, &c->lc);
   c->check();
   CUDA_OK(cudaMemcpyAsync(c->hsmall, dTot, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, dMax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
   long long total;
-  int maxCount;
   std::memcpy(&total, c->hsmall, sizeof(long long));
-  std::memcpy(&maxCount, c->hsmall + 40, sizeof(int));
   c->nnbr = total;
-  c->nbr.ensure(std::max<long long>(1, total) * sizeof(uint32_t));
-  if (cap > 0 && maxCount <= cap) {
-    Scope sc(c->prof, "neighbor_compact");
-    launchNeighborCompact(c->nbTmp.as<uint32_t>(), cap, c->nbrStart.as<long long>(), n, c->nbr.as<uint32_t>(),
-                          c->stream, &c->lc);
-  } else {
-    Scope sc(c->prof, "neighbor_fill");
-    launchNeighborFill(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->nbrStart.as<long long>(),
-                       c->nbr.as<uint32_t>(), ext2, c->stream, &c->lc);
-  }
-  // capacity for the next build: the largest count with a margin, in steps of 32
-  c->nbCap = ((maxCount + maxCount / 8 + 16 + 31) / 32) * 32;
   c->check();
   c->haveNeighbors = true;
 }
 
 void ensurePacc(sphgpu_ctx* c) {
   const size_t per = c->cfg.precision == SPHGPU_PRECISION_FP32 ? sizeof(float) : sizeof(double);
-  c->pacc.ensure(std::max<long long>(1, c->nnbr) * 3 * per);
+  c->pacc.ensure(std::max<size_t>(1, c->nbSlots()) * 3 * per);
 }
 
 void prepare32(sphgpu_ctx* c) {
@@ -466,9 +488,34 @@ void gradh(sphgpu_ctx* c) {
 void evalDerivs(sphgpu_ctx* c) {
   ensurePacc(c);
   if (c->fp32()) {
+    // Autotuner: time each register/occupancy variant of the pair kernel once
+    // per problem size (the kernel is a pure function of its inputs, so the
+    // trial launches leave the same results) and keep the fastest.
+    if (c->pairVariant < 0 || c->tunedN != c->n) {
+      cudaEvent_t e0, e1;
+      CUDA_OK(cudaEventCreate(&e0));
+      CUDA_OK(cudaEventCreate(&e1));
+      float best = 1e30f;
+      int bestV = 1;
+      for (int v = 0; v < 3; ++v) {
+        CUDA_OK(cudaEventRecord(e0, c->stream));
+        launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+                       c->pacc.as<float>(), v, c->stream, &c->lc);
+        CUDA_OK(cudaEventRecord(e1, c->stream));
+        CUDA_OK(cudaEventSynchronize(e1));
+        c->check();
+        float ms = 0.f;
+        CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; bestV = v; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      c->pairVariant = bestV;
+      c->tunedN = c->n;
+    }
     Scope sc(c->prof, "pair_fp32");
     launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
-                   c->pacc.as<float>(), 128, c->stream, &c->lc);
+                   c->pacc.as<float>(), c->pairVariant, c->stream, &c->lc);
   } else {
     Scope sc(c->prof, "pair_fp64");
     launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists, c->pacc.as<double>(),
@@ -725,7 +772,7 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->nbTmp};
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);
@@ -917,7 +964,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   double* st = c->stage.as<double>();
   if (isNb) {
     if (!c->haveNeighbors) throw Error(SPHGPU_E_STATE, "no neighbour lists yet");
-    launchCountsOut(c->nbrStart.as<long long>(), c->origp(), st, n, c->stream, &c->lc);
+    launchCountsOut(c->counts.as<int>(), c->origp(), st, n, c->stream, &c->lc);
   } else if (isH) {
     launchGatherOutH(c->F, c->origp(), st, fs.first, n, c->stream, &c->lc);
   } else {
@@ -1001,20 +1048,22 @@ int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* 
   *npairs = (long)c->nnbr;
   if (!i_out) return SPHGPU_OK;
   const long n = c->n;
-  std::vector<int> orig(n);
-  std::vector<long long> st(n + 1);
-  std::vector<uint32_t> nb(std::max<long long>(1, c->nnbr)), cells(n);
+  const int cap = c->nbCap;
+  std::vector<int> orig(n), cnt(n);
+  std::vector<uint32_t> nb(std::max<size_t>(1, c->nbSlots())), cells(n);
   CUDA_OK(cudaMemcpyAsync(cells.data(), c->cellp(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(orig.data(), c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_OK(cudaMemcpyAsync(st.data(), c->nbrStart.p, (n + 1) * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_OK(cudaMemcpyAsync(nb.data(), c->nbr.p, c->nnbr * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(cnt.data(), c->counts.p, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(nb.data(), c->nbr.p, c->nbSlots() * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
+  long long k = 0;
   for (long i = 0; i < n; ++i)
-    for (long long k = st[i]; k < st[i + 1]; ++k) {
+    for (int q = 0; q < cnt[i]; ++q, ++k) {
+      const uint32_t e = nb[((size_t)(i >> 5) * cap + q) * 32 + (i & 31)];
       i_out[k] = orig[i];
-      j_out[k] = orig[nb[k] & kIndexMask];
+      j_out[k] = orig[e & kIndexMask];
       if (image) {
-        const int d = (int)(nb[k] >> kIndexBits);
+        const int d = (int)(e >> kIndexBits);
         int code = 0;
         for (int a = 0; a < 3; ++a) {
           const int ca = (int)((cells[i] >> (10 * a)) & 1023u);

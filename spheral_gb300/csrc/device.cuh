@@ -8,6 +8,13 @@ namespace dev {
 
 constexpr double kTiny30 = 1.0e-30;
 
+// Warp-interleaved neighbour storage: slot q of node i lives at
+// ((i / 32) * cap + q) * 32 + i % 32, so a warp reading slot q of its 32 nodes
+// touches one contiguous 128-byte line.
+__device__ __forceinline__ long long nbSlot(long i, int q, int cap) {
+  return ((long long)(i >> 5) * cap + q) * 32 + (i & 31);
+}
+
 __device__ __forceinline__ void unpackCell(uint32_t cc, int c[3]) {
   c[0] = (int)(cc & 1023u);
   c[1] = (int)((cc >> 10) & 1023u);
@@ -252,6 +259,107 @@ __device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const No
   F.f[F_HIDEAL][i] = 1.0 / hi1;
 }
 
+
+// FP32 variant of finalizeNode for the mixed mode: the per-node completion
+// (3x3 inverse, corrected gradient, IdealH lookup) in FP32, results stored in
+// the FP64 fields.  GB300 runs FP64 at a small fraction of the FP32 rate, so
+// per-node FP64 work is visible even next to a ~100-neighbour pair loop.
+__device__ __forceinline__ float hermiteLookup32(const double* __restrict__ v, const HydroParams& hp, float x) {
+  const int N = hp.hermN;
+  const float xmin = (float)hp.hermXmin, xmax = (float)hp.hermXmax, st = (float)hp.hermXstep;
+  if (x < xmin) return (float)v[0] + (float)v[N] * (x - xmin);
+  if (x > xmax) return (float)v[N - 1] + (float)v[2 * N - 1] * (x - xmin);
+  const int i0 = min(N - 2, (int)(fmaxf(0.0f, x - xmin) / st));
+  const float t = fmaxf(0.0f, fminf(1.0f, (x - xmin - i0 * st) / st));
+  const float t2 = t * t, t3 = t * t2;
+  return ((2.0f * t3 - 3.0f * t2 + 1.0f) * (float)v[i0] + (-2.0f * t3 + 3.0f * t2) * (float)v[i0 + 1] +
+          st * ((t3 - 2.0f * t2 + t) * (float)v[N + i0] + (t3 - t2) * (float)v[N + i0 + 1]));
+}
+
+struct NodeAcc32 {
+  float rhoSum, norm, gx, gy, gz, maxQ, effQ, xw, xdx, xdy, xdz, m0, m1x, m1y, m1z;
+  double dvx, dvy, dvz, deps;
+  float D[9], M[9];
+};
+
+__device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const NodeAcc32& a, int numNb,
+                                               const HydroParams& hp, const double* __restrict__ herm) {
+  const float mi = (float)F.f[F_MASS][i], rhoi = (float)F.f[F_RHO][i], ai = (float)F.f[F_HINV][i];
+  const float Hdeti = (ai * ai) * ai;
+  const float W0 = (float)hp.W0;
+  F.f[F_RHOSUM][i] = a.rhoSum + mi * W0 * Hdeti;
+  F.f[F_NORM][i] = a.norm + mi / rhoi * W0 * Hdeti;
+  float D[9], Mm[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { D[k] = a.D[k]; Mm[k] = a.M[k]; }
+  const float detM = (Mm[0] * Mm[4] * Mm[8] + Mm[1] * Mm[5] * Mm[6] + Mm[2] * Mm[3] * Mm[7] -
+                      Mm[0] * Mm[5] * Mm[7] - Mm[1] * Mm[3] * Mm[8] - Mm[2] * Mm[4] * Mm[6]);
+  const float irho = 1.0f / rhoi;
+  if (hp.correctVelGrad && fabsf(detM) > 1.0e-10f && numNb > 8) {
+    const float id = 1.0f / detM;
+    const float inv[9] = {(Mm[4] * Mm[8] - Mm[5] * Mm[7]) * id, (Mm[2] * Mm[7] - Mm[1] * Mm[8]) * id,
+                          (Mm[1] * Mm[5] - Mm[2] * Mm[4]) * id, (Mm[5] * Mm[6] - Mm[3] * Mm[8]) * id,
+                          (Mm[0] * Mm[8] - Mm[2] * Mm[6]) * id, (Mm[2] * Mm[3] - Mm[0] * Mm[5]) * id,
+                          (Mm[3] * Mm[7] - Mm[4] * Mm[6]) * id, (Mm[1] * Mm[6] - Mm[0] * Mm[7]) * id,
+                          (Mm[0] * Mm[4] - Mm[1] * Mm[3]) * id};
+    float R[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        R[3 * r + c] = D[3 * r] * inv[c] + D[3 * r + 1] * inv[3 + c] + D[3 * r + 2] * inv[6 + c];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { D[k] = R[k]; Mm[k] = inv[k]; }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) D[k] *= irho;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { F.f[F_DVDX_XX + k][i] = D[k]; F.f[F_M_XX + k][i] = Mm[k]; }
+  F.f[F_GRADRHO_X][i] = a.gx * irho;
+  F.f[F_GRADRHO_Y][i] = a.gy * irho;
+  F.f[F_GRADRHO_Z][i] = a.gz * irho;
+  const float trace = D[0] + D[4] + D[8];
+  F.f[F_DRHODT][i] = -(double)rhoi * trace;
+  F.f[F_DVDT_X][i] = a.dvx;
+  F.f[F_DVDT_Y][i] = a.dvy;
+  F.f[F_DVDT_Z][i] = a.dvz;
+  F.f[F_DEPSDT][i] = a.deps;
+  F.f[F_MAXQ][i] = a.maxQ;
+  F.f[F_EFFQ][i] = a.effQ;
+  float xw = a.xw;
+  const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
+  if (hp.xsph) {
+    xw += Hdeti * mi * irho * W0;
+    const float ws = fmaxf(1.0e-30f, xw);
+    F.f[F_DXDT_X][i] = vxi + a.xdx / ws;
+    F.f[F_DXDT_Y][i] = vyi + a.xdy / ws;
+    F.f[F_DXDT_Z][i] = vzi + a.xdz / ws;
+  } else {
+    F.f[F_DXDT_X][i] = vxi;
+    F.f[F_DXDT_Y][i] = vyi;
+    F.f[F_DXDT_Z][i] = vzi;
+  }
+  F.f[F_XSPHW][i] = xw;
+  F.f[F_XSPHDV_X][i] = a.xdx;
+  F.f[F_XSPHDV_Y][i] = a.xdy;
+  F.f[F_XSPHDV_Z][i] = a.xdz;
+  const NodeListParams L = cLists[li];
+  const float m0 = cbrtf(fmaxf(0.0f, a.m0));
+  F.f[F_M0][i] = m0;
+  F.f[F_M1_X][i] = a.m1x;
+  F.f[F_M1_Y][i] = a.m1y;
+  F.f[F_M1_Z][i] = a.m1z;
+  F.f[F_DHDT][i] = ((-F.f[F_HINV][i]) / 3.0) * (double)trace;
+  const float nPerh = (float)L.nPerh;
+  const bool iso = fabsf(m0) <= 1.0e-15f * fmaxf(1.0f, fabsf(m0));
+  const float cur = iso ? 0.5f * nPerh : fmaxf(0.0f, hermiteLookup32(herm, hp, m0));
+  const float s = fminf(4.0f, fmaxf(0.25f, nPerh / (cur + 1.0e-30f)));
+  const float aa = s < 1.0f ? 0.4f * (1.0f + s * s) : 0.4f * (1.0f + 1.0f / (s * s * s));
+  const double hi0 = 1.0 / F.f[F_HINV][i];
+  const double hi1 = fmin(L.hmax, fmax(L.hmin, hi0 * (double)(1.0f - aa + aa * s)));
+  F.f[F_HIDEAL][i] = 1.0 / hi1;
+}
 
 }  // namespace dev
 }  // namespace sph

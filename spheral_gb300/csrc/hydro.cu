@@ -96,16 +96,14 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 // positions settles every candidate outside a narrow band around the
 // threshold; candidates inside the band get the exact FP64 test with the
 // reference's operation order, so the neighbour sets are exact.
-// MODE 0: count only; 1: fill the CSR lists; 2: count and write into a
-// per-node buffer of capacity cap (entries beyond cap are counted, not written).
-template <int MODE>
+// WRITE false: count only; true: count and write the warp-interleaved lists
+// (slots beyond cap are counted, not written).
+template <bool WRITE>
 __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long n, Grid g,
                                                       const int* __restrict__ cellStart,
                                                       const int* __restrict__ cellEnd, int* __restrict__ counts,
-                                                      const long long* __restrict__ start, uint32_t* __restrict__ nbr,
-                                                      double ext2, float bandLo, float bandHi, int cap,
-                                                      int* __restrict__ maxCount) {
-  constexpr bool FILL = MODE == 1;
+                                                      uint32_t* __restrict__ nbr, double ext2, float bandLo,
+                                                      float bandHi, int cap, int* __restrict__ maxCount) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* __restrict__ X = F.f[F_X];
@@ -119,8 +117,6 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
   const float cellx = (float)g.cell[0], celly = (float)g.cell[1], cellz = (float)g.cell[2];
   const uint32_t mm = mirrorMask(g, ci);
   int cnt = 0;
-  long long w = FILL ? start[i] : 0;
-  uint32_t* __restrict__ tmp = MODE == 2 ? nbr + (long long)i * cap : nullptr;
   forEachCandidate(g, cc, cellStart, cellEnd, [&](int j, int dcode) {
     if (j == (int)i && dcode == 0) return;
     const float4 pj = P.posh[j];
@@ -140,29 +136,12 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
       inside = eta2Exact(A[i], qx, qy, qz) <= ext2 || eta2Exact(A[j], qx, qy, qz) <= ext2;
     }
     if (inside) {
-      const uint32_t entry = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-      if (FILL) nbr[w++] = entry;
-      else {
-        if (MODE == 2 && cnt < cap) tmp[cnt] = entry;
-        ++cnt;
-      }
+      if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
+      ++cnt;
     }
   });
-  if (!FILL) {
-    counts[i] = cnt;
-    atomicMax(maxCount, cnt);
-  }
-}
-
-// Copy per-node capacity buffers into the CSR lists (one warp per node).
-__global__ void compactKernel(const uint32_t* __restrict__ tmp, int cap, const long long* __restrict__ start, long n,
-                              uint32_t* __restrict__ nbr) {
-  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (w >= n) return;
-  const long long s0 = start[w], cnt = start[w + 1] - s0;
-  const uint32_t* src = tmp + w * (long long)cap;
-  for (long long c = lane; c < cnt; c += 32) nbr[s0 + c] = src[c];
+  counts[i] = cnt;
+  atomicMax(maxCount, cnt);
 }
 
 //------------------------------------------------------------------------------
@@ -190,8 +169,9 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
   const double Hdeti = (ai * ai) * ai;
   const double self = mi * (Hdeti * smem[0]);
   double sum = 0.0;
-  const long long e = nl.start[i + 1];
-  for (long long k = nl.start[i]; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j];
@@ -230,8 +210,9 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
   const double xi = X[i], yi = Y[i], zi = Z[i], ai = F.f[F_HINV][i];
   const double Hdeti = (ai * ai) * ai;
   double wsum = 0.0, gsum = 0.0;
-  const long long s = nl.start[i], e = nl.start[i + 1];
-  for (long long k = s; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j];
@@ -246,7 +227,7 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
     }
   }
   double omega;
-  if (e == s) omega = 1.0;
+  if (cnt == 0) omega = 1.0;
   else omega = fmax(1.0e-30, -gsum / (3.0 * (wsum + Hdeti * hp.W0)));
   F.f[F_OMEGA][i] = omega;
 }
@@ -298,8 +279,9 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
 #pragma unroll
   for (int k = 0; k < 9; ++k) { a.D[k] = 0.0; a.M[k] = 0.0; }
 
-  const long long s = nl.start[i], e = nl.start[i + 1];
-  for (long long k = s; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j], vxj = VX[j], vyj = VY[j], vzj = VZ[j];
@@ -400,7 +382,7 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
     const double fwW = fw * WSPHi;
     a.m1x -= fwW * eix; a.m1y -= fwW * eiy; a.m1z -= fwW * eiz;
   }
-  finalizeNode(F, i, li, a, mi, rhoi, vxi, vyi, vzi, ai, (int)(e - s), hp, t.herm);
+  finalizeNode(F, i, li, a, mi, rhoi, vxi, vyi, vzi, ai, cnt, hp, t.herm);
 }
 
 //------------------------------------------------------------------------------
@@ -443,8 +425,9 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
       if (velDt < best) { best = velDt; reason = 4; }
     }
     const double nsi = 1.0 / ai / maxNperh;
-    const long long e = nl.start[i + 1];
-    for (long long k = nl.start[i]; k < e; ++k) {
+    const int cnt = nl.count[i];
+    for (int q = 0; q < cnt; ++q) {
+      const long long k = nbSlot(i, q, nl.cap);
       const uint32_t ent = nl.nbr[k];
       const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
       double vxj = F.f[F_VX][j], vyj = F.f[F_VY][j], vzj = F.f[F_VZ][j];
@@ -511,8 +494,9 @@ __global__ void __launch_bounds__(128) energyKernel(Fields F, long n, Grid g, Ne
   const double vxi = VX[i] + AX[i] * hdt, vyi = VY[i] + AY[i] * hdt, vzi = VZ[i] + AZ[i] * hdt;
   const double d0i = D0[i];
   double sum = 0.0;
-  const long long e = nl.start[i + 1];
-  for (long long k = nl.start[i]; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double vxj = VX[j], vyj = VY[j], vzj = VZ[j], axj = AX[j], ayj = AY[j], azj = AZ[j];
@@ -692,11 +676,11 @@ __global__ void gatherOutHKernel(Fields F, const int* __restrict__ orig, double*
   const double a = F.f[field][k];
   o[0] = a; o[1] = 0.0; o[2] = 0.0; o[3] = a; o[4] = 0.0; o[5] = a;
 }
-__global__ void countsOutKernel(const long long* __restrict__ start, const int* __restrict__ orig,
+__global__ void countsOutKernel(const int* __restrict__ counts, const int* __restrict__ orig,
                                 double* __restrict__ stage, long n) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  stage[orig[k]] = (double)(start[k + 1] - start[k]);
+  stage[orig[k]] = (double)counts[k];
 }
 
 inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -737,31 +721,17 @@ static void neighborBand(const Grid& g, double ext2, float& lo, float& hi) {
   lo = (float)(ext2 * (1.0 - 2.0e-3));
   hi = (float)(ext2 * (1.0 + 2.0e-3));
 }
-void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                         int* counts, int* maxCount, uint32_t* tmp, int cap, double ext2, cudaStream_t s,
-                         LaunchCounter* lc) {
+void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                     int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,
+                     LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
-  if (tmp)
-    neighborKernel<2><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, tmp, ext2, lo,
-                                                       hi, cap, maxCount);
+  if (nbr)
+    neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nbr, ext2, lo, hi,
+                                                          cap, maxCount);
   else
-    neighborKernel<0><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, nullptr, ext2,
-                                                       lo, hi, 0, maxCount);
-  lc->add(1);
-}
-void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                        const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc) {
-  float lo, hi;
-  neighborBand(g, ext2, lo, hi);
-  neighborKernel<1><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, nullptr, start, nbr, ext2, lo, hi,
-                                                     0, nullptr);
-  lc->add(1);
-}
-void launchNeighborCompact(const uint32_t* tmp, int cap, const long long* start, long n, uint32_t* nbr,
-                           cudaStream_t s, LaunchCounter* lc) {
-  const long threads = n * 32;
-  compactKernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(tmp, cap, start, n, nbr);
+    neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, ext2, lo,
+                                                           hi, 0, maxCount);
   lc->add(1);
 }
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -858,9 +828,8 @@ void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long 
   gatherOutHKernel<<<gridFor(n, 256), 256, 0, s>>>(F, orig, stage, field, n);
   lc->add(1);
 }
-void launchCountsOut(const long long* start, const int* orig, double* stage, long n, cudaStream_t s,
-                     LaunchCounter* lc) {
-  countsOutKernel<<<gridFor(n, 256), 256, 0, s>>>(start, orig, stage, n);
+void launchCountsOut(const int* counts, const int* orig, double* stage, long n, cudaStream_t s, LaunchCounter* lc) {
+  countsOutKernel<<<gridFor(n, 256), 256, 0, s>>>(counts, orig, stage, n);
   lc->add(1);
 }
 

@@ -67,15 +67,33 @@ __device__ __forceinline__ void lookup32(const float* __restrict__ tw, const flo
 
 //------------------------------------------------------------------------------
 // SPH pair loop (src/SPH/SPH.cc:294-470) + SPHSmoothingScale moments, FP32.
+// Every operation that enters the pair force is deterministic and appears in
+// the same order from both sides of the pair (explicit fma / rn intrinsics,
+// MUFU reciprocal square root and fast division), so slot (j, i) holds the
+// bitwise negation of slot (i, j).
 //------------------------------------------------------------------------------
-template <bool XSPH, bool COMPAT>
-__global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
+__device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, const float2* __restrict__ tb, int N1,
+                                             float invStep, float eta, float extent, float& w, float& gr) {
+  if (eta < extent) {
+    const int k = min(N1, (int)(eta * invStep));
+    const float4 A = ta[k];
+    const float2 B = tb[k];
+    w = __fmaf_rn(__fmaf_rn(A.z, eta, A.y), eta, A.x);
+    gr = __fmaf_rn(__fmaf_rn(B.y, eta, B.x), eta, A.w);
+  } else {
+    w = 0.0f;
+    gr = 0.0f;
+  }
+}
+
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB>
+__global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
-  __shared__ float tw[kMaxTable];
-  __shared__ float tg[kMaxTable];
-  const int ntab = 3 * (hp.tableN1 + 1);
-  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { tw[k] = t.w32[k]; tg[k] = t.g32[k]; }
+  __shared__ float4 ta[kMaxTable / 3];
+  __shared__ float2 tb[kMaxTable / 3];
+  const int nint = hp.tableN1 + 1;
+  for (int k = threadIdx.x; k < nint; k += blockDim.x) { ta[k] = t.p32a[k]; tb[k] = t.p32b[k]; }
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -84,16 +102,17 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
   const uint32_t mm = mirrorMask(g, ci);
   const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
   const float4 pi = P.posh[i], vi = P.velm[i], thi = P.thermo[i];
-  const int li = list[i];
+  const int li = MULTI ? list[i] : 0;
   const float ai = pi.w, mi = vi.w, rhoi = thi.x, Pi = thi.y, csi = thi.z, sOi = thi.w;
   const float Hdeti = ai * ai * ai;
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   const float Cl = (float)hp.Cl, Cq = (float)hp.Cq, eps2 = (float)hp.eps2;
   const float epsT = (float)hp.epsTensile, WnPerh = (float)hp.WnPerh;
-  const float tiny = 1.0e-30f;
-  const float mrhoi = mi / rhoi;
-  const float Prhoi0 = sOi * Pi / (rhoi * rhoi);
+  const float iri = __frcp_rn(rhoi);
+  const float mrhoi = mi * iri;
+  const float Prhoi0 = __fmul_rn(__fmul_rn(__fmul_rn(sOi, Pi), iri), iri);
+  const float mClci = __fmul_rn(-Cl, csi);
 
   float rhoSum = 0.f, norm = 0.f, maxQ = 0.f, effQ = 0.f, xw = 0.f, xdx = 0.f, xdy = 0.f, xdz = 0.f;
   float sdx = 0.f, cdx = 0.f, sdy = 0.f, cdy = 0.f, sdz = 0.f, cdz = 0.f, se = 0.f, ce = 0.f;
@@ -102,8 +121,9 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
 #pragma unroll
   for (int k = 0; k < 9; ++k) { D[k] = 0.f; M[k] = 0.f; }
 
-  const long long s = nl.start[i], e = nl.start[i + 1];
-  for (long long k = s; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     const float4 pj = P.posh[j], vj4 = P.velm[j], thj = P.thermo[j];
@@ -112,49 +132,50 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
     float vxj = vj4.x, vyj = vj4.y, vzj = vj4.z;
     mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
     const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z, sOj = thj.w;
-    const int lj = list[j];
+    const bool same = MULTI ? (list[j] == li) : true;
     const float Hdetj = aj * aj * aj;
+    const float irj = __frcp_rn(rhoj);
 
     const float eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
     const float ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
-    // explicit fused forms: node j evaluates this pair with bitwise the same arithmetic
     const float e2i = __fmaf_rn(eiz, eiz, __fmaf_rn(eiy, eiy, __fmul_rn(eix, eix)));
     const float e2j = __fmaf_rn(ejz, ejz, __fmaf_rn(ejy, ejy, __fmul_rn(ejx, ejx)));
-    const float etai = sqrtf(e2i), etaj = sqrtf(e2j);
+    const float ri = rsqrtf(fmaxf(e2i, 1.0e-30f)), rj = rsqrtf(fmaxf(e2j, 1.0e-30f));
+    const float etai = __fmul_rn(e2i, ri), etaj = __fmul_rn(e2j, rj);
     float Wi, gi, Wj, gj;
-    lookup32(tw, tg, N1, invStep, etai, extent, Wi, gi);
-    lookup32(tw, tg, N1, invStep, etaj, extent, Wj, gj);
+    lookupPacked(ta, tb, N1, invStep, etai, extent, Wi, gi);
+    lookupPacked(ta, tb, N1, invStep, etaj, extent, Wj, gj);
     const float WSPHi = fabsf(gi);
     Wi *= Hdeti;
     Wj *= Hdetj;
-    // gradW = gW H eta/|eta| = (Hdet g a / |eta|) eta
-    const float fi = __fmul_rn(__fmul_rn(Hdeti, gi), ai) / fmaxf(tiny, etai);
-    const float fj = __fmul_rn(__fmul_rn(Hdetj, gj), aj) / fmaxf(tiny, etaj);
+    // gradW = gW H eta/|eta|
+    const float fi = __fmul_rn(__fmul_rn(__fmul_rn(Hdeti, gi), ai), ri);
+    const float fj = __fmul_rn(__fmul_rn(__fmul_rn(Hdetj, gj), aj), rj);
     const float gwix = fi * eix, gwiy = fi * eiy, gwiz = fi * eiz;
     const float gwjx = fj * ejx, gwjy = fj * ejy, gwjz = fj * ejz;
 
-    if (lj == li) {
+    if (same) {
       rhoSum += mj * Wi;
       norm += mrhoi * Wi;
     }
     const float vx = vi.x - vxj, vy = vi.y - vyj, vz = vi.z - vzj;
-    const float mui = __fmaf_rn(vz, eiz, __fmaf_rn(vy, eiy, __fmul_rn(vx, eix))) / __fadd_rn(e2i, eps2);
-    const float muj = __fmaf_rn(vz, ejz, __fmaf_rn(vy, ejy, __fmul_rn(vx, ejx))) / __fadd_rn(e2j, eps2);
-    float li_ = hp.linearInExpansion ? mui : fminf(0.f, mui);
-    float lj_ = hp.linearInExpansion ? muj : fminf(0.f, muj);
-    float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : fminf(0.f, mui) * fminf(0.f, mui);
-    float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : fminf(0.f, muj) * fminf(0.f, muj);
-    const float ei = __fmaf_rn(Cq, qi_, __fmul_rn(__fmul_rn(-Cl, csi), li_));
+    const float mui = __fdividef(__fmaf_rn(vz, eiz, __fmaf_rn(vy, eiy, __fmul_rn(vx, eix))), __fadd_rn(e2i, eps2));
+    const float muj = __fdividef(__fmaf_rn(vz, ejz, __fmaf_rn(vy, ejy, __fmul_rn(vx, ejx))), __fadd_rn(e2j, eps2));
+    const float li_ = hp.linearInExpansion ? mui : fminf(0.f, mui);
+    const float lj_ = hp.linearInExpansion ? muj : fminf(0.f, muj);
+    const float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : li_ * li_;
+    const float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : lj_ * lj_;
+    const float ei = __fmaf_rn(Cq, qi_, __fmul_rn(mClci, li_));
     const float ej = __fmaf_rn(Cq, qj_, __fmul_rn(__fmul_rn(-Cl, csj), lj_));
-    const float qai = __fmul_rn(0.5f, ei / rhoi), qaj = __fmul_rn(0.5f, ej / rhoj);
+    const float qai = __fmul_rn(0.5f, __fmul_rn(ei, iri)), qaj = __fmul_rn(0.5f, __fmul_rn(ej, irj));
     const float Qi = rhoi * ei;
     maxQ = fmaxf(maxQ, Qi);
-    effQ += mj * Qi * Wi / rhoj;
-    float Prhoi = Prhoi0, Prhoj = sOj * Pj / (rhoj * rhoj);
+    effQ += mj * Qi * Wi * irj;
+    float Prhoi = Prhoi0, Prhoj = __fmul_rn(__fmul_rn(__fmul_rn(sOj, Pj), irj), irj);
     if (epsT != 0.f) {
-      const float ri = Wi / (Hdeti * WnPerh), rj = Wj / (Hdetj * WnPerh);
-      Prhoi = sOi * (Pi + epsT * (ri * ri * ri * ri) * (Pi < 0.f ? -Pi : 0.f)) / (rhoi * rhoi);
-      Prhoj = sOj * (Pj + epsT * (rj * rj * rj * rj) * (Pj < 0.f ? -Pj : 0.f)) / (rhoj * rhoj);
+      const float ti = Wi / (Hdeti * WnPerh), tj = Wj / (Hdetj * WnPerh);
+      Prhoi = __fmul_rn(__fmul_rn(__fmul_rn(sOi, Pi + epsT * (ti * ti * ti * ti) * (Pi < 0.f ? -Pi : 0.f)), iri), iri);
+      Prhoj = __fmul_rn(__fmul_rn(__fmul_rn(sOj, Pj + epsT * (tj * tj * tj * tj) * (Pj < 0.f ? -Pj : 0.f)), irj), irj);
     }
     // symmetric-order pair force: (Prho_i + Q_i/2) gradW_i + (Prho_j + Q_j/2) gradW_j
     const float ci_ = __fadd_rn(Prhoi, qai), cj_ = __fadd_rn(Prhoj, qaj);
@@ -171,13 +192,13 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
       pacc[3 * k + 2] = paz;
     }
     const float vg = vx * gwix + vy * gwiy + vz * gwiz;
-    kahanAdd(se, ce, mj * (Prhoi * vg + qai * vg));
+    kahanAdd(se, ce, mj * (Prhoi + qai) * vg);
     const float mvx = mj * vx, mvy = mj * vy, mvz = mj * vz;
     D[0] -= mvx * gwix; D[1] -= mvx * gwiy; D[2] -= mvx * gwiz;
     D[3] -= mvy * gwix; D[4] -= mvy * gwiy; D[5] -= mvy * gwiz;
     D[6] -= mvz * gwix; D[7] -= mvz * gwiy; D[8] -= mvz * gwiz;
     if (XSPH) {
-      const float wx = 0.5f * (mrhoi * Wi + mj / rhoj * Wj);
+      const float wx = 0.5f * (mrhoi * Wi + mj * irj * Wj);
       xw += wx;
       xdx -= wx * vx; xdy -= wx * vy; xdz -= wx * vz;
     }
@@ -187,12 +208,12 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
     M[0] -= mrx * gwix; M[1] -= mrx * gwiy; M[2] -= mrx * gwiz;
     M[3] -= mry * gwix; M[4] -= mry * gwiy; M[5] -= mry * gwiz;
     M[6] -= mrz * gwix; M[7] -= mrz * gwiy; M[8] -= mrz * gwiz;
-    const float fw = (lj != li) ? mj * rhoi / (mi * rhoj) : 1.0f;
+    const float fw = same ? 1.0f : mj * rhoi / (mi * rhoj);
     const float fwW = fw * WSPHi;
     m0 += fwW;
     m1x -= fwW * eix; m1y -= fwW * eiy; m1z -= fwW * eiz;
   }
-  NodeAcc a;
+  NodeAcc32 a;
   a.rhoSum = rhoSum; a.norm = norm;
   a.dvx = kahanValue(sdx, cdx); a.dvy = kahanValue(sdy, cdy); a.dvz = kahanValue(sdz, cdz);
   a.deps = kahanValue(se, ce);
@@ -201,8 +222,7 @@ __global__ void __launch_bounds__(128) pairKernelFP32(Fields F, Fields32 P, cons
   a.m0 = m0; a.m1x = m1x; a.m1y = m1y; a.m1z = m1z;
 #pragma unroll
   for (int k = 0; k < 9; ++k) { a.D[k] = D[k]; a.M[k] = M[k]; }
-  finalizeNode(F, i, li, a, F.f[F_MASS][i], F.f[F_RHO][i], F.f[F_VX][i], F.f[F_VY][i], F.f[F_VZ][i],
-               F.f[F_HINV][i], (int)(e - s), hp, t.herm);
+  finalizeNode32(F, i, MULTI ? li : list[i], a, cnt, hp, t.herm);
 }
 
 //------------------------------------------------------------------------------
@@ -226,8 +246,9 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   float s = 0.f, c = 0.f;
-  const long long e = nl.start[i + 1];
-  for (long long k = nl.start[i]; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     const float4 pj = P.posh[j];
@@ -269,8 +290,9 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   float ws = 0.f, wc = 0.f, gs = 0.f, gc = 0.f;
-  const long long s = nl.start[i], e = nl.start[i + 1];
-  for (long long k = s; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
@@ -284,7 +306,7 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
   const double a = F.f[F_HINV][i];
   const double Hdet = (a * a) * a;
   double omega;
-  if (e == s) omega = 1.0;
+  if (cnt == 0) omega = 1.0;
   else omega = fmax(1.0e-30, -(Hdet * kahanValue(gs, gc)) / (3.0 * (Hdet * kahanValue(ws, wc) + Hdet * hp.W0)));
   F.f[F_OMEGA][i] = omega;
   P.thermo[i].w = (float)(omega / (omega * omega + 1.0e-30));
@@ -328,8 +350,9 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
     const float4 vi = P.velm[i];
     const float hi = 1.0f / P.posh[i].w;
     float bestPair = 3.0e38f;
-    const long long e = nl.start[i + 1];
-    for (long long k = nl.start[i]; k < e; ++k) {
+    const int cnt = nl.count[i];
+    for (int q = 0; q < cnt; ++q) {
+      const long long k = nbSlot(i, q, nl.cap);
       const uint32_t ent = nl.nbr[k];
       const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
       const float4 vj = P.velm[j];
@@ -400,8 +423,9 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
   const float d0i = (float)vi.w;
   const float feps = (float)DBL_EPSILON;
   double sum = 0.0;
-  const long long e = nl.start[i + 1];
-  for (long long k = nl.start[i]; k < e; ++k) {
+  const int cnt = nl.count[i];
+  for (int q = 0; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     const double4 vj = v12[j];
@@ -432,19 +456,30 @@ void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, L
   lc->add(1);
 }
 
+// variant: minimum resident blocks per SM requested from the compiler for the
+// common path (compatible energy, no XSPH, one NodeList): 0 -> 4 (no
+// register cap below 128), 1 -> 5 (<= 102 registers, no spills), 2 -> 6
+// (<= 85 registers, small spills).  Chosen at run time by the autotuner.
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                    HydroParams hp, const NodeListParams* lists, float* pacc, int blockSize, cudaStream_t s,
+                    HydroParams hp, const NodeListParams* lists, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc) {
   cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
-  (void)blockSize;
   const int b = 128;
-  if (hp.xsph) {
-    if (hp.compatible) pairKernelFP32<true, true><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
-    else pairKernelFP32<true, false><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+  const unsigned gb = gridFor(n, b);
+  const bool multi = hp.numLists > 1;
+#define SPH_PAIR32(X, C, M, MB) pairKernelFP32<X, C, M, MB><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
+  if (!hp.xsph && hp.compatible && !multi) {
+    if (variant == 0) SPH_PAIR32(false, true, false, 4);
+    else if (variant == 2) SPH_PAIR32(false, true, false, 6);
+    else SPH_PAIR32(false, true, false, 5);
+  } else if (hp.xsph) {
+    if (hp.compatible) { if (multi) SPH_PAIR32(true, true, true, 5); else SPH_PAIR32(true, true, false, 5); }
+    else { if (multi) SPH_PAIR32(true, false, true, 5); else SPH_PAIR32(true, false, false, 5); }
   } else {
-    if (hp.compatible) pairKernelFP32<false, true><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
-    else pairKernelFP32<false, false><<<gridFor(n, b), b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+    if (hp.compatible) SPH_PAIR32(false, true, true, 5);
+    else { if (multi) SPH_PAIR32(false, false, true, 5); else SPH_PAIR32(false, false, false, 5); }
   }
+#undef SPH_PAIR32
   lc->add(1);
 }
 

@@ -12,11 +12,14 @@ struct TableDev {
   const double* herm;   // 2*hermN Hermite knots of the nperh lookup (values, slopes)
   const float* w32;     // FP32 copies for the FP32 pair loop
   const float* g32;
+  const float4* p32a;   // per interval (w0, w1, w2, g0) in FP32
+  const float2* p32b;   // per interval (g1, g2) in FP32
 };
 
 struct NeighborLists {
-  const long long* start;   // n+1 offsets
-  const uint32_t* nbr;      // entries: index | cell-offset code << 26
+  const uint32_t* nbr;      // entries (index | cell-offset code << 26), warp-interleaved with capacity cap
+  const int* count;         // neighbours per node
+  int cap;                  // slots per node
   const uint32_t* cell;     // home cell of every node (packed, 10 bits per axis)
 };
 
@@ -33,15 +36,12 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
                    cudaStream_t s, LaunchCounter* lc);
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
-// Counts neighbours (and, with tmp != nullptr, writes them into a per-node
-// buffer of capacity cap); *maxCount (device) receives the largest count.
-void launchNeighborCount(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                         int* counts, int* maxCount, uint32_t* tmp, int cap, double ext2, cudaStream_t s,
-                         LaunchCounter* lc);
-void launchNeighborCompact(const uint32_t* tmp, int cap, const long long* start, long n, uint32_t* nbr,
-                           cudaStream_t s, LaunchCounter* lc);
-void launchNeighborFill(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                        const long long* start, uint32_t* nbr, double ext2, cudaStream_t s, LaunchCounter* lc);
+// Counts the neighbours of every node and, with nbr != nullptr, writes them
+// into the warp-interleaved lists of capacity cap (entries beyond cap are
+// counted, not written); *maxCount (device) receives the largest count.
+void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
+                     int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,
+                     LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -51,7 +51,7 @@ void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroPa
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                     const NodeListParams* lists, double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                    HydroParams hp, const NodeListParams* lists, float* pacc, int blockSize, cudaStream_t s,
+                    HydroParams hp, const NodeListParams* lists, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);
 void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
 void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
@@ -86,8 +86,7 @@ void launchGatherOut(Fields F, const int* orig, double* stage, int first, int nc
 void launchScatterIn(Fields F, const int* orig, const double* stage, int first, int ncomp, int stride, long n,
                      cudaStream_t s, LaunchCounter* lc);
 void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long n, cudaStream_t s, LaunchCounter* lc);
-void launchCountsOut(const long long* start, const int* orig, double* stage, long n, cudaStream_t s,
-                     LaunchCounter* lc);
+void launchCountsOut(const int* counts, const int* orig, double* stage, long n, cudaStream_t s, LaunchCounter* lc);
 // check finite / positive state: writes a flag
 void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc);
 
