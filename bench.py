@@ -211,7 +211,7 @@ def run_ours(args, ws, rank, local, dist):
         eng.step()
     e0 = eng.conservation()
     pair_kernel = "pair_fp32" if args.precision == "fp32" else "pair_fp64"
-    names = [pair_kernel, "neighbor_count", "neighbors", "sum_density", "dt", "energy", "gradh", "radix_sort",
+    names = [pair_kernel, "neighbor_count", "neighbors", "neighbor_items", "sum_density", "dt", "energy", "gradh", "radix_sort",
              "permute", "update", "prepare_fp32", "enforce", "cell_keys", "bounds", "cell_ranges"]
     eng.profile(True)
     barrier(dist)

@@ -136,6 +136,9 @@ struct sphgpu_ctx {
   size_t cellSpace = 0;
   long long nnbr = 0;
   int nbCap = 0;             // slots per node of the warp-interleaved neighbour lists (0: not sized yet)
+  int nbCapNext = 0;         // smaller capacity to adopt at the next build (0: keep)
+  DBuf itemFlag, items;      // work items of the warp-cooperative neighbour search
+  int nItems = 0;
   bool haveNeighbors = false;
   // scratch
   DBuf scratch, small;
@@ -422,11 +425,31 @@ void buildNeighbors(sphgpu_ctx* c) {
     return m;
   };
   auto capFor = [](int m) { return std::max(32, ((m + m / 8 + 16 + 31) / 32) * 32); };
+  // work items: first node of every chunk of up to 32 nodes of a cell
+  c->itemFlag.ensure(n * sizeof(int));
+  c->items.ensure(n * sizeof(int));
+  {
+    Scope sc(c->prof, "neighbor_items");
+    long long* pos = c->nbrStart.as<long long>();
+    launchItemFlags(k, n, c->cellStart.as<int>(), c->itemFlag.as<int>(), c->stream, &c->lc);
+    scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, pos + n, c->stream, &c->lc);
+    launchItemFill(c->itemFlag.as<int>(), pos, n, c->items.as<int>(), c->stream, &c->lc);
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 41, pos + n, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    long long ni;
+    std::memcpy(&ni, c->hsmall + 41, sizeof(long long));
+    c->nItems = (int)ni;
+  }
+  c->check();
+  if (c->nbCapNext > 0) {   // adopt a smaller capacity decided at the previous build
+    c->nbCap = c->nbCapNext;
+    c->nbCapNext = 0;
+  }
   if (c->nbCap == 0) {   // first build: size the lists with a counting pass
     CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     Scope sc(c->prof, "neighbor_count");
-    launchNeighbors(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
-                    nullptr, 0, ext2, c->stream, &c->lc);
+    launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, g, c->cellStart.as<int>(),
+                        c->cellEnd.as<int>(), c->counts.as<int>(), dMax, nullptr, 0, ext2, c->stream, &c->lc);
     c->check();
     c->nbCap = capFor(readMax());
   }
@@ -435,13 +458,14 @@ void buildNeighbors(sphgpu_ctx* c) {
     CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     {
       Scope sc(c->prof, "neighbors");
-      launchNeighbors(c->F, c->f32(), n, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
-                      c->nbr.as<uint32_t>(), c->nbCap, ext2, c->stream, &c->lc);
+      launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, g, c->cellStart.as<int>(),
+                          c->cellEnd.as<int>(), c->counts.as<int>(), dMax, c->nbr.as<uint32_t>(), c->nbCap, ext2,
+                          c->stream, &c->lc);
     }
     c->check();
     const int m = readMax();
     if (m <= c->nbCap) {
-      if (capFor(m) * 2 < c->nbCap) c->nbCap = capFor(m);   // shrink on the next build
+      if (capFor(m) * 2 < c->nbCap) c->nbCapNext = capFor(m);   // shrink at the next build, not now
       break;
     }
     c->nbCap = capFor(m);   // overflow: enlarge and rebuild
@@ -609,9 +633,9 @@ double step(sphgpu_ctx* c, double maxTime) {
   if (c->cfg.compatible_energy) {
     Scope sc(c->prof, "energy");
     if (c->fp32()) {
-      c->v12.ensure(c->n * sizeof(double4));
-      launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<double4>(), dt,
-                                 c->stream, &c->lc);
+      c->v12.ensure(c->n * 2 * sizeof(float4));
+      launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<float4>(),
+                                 c->v12.as<float4>() + c->n, dt, c->stream, &c->lc);
     }
     else
       launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);
@@ -772,7 +796,7 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12};
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->itemFlag, &c->items};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);

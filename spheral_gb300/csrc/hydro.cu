@@ -144,6 +144,124 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
   atomicMax(maxCount, cnt);
 }
 
+// Warp-cooperative form of the same search.  One warp owns a chunk of up to
+// 32 consecutive nodes of one cell (an "item"), so the 27 candidate cells,
+// their offset codes and mirror flags are uniform across the warp.  Each
+// candidate cell is read in coalesced batches of 32 nodes that are broadcast
+// lane to lane; every lane tests its own node against the batch.  Candidates
+// are visited in the same order as neighborKernel, so the lists are identical.
+template <bool WRITE>
+__global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
+                                                          int nItems, Grid g, const int* __restrict__ cellStart,
+                                                          const int* __restrict__ cellEnd, int* __restrict__ counts,
+                                                          uint32_t* __restrict__ nbr, double ext2, float bandLo,
+                                                          float bandHi, int cap, int* __restrict__ maxCount) {
+  const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (item >= nItems) return;   // warp-uniform
+  const int k0 = items[item];
+  const uint32_t cc = P.cell[k0];
+  int hc[3];
+  unpackCell(cc, hc);
+  const uint32_t homeKey = morton3((uint32_t)hc[0], (uint32_t)hc[1], (uint32_t)hc[2]);
+  const int k1 = min(k0 + 32, cellEnd[homeKey]);
+  const long i = k0 + lane;
+  const bool active = i < k1;
+  const float4 pi = active ? P.posh[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float ai2 = pi.w * pi.w;
+  const uint32_t mm = mirrorMask(g, hc);
+  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  int cnt = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int d[3] = {dx, dy, dz};
+        int cell[3];
+        int dcode = 0;
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          int nn = hc[a] + d[a];
+          if (d[a] != 0) dcode |= (d[a] < 0 ? 1 : 2) << (2 * a);
+          if (nn < 0) {
+            if (g.kindLo[a] == AXIS_PERIODIC) nn = g.nc[a] - 1;
+            else if (g.kindLo[a] == AXIS_REFLECT) nn = 0;
+            else ok = false;
+          } else if (nn >= g.nc[a]) {
+            if (g.kindHi[a] == AXIS_PERIODIC) nn = 0;
+            else if (g.kindHi[a] == AXIS_REFLECT) nn = g.nc[a] - 1;
+            else ok = false;
+          }
+          cell[a] = nn;
+        }
+        if (!ok) continue;
+        const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
+        const int s = cellStart[key], e = cellEnd[key];
+        const uint32_t mir = (uint32_t)dcode & mm;
+        const int d0 = dcode & 3, d1 = (dcode >> 2) & 3, d2 = (dcode >> 4) & 3;
+        const float ox = d0 == 1 ? cx : (d0 == 2 ? -cx : 0.0f);
+        const float oy = d1 == 1 ? cy : (d1 == 2 ? -cy : 0.0f);
+        const float oz = d2 == 1 ? cz : (d2 == 2 ? -cz : 0.0f);
+        for (int base = s; base < e; base += 32) {
+          const int jj = base + lane;
+          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (jj < e) q = P.posh[jj];
+          if (mir) {
+            if (mir & 3u) q.x = cx - q.x;
+            if (mir & 12u) q.y = cy - q.y;
+            if (mir & 48u) q.z = cz - q.z;
+          }
+          const int nval = min(32, e - base);
+          for (int t = 0; t < nval; ++t) {
+            const float xj = __shfl_sync(0xffffffffu, q.x, t);
+            const float yj = __shfl_sync(0xffffffffu, q.y, t);
+            const float zj = __shfl_sync(0xffffffffu, q.z, t);
+            const float aj = __shfl_sync(0xffffffffu, q.w, t);
+            const int j = base + t;
+            if (!active || (j == (int)i && dcode == 0)) continue;
+            const float rx = __fadd_rn(__fsub_rn(pi.x, xj), ox);
+            const float ry = __fadd_rn(__fsub_rn(pi.y, yj), oy);
+            const float rz = __fadd_rn(__fsub_rn(pi.z, zj), oz);
+            const float r2 = rx * rx + ry * ry + rz * rz;
+            const float e2 = fminf(ai2, aj * aj) * r2;
+            bool inside;
+            if (e2 < bandLo) inside = true;
+            else if (e2 > bandHi) inside = false;
+            else {
+              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+              imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                           qz = __dsub_rn(F.f[F_Z][i], zjd);
+              inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+            }
+            if (inside) {
+              if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
+              ++cnt;
+            }
+          }
+        }
+      }
+  if (active) {
+    counts[i] = cnt;
+    atomicMax(maxCount, cnt);
+  }
+}
+
+// Items of the warp search: the first node of every chunk of up to 32 nodes
+// of a cell.  flag pass + scan + fill.
+__global__ void itemFlagKernel(const uint32_t* __restrict__ keys, long n, const int* __restrict__ cellStart,
+                               int* __restrict__ flag) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  flag[k] = ((k - cellStart[keys[k]]) % 32 == 0) ? 1 : 0;
+}
+__global__ void itemFillKernel(const int* __restrict__ flag, const long long* __restrict__ pos, long n,
+                               int* __restrict__ items) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  if (flag[k]) items[pos[k]] = (int)k;
+}
+
 //------------------------------------------------------------------------------
 // computeSPHSumMassDensity (src/SPH/computeSPHSumMassDensity.cc:15-87),
 // gathered: rho_i = m_i W(0) Hdet_i + sum_j m W(|Hj ri - Hj rj|, Hdet_j) with
@@ -830,6 +948,31 @@ void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long 
 }
 void launchCountsOut(const int* counts, const int* orig, double* stage, long n, cudaStream_t s, LaunchCounter* lc) {
   countsOutKernel<<<gridFor(n, 256), 256, 0, s>>>(counts, orig, stage, n);
+  lc->add(1);
+}
+
+void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int* flag, cudaStream_t s,
+                     LaunchCounter* lc) {
+  itemFlagKernel<<<gridFor(n, 256), 256, 0, s>>>(keys, n, cellStart, flag);
+  lc->add(1);
+}
+void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc) {
+  itemFillKernel<<<gridFor(n, 256), 256, 0, s>>>(flag, pos, n, items);
+  lc->add(1);
+}
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, Grid g,
+                         const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
+                         double ext2, cudaStream_t s, LaunchCounter* lc) {
+  float lo, hi;
+  neighborBand(g, ext2, lo, hi);
+  const long threads = (long)nItems * 32;
+  const unsigned gb = (unsigned)((threads + 127) / 128);
+  if (nbr)
+    neighborWarpKernel<true><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts, nbr, ext2, lo,
+                                                 hi, cap, maxCount);
+  else
+    neighborWarpKernel<false><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts, nullptr, ext2,
+                                                  lo, hi, 0, maxCount);
   lc->add(1);
 }
 

@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
   const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
   const float4 pi = P.posh[i];
   const float mi = P.velm[i].w;
-  const int li = list[i];
+  const bool multi = hp.numLists > 1;
+  const int li = multi ? list[i] : 0;
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   float s = 0.f, c = 0.f;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
     if (eta < extent) {
       const int i0 = 3 * min(N1, (int)(eta * invStep));
       const float w = (aj * aj * aj) * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
-      kahanAdd(s, c, (list[j] == li ? P.velm[j].w : mi) * w);
+      kahanAdd(s, c, ((multi ? list[j] == li : true) ? P.velm[j].w : mi) * w);
     }
   }
   const double a = F.f[F_HINV][i];
@@ -404,45 +405,55 @@ __global__ void dtFinalKernel32(const double* __restrict__ part, int nb, double*
 // to FP32 and the FP32 pair acceleration; the weighted shares are summed and
 // applied to the specific energy in FP64.
 //------------------------------------------------------------------------------
-__global__ void halfStepVelocityKernel(Fields F, long n, double hdt, double4* __restrict__ v12) {
+__global__ void halfStepVelocityKernel(Fields F, long n, double hdt, float4* __restrict__ vhi,
+                                       float4* __restrict__ vlo) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  v12[i] = make_double4(F.f[F_VX][i] + F.f[F_DVDT_X][i] * hdt, F.f[F_VY][i] + F.f[F_DVDT_Y][i] * hdt,
-                        F.f[F_VZ][i] + F.f[F_DVDT_Z][i] * hdt, F.f[F_DEPSDT][i]);
+  // v12 = v + a dt/2 in FP64, stored as an unevaluated float pair hi + lo
+  const double x = F.f[F_VX][i] + F.f[F_DVDT_X][i] * hdt;
+  const double y = F.f[F_VY][i] + F.f[F_DVDT_Y][i] * hdt;
+  const double z = F.f[F_VZ][i] + F.f[F_DVDT_Z][i] * hdt;
+  const float hx = (float)x, hy = (float)y, hz = (float)z;
+  vhi[i] = make_float4(hx, hy, hz, (float)F.f[F_DEPSDT][i]);
+  vlo[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.0f);
 }
 
 __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, NeighborLists nl,
-                                                      const double4* __restrict__ v12, const float* __restrict__ pacc,
-                                                      double dt) {
+                                                      const float4* __restrict__ vhi, const float4* __restrict__ vlo,
+                                                      const float* __restrict__ pacc, double dt) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   int ci[3];
   unpackCell(nl.cell[i], ci);
   const uint32_t mm = mirrorMask(g, ci);
-  const double4 vi = v12[i];
-  const float d0i = (float)vi.w;
+  const float4 hi = vhi[i], lo = vlo[i];
+  const float d0i = hi.w;
   const float feps = (float)DBL_EPSILON;
-  double sum = 0.0;
+  float s = 0.0f, c = 0.0f;
   const int cnt = nl.count[i];
   for (int q = 0; q < cnt; ++q) {
     const long long k = nbSlot(i, q, nl.cap);
     const uint32_t ent = nl.nbr[k];
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
-    const double4 vj = v12[j];
-    double vxj = vj.x, vyj = vj.y, vzj = vj.z;
+    const float4 hj = vhi[j], lj = vlo[j];
+    float hx = hj.x, hy = hj.y, hz = hj.z, lx = lj.x, ly = lj.y, lz = lj.z;
     const uint32_t mir = (uint32_t)dcode & mm;
     if (mir) {
-      if (mir & 3u) vxj = -vxj;
-      if (mir & 12u) vyj = -vyj;
-      if (mir & 48u) vzj = -vzj;
+      if (mir & 3u) { hx = -hx; lx = -lx; }
+      if (mir & 12u) { hy = -hy; ly = -ly; }
+      if (mir & 48u) { hz = -hz; lz = -lz; }
     }
-    const float wx = (float)(vxj - vi.x), wy = (float)(vyj - vi.y), wz = (float)(vzj - vi.z);
+    // (hi_j - hi_i) + (lo_j - lo_i): the FP64 difference to FP32 rounding
+    const float wx = __fadd_rn(__fsub_rn(hx, hi.x), __fsub_rn(lx, lo.x));
+    const float wy = __fadd_rn(__fsub_rn(hy, hi.y), __fsub_rn(ly, lo.y));
+    const float wz = __fadd_rn(__fsub_rn(hz, hi.z), __fsub_rn(lz, lo.z));
     const float du = __fmaf_rn(wz, pacc[3 * k + 2], __fmaf_rn(wy, pacc[3 * k + 1], __fmul_rn(wx, pacc[3 * k])));
     const float sg = du < 0.0f ? -1.0f : 1.0f;
     const float weighti = fmaxf(feps, d0i * sg);
-    const float weightj = fmaxf(feps, (float)vj.w * sg);
-    sum += (double)(weighti / (weighti + weightj) * du);
+    const float weightj = fmaxf(feps, hj.w * sg);
+    kahanAdd(s, c, __fdividef(weighti, weighti + weightj) * du);
   }
+  const double sum = kahanValue(s, c);
   F.f[F_DEPS_COMPAT][i] = sum;
   F.f[F_EPS][i] += sum * dt;
 }
@@ -506,10 +517,10 @@ void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Neigh
   lc->add(2);
 }
 
-void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, double4* v12,
-                                double dt, cudaStream_t s, LaunchCounter* lc) {
-  halfStepVelocityKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, 0.5 * dt, v12);
-  energyKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, v12, pacc, dt);
+void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
+                                float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc) {
+  halfStepVelocityKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, 0.5 * dt, vhi, vlo);
+  energyKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
   lc->add(2);
 }
 

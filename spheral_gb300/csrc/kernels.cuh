@@ -42,6 +42,12 @@ void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* c
 void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
                      int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,
                      LaunchCounter* lc);
+// Warp-cooperative search over items (first node of each <= 32-node chunk of a cell).
+void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int* flag, cudaStream_t s, LaunchCounter* lc);
+void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc);
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, Grid g,
+                         const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
+                         double ext2, cudaStream_t s, LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -67,8 +73,8 @@ void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, Hydro
               cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
                             double dt, cudaStream_t s, LaunchCounter* lc);
-void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, double4* v12,
-                                double dt, cudaStream_t s, LaunchCounter* lc);
+void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
+                                float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc);
 void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
