@@ -561,12 +561,14 @@ void evalDerivs(sphgpu_ctx* c) {
 }
 
 // Integrator::selectDt (src/Integrator/Integrator.cc:116-169).
-double packageDt(sphgpu_ctx* c, int* reason) {
+// fusedDone: the mixed-mode density sweep already left the dt vote in small[0..1].
+double packageDt(sphgpu_ctx* c, int* reason, bool fusedDone = false) {
   Scope sc(c->prof, "dt");
   const long nb = (c->n + 127) / 128;
   c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
   double* d = c->small.as<double>();
-  if (c->fp32())
+  if (fusedDone) {
+  } else if (c->fp32())
     launchDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(),
                  c->scratch.as<double>(), (int)(2 * nb), d, c->stream, &c->lc);
   else
@@ -585,10 +587,10 @@ double packageDt(sphgpu_ctx* c, int* reason) {
   return dt;
 }
 
-double selectDt(sphgpu_ctx* c, double dtMin, double dtMax) {
+double selectDt(sphgpu_ctx* c, double dtMin, double dtMax, bool fusedDone = false) {
   double dt = dtMax;
   int r;
-  const double v = packageDt(c, &r);
+  const double v = packageDt(c, &r, fusedDone);
   if (v > 0.0 && v < dt) dt = v;
   dt *= c->dtMultiplier;
   dt = std::min(dt, c->cfg.dt_growth * c->lastDt);
@@ -612,9 +614,22 @@ double step(sphgpu_ctx* c, double maxTime) {
   requireState(c);
   refreshParams(c);
   buildNeighbors(c);                                 // Integrator::setGhostNodes + connectivity
-  if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) sumDensity(c);   // preStepInitialize
+  bool fused = false;
+  if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
+    if (c->fp32()) {
+      Scope sc(c->prof, "density_dt");
+      const long nb = (c->n + 127) / 128;
+      c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
+      launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+                          c->maxNperh(), c->scratch.as<double>(), c->small.as<double>(), c->stream, &c->lc);
+      c->check();
+      fused = true;
+    } else {
+      sumDensity(c);
+    }
+  }
   const double t = c->time;
-  const double dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t));
+  const double dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t), fused);
   const double hdt = 0.5 * dt;
   {
     Scope sc(c->prof, "update");

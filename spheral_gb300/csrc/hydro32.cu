@@ -271,6 +271,97 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
 }
 
 //------------------------------------------------------------------------------
+// Fused start-of-step sweep of the mixed mode: the density sum
+// (computeSPHSumMassDensity.cc:15-87) and the time-step vote
+// (GenericHydro.cc:113-381, pairwise velocity limit on the same neighbour
+// data, node limits with the new density) in one pass over the lists.
+//------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n,
+                                                         Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                                                         double maxNperh, double* __restrict__ part) {
+  __shared__ float tw[kMaxTable];
+  __shared__ double sv[128];
+  __shared__ int sr[128];
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) tw[k] = t.w32[k];
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  double best = DBL_MAX;
+  int reason = -1;
+  if (i < n) {
+    int ci[3];
+    unpackCell(P.cell[i], ci);
+    const uint32_t mm = mirrorMask(g, ci);
+    const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+    const float4 pi = P.posh[i], vi = P.velm[i];
+    const float mi = vi.w;
+    const bool multi = hp.numLists > 1;
+    const int li = multi ? list[i] : 0;
+    const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
+    const int N1 = hp.tableN1;
+    const float hi = 1.0f / pi.w;
+    float s = 0.f, c = 0.f, bestPair = 3.0e38f;
+    const int cnt = nl.count[i];
+    for (int q = 0; q < cnt; ++q) {
+      const long long k = nbSlot(i, q, nl.cap);
+      const uint32_t ent = nl.nbr[k];
+      const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+      const float4 pj = P.posh[j], vj = P.velm[j];
+      float rx, ry, rz;
+      relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
+      const float aj = pj.w;
+      const float eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+      if (eta < extent) {
+        const int i0 = 3 * min(N1, (int)(eta * invStep));
+        const float w = (aj * aj * aj) * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
+        kahanAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w);
+      }
+      float vxj = vj.x, vyj = vj.y, vzj = vj.z;
+      mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
+      const float dx = vi.x - vxj, dy = vi.y - vyj, dz = vi.z - vzj;
+      const float hmin = fminf(hi, 1.0f / aj);
+      bestPair = fminf(bestPair, hmin / fmaxf(1.0e-30f, sqrtf(dx * dx + dy * dy + dz * dz)));
+    }
+    const double a = F.f[F_HINV][i];
+    const double rho = F.f[F_MASS][i] * (((a * a) * a) * hp.W0) + kahanValue(s, c);
+    F.f[F_RHO][i] = rho;
+    P.thermo[i].x = (float)rho;
+    // node limits
+    const double tiny = DBL_EPSILON;
+    const NodeListParams L = cLists[multi ? li : list[i]];
+    const double nodeScalei = 1.0 / a / L.nPerh;
+    const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
+    const double csDt = nodeScalei / (F.f[F_CS][i] + tiny);
+    if (csDt < best) { best = csDt; reason = 0; }
+    const double csqDt = nodeScalei / (sqrt(F.f[F_MAXQ][i] / rho) + tiny);
+    if (csqDt < best) { best = csqDt; reason = 1; }
+    const double divvDt = 1.0 / (fabs(F.f[F_DVDX_XX][i] + F.f[F_DVDX_YY][i] + F.f[F_DVDX_ZZ][i]) + tiny);
+    if (divvDt < best) { best = divvDt; reason = 2; }
+    const double vmag = sqrt(vxi * vxi + vyi * vyi + vzi * vzi);
+    const double ax = F.f[F_DVDT_X][i], ay = F.f[F_DVDT_Y][i], az = F.f[F_DVDT_Z][i];
+    const double dtAcc = 0.1 * fmax(nodeScalei / (vmag + tiny), vmag / (sqrt(ax * ax + ay * ay + az * az) + tiny));
+    if (dtAcc < best) { best = dtAcc; reason = 3; }
+    if (hp.useVelMagDt) {
+      const double velDt = nodeScalei / (vmag + 1.0e-10);
+      if (velDt < best) { best = velDt; reason = 4; }
+    }
+    const double pairDt = (double)bestPair / maxNperh;
+    if (pairDt < best) { best = pairDt; reason = 5; }
+  }
+  sv[threadIdx.x] = best;
+  sr[threadIdx.x] = reason;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && sv[threadIdx.x + o] < sv[threadIdx.x]) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      sr[threadIdx.x] = sr[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = sv[0]; part[2 * blockIdx.x + 1] = (double)sr[0]; }
+}
+
+//------------------------------------------------------------------------------
 // Grad-h correction, FP32 sums (computeSPHOmegaGradhCorrection.cc:15-116).
 //------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl,
@@ -521,6 +612,16 @@ void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, cons
                                 float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc) {
   halfStepVelocityKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, 0.5 * dt, vhi, vlo);
   energyKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
+  lc->add(2);
+}
+
+void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                         HydroParams hp, const NodeListParams* lists, double maxNperh, double* dScratch,
+                         double* dOut, cudaStream_t s, LaunchCounter* lc) {
+  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+  const int nb = (int)gridFor(n, 128);
+  densityDtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
 }
 

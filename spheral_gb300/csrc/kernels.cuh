@@ -67,6 +67,10 @@ void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, T
 void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
                   const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
                   cudaStream_t s, LaunchCounter* lc);
+// Mixed mode: density sum and dt vote fused in one sweep (dOut as launchDt).
+void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                         HydroParams hp, const NodeListParams* lists, double maxNperh, double* dScratch,
+                         double* dOut, cudaStream_t s, LaunchCounter* lc);
 // dt: writes per-block (value, reason) pairs then a final min into dOut[0], dOut[1] (reason as double)
 void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
               const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
