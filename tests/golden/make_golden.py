@@ -1,0 +1,40 @@
+"""Generate the golden Sod profiles from the reference's own analytic solution.
+
+Runs only where the reference source tree is available (it imports
+tests/functional/Hydro/Sod/SodAnalyticSolution.py from it, a pure-Python
+module); the output, sod_analytic.npz, is committed and read by the tests.
+
+Configuration: the 3-D planar Sod tube of spheral_gb300.problems.sod (x in
+[0, 2], interface at x = 1, rho 1 / 0.25, P 1 / 0.1795, gamma 5/3), profiles
+of density, velocity, specific energy and pressure at t = 0.05, 0.10, 0.15
+on 401 points.
+"""
+import os
+import sys
+
+import numpy as np
+
+REF = "/root/reference/tests/functional/Hydro/Sod"
+
+
+def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analytic.npz")):
+    sys.path.insert(0, REF)
+    from SodAnalyticSolution import SodSolutionGasGas
+    g = 5.0 / 3.0
+    x = [2.0 * k / 400.0 for k in range(401)]
+    data = {"x": np.array(x)}
+    for t in (0.05, 0.10, 0.15):
+        sol = SodSolutionGasGas(nPoints=401, gamma1=g, gamma2=g, rho1=1.0, P1=1.0, rho2=0.25, P2=0.1795,
+                                x0=0.0, x1=1.0, x2=2.0, h1=0.01, h2=0.01)
+        xs, v, u, rho, P, h, gam = sol.solution(t, list(x))
+        key = "t%.2f" % t
+        data[key + "_rho"] = np.array(rho)
+        data[key + "_v"] = np.array(v)
+        data[key + "_u"] = np.array(u)
+        data[key + "_P"] = np.array(P)
+    np.savez(out, **data)
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    main()

@@ -145,3 +145,47 @@ def test_small_periodic_box_rejected(native_lib):
     with pytest.raises(_native.SphGpuError) as e:
         eng.initialize()
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sod_against_reference_analytic_solution(native_lib, oracle_mod, precision):
+    """GPU Sod tube to t = 0.1 against the reference's analytic solution
+    (golden fixture) and, in FP64, against the oracle run of the same steps."""
+    import os
+    from spheral_gb300.engine import Engine
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "sod_analytic.npz"))
+    p = problems.sod(nx1=16, ny1=20)
+    eng = Engine.from_problem(p, precision=precision)
+    eng.initialize()
+    steps = 0
+    while eng.time < 0.10 - 1e-12:
+        eng.step(0.10)
+        steps += 1
+    x = eng.field("position")[:, 0]
+    rho = eng.field("massDensity")
+    l1 = float(np.mean(np.abs(rho - np.interp(x, d["x"], d["t0.10_rho"]))))
+    assert l1 < 0.02, l1
+    if precision == "fp64":
+        orc = oracle_mod.Oracle(p)
+        orc.initialize()
+        for _ in range(steps):
+            orc.step(0.10)
+        bad = compare_fields(eng, orc, ["position", "velocity", "massDensity", "specificThermalEnergy"], 1e-8)
+        assert not bad, bad
+
+
+def test_nonfinite_state_reported(native_lib):
+    """Host-side fault injection: a non-finite specific energy must surface as
+    SPHGPU_E_NAN from the step, not as silent propagation."""
+    from spheral_gb300 import _native
+    from spheral_gb300.engine import Engine
+    p = problems.random_box(n_side=12, seed=3)
+    eng = Engine.from_problem(p)
+    eng.initialize()
+    eps = eng.field("specificThermalEnergy")
+    eps[17] = np.nan
+    eng.set_field("specificThermalEnergy", eps)
+    with pytest.raises(_native.SphGpuError) as e:
+        eng.step()
+        eng.step()
+    assert e.value.code == 5

@@ -167,3 +167,25 @@ def test_oracle_compatible_energy_conserves(oracle_mod, bc):
     if bc == "periodic":
         scale = np.sum(p.mass * np.linalg.norm(p.vel, axis=1))
         assert np.all(np.abs(c1[1:4] - c0[1:4]) <= 1.0e-12 * scale)
+
+
+def _sod_l1(field_x, field_rho, t):
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "sod_analytic.npz"))
+    ra = np.interp(field_x, d["x"], d["t%.2f_rho" % t])
+    return float(np.mean(np.abs(field_rho - ra)))
+
+
+def test_oracle_sod_matches_reference_analytic_solution(oracle_mod):
+    """CheapRK2 + compatible-energy SPH on the 3-D Sod tube against the
+    reference's analytic Riemann solution (tests/golden/sod_analytic.npz,
+    from tests/functional/Hydro/Sod/SodAnalyticSolution.py): mean |rho - rho_exact|
+    over the nodes at t = 0.1 below 0.02 (measured 0.007 at this resolution)."""
+    p = problems.sod(nx1=16, ny1=20)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    while o.time < 0.10 - 1e-12:
+        o.step(0.10)
+    assert abs(o.time - 0.10) < 1e-12
+    l1 = _sod_l1(o.field("position")[:, 0], o.field("massDensity"), 0.10)
+    assert l1 < 0.02, l1
