@@ -227,6 +227,25 @@ int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
 /* Wait for all work on the handle's stream. */
 int sphgpu_synchronize(sphgpu_handle h);
 
+/* Allocation-free conserved totals.  This entry point has no counterpart in
+ * the reference; it exists for callers that cannot allocate GPU memory while
+ * they run -- codes that hand the library slices of their own pre-allocated
+ * device pools, code inside regions where an allocation would synchronise the
+ * device, drivers whose footprint must stay fixed once started.  It computes
+ * the same {mass, px, py, pz, kinetic, thermal, 1/2 sum m phi, total} as
+ * sphgpu_conservation from caller device arrays (mass[n], vel[3n] in Vector
+ * layout, eps[n], pot[n] or NULL) into the caller device array out[8], and
+ * calls no cudaMalloc, cudaFree or allocating library routine.  Its scratch is
+ * a fixed 57,344-byte array inside the library that every GPU loading the
+ * library holds until the process exits and that all calls on a device share:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device looks up the scratch address (make it before any
+ * stream capture).  n must be 1..67,108,864 (SPHGPU_E_OVERFLOW above that,
+ * SPHGPU_E_ARG for n <= 0 or null pointers).  Work is queued on `stream` (a
+ * cudaStream_t, NULL for the default stream) and is not waited for. */
+int sphgpu_conservation_noalloc(const double* mass, const double* vel, const double* eps, const double* pot, long n,
+                                double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
