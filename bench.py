@@ -1,7 +1,7 @@
 """Benchmark: SPH pair-interactions/s of the CheapSynchronousRK2 hydro step.
 
 Workload (default): 3-D Kelvin-Helmholtz in a periodic unit cube, two
-lattices of 112 and 140 nodes per unit length (2,074,464 nodes, the nearest
+lattices of 112 and 142 nodes per unit length (2,134,108 nodes, the nearest
 two-lattice set to 128^3 with a 2^(-1/3) spacing ratio), nPerh 1.51, Monaghan-
 Gingold Q (Cl = Cq = 1), compatible energy, RigorousSumDensity, CFL 0.5.  One
 step = one full CheapSynchronousRK2 step (neighbour build, density sum, dt,
@@ -131,6 +131,10 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
+def make_workload_name(args):
+    return None, {"kh": "kelvin_helmholtz_3d", "sweep": "sweep_box", "sod": "sod_planar_3d"}[args.workload]
+
+
 def make_workload(args):
     from spheral_gb300 import problems
     if args.workload == "kh":
@@ -142,7 +146,7 @@ def make_workload(args):
     raise SystemExit("unknown workload")
 
 
-def cpu_baseline(args, threads=None):
+def cpu_baseline(args, steps=None, warmup=1):
     """Oracle CheapRK2 steps on a bounded sample of the workload (same
     generator, smaller lattice); returns pairs/s and the sample description."""
     from oracle import oracle as orc
@@ -156,8 +160,9 @@ def cpu_baseline(args, threads=None):
         p = problems.sod(nx1=args.cpu_n1)
     o = orc.Oracle(p)
     o.initialize()
-    o.step()   # warm-up step (first step allocates)
-    steps = args.cpu_steps
+    for _ in range(max(1, warmup)):   # the first step allocates
+        o.step()
+    steps = args.cpu_steps if steps is None else steps
     t0 = time.perf_counter()
     pairs = 0
     for _ in range(steps):
@@ -171,15 +176,16 @@ def cpu_baseline(args, threads=None):
 def run_reference(args, ws, rank, dist):
     if rank != 0:
         return
-    val, info = cpu_baseline(args)
+    val, info = cpu_baseline(args, steps=args.steps, warmup=args.warmup)
     sample = (f"{info['steps']} CheapSynchronousRK2 steps of the same generator at n1={args.cpu_n1} "
               f"({info['n']} nodes, {info['pairs_per_step']:.0f} pairs/step), {info['seconds']:.1f} s")
+    _, wname = make_workload_name(args)
     line = {
-        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": info["steps"], "warmup": 1,
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": info["steps"], "warmup": args.warmup,
         "ms_per_step": 1e3 * info["seconds"] / info["steps"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "impl": "reference",
-        "config": {"workload": "kelvin_helmholtz_3d" if args.workload == "kh" else args.workload,
-                   "sample_n": info["n"]},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, no external data)",
+        "impl": "reference",
+        "config": {"workload": wname, "sample_n": info["n"], "sample_n1": args.cpu_n1},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": sample},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -211,7 +217,8 @@ def run_ours(args, ws, rank, local, dist):
         eng.step()
     e0 = eng.conservation()
     pair_kernel = "pair_fp32" if args.precision == "fp32" else "pair_fp64"
-    names = [pair_kernel, "neighbor_count", "neighbors", "neighbor_items", "sum_density", "dt", "energy", "gradh", "radix_sort",
+    names = [pair_kernel, "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt", "energy",
+             "gradh", "radix_sort",
              "permute", "update", "prepare_fp32", "enforce", "cell_keys", "bounds", "cell_ranges"]
     eng.profile(True)
     barrier(dist)
@@ -328,8 +335,8 @@ def main():
     ap.add_argument("--neighbors", type=int, default=64)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--cpu-n1", type=int, default=40)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-n1", type=int, default=56)
+    ap.add_argument("--cpu-steps", type=int, default=6)
     args = ap.parse_args()
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
