@@ -37,6 +37,11 @@ METRIC = "SPH pair-interactions/sec at stated energy error: mixed vs FP64 GPU vs
 UNIT = "pair-interactions/s"
 FLOP_PER_PAIR = 456        # algorithmic FLOPs of the reference pair body per unordered pair
 VALUES_PER_NODE = 63       # per-node state read + derivatives written by the pair loop
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unordered pair
+# of one pairKernelFP32 launch, from an ncu --set full capture of
+# kelvin_helmholtz(n1=64) (862 MB for 21.76 M pairs); traffic grows in
+# proportion to the pairs, so it is scaled by the pairs of the launch.
+TRAFFIC_BYTES_PER_PAIR = {"fp32": 39.6}
 
 
 def peaks():
@@ -62,7 +67,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -307,7 +312,10 @@ def run_ours(args, ws, rank, local, dist):
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved_gbs / hbm) if achieved_gbs else None, "traffic": None,
+                     "frac": (achieved_gbs / hbm) if achieved_gbs else None,
+                     "traffic": (TRAFFIC_BYTES_PER_PAIR[args.precision] * pairs_per_launch
+                                 if args.precision in TRAFFIC_BYTES_PER_PAIR else None),
+                     "traffic_source": "ncu capture at n1=64 scaled by pairs per launch",
                      "peak_kind": peak_kind, "kernel": pair_kernel,
                      "algorithmic_bytes_per_pair": b_pair, "pairs_per_launch": pairs_per_launch,
                      "avg_launch_ms": avg_ms},
@@ -326,7 +334,7 @@ def run_ours(args, ws, rank, local, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod"])

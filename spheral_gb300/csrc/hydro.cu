@@ -102,8 +102,8 @@ template <bool WRITE>
 __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long n, Grid g,
                                                       const int* __restrict__ cellStart,
                                                       const int* __restrict__ cellEnd, int* __restrict__ counts,
-                                                      uint32_t* __restrict__ nbr, double ext2, float bandLo,
-                                                      float bandHi, int cap, int* __restrict__ maxCount) {
+                                                      uint32_t* __restrict__ nbr, double ext2, float bandA,
+                                                      float bandB, int cap, int* __restrict__ maxCount) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* __restrict__ X = F.f[F_X];
@@ -114,6 +114,10 @@ __global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long
   int ci[3];
   unpackCell(cc, ci);
   const float4 pi = P.posh[i];
+  const float del = __fmaf_rn(bandA, pi.w, bandB);   // per-node band half-width (relative)
+  const float e2t = (float)ext2;
+  const float bandLo = del < 0.5f ? e2t * (1.0f - del) : -1.0f;
+  const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
   const float cellx = (float)g.cell[0], celly = (float)g.cell[1], cellz = (float)g.cell[2];
   const uint32_t mm = mirrorMask(g, ci);
   int cnt = 0;
@@ -154,8 +158,8 @@ template <bool WRITE>
 __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
-                                                          uint32_t* __restrict__ nbr, double ext2, float bandLo,
-                                                          float bandHi, int cap, int* __restrict__ maxCount) {
+                                                          uint32_t* __restrict__ nbr, double ext2, float bandA,
+                                                          float bandB, int cap, int* __restrict__ maxCount) {
   const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (item >= nItems) return;   // warp-uniform
@@ -169,6 +173,10 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const bool active = i < k1;
   const float4 pi = active ? P.posh[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float ai2 = pi.w * pi.w;
+  const float del = __fmaf_rn(bandA, pi.w, bandB);   // per-node band half-width (relative)
+  const float e2t = (float)ext2;
+  const float bandLo = del < 0.5f ? e2t * (1.0f - del) : -1.0f;
+  const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
   int cnt = 0;
@@ -832,12 +840,21 @@ void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* c
   cellRangeKernel<<<gridFor(n, 256), 256, 0, s>>>(sortedKeys, n, cellStart, cellEnd);
   lc->add(1);
 }
-// Band of the FP32 pre-filter on (H r)^2 around ext^2 = 4: wide enough for
-// the FP32 rounding of cell-relative separations (<= ~4e-7 of a cell).
-static void neighborBand(const Grid& g, double ext2, float& lo, float& hi) {
-  (void)g;
-  lo = (float)(ext2 * (1.0 - 2.0e-3));
-  hi = (float)(ext2 * (1.0 + 2.0e-3));
+// Band of the FP32 pre-filter on e2 = min(a_i, a_j)^2 r^2 around ext^2
+// (a = 1/h).  Every cell-relative coordinate is within about one cell size C
+// of its cell origin, so each FP32 separation component carries at most
+// ~10 u C of rounding (u = 2^-24: the cell-relative positions, the mirror,
+// the difference and the periodic offset), and near the threshold
+// (a r ~ ext) |e2_fp32 - e2| <= ext^2 (20 sqrt(3) u C a / ext + 7 u).  The
+// band used is four times that bound, evaluated with a = a_i >= min(a_i, a_j):
+// delta_i = bandA a_i + bandB.  A node whose delta reaches 1/2 takes the exact
+// test on every candidate.
+static void neighborBand(const Grid& g, double ext2, float& bandA, float& bandB) {
+  const double u = 1.0 / 16777216.0;
+  const double cmax = std::max(g.cell[0], std::max(g.cell[1], g.cell[2]));
+  const double ext = std::sqrt(ext2);
+  bandA = (float)(4.0 * 20.0 * std::sqrt(3.0) * u * cmax / ext);
+  bandB = (float)(4.0 * 7.0 * u);
 }
 void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
                      int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,

@@ -228,11 +228,13 @@ def sweep_box(n_side=256, neighbors=64, seed=5, jitter=0.1):
                    meta=dict(n_side=n_side, neighbors=neighbors, seed=seed))
 
 
-def random_box(n_side=12, seed=11, nPerh=1.51, jitter=0.2, vel_scale=0.3, boundaries="periodic", two_lists=False):
+def random_box(n_side=12, seed=11, nPerh=1.51, jitter=0.2, vel_scale=0.3, boundaries="periodic", two_lists=False,
+               gravity=False):
     """Small irregular test box: jittered lattice, 20% mass noise, random
     velocities and energies, per-node h noise, so every derivative term is
     non-trivial.  boundaries: 'periodic' (all axes), 'reflecting' (walls on
-    x, periodic y z) or 'open'."""
+    x, periodic y z) or 'open'.  gravity: add TreeGravity (G = 1, opening
+    0.5, softening 0.01; meaningful with open boundaries only)."""
     rng = np.random.default_rng(seed)
     d = 1.0 / n_side
     pos = _lattice(n_side, n_side, n_side, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
@@ -257,6 +259,8 @@ def random_box(n_side=12, seed=11, nPerh=1.51, jitter=0.2, vel_scale=0.3, bounda
         bcs = []
     cfg = dict(cfl=0.25, compatible_energy=True, gradh_correction=True, xsph=False, correct_velocity_gradient=True,
                Cl=1.0, Cq=1.0, dt_min=0.0, dt_max=0.1, dt_growth=2.0, last_dt=1.0e-3)
+    if gravity:
+        cfg.update(gravity=True, G=1.0, softening=0.01, opening=0.5, ftimestep=0.1)
     nodelist = None
     nls = [dict(nPerh=nPerh, hmin=1e-6, hmax=0.5, rhoMin=1e-10, rhoMax=1e10, gamma=GAMMA)]
     if two_lists:
