@@ -268,6 +268,36 @@ def run_ours(args, ws, rank, local, dist):
                 "ms_per_step": ms64 / args.fp64_steps}
         e64.close()
 
+    # Energy-conservation error of the mixed-precision run over a long run:
+    # keep stepping the same engine to energy_steps steps after warm-up.
+    done = args.steps + args.e2e_steps
+    for _ in range(max(0, args.energy_steps - done)):
+        eng.step()
+    e_end = eng.conservation()
+    long_steps = max(done, args.energy_steps)
+    long_err = abs(e_end[7] - e0[7]) / abs(e0[7])
+
+    # Optional accuracy comparison: fresh FP32 and FP64 runs of the same
+    # problem for the same number of steps.
+    compare = None
+    if args.fp64_compare_steps > 0 and args.precision == "fp32":
+        runs = {}
+        for prec in ("fp32", "fp64"):
+            e = Engine.from_problem(prob, precision=prec, device=local)
+            e.initialize()
+            c0 = e.conservation()
+            e.advance(args.fp64_compare_steps)
+            c1 = e.conservation()
+            runs[prec] = dict(rho=e.field("massDensity"), eps=e.field("specificThermalEnergy"),
+                              vel=e.field("velocity"), t=e.time, err=abs(c1[7] - c0[7]) / abs(c0[7]))
+            e.close()
+        a, b = runs["fp32"], runs["fp64"]
+        rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+        compare = {"steps": args.fp64_compare_steps, "time_fp32": a["t"], "time_fp64": b["t"],
+                   "energy_error_fp32": a["err"], "energy_error_fp64": b["err"],
+                   "max_rel_diff_rho": rel(a["rho"], b["rho"]), "max_rel_diff_eps": rel(a["eps"], b["eps"]),
+                   "max_rel_diff_vel": rel(a["vel"], b["vel"])}
+
     if rank != 0:
         return
     hbm, peak_kind, pk = peaks()
@@ -302,8 +332,10 @@ def run_ours(args, ws, rank, local, dist):
                       "criterion, integration, compatible energy and tallies") if args.precision == "fp32"
         else "FP64 throughout",
         "data": "synthetic (seeded generator, no external data)",
-        "energy_error": energy_err,
-        "energy_error_steps": args.steps,
+        "energy_error": long_err,
+        "energy_error_steps": long_steps,
+        "energy_error_timed_steps": energy_err,
+        "fp32_vs_fp64": compare,
         "config": {"workload": wname, "n": n, "n1": prob.meta.get("n1"), "n2": prob.meta.get("n2"),
                    "mean_neighbors": k_mean, "pairs_per_step": pairs / args.steps,
                    "cache": "inputs larger than L2 (state + neighbour lists > 1 GB)",
@@ -331,18 +363,90 @@ def run_ours(args, ws, rank, local, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args, ws, rank, local, dist):
+    """Batched ensemble: args.boxes turbulent boxes with log-uniform particle
+    counts (4,096 to 262,144, seeded), all advanced by sphgpu_ensemble_advance
+    (one stream per box, host threads feeding them), against one large box
+    of about the same total size advanced alone."""
+    from spheral_gb300.engine import Engine
+    import torch
+    probs = problems_ensemble(args.boxes)
+    engines = [Engine.from_problem(p, precision=args.precision, device=local) for p in probs]
+    for e in engines:
+        e.initialize()
+    Engine.ensemble_advance(engines, args.warmup, nthreads=args.threads)
+    e0 = [e.conservation()[7] for e in engines]
+    before = sum(e.neighbor_entries() // 2 for e in engines)
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        Engine.ensemble_advance(engines, args.steps, nthreads=args.threads)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    wall = max_over_ranks(dist, wall)
+    after = sum(e.neighbor_entries() // 2 for e in engines)
+    pairs = 0.5 * (before + after) * args.steps
+    value = ws * pairs / wall
+    errs = [abs(e.conservation()[7] - a) / abs(a) for e, a in zip(engines, e0)]
+    ntot = sum(p.n for p in probs)
+    for e in engines:
+        e.close()
+    # single large box of about the same total size, advanced alone
+    from spheral_gb300 import problems
+    side = int(round(ntot ** (1.0 / 3.0)))
+    big = Engine.from_problem(problems.turbulent_box(side, 1), precision=args.precision, device=local)
+    big.initialize()
+    big.advance(args.warmup)
+    torch.cuda.synchronize()
+    bsteps = max(3, min(args.steps, 30))
+    b_before = big.neighbor_entries() // 2
+    t0 = time.perf_counter()
+    big.advance(bsteps)
+    torch.cuda.synchronize()
+    bwall = time.perf_counter() - t0
+    b_pairs = 0.5 * (b_before + big.neighbor_entries() // 2) * bsteps
+    single = b_pairs / bwall
+    big.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32" if args.precision == "fp32" else "f64", "data": "synthetic (seeded generator, no external data)",
+        "config": {"workload": f"ensemble_{args.boxes}_turbulent_boxes", "boxes": args.boxes, "n_total": ntot,
+                   "n_min": min(p.n for p in probs), "n_max": max(p.n for p in probs),
+                   "host_threads": args.threads or os.cpu_count(), "timer": "host wall clock, device synchronised",
+                   "parallelism": f"replicas x{ws}"},
+        "energy_error_max_over_boxes": max(errs),
+        "single_large_run": {"n": side ** 3, "value": single, "unit": UNIT, "steps": bsteps},
+        "ensemble_over_single": value / single,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def problems_ensemble(nboxes):
+    from spheral_gb300 import problems
+    return problems.ensemble(nboxes)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod"])
+    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble"])
+    ap.add_argument("--boxes", type=int, default=256)
+    ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--n1", type=int, default=112)
     ap.add_argument("--neighbors", type=int, default=64)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--energy-steps", type=int, default=1000)
+    ap.add_argument("--fp64-compare-steps", type=int, default=0)
     ap.add_argument("--cpu-n1", type=int, default=56)
     ap.add_argument("--cpu-steps", type=int, default=6)
     args = ap.parse_args()
@@ -352,7 +456,10 @@ def main():
     else:
         from spheral_gb300 import build
         build.build()
-        run_ours(args, ws, rank, local, dist)
+        if args.workload == "ensemble":
+            run_ensemble(args, ws, rank, local, dist)
+        else:
+            run_ours(args, ws, rank, local, dist)
     if dist is not None:
         dist.destroy_process_group()
 

@@ -171,6 +171,23 @@ int sphgpu_step(sphgpu_handle h, double max_time, double* dt_out);
 /* nsteps calls of sphgpu_step (stops early at max_time). */
 int sphgpu_advance(sphgpu_handle h, int nsteps, double max_time);
 
+/* Batched ensemble: nsteps CheapSynchronousRK2 steps on each of nboxes
+ * independent handles (separate problems, e.g. turbulent boxes of uneven
+ * sizes).  Handles are spread over nthreads host threads (0: one per
+ * hardware thread), largest particle count first onto the least-loaded
+ * thread; every handle runs on its own stream, so the GPU overlaps the
+ * kernels of different boxes and small boxes do not leave it idle.  Each
+ * box's result is bitwise that of sphgpu_advance on the handle alone.  The
+ * handles must be distinct and not used by other threads meanwhile.  On a
+ * failure the remaining boxes stop at their next step boundary, *failed (if
+ * not NULL) receives the index of the first failing handle (else -1) and its
+ * code is returned; that handle's sphgpu_last_error has the message.
+ * Replaces: running one Spheral problem per process for a parameter study
+ * (no single reference entry point; the SpheralController loop,
+ * src/SimulationControl/SpheralController.py, per box). */
+int sphgpu_ensemble_advance(sphgpu_handle* handles, int nboxes, int nsteps, double max_time, int nthreads,
+                            int* failed);
+
 /* Download / overwrite a field by reference name (caller node order).
  * Names: position velocity mass massDensity specificThermalEnergy H pressure
  * soundSpeed omegaGradh massDensitySum normalization DxDt DvDt DrhoDt DepsDt

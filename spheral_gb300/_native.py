@@ -88,6 +88,7 @@ SIGNATURES = {
     "sphgpu_dt": (_i, [_vp, _dp, _ip]),
     "sphgpu_step": (_i, [_vp, _d, _dp]),
     "sphgpu_advance": (_i, [_vp, _i, _d]),
+    "sphgpu_ensemble_advance": (_i, [_vp, _i, _i, _d, _i, _vp]),
     "sphgpu_get_field": (_i, [_vp, _cp, _dp, _ip]),
     "sphgpu_set_field": (_i, [_vp, _cp, _dp]),
     "sphgpu_get_pairs": (_i, [_vp, _ip, _ip, _ip, _lp]),

@@ -4,11 +4,14 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace sph {
@@ -112,6 +115,7 @@ struct sphgpu_ctx {
 
   // parameters
   NodeListParams lists[kMaxNodeLists]{};
+  DBuf dLists;   // device copy of lists
   int numLists = 0;
   std::vector<Boundary> bcs;
   HydroParams hp{};
@@ -285,6 +289,11 @@ void refreshParams(sphgpu_ctx* c) {
   hp.cfl = g.cfl;
   hp.numLists = std::max(1, c->numLists);
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
+  // NodeList table in device memory, one per handle (handles on different
+  // streams never share it).
+  c->dLists.ensure(sizeof(c->lists));
+  CUDA_OK(cudaMemcpyAsync(c->dLists.p, c->lists, sizeof(c->lists), cudaMemcpyHostToDevice, c->stream));
+  hp.lists = c->dLists.as<NodeListParams>();
 }
 
 void requireState(sphgpu_ctx* c) {
@@ -523,7 +532,7 @@ void evalDerivs(sphgpu_ctx* c) {
       int bestV = 1;
       for (int v = 0; v < 3; ++v) {
         CUDA_OK(cudaEventRecord(e0, c->stream));
-        launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+        launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                        c->pacc.as<float>(), v, c->stream, &c->lc);
         CUDA_OK(cudaEventRecord(e1, c->stream));
         CUDA_OK(cudaEventSynchronize(e1));
@@ -538,11 +547,11 @@ void evalDerivs(sphgpu_ctx* c) {
       c->tunedN = c->n;
     }
     Scope sc(c->prof, "pair_fp32");
-    launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+    launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                    c->pacc.as<float>(), c->pairVariant, c->stream, &c->lc);
   } else {
     Scope sc(c->prof, "pair_fp64");
-    launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists, c->pacc.as<double>(),
+    launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->pacc.as<double>(),
                    128, c->stream, &c->lc);
   }
   c->check();
@@ -569,10 +578,10 @@ double packageDt(sphgpu_ctx* c, int* reason, bool fusedDone = false) {
   double* d = c->small.as<double>();
   if (fusedDone) {
   } else if (c->fp32())
-    launchDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(),
+    launchDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->hp, c->maxNperh(),
                  c->scratch.as<double>(), (int)(2 * nb), d, c->stream, &c->lc);
   else
-    launchDt(c->F, c->listp(), c->n, c->grid, c->nl(), c->hp, c->lists, c->maxNperh(), c->scratch.as<double>(),
+    launchDt(c->F, c->listp(), c->n, c->grid, c->nl(), c->hp, c->maxNperh(), c->scratch.as<double>(),
              (int)(2 * nb), d, c->stream, &c->lc);
   c->check();
   CUDA_OK(cudaMemcpyAsync(c->hsmall, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -620,7 +629,7 @@ double step(sphgpu_ctx* c, double maxTime) {
       Scope sc(c->prof, "density_dt");
       const long nb = (c->n + 127) / 128;
       c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
-      launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->lists,
+      launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                           c->maxNperh(), c->scratch.as<double>(), c->small.as<double>(), c->stream, &c->lc);
       c->check();
       fused = true;
@@ -634,7 +643,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   {
     Scope sc(c->prof, "update");
     launchSaveState0(c->F, c->n, c->stream, &c->lc);
-    launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, hdt, true, c->cfg.gravity != 0, c->stream, &c->lc);
+    launchUpdate(c->F, c->listp(), c->n, c->hp, hdt, true, c->cfg.gravity != 0, c->stream, &c->lc);
   }
   c->check();
   prepare32(c);
@@ -657,7 +666,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   }
   {
     Scope sc(c->prof, "update");
-    launchUpdate(c->F, c->listp(), c->n, c->lists, c->hp, dt, false, c->cfg.gravity != 0, c->stream, &c->lc);
+    launchUpdate(c->F, c->listp(), c->n, c->hp, dt, false, c->cfg.gravity != 0, c->stream, &c->lc);
   }
   c->check();
   prepare32(c);
@@ -811,7 +820,8 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->itemFlag, &c->items};
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->itemFlag, &c->items,
+                  &c->dLists};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);
@@ -915,7 +925,7 @@ int sphgpu_initialize(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
   refreshParams(c);
-  launchEOS(c->F, c->listp(), c->n, c->lists, c->stream, &c->lc);
+  launchEOS(c->F, c->listp(), c->n, c->hp.lists, c->stream, &c->lc);
   c->check();
   buildNeighbors(c);
   if (c->cfg.gradh_correction) gradh(c);
@@ -987,6 +997,63 @@ int sphgpu_advance(sphgpu_handle c, int nsteps, double max_time) {
   for (int k = 0; k < nsteps && c->time < max_time; ++k) step(c, max_time);
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
+}
+
+int sphgpu_ensemble_advance(sphgpu_handle* handles, int nboxes, int nsteps, double max_time, int nthreads,
+                            int* failed) {
+  if (failed) *failed = -1;
+  if (!handles || nboxes <= 0 || nsteps < 0) return SPHGPU_E_ARG;
+  {
+    std::vector<sphgpu_handle> seen(handles, handles + nboxes);
+    std::sort(seen.begin(), seen.end());
+    if (!seen.front() || std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return SPHGPU_E_ARG;
+  }
+  int nt = nthreads > 0 ? nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
+  nt = std::max(1, std::min(nt, nboxes));
+  // Longest-processing-time first: boxes by particle count, each onto the
+  // least-loaded thread.
+  std::vector<int> order(nboxes);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return handles[a]->n > handles[b]->n; });
+  std::vector<std::vector<int>> work(nt);
+  std::vector<long> load(nt, 0);
+  for (int b : order) {
+    const int t = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    work[t].push_back(b);
+    load[t] += std::max(1L, handles[b]->n);
+  }
+  std::vector<int> rc(nboxes, SPHGPU_OK);
+  std::atomic<int> stop{0};
+  auto body = [&](int t) {
+    auto run = [&](int b, bool finish) {
+      sphgpu_ctx* c = handles[b];
+      try {
+        CUDA_OK(cudaSetDevice(c->cfg.device));
+        if (finish) CUDA_OK(cudaStreamSynchronize(c->stream));
+        else if (c->time < max_time) step(c, max_time);
+      } catch (const Error& e) {
+        rc[b] = fail(c, e);
+      } catch (const std::exception& e) {
+        rc[b] = failStd(c, e);
+      }
+      if (rc[b] != SPHGPU_OK) stop.store(1);
+    };
+    for (int k = 0; k < nsteps && !stop.load(); ++k)
+      for (int b : work[t])
+        if (rc[b] == SPHGPU_OK && !stop.load()) run(b, false);
+    for (int b : work[t])
+      if (rc[b] == SPHGPU_OK) run(b, true);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(body, t);
+  body(0);
+  for (auto& th : pool) th.join();
+  for (int b = 0; b < nboxes; ++b)
+    if (rc[b] != SPHGPU_OK) {
+      if (failed) *failed = b;
+      return rc[b];
+    }
+  return SPHGPU_OK;
 }
 
 int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp) {

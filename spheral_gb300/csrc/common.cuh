@@ -42,6 +42,7 @@ struct HydroParams {
   double extent;      // kernel extent
   int hermN;          // Hermite knots of the nperh lookup
   double hermXmin, hermXmax, hermXstep;
+  const NodeListParams* lists;   // device table of the NodeLists (kMaxNodeLists entries)
 };
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,

@@ -160,7 +160,6 @@ __device__ __forceinline__ double blockSum(double v, double* sm) {
   return v;
 }
 
-static __constant__ NodeListParams cLists[kMaxNodeLists];
 
 __device__ __forceinline__ double hermiteLookup(const double* __restrict__ v, const HydroParams& hp, double x) {
   // CubicHermiteInterpolatorView::operator() (CubicHermiteInterpolatorViewInline.hh:10-36)
@@ -242,7 +241,7 @@ __device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const No
   F.f[F_XSPHDV_Y][i] = a.xdy;
   F.f[F_XSPHDV_Z][i] = a.xdz;
   // SPHSmoothingScale finalize (SPHSmoothingScale.cc:235-270)
-  const NodeListParams L = cLists[li];
+  const NodeListParams L = hp.lists[li];
   const double m0s = fmax(0.0, a.m0);
   const double m0 = m0s < 0.0 ? -pow(-m0s, 0.3333333333333333) : pow(m0s, 0.3333333333333333);
   F.f[F_M0][i] = m0;
@@ -344,7 +343,7 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
   F.f[F_XSPHDV_X][i] = a.xdx;
   F.f[F_XSPHDV_Y][i] = a.xdy;
   F.f[F_XSPHDV_Z][i] = a.xdz;
-  const NodeListParams L = cLists[li];
+  const NodeListParams L = hp.lists[li];
   const float m0 = cbrtf(fmaxf(0.0f, a.m0));
   F.f[F_M0][i] = m0;
   F.f[F_M1_X][i] = a.m1x;

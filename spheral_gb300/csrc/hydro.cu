@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
   if (i < n) {
     int hc[3];
     unpackCell(nl.cell[i], hc);
-    const NodeListParams L = cLists[list[i]];
+    const NodeListParams L = hp.lists[list[i]];
     const double ai = F.f[F_HINV][i];
     const double nodeScalei = 1.0 / ai / L.nPerh;
     const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
@@ -670,11 +670,11 @@ __global__ void restoreState0Kernel(Fields F, long n) {
   F.f[F_RHO][i] = F.f[F_RHO0][i]; F.f[F_EPS][i] = F.f[F_EPS0][i]; F.f[F_HINV][i] = F.f[F_HINV0][i];
 }
 
-__global__ void updateKernel(Fields F, const int* __restrict__ list, long n, double mult, int mid, int gravity,
-                             int epsIncrement) {
+__global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
+                             double mult, int mid, int gravity, int epsIncrement) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const NodeListParams L = cLists[list[i]];
+  const NodeListParams L = lists[list[i]];
   if (epsIncrement) F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
   F.f[F_X][i] += mult * F.f[F_DXDT_X][i];
   F.f[F_Y][i] += mult * F.f[F_DXDT_Y][i];
@@ -697,10 +697,10 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, dou
   eosNode(F, i, L);
 }
 
-__global__ void eosKernel(Fields F, const int* __restrict__ list, long n) {
+__global__ void eosKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  eosNode(F, i, cLists[list[i]]);
+  eosNode(F, i, lists[list[i]]);
 }
 
 // Boundary::setAllViolationNodes + enforceBoundary (PlanarBoundary.cc:153-190,
@@ -882,8 +882,7 @@ void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroPa
   lc->add(1);
 }
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
-                    const NodeListParams* lists, double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
+                    double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc) {
   const size_t sm = sizeof(double) * 6 * (hp.tableN1 + 1);
   const int b = 128;
   (void)blockSize;
@@ -897,9 +896,8 @@ void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl,
   lc->add(1);
 }
 void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
-              const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+              double maxNperh, double* dScratch, int nScratch, double* dOut,
               cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
   const int nb = (int)gridFor(n, 128);
   (void)nScratch;
   dtKernel<<<nb, 128, 0, s>>>(F, list, n, g, nl, hp, maxNperh, dScratch);
@@ -920,16 +918,14 @@ void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
   restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
   lc->add(1);
 }
-void launchUpdate(Fields F, const int* list, long n, const NodeListParams* lists, HydroParams hp, double mult,
+void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
                   bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
   const int epsInc = (mid || !hp.compatible) ? 1 : 0;
-  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc);
+  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
-  eosKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n);
+  eosKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, lists);
   lc->add(1);
 }
 void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc) {

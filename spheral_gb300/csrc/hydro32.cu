@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     P.thermo[i].x = (float)rho;
     // node limits
     const double tiny = DBL_EPSILON;
-    const NodeListParams L = cLists[multi ? li : list[i]];
+    const NodeListParams L = hp.lists[multi ? li : list[i]];
     const double nodeScalei = 1.0 / a / L.nPerh;
     const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
     const double csDt = nodeScalei / (F.f[F_CS][i] + tiny);
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
     int ci[3];
     unpackCell(P.cell[i], ci);
     const uint32_t mm = mirrorMask(g, ci);
-    const NodeListParams L = cLists[list[i]];
+    const NodeListParams L = hp.lists[list[i]];
     const double ai = F.f[F_HINV][i];
     const double nodeScalei = 1.0 / ai / L.nPerh;
     const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
@@ -563,9 +563,8 @@ void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, L
 // register cap below 128), 1 -> 5 (<= 102 registers, no spills), 2 -> 6
 // (<= 85 registers, small spills).  Chosen at run time by the autotuner.
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                    HydroParams hp, const NodeListParams* lists, float* pacc, int variant, cudaStream_t s,
+                    HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
   const int b = 128;
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
@@ -598,9 +597,8 @@ void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, T
 }
 
 void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
-                  const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+                  double maxNperh, double* dScratch, int nScratch, double* dOut,
                   cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
   (void)nScratch;
   const int nb = (int)gridFor(n, 128);
   dtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
@@ -616,9 +614,8 @@ void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, cons
 }
 
 void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                         HydroParams hp, const NodeListParams* lists, double maxNperh, double* dScratch,
+                         HydroParams hp, double maxNperh, double* dScratch,
                          double* dOut, cudaStream_t s, LaunchCounter* lc) {
-  cudaMemcpyToSymbolAsync(cLists, lists, sizeof(NodeListParams) * kMaxNodeLists, 0, cudaMemcpyHostToDevice, s);
   const int nb = (int)gridFor(n, 128);
   densityDtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);

@@ -55,9 +55,9 @@ void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists n
 void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
                  LaunchCounter* lc);
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
-                    const NodeListParams* lists, double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
+                    double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                    HydroParams hp, const NodeListParams* lists, float* pacc, int variant, cudaStream_t s,
+                    HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);
 void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
 void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
@@ -65,15 +65,15 @@ void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid 
 void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                      cudaStream_t s, LaunchCounter* lc);
 void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
-                  const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+                  double maxNperh, double* dScratch, int nScratch, double* dOut,
                   cudaStream_t s, LaunchCounter* lc);
 // Mixed mode: density sum and dt vote fused in one sweep (dOut as launchDt).
 void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                         HydroParams hp, const NodeListParams* lists, double maxNperh, double* dScratch,
+                         HydroParams hp, double maxNperh, double* dScratch,
                          double* dOut, cudaStream_t s, LaunchCounter* lc);
 // dt: writes per-block (value, reason) pairs then a final min into dOut[0], dOut[1] (reason as double)
 void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
-              const NodeListParams* lists, double maxNperh, double* dScratch, int nScratch, double* dOut,
+              double maxNperh, double* dScratch, int nScratch, double* dOut,
               cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
                             double dt, cudaStream_t s, LaunchCounter* lc);
@@ -83,8 +83,9 @@ void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
 // already advanced by the compatible-energy sweep when compatible).
-void launchUpdate(Fields F, const int* list, long n, const NodeListParams* lists, HydroParams hp, double mult,
+void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
                   bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc);
+// lists: device table of NodeListParams (HydroParams::lists).
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc);
 void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
 // out[0..7] conservation totals

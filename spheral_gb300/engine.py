@@ -130,6 +130,21 @@ class Engine:
     def synchronize(self):
         self._chk(self.L.sphgpu_synchronize(self.h))
 
+    @staticmethod
+    def ensemble_advance(engines, nsteps, max_time=1.0e300, nthreads=0):
+        """nsteps steps of every engine at once (sphgpu_ensemble_advance):
+        the boxes run concurrently on their own streams from nthreads host
+        threads; each box ends bitwise as if advanced alone."""
+        if not engines:
+            return
+        L = N.lib()
+        arr = (ctypes.c_void_p * len(engines))(*[e.h for e in engines])
+        failed = ctypes.c_int(-1)
+        rc = L.sphgpu_ensemble_advance(arr, len(engines), nsteps, max_time, nthreads, ctypes.byref(failed))
+        if rc != N.SPHGPU_OK:
+            h = engines[failed.value].h if failed.value >= 0 else None
+            N.check(h, rc)
+
     # -- inspection -----------------------------------------------------------
     def field(self, name):
         nc = FIELD_NCOMP[name]
