@@ -137,7 +137,8 @@ def max_over_ranks(dist, v):
 
 
 def make_workload_name(args):
-    return None, {"kh": "kelvin_helmholtz_3d", "sweep": "sweep_box", "sod": "sod_planar_3d"}[args.workload]
+    return None, {"kh": "kelvin_helmholtz_3d", "sweep": "sweep_box", "sod": "sod_planar_3d",
+                  "evrard": "evrard_collapse_3d"}[args.workload]
 
 
 def make_workload(args):
@@ -148,6 +149,8 @@ def make_workload(args):
         return problems.sweep_box(n_side=args.n1, neighbors=args.neighbors), "sweep_box"
     if args.workload == "sod":
         return problems.sod(nx1=args.n1), "sod_planar_3d"
+    if args.workload == "evrard":
+        return problems.evrard(n=args.n_evrard), "evrard_collapse_3d"
     raise SystemExit("unknown workload")
 
 
@@ -161,6 +164,8 @@ def cpu_baseline(args, steps=None, warmup=1):
         p = problems.kelvin_helmholtz(n1=args.cpu_n1)
     elif args.workload == "sweep":
         p = problems.sweep_box(n_side=args.cpu_n1, neighbors=args.neighbors)
+    elif args.workload == "evrard":
+        p = problems.evrard(n=65536)
     else:
         p = problems.sod(nx1=args.cpu_n1)
     o = orc.Oracle(p)
@@ -222,7 +227,8 @@ def run_ours(args, ws, rank, local, dist):
         eng.step()
     e0 = eng.conservation()
     pair_kernel = "pair_fp32" if args.precision == "fp32" else "pair_fp64"
-    names = [pair_kernel, "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt", "energy",
+    names = [pair_kernel, "gravity", "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt",
+             "energy",
              "gradh", "radix_sort",
              "permute", "update", "prepare_fp32", "enforce", "cell_keys", "bounds", "cell_ranges"]
     eng.profile(True)
@@ -231,6 +237,7 @@ def run_ours(args, ws, rank, local, dist):
         ms, pairs, launches, prof = time_steps(eng, args.steps, names)
     eng.profile(False)
     ms = max_over_ranks(dist, ms)
+    pair_variant = eng.pair_variant()[0] if args.precision == "fp32" else None
     e1 = eng.conservation()
     energy_err = abs(e1[7] - e0[7]) / abs(e0[7])
     value = ws * pairs / (ms / 1e3)
@@ -343,6 +350,7 @@ def run_ours(args, ws, rank, local, dist):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
+        "pair_variant": pair_variant,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved_gbs / hbm) if achieved_gbs else None,
                      "traffic": (TRAFFIC_BYTES_PER_PAIR[args.precision] * pairs_per_launch
@@ -437,7 +445,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble"])
+    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard"])
+    ap.add_argument("--n-evrard", type=int, default=1048576)
     ap.add_argument("--boxes", type=int, default=256)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])

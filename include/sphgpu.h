@@ -241,6 +241,15 @@ int sphgpu_timer_start(sphgpu_handle h);
 int sphgpu_timer_stop(sphgpu_handle h, double* ms);
 /* Ordered neighbour entries of the current lists (2x the unordered pairs). */
 int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
+/* Mixed-mode pair kernel variant (register budget / software pipelining of
+ * the neighbour loop).  By default (-1) the fastest of the variants is picked
+ * by timing each once per problem size; sphgpu_set_pair_variant pins one
+ * (0 .. *nvariants-1 from sphgpu_get_pair_variant), or -1 to re-enable the
+ * autotuner.  sphgpu_get_pair_variant returns the variant in use (-1 before
+ * the first mixed-mode evaluation).  No reference counterpart (tuning only). */
+int sphgpu_set_pair_variant(sphgpu_handle h, int variant);
+int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
+
 /* Wait for all work on the handle's stream. */
 int sphgpu_synchronize(sphgpu_handle h);
 

@@ -89,6 +89,8 @@ SIGNATURES = {
     "sphgpu_step": (_i, [_vp, _d, _dp]),
     "sphgpu_advance": (_i, [_vp, _i, _d]),
     "sphgpu_ensemble_advance": (_i, [_vp, _i, _i, _d, _i, _vp]),
+    "sphgpu_set_pair_variant": (_i, [_vp, _i]),
+    "sphgpu_get_pair_variant": (_i, [_vp, _ip, _ip]),
     "sphgpu_get_field": (_i, [_vp, _cp, _dp, _ip]),
     "sphgpu_set_field": (_i, [_vp, _cp, _dp]),
     "sphgpu_get_pairs": (_i, [_vp, _ip, _ip, _ip, _lp]),

@@ -155,6 +155,7 @@ struct sphgpu_ctx {
   bool initialized = false;
   cudaEvent_t tA = nullptr, tB = nullptr;
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
+  bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
   long tunedN = 0;
 
   Fields fieldsOf(DBuf& bank) {
@@ -524,13 +525,13 @@ void evalDerivs(sphgpu_ctx* c) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
     // trial launches leave the same results) and keep the fastest.
-    if (c->pairVariant < 0 || c->tunedN != c->n) {
+    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n)) {
       cudaEvent_t e0, e1;
       CUDA_OK(cudaEventCreate(&e0));
       CUDA_OK(cudaEventCreate(&e1));
       float best = 1e30f;
       int bestV = 1;
-      for (int v = 0; v < 3; ++v) {
+      for (int v = 0; v < kPairVariants; ++v) {
         CUDA_OK(cudaEventRecord(e0, c->stream));
         launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                        c->pacc.as<float>(), v, c->stream, &c->lc);
@@ -559,7 +560,8 @@ void evalDerivs(sphgpu_ctx* c) {
     Scope sc(c->prof, "gravity");
     char msg[256] = {0};
     double* d = c->small.as<double>() + 16;
-    const int rc = gravityEvaluate(c->grav, c->F, c->n, c->cfg.G, c->cfg.softening, c->cfg.opening, d, c->stream,
+    const int rc = gravityEvaluate(c->grav, c->F, c->n, c->cfg.G, c->cfg.softening, c->cfg.opening, c->fp32(), d,
+                                   c->stream,
                                    &c->lc, msg, sizeof(msg));
     if (rc != SPHGPU_OK) throw Error(rc, std::string("gravity: ") + msg);
     CUDA_OK(cudaMemcpyAsync(c->hsmall + 16, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -996,6 +998,21 @@ int sphgpu_advance(sphgpu_handle c, int nsteps, double max_time) {
   API_BEGIN(c)
   for (int k = 0; k < nsteps && c->time < max_time; ++k) step(c, max_time);
   CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_set_pair_variant(sphgpu_handle c, int variant) {
+  API_BEGIN(c)
+  if (variant < -1 || variant >= kPairVariants) throw Error(SPHGPU_E_ARG, "pair variant out of range");
+  c->pairVariant = variant;
+  c->pinnedVariant = variant >= 0;
+  API_END(c)
+}
+
+int sphgpu_get_pair_variant(sphgpu_handle c, int* variant, int* nvariants) {
+  API_BEGIN(c)
+  if (variant) *variant = c->pairVariant;
+  if (nvariants) *nvariants = kPairVariants;
   API_END(c)
 }
 

@@ -33,6 +33,16 @@
 // Forces, potentials and the decision are evaluated in FP64 with the
 // reference's expressions (no fused multiply-add in the opening test);
 // summation order is pre-order instead of level order.
+//
+// Mixed precision (the mixed-mode package).  GB300's FP64 pipe is thin, so
+// the mixed walk evaluates each interaction in FP32 on double-float
+// (hi + lo) coordinates -- the separation (hi_c - hi_i) + (lo_c - lo_i)
+// carries FP32 relative precision at any distance -- and sums the terms with
+// compensated (Kahan) FP32 accumulators that leave the kernel as the FP64
+// value s - c.  The far/near decision compares the FP32 r^2 with the FP32
+// threshold; inside a guard band of +-4e-6 (far above the FP32 error of both)
+// it is retaken in FP64 with the reference's expression, so the set of far
+// cells and opened leaves is the FP64 walk's.
 #include "kernels.cuh"
 #include "sort.cuh"
 #include "../../include/sphgpu.h"
@@ -72,6 +82,25 @@ __device__ __forceinline__ TreeNode loadNode(const TreeNode* __restrict__ p) {
   const double2 a = __ldg(reinterpret_cast<const double2*>(p));
   const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
   return TreeNode{a.x, a.y, b.x, b.y};
+}
+
+// Mixed-walk copies: double-float centre of mass, FP32 mass, FP32 opening
+// threshold thr[level] + rcm2cc2; same skip/start/count/lvl.
+struct __align__(16) TreeCell32 {
+  float xh, yh, zh, M;
+  float xl, yl, zl, open2;
+  int skip, start, count, lvl;
+};
+static_assert(sizeof(TreeCell32) == 48, "TreeCell32 layout");
+
+struct __align__(32) TreeNode32 {
+  float xh, yh, zh, m;
+  float xl, yl, zl, pad;
+};
+
+__device__ __forceinline__ void splitDF(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
 }
 
 struct GBuf {
@@ -207,12 +236,23 @@ __global__ void gatherHiKernel(const uint64_t* __restrict__ key64, const int* __
 
 // Tree-ordered node data and the shared-level count cpl(k).
 __global__ void treeNodesKernel(Fields F, const uint64_t* __restrict__ key64, const int* __restrict__ vals, long n,
-                                uint64_t* __restrict__ skey, TreeNode* __restrict__ tpos) {
+                                uint64_t* __restrict__ skey, TreeNode* __restrict__ tpos,
+                                TreeNode32* __restrict__ tpos32) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int i = vals[k];
   skey[k] = key64[i];
-  tpos[k] = TreeNode{F.f[F_X][i], F.f[F_Y][i], F.f[F_Z][i], F.f[F_MASS][i]};
+  const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i], m = F.f[F_MASS][i];
+  tpos[k] = TreeNode{x, y, z, m};
+  if (tpos32) {
+    TreeNode32 t;
+    splitDF(x, t.xh, t.xl);
+    splitDF(y, t.yh, t.yl);
+    splitDF(z, t.zh, t.zl);
+    t.m = (float)m;
+    t.pad = 0.0f;
+    tpos32[k] = t;
+  }
 }
 
 __device__ __forceinline__ int sharedLevels(const uint64_t* __restrict__ skey, long n, long k) {
@@ -412,6 +452,157 @@ __global__ void __launch_bounds__(128) treeWalkKernel(const TreeCell* __restrict
   }
 }
 
+__global__ void cells32Kernel(const TreeCell* __restrict__ cells, long long numCells,
+                              const double* __restrict__ thrLevel, TreeCell32* __restrict__ c32) {
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= numCells) return;
+  const TreeCell cl = cells[c];
+  TreeCell32 o;
+  splitDF(cl.x, o.xh, o.xl);
+  splitDF(cl.y, o.yh, o.yl);
+  splitDF(cl.z, o.zh, o.zl);
+  o.M = (float)cl.M;
+  o.open2 = (float)__dadd_rn(thrLevel[cl.lvl & 255], cl.r2cc);
+  o.skip = cl.skip;
+  o.start = cl.start;
+  o.count = cl.count;
+  o.lvl = cl.lvl;
+  c32[c] = o;
+}
+
+__device__ __forceinline__ void kahan(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+// FP32 monopole term on a double-float separation: a += M/(r^2+eps^2) rhat,
+// phi -= M/sqrt(r^2+eps^2), compensated sums.
+struct Acc32 {
+  float sx, sy, sz, sp, cx, cy, cz, cp;
+};
+
+__device__ __forceinline__ void addMonopole32(float M, float dx, float dy, float dz, float r2, float soft2,
+                                              Acc32& a) {
+  const float ir = r2 > 1.0e-30f ? rsqrtf(r2) : 0.0f;
+  const float nx = r2 > 1.0e-30f ? dx * ir : 1.0f, ny = dy * ir, nz = dz * ir;
+  const float irs = rsqrtf(r2 + soft2);
+  const float f = M * (irs * irs);
+  kahan(a.sx, a.cx, f * nx);
+  kahan(a.sy, a.cy, f * ny);
+  kahan(a.sz, a.cz, f * nz);
+  kahan(a.sp, a.cp, -M * irs);
+}
+
+__global__ void __launch_bounds__(128) treeWalkMixedKernel(
+    const TreeCell32* __restrict__ c32, const TreeCell* __restrict__ cells, long long numCells,
+    const TreeNode32* __restrict__ t32, const TreeNode* __restrict__ tpos, const int* __restrict__ vals, long n,
+    const double* __restrict__ thrLevel, double soft2d, double softening, double G, Fields F,
+    unsigned long long* __restrict__ dtBits, double* __restrict__ energyPart) {
+  __shared__ double thr[kMaxLevel + 1];
+  __shared__ double esum[4];
+  __shared__ double dmin[4];
+  if (threadIdx.x <= kMaxLevel) thr[threadIdx.x] = thrLevel[threadIdx.x];
+  __syncthreads();
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool valid = k < n;
+  TreeNode32 me{0, 0, 0, 0, 0, 0, 0, 0};
+  double xd = 0, yd = 0, zd = 0, mi = 0;
+  if (valid) {
+    me = t32[k];
+    const TreeNode p = tpos[k];
+    xd = p.x; yd = p.y; zd = p.z; mi = p.m;
+  }
+  const float soft2 = (float)soft2d;
+  constexpr float kBand = 4.0e-6f;
+  Acc32 acc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  unsigned until = valid ? 0u : 0xFFFFFFFFu;
+  unsigned c = 1;
+  const unsigned nc = (unsigned)numCells;
+  if (__all_sync(0xffffffffu, !valid)) c = nc;
+  while (c < nc) {
+    const float4* cp = reinterpret_cast<const float4*>(c32 + c);
+    const float4 qa = __ldg(cp), qb = __ldg(cp + 1);
+    const int4 qi = __ldg(reinterpret_cast<const int4*>(cp + 2));
+    const unsigned skip = (unsigned)qi.x;
+    const int start = qi.y, count = qi.z, level = qi.w & 255, leaf = qi.w >> 8;
+    bool descend = false;
+    if (c >= until) {
+      const float dx = __fadd_rn(__fsub_rn(qa.x, me.xh), __fsub_rn(qb.x, me.xl));
+      const float dy = __fadd_rn(__fsub_rn(qa.y, me.yh), __fsub_rn(qb.y, me.yl));
+      const float dz = __fadd_rn(__fsub_rn(qa.z, me.zh), __fsub_rn(qb.z, me.zl));
+      const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+      const float o2 = qb.w;
+      bool far;
+      if (r2 > o2 * (1.0f + kBand)) far = true;
+      else if (r2 < o2 * (1.0f - kBand)) far = false;
+      else {   // guard band: the reference's FP64 test
+        const TreeCell& cd = cells[c];
+        const double ex = __dsub_rn(cd.x, xd), ey = __dsub_rn(cd.y, yd), ez = __dsub_rn(cd.z, zd);
+        const double q2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+        far = q2 > __dadd_rn(thr[level], cd.r2cc);
+      }
+      if (far) {
+        addMonopole32(qa.w, dx, dy, dz, r2, soft2, acc);
+        until = skip;
+      } else if (leaf) {
+        for (int j = start; j < start + count; ++j) {
+          const TreeNode32 p = t32[j];
+          const float ex = __fadd_rn(__fsub_rn(p.xh, me.xh), __fsub_rn(p.xl, me.xl));
+          const float ey = __fadd_rn(__fsub_rn(p.yh, me.yh), __fsub_rn(p.yl, me.yl));
+          const float ez = __fadd_rn(__fsub_rn(p.zh, me.zh), __fsub_rn(p.zl, me.zl));
+          const float q2 = __fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex)));
+          const float lim = 1.0e-10f * soft2;
+          bool use;
+          if (q2 > lim * 1.001f) use = true;
+          else if (q2 < lim * 0.999f) use = false;
+          else {   // the reference's r2 / soft2 > 1e-10 in FP64
+            const TreeNode pd = tpos[j];
+            const double fx = __dsub_rn(pd.x, xd), fy = __dsub_rn(pd.y, yd), fz = __dsub_rn(pd.z, zd);
+            const double w2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
+            use = __ddiv_rn(w2, soft2d) > 1.0e-10;
+          }
+          if (use) addMonopole32(p.m, ex, ey, ez, q2, soft2, acc);
+        }
+        until = skip;
+      } else {
+        descend = true;
+      }
+    }
+    if (__any_sync(0xffffffffu, descend)) ++c;
+    else c = __reduce_min_sync(0xffffffffu, until);
+  }
+  double vote = DBL_MAX, e = 0.0;
+  if (valid) {
+    const double ax = (double)acc.sx - (double)acc.cx, ay = (double)acc.sy - (double)acc.cy;
+    const double az = (double)acc.sz - (double)acc.cz, phi = (double)acc.sp - (double)acc.cp;
+    const int i = vals[k];
+    F.f[F_GRAV_X][i] = G * ax;
+    F.f[F_GRAV_Y][i] = G * ay;
+    F.f[F_GRAV_Z][i] = G * az;
+    const double pot = G * phi;
+    F.f[F_POT][i] = pot;
+    const double amag = sqrt(ax * ax + ay * ay + az * az);
+    if (amag > 0.0) vote = sqrt(softening / amag);
+    e = 0.5 * mi * pot;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    vote = fmin(vote, __shfl_xor_sync(0xffffffffu, vote, o));
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+  }
+  if (lane == 0) { dmin[warp] = vote; esum[warp] = e; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = dmin[0], sm = esum[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { v = fmin(v, dmin[w]); sm += esum[w]; }
+    energyPart[blockIdx.x] = sm;
+    atomicMin(dtBits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
 __global__ void walkFinalKernel(const double* __restrict__ energyPart, int nb, const unsigned long long* dtBits,
                                 double G, double* __restrict__ out) {
   __shared__ double sm[32];
@@ -442,7 +633,7 @@ __global__ void zeroGravityKernel(Fields F, long n, double G, double* __restrict
 
 struct GravityWork {
   GBuf part, box, thr, dtBits, key64, lo, lo2, vals, vals2, sortWs, skey, tpos, nc, off, scanWs, total, cells, mx,
-      energy;
+      energy, tpos32, cells32;
   long long* hTotal = nullptr;
   long long lastCells = 0;
 };
@@ -457,7 +648,7 @@ void gravityDestroy(GravityWork* w) {
   if (!w) return;
   GBuf* all[] = {&w->part, &w->box, &w->thr, &w->dtBits, &w->key64, &w->lo, &w->lo2, &w->vals, &w->vals2,
                  &w->sortWs, &w->skey, &w->tpos, &w->nc, &w->off, &w->scanWs, &w->total, &w->cells, &w->mx,
-                 &w->energy};
+                 &w->energy, &w->tpos32, &w->cells32};
   for (GBuf* b : all) b->release();
   if (w->hTotal) cudaFreeHost(w->hTotal);
   delete w;
@@ -465,8 +656,8 @@ void gravityDestroy(GravityWork* w) {
 
 long long gravityNumCells(const GravityWork* w) { return w ? w->lastCells : 0; }
 
-int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening, double opening, double* dOut,
-                    cudaStream_t s, LaunchCounter* lc, char* err, int errlen) {
+int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening, double opening, bool mixed,
+                    double* dOut, cudaStream_t s, LaunchCounter* lc, char* err, int errlen) {
 #define GCHK(expr)                                                                     \
   do {                                                                                 \
     const cudaError_t e_ = (expr);                                                     \
@@ -500,6 +691,7 @@ int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening
   GCHK(w->vals2.ensure(n * sizeof(int)));
   GCHK(w->sortWs.ensure(radixSortWorkspaceBytes(n)));
   GCHK(w->tpos.ensure(n * sizeof(TreeNode)));
+  if (mixed) GCHK(w->tpos32.ensure(n * sizeof(TreeNode32)));
   GCHK(w->nc.ensure(n * sizeof(int)));
   GCHK(w->off.ensure((n + 1) * sizeof(long long)));
   GCHK(w->scanWs.ensure(scanWorkspaceBytes(n)));
@@ -522,7 +714,8 @@ int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening
   lc->add(1);
   radixSortPairs(keys, vals, keysAlt, valsAlt, n, 30, w->sortWs.p, s, lc);
   treeNodesKernel<<<blocksFor(n, kThreads), kThreads, 0, s>>>(F, w->key64.as<uint64_t>(), vals, n,
-                                                             w->skey.as<uint64_t>(), w->tpos.as<TreeNode>());
+                                                             w->skey.as<uint64_t>(), w->tpos.as<TreeNode>(),
+                                                             mixed ? w->tpos32.as<TreeNode32>() : nullptr);
   chainCountKernel<<<blocksFor(n, kThreads), kThreads, 0, s>>>(w->skey.as<uint64_t>(), n, w->nc.as<int>());
   lc->add(2);
   scanExclusive<int>(w->nc.as<int>(), w->off.as<long long>(), n, w->scanWs.p, w->total.as<long long>(), s, lc);
@@ -546,9 +739,19 @@ int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening
                                               w->box.as<double>(), w->mx.as<double>());
   }
   lc->add(kMaxLevel + 1);
-  treeWalkKernel<<<nbWalk, 128, 0, s>>>(cells, numCells, w->tpos.as<TreeNode>(), vals, n, w->thr.as<double>(),
-                                        softening * softening, softening, G, F,
-                                        w->dtBits.as<unsigned long long>(), w->energy.as<double>());
+  if (mixed) {
+    GCHK(w->cells32.ensure(numCells * sizeof(TreeCell32)));
+    cells32Kernel<<<nbCells, kThreads, 0, s>>>(cells, numCells, w->thr.as<double>(), w->cells32.as<TreeCell32>());
+    treeWalkMixedKernel<<<nbWalk, 128, 0, s>>>(w->cells32.as<TreeCell32>(), cells, numCells,
+                                               w->tpos32.as<TreeNode32>(), w->tpos.as<TreeNode>(), vals, n,
+                                               w->thr.as<double>(), softening * softening, softening, G, F,
+                                               w->dtBits.as<unsigned long long>(), w->energy.as<double>());
+    lc->add(1);
+  } else {
+    treeWalkKernel<<<nbWalk, 128, 0, s>>>(cells, numCells, w->tpos.as<TreeNode>(), vals, n, w->thr.as<double>(),
+                                          softening * softening, softening, G, F,
+                                          w->dtBits.as<unsigned long long>(), w->energy.as<double>());
+  }
   walkFinalKernel<<<1, 256, 0, s>>>(w->energy.as<double>(), nbWalk, w->dtBits.as<unsigned long long>(), G, dOut);
   lc->add(2);
   GCHK(cudaGetLastError());

@@ -160,8 +160,9 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
                                                           uint32_t* __restrict__ nbr, double ext2, float bandA,
                                                           float bandB, int cap, int* __restrict__ maxCount) {
+  __shared__ float4 stage[4][32];   // one candidate batch per warp (128-thread blocks)
   const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   if (item >= nItems) return;   // warp-uniform
   const int k0 = items[item];
   const uint32_t cc = P.cell[k0];
@@ -219,34 +220,41 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
             if (mir & 12u) q.y = cy - q.y;
             if (mir & 48u) q.z = cz - q.z;
           }
+          // Stage the batch in shared memory: each lane then reads every
+          // candidate with one broadcast load.
+          stage[wib][lane] = q;
+          __syncwarp();
           const int nval = min(32, e - base);
-          for (int t = 0; t < nval; ++t) {
-            const float xj = __shfl_sync(0xffffffffu, q.x, t);
-            const float yj = __shfl_sync(0xffffffffu, q.y, t);
-            const float zj = __shfl_sync(0xffffffffu, q.z, t);
-            const float aj = __shfl_sync(0xffffffffu, q.w, t);
-            const int j = base + t;
-            if (!active || (j == (int)i && dcode == 0)) continue;
-            const float rx = __fadd_rn(__fsub_rn(pi.x, xj), ox);
-            const float ry = __fadd_rn(__fsub_rn(pi.y, yj), oy);
-            const float rz = __fadd_rn(__fsub_rn(pi.z, zj), oz);
-            const float r2 = rx * rx + ry * ry + rz * rz;
-            const float e2 = fminf(ai2, aj * aj) * r2;
-            bool inside;
-            if (e2 < bandLo) inside = true;
-            else if (e2 > bandHi) inside = false;
-            else {
-              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-              imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
-              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
-                           qz = __dsub_rn(F.f[F_Z][i], zjd);
-              inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
-            }
-            if (inside) {
-              if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-              ++cnt;
+          // the home cell's own batch contains node i itself
+          const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
+          if (active) {
+            for (int t = 0; t < nval; ++t) {
+              if (t == self) continue;
+              const float4 cq = stage[wib][t];
+              const int j = base + t;
+              const float xj = cq.x, yj = cq.y, zj = cq.z, aj = cq.w;
+              const float rx = __fadd_rn(__fsub_rn(pi.x, xj), ox);
+              const float ry = __fadd_rn(__fsub_rn(pi.y, yj), oy);
+              const float rz = __fadd_rn(__fsub_rn(pi.z, zj), oz);
+              const float r2 = rx * rx + ry * ry + rz * rz;
+              const float e2 = fminf(ai2, aj * aj) * r2;
+              bool inside;
+              if (e2 < bandLo) inside = true;
+              else if (e2 > bandHi) inside = false;
+              else {
+                double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+                imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+                const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                             qz = __dsub_rn(F.f[F_Z][i], zjd);
+                inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+              }
+              if (inside) {
+                if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
+                ++cnt;
+              }
             }
           }
+          __syncwarp();
         }
       }
   if (active) {

@@ -86,7 +86,7 @@ __device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, cons
   }
 }
 
-template <bool XSPH, bool COMPAT, bool MULTI, int MINB>
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF>
 __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
@@ -122,11 +122,37 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   for (int k = 0; k < 9; ++k) { D[k] = 0.f; M[k] = 0.f; }
 
   const int cnt = nl.count[i];
+  // PF: software pipeline over the neighbour list -- the entry two slots
+  // ahead and the node data one slot ahead are loaded while the current pair
+  // is evaluated, so the gathers overlap the arithmetic.
+  uint32_t entA = 0u, entB = 0u;
+  float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA, thA = pjA;
+  if (PF) {
+    if (cnt > 0) {
+      entA = nl.nbr[nbSlot(i, 0, nl.cap)];
+      const int j0 = (int)(entA & kIndexMask);
+      pjA = P.posh[j0]; vjA = P.velm[j0]; thA = P.thermo[j0];
+    }
+    if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
+  }
   for (int q = 0; q < cnt; ++q) {
     const long long k = nbSlot(i, q, nl.cap);
-    const uint32_t ent = nl.nbr[k];
+    uint32_t ent;
+    float4 pj, vj4, thj;
+    if (PF) {
+      ent = entA; pj = pjA; vj4 = vjA; thj = thA;
+      if (q + 1 < cnt) {
+        const int jn = (int)(entB & kIndexMask);
+        pjA = P.posh[jn]; vjA = P.velm[jn]; thA = P.thermo[jn];
+        entA = entB;
+      }
+      if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
+    } else {
+      ent = nl.nbr[k];
+      const int jj = (int)(ent & kIndexMask);
+      pj = P.posh[jj]; vj4 = P.velm[jj]; thj = P.thermo[jj];
+    }
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
-    const float4 pj = P.posh[j], vj4 = P.velm[j], thj = P.thermo[j];
     float rx, ry, rz;
     relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
     float vxj = vj4.x, vyj = vj4.y, vzj = vj4.z;
@@ -302,11 +328,25 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     const float hi = 1.0f / pi.w;
     float s = 0.f, c = 0.f, bestPair = 3.0e38f;
     const int cnt = nl.count[i];
+    // software pipeline: entry two slots ahead, node data one slot ahead
+    uint32_t entA = 0u, entB = 0u;
+    float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA;
+    if (cnt > 0) {
+      entA = nl.nbr[nbSlot(i, 0, nl.cap)];
+      const int j0 = (int)(entA & kIndexMask);
+      pjA = P.posh[j0]; vjA = P.velm[j0];
+    }
+    if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
     for (int q = 0; q < cnt; ++q) {
-      const long long k = nbSlot(i, q, nl.cap);
-      const uint32_t ent = nl.nbr[k];
+      const uint32_t ent = entA;
+      const float4 pj = pjA, vj = vjA;
+      if (q + 1 < cnt) {
+        const int jn = (int)(entB & kIndexMask);
+        pjA = P.posh[jn]; vjA = P.velm[jn];
+        entA = entB;
+      }
+      if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
       const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
-      const float4 pj = P.posh[j], vj = P.velm[j];
       float rx, ry, rz;
       relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
       const float aj = pj.w;
@@ -522,11 +562,10 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
   const float feps = (float)DBL_EPSILON;
   float s = 0.0f, c = 0.0f;
   const int cnt = nl.count[i];
-  for (int q = 0; q < cnt; ++q) {
-    const long long k = nbSlot(i, q, nl.cap);
-    const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
-    const float4 hj = vhi[j], lj = vlo[j];
+  // One slot: du = (v_j - v_i) . pacc_ij with the half-step velocities as
+  // hi + lo float pairs, split by the DepsDt0 weights.
+  auto slot = [&](uint32_t ent, float4 hj, float4 lj, float p0, float p1, float p2) {
+    const int dcode = (int)(ent >> kIndexBits);
     float hx = hj.x, hy = hj.y, hz = hj.z, lx = lj.x, ly = lj.y, lz = lj.z;
     const uint32_t mir = (uint32_t)dcode & mm;
     if (mir) {
@@ -538,11 +577,38 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
     const float wx = __fadd_rn(__fsub_rn(hx, hi.x), __fsub_rn(lx, lo.x));
     const float wy = __fadd_rn(__fsub_rn(hy, hi.y), __fsub_rn(ly, lo.y));
     const float wz = __fadd_rn(__fsub_rn(hz, hi.z), __fsub_rn(lz, lo.z));
-    const float du = __fmaf_rn(wz, pacc[3 * k + 2], __fmaf_rn(wy, pacc[3 * k + 1], __fmul_rn(wx, pacc[3 * k])));
+    const float du = __fmaf_rn(wz, p2, __fmaf_rn(wy, p1, __fmul_rn(wx, p0)));
     const float sg = du < 0.0f ? -1.0f : 1.0f;
     const float weighti = fmaxf(feps, d0i * sg);
     const float weightj = fmaxf(feps, hj.w * sg);
     kahanAdd(s, c, __fdividef(weighti, weighti + weightj) * du);
+  };
+  // Batches of four slots: all their loads are issued before any is used,
+  // so four gathers and pair-acceleration reads are in flight together.
+  constexpr int B = 4;
+  int q = 0;
+  for (; q + B <= cnt; q += B) {
+    uint32_t e[B];
+    float4 H[B], L[B];
+    float p[B][3];
+#pragma unroll
+    for (int u = 0; u < B; ++u) e[u] = nl.nbr[nbSlot(i, q + u, nl.cap)];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const long long k = nbSlot(i, q + u, nl.cap);
+      const int j = (int)(e[u] & kIndexMask);
+      H[u] = vhi[j];
+      L[u] = vlo[j];
+      p[u][0] = pacc[3 * k]; p[u][1] = pacc[3 * k + 1]; p[u][2] = pacc[3 * k + 2];
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) slot(e[u], H[u], L[u], p[u][0], p[u][1], p[u][2]);
+  }
+  for (; q < cnt; ++q) {
+    const long long k = nbSlot(i, q, nl.cap);
+    const uint32_t ent = nl.nbr[k];
+    const int j = (int)(ent & kIndexMask);
+    slot(ent, vhi[j], vlo[j], pacc[3 * k], pacc[3 * k + 1], pacc[3 * k + 2]);
   }
   const double sum = kahanValue(s, c);
   F.f[F_DEPS_COMPAT][i] = sum;
@@ -558,27 +624,37 @@ void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, L
   lc->add(1);
 }
 
-// variant: minimum resident blocks per SM requested from the compiler for the
-// common path (compatible energy, no XSPH, one NodeList): 0 -> 4 (no
-// register cap below 128), 1 -> 5 (<= 102 registers, no spills), 2 -> 6
-// (<= 85 registers, small spills).  Chosen at run time by the autotuner.
+// variant (common path: compatible energy, no XSPH, one NodeList): the
+// minimum resident blocks per SM requested from the compiler -- 4 (no
+// register cap below 128), 5 (<= 102 registers), 6 (<= 85 registers) -- for
+// variants 0-2 without and 3-5 with the software-pipelined neighbour loop.
+// Chosen at run time by the autotuner (kPairVariants).
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc) {
   const int b = 128;
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
-#define SPH_PAIR32(X, C, M, MB) pairKernelFP32<X, C, M, MB><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
+#define SPH_PAIR32(X, C, M, MB, PF) \
+  pairKernelFP32<X, C, M, MB, PF><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
   if (!hp.xsph && hp.compatible && !multi) {
-    if (variant == 0) SPH_PAIR32(false, true, false, 4);
-    else if (variant == 2) SPH_PAIR32(false, true, false, 6);
-    else SPH_PAIR32(false, true, false, 5);
+    switch (variant) {
+      case 0: SPH_PAIR32(false, true, false, 4, false); break;
+      case 2: SPH_PAIR32(false, true, false, 6, false); break;
+      case 3: SPH_PAIR32(false, true, false, 4, true); break;
+      case 4: SPH_PAIR32(false, true, false, 5, true); break;
+      case 5: SPH_PAIR32(false, true, false, 6, true); break;
+      default: SPH_PAIR32(false, true, false, 5, false); break;
+    }
   } else if (hp.xsph) {
-    if (hp.compatible) { if (multi) SPH_PAIR32(true, true, true, 5); else SPH_PAIR32(true, true, false, 5); }
-    else { if (multi) SPH_PAIR32(true, false, true, 5); else SPH_PAIR32(true, false, false, 5); }
+    if (hp.compatible) {
+      if (multi) SPH_PAIR32(true, true, true, 5, false); else SPH_PAIR32(true, true, false, 5, false);
+    } else {
+      if (multi) SPH_PAIR32(true, false, true, 5, false); else SPH_PAIR32(true, false, false, 5, false);
+    }
   } else {
-    if (hp.compatible) SPH_PAIR32(false, true, true, 5);
-    else { if (multi) SPH_PAIR32(false, false, true, 5); else SPH_PAIR32(false, false, false, 5); }
+    if (hp.compatible) SPH_PAIR32(false, true, true, 5, false);
+    else { if (multi) SPH_PAIR32(false, false, true, 5, false); else SPH_PAIR32(false, false, false, 5, false); }
   }
 #undef SPH_PAIR32
   lc->add(1);

@@ -56,6 +56,7 @@ void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroPa
                  LaunchCounter* lc);
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                     double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
+constexpr int kPairVariants = 6;   // autotuned variants of launchPairFP32 (common path)
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);
@@ -108,7 +109,10 @@ void gravityDestroy(GravityWork* w);
 // Build the octree of the current positions and walk it; writes F_GRAV_*,
 // F_POT (already multiplied by G) and returns dtMinAcc via dOut[0], extra
 // energy via dOut[1].
-int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening, double opening, double* dOut,
+// mixed: FP32 interaction terms on double-float coordinates with compensated
+// accumulation (decisions as in FP64); otherwise FP64 throughout.
+int gravityEvaluate(GravityWork* w, Fields F, long n, double G, double softening, double opening, bool mixed,
+                    double* dOut,
                     cudaStream_t s, LaunchCounter* lc, char* err, int errlen);
 
 }  // namespace sph

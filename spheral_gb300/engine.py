@@ -130,6 +130,15 @@ class Engine:
     def synchronize(self):
         self._chk(self.L.sphgpu_synchronize(self.h))
 
+    def pair_variant(self):
+        """(variant in use, number of variants) of the mixed-mode pair kernel."""
+        v, nv = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.L.sphgpu_get_pair_variant(self.h, ctypes.byref(v), ctypes.byref(nv)))
+        return v.value, nv.value
+
+    def set_pair_variant(self, v):
+        self._chk(self.L.sphgpu_set_pair_variant(self.h, v))
+
     @staticmethod
     def ensemble_advance(engines, nsteps, max_time=1.0e300, nthreads=0):
         """nsteps steps of every engine at once (sphgpu_ensemble_advance):

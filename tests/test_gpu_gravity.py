@@ -64,10 +64,14 @@ def test_tree_gravity_dt_vote(native_lib, oracle_mod, case):
     assert abs(dg - do) <= 1e-12 * do, (dg, do, reason)
 
 
-def test_tree_gravity_in_mixed_mode(native_lib, oracle_mod):
-    """The walk is FP64 in both precision modes."""
-    p, eng, orc = _gravity_pair(oracle_mod, CASES["evrard_4096"], precision="fp32")
-    bad = compare_fields(eng, orc, ["DvDtGravity", "potential"], 1e-12)
+@pytest.mark.parametrize("case", ["evrard_20000", "clustered", "uniform_box"])
+def test_tree_gravity_in_mixed_mode(native_lib, oracle_mod, case):
+    """Mixed walk: FP32 terms on double-float separations with compensated
+    sums, FP64 decisions in the guard band.  Same far/near sets as the FP64
+    walk, so the only differences are FP32 rounding of each term: normwise
+    <= 2e-6 of the oracle (measured ~1e-7)."""
+    p, eng, orc = _gravity_pair(oracle_mod, CASES[case], precision="fp32")
+    bad = compare_fields(eng, orc, ["DvDtGravity", "potential"], 2e-6)
     assert not bad, bad
 
 
