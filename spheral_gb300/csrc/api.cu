@@ -154,6 +154,7 @@ struct sphgpu_ctx {
   GravityWork* grav = nullptr;
   bool initialized = false;
   cudaEvent_t tA = nullptr, tB = nullptr;
+  int itemWidth = 32;        // lanes per work item of the neighbour search
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
   bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
   long tunedN = 0;
@@ -435,13 +436,17 @@ void buildNeighbors(sphgpu_ctx* c) {
     return m;
   };
   auto capFor = [](int m) { return std::max(32, ((m + m / 8 + 16 + 31) / 32) * 32); };
-  // work items: first node of every chunk of up to 32 nodes of a cell
+  // work items: first node of every chunk of up to `width` nodes of a cell;
+  // the group width follows the mean occupancy of the cells so that few
+  // lanes of a group idle (a chunk rarely has fewer nodes than lanes).
+  const double occupancy = (double)n / ((double)g.nc[0] * g.nc[1] * g.nc[2]);
+  c->itemWidth = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
   {
     Scope sc(c->prof, "neighbor_items");
     long long* pos = c->nbrStart.as<long long>();
-    launchItemFlags(k, n, c->cellStart.as<int>(), c->itemFlag.as<int>(), c->stream, &c->lc);
+    launchItemFlags(k, n, c->cellStart.as<int>(), c->itemWidth, c->itemFlag.as<int>(), c->stream, &c->lc);
     scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, pos + n, c->stream, &c->lc);
     launchItemFill(c->itemFlag.as<int>(), pos, n, c->items.as<int>(), c->stream, &c->lc);
     CUDA_OK(cudaMemcpyAsync(c->hsmall + 41, pos + n, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
@@ -458,7 +463,7 @@ void buildNeighbors(sphgpu_ctx* c) {
   if (c->nbCap == 0) {   // first build: size the lists with a counting pass
     CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     Scope sc(c->prof, "neighbor_count");
-    launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, g, c->cellStart.as<int>(),
+    launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, c->itemWidth, g, c->cellStart.as<int>(),
                         c->cellEnd.as<int>(), c->counts.as<int>(), dMax, nullptr, 0, ext2, c->stream, &c->lc);
     c->check();
     c->nbCap = capFor(readMax());
@@ -468,7 +473,7 @@ void buildNeighbors(sphgpu_ctx* c) {
     CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     {
       Scope sc(c->prof, "neighbors");
-      launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, g, c->cellStart.as<int>(),
+      launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, c->itemWidth, g, c->cellStart.as<int>(),
                           c->cellEnd.as<int>(), c->counts.as<int>(), dMax, c->nbr.as<uint32_t>(), c->nbCap, ext2,
                           c->stream, &c->lc);
     }

@@ -96,80 +96,64 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 // positions settles every candidate outside a narrow band around the
 // threshold; candidates inside the band get the exact FP64 test with the
 // reference's operation order, so the neighbour sets are exact.
+//
+// The search is group-cooperative.  A group of W lanes (W = 8, 16 or 32,
+// chosen from the mean cell occupancy so few lanes idle) owns a chunk of up
+// to W consecutive nodes of one cell (an "item"), so the 27 candidate cells,
+// their offset codes and mirror flags are uniform across the group.  Each
+// candidate cell is read in coalesced batches of W nodes staged in shared
+// memory; every lane tests its own node against the batch.  Candidate cells
+// are visited in a fixed order (dz, dy, dx from -1 to 1) and nodes within a
+// cell in sorted order, so every list has a reproducible order.
 // WRITE false: count only; true: count and write the warp-interleaved lists
 // (slots beyond cap are counted, not written).
-template <bool WRITE>
-__global__ void __launch_bounds__(128) neighborKernel(Fields F, Fields32 P, long n, Grid g,
-                                                      const int* __restrict__ cellStart,
-                                                      const int* __restrict__ cellEnd, int* __restrict__ counts,
-                                                      uint32_t* __restrict__ nbr, double ext2, float bandA,
-                                                      float bandB, int cap, int* __restrict__ maxCount) {
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* __restrict__ X = F.f[F_X];
-  const double* __restrict__ Y = F.f[F_Y];
-  const double* __restrict__ Z = F.f[F_Z];
-  const double* __restrict__ A = F.f[F_HINV];
-  const uint32_t cc = P.cell[i];
-  int ci[3];
-  unpackCell(cc, ci);
-  const float4 pi = P.posh[i];
-  const float del = __fmaf_rn(bandA, pi.w, bandB);   // per-node band half-width (relative)
-  const float e2t = (float)ext2;
-  const float bandLo = del < 0.5f ? e2t * (1.0f - del) : -1.0f;
-  const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
-  const float cellx = (float)g.cell[0], celly = (float)g.cell[1], cellz = (float)g.cell[2];
-  const uint32_t mm = mirrorMask(g, ci);
-  int cnt = 0;
-  forEachCandidate(g, cc, cellStart, cellEnd, [&](int j, int dcode) {
-    if (j == (int)i && dcode == 0) return;
-    const float4 pj = P.posh[j];
-    float rx, ry, rz;
-    relSep(pi, pj, dcode, mm, cellx, celly, cellz, rx, ry, rz);
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    const float e2i = pi.w * pi.w * r2, e2j = pj.w * pj.w * r2;
-    const float e2 = fminf(e2i, e2j);
-    bool inside;
-    if (e2 < bandLo) inside = true;
-    else if (e2 > bandHi) inside = false;
-    else {
-      const double xi = X[i], yi = Y[i], zi = Z[i];
-      double xj = X[j], yj = Y[j], zj = Z[j];
-      imagePos(g, imageCode(g, ci, dcode), xj, yj, zj);
-      const double qx = __dsub_rn(xi, xj), qy = __dsub_rn(yi, yj), qz = __dsub_rn(zi, zj);
-      inside = eta2Exact(A[i], qx, qy, qz) <= ext2 || eta2Exact(A[j], qx, qy, qz) <= ext2;
-    }
-    if (inside) {
-      if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-      ++cnt;
-    }
-  });
-  counts[i] = cnt;
-  atomicMax(maxCount, cnt);
-}
-
-// Warp-cooperative form of the same search.  One warp owns a chunk of up to
-// 32 consecutive nodes of one cell (an "item"), so the 27 candidate cells,
-// their offset codes and mirror flags are uniform across the warp.  Each
-// candidate cell is read in coalesced batches of 32 nodes that are broadcast
-// lane to lane; every lane tests its own node against the batch.  Candidates
-// are visited in the same order as neighborKernel, so the lists are identical.
-template <bool WRITE>
+template <bool WRITE, int W>
 __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
                                                           uint32_t* __restrict__ nbr, double ext2, float bandA,
                                                           float bandB, int cap, int* __restrict__ maxCount) {
-  __shared__ float4 stage[4][32];   // one candidate batch per warp (128-thread blocks)
-  const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  if (item >= nItems) return;   // warp-uniform
+  constexpr int G = 128 / W;             // groups per 128-thread block
+  __shared__ float4 stage[G][W];         // one candidate batch per group
+  __shared__ int2 range[G][27];          // node ranges of the 27 candidate cells
+  const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) / W);
+  const int lane = threadIdx.x % W, wib = threadIdx.x / W;
+  // lanes of this group within the warp
+  const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << ((threadIdx.x & 31) / W * W));
+  if (item >= nItems) return;   // group-uniform
   const int k0 = items[item];
   const uint32_t cc = P.cell[k0];
   int hc[3];
   unpackCell(cc, hc);
-  const uint32_t homeKey = morton3((uint32_t)hc[0], (uint32_t)hc[1], (uint32_t)hc[2]);
-  const int k1 = min(k0 + 32, cellEnd[homeKey]);
+  // The 27 cell ranges are independent loads: fetch them lane-parallel so
+  // their latencies overlap.  Cell t is (dx, dy, dz) = (t%3, t/3%3, t/9) - 1.
+  for (int t = lane; t < 27; t += W) {
+    const int d[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
+    int cell[3];
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      int nn = hc[a] + d[a];
+      if (nn < 0) {
+        if (g.kindLo[a] == AXIS_PERIODIC) nn = g.nc[a] - 1;
+        else if (g.kindLo[a] == AXIS_REFLECT) nn = 0;
+        else ok = false;
+      } else if (nn >= g.nc[a]) {
+        if (g.kindHi[a] == AXIS_PERIODIC) nn = 0;
+        else if (g.kindHi[a] == AXIS_REFLECT) nn = g.nc[a] - 1;
+        else ok = false;
+      }
+      cell[a] = nn;
+    }
+    int2 r = make_int2(0, 0);
+    if (ok) {
+      const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
+      r = make_int2(cellStart[key], cellEnd[key]);
+    }
+    range[wib][t] = r;
+  }
+  __syncwarp(gmask);
+  const int k1 = min(k0 + W, range[wib][13].y);   // cell 13 is the home cell
   const long i = k0 + lane;
   const bool active = i < k1;
   const float4 pi = active ? P.posh[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -181,95 +165,86 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
   int cnt = 0;
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int d[3] = {dx, dy, dz};
-        int cell[3];
-        int dcode = 0;
-        bool ok = true;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          int nn = hc[a] + d[a];
-          if (d[a] != 0) dcode |= (d[a] < 0 ? 1 : 2) << (2 * a);
-          if (nn < 0) {
-            if (g.kindLo[a] == AXIS_PERIODIC) nn = g.nc[a] - 1;
-            else if (g.kindLo[a] == AXIS_REFLECT) nn = 0;
-            else ok = false;
-          } else if (nn >= g.nc[a]) {
-            if (g.kindHi[a] == AXIS_PERIODIC) nn = 0;
-            else if (g.kindHi[a] == AXIS_REFLECT) nn = g.nc[a] - 1;
-            else ok = false;
+  // first batch of the first non-empty cell, loaded ahead of use
+  int tn = 0;
+  while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
+  float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (tn < 27 && range[wib][tn].x + lane < range[wib][tn].y) qn = P.posh[range[wib][tn].x + lane];
+  while (tn < 27) {
+    const int t = tn;
+    const int s = range[wib][t].x, e = range[wib][t].y;
+    const int d0 = t % 3, d1 = (t / 3) % 3, d2 = t / 9;   // 0, 1, 2 for -1, 0, +1
+    const int dcode = (d0 == 0 ? 1 : (d0 == 2 ? 2 : 0)) | ((d1 == 0 ? 1 : (d1 == 2 ? 2 : 0)) << 2) |
+                      ((d2 == 0 ? 1 : (d2 == 2 ? 2 : 0)) << 4);
+    const uint32_t mir = (uint32_t)dcode & mm;
+    const float ox = d0 == 0 ? cx : (d0 == 2 ? -cx : 0.0f);
+    const float oy = d1 == 0 ? cy : (d1 == 2 ? -cy : 0.0f);
+    const float oz = d2 == 0 ? cz : (d2 == 2 ? -cz : 0.0f);
+    // next non-empty cell
+    ++tn;
+    while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
+    for (int base = s; base < e; base += W) {
+      float4 q = qn;
+      if (base + W < e) {            // another batch of this cell follows
+        qn = (base + W + lane < e) ? P.posh[base + W + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+      } else if (tn < 27) {          // last batch: prefetch the next cell's first batch
+        const int sn = range[wib][tn].x, en = range[wib][tn].y;
+        qn = (sn + lane < en) ? P.posh[sn + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      if (mir) {
+        if (mir & 3u) q.x = cx - q.x;
+        if (mir & 12u) q.y = cy - q.y;
+        if (mir & 48u) q.z = cz - q.z;
+      }
+      // Stage the batch in shared memory: each lane then reads every
+      // candidate with one broadcast load.
+      stage[wib][lane] = q;
+      __syncwarp(gmask);
+      const int nval = min(W, e - base);
+      // the home cell's own batch contains node i itself
+      const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
+      if (active) {
+        for (int u = 0; u < nval; ++u) {
+          if (u == self) continue;
+          const float4 cq = stage[wib][u];
+          const int j = base + u;
+          const float rx = __fadd_rn(__fsub_rn(pi.x, cq.x), ox);
+          const float ry = __fadd_rn(__fsub_rn(pi.y, cq.y), oy);
+          const float rz = __fadd_rn(__fsub_rn(pi.z, cq.z), oz);
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          const float e2 = fminf(ai2, cq.w * cq.w) * r2;
+          bool inside;
+          if (e2 < bandLo) inside = true;
+          else if (e2 > bandHi) inside = false;
+          else {
+            double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+            imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+            const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                         qz = __dsub_rn(F.f[F_Z][i], zjd);
+            inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
           }
-          cell[a] = nn;
-        }
-        if (!ok) continue;
-        const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
-        const int s = cellStart[key], e = cellEnd[key];
-        const uint32_t mir = (uint32_t)dcode & mm;
-        const int d0 = dcode & 3, d1 = (dcode >> 2) & 3, d2 = (dcode >> 4) & 3;
-        const float ox = d0 == 1 ? cx : (d0 == 2 ? -cx : 0.0f);
-        const float oy = d1 == 1 ? cy : (d1 == 2 ? -cy : 0.0f);
-        const float oz = d2 == 1 ? cz : (d2 == 2 ? -cz : 0.0f);
-        for (int base = s; base < e; base += 32) {
-          const int jj = base + lane;
-          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (jj < e) q = P.posh[jj];
-          if (mir) {
-            if (mir & 3u) q.x = cx - q.x;
-            if (mir & 12u) q.y = cy - q.y;
-            if (mir & 48u) q.z = cz - q.z;
+          if (inside) {
+            if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
+            ++cnt;
           }
-          // Stage the batch in shared memory: each lane then reads every
-          // candidate with one broadcast load.
-          stage[wib][lane] = q;
-          __syncwarp();
-          const int nval = min(32, e - base);
-          // the home cell's own batch contains node i itself
-          const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
-          if (active) {
-            for (int t = 0; t < nval; ++t) {
-              if (t == self) continue;
-              const float4 cq = stage[wib][t];
-              const int j = base + t;
-              const float xj = cq.x, yj = cq.y, zj = cq.z, aj = cq.w;
-              const float rx = __fadd_rn(__fsub_rn(pi.x, xj), ox);
-              const float ry = __fadd_rn(__fsub_rn(pi.y, yj), oy);
-              const float rz = __fadd_rn(__fsub_rn(pi.z, zj), oz);
-              const float r2 = rx * rx + ry * ry + rz * rz;
-              const float e2 = fminf(ai2, aj * aj) * r2;
-              bool inside;
-              if (e2 < bandLo) inside = true;
-              else if (e2 > bandHi) inside = false;
-              else {
-                double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-                imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
-                const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
-                             qz = __dsub_rn(F.f[F_Z][i], zjd);
-                inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
-              }
-              if (inside) {
-                if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-                ++cnt;
-              }
-            }
-          }
-          __syncwarp();
         }
       }
-  if (active) {
-    counts[i] = cnt;
-    atomicMax(maxCount, cnt);
+      __syncwarp(gmask);
+    }
   }
+  if (active) counts[i] = cnt;
+  // one atomic per group: a per-node atomic on a single address serialises
+  const int gmax = __reduce_max_sync(gmask, active ? cnt : 0);
+  if (lane == 0) atomicMax(maxCount, gmax);
 }
 
 // Items of the warp search: the first node of every chunk of up to 32 nodes
 // of a cell.  flag pass + scan + fill.
 __global__ void itemFlagKernel(const uint32_t* __restrict__ keys, long n, const int* __restrict__ cellStart,
-                               int* __restrict__ flag) {
+                               int width, int* __restrict__ flag) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  flag[k] = ((k - cellStart[keys[k]]) % 32 == 0) ? 1 : 0;
+  flag[k] = ((k - cellStart[keys[k]]) % width == 0) ? 1 : 0;
 }
 __global__ void itemFillKernel(const int* __restrict__ flag, const long long* __restrict__ pos, long n,
                                int* __restrict__ items) {
@@ -864,19 +839,6 @@ static void neighborBand(const Grid& g, double ext2, float& bandA, float& bandB)
   bandA = (float)(4.0 * 20.0 * std::sqrt(3.0) * u * cmax / ext);
   bandB = (float)(4.0 * 7.0 * u);
 }
-void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                     int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,
-                     LaunchCounter* lc) {
-  float lo, hi;
-  neighborBand(g, ext2, lo, hi);
-  if (nbr)
-    neighborKernel<true><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nbr, ext2, lo, hi,
-                                                          cap, maxCount);
-  else
-    neighborKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, P, n, g, cellStart, cellEnd, counts, nullptr, ext2, lo,
-                                                           hi, 0, maxCount);
-  lc->add(1);
-}
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                       cudaStream_t s, LaunchCounter* lc) {
   const size_t sm = sizeof(double) * 3 * (hp.tableN1 + 1);
@@ -972,28 +934,31 @@ void launchCountsOut(const int* counts, const int* orig, double* stage, long n, 
   lc->add(1);
 }
 
-void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int* flag, cudaStream_t s,
+void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int width, int* flag, cudaStream_t s,
                      LaunchCounter* lc) {
-  itemFlagKernel<<<gridFor(n, 256), 256, 0, s>>>(keys, n, cellStart, flag);
+  itemFlagKernel<<<gridFor(n, 256), 256, 0, s>>>(keys, n, cellStart, width, flag);
   lc->add(1);
 }
 void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc) {
   itemFillKernel<<<gridFor(n, 256), 256, 0, s>>>(flag, pos, n, items);
   lc->add(1);
 }
-void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, Grid g,
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, int width, Grid g,
                          const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
                          double ext2, cudaStream_t s, LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
-  const long threads = (long)nItems * 32;
+  const long threads = (long)nItems * width;
   const unsigned gb = (unsigned)((threads + 127) / 128);
-  if (nbr)
-    neighborWarpKernel<true><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts, nbr, ext2, lo,
-                                                 hi, cap, maxCount);
-  else
-    neighborWarpKernel<false><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts, nullptr, ext2,
-                                                  lo, hi, 0, maxCount);
+#define SPH_NBR(WR, WD)                                                                                        \
+  neighborWarpKernel<WR, WD><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts,        \
+                                                WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount)
+  if (nbr) {
+    if (width == 8) SPH_NBR(true, 8); else if (width == 16) SPH_NBR(true, 16); else SPH_NBR(true, 32);
+  } else {
+    if (width == 8) SPH_NBR(false, 8); else if (width == 16) SPH_NBR(false, 16); else SPH_NBR(false, 32);
+  }
+#undef SPH_NBR
   lc->add(1);
 }
 

@@ -36,16 +36,13 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
                    cudaStream_t s, LaunchCounter* lc);
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
-// Counts the neighbours of every node and, with nbr != nullptr, writes them
-// into the warp-interleaved lists of capacity cap (entries beyond cap are
-// counted, not written); *maxCount (device) receives the largest count.
-void launchNeighbors(const Fields& F, Fields32 P, long n, Grid g, const int* cellStart, const int* cellEnd,
-                     int* counts, int* maxCount, uint32_t* nbr, int cap, double ext2, cudaStream_t s,
+// Group-cooperative neighbour search over items (first node of each chunk of
+// up to `width` nodes of a cell).
+// width: nodes per work item of the group-cooperative search (8, 16 or 32).
+void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int width, int* flag, cudaStream_t s,
                      LaunchCounter* lc);
-// Warp-cooperative search over items (first node of each <= 32-node chunk of a cell).
-void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int* flag, cudaStream_t s, LaunchCounter* lc);
 void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc);
-void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, Grid g,
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, int width, Grid g,
                          const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
                          double ext2, cudaStream_t s, LaunchCounter* lc);
 

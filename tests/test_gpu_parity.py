@@ -26,6 +26,9 @@ CASES = {
     "two_lists": lambda: problems.random_box(n_side=12, seed=24, boundaries="periodic", two_lists=True),
     "sod": lambda: problems.sod(nx1=16, ny1=20),
     "kh": lambda: problems.kelvin_helmholtz(n1=16),
+    # low cell occupancy: the neighbour search runs 8- and 16-lane groups
+    "sweep_k32": lambda: problems.sweep_box(n_side=24, neighbors=32),
+    "sweep_k64": lambda: problems.sweep_box(n_side=20, neighbors=64),
 }
 
 
