@@ -142,7 +142,6 @@ struct sphgpu_ctx {
   int nbCap = 0;             // slots per node of the warp-interleaved neighbour lists (0: not sized yet)
   int nbCapNext = 0;         // smaller capacity to adopt at the next build (0: keep)
   DBuf itemFlag, items;      // work items of the warp-cooperative neighbour search
-  int nItems = 0;
   bool haveNeighbors = false;
   // scratch
   DBuf scratch, small;
@@ -155,6 +154,9 @@ struct sphgpu_ctx {
   bool initialized = false;
   cudaEvent_t tA = nullptr, tB = nullptr;
   int itemWidth = 32;        // lanes per work item of the neighbour search
+  int itemBound = 0;         // upper bound on the number of work items
+  DBuf itemCount;            // device: number of work items
+  bool capCheckPending = false, totalPending = false;
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
   bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
   long tunedN = 0;
@@ -366,11 +368,44 @@ void buildGrid(sphgpu_ctx* c) {
   c->grid = g;
 }
 
+int capFor(int m) { return std::max(32, ((m + m / 8 + 16 + 31) / 32) * 32); }
+int* maxCountPtr(sphgpu_ctx* c) { return reinterpret_cast<int*>(c->small.as<double>() + 40); }
+int readMaxCount(sphgpu_ctx* c) {
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, maxCountPtr(c), sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  int m;
+  std::memcpy(&m, c->hsmall + 40, sizeof(int));
+  return m;
+}
+// Write pass of the neighbour search into lists of capacity nbCap; the
+// largest count lands in the maxCount slot.
+void writeLists(sphgpu_ctx* c) {
+  c->nbr.ensure(std::max<size_t>(1, c->nbSlots()) * sizeof(uint32_t));
+  CUDA_OK(cudaMemsetAsync(maxCountPtr(c), 0, sizeof(int), c->stream));
+  Scope sc(c->prof, "neighbors");
+  launchNeighborsWarp(c->F, c->f32(), c->n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
+                      c->itemWidth, c->grid, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
+                      maxCountPtr(c), c->nbr.as<uint32_t>(), c->nbCap, c->hp.extent * c->hp.extent, c->stream,
+                      &c->lc);
+  c->check();
+}
+// CSR offsets of the lists (caller-order transfers) and their total, read
+// back without a synchronisation.
+void scanTotals(sphgpu_ctx* c) {
+  const long n = c->n;
+  long long* dTot = c->nbrStart.as<long long>() + n;
+  scanExclusive<int>(c->counts.as<int>(), c->nbrStart.as<long long>(), n, c->scanWs.p, dTot, c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 42, dTot, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+  c->totalPending = true;
+}
+bool resolveNeighbors(sphgpu_ctx* c);
+
 //------------------------------------------------------------------------------
 // Neighbour build: cell keys -> stable radix sort -> permute every field ->
 // cell ranges -> count -> scan -> fill.
 //------------------------------------------------------------------------------
-void buildNeighbors(sphgpu_ctx* c) {
+void buildNeighbors(sphgpu_ctx* c, bool deferCheck = false) {
   const long n = c->n;
   buildGrid(c);
   const Grid& g = c->grid;
@@ -426,34 +461,23 @@ void buildNeighbors(sphgpu_ctx* c) {
   c->counts.ensure(n * sizeof(int));
   c->nbrStart.ensure((n + 1) * sizeof(long long));
   c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
-  const double ext2 = c->hp.extent * c->hp.extent;
-  int* dMax = reinterpret_cast<int*>(c->small.as<double>() + 40);
-  auto readMax = [&]() {
-    CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, dMax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
-    int m;
-    std::memcpy(&m, c->hsmall + 40, sizeof(int));
-    return m;
-  };
-  auto capFor = [](int m) { return std::max(32, ((m + m / 8 + 16 + 31) / 32) * 32); };
+  c->itemCount.ensure(sizeof(long long));
   // work items: first node of every chunk of up to `width` nodes of a cell;
   // the group width follows the mean occupancy of the cells so that few
   // lanes of a group idle (a chunk rarely has fewer nodes than lanes).
-  const double occupancy = (double)n / ((double)g.nc[0] * g.nc[1] * g.nc[2]);
+  const double cellsTotal = (double)g.nc[0] * g.nc[1] * g.nc[2];
+  const double occupancy = (double)n / cellsTotal;
   c->itemWidth = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
+  // every non-empty cell adds at most one partial chunk
+  c->itemBound = (int)std::min<double>((double)n, (double)(n / c->itemWidth) + cellsTotal);
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
   {
     Scope sc(c->prof, "neighbor_items");
     long long* pos = c->nbrStart.as<long long>();
     launchItemFlags(k, n, c->cellStart.as<int>(), c->itemWidth, c->itemFlag.as<int>(), c->stream, &c->lc);
-    scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, pos + n, c->stream, &c->lc);
+    scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, c->itemCount.as<long long>(), c->stream, &c->lc);
     launchItemFill(c->itemFlag.as<int>(), pos, n, c->items.as<int>(), c->stream, &c->lc);
-    CUDA_OK(cudaMemcpyAsync(c->hsmall + 41, pos + n, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OK(cudaStreamSynchronize(c->stream));
-    long long ni;
-    std::memcpy(&ni, c->hsmall + 41, sizeof(long long));
-    c->nItems = (int)ni;
   }
   c->check();
   if (c->nbCapNext > 0) {   // adopt a smaller capacity decided at the previous build
@@ -461,40 +485,64 @@ void buildNeighbors(sphgpu_ctx* c) {
     c->nbCapNext = 0;
   }
   if (c->nbCap == 0) {   // first build: size the lists with a counting pass
+    int* dMax = maxCountPtr(c);
     CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
     Scope sc(c->prof, "neighbor_count");
-    launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, c->itemWidth, g, c->cellStart.as<int>(),
-                        c->cellEnd.as<int>(), c->counts.as<int>(), dMax, nullptr, 0, ext2, c->stream, &c->lc);
+    launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
+                        c->itemWidth, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
+                        nullptr, 0, c->hp.extent * c->hp.extent, c->stream, &c->lc);
     c->check();
-    c->nbCap = capFor(readMax());
+    c->nbCap = capFor(readMaxCount(c));
   }
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    c->nbr.ensure(std::max<size_t>(1, c->nbSlots()) * sizeof(uint32_t));
-    CUDA_OK(cudaMemsetAsync(dMax, 0, sizeof(int), c->stream));
-    {
-      Scope sc(c->prof, "neighbors");
-      launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->nItems, c->itemWidth, g, c->cellStart.as<int>(),
-                          c->cellEnd.as<int>(), c->counts.as<int>(), dMax, c->nbr.as<uint32_t>(), c->nbCap, ext2,
-                          c->stream, &c->lc);
+  writeLists(c);
+  if (deferCheck) {
+    // The capacity check and the entry total are read at the caller's next
+    // stream synchronisation (resolveNeighbors).
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 40, maxCountPtr(c), sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    c->capCheckPending = true;
+  } else {
+    while (true) {
+      const int m = readMaxCount(c);
+      if (m <= c->nbCap) {
+        if (capFor(m) * 2 < c->nbCap) c->nbCapNext = capFor(m);   // shrink at the next build, not now
+        break;
+      }
+      c->nbCap = capFor(m);   // overflow: enlarge and rewrite
+      writeLists(c);
     }
-    c->check();
-    const int m = readMax();
-    if (m <= c->nbCap) {
-      if (capFor(m) * 2 < c->nbCap) c->nbCapNext = capFor(m);   // shrink at the next build, not now
-      break;
-    }
-    c->nbCap = capFor(m);   // overflow: enlarge and rebuild
   }
-  long long* dTot = c->nbrStart.as<long long>() + n;
-  scanExclusive<int>(c->counts.as<int>(), c->nbrStart.as<long long>(), n, c->scanWs.p, dTot, c->stream, &c->lc);
-  c->check();
-  CUDA_OK(cudaMemcpyAsync(c->hsmall, dTot, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_OK(cudaStreamSynchronize(c->stream));
-  long long total;
-  std::memcpy(&total, c->hsmall, sizeof(long long));
-  c->nnbr = total;
-  c->check();
+  scanTotals(c);
   c->haveNeighbors = true;
+  if (!deferCheck) resolveNeighbors(c);
+}
+
+// Reads the deferred capacity check and entry total after a stream
+// synchronisation.  Returns true when the lists overflowed and were rewritten
+// with a larger capacity (the caller must redo sweeps that used them).
+bool resolveNeighbors(sphgpu_ctx* c) {
+  bool regrown = false;
+  if (c->capCheckPending) {
+    c->capCheckPending = false;
+    int m;
+    std::memcpy(&m, c->hsmall + 40, sizeof(int));
+    if (m > c->nbCap) {
+      do {
+        c->nbCap = capFor(m);
+        writeLists(c);
+        m = readMaxCount(c);
+      } while (m > c->nbCap);
+      scanTotals(c);
+      regrown = true;
+    } else if (capFor(m) * 2 < c->nbCap) {
+      c->nbCapNext = capFor(m);
+    }
+  }
+  if (c->totalPending) {
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    std::memcpy(&c->nnbr, c->hsmall + 42, sizeof(long long));
+    c->totalPending = false;
+  }
+  return regrown;
 }
 
 void ensurePacc(sphgpu_ctx* c) {
@@ -629,23 +677,33 @@ void checkState(sphgpu_ctx* c, const char* where) {
 double step(sphgpu_ctx* c, double maxTime) {
   requireState(c);
   refreshParams(c);
-  buildNeighbors(c);                                 // Integrator::setGhostNodes + connectivity
+  buildNeighbors(c, true);                           // Integrator::setGhostNodes + connectivity
   bool fused = false;
-  if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
-    if (c->fp32()) {
-      Scope sc(c->prof, "density_dt");
-      const long nb = (c->n + 127) / 128;
-      c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
-      launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
-                          c->maxNperh(), c->scratch.as<double>(), c->small.as<double>(), c->stream, &c->lc);
-      c->check();
-      fused = true;
-    } else {
-      sumDensity(c);
+  auto preStep = [&]() {
+    if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
+      if (c->fp32()) {
+        Scope sc(c->prof, "density_dt");
+        const long nb = (c->n + 127) / 128;
+        c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
+        launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
+                            c->maxNperh(), c->scratch.as<double>(), c->small.as<double>(), c->stream, &c->lc);
+        c->check();
+        fused = true;
+      } else {
+        sumDensity(c);
+      }
     }
-  }
+  };
+  preStep();
   const double t = c->time;
-  const double dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t), fused);
+  double dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t), fused);
+  // The dt read synchronised the stream: settle the deferred list check.  A
+  // list that overflowed its capacity was rewritten larger; redo the sweeps
+  // that read it.
+  if (resolveNeighbors(c)) {
+    preStep();
+    dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t), fused);
+  }
   const double hdt = 0.5 * dt;
   {
     Scope sc(c->prof, "update");
@@ -1173,6 +1231,7 @@ int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* 
   API_BEGIN(c)
   if (!npairs) throw Error(SPHGPU_E_ARG, "null npairs");
   if (!c->haveNeighbors) throw Error(SPHGPU_E_STATE, "no neighbour lists yet");
+  resolveNeighbors(c);
   *npairs = (long)c->nnbr;
   if (!i_out) return SPHGPU_OK;
   const long n = c->n;
@@ -1277,6 +1336,7 @@ int sphgpu_timer_stop(sphgpu_handle c, double* ms) {
 }
 int sphgpu_neighbor_count(sphgpu_handle c, long* entries) {
   API_BEGIN(c)
+  if (c->haveNeighbors) resolveNeighbors(c);
   if (entries) *entries = (long)c->nnbr;
   API_END(c)
 }

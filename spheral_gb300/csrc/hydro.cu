@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
                                                           uint32_t* __restrict__ nbr, double ext2, float bandA,
-                                                          float bandB, int cap, int* __restrict__ maxCount) {
+                                                          float bandB, int cap, int* __restrict__ maxCount,
+                                                          const long long* __restrict__ dItems) {
   constexpr int G = 128 / W;             // groups per 128-thread block
   __shared__ float4 stage[G][W];         // one candidate batch per group
   __shared__ int2 range[G][27];          // node ranges of the 27 candidate cells
@@ -120,7 +121,8 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const int lane = threadIdx.x % W, wib = threadIdx.x / W;
   // lanes of this group within the warp
   const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << ((threadIdx.x & 31) / W * W));
-  if (item >= nItems) return;   // group-uniform
+  // the grid is sized for an upper bound; the item count itself is on the device
+  if (item >= min((long long)nItems, *dItems)) return;   // group-uniform
   const int k0 = items[item];
   const uint32_t cc = P.cell[k0];
   int hc[3];
@@ -232,7 +234,10 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
       __syncwarp(gmask);
     }
   }
-  if (active) counts[i] = cnt;
+  // The stored count never exceeds the capacity: sweeps that run before an
+  // overflow is noticed read only written slots.  The true maximum goes to
+  // maxCount (the overflow signal).
+  if (active) counts[i] = WRITE ? min(cnt, cap) : cnt;
   // one atomic per group: a per-node atomic on a single address serialises
   const int gmax = __reduce_max_sync(gmask, active ? cnt : 0);
   if (lane == 0) atomicMax(maxCount, gmax);
@@ -943,16 +948,16 @@ void launchItemFill(const int* flag, const long long* pos, long n, int* items, c
   itemFillKernel<<<gridFor(n, 256), 256, 0, s>>>(flag, pos, n, items);
   lc->add(1);
 }
-void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, int width, Grid g,
-                         const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
-                         double ext2, cudaStream_t s, LaunchCounter* lc) {
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
+                         int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
+                         uint32_t* nbr, int cap, double ext2, cudaStream_t s, LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
   const long threads = (long)nItems * width;
   const unsigned gb = (unsigned)((threads + 127) / 128);
 #define SPH_NBR(WR, WD)                                                                                        \
   neighborWarpKernel<WR, WD><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts,        \
-                                                WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount)
+                                                WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount, dItems)
   if (nbr) {
     if (width == 8) SPH_NBR(true, 8); else if (width == 16) SPH_NBR(true, 16); else SPH_NBR(true, 32);
   } else {

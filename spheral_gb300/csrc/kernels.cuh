@@ -42,9 +42,11 @@ void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* c
 void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int width, int* flag, cudaStream_t s,
                      LaunchCounter* lc);
 void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc);
-void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, int width, Grid g,
-                         const int* cellStart, const int* cellEnd, int* counts, int* maxCount, uint32_t* nbr, int cap,
-                         double ext2, cudaStream_t s, LaunchCounter* lc);
+// nItems: an upper bound on the item count (sizes the grid); *dItems (device)
+// holds the count itself.
+void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
+                         int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
+                         uint32_t* nbr, int cap, double ext2, cudaStream_t s, LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,

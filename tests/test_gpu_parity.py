@@ -192,3 +192,31 @@ def test_nonfinite_state_reported(native_lib):
         eng.step()
         eng.step()
     assert e.value.code == 5
+
+
+def test_list_capacity_regrows_inside_step(native_lib, oracle_mod):
+    """A step whose neighbour counts outgrow the list capacity sized at the
+    previous build: the step detects the overflow at its first
+    synchronisation, rewrites the lists larger and redoes the sweeps, so the
+    lists still equal the oracle's connectivity of the state it started from."""
+    from spheral_gb300.engine import Engine
+    p = problems.random_box(n_side=12, seed=25, boundaries="open")
+    eng = Engine.from_problem(p)
+    eng.initialize()
+    eng.step()
+    st = {f: np.ascontiguousarray(eng.field(f)) for f in
+          ("position", "velocity", "mass", "massDensity", "specificThermalEnergy", "H")}
+    centre = st["position"].mean(axis=0)
+    pos2 = np.ascontiguousarray(centre + 0.6 * (st["position"] - centre))   # ~4.6x the neighbours
+    eng.upload_state(pos2, st["velocity"], st["mass"], st["massDensity"], st["specificThermalEnergy"], st["H"])
+    eng.step()
+    i, j, im = eng.pairs()
+    got = set(zip(i.tolist(), j.tolist(), im.tolist()))
+    H = st["H"].reshape(-1, 6) if st["H"].ndim == 1 else st["H"]
+    p2 = problems.Problem("compressed", pos2, st["velocity"], st["mass"], st["massDensity"],
+                          st["specificThermalEnergy"], 1.0 / H[:, 0], None, p.nodelists, [], p.config)
+    orc = oracle_mod.Oracle(p2)
+    orc.connectivity()
+    want = ordered_pairs_from_oracle(orc, ())
+    assert got == want
+    assert len(got) > 3 * len(p.pos) * 20
