@@ -366,27 +366,31 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     const double rho = F.f[F_MASS][i] * (((a * a) * a) * hp.W0) + kahanValue(s, c);
     F.f[F_RHO][i] = rho;
     P.thermo[i].x = (float)rho;
-    // node limits
-    const double tiny = DBL_EPSILON;
+    // Node limits of GenericHydro::dt in FP32 (the vote only picks the
+    // minimum; GB300's FP64 divide and square root sequences would dominate
+    // the sweep otherwise).
+    const float tiny = (float)DBL_EPSILON;
     const NodeListParams L = hp.lists[multi ? li : list[i]];
-    const double nodeScalei = 1.0 / a / L.nPerh;
-    const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
-    const double csDt = nodeScalei / (F.f[F_CS][i] + tiny);
-    if (csDt < best) { best = csDt; reason = 0; }
-    const double csqDt = nodeScalei / (sqrt(F.f[F_MAXQ][i] / rho) + tiny);
-    if (csqDt < best) { best = csqDt; reason = 1; }
-    const double divvDt = 1.0 / (fabs(F.f[F_DVDX_XX][i] + F.f[F_DVDX_YY][i] + F.f[F_DVDX_ZZ][i]) + tiny);
-    if (divvDt < best) { best = divvDt; reason = 2; }
-    const double vmag = sqrt(vxi * vxi + vyi * vyi + vzi * vzi);
-    const double ax = F.f[F_DVDT_X][i], ay = F.f[F_DVDT_Y][i], az = F.f[F_DVDT_Z][i];
-    const double dtAcc = 0.1 * fmax(nodeScalei / (vmag + tiny), vmag / (sqrt(ax * ax + ay * ay + az * az) + tiny));
-    if (dtAcc < best) { best = dtAcc; reason = 3; }
+    const float nodeScalei = 1.0f / (pi.w * (float)L.nPerh);
+    float bestf = 3.0e38f;
+    const float csDt = nodeScalei / (P.thermo[i].z + tiny);
+    if (csDt < bestf) { bestf = csDt; reason = 0; }
+    const float csqDt = nodeScalei / (sqrtf((float)F.f[F_MAXQ][i] / (float)rho) + tiny);
+    if (csqDt < bestf) { bestf = csqDt; reason = 1; }
+    const float divv = (float)(F.f[F_DVDX_XX][i] + F.f[F_DVDX_YY][i] + F.f[F_DVDX_ZZ][i]);
+    const float divvDt = 1.0f / (fabsf(divv) + tiny);
+    if (divvDt < bestf) { bestf = divvDt; reason = 2; }
+    const float vmag = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z);
+    const float ax = (float)F.f[F_DVDT_X][i], ay = (float)F.f[F_DVDT_Y][i], az = (float)F.f[F_DVDT_Z][i];
+    const float dtAcc = 0.1f * fmaxf(nodeScalei / (vmag + tiny), vmag / (sqrtf(ax * ax + ay * ay + az * az) + tiny));
+    if (dtAcc < bestf) { bestf = dtAcc; reason = 3; }
     if (hp.useVelMagDt) {
-      const double velDt = nodeScalei / (vmag + 1.0e-10);
-      if (velDt < best) { best = velDt; reason = 4; }
+      const float velDt = nodeScalei / (vmag + 1.0e-10f);
+      if (velDt < bestf) { bestf = velDt; reason = 4; }
     }
-    const double pairDt = (double)bestPair / maxNperh;
-    if (pairDt < best) { best = pairDt; reason = 5; }
+    const float pairDt = bestPair / (float)maxNperh;
+    if (pairDt < bestf) { bestf = pairDt; reason = 5; }
+    best = (double)bestf;
   }
   sv[threadIdx.x] = best;
   sr[threadIdx.x] = reason;
@@ -585,14 +589,25 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
   };
   // Batches of four slots: all their loads are issued before any is used,
   // so four gathers and pair-acceleration reads are in flight together.
+  // The entries of the next batch are loaded while this batch's gathers
+  // are in flight.
   constexpr int B = 4;
   int q = 0;
+  uint32_t en[B];
+  if (B <= cnt) {
+#pragma unroll
+    for (int u = 0; u < B; ++u) en[u] = nl.nbr[nbSlot(i, u, nl.cap)];
+  }
   for (; q + B <= cnt; q += B) {
     uint32_t e[B];
     float4 H[B], L[B];
     float p[B][3];
 #pragma unroll
-    for (int u = 0; u < B; ++u) e[u] = nl.nbr[nbSlot(i, q + u, nl.cap)];
+    for (int u = 0; u < B; ++u) e[u] = en[u];
+    if (q + 2 * B <= cnt) {
+#pragma unroll
+      for (int u = 0; u < B; ++u) en[u] = nl.nbr[nbSlot(i, q + B + u, nl.cap)];
+    }
 #pragma unroll
     for (int u = 0; u < B; ++u) {
       const long long k = nbSlot(i, q + u, nl.cap);

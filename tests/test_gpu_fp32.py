@@ -89,3 +89,14 @@ def test_fp32_tracks_fp64(native_lib):
         x, y = a.field(name), b.field(name)
         err = np.max(np.abs(x - y)) / np.max(np.abs(y))
         assert err < tol, (name, err)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fp32_step_dt_close(native_lib, oracle_mod, case):
+    """The time step of the mixed step (density sum and dt vote fused, node
+    limits in FP32) within 1e-5 of the FP64 oracle's over three steps."""
+    p, eng, orc = _pair(oracle_mod, CASES[case])
+    for _ in range(3):
+        dg = eng.step()
+        do = orc.step()
+        assert abs(dg - do) <= 1e-5 * do, (dg, do)
