@@ -167,6 +167,8 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
   int cnt = 0;
+  // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
+  uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;
   // first batch of the first non-empty cell, loaded ahead of use
   int tn = 0;
   while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
@@ -198,6 +200,7 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         if (mir & 12u) q.y = cy - q.y;
         if (mir & 48u) q.z = cz - q.z;
       }
+      q.w = q.w * q.w;   // (h_j^-1)^2
       // Stage the batch in shared memory: each lane then reads every
       // candidate with one broadcast load.
       stage[wib][lane] = q;
@@ -206,28 +209,29 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
       // the home cell's own batch contains node i itself
       const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
       if (active) {
+        const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
+        // this node shifted by the cell offset: r = (x_i + o) - x_j
+        const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
+#pragma unroll 4
         for (int u = 0; u < nval; ++u) {
-          if (u == self) continue;
           const float4 cq = stage[wib][u];
-          const int j = base + u;
-          const float rx = __fadd_rn(__fsub_rn(pi.x, cq.x), ox);
-          const float ry = __fadd_rn(__fsub_rn(pi.y, cq.y), oy);
-          const float rz = __fadd_rn(__fsub_rn(pi.z, cq.z), oz);
+          const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
           const float r2 = rx * rx + ry * ry + rz * rz;
-          const float e2 = fminf(ai2, cq.w * cq.w) * r2;
-          bool inside;
-          if (e2 < bandLo) inside = true;
-          else if (e2 > bandHi) inside = false;
-          else {
-            double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-            imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
-            const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
-                         qz = __dsub_rn(F.f[F_Z][i], zjd);
-            inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
-          }
-          if (inside) {
-            if (WRITE && cnt < cap) nbr[nbSlot(i, cnt, cap)] = (uint32_t)j | ((uint32_t)dcode << kIndexBits);
-            ++cnt;
+          const float e2 = fminf(ai2, cq.w) * r2;
+          if (e2 <= bandHi) {
+            bool inside = true;
+            if (e2 >= bandLo) {   // guard band: the exact FP64 criterion (rare)
+              const int j = base + u;
+              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+              imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                           qz = __dsub_rn(F.f[F_Z][i], zjd);
+              inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+            }
+            if (inside && u != self) {
+              if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
+              ++cnt;
+            }
           }
         }
       }
