@@ -51,6 +51,9 @@ extern "C" {
 #define SPHGPU_DENSITY_RIGOROUS_SUM 0   /* MassDensityType::RigorousSumDensity */
 #define SPHGPU_DENSITY_INTEGRATE 1      /* MassDensityType::IntegrateDensity   */
 
+#define SPHGPU_VISCOSITY_MONAGHAN_GINGOLD 0          /* MonaghanGingoldViscosity        */
+#define SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD 1  /* LimitedMonaghanGingoldViscosity (the SPH() factory default) */
+
 typedef struct sphgpu_ctx* sphgpu_handle;
 
 /* Package, artificial-viscosity, integrator and gravity settings.  Field
@@ -60,7 +63,11 @@ typedef struct sphgpu_ctx* sphgpu_handle;
  *   MonaghanGingoldViscosity     src/ArtificialViscosity/MonaghanGingoldViscosity.cc:25-37
  *   ArtificialViscosityHandle    src/ArtificialViscosity/ArtificialViscosityHandle.cc:36-54 (epsilon2)
  *   Integrator dtMin/dtMax/dtGrowth  src/Integrator/Integrator.cc:43-47
- *   OctTreeGravity(G, softeningLength, opening, ftimestep) src/Gravity/TreeGravity.cc:88-115 */
+ *   OctTreeGravity(G, softeningLength, opening, ftimestep) src/Gravity/TreeGravity.cc:88-115
+ *   LimitedMonaghanGingoldViscosity(Cl, Cq, kernel, linearInExpansion,
+ *     quadraticInExpansion, etaCritFrac, etaFoldFrac)
+ *                                src/ArtificialViscosity/LimitedMonaghanGingoldViscosity.cc:39-53,
+ *                                defaults src/PYB11/ArtificialViscosity/LimitedMonaghanGingoldViscosity.py:31-32 */
 typedef struct sphgpu_config {
   int num_table_points;             /* TableKernel(BSplineKernel3d(), numPoints)           */
   double cfl;
@@ -79,6 +86,8 @@ typedef struct sphgpu_config {
   double G, softening, opening, ftimestep;
   int precision;                    /* SPHGPU_PRECISION_*                                  */
   int device;                       /* CUDA device ordinal                                 */
+  int viscosity;                    /* SPHGPU_VISCOSITY_*                                  */
+  double eta_crit_frac, eta_fold_frac;  /* limited Q: full Q below etaCritFrac/nPerh      */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,

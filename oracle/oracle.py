@@ -43,6 +43,9 @@ class OrcConfig(ctypes.Structure):
         ("softening", ctypes.c_double),
         ("opening", ctypes.c_double),
         ("ftimestep", ctypes.c_double),
+        ("viscosity", ctypes.c_int),
+        ("eta_crit_frac", ctypes.c_double),
+        ("eta_fold_frac", ctypes.c_double),
     ]
 
 
@@ -119,13 +122,16 @@ def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
 
 
+# artificial viscosity of the SPH package
+VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
+
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
     "pressure": 1, "soundSpeed": 1, "omegaGradh": 1, "massDensitySum": 1, "normalization": 1, "DxDt": 3,
     "DvDt": 3, "DrhoDt": 1, "DepsDt": 1, "DvDx": 9, "internalDvDx": 9, "gradRho": 3, "M": 9, "localM": 9,
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
-    "DepsDtCompatible": 1,
+    "DepsDtCompatible": 1, "ArtificialViscosityVelocityGradient": 9,
 }
 
 
@@ -163,6 +169,9 @@ class Oracle:
         c.softening = cfg.get("softening", 0.01)
         c.opening = cfg.get("opening", 0.5)
         c.ftimestep = cfg.get("ftimestep", 0.1)
+        c.viscosity = VISCOSITY[cfg.get("viscosity", "monaghan_gingold")]
+        c.eta_crit_frac = cfg.get("eta_crit_frac", 1.0)
+        c.eta_fold_frac = cfg.get("eta_fold_frac", 0.2)
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))

@@ -397,6 +397,9 @@ struct Config {
   double epsTensile = 0.0, nTensile = 4.0;
   double Cl = 1.0, Cq = 1.0, eps2 = 1.0e-2;
   int linearInExpansion = 0, quadraticInExpansion = 0;
+  // 0 MonaghanGingoldViscosity, 1 LimitedMonaghanGingoldViscosity
+  int viscosity = 0;
+  double etaCritFrac = 1.0, etaFoldFrac = 0.2;
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
   double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
@@ -445,6 +448,9 @@ struct Problem {
   vector<V3> DxDt, DvDt, gradRho, XSPHDeltaV, massFirst, DvDtGrav;
   vector<T9> DvDx, localDvDx, M, localM;
   vector<ST> DHDt, Hideal;
+  // ArtificialViscosityVelocityGradient: the Q's copy of DvDx, a state field
+  // (ArtificialViscosityHandle.cc:52,78-79; zero until the first copy)
+  vector<T9> DvDxQ;
   vector<V3> pairAccel;   // per pair
   vector<double> potential;
   double extraEnergy = 0.0, dtMinAcc = std::numeric_limits<double>::max();
@@ -477,6 +483,25 @@ struct Problem {
     keepResize(XSPHDeltaV, nInt, nTot); keepResize(massFirst, nInt, nTot); keepResize(DvDtGrav, nInt, nTot);
     keepResize(DvDx, nInt, nTot); keepResize(localDvDx, nInt, nTot); keepResize(M, nInt, nTot); keepResize(localM, nInt, nTot);
     keepResize(DHDt, nInt, nTot); keepResize(Hideal, nInt, nTot); keepResize(potential, nInt, nTot);
+    if ((int)DvDxQ.size() < nInt) DvDxQ.assign(nInt, T9{});
+    DvDxQ.resize(nTot);
+  }
+  // ArtificialViscosityHandle::postStateUpdate (ArtificialViscosityHandle.cc:167-183):
+  // without a rigorous gradient the Q copies the hydro's DvDx; its ghost
+  // values follow at the next applyGhostBoundaries (tensors reflect as R T R).
+  void copyQVelocityGradient() {
+    if (cfg.viscosity != 1) return;
+    for (int i = 0; i < nInt; ++i) DvDxQ[i] = DvDx[i];
+    applyGhostQGradient();
+  }
+  // ArtificialViscosityHandle::applyGhostBoundaries (ArtificialViscosityHandle.cc:96-110)
+  void applyGhostQGradient() {
+    if (cfg.viscosity != 1 || (int)DvDxQ.size() < nTot) return;
+    applyGhostField(DvDxQ, [](T9& t, int a) {
+      if (a == 0) { t.xy = -t.xy; t.xz = -t.xz; t.yx = -t.yx; t.zx = -t.zx; }
+      else if (a == 1) { t.xy = -t.xy; t.yx = -t.yx; t.yz = -t.yz; t.zy = -t.zy; }
+      else { t.xz = -t.xz; t.zx = -t.zx; t.yz = -t.yz; t.zy = -t.zy; }
+    });
   }
 
   double hmaxOf(const ST& Hi) const { return 1.0 / minElem(eigenValuesS(Hi)); }
@@ -573,6 +598,7 @@ struct Problem {
         }
       }
     }
+    applyGhostQGradient();
   }
   template <class T, class Fn>
   void applyGhostField(vector<T>& f, Fn reflect) {
@@ -768,12 +794,42 @@ struct Problem {
       return *this;
     }
   };
-  void QPiij(double& QPiij_, double& QPiji_, double& Qij, double& Qji, const V3& etai, const V3& vi, double rhoi,
-             double csi, const V3& etaj, const V3& vj, double rhoj, double csj) const {
+  static V3 dotTV(const T9& t, const V3& v) {            // GeomTensorInline.hh: Tensor.dot(Vector)
+    return {t.xx * v.x + t.xy * v.y + t.xz * v.z, t.yx * v.x + t.yy * v.y + t.yz * v.z,
+            t.zx * v.x + t.zy * v.y + t.zz * v.z};
+  }
+  static double limiterVL(double x) {                    // LimitedMonaghanGingoldViscosity.cc:26-32 (van Leer)
+    return x > 0.0 ? 2.0 / (1.0 + x) * 2.0 * x / (1.0 + x) : 0.0;
+  }
+  // MonaghanGingoldViscosity::QPiij (MonaghanGingoldViscosity.cc:41-101) and,
+  // with cfg.viscosity == 1, LimitedMonaghanGingoldViscosity::QPiij
+  // (LimitedMonaghanGingoldViscosity.cc:113-213): the velocities are first
+  // corrected along the pair by the van Leer limited DvDx of the Q.
+  void QPiij(double& QPiij_, double& QPiji_, double& Qij, double& Qji, const V3& xi, const V3& etai, const V3& vi,
+             double rhoi, double csi, const V3& xj, const V3& etaj, const V3& vj, double rhoj, double csj,
+             const T9& DvDxi, const T9& DvDxj) const {
     const double fCli = 1.0, fCqi = 1.0, fClj = 1.0, fCqj = 1.0, fshear = 1.0;
     const double Clij = 0.5 * (fCli + fClj) * fshear * cfg.Cl;
     const double Cqij = 0.5 * (fCqi + fCqj) * fshear * cfg.Cq;
-    const V3 vij = sub(vi, vj);
+    V3 vij = sub(vi, vj);
+    if (cfg.viscosity == 1) {
+      const double nPerh = lists[0].nPerh;
+      const double etaCrit = cfg.etaCritFrac / nPerh, etaFold = cfg.etaFoldFrac / nPerh;
+      const V3 xij = mul(0.5, sub(xi, xj));
+      const double gradi = dot(dotTV(DvDxi, xij), xij);
+      const double gradj = dot(dotTV(DvDxj, xij), xij);
+      const double ri = gradi / (sgn(gradj) * std::max(1.0e-30, std::fabs(gradj)));
+      const double rj = gradj / (sgn(gradi) * std::max(1.0e-30, std::fabs(gradi)));
+      double phi = limiterVL(std::min(ri, rj));
+      const double etaij = std::min(mag(etai), mag(etaj));
+      if (etaij < etaCrit) {
+        const double z = (etaij - etaCrit) / etaFold;
+        phi *= std::exp(-(z * z));
+      }
+      const V3 vi1 = sub(vi, mul(phi, dotTV(DvDxi, xij)));
+      const V3 vj1 = add(vj, mul(phi, dotTV(DvDxj, xij)));
+      vij = sub(vi1, vj1);
+    }
     const double mui = dot(vij, etai) / (mag2(etai) + cfg.eps2);
     const double muj = dot(vij, etaj) / (mag2(etaj) + cfg.eps2);
     const double li = cfg.linearInExpansion ? mui : std::min(0.0, mui);
@@ -818,7 +874,7 @@ struct Problem {
       }
       const V3 vij = sub(vi, vj);
       double QPi_ij, QPi_ji, Qi, Qj;
-      QPiij(QPi_ij, QPi_ji, Qi, Qj, etai, vi, rhoi, ci, etaj, vj, rhoj, cj);
+      QPiij(QPi_ij, QPi_ji, Qi, Qj, ri, etai, vi, rhoi, ci, rj, etaj, vj, rhoj, cj, DvDxQ[i], DvDxQ[j]);
       const V3 Qacci = mul(0.5, mul(QPi_ij, gradWQi)), Qaccj = mul(0.5, mul(QPi_ji, gradWQj));
       const double workQi = dot(vij, Qacci), workQj = dot(vij, Qaccj);
       ai.maxQ = std::max(ai.maxQ, Qi); aj.maxQ = std::max(aj.maxQ, Qj);
@@ -1228,6 +1284,7 @@ struct Problem {
     stateUpdate(hdt, true);
     time = t + hdt;
     applyGhostState();
+    copyQVelocityGradient();
     if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
     // derivatives at the midpoint
     if (cfg.gravity) buildTree();
@@ -1239,6 +1296,7 @@ struct Problem {
     stateUpdate(dt, false);
     time = t + dt;
     applyGhostState();
+    copyQVelocityGradient();
     if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
     enforceBoundaries();
     ++cycle;
@@ -1278,6 +1336,8 @@ struct orc_config {
   double dt_min, dt_max, dt_growth, last_dt, time;
   int gravity;
   double G, softening, opening, ftimestep;
+  int viscosity;
+  double eta_crit_frac, eta_fold_frac;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1290,6 +1350,7 @@ void* orc_create(const orc_config* c) {
   g.Cl = c->Cl; g.Cq = c->Cq; g.eps2 = c->eps2; g.linearInExpansion = c->linear_in_expansion;
   g.quadraticInExpansion = c->quadratic_in_expansion; g.dtMin = c->dt_min; g.dtMax = c->dt_max; g.dtGrowth = c->dt_growth;
   g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
+  g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;
@@ -1420,6 +1481,7 @@ int orc_get_field(void* h, const char* name, double* out) {
   if (s == "DrhoDt") return sc(p->DrhoDt);
   if (s == "DepsDt") return sc(p->DepsDt);
   if (s == "DvDx") return t9(p->DvDx);
+  if (s == "ArtificialViscosityVelocityGradient") return t9(p->DvDxQ);
   if (s == "internalDvDx") return t9(p->localDvDx);
   if (s == "gradRho") return v3(p->gradRho);
   if (s == "M") return t9(p->M);

@@ -56,6 +56,9 @@ class Config(ctypes.Structure):
         ("ftimestep", ctypes.c_double),
         ("precision", ctypes.c_int),
         ("device", ctypes.c_int),
+        ("viscosity", ctypes.c_int),
+        ("eta_crit_frac", ctypes.c_double),
+        ("eta_fold_frac", ctypes.c_double),
     ]
 
 

@@ -116,6 +116,7 @@ struct sphgpu_ctx {
   // parameters
   NodeListParams lists[kMaxNodeLists]{};
   DBuf dLists;   // device copy of lists
+  DBuf dvq;      // limited Q, mixed mode: FP32 copy of the Q's DvDx (3 float4 per node)
   int numLists = 0;
   std::vector<Boundary> bcs;
   HydroParams hp{};
@@ -196,6 +197,7 @@ struct sphgpu_ctx {
     p.velm = velm.as<float4>();
     p.thermo = thermo.as<float4>();
     p.cell = cellp();
+    p.dvq = dvq.p ? dvq.as<float4>() : nullptr;
     return p;
   }
   bool fp32() const { return cfg.precision == SPHGPU_PRECISION_FP32; }
@@ -292,6 +294,11 @@ void refreshParams(sphgpu_ctx* c) {
   hp.eps2 = g.eps2;
   hp.cfl = g.cfl;
   hp.numLists = std::max(1, c->numLists);
+  // LimitedMonaghanGingoldViscosity: etaCrit = etaCritFrac / nPerh of the first
+  // NodeList (LimitedMonaghanGingoldViscosity.cc:148-154)
+  hp.limitedQ = g.viscosity == SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD ? 1 : 0;
+  hp.etaCrit = g.eta_crit_frac / c->lists[0].nPerh;
+  hp.etaFold = g.eta_fold_frac / c->lists[0].nPerh;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -434,8 +441,8 @@ void buildNeighbors(sphgpu_ctx* c, bool deferCheck = false) {
     Scope sc(c->prof, "permute");
     const int nx = 1 - c->cur;
     launchPermute(c->F, c->Falt, v, c->orig[c->cur].as<int>(), c->orig[nx].as<int>(), c->list[c->cur].as<int>(),
-                  c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n, c->stream,
-                  &c->lc);
+                  c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n,
+                  c->hp.limitedQ != 0, c->stream, &c->lc);
     std::swap(c->bankA, c->bankB);
     std::swap(c->F, c->Falt);
     c->cur = nx;
@@ -550,6 +557,15 @@ void ensurePacc(sphgpu_ctx* c) {
   c->pacc.ensure(std::max<size_t>(1, c->nbSlots()) * 3 * per);
 }
 
+// LimitedMonaghanGingoldViscosity reads the Q's own copy of DvDx, refreshed
+// from the hydro's at every postStateUpdate (ArtificialViscosityHandle.cc:167-183).
+void copyQGradient(sphgpu_ctx* c) {
+  if (!c->hp.limitedQ) return;
+  Scope sc(c->prof, "update");
+  launchCopyQGradient(c->F, c->n, c->stream, &c->lc);
+  c->check();
+}
+
 void prepare32(sphgpu_ctx* c) {
   if (!c->fp32()) return;
   Scope sc(c->prof, "prepare_fp32");
@@ -574,6 +590,11 @@ void gradh(sphgpu_ctx* c) {
 }
 void evalDerivs(sphgpu_ctx* c) {
   ensurePacc(c);
+  if (c->fp32() && c->hp.limitedQ) {   // FP32 mirror of the Q's DvDx in the current node order
+    c->dvq.ensure((size_t)c->n * 3 * sizeof(float4));
+    launchQGradient32(c->F, c->dvq.as<float4>(), c->n, c->stream, &c->lc);
+    c->check();
+  }
   if (c->fp32()) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
@@ -713,6 +734,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   c->check();
   prepare32(c);
   c->time = t + hdt;
+  copyQGradient(c);                                  // postStateUpdate (mid): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
   {
@@ -736,6 +758,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   c->check();
   prepare32(c);
   c->time = t + dt;
+  copyQGradient(c);                                  // postStateUpdate (end): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
   {
     Scope sc(c->prof, "enforce");
@@ -764,7 +787,8 @@ bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb) {
       {"M", {F_M_XX, 9}}, {"localM", {F_M_XX, 9}}, {"maxViscousPressure", {F_MAXQ, 1}},
       {"effViscousPressure", {F_EFFQ, 1}}, {"XSPHWeightSum", {F_XSPHW, 1}}, {"XSPHDeltaV", {F_XSPHDV_X, 3}},
       {"massZerothMoment", {F_M0, 1}}, {"massFirstMoment", {F_M1_X, 3}}, {"DvDtGravity", {F_GRAV_X, 3}},
-      {"potential", {F_POT, 1}}, {"DepsDtCompatible", {F_DEPS_COMPAT, 1}}};
+      {"potential", {F_POT, 1}}, {"DepsDtCompatible", {F_DEPS_COMPAT, 1}},
+      {"ArtificialViscosityVelocityGradient", {F_DVDXQ_XX, 9}}};
   if (s == "H" || s == "Hideal" || s == "DHDt") {
     isH = true;
     fs = {s == "H" ? F_HINV : (s == "Hideal" ? F_HIDEAL : F_DHDT), 6};
@@ -836,6 +860,9 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->ftimestep = 0.1;
   c->precision = SPHGPU_PRECISION_FP64;
   c->device = 0;
+  c->viscosity = SPHGPU_VISCOSITY_MONAGHAN_GINGOLD;
+  c->eta_crit_frac = 1.0;
+  c->eta_fold_frac = 0.2;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -846,6 +873,10 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
     c->cfg = *cfg;
     if (cfg->precision != SPHGPU_PRECISION_FP64 && cfg->precision != SPHGPU_PRECISION_FP32)
       throw Error(SPHGPU_E_ARG, "unknown precision mode");
+    if (cfg->viscosity != SPHGPU_VISCOSITY_MONAGHAN_GINGOLD && cfg->viscosity != SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD)
+      throw Error(SPHGPU_E_UNSUPPORTED, "unknown artificial viscosity");
+    if (cfg->viscosity == SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD && !(cfg->eta_fold_frac > 0.0))
+      throw Error(SPHGPU_E_ARG, "etaFoldFrac must be positive");
     if (cfg->density_update != SPHGPU_DENSITY_RIGOROUS_SUM && cfg->density_update != SPHGPU_DENSITY_INTEGRATE)
       throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
     CUDA_OK(cudaSetDevice(cfg->device));
@@ -886,7 +917,7 @@ int sphgpu_destroy(sphgpu_handle c) {
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
                   &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->itemFlag, &c->items,
-                  &c->dLists};
+                  &c->dLists, &c->dvq};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);

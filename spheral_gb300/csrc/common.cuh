@@ -43,6 +43,8 @@ struct HydroParams {
   int hermN;          // Hermite knots of the nperh lookup
   double hermXmin, hermXmax, hermXstep;
   const NodeListParams* lists;   // device table of the NodeLists (kMaxNodeLists entries)
+  int limitedQ;                  // LimitedMonaghanGingoldViscosity instead of MonaghanGingoldViscosity
+  double etaCrit, etaFold;       // its full-Q distance and fold width in eta
 };
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,

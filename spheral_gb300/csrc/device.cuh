@@ -120,6 +120,20 @@ __device__ __forceinline__ void imageVec(const Grid& g, int code, double& x, dou
   }
 }
 
+// Tensor seen through the image: a mirror along axis a is R = I - 2 e_a e_a,
+// and R T R flips every component with exactly one index on a mirrored axis.
+__device__ __forceinline__ void imageTensor(const Grid& g, int code, double* T) {
+  if (code) {
+    const double s[3] = {mirrored(code & 3, g.kindLo[0], g.kindHi[0]) ? -1.0 : 1.0,
+                         mirrored((code >> 2) & 3, g.kindLo[1], g.kindHi[1]) ? -1.0 : 1.0,
+                         mirrored((code >> 4) & 3, g.kindLo[2], g.kindHi[2]) ? -1.0 : 1.0};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) T[3 * r + c] *= s[r] * s[c];
+  }
+}
+
 // QuadraticInterpolatorView lookup shared by W and dW/deta
 // (src/Utilities/QuadraticInterpolatorViewInline.hh:17-21,71-77).
 __device__ __forceinline__ int tableIndex(double eta, int N1, double xstep) {

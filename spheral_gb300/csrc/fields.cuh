@@ -18,6 +18,9 @@ enum FieldId {
   F_RHOSUM, F_NORM, F_MAXQ, F_EFFQ, F_XSPHW, F_XSPHDV_X, F_XSPHDV_Y, F_XSPHDV_Z,
   F_DHDT, F_HIDEAL, F_M0, F_M1_X, F_M1_Y, F_M1_Z,
   F_GRAV_X, F_GRAV_Y, F_GRAV_Z, F_POT, F_DEPS_COMPAT,
+  // the limited Q's copy of DvDx (state field ArtificialViscosityVelocityGradient);
+  // permuted only when that Q is in use
+  F_DVDXQ_XX, F_DVDXQ_XY, F_DVDXQ_XZ, F_DVDXQ_YX, F_DVDXQ_YY, F_DVDXQ_YZ, F_DVDXQ_ZX, F_DVDXQ_ZY, F_DVDXQ_ZZ,
   F_NUM_PERMUTED,
   // beginning-of-step copies (not permuted: written after the sort)
   F_X0 = F_NUM_PERMUTED, F_Y0, F_Z0, F_VX0, F_VY0, F_VZ0, F_RHO0, F_EPS0, F_HINV0,
@@ -34,6 +37,7 @@ struct Fields32 {
   float4* velm;     // (vx, vy, vz, m)
   float4* thermo;   // (rho, P/rho^2 * Omega^-1, cs, unused)
   uint32_t* cell;   // packed cell coordinates (10 bits per axis)
+  float4* dvq;      // limited Q: DvDx of the Q as 3 float4 per node (xx xy xz yx | yy yz zx zy | zz - - -)
 };
 
 }  // namespace sph

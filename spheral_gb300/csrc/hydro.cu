@@ -70,12 +70,13 @@ __global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ k
 
 __global__ void permuteKernel(Fields Fin, Fields Fout, const int* __restrict__ perm, const int* __restrict__ origIn,
                               int* __restrict__ origOut, const int* __restrict__ listIn, int* __restrict__ listOut,
-                              const uint32_t* __restrict__ cellIn, uint32_t* __restrict__ cellOut, long n) {
+                              const uint32_t* __restrict__ cellIn, uint32_t* __restrict__ cellOut, long n,
+                              int nfields) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = perm[k];
 #pragma unroll 4
-  for (int f = 0; f < F_NUM_PERMUTED; ++f) Fout.f[f][k] = Fin.f[f][p];
+  for (int f = 0; f < nfields; ++f) Fout.f[f][k] = Fin.f[f][p];
   origOut[k] = origIn[p];
   listOut[k] = listIn[p];
   cellOut[k] = cellIn[p];
@@ -390,6 +391,9 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
   const double tiny = kTiny30;
   const double Clij = 0.5 * (1.0 + 1.0) * 1.0 * hp.Cl;
   const double Cqij = 0.5 * (1.0 + 1.0) * 1.0 * hp.Cq;
+  double DQi[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) DQi[k] = hp.limitedQ ? F.f[F_DVDXQ_XX + k][i] : 0.0;
 
   NodeAcc a;
   a.rhoSum = a.norm = a.dvx = a.dvy = a.dvz = a.deps = a.gx = a.gy = a.gz = 0.0;
@@ -442,9 +446,38 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
       a.norm += mi / rhoi * Wi;
     }
     const double vijx = vxi - vxj, vijy = vyi - vyj, vijz = vzi - vzj;
-    // Monaghan-Gingold Q
-    const double mui = (vijx * eix + vijy * eiy + vijz * eiz) / (etaMag2i + hp.eps2);
-    const double muj = (vijx * ejx + vijy * ejy + vijz * ejz) / (etaMag2j + hp.eps2);
+    // Monaghan-Gingold Q; the limited form first corrects the two velocities
+    // along the pair with the Q's DvDx (LimitedMonaghanGingoldViscosity.cc:171-200)
+    double vqx = vijx, vqy = vijy, vqz = vijz;
+    if (hp.limitedQ) {
+      double Dj[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Dj[k] = F.f[F_DVDXQ_XX + k][j];
+      imageTensor(g, code, Dj);
+      const double hx = 0.5 * rx, hy = 0.5 * ry, hz = 0.5 * rz;
+      const double aix = DQi[0] * hx + DQi[1] * hy + DQi[2] * hz;
+      const double aiy = DQi[3] * hx + DQi[4] * hy + DQi[5] * hz;
+      const double aiz = DQi[6] * hx + DQi[7] * hy + DQi[8] * hz;
+      const double ajx = Dj[0] * hx + Dj[1] * hy + Dj[2] * hz;
+      const double ajy = Dj[3] * hx + Dj[4] * hy + Dj[5] * hz;
+      const double ajz = Dj[6] * hx + Dj[7] * hy + Dj[8] * hz;
+      const double gri = aix * hx + aiy * hy + aiz * hz;
+      const double grj = ajx * hx + ajy * hy + ajz * hz;
+      const double rri = gri / ((grj < 0.0 ? -1.0 : 1.0) * fmax(1.0e-30, fabs(grj)));
+      const double rrj = grj / ((gri < 0.0 ? -1.0 : 1.0) * fmax(1.0e-30, fabs(gri)));
+      const double xl = fmin(rri, rrj);
+      double phi = xl > 0.0 ? 2.0 / (1.0 + xl) * 2.0 * xl / (1.0 + xl) : 0.0;   // van Leer
+      const double etaij = fmin(etaMagi, etaMagj);
+      if (etaij < hp.etaCrit) {
+        const double z = (etaij - hp.etaCrit) / hp.etaFold;
+        phi *= exp(-(z * z));
+      }
+      vqx = (vxi - phi * aix) - (vxj + phi * ajx);
+      vqy = (vyi - phi * aiy) - (vyj + phi * ajy);
+      vqz = (vzi - phi * aiz) - (vzj + phi * ajz);
+    }
+    const double mui = (vqx * eix + vqy * eiy + vqz * eiz) / (etaMag2i + hp.eps2);
+    const double muj = (vqx * ejx + vqy * ejy + vqz * ejz) / (etaMag2j + hp.eps2);
     const double lmi = hp.linearInExpansion ? mui : fmin(0.0, mui);
     const double lmj = hp.linearInExpansion ? muj : fmin(0.0, muj);
     const double qmi = hp.quadraticInExpansion ? -(mui < 0.0 ? -1.0 : 1.0) * mui * mui : fmin(0.0, mui) * fmin(0.0, mui);
@@ -821,10 +854,37 @@ void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, 
   cellKeyKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, g, keys, vals, cellc);
   lc->add(1);
 }
+// ArtificialViscosityHandle::postStateUpdate: the Q's DvDx = the hydro DvDx.
+__global__ void copyQGradientKernel(Fields F, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) F.f[F_DVDXQ_XX + k][i] = F.f[F_DVDX_XX + k][i];
+}
+// FP32 mirror of the Q's DvDx for the mixed pair sweep.
+__global__ void qGradient32Kernel(Fields F, float4* __restrict__ dvq, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float v[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) v[k] = (float)F.f[F_DVDXQ_XX + k][i];
+  dvq[3 * i] = make_float4(v[0], v[1], v[2], v[3]);
+  dvq[3 * i + 1] = make_float4(v[4], v[5], v[6], v[7]);
+  dvq[3 * i + 2] = make_float4(v[8], 0.0f, 0.0f, 0.0f);
+}
+void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
+  copyQGradientKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
+  lc->add(1);
+}
+void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc) {
+  qGradient32Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, dvq, n);
+  lc->add(1);
+}
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   cudaStream_t s, LaunchCounter* lc) {
-  permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n);
+                   bool withQGradient, cudaStream_t s, LaunchCounter* lc) {
+  permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n,
+                                                withQGradient ? (int)F_NUM_PERMUTED : (int)F_DVDXQ_XX);
   lc->add(1);
 }
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,

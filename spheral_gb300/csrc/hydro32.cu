@@ -86,7 +86,7 @@ __device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, cons
   }
 }
 
-template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF>
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF, bool LIMQ>
 __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
@@ -109,6 +109,13 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   const int N1 = hp.tableN1;
   const float Cl = (float)hp.Cl, Cq = (float)hp.Cq, eps2 = (float)hp.eps2;
   const float epsT = (float)hp.epsTensile, WnPerh = (float)hp.WnPerh;
+  float DQi[9];   // the limited Q's DvDx of node i
+  if (LIMQ) {
+    const float4 d0 = P.dvq[3 * i], d1 = P.dvq[3 * i + 1], d2 = P.dvq[3 * i + 2];
+    DQi[0] = d0.x; DQi[1] = d0.y; DQi[2] = d0.z; DQi[3] = d0.w;
+    DQi[4] = d1.x; DQi[5] = d1.y; DQi[6] = d1.z; DQi[7] = d1.w; DQi[8] = d2.x;
+  }
+  const float etaCrit = (float)hp.etaCrit, etaFold = (float)hp.etaFold;
   const float iri = __frcp_rn(rhoi);
   const float mrhoi = mi * iri;
   const float Prhoi0 = __fmul_rn(__fmul_rn(__fmul_rn(sOi, Pi), iri), iri);
@@ -185,12 +192,50 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
       norm += mrhoi * Wi;
     }
     const float vx = vi.x - vxj, vy = vi.y - vyj, vz = vi.z - vzj;
-    const float mui = __fdividef(__fmaf_rn(vz, eiz, __fmaf_rn(vy, eiy, __fmul_rn(vx, eix))), __fadd_rn(e2i, eps2));
-    const float muj = __fdividef(__fmaf_rn(vz, ejz, __fmaf_rn(vy, ejy, __fmul_rn(vx, ejx))), __fadd_rn(e2j, eps2));
-    const float li_ = hp.linearInExpansion ? mui : fminf(0.f, mui);
-    const float lj_ = hp.linearInExpansion ? muj : fminf(0.f, muj);
-    const float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : li_ * li_;
-    const float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : lj_ * lj_;
+    float vqx = vx, vqy = vy, vqz = vz;
+    if (LIMQ) {
+      // LimitedMonaghanGingoldViscosity.cc:171-200 in a form symmetric in
+      // (i, j): v_q = v_ij - phi (DvDx_i + DvDx_j) x_ij with x_ij = r/2, so
+      // the pair force stays bitwise antisymmetric.
+      const float4 d0 = P.dvq[3 * (long)j], d1 = P.dvq[3 * (long)j + 1], d2 = P.dvq[3 * (long)j + 2];
+      float Dj[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
+      const uint32_t mq = (uint32_t)dcode & mm;
+      if (mq) {
+        const float sg[3] = {(mq & 3u) ? -1.f : 1.f, (mq & 12u) ? -1.f : 1.f, (mq & 48u) ? -1.f : 1.f};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) Dj[3 * r + cc] *= sg[r] * sg[cc];
+      }
+      const float hx = 0.5f * rx, hy = 0.5f * ry, hz = 0.5f * rz;
+      const float aix = __fmaf_rn(DQi[2], hz, __fmaf_rn(DQi[1], hy, __fmul_rn(DQi[0], hx)));
+      const float aiy = __fmaf_rn(DQi[5], hz, __fmaf_rn(DQi[4], hy, __fmul_rn(DQi[3], hx)));
+      const float aiz = __fmaf_rn(DQi[8], hz, __fmaf_rn(DQi[7], hy, __fmul_rn(DQi[6], hx)));
+      const float ajx = __fmaf_rn(Dj[2], hz, __fmaf_rn(Dj[1], hy, __fmul_rn(Dj[0], hx)));
+      const float ajy = __fmaf_rn(Dj[5], hz, __fmaf_rn(Dj[4], hy, __fmul_rn(Dj[3], hx)));
+      const float ajz = __fmaf_rn(Dj[8], hz, __fmaf_rn(Dj[7], hy, __fmul_rn(Dj[6], hx)));
+      const float gri = __fmaf_rn(aiz, hz, __fmaf_rn(aiy, hy, __fmul_rn(aix, hx)));
+      const float grj = __fmaf_rn(ajz, hz, __fmaf_rn(ajy, hy, __fmul_rn(ajx, hx)));
+      const float rri = __fdiv_rn(gri, (grj < 0.f ? -1.f : 1.f) * fmaxf(1.0e-30f, fabsf(grj)));
+      const float rrj = __fdiv_rn(grj, (gri < 0.f ? -1.f : 1.f) * fmaxf(1.0e-30f, fabsf(gri)));
+      const float xl = fminf(rri, rrj);
+      float phi = xl > 0.f ? __fdiv_rn(4.0f * xl, __fmul_rn(1.0f + xl, 1.0f + xl)) : 0.f;   // van Leer
+      const float etaij = fminf(etai, etaj);
+      if (etaij < etaCrit) {
+        const float z = __fdiv_rn(etaij - etaCrit, etaFold);
+        phi *= expf(-(z * z));
+      }
+      vqx = __fsub_rn(vx, __fmul_rn(phi, __fadd_rn(aix, ajx)));
+      vqy = __fsub_rn(vy, __fmul_rn(phi, __fadd_rn(aiy, ajy)));
+      vqz = __fsub_rn(vz, __fmul_rn(phi, __fadd_rn(aiz, ajz)));
+    }
+    const float mui = __fdividef(__fmaf_rn(vqz, eiz, __fmaf_rn(vqy, eiy, __fmul_rn(vqx, eix))), __fadd_rn(e2i, eps2));
+    const float muj = __fdividef(__fmaf_rn(vqz, ejz, __fmaf_rn(vqy, ejy, __fmul_rn(vqx, ejx))), __fadd_rn(e2j, eps2));
+    const float mni = fminf(0.f, mui), mnj = fminf(0.f, muj);
+    const float li_ = hp.linearInExpansion ? mui : mni;
+    const float lj_ = hp.linearInExpansion ? muj : mnj;
+    const float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : mni * mni;
+    const float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : mnj * mnj;
     const float ei = __fmaf_rn(Cq, qi_, __fmul_rn(mClci, li_));
     const float ej = __fmaf_rn(Cq, qj_, __fmul_rn(__fmul_rn(-Cl, csj), lj_));
     const float qai = __fmul_rn(0.5f, __fmul_rn(ei, iri)), qaj = __fmul_rn(0.5f, __fmul_rn(ej, irj));
@@ -650,26 +695,35 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
   const int b = 128;
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
-#define SPH_PAIR32(X, C, M, MB, PF) \
-  pairKernelFP32<X, C, M, MB, PF><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
-  if (!hp.xsph && hp.compatible && !multi) {
+#define SPH_PAIR32(X, C, M, MB, PF, LQ) \
+  pairKernelFP32<X, C, M, MB, PF, LQ><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
+  if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity: one variant per path
+    if (!hp.xsph && hp.compatible && !multi) SPH_PAIR32(false, true, false, 4, true, true);
+    else if (hp.xsph) {
+      if (hp.compatible) SPH_PAIR32(true, true, true, 4, false, true);
+      else SPH_PAIR32(true, false, true, 4, false, true);
+    } else {
+      if (hp.compatible) SPH_PAIR32(false, true, true, 4, false, true);
+      else SPH_PAIR32(false, false, true, 4, false, true);
+    }
+  } else if (!hp.xsph && hp.compatible && !multi) {
     switch (variant) {
-      case 0: SPH_PAIR32(false, true, false, 4, false); break;
-      case 2: SPH_PAIR32(false, true, false, 6, false); break;
-      case 3: SPH_PAIR32(false, true, false, 4, true); break;
-      case 4: SPH_PAIR32(false, true, false, 5, true); break;
-      case 5: SPH_PAIR32(false, true, false, 6, true); break;
-      default: SPH_PAIR32(false, true, false, 5, false); break;
+      case 0: SPH_PAIR32(false, true, false, 4, false, false); break;
+      case 2: SPH_PAIR32(false, true, false, 6, false, false); break;
+      case 3: SPH_PAIR32(false, true, false, 4, true, false); break;
+      case 4: SPH_PAIR32(false, true, false, 5, true, false); break;
+      case 5: SPH_PAIR32(false, true, false, 6, true, false); break;
+      default: SPH_PAIR32(false, true, false, 5, false, false); break;
     }
   } else if (hp.xsph) {
     if (hp.compatible) {
-      if (multi) SPH_PAIR32(true, true, true, 5, false); else SPH_PAIR32(true, true, false, 5, false);
+      if (multi) SPH_PAIR32(true, true, true, 5, false, false); else SPH_PAIR32(true, true, false, 5, false, false);
     } else {
-      if (multi) SPH_PAIR32(true, false, true, 5, false); else SPH_PAIR32(true, false, false, 5, false);
+      if (multi) SPH_PAIR32(true, false, true, 5, false, false); else SPH_PAIR32(true, false, false, 5, false, false);
     }
   } else {
-    if (hp.compatible) SPH_PAIR32(false, true, true, 5, false);
-    else { if (multi) SPH_PAIR32(false, false, true, 5, false); else SPH_PAIR32(false, false, false, 5, false); }
+    if (hp.compatible) SPH_PAIR32(false, true, true, 5, false, false);
+    else { if (multi) SPH_PAIR32(false, false, true, 5, false, false); else SPH_PAIR32(false, false, false, 5, false, false); }
   }
 #undef SPH_PAIR32
   lc->add(1);

@@ -31,9 +31,13 @@ void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, doubl
 // Neighbour build -------------------------------------------------------------
 void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, uint32_t* cellc, cudaStream_t s,
                     LaunchCounter* lc);
+// withQGradient: also move the limited Q's DvDx copy.
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   cudaStream_t s, LaunchCounter* lc);
+                   bool withQGradient, cudaStream_t s, LaunchCounter* lc);
+// The limited Q's DvDx <- the hydro DvDx; and its FP32 mirror (3 float4 per node).
+void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
+void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc);
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
 // Group-cooperative neighbour search over items (first node of each chunk of

@@ -17,17 +17,22 @@ FIELD_NCOMP = {
     "DvDt": 3, "DrhoDt": 1, "DepsDt": 1, "DvDx": 9, "internalDvDx": 9, "gradRho": 3, "M": 9, "localM": 9,
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
-    "DepsDtCompatible": 1, "numNeighbors": 1,
+    "DepsDtCompatible": 1, "numNeighbors": 1, "ArtificialViscosityVelocityGradient": 9,
 }
 
 DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acceleration", "velocity magnitude",
               "pairwise velocity difference", "gravity"]
 
 
+VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
+
+
 def config_from_dict(cfg, precision="fp64", device=0):
     c = N.default_config()
     for k, v in cfg.items():
-        if k in dict(N.Config._fields_):
+        if k == "viscosity" and isinstance(v, str):
+            c.viscosity = VISCOSITY[v]
+        elif k in dict(N.Config._fields_):
             setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
     c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)
     c.device = device
