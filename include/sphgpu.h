@@ -259,6 +259,20 @@ int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
 int sphgpu_set_pair_variant(sphgpu_handle h, int variant);
 int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
 
+/* Checkpoint and restart.  Replaces: SPHBase::dumpState / restoreState
+ * (src/SPH/SPHBase.cc:711-768) with the integrator's time, last dt and cycle,
+ * written through the caller's FileIO.  sphgpu_checkpoint_size gives the byte
+ * count of the image of the current state; sphgpu_checkpoint copies it into
+ * the caller's buffer; sphgpu_restore loads an image into a handle created
+ * with the same configuration, NodeLists and boundaries (no set_particles
+ * needed).  The image keeps the library's internal node order and kernel
+ * variant, so a restored run continues bitwise as the uninterrupted one.
+ * SPHGPU_E_ARG for a buffer that is not such an image, SPHGPU_E_STATE for an
+ * image of another precision mode, viscosity or NodeList set. */
+int sphgpu_checkpoint_size(sphgpu_handle h, size_t* bytes);
+int sphgpu_checkpoint(sphgpu_handle h, void* buffer, size_t bytes);
+int sphgpu_restore(sphgpu_handle h, const void* buffer, size_t bytes);
+
 /* Wait for all work on the handle's stream. */
 int sphgpu_synchronize(sphgpu_handle h);
 

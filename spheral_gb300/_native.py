@@ -93,6 +93,9 @@ SIGNATURES = {
     "sphgpu_advance": (_i, [_vp, _i, _d]),
     "sphgpu_ensemble_advance": (_i, [_vp, _i, _i, _d, _i, _vp]),
     "sphgpu_set_pair_variant": (_i, [_vp, _i]),
+    "sphgpu_checkpoint_size": (_i, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "sphgpu_checkpoint": (_i, [_vp, _vp, ctypes.c_size_t]),
+    "sphgpu_restore": (_i, [_vp, _vp, ctypes.c_size_t]),
     "sphgpu_get_pair_variant": (_i, [_vp, _ip, _ip]),
     "sphgpu_get_field": (_i, [_vp, _cp, _dp, _ip]),
     "sphgpu_set_field": (_i, [_vp, _cp, _dp]),

@@ -829,6 +829,20 @@ int failStd(sphgpu_ctx* c, const std::exception& e) {
 
 }  // namespace
 
+namespace {
+struct CheckpointHeader {
+  char magic[8];
+  int32_t version, nfields;
+  int64_t n, cycle;
+  double time, lastDt, dtMultiplier, dtMinAcc, extraEnergy;
+  int32_t precision, numLists, pairVariant, viscosity;
+};
+constexpr char kCheckpointMagic[8] = {'S', 'P', 'H', 'G', 'P', 'U', 'C', 'K'};
+size_t checkpointBytes(long n) {
+  return sizeof(CheckpointHeader) + (size_t)F_NUM_PERMUTED * n * sizeof(double) + 2 * (size_t)n * sizeof(int);
+}
+}  // namespace
+
 extern "C" {
 
 void sphgpu_default_config(sphgpu_config* c) {
@@ -1013,6 +1027,97 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   CUDA_OK(cudaMemcpy(c->list[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   c->haveNeighbors = false;
   c->initialized = false;
+  refreshParams(c);
+  API_END(c)
+}
+
+//------------------------------------------------------------------------------
+// Checkpoint / restart (the package's dumpState / restoreState,
+// src/SPH/SPHBase.cc:711-768, plus the integrator's time, last dt and cycle).
+// The image keeps the internal node order, so a restored run continues
+// bitwise as the uninterrupted one.
+//------------------------------------------------------------------------------
+
+int sphgpu_checkpoint_size(sphgpu_handle c, size_t* bytes) {
+  API_BEGIN(c)
+  if (!bytes) throw Error(SPHGPU_E_ARG, "null size");
+  requireState(c);
+  *bytes = checkpointBytes(c->n);
+  API_END(c)
+}
+
+int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
+  API_BEGIN(c)
+  requireState(c);
+  if (!buffer || bytes < checkpointBytes(c->n)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
+  const long n = c->n;
+  CheckpointHeader h{};
+  std::memcpy(h.magic, kCheckpointMagic, 8);
+  h.version = 1;
+  h.nfields = F_NUM_PERMUTED;
+  h.n = n;
+  h.cycle = c->cycle;
+  h.time = c->time;
+  h.lastDt = c->lastDt;
+  h.dtMultiplier = c->dtMultiplier;
+  h.dtMinAcc = c->dtMinAcc;
+  h.extraEnergy = c->extraEnergy;
+  h.precision = c->cfg.precision;
+  h.numLists = c->numLists;
+  h.pairVariant = c->pairVariant;
+  h.viscosity = c->cfg.viscosity;
+  char* out = static_cast<char*>(buffer);
+  std::memcpy(out, &h, sizeof(h));
+  out += sizeof(h);
+  for (int f = 0; f < F_NUM_PERMUTED; ++f, out += n * sizeof(double))
+    CUDA_OK(cudaMemcpyAsync(out, c->F.f[f], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaMemcpyAsync(out, c->origp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  out += n * sizeof(int);
+  CUDA_OK(cudaMemcpyAsync(out, c->listp(), n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
+  API_BEGIN(c)
+  if (!buffer || bytes < sizeof(CheckpointHeader)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
+  CheckpointHeader h;
+  std::memcpy(&h, buffer, sizeof(h));
+  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1 || h.nfields != F_NUM_PERMUTED)
+    throw Error(SPHGPU_E_ARG, "not a checkpoint of this library version");
+  if (h.n <= 0 || h.n >= kMaxNodes || bytes < checkpointBytes((long)h.n))
+    throw Error(SPHGPU_E_ARG, "checkpoint size does not match its node count");
+  if (h.precision != c->cfg.precision || h.viscosity != c->cfg.viscosity)
+    throw Error(SPHGPU_E_STATE, "checkpoint written with another precision mode or viscosity");
+  if (h.numLists > std::max(1, c->numLists))
+    throw Error(SPHGPU_E_STATE, "checkpoint uses NodeLists that are not set on this handle");
+  const long n = (long)h.n;
+  ensureCapacity(c, n);
+  c->n = n;
+  c->cur = 0;
+  c->F = c->fieldsOf(c->bankA);
+  c->Falt = c->fieldsOf(c->bankB);
+  CUDA_OK(cudaMemsetAsync(c->bankA.p, 0, c->bankA.bytes, c->stream));
+  const char* in = static_cast<const char*>(buffer) + sizeof(h);
+  for (int f = 0; f < F_NUM_PERMUTED; ++f, in += n * sizeof(double))
+    CUDA_OK(cudaMemcpyAsync(c->F.f[f], in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(cudaMemcpyAsync(c->orig[0].p, in, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  in += n * sizeof(int);
+  CUDA_OK(cudaMemcpyAsync(c->list[0].p, in, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->numLists = std::max(c->numLists, (int)h.numLists);
+  c->cycle = h.cycle;
+  c->time = h.time;
+  c->lastDt = h.lastDt;
+  c->dtMultiplier = h.dtMultiplier;
+  c->dtMinAcc = h.dtMinAcc;
+  c->extraEnergy = h.extraEnergy;
+  c->pairVariant = h.pairVariant;   // same kernel variant: same rounding as the uninterrupted run
+  c->tunedN = n;
+  c->nbCap = 0;
+  c->nbCapNext = 0;
+  c->haveNeighbors = false;
+  c->initialized = true;
   refreshParams(c);
   API_END(c)
 }

@@ -135,6 +135,19 @@ class Engine:
     def synchronize(self):
         self._chk(self.L.sphgpu_synchronize(self.h))
 
+    def checkpoint(self):
+        """The restart image of the current state (bytes)."""
+        size = ctypes.c_size_t()
+        self._chk(self.L.sphgpu_checkpoint_size(self.h, ctypes.byref(size)))
+        buf = np.empty(size.value, dtype=np.uint8)
+        self._chk(self.L.sphgpu_checkpoint(self.h, buf.ctypes.data, size.value))
+        return buf.tobytes()
+
+    def restore(self, image):
+        buf = np.frombuffer(image, dtype=np.uint8)
+        self._chk(self.L.sphgpu_restore(self.h, buf.ctypes.data, buf.size))
+        self.n = int(np.frombuffer(image[16:24], dtype=np.int64)[0])
+
     def pair_variant(self):
         """(variant in use, number of variants) of the mixed-mode pair kernel."""
         v, nv = ctypes.c_int(), ctypes.c_int()
