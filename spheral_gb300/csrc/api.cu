@@ -412,7 +412,11 @@ bool resolveNeighbors(sphgpu_ctx* c);
 // Neighbour build: cell keys -> stable radix sort -> permute every field ->
 // cell ranges -> count -> scan -> fill.
 //------------------------------------------------------------------------------
-void buildNeighbors(sphgpu_ctx* c, bool deferCheck = false) {
+// inStep: called at the start of sphgpu_step -- the capacity check is left
+// to the step's dt synchronisation and only the carried fields are permuted
+// (the step rewrites the others before it returns).
+void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
+  const bool deferCheck = inStep;
   const long n = c->n;
   buildGrid(c);
   const Grid& g = c->grid;
@@ -442,7 +446,7 @@ void buildNeighbors(sphgpu_ctx* c, bool deferCheck = false) {
     const int nx = 1 - c->cur;
     launchPermute(c->F, c->Falt, v, c->orig[c->cur].as<int>(), c->orig[nx].as<int>(), c->list[c->cur].as<int>(),
                   c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n,
-                  c->hp.limitedQ != 0, c->stream, &c->lc);
+                  inStep, c->stream, &c->lc);
     std::swap(c->bankA, c->bankB);
     std::swap(c->F, c->Falt);
     c->cur = nx;
@@ -729,10 +733,11 @@ double step(sphgpu_ctx* c, double maxTime) {
   {
     Scope sc(c->prof, "update");
     launchSaveState0(c->F, c->n, c->stream, &c->lc);
-    launchUpdate(c->F, c->listp(), c->n, c->hp, hdt, true, c->cfg.gravity != 0, c->stream, &c->lc);
+    const Fields32 m32 = c->f32();
+    launchUpdate(c->F, c->listp(), c->n, c->hp, hdt, true, c->cfg.gravity != 0, c->fp32() ? &m32 : nullptr, c->grid,
+                 c->stream, &c->lc);
   }
   c->check();
-  prepare32(c);
   c->time = t + hdt;
   copyQGradient(c);                                  // postStateUpdate (mid): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
@@ -753,10 +758,11 @@ double step(sphgpu_ctx* c, double maxTime) {
   }
   {
     Scope sc(c->prof, "update");
-    launchUpdate(c->F, c->listp(), c->n, c->hp, dt, false, c->cfg.gravity != 0, c->stream, &c->lc);
+    const Fields32 m32 = c->f32();
+    launchUpdate(c->F, c->listp(), c->n, c->hp, dt, false, c->cfg.gravity != 0, c->fp32() ? &m32 : nullptr, c->grid,
+                 c->stream, &c->lc);
   }
   c->check();
-  prepare32(c);
   c->time = t + dt;
   copyQGradient(c);                                  // postStateUpdate (end): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
@@ -900,7 +906,7 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
     CUDA_OK(cudaMallocHost(&c->hsmall, 64 * sizeof(double)));
     c->time = cfg->time;
     c->lastDt = cfg->last_dt;
-    c->lists[0] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308};
+    c->lists[0] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308, 1e20, 1e-20};
     c->numLists = 0;
     if (cfg->gravity) c->grav = gravityCreate();
     // Build the default cubic B-spline table.
@@ -968,7 +974,7 @@ int sphgpu_set_nodelist(sphgpu_handle c, int k, double nPerh, double hmin, doubl
   if (!(nPerh > 0.0) || !(hmin > 0.0) || !(hmax >= hmin) || !(gamma > 1.0))
     throw Error(SPHGPU_E_ARG, "bad nodelist parameters");
   c->lists[k] = NodeListParams{nPerh, hmin, hmax, rhoMin, rhoMax, gamma, -1.7976931348623157e308,
-                               1.7976931348623157e308};
+                               1.7976931348623157e308, 1.0 / hmin, 1.0 / hmax};
   c->numLists = std::max(c->numLists, k + 1);
   refreshParams(c);
   API_END(c)
@@ -1278,6 +1284,8 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   FieldSpec fs;
   bool isH, isNb;
   if (!fieldSpec(name, fs, isH, isNb)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  if (fs.first == F_DVDXQ_XX && !c->hp.limitedQ)
+    throw Error(SPHGPU_E_STATE, "ArtificialViscosityVelocityGradient exists only with the limited Q");
   if (ncomp) *ncomp = fs.ncomp;
   if (!out) return SPHGPU_OK;
   requireState(c);

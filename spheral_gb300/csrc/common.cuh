@@ -28,6 +28,7 @@ struct Grid {
 
 struct NodeListParams {
   double nPerh, hmin, hmax, rhoMin, rhoMax, gamma, minP, maxP;
+  double hminInv, hmaxInv;   // 1/hmin, 1/hmax (computed on the host)
 };
 
 struct HydroParams {

@@ -363,15 +363,16 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
   F.f[F_M1_X][i] = a.m1x;
   F.f[F_M1_Y][i] = a.m1y;
   F.f[F_M1_Z][i] = a.m1z;
-  F.f[F_DHDT][i] = ((-F.f[F_HINV][i]) / 3.0) * (double)trace;
+  // FP32 forms of DHDt = -(H/3) tr(DvDx) and of the IdealH clamp
+  // 1/clamp(h0 f, hmin, hmax) = clamp(H0 / f, 1/hmax, 1/hmin): no FP64 divide.
+  F.f[F_DHDT][i] = (double)(-(ai * (1.0f / 3.0f)) * trace);
   const float nPerh = (float)L.nPerh;
   const bool iso = fabsf(m0) <= 1.0e-15f * fmaxf(1.0f, fabsf(m0));
   const float cur = iso ? 0.5f * nPerh : fmaxf(0.0f, hermiteLookup32(herm, hp, m0));
   const float s = fminf(4.0f, fmaxf(0.25f, nPerh / (cur + 1.0e-30f)));
   const float aa = s < 1.0f ? 0.4f * (1.0f + s * s) : 0.4f * (1.0f + 1.0f / (s * s * s));
-  const double hi0 = 1.0 / F.f[F_HINV][i];
-  const double hi1 = fmin(L.hmax, fmax(L.hmin, hi0 * (double)(1.0f - aa + aa * s)));
-  F.f[F_HIDEAL][i] = 1.0 / hi1;
+  const double hid = (double)(ai / (1.0f - aa + aa * s));
+  F.f[F_HIDEAL][i] = fmin(L.hminInv, fmax(L.hmaxInv, hid));
 }
 
 }  // namespace dev

@@ -695,31 +695,62 @@ __global__ void restoreState0Kernel(Fields F, long n) {
   F.f[F_RHO][i] = F.f[F_RHO0][i]; F.f[F_EPS][i] = F.f[F_EPS0][i]; F.f[F_HINV][i] = F.f[F_HINV0][i];
 }
 
+// P != nullptr (mixed mode): the FP32 mirrors of the new state are written
+// here as well (the prepare pass folded into the update).
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
-                             double mult, int mid, int gravity, int epsIncrement) {
+                             double mult, int mid, int gravity, int epsIncrement, Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
   if (epsIncrement) F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
-  F.f[F_X][i] += mult * F.f[F_DXDT_X][i];
-  F.f[F_Y][i] += mult * F.f[F_DXDT_Y][i];
-  F.f[F_Z][i] += mult * F.f[F_DXDT_Z][i];
+  const double x = F.f[F_X][i] + mult * F.f[F_DXDT_X][i];
+  const double y = F.f[F_Y][i] + mult * F.f[F_DXDT_Y][i];
+  const double z = F.f[F_Z][i] + mult * F.f[F_DXDT_Z][i];
+  F.f[F_X][i] = x;
+  F.f[F_Y][i] = y;
+  F.f[F_Z][i] = z;
   // velocity: "delta velocity hydro" sorts before "delta velocity" (gravity)
-  F.f[F_VX][i] += mult * F.f[F_DVDT_X][i];
-  F.f[F_VY][i] += mult * F.f[F_DVDT_Y][i];
-  F.f[F_VZ][i] += mult * F.f[F_DVDT_Z][i];
+  double vx = F.f[F_VX][i] + mult * F.f[F_DVDT_X][i];
+  double vy = F.f[F_VY][i] + mult * F.f[F_DVDT_Y][i];
+  double vz = F.f[F_VZ][i] + mult * F.f[F_DVDT_Z][i];
   if (gravity) {
-    F.f[F_VX][i] += mult * F.f[F_GRAV_X][i];
-    F.f[F_VY][i] += mult * F.f[F_GRAV_Y][i];
-    F.f[F_VZ][i] += mult * F.f[F_GRAV_Z][i];
+    vx += mult * F.f[F_GRAV_X][i];
+    vy += mult * F.f[F_GRAV_Y][i];
+    vz += mult * F.f[F_GRAV_Z][i];
   }
-  F.f[F_RHO][i] = fmin(L.rhoMax, fmax(L.rhoMin, F.f[F_RHO][i] + mult * F.f[F_DRHODT][i]));
-  const double hminInv = 1.0 / L.hmin, hmaxInv = 1.0 / L.hmax;
+  F.f[F_VX][i] = vx;
+  F.f[F_VY][i] = vy;
+  F.f[F_VZ][i] = vz;
+  const double rho = fmin(L.rhoMax, fmax(L.rhoMin, F.f[F_RHO][i] + mult * F.f[F_DRHODT][i]));
+  F.f[F_RHO][i] = rho;
+  const double hminInv = L.hminInv, hmaxInv = L.hmaxInv;
   double h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
   if (h < hmaxInv) h = hmaxInv;
   if (h > hminInv) h = hminInv;
   F.f[F_HINV][i] = h;
-  eosNode(F, i, L);
+  if (P.posh) {
+    // Mixed mode: the sound speed feeds only FP32 sweeps (Q, dt vote), so it
+    // is evaluated in FP32 (an FP64 square root costs many cycles of GB300's
+    // thin FP64 pipe).
+    const double eps = F.f[F_EPS][i];
+    double p = (L.gamma - 1.0) * rho * eps;
+    p = p < L.minP ? L.minP : (p > L.maxP ? L.maxP : p);
+    F.f[F_P][i] = p;
+    F.f[F_CS][i] = (double)sqrtf(fmaxf(0.0f, (float)(L.gamma * (L.gamma - 1.0) * eps)));
+  } else {
+    eosNode(F, i, L);
+  }
+  if (P.posh) {
+    int c[3];
+    unpackCell(P.cell[i], c);
+    const double ox = g.lo[0] + c[0] * g.cell[0];
+    const double oy = g.lo[1] + c[1] * g.cell[1];
+    const double oz = g.lo[2] + c[2] * g.cell[2];
+    P.posh[i] = make_float4((float)(x - ox), (float)(y - oy), (float)(z - oz), (float)h);
+    P.velm[i] = make_float4((float)vx, (float)vy, (float)vz, (float)F.f[F_MASS][i]);
+    const float om = (float)F.f[F_OMEGA][i];
+    P.thermo[i] = make_float4((float)rho, (float)F.f[F_P][i], (float)F.f[F_CS][i], om / (om * om + 1.0e-30f));
+  }
 }
 
 __global__ void eosKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists) {
@@ -882,9 +913,9 @@ void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCoun
 }
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool withQGradient, cudaStream_t s, LaunchCounter* lc) {
+                   bool carriedOnly, cudaStream_t s, LaunchCounter* lc) {
   permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n,
-                                                withQGradient ? (int)F_NUM_PERMUTED : (int)F_DVDXQ_XX);
+                                                carriedOnly ? (int)F_NUM_CARRIED : (int)F_NUM_PERMUTED);
   lc->add(1);
 }
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
@@ -958,9 +989,12 @@ void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
   lc->add(1);
 }
 void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
-                  bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc) {
+                  bool mid, bool gravity, const Fields32* mirror, const Grid& g, cudaStream_t s, LaunchCounter* lc) {
   const int epsInc = (mid || !hp.compatible) ? 1 : 0;
-  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc);
+  Fields32 P{};
+  if (mirror) P = *mirror;
+  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc, P,
+                                               g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

@@ -370,8 +370,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     const int li = multi ? list[i] : 0;
     const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
     const int N1 = hp.tableN1;
-    const float hi = 1.0f / pi.w;
-    float s = 0.f, c = 0.f, bestPair = 3.0e38f;
+    float s = 0.f, c = 0.f, worstPair = 0.0f;
     const int cnt = nl.count[i];
     // software pipeline: entry two slots ahead, node data one slot ahead
     uint32_t entA = 0u, entB = 0u;
@@ -404,9 +403,12 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
       float vxj = vj.x, vyj = vj.y, vzj = vj.z;
       mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
       const float dx = vi.x - vxj, dy = vi.y - vyj, dz = vi.z - vzj;
-      const float hmin = fminf(hi, 1.0f / aj);
-      bestPair = fminf(bestPair, hmin / fmaxf(1.0e-30f, sqrtf(dx * dx + dy * dy + dz * dz)));
+      // min over pairs of min(h_i, h_j)/|v_ij| = 1/sqrt(max over pairs of
+      // (max(a_i, a_j) |v_ij|)^2): no division or root per pair
+      const float am = fmaxf(pi.w, aj);
+      worstPair = fmaxf(worstPair, (am * am) * (dx * dx + dy * dy + dz * dz));
     }
+    const float bestPair = worstPair > 0.0f ? rsqrtf(worstPair) : 3.0e38f;
     const double a = F.f[F_HINV][i];
     const double rho = F.f[F_MASS][i] * (((a * a) * a) * hp.W0) + kahanValue(s, c);
     F.f[F_RHO][i] = rho;
@@ -455,10 +457,10 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
 //------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl,
                                                      TableDev t, HydroParams hp) {
-  __shared__ float tw[kMaxTable];
-  __shared__ float tg[kMaxTable];
-  const int ntab = 3 * (hp.tableN1 + 1);
-  for (int k = threadIdx.x; k < ntab; k += blockDim.x) { tw[k] = t.w32[k]; tg[k] = t.g32[k]; }
+  __shared__ float4 ta[kMaxTable / 3];
+  __shared__ float2 tb[kMaxTable / 3];
+  const int nint = hp.tableN1 + 1;
+  for (int k = threadIdx.x; k < nint; k += blockDim.x) { ta[k] = t.p32a[k]; tb[k] = t.p32b[k]; }
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -472,25 +474,37 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
   const int N1 = hp.tableN1;
   float ws = 0.f, wc = 0.f, gs = 0.f, gc = 0.f;
   const int cnt = nl.count[i];
+  // software pipeline: entry two slots ahead, node position one slot ahead
+  uint32_t entA = 0u, entB = 0u;
+  float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (cnt > 0) {
+    entA = nl.nbr[nbSlot(i, 0, nl.cap)];
+    pjA = P.posh[(int)(entA & kIndexMask)];
+  }
+  if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
   for (int q = 0; q < cnt; ++q) {
-    const long long k = nbSlot(i, q, nl.cap);
-    const uint32_t ent = nl.nbr[k];
-    const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
+    const uint32_t ent = entA;
+    const float4 pj = pjA;
+    if (q + 1 < cnt) {
+      pjA = P.posh[(int)(entB & kIndexMask)];
+      entA = entB;
+    }
+    if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
+    const int dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
-    relSep(pi, P.posh[j], dcode, mm, cx, cy, cz, rx, ry, rz);
+    relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
     const float eta = ai * sqrtf(rx * rx + ry * ry + rz * rz);
     float w, gr;
-    lookup32(tw, tg, N1, invStep, eta, extent, w, gr);
+    lookupPacked(ta, tb, N1, invStep, eta, extent, w, gr);
     kahanAdd(ws, wc, w);
     kahanAdd(gs, gc, eta * gr);
   }
-  const double a = F.f[F_HINV][i];
-  const double Hdet = (a * a) * a;
-  double omega;
-  if (cnt == 0) omega = 1.0;
-  else omega = fmax(1.0e-30, -(Hdet * kahanValue(gs, gc)) / (3.0 * (Hdet * kahanValue(ws, wc) + Hdet * hp.W0)));
-  F.f[F_OMEGA][i] = omega;
-  P.thermo[i].w = (float)(omega / (omega * omega + 1.0e-30));
+  // Omega = -sum eta dW/deta / (3 (sum W + W0)) (Hdet cancels), in FP32 from
+  // the compensated sums
+  float omega = 1.0f;
+  if (cnt > 0) omega = fmaxf(1.0e-30f, -(gs - gc) / (3.0f * ((ws - wc) + (float)hp.W0)));
+  F.f[F_OMEGA][i] = (double)omega;
+  P.thermo[i].w = omega / (omega * omega + 1.0e-30f);
 }
 
 //------------------------------------------------------------------------------

@@ -31,10 +31,12 @@ void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, doubl
 // Neighbour build -------------------------------------------------------------
 void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, uint32_t* cellc, cudaStream_t s,
                     LaunchCounter* lc);
-// withQGradient: also move the limited Q's DvDx copy.
+// carriedOnly: move only the state and the derivatives the next step reads
+// before recomputing them (the step rewrites every other field before it
+// returns); otherwise every permuted field.
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool withQGradient, cudaStream_t s, LaunchCounter* lc);
+                   bool carriedOnly, cudaStream_t s, LaunchCounter* lc);
 // The limited Q's DvDx <- the hydro DvDx; and its FP32 mirror (3 float4 per node).
 void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc);
@@ -86,9 +88,10 @@ void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, cons
 void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
-// already advanced by the compatible-energy sweep when compatible).
+// already advanced by the compatible-energy sweep when compatible).  mirror:
+// also refresh the FP32 mirrors of the new state (mixed mode), cells of grid g.
 void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
-                  bool mid, bool gravity, cudaStream_t s, LaunchCounter* lc);
+                  bool mid, bool gravity, const Fields32* mirror, const Grid& g, cudaStream_t s, LaunchCounter* lc);
 // lists: device table of NodeListParams (HydroParams::lists).
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc);
 void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
