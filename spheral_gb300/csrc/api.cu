@@ -366,12 +366,14 @@ void buildGrid(sphgpu_ctx* c) {
     g.lo[a] = lo;
     g.hi[a] = hi;
     g.cell[a] = cell;
+    g.cellf[a] = (float)cell;
     g.nc[a] = nc;
     if (g.kindLo[a] != AXIS_PERIODIC) {   // open sides: the grid origin follows the data
       if (g.kindLo[a] == AXIS_OPEN) g.wallLo[a] = lo;
       if (g.kindHi[a] == AXIS_OPEN) g.wallHi[a] = hi;
     }
   }
+  g.ext2f = (float)(c->hp.extent * c->hp.extent);
   c->grid = g;
 }
 

@@ -24,6 +24,8 @@ struct Grid {
   int kindHi[3];       // AxisKind of the high side
   double wallLo[3];    // reflecting wall coordinates / periodic planes
   double wallHi[3];
+  float cellf[3];      // cell edges rounded to FP32 (set on the host: no device conversions)
+  float ext2f;         // kernel extent squared, FP32
 };
 
 struct NodeListParams {

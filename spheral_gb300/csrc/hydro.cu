@@ -162,11 +162,11 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const float4 pi = active ? P.posh[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float ai2 = pi.w * pi.w;
   const float del = __fmaf_rn(bandA, pi.w, bandB);   // per-node band half-width (relative)
-  const float e2t = (float)ext2;
+  const float e2t = g.ext2f;
   const float bandLo = del < 0.5f ? e2t * (1.0f - del) : -1.0f;
   const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
   const uint32_t mm = mirrorMask(g, hc);
-  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   int cnt = 0;
   // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
   uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;

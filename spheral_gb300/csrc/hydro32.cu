@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   int ci[3];
   unpackCell(P.cell[i], ci);
   const uint32_t mm = mirrorMask(g, ci);
-  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   const float4 pi = P.posh[i], vi = P.velm[i], thi = P.thermo[i];
   const int li = MULTI ? list[i] : 0;
   const float ai = pi.w, mi = vi.w, rhoi = thi.x, Pi = thi.y, csi = thi.z, sOi = thi.w;
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
   int ci[3];
   unpackCell(P.cell[i], ci);
   const uint32_t mm = mirrorMask(g, ci);
-  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   const float4 pi = P.posh[i];
   const float mi = P.velm[i].w;
   const bool multi = hp.numLists > 1;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     int ci[3];
     unpackCell(P.cell[i], ci);
     const uint32_t mm = mirrorMask(g, ci);
-    const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+    const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
     const float4 pi = P.posh[i], vi = P.velm[i];
     const float mi = vi.w;
     const bool multi = hp.numLists > 1;
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
   int ci[3];
   unpackCell(P.cell[i], ci);
   const uint32_t mm = mirrorMask(g, ci);
-  const float cx = (float)g.cell[0], cy = (float)g.cell[1], cz = (float)g.cell[2];
+  const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   const float4 pi = P.posh[i];
   const float ai = pi.w;
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
