@@ -158,6 +158,8 @@ struct sphgpu_ctx {
   int itemBound = 0;         // upper bound on the number of work items
   DBuf itemCount;            // device: number of work items
   bool capCheckPending = false, totalPending = false;
+  double cachedBounds[7] = {};   // min h^-1, min x y z, max x y z of the current state
+  bool boundsValid = false;      // cachedBounds describe the current state
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
   bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
   long tunedN = 0;
@@ -320,21 +322,26 @@ void requireState(sphgpu_ctx* c) {
 //------------------------------------------------------------------------------
 void buildGrid(sphgpu_ctx* c) {
   Scope sc(c->prof, "bounds");
-  double* d = c->small.as<double>();
-  c->scratch.ensure(7 * sizeof(double) * 4096);
-  launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, d, c->stream, &c->lc);
-  c->check();
-  CUDA_OK(cudaMemcpyAsync(c->hsmall, d, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_OK(cudaStreamSynchronize(c->stream));
-  const double minHinv = c->hsmall[0];
+  if (!c->boundsValid) {   // the bounds of the last step's check describe a changed state
+    double* d = c->small.as<double>() + 20;
+    c->scratch.ensure(7 * sizeof(double) * 4096);
+    launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, d, c->stream, &c->lc);
+    c->check();
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, d, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaStreamSynchronize(c->stream));
+    std::memcpy(c->cachedBounds, c->hsmall + 20, sizeof(c->cachedBounds));
+  }
+  c->boundsValid = false;   // consumed: the step moves the nodes
+  const double* bnd = c->cachedBounds;
+  const double minHinv = bnd[0];
   if (!(minHinv > 0.0) || !std::isfinite(minHinv)) throw Error(SPHGPU_E_NAN, "non-positive or non-finite H");
   const double hmax = 1.0 / minHinv;
   const double support = c->hp.extent * hmax * (1.0 + 1.0e-9);
   Grid g{};
   for (int a = 0; a < 3; ++a) {
     g.kindLo[a] = g.kindHi[a] = AXIS_OPEN;
-    g.wallLo[a] = c->hsmall[1 + a];
-    g.wallHi[a] = c->hsmall[4 + a];
+    g.wallLo[a] = bnd[1 + a];
+    g.wallHi[a] = bnd[4 + a];
   }
   for (const auto& b : c->bcs) {
     if (b.type == SPHGPU_BOUNDARY_PERIODIC) {
@@ -350,8 +357,8 @@ void buildGrid(sphgpu_ctx* c) {
     }
   }
   for (int a = 0; a < 3; ++a) {
-    const double lo = g.kindLo[a] == AXIS_OPEN ? c->hsmall[1 + a] : g.wallLo[a];
-    const double hi = g.kindHi[a] == AXIS_OPEN ? c->hsmall[4 + a] : g.wallHi[a];
+    const double lo = g.kindLo[a] == AXIS_OPEN ? bnd[1 + a] : g.wallLo[a];
+    const double hi = g.kindHi[a] == AXIS_OPEN ? bnd[4 + a] : g.wallHi[a];
     const double L = hi - lo;
     int nc = (int)std::min(1024.0, std::floor(L / support));
     if (g.kindLo[a] == AXIS_PERIODIC) {
@@ -689,15 +696,23 @@ double selectDt(sphgpu_ctx* c, double dtMin, double dtMax, bool fusedDone = fals
   return dt;
 }
 
+// The end-of-step check also takes the bounds the next neighbour build needs
+// (min h^-1, bounding box), read back in the same synchronisation.
 void checkState(sphgpu_ctx* c, const char* where) {
   int* flag = reinterpret_cast<int*>(c->small.as<double>() + 30);
   CUDA_OK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
   launchCheckState(c->F, c->n, flag, c->stream, &c->lc);
+  double* b = c->small.as<double>() + 20;
+  c->scratch.ensure(7 * sizeof(double) * 4096);
+  launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, b, c->stream, &c->lc);
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, b, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(c->hsmall + 30, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
   int h;
   std::memcpy(&h, c->hsmall + 30, sizeof(int));
   if (h) throw Error(SPHGPU_E_NAN, std::string("non-finite or non-positive state after ") + where);
+  std::memcpy(c->cachedBounds, c->hsmall + 20, sizeof(c->cachedBounds));
+  c->boundsValid = true;
 }
 
 // CheapSynchronousRK2::step (src/Integrator/CheapSynchronousRK2.cc:40-132).
@@ -997,6 +1012,7 @@ int sphgpu_add_boundary(sphgpu_handle c, int type, int axis, double lo, double h
 int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const double* vel, const double* mass,
                          const double* rho, const double* eps, const double* H, const int* nodelist) {
   API_BEGIN(c)
+  c->boundsValid = false;   // the state changes: bounds are measured again
   if (n <= 0 || n >= kMaxNodes) throw Error(SPHGPU_E_ARG, "particle count out of range");
   if (!pos || !vel || !mass || !rho || !eps || !H) throw Error(SPHGPU_E_ARG, "null particle array");
   if (c->numLists == 0) c->numLists = 1;
@@ -1088,6 +1104,7 @@ int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
 
 int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
   API_BEGIN(c)
+  c->boundsValid = false;   // the state changes: bounds are measured again
   if (!buffer || bytes < sizeof(CheckpointHeader)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
   CheckpointHeader h;
   std::memcpy(&h, buffer, sizeof(h));
@@ -1310,6 +1327,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
 
 int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   API_BEGIN(c)
+  c->boundsValid = false;   // the state changes: bounds are measured again
   if (!name || !in) throw Error(SPHGPU_E_ARG, "null argument");
   FieldSpec fs;
   bool isH, isNb;
@@ -1330,6 +1348,7 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
 int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, const double* mass, const double* rho,
                         const double* eps, const double* H) {
   API_BEGIN(c)
+  c->boundsValid = false;   // the state changes: bounds are measured again
   requireState(c);
   const long n = c->n;
   c->stage.ensure((size_t)n * 15 * sizeof(double));
