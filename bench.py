@@ -434,6 +434,59 @@ def run_ensemble(args, ws, rank, local, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_evrard_validation(args, ws, rank, local, dist):
+    """The Evrard collapse (1,048,576 nodes, mixed mode) integrated to
+    t = 0.8 and its radial profiles against the comparison profiles the
+    reference ships with its functional test
+    (tests/functional/EvrardSphericalCollapse/{rho,vel,entropy}.dat, kept as
+    tests/golden/evrard_profiles.npz)."""
+    from spheral_gb300 import problems
+    from spheral_gb300.engine import Engine
+    import torch
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "evrard_profiles.npz"))
+    p = problems.evrard(n=args.n_evrard)
+    eng = Engine.from_problem(p, precision=args.precision, device=local)
+    eng.initialize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps = 0
+    while eng.time < args.goal_time * (1.0 - 1e-12) and steps < args.max_steps:
+        eng.advance(200, args.goal_time)
+        steps += 200
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    x = eng.field("position")
+    v = eng.field("velocity")
+    rho = eng.field("massDensity")
+    P = eng.field("pressure")
+    r = np.linalg.norm(x, axis=1)
+    vr = np.sum(v * x, axis=1) / np.maximum(r, 1e-30)
+    A = P / rho ** (5.0 / 3.0)
+    edges = np.logspace(np.log10(0.01), 0.0, 41)
+    mid = np.sqrt(edges[1:] * edges[:-1])
+    idx = np.digitize(r, edges) - 1
+    prof = {k: np.array([np.median(a[idx == b]) if np.any(idx == b) else np.nan for b in range(len(mid))])
+            for k, a in (("rho", rho), ("vel", vr), ("entropy", A))}
+    sel = (mid > 0.05) & (mid < 0.7)
+    out = {}
+    for k in ("rho", "vel", "entropy"):
+        rr, vv = ref[k + "_r"], ref[k]
+        want = np.interp(np.log(mid[sel]), np.log(rr), vv)
+        got = prof[k][sel]
+        ok = np.isfinite(got)
+        if k == "vel":
+            out["L1_vr_over_max"] = float(np.mean(np.abs(got[ok] - want[ok])) / np.max(np.abs(vv)))
+        else:
+            out["mean_abs_log10_" + k] = float(np.mean(np.abs(np.log10(got[ok] / want[ok]))))
+    if rank != 0:
+        return
+    line = {"workload": "evrard_collapse_3d", "n": p.n, "goal_time": args.goal_time, "time": eng.time, "steps": steps,
+            "wall_s": wall, "precision": args.precision, "validation": out,
+            "profile_r": [float(a) for a in mid], "profile_rho": [float(a) for a in prof["rho"]],
+            "profile_vr": [float(a) for a in prof["vel"]], "profile_entropy": [float(a) for a in prof["entropy"]]}
+    print(json.dumps(line), flush=True)
+
+
 def problems_ensemble(nboxes):
     from spheral_gb300 import problems
     return problems.ensemble(nboxes)
@@ -447,6 +500,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard"])
     ap.add_argument("--n-evrard", type=int, default=1048576)
+    ap.add_argument("--validate", action="store_true", help="evrard: integrate to --goal-time and compare profiles")
+    ap.add_argument("--goal-time", type=float, default=0.8)
+    ap.add_argument("--max-steps", type=int, default=100000)
     ap.add_argument("--boxes", type=int, default=256)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
@@ -467,6 +523,8 @@ def main():
         build.build()
         if args.workload == "ensemble":
             run_ensemble(args, ws, rank, local, dist)
+        elif args.workload == "evrard" and args.validate:
+            run_evrard_validation(args, ws, rank, local, dist)
         else:
             run_ours(args, ws, rank, local, dist)
     if dist is not None:

@@ -1,8 +1,11 @@
-"""Generate the golden Sod profiles from the reference's own analytic solution.
+"""Generate the golden fixtures from the reference's own test data.
 
-Runs only where the reference source tree is available (it imports
-tests/functional/Hydro/Sod/SodAnalyticSolution.py from it, a pure-Python
-module); the output, sod_analytic.npz, is committed and read by the tests.
+Runs only where the reference source tree is available: it imports
+tests/functional/Hydro/Sod/SodAnalyticSolution.py (a pure-Python module) for
+sod_analytic.npz, and reads the Evrard collapse comparison profiles of
+tests/functional/EvrardSphericalCollapse/{rho,vel,entropy}.dat for
+evrard_profiles.npz.  The outputs are committed and read by the tests and
+the bench.
 
 Configuration: the 3-D planar Sod tube of spheral_gb300.problems.sod (x in
 [0, 2], interface at x = 1, rho 1 / 0.25, P 1 / 0.1795, gamma 5/3), profiles
@@ -15,6 +18,7 @@ import sys
 import numpy as np
 
 REF = "/root/reference/tests/functional/Hydro/Sod"
+EVRARD = "/root/reference/tests/functional/EvrardSphericalCollapse"
 
 
 def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analytic.npz")):
@@ -32,6 +36,18 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analy
         data[key + "_v"] = np.array(v)
         data[key + "_u"] = np.array(u)
         data[key + "_P"] = np.array(P)
+    np.savez(out, **data)
+    print("wrote", out)
+    evrard()
+
+
+def evrard(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "evrard_profiles.npz")):
+    """Radial profiles at t = 0.8 of the Evrard collapse (columns r, value)."""
+    data = {}
+    for name in ("rho", "vel", "entropy"):
+        a = np.loadtxt(os.path.join(EVRARD, name + ".dat"))
+        data[name + "_r"] = a[:, 0]
+        data[name] = a[:, 1]
     np.savez(out, **data)
     print("wrote", out)
 
