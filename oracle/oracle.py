@@ -46,6 +46,8 @@ class OrcConfig(ctypes.Structure):
         ("viscosity", ctypes.c_int),
         ("eta_crit_frac", ctypes.c_double),
         ("eta_fold_frac", ctypes.c_double),
+        ("smoothing_scale", ctypes.c_int),
+        ("fix_shape", ctypes.c_int),
     ]
 
 
@@ -105,6 +107,9 @@ def lib():
             "orc_bspline_value": (d, [d]),
             "orc_bspline_grad": (d, [d]),
             "orc_num_threads": (i, []),
+            "orc_set_nodelist_hminratio": (i, [vp, i, d]),
+            "orc_sym_eigen": (i, [dp, dp, dp]),
+            "orc_smoothing_scale_derivative": (i, [dp, dp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -124,6 +129,8 @@ def _ip(a):
 
 # artificial viscosity of the SPH package
 VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
+# smoothing-scale package: SPHSmoothingScale or ASPHClassicSmoothingScale
+SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
 
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
@@ -131,7 +138,7 @@ FIELD_NCOMP = {
     "DvDt": 3, "DrhoDt": 1, "DepsDt": 1, "DvDx": 9, "internalDvDx": 9, "gradRho": 3, "M": 9, "localM": 9,
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
-    "DepsDtCompatible": 1, "ArtificialViscosityVelocityGradient": 9,
+    "DepsDtCompatible": 1, "ArtificialViscosityVelocityGradient": 9, "massSecondMoment": 6,
 }
 
 
@@ -172,12 +179,15 @@ class Oracle:
         c.viscosity = VISCOSITY[cfg.get("viscosity", "monaghan_gingold")]
         c.eta_crit_frac = cfg.get("eta_crit_frac", 1.0)
         c.eta_fold_frac = cfg.get("eta_fold_frac", 0.2)
+        c.smoothing_scale = SMOOTHING_SCALE[cfg.get("smoothing_scale", "sph")]
+        c.fix_shape = int(cfg.get("fix_shape", False))
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))
         for k, nl in enumerate(problem.nodelists):
             self.L.orc_set_nodelist(self.h, k, nl["nPerh"], nl["hmin"], nl["hmax"], nl["rhoMin"], nl["rhoMax"],
                                     nl["gamma"])
+            self.L.orc_set_nodelist_hminratio(self.h, k, nl.get("hminratio", 0.1))
         for b in problem.boundaries:
             self.L.orc_add_boundary(self.h, b["type"], b["axis"], b["lo"], b["hi"], b.get("wall_high", 0))
         n = problem.n
@@ -301,3 +311,23 @@ def bspline_grad(eta):
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def sym_eigen(a6):
+    """Eigen-pairs of the symmetric tensor (xx, xy, xz, yy, yz, zz) as the
+    oracle's ASPH smoothing scale computes them: (values[3], vectors[3, 3])
+    with eigenvector k in column k."""
+    a = np.ascontiguousarray(a6, dtype=np.float64)
+    vals = np.zeros(3)
+    vecs = np.zeros(9)
+    lib().orc_sym_eigen(_dp(a), _dp(vals), _dp(vecs))
+    return vals, vecs.reshape(3, 3)
+
+
+def smoothing_scale_derivative(h6, dvdx9):
+    """The ASPH tensor DH/Dt of one node."""
+    h = np.ascontiguousarray(h6, dtype=np.float64)
+    d = np.ascontiguousarray(dvdx9, dtype=np.float64)
+    out = np.zeros(6)
+    lib().orc_smoothing_scale_derivative(_dp(h), _dp(d), _dp(out))
+    return out

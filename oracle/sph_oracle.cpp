@@ -168,6 +168,123 @@ static inline double pow4(double x) { return x * x * x * x; }
 static inline double rootnu3(double x) { return sgn(x) * std::pow(std::fabs(x), 0.3333333333333333); }
 
 //------------------------------------------------------------------------------
+// Symmetric-tensor functions of the ASPH smoothing scale.
+//------------------------------------------------------------------------------
+static inline ST divS(const ST& H, double s) { return {H.xx / s, H.xy / s, H.xz / s, H.yy / s, H.yz / s, H.zz / s}; }
+static inline ST identityS() { return {1.0, 0.0, 0.0, 1.0, 0.0, 1.0}; }
+static inline void addS(ST& a, const ST& b) { a.xx += b.xx; a.xy += b.xy; a.xz += b.xz; a.yy += b.yy; a.yz += b.yz; a.zz += b.zz; }
+// GeomSymmetricTensor<3>::Inverse (GeomSymmetricTensorInline.hh:1650-1661)
+static inline ST inverseS(const ST& a) {
+  const double d = detS(a);
+  return {(a.yy * a.zz - a.yz * a.yz) / d, (a.yz * a.xz - a.xy * a.zz) / d, (a.xy * a.yz - a.yy * a.xz) / d,
+          (a.xx * a.zz - a.xz * a.xz) / d, (a.xy * a.xz - a.xx * a.yz) / d, (a.xx * a.yy - a.xy * a.xy) / d};
+}
+// Eigen-pairs of a symmetric tensor (GeomSymmetricTensor<3>::eigenVectors,
+// GeomSymmetricTensorInline.hh:2309-2345): the tensor is scaled by its largest
+// element and elements below 1e-20 are zeroed, as there; the reference then
+// calls Eigen's SelfAdjointEigenSolver (Eigen 5.0.0, not vendored).  This
+// restatement diagonalises with cyclic Jacobi rotations, which converge to the
+// same eigen-pairs to rounding; every use below is a function of the tensor
+// (V f(lambda) V^T), so neither the order nor the signs of the pairs matter.
+// vec[r][k]: component r of eigenvector k.
+struct EigS { double val[3]; double vec[3][3]; };
+static EigS eigenVectorsS(const ST& H) {
+  const double fscale = std::max(10.0 * kDblEps, maxAbsS(H));
+  const double fi = 1.0 / fscale;
+  auto z = [](double x) { return std::fabs(x) < 1.0e-20 ? 0.0 : x; };
+  double a[3][3] = {{z(H.xx * fi), z(H.xy * fi), z(H.xz * fi)},
+                    {z(H.xy * fi), z(H.yy * fi), z(H.yz * fi)},
+                    {z(H.xz * fi), z(H.yz * fi), z(H.zz * fi)}};
+  double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  static const int P[3] = {0, 0, 1}, Q[3] = {1, 2, 2};
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    if (off <= 1.0e-40) break;
+    for (int r = 0; r < 3; ++r) {
+      const int p = P[r], q = Q[r];
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      const double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+      const double t = sgn(theta) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+      a[p][p] -= t * apq;
+      a[q][q] += t * apq;
+      a[p][q] = a[q][p] = 0.0;
+      const int o = 3 - p - q;   // the third index
+      const double aop = a[o][p], aoq = a[o][q];
+      a[o][p] = a[p][o] = c * aop - s * aoq;
+      a[o][q] = a[q][o] = s * aop + c * aoq;
+      for (int k = 0; k < 3; ++k) {
+        const double vp = v[k][p], vq = v[k][q];
+        v[k][p] = c * vp - s * vq;
+        v[k][q] = s * vp + c * vq;
+      }
+    }
+  }
+  EigS e;
+  for (int k = 0; k < 3; ++k) {
+    e.val[k] = a[k][k] * fscale;
+    const double nrm = 1.0 / std::sqrt(v[0][k] * v[0][k] + v[1][k] * v[1][k] + v[2][k] * v[2][k]);
+    for (int r = 0; r < 3; ++r) e.vec[r][k] = v[r][k] * nrm;
+  }
+  return e;
+}
+// diag(d) rotated back to the frame of the eigenvectors (rotationalTransform).
+static ST fromEigen(const double d[3], const double V[3][3]) {
+  ST r;
+  auto el = [&](int i, int j) { return V[i][0] * d[0] * V[j][0] + V[i][1] * d[1] * V[j][1] + V[i][2] * d[2] * V[j][2]; };
+  r.xx = el(0, 0); r.xy = el(0, 1); r.xz = el(0, 2); r.yy = el(1, 1); r.yz = el(1, 2); r.zz = el(2, 2);
+  return r;
+}
+// enforceMinEigenValue / enforceMaxEigenValue (GeomSymmetricTensorInline.hh:2578-2640):
+// the tensor is returned unchanged when no eigenvalue needs the bound.
+static ST enforceMinEig(const ST& H, double x) {
+  const EigS e = eigenVectorsS(H);
+  if (std::min(e.val[0], std::min(e.val[1], e.val[2])) >= x) return H;
+  const double d[3] = {std::max(e.val[0], x), std::max(e.val[1], x), std::max(e.val[2], x)};
+  return fromEigen(d, e.vec);
+}
+static ST enforceMaxEig(const ST& H, double x) {
+  const EigS e = eigenVectorsS(H);
+  if (std::max(e.val[0], std::max(e.val[1], e.val[2])) <= x) return H;
+  const double d[3] = {std::min(e.val[0], x), std::min(e.val[1], x), std::min(e.val[2], x)};
+  return fromEigen(d, e.vec);
+}
+// GeomSymmetricTensor::sqrt (GeomSymmetricTensorInline.hh:2497-2510)
+static ST sqrtS(const ST& H) {
+  const EigS e = eigenVectorsS(H);
+  const double d[3] = {std::sqrt(std::max(0.0, e.val[0])), std::sqrt(std::max(0.0, e.val[1])),
+                       std::sqrt(std::max(0.0, e.val[2]))};
+  return fromEigen(d, e.vec);
+}
+// Tensor DH/Dt of ASPH (SmoothingScaleUtilities.hh, smoothingScaleDerivative
+// for Dim<3>): the rate of H under the velocity gradient with the rotation of
+// the frame taken out.
+static ST smoothingScaleDerivative3(const ST& H, const T9& D) {
+  const double AA = H.xx * D.xy - H.xy * (D.xx - D.yy) + H.xz * D.zy - H.yy * D.yx - H.yz * D.zx;
+  const double BB = H.xx * D.xz + H.xy * D.yz - H.xz * (D.xx - D.zz) - H.yz * D.yx - H.zz * D.zx;
+  const double CC = H.xy * D.xz + H.yy * D.yz - H.yz * (D.yy - D.zz) - H.xz * D.xy - H.zz * D.zy;
+  const double thpt = H.yy + H.zz;
+  const double Ga = (H.xx + H.yy) * thpt - H.xz * H.xz;
+  const double Gb = (H.yy + H.zz) * H.yz + H.xy * H.xz;
+  const double Gc = (H.xx + H.zz) * thpt - H.xy * H.xy;
+  const double Gd = thpt * AA + H.xz * CC;
+  const double Ge = thpt * BB - H.xy * CC;
+  const double ack = 1.0 / (Ga * Gc - Gb * Gb);
+  const double Gdot = (Gc * Gd - Gb * Ge) * ack;
+  const double Tdot = (Gb * Gd - Ga * Ge) * ack;
+  const double Phidot = (H.xz * Gdot + H.xy * Tdot + CC) / thpt;
+  ST r;
+  r.xx = -H.xx * D.xx + H.xy * (Gdot - D.yx) - H.xz * (Tdot + D.zx);
+  r.xy = H.yy * Gdot - H.yz * Tdot - H.xx * D.xy - H.xy * D.yy - H.xz * D.zy;
+  r.xz = H.yz * Gdot - H.zz * Tdot - H.xx * D.xz - H.xy * D.yz - H.xz * D.zz;
+  r.yy = H.yz * (Phidot - D.zy) - H.xy * (Gdot + D.xy) - H.yy * D.yy;
+  r.yz = H.xy * Tdot - H.yy * Phidot - H.xz * D.xy - H.yz * D.yy - H.zz * D.zy;
+  r.zz = H.xz * (Tdot - D.xz) - H.yz * (Phidot + D.yz) - H.zz * D.zz;
+  return r;
+}
+
+//------------------------------------------------------------------------------
 // Cubic B-spline (3-D), BSplineKernelInline.hh:28-93.
 //------------------------------------------------------------------------------
 struct BSpline3 {
@@ -371,6 +488,7 @@ struct TableKernel {
 //------------------------------------------------------------------------------
 struct NodeListParams {
   double nPerh = 1.51, hmin = 1e-20, hmax = 1e20, rhoMin = 1e-10, rhoMax = 1e10, gamma = 5.0 / 3.0;
+  double hminratio = 0.1;   // NodeList::hminratio (FluidNodeList default 0.1)
   double minP = -std::numeric_limits<double>::max(), maxP = std::numeric_limits<double>::max();
 };
 
@@ -400,6 +518,9 @@ struct Config {
   // 0 MonaghanGingoldViscosity, 1 LimitedMonaghanGingoldViscosity
   int viscosity = 0;
   double etaCritFrac = 1.0, etaFoldFrac = 0.2;
+  // 0 SPHSmoothingScale, 1 ASPHClassicSmoothingScale (SPHHydros.py:130-138, ASPH="CLASSIC")
+  int smoothingScale = 0;
+  int fixShape = 0;          // ASPHClassicSmoothingScale fixShape
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
   double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
@@ -447,7 +568,7 @@ struct Problem {
   vector<double> rhoSum, normalization, DrhoDt, DepsDt, maxQ, effQ, XSPHWeightSum, massZeroth, DepsDtCompat;
   vector<V3> DxDt, DvDt, gradRho, XSPHDeltaV, massFirst, DvDtGrav;
   vector<T9> DvDx, localDvDx, M, localM;
-  vector<ST> DHDt, Hideal;
+  vector<ST> DHDt, Hideal, massSecond;
   // ArtificialViscosityVelocityGradient: the Q's copy of DvDx, a state field
   // (ArtificialViscosityHandle.cc:52,78-79; zero until the first copy)
   vector<T9> DvDxQ;
@@ -469,7 +590,7 @@ struct Problem {
     if ((int)rhoSum.size() != nInt) {
       z(rhoSum); z(normalization); z(DrhoDt); z(DepsDt); z(maxQ); z(effQ); z(XSPHWeightSum); z(massZeroth); z(DepsDtCompat);
       zv(DxDt); zv(DvDt); zv(gradRho); zv(XSPHDeltaV); zv(massFirst); zv(DvDtGrav);
-      zt(DvDx); zt(localDvDx); zt(M); zt(localM); zs(DHDt); zs(Hideal); z(potential);
+      zt(DvDx); zt(localDvDx); zt(M); zt(localM); zs(DHDt); zs(Hideal); zs(massSecond); z(potential);
     }
   }
   // Resize derivative arrays to nTot, preserving internal values (ghost
@@ -482,7 +603,8 @@ struct Problem {
     keepResize(DxDt, nInt, nTot); keepResize(DvDt, nInt, nTot); keepResize(gradRho, nInt, nTot);
     keepResize(XSPHDeltaV, nInt, nTot); keepResize(massFirst, nInt, nTot); keepResize(DvDtGrav, nInt, nTot);
     keepResize(DvDx, nInt, nTot); keepResize(localDvDx, nInt, nTot); keepResize(M, nInt, nTot); keepResize(localM, nInt, nTot);
-    keepResize(DHDt, nInt, nTot); keepResize(Hideal, nInt, nTot); keepResize(potential, nInt, nTot);
+    keepResize(DHDt, nInt, nTot); keepResize(Hideal, nInt, nTot); keepResize(massSecond, nInt, nTot);
+    keepResize(potential, nInt, nTot);
     if ((int)DvDxQ.size() < nInt) DvDxQ.assign(nInt, T9{});
     DvDxQ.resize(nTot);
   }
@@ -786,9 +908,10 @@ struct Problem {
     double rhoSum = 0, norm = 0, DepsDt = 0, maxQ = 0, effQ = 0, xsphW = 0, m0 = 0;
     V3 DvDt, gradRho, xsphDV, m1;
     T9 DvDx, localDvDx, M, localM;
+    ST m2;
     PairAcc& operator+=(const PairAcc& o) {
       rhoSum += o.rhoSum; norm += o.norm; DepsDt += o.DepsDt; maxQ = std::max(maxQ, o.maxQ); effQ += o.effQ;
-      xsphW += o.xsphW; m0 += o.m0;
+      xsphW += o.xsphW; m0 += o.m0; addS(m2, o.m2);
       DvDt = add(DvDt, o.DvDt); gradRho = add(gradRho, o.gradRho); xsphDV = add(xsphDV, o.xsphDV); m1 = add(m1, o.m1);
       addT(DvDx, o.DvDx); addT(localDvDx, o.localDvDx); addT(M, o.M); addT(localM, o.localM);
       return *this;
@@ -906,6 +1029,16 @@ struct Problem {
       const double WSPHi = W.kernelValueSPH(etaMagi), WSPHj = W.kernelValueSPH(etaMagj);
       ai.m0 += fweightij * WSPHi; aj.m0 += 1.0 / fweightij * WSPHj;
       ai.m1 = sub(ai.m1, mul(fweightij * WSPHi, etai)); aj.m1 = add(aj.m1, mul(1.0 / fweightij * WSPHj, etaj));
+      if (cfg.smoothingScale == 1) {
+        // ASPHClassicSmoothingScale second moment (ASPHClassicSmoothingScale.cc:167-176):
+        // xij xij / |xij|^5 weighted by WSPH^2
+        const double rm = mag(rij);
+        const double f5 = safeInvVar(rm * rm * rm * rm * rm);
+        const ST xd{rij.x * rij.x * f5, rij.x * rij.y * f5, rij.x * rij.z * f5,
+                    rij.y * rij.y * f5, rij.y * rij.z * f5, rij.z * rij.z * f5};
+        addS(ai.m2, scaleS(fweightij * WSPHi * WSPHi, xd));
+        addS(aj.m2, scaleS(1.0 / fweightij * WSPHj * WSPHj, xd));
+      }
     });
     // SPH finalize, SPH.cc:480-552
     for (int i = 0; i < nInt; ++i) {
@@ -940,6 +1073,7 @@ struct Problem {
       } else {
         DxDt[i] = vi;
       }
+      if (cfg.smoothingScale == 1) { asphClassicFinalize(i, a, DvDxi); continue; }
       // SPHSmoothingScale finalize
       const auto& L = lists[list[i]];
       double m0 = rootnu3(std::max(0.0, a.m0));
@@ -955,6 +1089,49 @@ struct Problem {
       const double hinv = 1.0 / hi1;
       Hideal[i] = ST{hinv * 1.0, hinv * 0.0, hinv * 0.0, hinv * 1.0, hinv * 0.0, hinv * 1.0};
     }
+  }
+
+  // ASPHClassicSmoothingScale::evaluateDerivatives, the node part
+  // (ASPHClassicSmoothingScale.cc:180-291): DHDt from the tensor rate; the
+  // shape of Hideal from the normalised second moment of the neighbour
+  // distribution (eigenvalues floored at hminratio of the largest), its size
+  // from the zeroth moment as in the SPH IdealH, then the eigenvalues bounded
+  // by 1/hmax and min(1/hmin, max(1/hmax, smallest)/hminratio).
+  void asphClassicFinalize(int i, const PairAcc& a, const T9& DvDxi) {
+    const auto& L = lists[list[i]];
+    const double tiny = 1.0e-50;
+    const ST Hi = H[i];
+    DHDt[i] = smoothingScaleDerivative3(Hi, DvDxi);
+    const double m0 = rootnu3(std::max(0.0, a.m0));
+    massZeroth[i] = m0; massFirst[i] = a.m1; massSecond[i] = a.m2;
+    const double cur = fuzzyEqual(m0, 0.0) ? 0.5 * L.nPerh : W.equivalentNodesPerSmoothingScale(m0);
+    const double s = std::min(4.0, std::max(0.25, L.nPerh / cur));
+    const double psiweight = std::max(0.0, std::min(1.0, 2.0 / s - 1.0));
+    const ST& M2 = a.m2;
+    ST Hid;
+    if (psiweight > 0.0 && detS(M2) > 0.0 && minElem(eigenValuesS(M2)) > 0.0) {
+      ST psi = divS(M2, maxAbsS(M2));
+      if (detS(psi) > 1.0e-10) psi = divS(psi, rootnu3(std::fabs(detS(psi)) + tiny));
+      else psi = identityS();
+      EigS pe = eigenVectorsS(psi);
+      for (int k = 0; k < 3; ++k) pe.val[k] = 1.0 / std::sqrt(pe.val[k]);
+      const double psimin = std::max(pe.val[0], std::max(pe.val[1], pe.val[2])) * L.hminratio;
+      const double d[3] = {std::max(psimin, pe.val[0]), std::max(psimin, pe.val[1]), std::max(psimin, pe.val[2])};
+      psi = fromEigen(d, pe.vec);
+      psi = divS(psi, rootnu3(detS(psi) + tiny));
+      Hid = inverseS(sqrtS(psi));
+    } else {
+      Hid = identityS();
+    }
+    const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s + tiny));
+    if (cfg.fixShape) Hid = divS(Hi, 1.0 - aa + aa * s);
+    else Hid = scaleS(Hid, rootnu3(detS(Hi)) / (1.0 - aa + aa * s));
+    const EigS he = eigenVectorsS(Hid);
+    const double hminInv = safeInvVar(L.hmin), hmaxInv = safeInvVar(L.hmax);
+    const double hminEffInv = std::min(hminInv, std::max(hmaxInv, std::min(he.val[0], std::min(he.val[1], he.val[2]))) / L.hminratio);
+    double d[3];
+    for (int k = 0; k < 3; ++k) d[k] = std::max(hmaxInv, std::min(hminEffInv, he.val[k]));
+    Hideal[i] = fromEigen(d, he.vec);
   }
 
   // SPHBase::finalizeDerivatives: ghost values of DvDt and DepsDt.
@@ -1042,14 +1219,16 @@ struct Problem {
   // update from state0 (CheapSynchronousRK2.cc:105-110).
   //----------------------------------------------------------------------------
   static ST clampH(const ST& h, double minv, double maxv) {
-    // min(maxv, max(minv, H)) on the eigenvalues; exact for isotropic H.
+    // min(maxv, max(minv, H)): SymTensor min/max with a scalar bound the
+    // eigenvalues (GeomSymmetricTensorInline.hh:2745-2772); the isotropic
+    // case in closed form.
     if (isIsotropic(h)) {
       double a = h.xx;
       if (a < minv) a = minv;
       if (a > maxv) a = maxv;
       return ST{a, 0.0, 0.0, a, 0.0, a};
     }
-    return h;   // anisotropic H is not exercised on this path
+    return enforceMaxEig(enforceMinEig(h, minv), maxv);
   }
   void stateUpdate(double multiplier, bool midStep) {
     // specific thermal energy
@@ -1338,6 +1517,7 @@ struct orc_config {
   double G, softening, opening, ftimestep;
   int viscosity;
   double eta_crit_frac, eta_fold_frac;
+  int smoothing_scale, fix_shape;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1351,6 +1531,7 @@ void* orc_create(const orc_config* c) {
   g.quadraticInExpansion = c->quadratic_in_expansion; g.dtMin = c->dt_min; g.dtMax = c->dt_max; g.dtGrowth = c->dt_growth;
   g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
   g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
+  g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;
@@ -1363,6 +1544,31 @@ int orc_set_nodelist(void* h, int L, double nPerh, double hmin, double hmax, dou
   if ((int)p->lists.size() <= L) p->lists.resize(L + 1);
   auto& n = p->lists[L];
   n.nPerh = nPerh; n.hmin = hmin; n.hmax = hmax; n.rhoMin = rhoMin; n.rhoMax = rhoMax; n.gamma = gamma;
+  return 0;
+}
+int orc_set_nodelist_hminratio(void* h, int L, double hminratio) {
+  auto* p = static_cast<Problem*>(h);
+  if (L < 0) return 1;
+  if ((int)p->lists.size() <= L) p->lists.resize(L + 1);
+  p->lists[L].hminratio = hminratio;
+  return 0;
+}
+// Eigen-pairs of a symmetric tensor (xx, xy, xz, yy, yz, zz): vals[3],
+// vecs[9] row-major with eigenvector k in column k.
+int orc_sym_eigen(const double* a, double* vals, double* vecs) {
+  const orc::ST t{a[0], a[1], a[2], a[3], a[4], a[5]};
+  const orc::EigS e = orc::eigenVectorsS(t);
+  for (int k = 0; k < 3; ++k) vals[k] = e.val[k];
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) vecs[3 * r + k] = e.vec[r][k];
+  return 0;
+}
+// The ASPH tensor DH/Dt for one (H, DvDx).
+int orc_smoothing_scale_derivative(const double* h, const double* d, double* out) {
+  const orc::ST H{h[0], h[1], h[2], h[3], h[4], h[5]};
+  const orc::T9 D{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]};
+  const orc::ST r = orc::smoothingScaleDerivative3(H, D);
+  out[0] = r.xx; out[1] = r.xy; out[2] = r.xz; out[3] = r.yy; out[4] = r.yz; out[5] = r.zz;
   return 0;
 }
 // type 0 periodic (lo, hi); type 1 reflecting wall at lo (wall_high=0) or hi (wall_high=1)
@@ -1492,6 +1698,7 @@ int orc_get_field(void* h, const char* name, double* out) {
   if (s == "XSPHDeltaV") return v3(p->XSPHDeltaV);
   if (s == "DHDt") return s6(p->DHDt);
   if (s == "Hideal") return s6(p->Hideal);
+  if (s == "massSecondMoment") return s6(p->massSecond);
   if (s == "massZerothMoment") return sc(p->massZeroth);
   if (s == "massFirstMoment") return v3(p->massFirst);
   if (s == "DvDtGravity") return v3(p->DvDtGrav);

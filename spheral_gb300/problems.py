@@ -60,6 +60,7 @@ class Problem:
         p = Problem(self.name, self.pos.copy(), self.vel.copy(), self.mass.copy(), self.rho.copy(), self.eps.copy(),
                     1.0 / self.H[:, 0], self.nodelist.copy(), [dict(d) for d in self.nodelists],
                     [dict(b) for b in self.boundaries], dict(self.config), dict(self.meta))
+        p.H = self.H.copy()
         return p
 
 
@@ -268,3 +269,58 @@ def random_box(n_side=12, seed=11, nPerh=1.51, jitter=0.2, vel_scale=0.3, bounda
         nls.append(dict(nPerh=nPerh, hmin=1e-6, hmax=0.5, rhoMin=1e-10, rhoMax=1e10, gamma=1.4))
     return Problem("random_box", pos, vel, mass, rho, eps, h, nodelist, nls, bcs, cfg,
                    meta=dict(n_side=n_side, seed=seed, boundaries=boundaries))
+
+
+def stretched_box(nx=24, ny=18, nz=14, seed=13, nPerh=1.51, jitter=0.15, vel_scale=0.3, tilt=0.15,
+                  boundaries="periodic", hminratio=0.1, fix_shape=False):
+    """Anisotropic test box for the ASPH smoothing scale: a jittered
+    nx x ny x nz lattice in the unit cube (different spacing per axis), with
+    H = R diag(1/(nPerh dx), 1/(nPerh dy), 1/(nPerh dz)) R^T rotated per node
+    by small random angles (up to ``tilt`` radians) so H carries off-diagonal
+    terms, random velocities and energies.  Package settings select
+    ASPHClassicSmoothingScale.  boundaries: 'periodic' or 'reflecting'
+    (walls on x, periodic y z)."""
+    rng = np.random.default_rng(seed)
+    d = np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+    pos = _lattice(nx, ny, nz, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    n = len(pos)
+    pos = pos + rng.normal(0.0, 1.0, pos.shape) * (jitter * d)
+    if boundaries == "periodic":
+        pos = np.mod(pos, 1.0)
+        bcs = periodic_box_boundaries()
+    else:
+        pos[:, 0] = np.clip(pos[:, 0], 1e-9, 1.0 - 1e-9)
+        pos[:, 1:] = np.mod(pos[:, 1:], 1.0)
+        bcs = [dict(type=1, axis=0, lo=0.0, hi=1.0, wall_high=0), dict(type=1, axis=0, lo=0.0, hi=1.0, wall_high=1),
+               dict(type=0, axis=1, lo=0.0, hi=1.0), dict(type=0, axis=2, lo=0.0, hi=1.0)]
+    vol = d.prod()
+    mass = vol * (1.0 + 0.1 * rng.uniform(-1.0, 1.0, n))
+    rho = 1.0 + 0.05 * rng.uniform(-1.0, 1.0, n)
+    eps = 1.5 + 0.3 * rng.uniform(-1.0, 1.0, n)
+    vel = rng.normal(0.0, vel_scale, (n, 3))
+    cfg = dict(cfl=0.25, compatible_energy=True, gradh_correction=True, xsph=False, correct_velocity_gradient=True,
+               Cl=1.0, Cq=1.0, dt_min=0.0, dt_max=0.1, dt_growth=2.0, last_dt=1.0e-3,
+               smoothing_scale="asph_classic", fix_shape=bool(fix_shape))
+    nls = [dict(nPerh=nPerh, hmin=1e-6, hmax=0.5, rhoMin=1e-10, rhoMax=1e10, gamma=GAMMA, hminratio=hminratio)]
+    p = Problem("stretched_box", pos, vel, mass, rho, eps, np.full(n, nPerh * d.max()), None, nls, bcs, cfg,
+                meta=dict(nx=nx, ny=ny, nz=nz, seed=seed, boundaries=boundaries))
+    # per-node rotation R = Rz(c) Ry(b) Rx(a) of the principal axes
+    ang = rng.uniform(-tilt, tilt, (n, 3))
+    ca, sa = np.cos(ang[:, 0]), np.sin(ang[:, 0])
+    cb, sb = np.cos(ang[:, 1]), np.sin(ang[:, 1])
+    cc, sc = np.cos(ang[:, 2]), np.sin(ang[:, 2])
+    R = np.zeros((n, 3, 3))
+    R[:, 0, 0] = cc * cb
+    R[:, 0, 1] = cc * sb * sa - sc * ca
+    R[:, 0, 2] = cc * sb * ca + sc * sa
+    R[:, 1, 0] = sc * cb
+    R[:, 1, 1] = sc * sb * sa + cc * ca
+    R[:, 1, 2] = sc * sb * ca - cc * sa
+    R[:, 2, 0] = -sb
+    R[:, 2, 1] = cb * sa
+    R[:, 2, 2] = cb * ca
+    lam = 1.0 / (nPerh * d) * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, (n, 3)))
+    Hm = np.einsum("nik,nk,njk->nij", R, lam, R)
+    p.H = np.ascontiguousarray(np.stack([Hm[:, 0, 0], Hm[:, 0, 1], Hm[:, 0, 2], Hm[:, 1, 1], Hm[:, 1, 2],
+                                         Hm[:, 2, 2]], axis=1))
+    return p
