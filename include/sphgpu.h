@@ -54,6 +54,10 @@ extern "C" {
 #define SPHGPU_VISCOSITY_MONAGHAN_GINGOLD 0          /* MonaghanGingoldViscosity        */
 #define SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD 1  /* LimitedMonaghanGingoldViscosity (the SPH() factory default) */
 
+#define SPHGPU_SMOOTHING_SPH 0           /* SPHSmoothingScale: isotropic H = I/h                  */
+#define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
+                                            symmetric-tensor H; FP64 precision mode            */
+
 typedef struct sphgpu_ctx* sphgpu_handle;
 
 /* Package, artificial-viscosity, integrator and gravity settings.  Field
@@ -67,7 +71,10 @@ typedef struct sphgpu_ctx* sphgpu_handle;
  *   LimitedMonaghanGingoldViscosity(Cl, Cq, kernel, linearInExpansion,
  *     quadraticInExpansion, etaCritFrac, etaFoldFrac)
  *                                src/ArtificialViscosity/LimitedMonaghanGingoldViscosity.cc:39-53,
- *                                defaults src/PYB11/ArtificialViscosity/LimitedMonaghanGingoldViscosity.py:31-32 */
+ *                                defaults src/PYB11/ArtificialViscosity/LimitedMonaghanGingoldViscosity.py:31-32
+ *   ASPHClassicSmoothingScale(HUpdate, W, fixShape, radialOnly)
+ *                                src/SmoothingScale/ASPHClassicSmoothingScale.cc:34-46 (IdealH;
+ *                                radialOnly is not on this path) */
 typedef struct sphgpu_config {
   int num_table_points;             /* TableKernel(BSplineKernel3d(), numPoints)           */
   double cfl;
@@ -88,6 +95,8 @@ typedef struct sphgpu_config {
   int device;                       /* CUDA device ordinal                                 */
   int viscosity;                    /* SPHGPU_VISCOSITY_*                                  */
   double eta_crit_frac, eta_fold_frac;  /* limited Q: full Q below etaCritFrac/nPerh      */
+  int smoothing_scale;              /* SPHGPU_SMOOTHING_*                                  */
+  int fix_shape;                    /* ASPH fixShape: Hideal keeps the shape of H          */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,
@@ -125,6 +134,12 @@ int sphgpu_set_kernel_table(sphgpu_handle h, const double* w, const double* grad
 int sphgpu_set_nodelist(sphgpu_handle h, int nodelist, double nPerh, double hmin, double hmax,
                         double rhoMin, double rhoMax, double gamma);
 
+/* NodeList::hminratio (default 0.1): the ASPH smoothing scale keeps every
+ * eigenvalue of 1/h within 1/hminratio of the smallest.  Replaces: the
+ * hminratio argument of FluidNodeList (src/NodeList/FluidNodeLists.py:21)
+ * as read by ASPHClassicSmoothingScale.cc:219-288. */
+int sphgpu_set_nodelist_hminratio(sphgpu_handle h, int nodelist, double hminratio);
+
 /* Axis-aligned boundary.  type SPHGPU_BOUNDARY_PERIODIC: planes at lo and hi.
  * type SPHGPU_BOUNDARY_REFLECTING: one wall, at lo with normal +axis
  * (wall_high = 0) or at hi with normal -axis (wall_high = 1).
@@ -133,9 +148,11 @@ int sphgpu_set_nodelist(sphgpu_handle h, int nodelist, double nPerh, double hmin
  * whose ghost nodes become implicit periodic/mirror images. */
 int sphgpu_add_boundary(sphgpu_handle h, int type, int axis, double lo, double hi, int wall_high);
 
-/* Upload n internal nodes (host arrays, caller order).  H must be isotropic
- * (H = I/h, the form SPHSmoothingScale maintains); otherwise
- * SPHGPU_E_UNSUPPORTED.  nodelist may be NULL (all zero).
+/* Upload n internal nodes (host arrays, caller order).  H (xx xy xz yy yz zz
+ * per node) must be isotropic (H = I/h, the form SPHSmoothingScale
+ * maintains) unless the ASPH smoothing scale is selected, in which case it
+ * must be symmetric positive definite; otherwise SPHGPU_E_UNSUPPORTED /
+ * SPHGPU_E_NAN.  nodelist may be NULL (all zero).
  * Replaces: the registered state FieldLists of SPHBase::registerState
  * (src/SPH/SPHBase.cc:203-263). */
 int sphgpu_set_particles(sphgpu_handle h, long n, const double* pos, const double* vel, const double* mass,
@@ -202,7 +219,9 @@ int sphgpu_ensemble_advance(sphgpu_handle* handles, int nboxes, int nsteps, doub
  * soundSpeed omegaGradh massDensitySum normalization DxDt DvDt DrhoDt DepsDt
  * DvDx internalDvDx gradRho M localM maxViscousPressure effViscousPressure
  * XSPHWeightSum XSPHDeltaV DHDt Hideal massZerothMoment massFirstMoment
- * DvDtGravity potential DepsDtCompatible numNeighbors.
+ * DvDtGravity potential DepsDtCompatible numNeighbors
+ * ArtificialViscosityVelocityGradient (limited Q) massSecondMoment (ASPH).
+ * H, Hideal and DHDt are 6-component symmetric tensors.
  * *ncomp (may be NULL) receives the component count.
  * Replaces: State/StateDerivatives::fields(name, ...) (src/DataBase/State.hh:58-118). */
 int sphgpu_get_field(sphgpu_handle h, const char* name, double* out, int* ncomp);

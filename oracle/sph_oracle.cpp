@@ -685,8 +685,16 @@ struct Problem {
             im &= ~(3 << (2 * b.axis));
             im |= code << (2 * b.axis);
             image.push_back(im);
-            // position: mapPosition(pos(control), mExitPlane, mEnterPlane)
+            // position: mapPosition(pos(control), mExitPlane, mEnterPlane);
+            // H: applyGhostBoundary(Hfield) (PlanarBoundary::updateGhostNodes,
+            // PlanarBoundary.cc:291-327), reflected through a wall
             comp(pos[g], b.axis) = mapCoord(compc(pos[c], b.axis), wEx, sEx, wEn, sEn);
+            if (b.type == 1) {
+              ST& h = H[g];
+              if (b.axis == 0) { h.xy = -h.xy; h.xz = -h.xz; }
+              else if (b.axis == 1) { h.xy = -h.xy; h.yz = -h.yz; }
+              else { h.xz = -h.xz; h.yz = -h.yz; }
+            }
             b.control[sub].push_back(c);
             b.ghost[sub].push_back(g);
           }
@@ -1268,7 +1276,14 @@ struct Problem {
           const double sd = (p - wEn) * sEn;            // vec < plane: compare() == 1
           if (sd < 0.0 && !orc::fuzzyEqual(sd, 0.0)) {
             comp(pos[i], b.axis) = mapCoord(p, wEn, sEn, wEx, sEx);
-            if (b.type == 1) comp(vel[i], b.axis) = -compc(vel[i], b.axis);
+            if (b.type == 1) {
+              comp(vel[i], b.axis) = -compc(vel[i], b.axis);
+              // PlanarBoundary::updateViolationNodes: H -> (R H R).Symmetric()
+              ST& h = H[i];
+              if (b.axis == 0) { h.xy = -h.xy; h.xz = -h.xz; }
+              else if (b.axis == 1) { h.xy = -h.xy; h.yz = -h.yz; }
+              else { h.xz = -h.xz; h.yz = -h.yz; }
+            }
           }
         }
       }

@@ -59,6 +59,8 @@ class Config(ctypes.Structure):
         ("viscosity", ctypes.c_int),
         ("eta_crit_frac", ctypes.c_double),
         ("eta_fold_frac", ctypes.c_double),
+        ("smoothing_scale", ctypes.c_int),
+        ("fix_shape", ctypes.c_int),
     ]
 
 
@@ -81,6 +83,7 @@ SIGNATURES = {
     "sphgpu_build_bspline_table": (_i, [_i, _dp, _dp, _dp, _dp, _dp, _dp]),
     "sphgpu_set_kernel_table": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "sphgpu_set_nodelist": (_i, [_vp, _i, _d, _d, _d, _d, _d, _d]),
+    "sphgpu_set_nodelist_hminratio": (_i, [_vp, _i, _d]),
     "sphgpu_add_boundary": (_i, [_vp, _i, _i, _d, _d, _i]),
     "sphgpu_set_particles": (_i, [_vp, _l, _dp, _dp, _dp, _dp, _dp, _dp, _ip]),
     "sphgpu_initialize": (_i, [_vp]),

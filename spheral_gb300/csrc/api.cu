@@ -301,6 +301,8 @@ void refreshParams(sphgpu_ctx* c) {
   hp.limitedQ = g.viscosity == SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD ? 1 : 0;
   hp.etaCrit = g.eta_crit_frac / c->lists[0].nPerh;
   hp.etaFold = g.eta_fold_frac / c->lists[0].nPerh;
+  hp.asph = g.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? 1 : 0;
+  hp.fixShape = g.fix_shape ? 1 : 0;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -336,7 +338,9 @@ void buildGrid(sphgpu_ctx* c) {
   const double minHinv = bnd[0];
   if (!(minHinv > 0.0) || !std::isfinite(minHinv)) throw Error(SPHGPU_E_NAN, "non-positive or non-finite H");
   const double hmax = 1.0 / minHinv;
-  const double support = c->hp.extent * hmax * (1.0 + 1.0e-9);
+  // tensor H: the smallest eigenvalue comes from the closed form, good to
+  // ~1e-8 relative near degenerate pairs; the margin covers it
+  const double support = c->hp.extent * hmax * (1.0 + (c->hp.asph ? 1.0e-6 : 1.0e-9));
   Grid g{};
   for (int a = 0; a < 3; ++a) {
     g.kindLo[a] = g.kindHi[a] = AXIS_OPEN;
@@ -401,8 +405,8 @@ void writeLists(sphgpu_ctx* c) {
   Scope sc(c->prof, "neighbors");
   launchNeighborsWarp(c->F, c->f32(), c->n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
                       c->itemWidth, c->grid, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
-                      maxCountPtr(c), c->nbr.as<uint32_t>(), c->nbCap, c->hp.extent * c->hp.extent, c->stream,
-                      &c->lc);
+                      maxCountPtr(c), c->nbr.as<uint32_t>(), c->nbCap, c->hp.extent * c->hp.extent, c->hp.asph != 0,
+                      c->stream, &c->lc);
   c->check();
 }
 // CSR offsets of the lists (caller-order transfers) and their total, read
@@ -455,7 +459,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     const int nx = 1 - c->cur;
     launchPermute(c->F, c->Falt, v, c->orig[c->cur].as<int>(), c->orig[nx].as<int>(), c->list[c->cur].as<int>(),
                   c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n,
-                  inStep, c->stream, &c->lc);
+                  inStep, c->hp.asph != 0, c->stream, &c->lc);
     std::swap(c->bankA, c->bankB);
     std::swap(c->F, c->Falt);
     c->cur = nx;
@@ -510,7 +514,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     Scope sc(c->prof, "neighbor_count");
     launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
                         c->itemWidth, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
-                        nullptr, 0, c->hp.extent * c->hp.extent, c->stream, &c->lc);
+                        nullptr, 0, c->hp.extent * c->hp.extent, c->hp.asph != 0, c->stream, &c->lc);
     c->check();
     c->nbCap = capFor(readMaxCount(c));
   }
@@ -749,7 +753,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   const double hdt = 0.5 * dt;
   {
     Scope sc(c->prof, "update");
-    launchSaveState0(c->F, c->n, c->stream, &c->lc);
+    launchSaveState0(c->F, c->n, c->hp.asph != 0, c->stream, &c->lc);
     const Fields32 m32 = c->f32();
     launchUpdate(c->F, c->listp(), c->n, c->hp, hdt, true, c->cfg.gravity != 0, c->fp32() ? &m32 : nullptr, c->grid,
                  c->stream, &c->lc);
@@ -761,7 +765,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
   {
     Scope sc(c->prof, "update");
-    launchRestoreState0(c->F, c->n, c->stream, &c->lc);
+    launchRestoreState0(c->F, c->n, c->hp.asph != 0, c->stream, &c->lc);
   }
   if (c->cfg.compatible_energy) {
     Scope sc(c->prof, "energy");
@@ -785,7 +789,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
   {
     Scope sc(c->prof, "enforce");
-    launchEnforce(c->F, c->n, c->grid, c->stream, &c->lc);
+    launchEnforce(c->F, c->n, c->grid, c->hp.asph != 0, c->stream, &c->lc);
   }
   c->check();
   checkState(c, "the step");
@@ -798,7 +802,8 @@ struct FieldSpec {
   int first;
   int ncomp;
 };
-bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb) {
+// asph: H, Hideal and DHDt are the tensor fields (and massSecondMoment exists).
+bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb, bool asph) {
   isH = false;
   isNumNb = false;
   static const std::map<std::string, FieldSpec> m = {
@@ -812,6 +817,10 @@ bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb) {
       {"massZerothMoment", {F_M0, 1}}, {"massFirstMoment", {F_M1_X, 3}}, {"DvDtGravity", {F_GRAV_X, 3}},
       {"potential", {F_POT, 1}}, {"DepsDtCompatible", {F_DEPS_COMPAT, 1}},
       {"ArtificialViscosityVelocityGradient", {F_DVDXQ_XX, 9}}};
+  if (asph && (s == "H" || s == "Hideal" || s == "DHDt" || s == "massSecondMoment")) {
+    fs = {s == "H" ? F_HT_XX : (s == "Hideal" ? F_HIDEALT_XX : (s == "DHDt" ? F_DHDTT_XX : F_M2_XX)), 6};
+    return true;
+  }
   if (s == "H" || s == "Hideal" || s == "DHDt") {
     isH = true;
     fs = {s == "H" ? F_HINV : (s == "Hideal" ? F_HIDEAL : F_DHDT), 6};
@@ -858,7 +867,7 @@ struct CheckpointHeader {
   int32_t version, nfields;
   int64_t n, cycle;
   double time, lastDt, dtMultiplier, dtMinAcc, extraEnergy;
-  int32_t precision, numLists, pairVariant, viscosity;
+  int32_t precision, numLists, pairVariant, viscosity, smoothingScale, fixShape;
 };
 constexpr char kCheckpointMagic[8] = {'S', 'P', 'H', 'G', 'P', 'U', 'C', 'K'};
 size_t checkpointBytes(long n) {
@@ -900,6 +909,8 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->viscosity = SPHGPU_VISCOSITY_MONAGHAN_GINGOLD;
   c->eta_crit_frac = 1.0;
   c->eta_fold_frac = 0.2;
+  c->smoothing_scale = SPHGPU_SMOOTHING_SPH;
+  c->fix_shape = 0;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -916,6 +927,10 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_ARG, "etaFoldFrac must be positive");
     if (cfg->density_update != SPHGPU_DENSITY_RIGOROUS_SUM && cfg->density_update != SPHGPU_DENSITY_INTEGRATE)
       throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
+    if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
+      throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
+    if (cfg->smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC && cfg->precision != SPHGPU_PRECISION_FP64)
+      throw Error(SPHGPU_E_UNSUPPORTED, "the ASPH smoothing scale runs in the FP64 precision mode");
     CUDA_OK(cudaSetDevice(cfg->device));
     CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->prof.s = c->stream;
@@ -923,7 +938,8 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
     CUDA_OK(cudaMallocHost(&c->hsmall, 64 * sizeof(double)));
     c->time = cfg->time;
     c->lastDt = cfg->last_dt;
-    c->lists[0] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308, 1e20, 1e-20};
+    for (int k = 0; k < kMaxNodeLists; ++k)
+      c->lists[k] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308, 1e20, 1e-20, 0.1};
     c->numLists = 0;
     if (cfg->gravity) c->grav = gravityCreate();
     // Build the default cubic B-spline table.
@@ -991,8 +1007,17 @@ int sphgpu_set_nodelist(sphgpu_handle c, int k, double nPerh, double hmin, doubl
   if (!(nPerh > 0.0) || !(hmin > 0.0) || !(hmax >= hmin) || !(gamma > 1.0))
     throw Error(SPHGPU_E_ARG, "bad nodelist parameters");
   c->lists[k] = NodeListParams{nPerh, hmin, hmax, rhoMin, rhoMax, gamma, -1.7976931348623157e308,
-                               1.7976931348623157e308, 1.0 / hmin, 1.0 / hmax};
+                               1.7976931348623157e308, 1.0 / hmin, 1.0 / hmax, c->lists[k].hminratio};
   c->numLists = std::max(c->numLists, k + 1);
+  refreshParams(c);
+  API_END(c)
+}
+
+int sphgpu_set_nodelist_hminratio(sphgpu_handle c, int k, double hminratio) {
+  API_BEGIN(c)
+  if (k < 0 || k >= kMaxNodeLists) throw Error(SPHGPU_E_ARG, "nodelist index out of range");
+  if (!(hminratio > 0.0) || hminratio > 1.0) throw Error(SPHGPU_E_ARG, "hminratio must be in (0, 1]");
+  c->lists[k].hminratio = hminratio;
   refreshParams(c);
   API_END(c)
 }
@@ -1016,11 +1041,20 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   if (n <= 0 || n >= kMaxNodes) throw Error(SPHGPU_E_ARG, "particle count out of range");
   if (!pos || !vel || !mass || !rho || !eps || !H) throw Error(SPHGPU_E_ARG, "null particle array");
   if (c->numLists == 0) c->numLists = 1;
+  const bool asph = c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC;
   for (long i = 0; i < n; ++i) {
     const double* h = H + 6 * i;
-    if (h[1] != 0.0 || h[2] != 0.0 || h[4] != 0.0 || h[0] != h[3] || h[0] != h[5])
-      throw Error(SPHGPU_E_UNSUPPORTED, "H must be isotropic (H = I/h) on node " + std::to_string(i));
-    if (!(h[0] > 0.0)) throw Error(SPHGPU_E_NAN, "non-positive H on node " + std::to_string(i));
+    if (asph) {   // symmetric positive definite: leading minors positive (Sylvester)
+      const double m2 = h[0] * h[3] - h[1] * h[1];
+      const double m3 = h[0] * (h[3] * h[5] - h[4] * h[4]) - h[1] * (h[1] * h[5] - h[4] * h[2]) +
+                        h[2] * (h[1] * h[4] - h[3] * h[2]);
+      if (!(h[0] > 0.0) || !(m2 > 0.0) || !(m3 > 0.0))
+        throw Error(SPHGPU_E_NAN, "H not positive definite on node " + std::to_string(i));
+    } else {
+      if (h[1] != 0.0 || h[2] != 0.0 || h[4] != 0.0 || h[0] != h[3] || h[0] != h[5])
+        throw Error(SPHGPU_E_UNSUPPORTED, "H must be isotropic (H = I/h) on node " + std::to_string(i));
+      if (!(h[0] > 0.0)) throw Error(SPHGPU_E_NAN, "non-positive H on node " + std::to_string(i));
+    }
     if (nodelist && (nodelist[i] < 0 || nodelist[i] >= c->numLists))
       throw Error(SPHGPU_E_ARG, "nodelist id out of range on node " + std::to_string(i));
   }
@@ -1040,7 +1074,13 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   up(F_MASS, mass, 1, 0);
   up(F_RHO, rho, 1, 0);
   up(F_EPS, eps, 1, 0);
-  up(F_HINV, H, 6, 0);
+  if (asph) {
+    for (int k = 0; k < 6; ++k) up(F_HT_XX + k, H, 6, k);
+    launchTensorExtent(c->F, n, c->stream, &c->lc);
+    c->check();
+  } else {
+    up(F_HINV, H, 6, 0);
+  }
   for (long i = 0; i < n; ++i) tmp[i] = 1.0;
   CUDA_OK(cudaMemcpyAsync(c->F.f[F_OMEGA], tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
@@ -1077,7 +1117,7 @@ int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
   const long n = c->n;
   CheckpointHeader h{};
   std::memcpy(h.magic, kCheckpointMagic, 8);
-  h.version = 1;
+  h.version = 2;
   h.nfields = F_NUM_PERMUTED;
   h.n = n;
   h.cycle = c->cycle;
@@ -1090,6 +1130,8 @@ int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
   h.numLists = c->numLists;
   h.pairVariant = c->pairVariant;
   h.viscosity = c->cfg.viscosity;
+  h.smoothingScale = c->cfg.smoothing_scale;
+  h.fixShape = c->cfg.fix_shape;
   char* out = static_cast<char*>(buffer);
   std::memcpy(out, &h, sizeof(h));
   out += sizeof(h);
@@ -1108,12 +1150,13 @@ int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
   if (!buffer || bytes < sizeof(CheckpointHeader)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
   CheckpointHeader h;
   std::memcpy(&h, buffer, sizeof(h));
-  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1 || h.nfields != F_NUM_PERMUTED)
+  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 2 || h.nfields != F_NUM_PERMUTED)
     throw Error(SPHGPU_E_ARG, "not a checkpoint of this library version");
   if (h.n <= 0 || h.n >= kMaxNodes || bytes < checkpointBytes((long)h.n))
     throw Error(SPHGPU_E_ARG, "checkpoint size does not match its node count");
-  if (h.precision != c->cfg.precision || h.viscosity != c->cfg.viscosity)
-    throw Error(SPHGPU_E_STATE, "checkpoint written with another precision mode or viscosity");
+  if (h.precision != c->cfg.precision || h.viscosity != c->cfg.viscosity ||
+      h.smoothingScale != c->cfg.smoothing_scale || h.fixShape != c->cfg.fix_shape)
+    throw Error(SPHGPU_E_STATE, "checkpoint written with another precision mode, viscosity or smoothing scale");
   if (h.numLists > std::max(1, c->numLists))
     throw Error(SPHGPU_E_STATE, "checkpoint uses NodeLists that are not set on this handle");
   const long n = (long)h.n;
@@ -1302,7 +1345,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   if (!name) throw Error(SPHGPU_E_ARG, "null field name");
   FieldSpec fs;
   bool isH, isNb;
-  if (!fieldSpec(name, fs, isH, isNb)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
   if (fs.first == F_DVDXQ_XX && !c->hp.limitedQ)
     throw Error(SPHGPU_E_STATE, "ArtificialViscosityVelocityGradient exists only with the limited Q");
   if (ncomp) *ncomp = fs.ncomp;
@@ -1331,7 +1374,8 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   if (!name || !in) throw Error(SPHGPU_E_ARG, "null argument");
   FieldSpec fs;
   bool isH, isNb;
-  if (!fieldSpec(name, fs, isH, isNb) || isNb) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0) || isNb)
+    throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
   requireState(c);
   const long n = c->n;
   c->stage.ensure((size_t)n * fs.ncomp * sizeof(double));
@@ -1339,6 +1383,7 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   CUDA_OK(cudaMemcpyAsync(st, in, (size_t)n * fs.ncomp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   if (isH) launchScatterIn(c->F, c->origp(), st, fs.first, 1, 6, n, c->stream, &c->lc);
   else launchScatterIn(c->F, c->origp(), st, fs.first, fs.ncomp, fs.ncomp, n, c->stream, &c->lc);
+  if (fs.first == F_HT_XX) launchTensorExtent(c->F, n, c->stream, &c->lc);
   c->check();
   if (c->haveNeighbors) prepare32(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
@@ -1354,8 +1399,9 @@ int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, c
   c->stage.ensure((size_t)n * 15 * sizeof(double));
   double* st = c->stage.as<double>();
   struct Item { const double* p; int first, ncomp, stride; };
+  const bool asph = c->hp.asph != 0;
   const Item items[] = {{pos, F_X, 3, 3}, {vel, F_VX, 3, 3}, {mass, F_MASS, 1, 1}, {rho, F_RHO, 1, 1},
-                        {eps, F_EPS, 1, 1}, {H, F_HINV, 1, 6}};
+                        {eps, F_EPS, 1, 1}, {H, asph ? (int)F_HT_XX : (int)F_HINV, asph ? 6 : 1, 6}};
   size_t off = 0;
   for (const auto& it : items) {
     if (!it.p) continue;
@@ -1364,6 +1410,7 @@ int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, c
     launchScatterIn(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
     off += (size_t)n * it.stride;
   }
+  if (asph && H) launchTensorExtent(c->F, n, c->stream, &c->lc);
   c->check();
   if (c->haveNeighbors) prepare32(c);
   API_END(c)
@@ -1376,12 +1423,13 @@ int sphgpu_download_state(sphgpu_handle c, double* pos, double* vel, double* rho
   c->stage.ensure((size_t)n * 14 * sizeof(double));
   double* st = c->stage.as<double>();
   struct Item { double* p; int first, ncomp, stride; };
+  const bool asph = c->hp.asph != 0;
   const Item items[] = {{pos, F_X, 3, 3}, {vel, F_VX, 3, 3}, {rho, F_RHO, 1, 1}, {eps, F_EPS, 1, 1},
-                        {H, F_HINV, 1, 6}};
+                        {H, asph ? (int)F_HT_XX : (int)F_HINV, asph ? 6 : 1, 6}};
   size_t off = 0;
   for (const auto& it : items) {
     if (!it.p) continue;
-    if (it.first == F_HINV) launchGatherOutH(c->F, c->origp(), st + off, F_HINV, n, c->stream, &c->lc);
+    if (it.first == F_HINV && !asph) launchGatherOutH(c->F, c->origp(), st + off, F_HINV, n, c->stream, &c->lc);
     else launchGatherOut(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
     CUDA_OK(cudaMemcpyAsync(it.p, st + off, (size_t)n * it.stride * sizeof(double), cudaMemcpyDeviceToHost,
                             c->stream));

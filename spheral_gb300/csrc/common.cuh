@@ -31,6 +31,7 @@ struct Grid {
 struct NodeListParams {
   double nPerh, hmin, hmax, rhoMin, rhoMax, gamma, minP, maxP;
   double hminInv, hmaxInv;   // 1/hmin, 1/hmax (computed on the host)
+  double hminratio;          // NodeList::hminratio (ASPH eigenvalue floor)
 };
 
 struct HydroParams {
@@ -48,6 +49,8 @@ struct HydroParams {
   const NodeListParams* lists;   // device table of the NodeLists (kMaxNodeLists entries)
   int limitedQ;                  // LimitedMonaghanGingoldViscosity instead of MonaghanGingoldViscosity
   double etaCrit, etaFold;       // its full-Q distance and fold width in eta
+  int asph;                      // ASPHClassicSmoothingScale: tensor H throughout
+  int fixShape;                  // ASPH fixShape: Hideal keeps the shape of H
 };
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,

@@ -2,6 +2,7 @@
 #pragma once
 #include "kernels.cuh"
 #include <cfloat>
+#include "tensor.cuh"
 
 namespace sph {
 namespace dev {
@@ -193,15 +194,17 @@ __device__ __forceinline__ double hermiteLookup(const double* __restrict__ v, co
 struct NodeAcc {
   double rhoSum, norm, dvx, dvy, dvz, deps, gx, gy, gz, maxQ, effQ, xw, xdx, xdy, xdz, m0, m1x, m1y, m1z;
   double D[9], M[9];
+  double m2[6];   // ASPH second moment (xx xy xz yy yz zz)
 };
 
-__device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const NodeAcc& a, double mi, double rhoi,
-                                             double vxi, double vyi, double vzi, double ai, int numNb,
-                                             const HydroParams& hp, const double* __restrict__ herm) {
-  const double Hdeti = (ai * ai) * ai;
+// SPH finalize (SPH.cc:480-552): self terms, the corrected velocity gradient,
+// continuity and XSPH; D returns the final DvDx.
+__device__ __forceinline__ void finalizeHydro(Fields& F, long i, const NodeAcc& a, double mi, double rhoi,
+                                              double vxi, double vyi, double vzi, double Hdeti, int numNb,
+                                              const HydroParams& hp, double* D) {
   F.f[F_RHOSUM][i] = a.rhoSum + mi * hp.W0 * Hdeti;
   F.f[F_NORM][i] = a.norm + mi / rhoi * hp.W0 * Hdeti;
-  double D[9], Mm[9];
+  double Mm[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) { D[k] = a.D[k]; Mm[k] = a.M[k]; }
   const double detM = (Mm[0] * Mm[4] * Mm[8] + Mm[1] * Mm[5] * Mm[6] + Mm[2] * Mm[3] * Mm[7] -
@@ -254,6 +257,14 @@ __device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const No
   F.f[F_XSPHDV_X][i] = a.xdx;
   F.f[F_XSPHDV_Y][i] = a.xdy;
   F.f[F_XSPHDV_Z][i] = a.xdz;
+}
+
+__device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const NodeAcc& a, double mi, double rhoi,
+                                             double vxi, double vyi, double vzi, double ai, int numNb,
+                                             const HydroParams& hp, const double* __restrict__ herm) {
+  double D[9];
+  finalizeHydro(F, i, a, mi, rhoi, vxi, vyi, vzi, (ai * ai) * ai, numNb, hp, D);
+  const double trace = D[0] + D[4] + D[8];
   // SPHSmoothingScale finalize (SPHSmoothingScale.cc:235-270)
   const NodeListParams L = hp.lists[li];
   const double m0s = fmax(0.0, a.m0);
@@ -272,6 +283,64 @@ __device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const No
   F.f[F_HIDEAL][i] = 1.0 / hi1;
 }
 
+
+__device__ __forceinline__ double rootnu3(double x) { return (x < 0.0 ? -1.0 : 1.0) * pow(fabs(x), 0.3333333333333333); }
+
+// ASPHClassicSmoothingScale node part (ASPHClassicSmoothingScale.cc:180-291):
+// tensor DH/Dt; the shape of Hideal from the normalised second moment of the
+// neighbour distribution (eigenvalues of psi^-1/2 floored at hminratio of the
+// largest), its size from the zeroth moment as in the SPH IdealH (or, with
+// fixShape, H itself rescaled); then the eigenvalues bounded by 1/hmax and
+// min(1/hmin, max(1/hmax, smallest) / hminratio).
+__device__ __forceinline__ void finalizeNodeASPH(Fields& F, long i, int li, const NodeAcc& a, const Sym& Hi,
+                                                 double mi, double rhoi, double vxi, double vyi, double vzi,
+                                                 int numNb, const HydroParams& hp, const double* __restrict__ herm) {
+  double D[9];
+  finalizeHydro(F, i, a, mi, rhoi, vxi, vyi, vzi, symDet(Hi), numNb, hp, D);
+  const double tiny = 1.0e-50;
+  const NodeListParams L = hp.lists[li];
+  storeSym(F, F_DHDTT_XX, i, smoothingScaleDerivative(Hi, D));
+  const double m0 = rootnu3(fmax(0.0, a.m0));
+  F.f[F_M0][i] = m0;
+  F.f[F_M1_X][i] = a.m1x;
+  F.f[F_M1_Y][i] = a.m1y;
+  F.f[F_M1_Z][i] = a.m1z;
+  const Sym M2{a.m2[0], a.m2[1], a.m2[2], a.m2[3], a.m2[4], a.m2[5]};
+  storeSym(F, F_M2_XX, i, M2);
+  const bool isolated = fabs(m0) <= 1.0e-15 * fmax(1.0, fabs(m0));
+  const double cur = isolated ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(herm, hp, m0));
+  const double s = fmin(4.0, fmax(0.25, L.nPerh / cur));
+  const double psiweight = fmax(0.0, fmin(1.0, 2.0 / s - 1.0));
+  Sym Hid{1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
+  double ev[3], V[3][3], d[3];
+  symEigenValues(M2, ev);
+  if (psiweight > 0.0 && symDet(M2) > 0.0 && fmin(ev[0], fmin(ev[1], ev[2])) > 0.0) {
+    Sym psi = symDiv(M2, symMaxAbs(M2));
+    const double dp = symDet(psi);
+    if (dp > 1.0e-10) psi = symDiv(psi, rootnu3(fabs(dp) + tiny));
+    else psi = Sym{1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
+    symEigen(psi, ev, V);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ev[k] = 1.0 / sqrt(ev[k]);
+    const double psimin = fmax(ev[0], fmax(ev[1], ev[2])) * L.hminratio;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = fmax(psimin, ev[k]);
+    psi = symFromEigen(d, V);
+    psi = symDiv(psi, rootnu3(symDet(psi) + tiny));
+    symEigen(psi, ev, V);   // psi^(1/2), then its inverse
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = sqrt(fmax(0.0, ev[k]));
+    Hid = symInverse(symFromEigen(d, V));
+  }
+  const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s + tiny));
+  if (hp.fixShape) Hid = symDiv(Hi, 1.0 - aa + aa * s);
+  else Hid = symScale(Hid, rootnu3(symDet(Hi)) / (1.0 - aa + aa * s));
+  symEigen(Hid, ev, V);
+  const double hminEffInv = fmin(L.hminInv, fmax(L.hmaxInv, fmin(ev[0], fmin(ev[1], ev[2]))) / L.hminratio);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = fmax(L.hmaxInv, fmin(hminEffInv, ev[k]));
+  storeSym(F, F_HIDEALT_XX, i, symFromEigen(d, V));
+}
 
 // FP32 variant of finalizeNode for the mixed mode: the per-node completion
 // (3x3 inverse, corrected gradient, IdealH lookup) in FP32, results stored in

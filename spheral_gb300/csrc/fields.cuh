@@ -15,6 +15,13 @@ enum FieldId {
   F_DRHODT, F_DEPSDT, F_DHDT, F_MAXQ,
   F_DVDX_XX, F_DVDX_XY, F_DVDX_XZ, F_DVDX_YX, F_DVDX_YY, F_DVDX_YZ, F_DVDX_ZX, F_DVDX_ZY, F_DVDX_ZZ,
   F_GRAV_X, F_GRAV_Y, F_GRAV_Z,
+  // ASPH (tensor H) only: H as a symmetric tensor (xx xy xz yy yz zz), its
+  // tensor DH/Dt and its largest eigenvalue (the dt node scale); F_HINV then
+  // holds the smallest eigenvalue (1/h_max of the node: cell size and the
+  // conservative neighbour pre-filter).  Permuted only in ASPH mode.
+  F_HT_XX, F_HT_XY, F_HT_XZ, F_HT_YY, F_HT_YZ, F_HT_ZZ,
+  F_DHDTT_XX, F_DHDTT_XY, F_DHDTT_XZ, F_DHDTT_YY, F_DHDTT_YZ, F_DHDTT_ZZ,
+  F_HLMAX,
   F_NUM_CARRIED,
   // derivatives every evaluation rewrites (StateDerivatives of SPH,
   // SPHSmoothingScale, TreeGravity)
@@ -25,10 +32,20 @@ enum FieldId {
   // the limited Q's copy of DvDx (state field ArtificialViscosityVelocityGradient,
   // refreshed from DvDx at every postStateUpdate)
   F_DVDXQ_XX, F_DVDXQ_XY, F_DVDXQ_XZ, F_DVDXQ_YX, F_DVDXQ_YY, F_DVDXQ_YZ, F_DVDXQ_ZX, F_DVDXQ_ZY, F_DVDXQ_ZZ,
+  // ASPH only: tensor Hideal and the second moment of the neighbour distribution
+  F_HIDEALT_XX, F_HIDEALT_XY, F_HIDEALT_XZ, F_HIDEALT_YY, F_HIDEALT_YZ, F_HIDEALT_ZZ,
+  F_M2_XX, F_M2_XY, F_M2_XZ, F_M2_YY, F_M2_YZ, F_M2_ZZ,
   F_NUM_PERMUTED,
   // beginning-of-step copies (not permuted: written after the sort)
   F_X0 = F_NUM_PERMUTED, F_Y0, F_Z0, F_VX0, F_VY0, F_VZ0, F_RHO0, F_EPS0, F_HINV0,
+  F_HT0_XX, F_HT0_XY, F_HT0_XZ, F_HT0_YY, F_HT0_YZ, F_HT0_ZZ,
   F_NUM_FIELDS
+};
+
+// Fields a permute moves (indices into Fields::f), chosen on the host.
+struct FieldSel {
+  int n;
+  unsigned char id[F_NUM_PERMUTED];
 };
 
 struct Fields {

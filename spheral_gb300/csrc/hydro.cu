@@ -71,12 +71,15 @@ __global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ k
 __global__ void permuteKernel(Fields Fin, Fields Fout, const int* __restrict__ perm, const int* __restrict__ origIn,
                               int* __restrict__ origOut, const int* __restrict__ listIn, int* __restrict__ listOut,
                               const uint32_t* __restrict__ cellIn, uint32_t* __restrict__ cellOut, long n,
-                              int nfields) {
+                              FieldSel sel) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = perm[k];
 #pragma unroll 4
-  for (int f = 0; f < nfields; ++f) Fout.f[f][k] = Fin.f[f][p];
+  for (int q = 0; q < sel.n; ++q) {
+    const int f = sel.id[q];
+    Fout.f[f][k] = Fin.f[f][p];
+  }
   origOut[k] = origIn[p];
   listOut[k] = listIn[p];
   cellOut[k] = cellIn[p];
@@ -108,7 +111,10 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 // cell in sorted order, so every list has a reproducible order.
 // WRITE false: count only; true: count and write the warp-interleaved lists
 // (slots beyond cap are counted, not written).
-template <bool WRITE, int W>
+// TENSOR (ASPH): h^-1 in the FP32 mirror is the smallest eigenvalue of H, so
+// the pre-filter bounds |H r| from below and every candidate inside its band
+// takes the exact FP64 tensor test.
+template <bool WRITE, int W, bool TENSOR>
 __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
@@ -167,6 +173,8 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
+  Sym Hi{};
+  if (TENSOR && active) Hi = loadSym(F, F_HT_XX, i);
   int cnt = 0;
   // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
   uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;
@@ -221,13 +229,20 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
           const float e2 = fminf(ai2, cq.w) * r2;
           if (e2 <= bandHi) {
             bool inside = true;
-            if (e2 >= bandLo) {   // guard band: the exact FP64 criterion (rare)
+            if (TENSOR || e2 >= bandLo) {   // guard band: the exact FP64 criterion (rare)
               const int j = base + u;
               double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-              imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+              const int code = imageCode(g, hc, dcode);
+              imagePos(g, code, xjd, yjd, zjd);
               const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
                            qz = __dsub_rn(F.f[F_Z][i], zjd);
-              inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+              if (TENSOR) {
+                Sym Hj = loadSym(F, F_HT_XX, j);
+                imageSym(g, code, Hj);
+                inside = eta2ExactSym(Hi, qx, qy, qz) <= ext2 || eta2ExactSym(Hj, qx, qy, qz) <= ext2;
+              } else {
+                inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+              }
             }
             if (inside && u != self) {
               if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
@@ -266,8 +281,10 @@ __global__ void itemFillKernel(const int* __restrict__ flag, const long long* __
 //------------------------------------------------------------------------------
 // computeSPHSumMassDensity (src/SPH/computeSPHSumMassDensity.cc:15-87),
 // gathered: rho_i = m_i W(0) Hdet_i + sum_j m W(|Hj ri - Hj rj|, Hdet_j) with
-// m = m_j for the same NodeList and m_i otherwise.
+// m = m_j for the same NodeList and m_i otherwise.  TENSOR: H_j a symmetric
+// tensor (ASPH), seen through the image of the entry.
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __restrict__ list, long n, Grid g,
                                                         NeighborLists nl, TableDev t, HydroParams hp) {
   extern __shared__ double smem[];
@@ -285,7 +302,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
   const double* __restrict__ Ms = F.f[F_MASS];
   const double xi = X[i], yi = Y[i], zi = Z[i], ai = A[i], mi = Ms[i];
   const int li = list[i];
-  const double Hdeti = (ai * ai) * ai;
+  const double Hdeti = TENSOR ? symDet(loadSym(F, F_HT_XX, i)) : (ai * ai) * ai;
   const double self = mi * (Hdeti * smem[0]);
   double sum = 0.0;
   const int cnt = nl.count[i];
@@ -295,13 +312,24 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
     const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
     double xj = X[j], yj = Y[j], zj = Z[j];
     imagePos(g, code, xj, yj, zj);
-    const double aj = A[j];
-    const double dx = __dsub_rn(__dmul_rn(aj, xi), __dmul_rn(aj, xj));
-    const double dy = __dsub_rn(__dmul_rn(aj, yi), __dmul_rn(aj, yj));
-    const double dz = __dsub_rn(__dmul_rn(aj, zi), __dmul_rn(aj, zj));
+    double dx, dy, dz, Hdetj;
+    if (TENSOR) {   // |Hj ri - Hj rj|
+      Sym Hj = loadSym(F, F_HT_XX, j);
+      imageSym(g, code, Hj);
+      double ax, ay, az, bx, by, bz;
+      symDot(Hj, xi, yi, zi, ax, ay, az);
+      symDot(Hj, xj, yj, zj, bx, by, bz);
+      dx = ax - bx; dy = ay - by; dz = az - bz;
+      Hdetj = symDet(Hj);
+    } else {
+      const double aj = A[j];
+      dx = __dsub_rn(__dmul_rn(aj, xi), __dmul_rn(aj, xj));
+      dy = __dsub_rn(__dmul_rn(aj, yi), __dmul_rn(aj, yj));
+      dz = __dsub_rn(__dmul_rn(aj, zi), __dmul_rn(aj, zj));
+      Hdetj = (aj * aj) * aj;
+    }
     const double eta = sqrt(dx * dx + dy * dy + dz * dz);
     if (eta < hp.extent) {
-      const double Hdetj = (aj * aj) * aj;
       const int i0 = tableIndex(eta, hp.tableN1, hp.tableXstep);
       const double Wj = Hdetj * tableEval(smem, i0, eta);
       sum += (list[j] == li ? Ms[j] : mi) * Wj;
@@ -313,6 +341,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel(Fields F, const int* __r
 //------------------------------------------------------------------------------
 // computeSPHOmegaGradhCorrection (src/SPH/computeSPHOmegaGradhCorrection.cc:15-116).
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, NeighborLists nl, TableDev t,
                                                    HydroParams hp) {
   extern __shared__ double smem[];
@@ -327,7 +356,9 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
   const double* __restrict__ Y = F.f[F_Y];
   const double* __restrict__ Z = F.f[F_Z];
   const double xi = X[i], yi = Y[i], zi = Z[i], ai = F.f[F_HINV][i];
-  const double Hdeti = (ai * ai) * ai;
+  Sym Hi{};
+  if (TENSOR) Hi = loadSym(F, F_HT_XX, i);
+  const double Hdeti = TENSOR ? symDet(Hi) : (ai * ai) * ai;
   double wsum = 0.0, gsum = 0.0;
   const int cnt = nl.count[i];
   for (int q = 0; q < cnt; ++q) {
@@ -337,7 +368,9 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
     double xj = X[j], yj = Y[j], zj = Z[j];
     imagePos(g, code, xj, yj, zj);
     const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
-    const double ex = ai * rx, ey = ai * ry, ez = ai * rz;
+    double ex, ey, ez;
+    if (TENSOR) symDot(Hi, rx, ry, rz, ex, ey, ez);
+    else { ex = ai * rx; ey = ai * ry; ez = ai * rz; }
     const double eta = sqrt(ex * ex + ey * ey + ez * ez);
     if (eta < hp.extent) {
       const int i0 = tableIndex(eta, hp.tableN1, hp.tableXstep);
@@ -356,7 +389,9 @@ __global__ void __launch_bounds__(128) gradhKernel(Fields F, long n, Grid g, Nei
 // MonaghanGingoldViscosity::QPiij (MonaghanGingoldViscosity.cc:41-101) and the
 // SPHSmoothingScale moments + IdealH (SPHSmoothingScale.cc:154-272), FP64.
 //------------------------------------------------------------------------------
-template <bool XSPH, bool COMPAT>
+// TENSOR: ASPH -- symmetric-tensor H_i, H_j (eta = H r, grad W = gW H eta^),
+// the ASPHClassicSmoothingScale second moment and its finalize.
+template <bool XSPH, bool COMPAT, bool TENSOR>
 __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __restrict__ list, long n, Grid g,
                                                       NeighborLists nl, TableDev t, HydroParams hp,
                                                       double* __restrict__ pacc) {
@@ -386,7 +421,9 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
   const double xi = X[i], yi = Y[i], zi = Z[i], vxi = VX[i], vyi = VY[i], vzi = VZ[i];
   const double mi = Ms[i], rhoi = RHO[i], Pi = PP[i], ci = CS[i], omi = OM[i], ai = A[i];
   const int li = list[i];
-  const double Hdeti = (ai * ai) * ai;
+  Sym Hi{};
+  if (TENSOR) Hi = loadSym(F, F_HT_XX, i);
+  const double Hdeti = TENSOR ? symDet(Hi) : (ai * ai) * ai;
   const double safeOmegai = omi / (omi * omi + kTiny30);
   const double tiny = kTiny30;
   const double Clij = 0.5 * (1.0 + 1.0) * 1.0 * hp.Cl;
@@ -400,6 +437,8 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
   a.maxQ = 0.0; a.effQ = a.xw = a.xdx = a.xdy = a.xdz = a.m0 = a.m1x = a.m1y = a.m1z = 0.0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) { a.D[k] = 0.0; a.M[k] = 0.0; }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.m2[k] = 0.0;
 
   const int cnt = nl.count[i];
   for (int q = 0; q < cnt; ++q) {
@@ -411,12 +450,23 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
     imageVec(g, code, vxj, vyj, vzj);
     const double mj = Ms[j], rhoj = RHO[j], Pj = PP[j], cj = CS[j], omj = OM[j], aj = A[j];
     const int lj = list[j];
-    const double Hdetj = (aj * aj) * aj;
+    Sym Hj{};
+    if (TENSOR) {
+      Hj = loadSym(F, F_HT_XX, j);
+      imageSym(g, code, Hj);
+    }
+    const double Hdetj = TENSOR ? symDet(Hj) : (aj * aj) * aj;
     const double safeOmegaj = omj / (omj * omj + kTiny30);
 
     const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
-    const double eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
-    const double ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
+    double eix, eiy, eiz, ejx, ejy, ejz;
+    if (TENSOR) {
+      symDot(Hi, rx, ry, rz, eix, eiy, eiz);
+      symDot(Hj, rx, ry, rz, ejx, ejy, ejz);
+    } else {
+      eix = ai * rx; eiy = ai * ry; eiz = ai * rz;
+      ejx = aj * rx; ejy = aj * ry; ejz = aj * rz;
+    }
     const double etaMag2i = eix * eix + eiy * eiy + eiz * eiz;
     const double etaMag2j = ejx * ejx + ejy * ejy + ejz * ejz;
     const double etaMagi = sqrt(etaMag2i), etaMagj = sqrt(etaMag2j);
@@ -437,9 +487,18 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
     const double WSPHi = fabs(gi);
     Wi *= Hdeti; Wj *= Hdetj;
     const double gWi = Hdeti * gi, gWj = Hdetj * gj;
-    const double gHi = gWi * ai, gHj = gWj * aj;
-    const double gwix = gHi * uix, gwiy = gHi * uiy, gwiz = gHi * uiz;
-    const double gwjx = gHj * ujx, gwjy = gHj * ujy, gwjz = gHj * ujz;
+    double gwix, gwiy, gwiz, gwjx, gwjy, gwjz;
+    if (TENSOR) {   // gW H eta^
+      double hx, hy, hz;
+      symDot(Hi, uix, uiy, uiz, hx, hy, hz);
+      gwix = gWi * hx; gwiy = gWi * hy; gwiz = gWi * hz;
+      symDot(Hj, ujx, ujy, ujz, hx, hy, hz);
+      gwjx = gWj * hx; gwjy = gWj * hy; gwjz = gWj * hz;
+    } else {
+      const double gHi = gWi * ai, gHj = gWj * aj;
+      gwix = gHi * uix; gwiy = gHi * uiy; gwiz = gHi * uiz;
+      gwjx = gHj * ujx; gwjy = gHj * ujy; gwjz = gHj * ujz;
+    }
 
     if (lj == li) {
       a.rhoSum += mj * Wi;
@@ -532,8 +591,16 @@ __global__ void __launch_bounds__(128) pairKernelFP64(Fields F, const int* __res
     a.m0 += fw * WSPHi;
     const double fwW = fw * WSPHi;
     a.m1x -= fwW * eix; a.m1y -= fwW * eiy; a.m1z -= fwW * eiz;
+    if (TENSOR) {   // ASPHClassicSmoothingScale second moment: WSPH^2 r r / |r|^5
+      const double rm = sqrt(rx * rx + ry * ry + rz * rz);
+      const double f5 = 1.0 / fmax(kTiny30, rm * rm * rm * rm * rm);
+      const double w2 = fwW * WSPHi;
+      a.m2[0] += w2 * (rx * rx * f5); a.m2[1] += w2 * (rx * ry * f5); a.m2[2] += w2 * (rx * rz * f5);
+      a.m2[3] += w2 * (ry * ry * f5); a.m2[4] += w2 * (ry * rz * f5); a.m2[5] += w2 * (rz * rz * f5);
+    }
   }
-  finalizeNode(F, i, li, a, mi, rhoi, vxi, vyi, vzi, ai, cnt, hp, t.herm);
+  if (TENSOR) finalizeNodeASPH(F, i, li, a, Hi, mi, rhoi, vxi, vyi, vzi, cnt, hp, t.herm);
+  else finalizeNode(F, i, li, a, mi, rhoi, vxi, vyi, vzi, ai, cnt, hp, t.herm);
 }
 
 //------------------------------------------------------------------------------
@@ -554,7 +621,9 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
     int hc[3];
     unpackCell(nl.cell[i], hc);
     const NodeListParams L = hp.lists[list[i]];
-    const double ai = F.f[F_HINV][i];
+    // max eigenvalue of H: h^-1 when isotropic, the stored extent for tensor H
+    const double* __restrict__ HX = F.f[hp.asph ? F_HLMAX : F_HINV];
+    const double ai = HX[i];
     const double nodeScalei = 1.0 / ai / L.nPerh;
     const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
     const double rhoi = F.f[F_RHO][i];
@@ -583,7 +652,7 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
       const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
       double vxj = F.f[F_VX][j], vyj = F.f[F_VY][j], vzj = F.f[F_VZ][j];
       imageVec(g, code, vxj, vyj, vzj);
-      const double nsj = 1.0 / F.f[F_HINV][j] / maxNperh;
+      const double nsj = 1.0 / HX[j] / maxNperh;
       const double dvx = vxi - vxj, dvy = vyi - vyj, dvz = vzi - vzj;
       const double vm = sqrt(dvx * dvx + dvy * dvy + dvz * dvz);
       const double dtv = fmin(nsi, nsj) * (1.0 / fmax(tiny, vm));
@@ -680,25 +749,47 @@ __device__ __forceinline__ void eosNode(Fields& F, long i, const NodeListParams&
   F.f[F_CS][i] = sqrt(fmax(0.0, L.gamma * (L.gamma - 1.0) * eps));
 }
 
-__global__ void saveState0Kernel(Fields F, long n) {
+__global__ void saveState0Kernel(Fields F, long n, int tensor) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   F.f[F_X0][i] = F.f[F_X][i]; F.f[F_Y0][i] = F.f[F_Y][i]; F.f[F_Z0][i] = F.f[F_Z][i];
   F.f[F_VX0][i] = F.f[F_VX][i]; F.f[F_VY0][i] = F.f[F_VY][i]; F.f[F_VZ0][i] = F.f[F_VZ][i];
   F.f[F_RHO0][i] = F.f[F_RHO][i]; F.f[F_EPS0][i] = F.f[F_EPS][i]; F.f[F_HINV0][i] = F.f[F_HINV][i];
+  if (tensor)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) F.f[F_HT0_XX + k][i] = F.f[F_HT_XX + k][i];
 }
-__global__ void restoreState0Kernel(Fields F, long n) {
+__global__ void restoreState0Kernel(Fields F, long n, int tensor) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   F.f[F_X][i] = F.f[F_X0][i]; F.f[F_Y][i] = F.f[F_Y0][i]; F.f[F_Z][i] = F.f[F_Z0][i];
   F.f[F_VX][i] = F.f[F_VX0][i]; F.f[F_VY][i] = F.f[F_VY0][i]; F.f[F_VZ][i] = F.f[F_VZ0][i];
   F.f[F_RHO][i] = F.f[F_RHO0][i]; F.f[F_EPS][i] = F.f[F_EPS0][i]; F.f[F_HINV][i] = F.f[F_HINV0][i];
+  if (tensor)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) F.f[F_HT_XX + k][i] = F.f[F_HT0_XX + k][i];
+}
+
+// Extent of tensor H (ASPH): smallest eigenvalue -> F_HINV (cell size,
+// neighbour pre-filter), largest -> F_HLMAX (dt node scale).
+__device__ __forceinline__ void storeExtent(Fields& F, long i, const Sym& h) {
+  double lmin, lmax;
+  symExtent(h, lmin, lmax);
+  F.f[F_HINV][i] = lmin;
+  F.f[F_HLMAX][i] = lmax;
+}
+__global__ void tensorExtentKernel(Fields F, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  storeExtent(F, i, loadSym(F, F_HT_XX, i));
 }
 
 // P != nullptr (mixed mode): the FP32 mirrors of the new state are written
 // here as well (the prepare pass folded into the update).
+// tensor (ASPH): H is the symmetric tensor, bounded on its eigenvalues
+// (IncrementBoundedState / ReplaceBoundedState with SymTensor min/max).
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
-                             double mult, int mid, int gravity, int epsIncrement, Fields32 P, Grid g) {
+                             double mult, int mid, int gravity, int epsIncrement, int tensor, Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
@@ -724,10 +815,27 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
   const double rho = fmin(L.rhoMax, fmax(L.rhoMin, F.f[F_RHO][i] + mult * F.f[F_DRHODT][i]));
   F.f[F_RHO][i] = rho;
   const double hminInv = L.hminInv, hmaxInv = L.hmaxInv;
-  double h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
-  if (h < hmaxInv) h = hmaxInv;
-  if (h > hminInv) h = hminInv;
-  F.f[F_HINV][i] = h;
+  double h;
+  if (tensor) {
+    Sym t;
+    if (mid) {
+      t = loadSym(F, F_HT_XX, i);
+      const Sym d = loadSym(F, F_DHDTT_XX, i);
+      t = Sym{t.xx + mult * d.xx, t.xy + mult * d.xy, t.xz + mult * d.xz, t.yy + mult * d.yy, t.yz + mult * d.yz,
+              t.zz + mult * d.zz};
+    } else {
+      t = loadSym(F, F_HIDEALT_XX, i);
+    }
+    t = symBound(t, hmaxInv, hminInv);
+    storeSym(F, F_HT_XX, i, t);
+    storeExtent(F, i, t);
+    h = F.f[F_HINV][i];
+  } else {
+    h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
+    if (h < hmaxInv) h = hmaxInv;
+    if (h > hminInv) h = hminInv;
+    F.f[F_HINV][i] = h;
+  }
   if (P.posh) {
     // Mixed mode: the sound speed feeds only FP32 sweeps (Q, dt vote), so it
     // is evaluated in FP32 (an FP64 square root costs many cycles of GB300's
@@ -763,9 +871,18 @@ __global__ void eosKernel(Fields F, const int* __restrict__ list, long n, const 
 // ReflectingBoundary.cc:465-473): nodes strictly outside a plane are mapped
 // back; reflecting walls also mirror the velocity.
 __device__ __forceinline__ bool fuzzyZero(double x) { return fabs(x) <= 1.0e-15 * fmax(1.0, fabs(x)); }
-__global__ void enforceKernel(Fields F, long n, Grid g) {
+// tensor: the H of a node mapped back through a reflecting wall is reflected
+// too (PlanarBoundary::updateViolationNodes -> enforceBoundary(Hfield),
+// (R H R).Symmetric()).
+__global__ void enforceKernel(Fields F, long n, Grid g, int tensor) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  auto reflectH = [&](int a) {
+    if (!tensor) return;
+    if (a == 0) { F.f[F_HT_XY][i] = -F.f[F_HT_XY][i]; F.f[F_HT_XZ][i] = -F.f[F_HT_XZ][i]; }
+    else if (a == 1) { F.f[F_HT_XY][i] = -F.f[F_HT_XY][i]; F.f[F_HT_YZ][i] = -F.f[F_HT_YZ][i]; }
+    else { F.f[F_HT_XZ][i] = -F.f[F_HT_XZ][i]; F.f[F_HT_YZ][i] = -F.f[F_HT_YZ][i]; }
+  };
   double* P[3] = {F.f[F_X], F.f[F_Y], F.f[F_Z]};
   double* V[3] = {F.f[F_VX], F.f[F_VY], F.f[F_VZ]};
 #pragma unroll
@@ -782,12 +899,14 @@ __global__ void enforceKernel(Fields F, long n, Grid g) {
         p = imageCoord(p, 1, AXIS_REFLECT, g.kindHi[a], lo, hi);
         P[a][i] = p;
         V[a][i] = -V[a][i];
+        reflectH(a);
       }
       const double sdHi2 = hi - p;
       if (g.kindHi[a] == AXIS_REFLECT && sdHi2 < 0.0 && !fuzzyZero(sdHi2)) {
         p = imageCoord(p, 2, g.kindLo[a], AXIS_REFLECT, lo, hi);
         P[a][i] = p;
         V[a][i] = -V[a][i];
+        reflectH(a);
       }
     }
   }
@@ -913,9 +1032,15 @@ void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCoun
 }
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool carriedOnly, cudaStream_t s, LaunchCounter* lc) {
+                   bool carriedOnly, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+  // the tensor-H fields move only in ASPH mode
+  FieldSel sel{};
+  for (int f = 0; f < (carriedOnly ? (int)F_NUM_CARRIED : (int)F_NUM_PERMUTED); ++f) {
+    const bool isTensor = (f >= F_HT_XX && f < F_NUM_CARRIED) || f >= F_HIDEALT_XX;
+    if (tensor || !isTensor) sel.id[sel.n++] = (unsigned char)f;
+  }
   permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n,
-                                                carriedOnly ? (int)F_NUM_CARRIED : (int)F_NUM_PERMUTED);
+                                                sel);
   lc->add(1);
 }
 void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
@@ -942,13 +1067,15 @@ static void neighborBand(const Grid& g, double ext2, float& bandA, float& bandB)
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                       cudaStream_t s, LaunchCounter* lc) {
   const size_t sm = sizeof(double) * 3 * (hp.tableN1 + 1);
-  sumDensityKernel<<<gridFor(n, 128), 128, sm, s>>>(F, list, n, g, nl, t, hp);
+  if (hp.asph) sumDensityKernel<true><<<gridFor(n, 128), 128, sm, s>>>(F, list, n, g, nl, t, hp);
+  else sumDensityKernel<false><<<gridFor(n, 128), 128, sm, s>>>(F, list, n, g, nl, t, hp);
   lc->add(1);
 }
 void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
                  LaunchCounter* lc) {
   const size_t sm = sizeof(double) * 6 * (hp.tableN1 + 1);
-  gradhKernel<<<gridFor(n, 128), 128, sm, s>>>(F, n, g, nl, t, hp);
+  if (hp.asph) gradhKernel<true><<<gridFor(n, 128), 128, sm, s>>>(F, n, g, nl, t, hp);
+  else gradhKernel<false><<<gridFor(n, 128), 128, sm, s>>>(F, n, g, nl, t, hp);
   lc->add(1);
 }
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -956,13 +1083,19 @@ void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl,
   const size_t sm = sizeof(double) * 6 * (hp.tableN1 + 1);
   const int b = 128;
   (void)blockSize;
-  if (hp.xsph) {
-    if (hp.compatible) pairKernelFP64<true, true><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
-    else pairKernelFP64<true, false><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+#define SPH_PAIR64(X, C, T) pairKernelFP64<X, C, T><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc)
+  if (hp.asph) {
+    if (hp.xsph) {
+      if (hp.compatible) SPH_PAIR64(true, true, true); else SPH_PAIR64(true, false, true);
+    } else {
+      if (hp.compatible) SPH_PAIR64(false, true, true); else SPH_PAIR64(false, false, true);
+    }
+  } else if (hp.xsph) {
+    if (hp.compatible) SPH_PAIR64(true, true, false); else SPH_PAIR64(true, false, false);
   } else {
-    if (hp.compatible) pairKernelFP64<false, true><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
-    else pairKernelFP64<false, false><<<gridFor(n, b), b, sm, s>>>(F, list, n, g, nl, t, hp, pacc);
+    if (hp.compatible) SPH_PAIR64(false, true, false); else SPH_PAIR64(false, false, false);
   }
+#undef SPH_PAIR64
   lc->add(1);
 }
 void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, HydroParams hp,
@@ -980,12 +1113,16 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
   else energyKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, pacc, pacc32, dt);
   lc->add(1);
 }
-void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
-  saveState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
+void launchSaveState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+  saveState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
   lc->add(1);
 }
-void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
-  restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
+void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+  restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
+  lc->add(1);
+}
+void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
+  tensorExtentKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
   lc->add(1);
 }
 void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
@@ -993,16 +1130,16 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   const int epsInc = (mid || !hp.compatible) ? 1 : 0;
   Fields32 P{};
   if (mirror) P = *mirror;
-  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc, P,
-                                               g);
+  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
+                                               hp.asph, P, g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {
   eosKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, lists);
   lc->add(1);
 }
-void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc) {
-  enforceKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, g);
+void launchEnforce(Fields F, long n, Grid g, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+  enforceKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, g, tensor ? 1 : 0);
   lc->add(1);
 }
 void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
@@ -1048,18 +1185,24 @@ void launchItemFill(const int* flag, const long long* pos, long n, int* items, c
 }
 void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
                          int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
-                         uint32_t* nbr, int cap, double ext2, cudaStream_t s, LaunchCounter* lc) {
+                         uint32_t* nbr, int cap, double ext2, bool tensor, cudaStream_t s, LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
   const long threads = (long)nItems * width;
   const unsigned gb = (unsigned)((threads + 127) / 128);
-#define SPH_NBR(WR, WD)                                                                                        \
-  neighborWarpKernel<WR, WD><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts,        \
-                                                WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount, dItems)
-  if (nbr) {
-    if (width == 8) SPH_NBR(true, 8); else if (width == 16) SPH_NBR(true, 16); else SPH_NBR(true, 32);
+#define SPH_NBR(WR, WD, TE)                                                                                        \
+  neighborWarpKernel<WR, WD, TE><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts,        \
+                                                    WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount, dItems)
+  if (tensor) {
+    if (nbr) {
+      if (width == 8) SPH_NBR(true, 8, true); else if (width == 16) SPH_NBR(true, 16, true); else SPH_NBR(true, 32, true);
+    } else {
+      if (width == 8) SPH_NBR(false, 8, true); else if (width == 16) SPH_NBR(false, 16, true); else SPH_NBR(false, 32, true);
+    }
+  } else if (nbr) {
+    if (width == 8) SPH_NBR(true, 8, false); else if (width == 16) SPH_NBR(true, 16, false); else SPH_NBR(true, 32, false);
   } else {
-    if (width == 8) SPH_NBR(false, 8); else if (width == 16) SPH_NBR(false, 16); else SPH_NBR(false, 32);
+    if (width == 8) SPH_NBR(false, 8, false); else if (width == 16) SPH_NBR(false, 16, false); else SPH_NBR(false, 32, false);
   }
 #undef SPH_NBR
   lc->add(1);

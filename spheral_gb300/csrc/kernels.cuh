@@ -36,7 +36,7 @@ void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, 
 // returns); otherwise every permuted field.
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool carriedOnly, cudaStream_t s, LaunchCounter* lc);
+                   bool carriedOnly, bool tensor, cudaStream_t s, LaunchCounter* lc);
 // The limited Q's DvDx <- the hydro DvDx; and its FP32 mirror (3 float4 per node).
 void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc);
@@ -52,7 +52,7 @@ void launchItemFill(const int* flag, const long long* pos, long n, int* items, c
 // holds the count itself.
 void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
                          int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
-                         uint32_t* nbr, int cap, double ext2, cudaStream_t s, LaunchCounter* lc);
+                         uint32_t* nbr, int cap, double ext2, bool tensor, cudaStream_t s, LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
@@ -85,8 +85,11 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
                             double dt, cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
                                 float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc);
-void launchSaveState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
-void launchRestoreState0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
+// tensor: also the tensor H (ASPH)
+void launchSaveState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
+void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
+// ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
+void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
 // already advanced by the compatible-energy sweep when compatible).  mirror:
 // also refresh the FP32 mirrors of the new state (mixed mode), cells of grid g.
@@ -94,7 +97,7 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
                   bool mid, bool gravity, const Fields32* mirror, const Grid& g, cudaStream_t s, LaunchCounter* lc);
 // lists: device table of NodeListParams (HydroParams::lists).
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc);
-void launchEnforce(Fields F, long n, Grid g, cudaStream_t s, LaunchCounter* lc);
+void launchEnforce(Fields F, long n, Grid g, bool tensor, cudaStream_t s, LaunchCounter* lc);
 // out[0..7] conservation totals
 void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
                         LaunchCounter* lc);

@@ -17,7 +17,7 @@ FIELD_NCOMP = {
     "DvDt": 3, "DrhoDt": 1, "DepsDt": 1, "DvDx": 9, "internalDvDx": 9, "gradRho": 3, "M": 9, "localM": 9,
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
-    "DepsDtCompatible": 1, "numNeighbors": 1, "ArtificialViscosityVelocityGradient": 9,
+    "DepsDtCompatible": 1, "numNeighbors": 1, "ArtificialViscosityVelocityGradient": 9, "massSecondMoment": 6,
 }
 
 DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acceleration", "velocity magnitude",
@@ -25,6 +25,8 @@ DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acc
 
 
 VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
+# smoothing-scale package: SPHSmoothingScale or ASPHClassicSmoothingScale
+SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
 
 
 def config_from_dict(cfg, precision="fp64", device=0):
@@ -32,6 +34,8 @@ def config_from_dict(cfg, precision="fp64", device=0):
     for k, v in cfg.items():
         if k == "viscosity" and isinstance(v, str):
             c.viscosity = VISCOSITY[v]
+        elif k == "smoothing_scale" and isinstance(v, str):
+            c.smoothing_scale = SMOOTHING_SCALE[v]
         elif k in dict(N.Config._fields_):
             setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
     c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)
@@ -79,8 +83,10 @@ class Engine:
         self._table_keep = arrs
         self._chk(self.L.sphgpu_set_kernel_table(self.h, *[N.dptr(a) for a in arrs]))
 
-    def set_nodelist(self, k, nPerh, hmin, hmax, rhoMin, rhoMax, gamma):
+    def set_nodelist(self, k, nPerh, hmin, hmax, rhoMin, rhoMax, gamma, hminratio=None):
         self._chk(self.L.sphgpu_set_nodelist(self.h, k, nPerh, hmin, hmax, rhoMin, rhoMax, gamma))
+        if hminratio is not None:
+            self._chk(self.L.sphgpu_set_nodelist_hminratio(self.h, k, hminratio))
 
     def add_boundary(self, type, axis, lo, hi, wall_high=0):
         self._chk(self.L.sphgpu_add_boundary(self.h, type, axis, lo, hi, wall_high))
@@ -96,7 +102,8 @@ class Engine:
 
     def load(self, problem):
         for k, nl in enumerate(problem.nodelists):
-            self.set_nodelist(k, nl["nPerh"], nl["hmin"], nl["hmax"], nl["rhoMin"], nl["rhoMax"], nl["gamma"])
+            self.set_nodelist(k, nl["nPerh"], nl["hmin"], nl["hmax"], nl["rhoMin"], nl["rhoMax"], nl["gamma"],
+                              nl.get("hminratio"))
         for b in problem.boundaries:
             self.add_boundary(b["type"], b["axis"], b["lo"], b["hi"], b.get("wall_high", 0))
         self.set_particles(problem.pos, problem.vel, problem.mass, problem.rho, problem.eps, problem.H,
