@@ -11,6 +11,8 @@ ideal-gas SPH problem runs on the GPU package with its imports changed:
     MonaghanGingoldViscosity(Clinear, Cquadratic, ...)         MonaghanGingoldViscosity.cc:25-37
     LimitedMonaghanGingoldViscosity(Clinear, Cquadratic, ..., etaCritFrac, etaFoldFrac)
     SPH(dataBase, W, Q, cfl, ..., XSPH, densityUpdate, epsTensile, nTensile)   src/SPH/SPHHydros.py:9-156
+    SPH(..., ASPH="CLASSIC") / ASPHClassicSmoothingScale(HUpdate, W, fixShape)
+                                                    src/SmoothingScale/ASPHClassicSmoothingScale.cc
     OctTreeGravity(G, softeningLength, opening, ftimestep)     src/Gravity/TreeGravity.cc:88-115
     Plane(point, normal), PeriodicBoundary(plane1, plane2), ReflectingBoundary(plane)
     CheapSynchronousRK2Integrator(dataBase, dtMin, dtMax, dtGrowth)   src/Integrator/CheapSynchronousRK2.hh
@@ -32,6 +34,39 @@ RigorousSumDensity = 0
 IntegrateDensity = 1
 # HEvolutionType
 IdealH = 0
+
+
+class SPHSmoothingScale:
+    """SPHSmoothingScale(HUpdate, W): isotropic H = I/h (the SPH() default)."""
+
+    def __init__(self, HUpdate=IdealH, W=None):
+        if HUpdate != IdealH:
+            raise NotImplementedError("only IdealH is on the GPU path")
+        self._cfg = dict(smoothing_scale="sph")
+
+
+class ASPHClassicSmoothingScale:
+    """ASPHClassicSmoothingScale(HUpdate, W, fixShape=False, radialOnly=False):
+    symmetric-tensor H shaped by the second moment of the neighbour
+    distribution (src/SmoothingScale/ASPHClassicSmoothingScale.cc).  Runs in
+    the FP64 precision mode; radialOnly is not on the GPU path."""
+
+    def __init__(self, HUpdate=IdealH, W=None, fixShape=False, radialOnly=False):
+        if HUpdate != IdealH:
+            raise NotImplementedError("only IdealH is on the GPU path")
+        if radialOnly:
+            raise NotImplementedError("radialOnly is not on the GPU path")
+        self._cfg = dict(smoothing_scale="asph_classic", fix_shape=bool(fixShape))
+
+
+class ASPHSmoothingScale:
+    """ASPHSmoothingScale shapes H from Voronoi cell moments (a tessellation
+    outside this path); with fixShape it reduces to scaling H, which the
+    classic form covers."""
+
+    def __init__(self, *args, **kwargs):
+        raise NotImplementedError("ASPHSmoothingScale needs Voronoi cells: use ASPH='CLASSIC' "
+                                  "(ASPHClassicSmoothingScale)")
 
 
 class BSplineKernel:
@@ -206,7 +241,8 @@ class ReflectingBoundary:
 
 class SPHHydro:
     def __init__(self, dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
-                 XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile, nTensile):
+                 XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile, nTensile,
+                 smoothingScaleMethod=None):
         self.dataBase, self.W, self.Q = dataBase, W, Q
         self.cfl = cfl
         self._cfg = dict(num_table_points=W.numPoints, cfl=cfl,
@@ -216,6 +252,8 @@ class SPHHydro:
                          sum_mass_density_over_all_nodelists=sumMassDensityOverAllNodeLists,
                          density_update=densityUpdate, eps_tensile=epsTensile, n_tensile=nTensile)
         self._cfg.update(Q._config())
+        self._smoothingScaleMethod = smoothingScaleMethod or SPHSmoothingScale(IdealH, W)
+        self._cfg.update(self._smoothingScaleMethod._cfg)
         self.boundaries = []
 
     def appendBoundary(self, bc):
@@ -230,9 +268,19 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
         HUpdate=IdealH, epsTensile=0.0, nTensile=4.0, damageRelieveRubble=False, strengthInDamage=False,
         xmin=None, xmax=None, etaMinAxis=0.1, ASPH=False, smoothingScaleMethod=None):
     """The SPH() factory (src/SPH/SPHHydros.py:9-156) with its defaults; the
-    default Q is LimitedMonaghanGingoldViscosity(1, 1) as in the factory."""
-    if ASPH or smoothingScaleMethod is not None:
-        raise NotImplementedError("ASPH needs Voronoi cell moments: not on the GPU path")
+    default Q is LimitedMonaghanGingoldViscosity(1, 1) as in the factory.
+    ASPH="CLASSIC" selects ASPHClassicSmoothingScale (SPHHydros.py:130-138);
+    ASPH=True (the Voronoi-based ASPHSmoothingScale) is not on this path."""
+    if smoothingScaleMethod is None:
+        if ASPH:
+            if isinstance(ASPH, str) and ASPH.upper() == "CLASSIC":
+                smoothingScaleMethod = ASPHClassicSmoothingScale(HUpdate, W)
+            else:
+                smoothingScaleMethod = ASPHSmoothingScale(HUpdate, W)
+        else:
+            smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
+    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale)):
+        raise NotImplementedError("unknown smoothing-scale package")
     if evolveTotalEnergy:
         raise NotImplementedError("evolveTotalEnergy is not on the GPU path")
     if HUpdate != IdealH or (filter or 0.0) != 0.0:
@@ -241,7 +289,7 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
         Q = LimitedMonaghanGingoldViscosity(1.0, 1.0)
     return SPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
                     XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile,
-                    nTensile)
+                    nTensile, smoothingScaleMethod)
 
 
 class OctTreeGravity:
@@ -286,7 +334,7 @@ class CheapSynchronousRK2Integrator:
         H = cat("H")
         nodelist = np.concatenate([np.full(nl.numInternalNodes, k, dtype=np.int32) for k, nl in enumerate(lists)])
         nls = [dict(nPerh=nl.nPerh, hmin=nl.hmin, hmax=nl.hmax, rhoMin=nl.rhoMin, rhoMax=nl.rhoMax,
-                    gamma=nl.eos.gamma) for nl in lists]
+                    gamma=nl.eos.gamma, hminratio=nl.hminratio) for nl in lists]
         prob = problems.Problem("script", cat("position"), cat("velocity"), cat("mass"), cat("massDensity"),
                                 cat("specificThermalEnergy"), 1.0 / H[:, 0], nodelist if len(lists) > 1 else None,
                                 nls, [b._spec for b in hydro.boundaries], cfg)

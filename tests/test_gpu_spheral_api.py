@@ -55,3 +55,43 @@ def test_spheral_style_advance_to_goal_time(native_lib):
     ref, nodes, integrator = _sod_script(steps=0)
     n = integrator.advance(0.02)
     assert n > 0 and abs(integrator.currentTime - 0.02) < 1e-14
+
+
+def test_spheral_style_asph_classic_matches_engine(native_lib):
+    # an anisotropic box through SPH(..., ASPH="CLASSIC") runs the same tensor-H step
+    from spheral_gb300.engine import Engine
+    ref = problems.stretched_box(seed=75)
+    W = S.TableKernel(S.BSplineKernel(), 1000)
+    nl = ref.nodelists[0]
+    nodes = S.makeFluidNodeList("fluid", S.GammaLawGas(5.0 / 3.0), hmin=nl["hmin"], hmax=nl["hmax"],
+                                hminratio=nl["hminratio"], nPerh=nl["nPerh"])
+    nodes.resize(ref.n)
+    nodes.positions()[:] = ref.pos
+    nodes.velocity()[:] = ref.vel
+    nodes.mass()[:] = ref.mass
+    nodes.massDensity()[:] = ref.rho
+    nodes.specificThermalEnergy()[:] = ref.eps
+    nodes.Hfield()[:] = ref.H
+    db = S.DataBase()
+    db.appendNodeList(nodes)
+    hydro = S.SPH(W=W, dataBase=db, Q=S.MonaghanGingoldViscosity(1.0, 1.0), XSPH=False, ASPH="CLASSIC")
+    for a in range(3):
+        lo = [0.0, 0.0, 0.0]
+        hi = [0.0, 0.0, 0.0]
+        hi[a] = 1.0
+        nrm = [0.0, 0.0, 0.0]
+        nrm[a] = 1.0
+        nrm2 = [0.0, 0.0, 0.0]
+        nrm2[a] = -1.0
+        hydro.appendBoundary(S.PeriodicBoundary(S.Plane(lo, nrm), S.Plane(hi, nrm2)))
+    integrator = S.CheapSynchronousRK2Integrator(db, dtMin=0.0, dtMax=0.1, dtGrowth=2.0)
+    integrator.lastDt = 1e-3
+    integrator.appendPhysicsPackage(hydro)
+    for _ in range(3):
+        integrator.step()
+    eng = Engine.from_problem(ref)
+    eng.initialize()
+    for _ in range(3):
+        eng.step()
+    assert np.array_equal(nodes.Hfield(), eng.field("H"))
+    assert np.array_equal(nodes.positions(), eng.field("position"))

@@ -35,6 +35,20 @@ def test_out_of_path_options_are_refused():
         S.PeriodicBoundary(S.Plane((0, 0, 0), (1, 0, 0)), S.Plane((1, 0, 0), (1, 0, 0)))
 
 
+def test_asph_classic_selects_tensor_h():
+    # SPH(..., ASPH="CLASSIC") builds ASPHClassicSmoothingScale (SPHHydros.py:130-138)
+    db = S.DataBase()
+    W = S.TableKernel(S.BSplineKernel(), 1000)
+    hydro = S.SPH(W=W, dataBase=db, ASPH="CLASSIC")
+    assert isinstance(hydro._smoothingScaleMethod, S.ASPHClassicSmoothingScale)
+    assert hydro._cfg["smoothing_scale"] == "asph_classic" and hydro._cfg["fix_shape"] is False
+    fixed = S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.ASPHClassicSmoothingScale(S.IdealH, W, fixShape=True))
+    assert fixed._cfg["fix_shape"] is True
+    assert S.SPH(W=W, dataBase=db)._cfg["smoothing_scale"] == "sph"
+    with pytest.raises(NotImplementedError):
+        S.ASPHClassicSmoothingScale(S.IdealH, W, radialOnly=True)
+
+
 def test_boundary_planes_map_to_axis_specs():
     p = S.PeriodicBoundary(S.Plane((0, 0, 0), (0, 1, 0)), S.Plane((0, 2, 0), (0, -1, 0)))
     assert p._spec == dict(type=0, axis=1, lo=0.0, hi=2.0)
