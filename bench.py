@@ -138,7 +138,14 @@ def max_over_ranks(dist, v):
 
 def make_workload_name(args):
     return None, {"kh": "kelvin_helmholtz_3d", "sweep": "sweep_box", "sod": "sod_planar_3d",
-                  "evrard": "evrard_collapse_3d"}[args.workload]
+                  "evrard": "evrard_collapse_3d", "asph": "asph_stretched_lattice_3d"}[args.workload]
+
+
+def asph_box(n1, seed=13):
+    """ASPHClassicSmoothingScale workload: the anisotropic jittered lattice
+    (spacings 1 : 1.25 : 1.6 across x y z) with rotated tensor H."""
+    from spheral_gb300 import problems
+    return problems.stretched_box(nx=int(round(1.25 * n1)), ny=n1, nz=int(round(0.8 * n1)), seed=seed)
 
 
 def make_workload(args):
@@ -151,6 +158,8 @@ def make_workload(args):
         return problems.sod(nx1=args.n1), "sod_planar_3d"
     if args.workload == "evrard":
         return problems.evrard(n=args.n_evrard), "evrard_collapse_3d"
+    if args.workload == "asph":
+        return asph_box(args.n1), "asph_stretched_lattice_3d"
     raise SystemExit("unknown workload")
 
 
@@ -166,6 +175,8 @@ def cpu_baseline(args, steps=None, warmup=1):
         p = problems.sweep_box(n_side=args.cpu_n1, neighbors=args.neighbors)
     elif args.workload == "evrard":
         p = problems.evrard(n=65536)
+    elif args.workload == "asph":
+        p = asph_box(args.cpu_n1)
     else:
         p = problems.sod(nx1=args.cpu_n1)
     o = orc.Oracle(p)
@@ -508,7 +519,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard"])
+    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard", "asph"])
     ap.add_argument("--n-evrard", type=int, default=1048576)
     ap.add_argument("--validate", action="store_true", help="evrard: integrate to --goal-time and compare profiles")
     ap.add_argument("--goal-time", type=float, default=0.8)

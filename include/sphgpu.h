@@ -56,7 +56,7 @@ extern "C" {
 
 #define SPHGPU_SMOOTHING_SPH 0           /* SPHSmoothingScale: isotropic H = I/h                  */
 #define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
-                                            symmetric-tensor H; FP64 precision mode            */
+                                            symmetric-tensor H                                  */
 
 typedef struct sphgpu_ctx* sphgpu_handle;
 

@@ -131,6 +131,7 @@ struct sphgpu_ctx {
   Fields F{}, Falt{};
   DBuf orig[2], list[2], cellc[2];
   DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
+  DBuf hten;                 // ASPH: FP32 mirror of tensor H (2 float4 per node)
   DBuf stage;                // host <-> device staging for caller-order transfers
   DBuf v12;                  // half-step velocities + DepsDt0 of the mixed-mode energy sweep
   int cur = 0;
@@ -200,6 +201,7 @@ struct sphgpu_ctx {
     p.thermo = thermo.as<float4>();
     p.cell = cellp();
     p.dvq = dvq.p ? dvq.as<float4>() : nullptr;
+    p.hten = cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? hten.as<float4>() : nullptr;
     return p;
   }
   bool fp32() const { return cfg.precision == SPHGPU_PRECISION_FP32; }
@@ -219,6 +221,8 @@ void ensureCapacity(sphgpu_ctx* c, long n) {
   c->posh.release(); c->posh.ensure(n * sizeof(float4));
   c->velm.release(); c->velm.ensure(n * sizeof(float4));
   c->thermo.release(); c->thermo.ensure(n * sizeof(float4));
+  c->hten.release();
+  if (c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC) c->hten.ensure(2 * n * sizeof(float4));
   for (int k = 0; k < 2; ++k) {
     c->orig[k].release(); c->orig[k].ensure(n * sizeof(int));
     c->list[k].release(); c->list[k].ensure(n * sizeof(int));
@@ -616,7 +620,8 @@ void evalDerivs(sphgpu_ctx* c) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
     // trial launches leave the same results) and keep the fastest.
-    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n)) {
+    // (the tensor-H kernel has a single variant: nothing to tune)
+    if (!c->pinnedVariant && !c->hp.asph && (c->pairVariant < 0 || c->tunedN != c->n)) {
       cudaEvent_t e0, e1;
       CUDA_OK(cudaEventCreate(&e0));
       CUDA_OK(cudaEventCreate(&e1));
@@ -929,8 +934,6 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
     if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
-    if (cfg->smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC && cfg->precision != SPHGPU_PRECISION_FP64)
-      throw Error(SPHGPU_E_UNSUPPORTED, "the ASPH smoothing scale runs in the FP64 precision mode");
     CUDA_OK(cudaSetDevice(cfg->device));
     CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->prof.s = c->stream;
@@ -969,7 +972,8 @@ int sphgpu_destroy(sphgpu_handle c) {
   for (auto& r : c->prof.pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
-                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->stage, &c->v12, &c->itemFlag, &c->items,
+                  &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->hten, &c->stage, &c->v12, &c->itemFlag,
+                  &c->items,
                   &c->dLists, &c->dvq};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }

@@ -284,23 +284,16 @@ __device__ __forceinline__ void finalizeNode(Fields& F, long i, int li, const No
 }
 
 
-__device__ __forceinline__ double rootnu3(double x) { return (x < 0.0 ? -1.0 : 1.0) * pow(fabs(x), 0.3333333333333333); }
-
 // ASPHClassicSmoothingScale node part (ASPHClassicSmoothingScale.cc:180-291):
-// tensor DH/Dt; the shape of Hideal from the normalised second moment of the
-// neighbour distribution (eigenvalues of psi^-1/2 floored at hminratio of the
-// largest), its size from the zeroth moment as in the SPH IdealH (or, with
-// fixShape, H itself rescaled); then the eigenvalues bounded by 1/hmax and
-// min(1/hmin, max(1/hmax, smallest) / hminratio).
+// tensor DH/Dt and Hideal (asphClassicHideal) from the moments.
 __device__ __forceinline__ void finalizeNodeASPH(Fields& F, long i, int li, const NodeAcc& a, const Sym& Hi,
                                                  double mi, double rhoi, double vxi, double vyi, double vzi,
                                                  int numNb, const HydroParams& hp, const double* __restrict__ herm) {
   double D[9];
   finalizeHydro(F, i, a, mi, rhoi, vxi, vyi, vzi, symDet(Hi), numNb, hp, D);
-  const double tiny = 1.0e-50;
   const NodeListParams L = hp.lists[li];
   storeSym(F, F_DHDTT_XX, i, smoothingScaleDerivative(Hi, D));
-  const double m0 = rootnu3(fmax(0.0, a.m0));
+  const double m0 = rootnu3T(fmax(0.0, a.m0));
   F.f[F_M0][i] = m0;
   F.f[F_M1_X][i] = a.m1x;
   F.f[F_M1_Y][i] = a.m1y;
@@ -310,36 +303,11 @@ __device__ __forceinline__ void finalizeNodeASPH(Fields& F, long i, int li, cons
   const bool isolated = fabs(m0) <= 1.0e-15 * fmax(1.0, fabs(m0));
   const double cur = isolated ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(herm, hp, m0));
   const double s = fmin(4.0, fmax(0.25, L.nPerh / cur));
-  const double psiweight = fmax(0.0, fmin(1.0, 2.0 / s - 1.0));
-  Sym Hid{1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
-  double ev[3], V[3][3], d[3];
+  double ev[3];
   symEigenValues(M2, ev);
-  if (psiweight > 0.0 && symDet(M2) > 0.0 && fmin(ev[0], fmin(ev[1], ev[2])) > 0.0) {
-    Sym psi = symDiv(M2, symMaxAbs(M2));
-    const double dp = symDet(psi);
-    if (dp > 1.0e-10) psi = symDiv(psi, rootnu3(fabs(dp) + tiny));
-    else psi = Sym{1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
-    symEigen(psi, ev, V);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) ev[k] = 1.0 / sqrt(ev[k]);
-    const double psimin = fmax(ev[0], fmax(ev[1], ev[2])) * L.hminratio;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) d[k] = fmax(psimin, ev[k]);
-    psi = symFromEigen(d, V);
-    psi = symDiv(psi, rootnu3(symDet(psi) + tiny));
-    symEigen(psi, ev, V);   // psi^(1/2), then its inverse
-#pragma unroll
-    for (int k = 0; k < 3; ++k) d[k] = sqrt(fmax(0.0, ev[k]));
-    Hid = symInverse(symFromEigen(d, V));
-  }
-  const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s + tiny));
-  if (hp.fixShape) Hid = symDiv(Hi, 1.0 - aa + aa * s);
-  else Hid = symScale(Hid, rootnu3(symDet(Hi)) / (1.0 - aa + aa * s));
-  symEigen(Hid, ev, V);
-  const double hminEffInv = fmin(L.hminInv, fmax(L.hmaxInv, fmin(ev[0], fmin(ev[1], ev[2]))) / L.hminratio);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = fmax(L.hmaxInv, fmin(hminEffInv, ev[k]));
-  storeSym(F, F_HIDEALT_XX, i, symFromEigen(d, V));
+  storeSym(F, F_HIDEALT_XX, i,
+           asphClassicHideal(M2, fmin(ev[0], fmin(ev[1], ev[2])) > 0.0, Hi, s, hp.fixShape != 0, L.hminInv,
+                             L.hmaxInv, L.hminratio));
 }
 
 // FP32 variant of finalizeNode for the mixed mode: the per-node completion
@@ -362,12 +330,16 @@ struct NodeAcc32 {
   float rhoSum, norm, gx, gy, gz, maxQ, effQ, xw, xdx, xdy, xdz, m0, m1x, m1y, m1z;
   double dvx, dvy, dvz, deps;
   float D[9], M[9];
+  float m2[6];      // TENSOR: ASPH second moment
+  float4 h0, h1;    // TENSOR: the node's H mirror
 };
 
+// TENSOR: ASPHClassicSmoothingScale in FP32 (tensor DH/Dt, asphClassicHideal).
+template <bool TENSOR>
 __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const NodeAcc32& a, int numNb,
                                                const HydroParams& hp, const double* __restrict__ herm) {
   const float mi = (float)F.f[F_MASS][i], rhoi = (float)F.f[F_RHO][i], ai = (float)F.f[F_HINV][i];
-  const float Hdeti = (ai * ai) * ai;
+  const float Hdeti = TENSOR ? a.h1.z : (ai * ai) * ai;
   const float W0 = (float)hp.W0;
   F.f[F_RHOSUM][i] = a.rhoSum + mi * W0 * Hdeti;
   F.f[F_NORM][i] = a.norm + mi / rhoi * W0 * Hdeti;
@@ -432,6 +404,22 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
   F.f[F_M1_X][i] = a.m1x;
   F.f[F_M1_Y][i] = a.m1y;
   F.f[F_M1_Z][i] = a.m1z;
+  if (TENSOR) {
+    const SymT<float> Hi{a.h0.x, a.h0.y, a.h0.z, a.h0.w, a.h1.x, a.h1.y};
+    storeSym(F, F_DHDTT_XX, i, smoothingScaleDerivative(Hi, D));
+    const SymT<float> M2{a.m2[0], a.m2[1], a.m2[2], a.m2[3], a.m2[4], a.m2[5]};
+    storeSym(F, F_M2_XX, i, M2);
+    const float nPerh = (float)L.nPerh;
+    const bool isolated = fabsf(m0) <= 1.0e-15f * fmaxf(1.0f, fabsf(m0));
+    const float cur = isolated ? 0.5f * nPerh : fmaxf(0.0f, hermiteLookup32(herm, hp, m0));
+    const float s = fminf(4.0f, fmaxf(0.25f, nPerh / cur));
+    // positive definite (Sylvester): every eigenvalue of M2 positive
+    const bool pd = M2.xx > 0.0f && M2.xx * M2.yy - M2.xy * M2.xy > 0.0f && symDet(M2) > 0.0f;
+    storeSym(F, F_HIDEALT_XX, i,
+             asphClassicHideal(M2, pd, Hi, s, hp.fixShape != 0, (float)L.hminInv, (float)L.hmaxInv,
+                               (float)L.hminratio));
+    return;
+  }
   // FP32 forms of DHDt = -(H/3) tr(DvDx) and of the IdealH clamp
   // 1/clamp(h0 f, hmin, hmax) = clamp(H0 / f, 1/hmax, 1/hmin): no FP64 divide.
   F.f[F_DHDT][i] = (double)(-(ai * (1.0f / 3.0f)) * trace);

@@ -59,6 +59,7 @@ struct Fields32 {
   float4* thermo;   // (rho, P/rho^2 * Omega^-1, cs, unused)
   uint32_t* cell;   // packed cell coordinates (10 bits per axis)
   float4* dvq;      // limited Q: DvDx of the Q as 3 float4 per node (xx xy xz yx | yy yz zx zy | zz - - -)
+  float4* hten;     // ASPH: tensor H as 2 float4 per node (xx xy xz yy | yz zz det(H) lambda_max)
 };
 
 }  // namespace sph

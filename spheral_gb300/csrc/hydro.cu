@@ -111,9 +111,24 @@ __global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* 
 // cell in sorted order, so every list has a reproducible order.
 // WRITE false: count only; true: count and write the warp-interleaved lists
 // (slots beyond cap are counted, not written).
+// Relative half-width of the FP32 band around |H r|^2 = ext^2 for a node with
+// eigenvalues in [lmin, lmax].  Each FP32 separation component carries at
+// most ~10 u C of rounding (C the largest cell edge, u = 2^-24), and the
+// products and sums of H r add ~4 u |H| |r| per component; near the threshold
+// (|H r| ~ ext, |r| <= ext / lmin) |H r| is then off by at most
+// 30 u C lmax + 12 u ext lmax / lmin and its square by
+// ext^2 u (60 C lmax / ext + 24 lmax / lmin + 3).  The band is four times that.
+__device__ __forceinline__ float tensorBand(float lmax, float lmin, const Grid& g) {
+  const float u = 5.9604645e-8f;
+  const float C = fmaxf(g.cellf[0], fmaxf(g.cellf[1], g.cellf[2]));
+  return 4.0f * u * (60.0f * C * lmax / sqrtf(g.ext2f) + 24.0f * lmax / lmin + 3.0f);
+}
+
 // TENSOR (ASPH): h^-1 in the FP32 mirror is the smallest eigenvalue of H, so
-// the pre-filter bounds |H r| from below and every candidate inside its band
-// takes the exact FP64 tensor test.
+// the scalar pre-filter bounds |H r| from below and rejects the far
+// candidates; the rest take |H_i r|^2 and |H_j r|^2 in FP32 from the tensor
+// mirror with a per-node band (tensorBand), and only those inside a band
+// take the exact FP64 tensor test.
 template <bool WRITE, int W, bool TENSOR>
 __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
@@ -123,6 +138,8 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
                                                           const long long* __restrict__ dItems) {
   constexpr int G = 128 / W;             // groups per 128-thread block
   __shared__ float4 stage[G][W];         // one candidate batch per group
+  constexpr int HW = TENSOR ? 2 * W : 1;
+  __shared__ float4 stageH[G][HW];       // TENSOR: the batch's H (xx xy xz yy | yz zz band .)
   __shared__ int2 range[G][27];          // node ranges of the 27 candidate cells
   const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) / W);
   const int lane = threadIdx.x % W, wib = threadIdx.x / W;
@@ -174,7 +191,16 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   Sym Hi{};
-  if (TENSOR && active) Hi = loadSym(F, F_HT_XX, i);
+  float4 hi0 = make_float4(0.f, 0.f, 0.f, 0.f), hi1 = hi0;
+  float tLo = 0.f, tHi = 0.f;
+  if (TENSOR && active) {
+    Hi = loadSym(F, F_HT_XX, i);
+    hi0 = P.hten[2 * i];
+    hi1 = P.hten[2 * i + 1];
+    const float dI = tensorBand(hi1.w, pi.w, g);
+    tLo = dI < 0.5f ? e2t * (1.0f - dI) : -1.0f;
+    tHi = dI < 0.5f ? e2t * (1.0f + dI) : FLT_MAX;
+  }
   int cnt = 0;
   // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
   uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;
@@ -182,7 +208,11 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   int tn = 0;
   while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
   float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (tn < 27 && range[wib][tn].x + lane < range[wib][tn].y) qn = P.posh[range[wib][tn].x + lane];
+  float4 hn0 = qn, hn1 = qn;
+  if (tn < 27 && range[wib][tn].x + lane < range[wib][tn].y) {
+    qn = P.posh[range[wib][tn].x + lane];
+    if (TENSOR) { hn0 = P.hten[2 * (range[wib][tn].x + lane)]; hn1 = P.hten[2 * (range[wib][tn].x + lane) + 1]; }
+  }
   while (tn < 27) {
     const int t = tn;
     const int s = range[wib][t].x, e = range[wib][t].y;
@@ -198,11 +228,25 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
     while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
     for (int base = s; base < e; base += W) {
       float4 q = qn;
+      float4 qh0 = hn0, qh1 = hn1;
       if (base + W < e) {            // another batch of this cell follows
-        qn = (base + W + lane < e) ? P.posh[base + W + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool ok = base + W + lane < e;
+        qn = ok ? P.posh[base + W + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (TENSOR && ok) { hn0 = P.hten[2 * (base + W + lane)]; hn1 = P.hten[2 * (base + W + lane) + 1]; }
       } else if (tn < 27) {          // last batch: prefetch the next cell's first batch
         const int sn = range[wib][tn].x, en = range[wib][tn].y;
-        qn = (sn + lane < en) ? P.posh[sn + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool ok = sn + lane < en;
+        qn = ok ? P.posh[sn + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (TENSOR && ok) { hn0 = P.hten[2 * (sn + lane)]; hn1 = P.hten[2 * (sn + lane) + 1]; }
+      }
+      if (TENSOR) {   // band of node j, then H_j seen through the mirrors
+        qh1.z = tensorBand(qh1.w, q.w, g);
+        const float sx = (mir & 3u) ? -1.f : 1.f, sy = (mir & 12u) ? -1.f : 1.f, sz = (mir & 48u) ? -1.f : 1.f;
+        qh0.y *= sx * sy;   // xy
+        qh0.z *= sx * sz;   // xz
+        qh1.x *= sy * sz;   // yz
+        stageH[wib][2 * lane] = qh0;
+        stageH[wib][2 * lane + 1] = qh1;
       }
       if (mir) {
         if (mir & 3u) q.x = cx - q.x;
@@ -229,7 +273,18 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
           const float e2 = fminf(ai2, cq.w) * r2;
           if (e2 <= bandHi) {
             bool inside = true;
-            if (TENSOR || e2 >= bandLo) {   // guard band: the exact FP64 criterion (rare)
+            bool exact = !TENSOR && e2 >= bandLo;
+            if (TENSOR) {   // FP32 tensor test, each side with its own band
+              const float4 h0 = stageH[wib][2 * u], h1 = stageH[wib][2 * u + 1];
+              const float e2i = eta2Sym32(hi0, hi1, rx, ry, rz);
+              const float e2j = eta2Sym32(h0, h1, rx, ry, rz);
+              const float jLo = h1.z < 0.5f ? e2t * (1.0f - h1.z) : -1.0f;
+              const float jHi = h1.z < 0.5f ? e2t * (1.0f + h1.z) : FLT_MAX;
+              if (e2i <= tLo || e2j <= jLo) inside = true;
+              else if (e2i >= tHi && e2j >= jHi) inside = false;
+              else exact = true;
+            }
+            if (exact) {   // guard band: the exact FP64 criterion (rare)
               const int j = base + u;
               double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
               const int code = imageCode(g, hc, dcode);
@@ -858,6 +913,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     P.velm[i] = make_float4((float)vx, (float)vy, (float)vz, (float)F.f[F_MASS][i]);
     const float om = (float)F.f[F_OMEGA][i];
     P.thermo[i] = make_float4((float)rho, (float)F.f[F_P][i], (float)F.f[F_CS][i], om / (om * om + 1.0e-30f));
+    if (P.hten) writeTensorMirror(F, P, i);
   }
 }
 

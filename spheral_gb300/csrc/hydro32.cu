@@ -50,6 +50,7 @@ __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   const double om = F.f[F_OMEGA][i];
   P.thermo[i] = make_float4((float)F.f[F_RHO][i], (float)F.f[F_P][i], (float)F.f[F_CS][i],
                             (float)(om / (om * om + 1.0e-30)));
+  if (P.hten) writeTensorMirror(F, P, i);
 }
 
 __device__ __forceinline__ void lookup32(const float* __restrict__ tw, const float* __restrict__ tg, int N1,
@@ -86,7 +87,11 @@ __device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, cons
   }
 }
 
-template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF, bool LIMQ>
+// TENSOR (ASPH): H_i, H_j from the FP32 tensor mirror (eta = H r,
+// grad W = gW H eta^, both in a fixed order so the pair force stays bitwise
+// antisymmetric), the second moment of ASPHClassicSmoothingScale and its
+// FP32 finalize.
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF, bool LIMQ, bool TENSOR>
 __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
@@ -104,7 +109,9 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   const float4 pi = P.posh[i], vi = P.velm[i], thi = P.thermo[i];
   const int li = MULTI ? list[i] : 0;
   const float ai = pi.w, mi = vi.w, rhoi = thi.x, Pi = thi.y, csi = thi.z, sOi = thi.w;
-  const float Hdeti = ai * ai * ai;
+  float4 hi0 = make_float4(0.f, 0.f, 0.f, 0.f), hi1 = hi0;
+  if (TENSOR) { hi0 = P.hten[2 * i]; hi1 = P.hten[2 * i + 1]; }
+  const float Hdeti = TENSOR ? hi1.z : ai * ai * ai;
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   const float Cl = (float)hp.Cl, Cq = (float)hp.Cq, eps2 = (float)hp.eps2;
@@ -124,33 +131,38 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   float rhoSum = 0.f, norm = 0.f, maxQ = 0.f, effQ = 0.f, xw = 0.f, xdx = 0.f, xdy = 0.f, xdz = 0.f;
   float sdx = 0.f, cdx = 0.f, sdy = 0.f, cdy = 0.f, sdz = 0.f, cdz = 0.f, se = 0.f, ce = 0.f;
   float gx = 0.f, gy = 0.f, gz = 0.f, m0 = 0.f, m1x = 0.f, m1y = 0.f, m1z = 0.f;
-  float D[9], M[9];
+  float D[9], M[9], m2[6];
 #pragma unroll
   for (int k = 0; k < 9; ++k) { D[k] = 0.f; M[k] = 0.f; }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) m2[k] = 0.f;
 
   const int cnt = nl.count[i];
   // PF: software pipeline over the neighbour list -- the entry two slots
   // ahead and the node data one slot ahead are loaded while the current pair
   // is evaluated, so the gathers overlap the arithmetic.
   uint32_t entA = 0u, entB = 0u;
-  float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA, thA = pjA;
+  float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA, thA = pjA, hA0 = pjA, hA1 = pjA;
   if (PF) {
     if (cnt > 0) {
       entA = nl.nbr[nbSlot(i, 0, nl.cap)];
       const int j0 = (int)(entA & kIndexMask);
       pjA = P.posh[j0]; vjA = P.velm[j0]; thA = P.thermo[j0];
+      if (TENSOR) { hA0 = P.hten[2 * j0]; hA1 = P.hten[2 * j0 + 1]; }
     }
     if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
   }
   for (int q = 0; q < cnt; ++q) {
     const long long k = nbSlot(i, q, nl.cap);
     uint32_t ent;
-    float4 pj, vj4, thj;
+    float4 pj, vj4, thj, hj0 = make_float4(0.f, 0.f, 0.f, 0.f), hj1 = hj0;
     if (PF) {
       ent = entA; pj = pjA; vj4 = vjA; thj = thA;
+      if (TENSOR) { hj0 = hA0; hj1 = hA1; }
       if (q + 1 < cnt) {
         const int jn = (int)(entB & kIndexMask);
         pjA = P.posh[jn]; vjA = P.velm[jn]; thA = P.thermo[jn];
+        if (TENSOR) { hA0 = P.hten[2 * jn]; hA1 = P.hten[2 * jn + 1]; }
         entA = entB;
       }
       if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
@@ -158,6 +170,7 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
       ent = nl.nbr[k];
       const int jj = (int)(ent & kIndexMask);
       pj = P.posh[jj]; vj4 = P.velm[jj]; thj = P.thermo[jj];
+      if (TENSOR) { hj0 = P.hten[2 * jj]; hj1 = P.hten[2 * jj + 1]; }
     }
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
@@ -166,11 +179,26 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
     const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z, sOj = thj.w;
     const bool same = MULTI ? (list[j] == li) : true;
-    const float Hdetj = aj * aj * aj;
+    if (TENSOR) {   // H_j through the mirrors of the entry
+      const uint32_t mq = (uint32_t)dcode & mm;
+      if (mq) {
+        const float sx = (mq & 3u) ? -1.f : 1.f, sy = (mq & 12u) ? -1.f : 1.f, sz = (mq & 48u) ? -1.f : 1.f;
+        hj0.y *= sx * sy;
+        hj0.z *= sx * sz;
+        hj1.x *= sy * sz;
+      }
+    }
+    const float Hdetj = TENSOR ? hj1.z : aj * aj * aj;
     const float irj = __frcp_rn(rhoj);
 
-    const float eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
-    const float ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
+    float eix, eiy, eiz, ejx, ejy, ejz;
+    if (TENSOR) {
+      symDot32(hi0, hi1, rx, ry, rz, eix, eiy, eiz);
+      symDot32(hj0, hj1, rx, ry, rz, ejx, ejy, ejz);
+    } else {
+      eix = ai * rx; eiy = ai * ry; eiz = ai * rz;
+      ejx = aj * rx; ejy = aj * ry; ejz = aj * rz;
+    }
     const float e2i = __fmaf_rn(eiz, eiz, __fmaf_rn(eiy, eiy, __fmul_rn(eix, eix)));
     const float e2j = __fmaf_rn(ejz, ejz, __fmaf_rn(ejy, ejy, __fmul_rn(ejx, ejx)));
     const float ri = rsqrtf(fmaxf(e2i, 1.0e-30f)), rj = rsqrtf(fmaxf(e2j, 1.0e-30f));
@@ -182,10 +210,21 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     Wi *= Hdeti;
     Wj *= Hdetj;
     // gradW = gW H eta/|eta|
-    const float fi = __fmul_rn(__fmul_rn(__fmul_rn(Hdeti, gi), ai), ri);
-    const float fj = __fmul_rn(__fmul_rn(__fmul_rn(Hdetj, gj), aj), rj);
-    const float gwix = fi * eix, gwiy = fi * eiy, gwiz = fi * eiz;
-    const float gwjx = fj * ejx, gwjy = fj * ejy, gwjz = fj * ejz;
+    float gwix, gwiy, gwiz, gwjx, gwjy, gwjz;
+    if (TENSOR) {
+      const float fi = __fmul_rn(__fmul_rn(Hdeti, gi), ri);
+      const float fj = __fmul_rn(__fmul_rn(Hdetj, gj), rj);
+      float hx, hy, hz;
+      symDot32(hi0, hi1, eix, eiy, eiz, hx, hy, hz);
+      gwix = __fmul_rn(fi, hx); gwiy = __fmul_rn(fi, hy); gwiz = __fmul_rn(fi, hz);
+      symDot32(hj0, hj1, ejx, ejy, ejz, hx, hy, hz);
+      gwjx = __fmul_rn(fj, hx); gwjy = __fmul_rn(fj, hy); gwjz = __fmul_rn(fj, hz);
+    } else {
+      const float fi = __fmul_rn(__fmul_rn(__fmul_rn(Hdeti, gi), ai), ri);
+      const float fj = __fmul_rn(__fmul_rn(__fmul_rn(Hdetj, gj), aj), rj);
+      gwix = fi * eix; gwiy = fi * eiy; gwiz = fi * eiz;
+      gwjx = fj * ejx; gwjy = fj * ejy; gwjz = fj * ejz;
+    }
 
     if (same) {
       rhoSum += mj * Wi;
@@ -283,6 +322,13 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     const float fwW = fw * WSPHi;
     m0 += fwW;
     m1x -= fwW * eix; m1y -= fwW * eiy; m1z -= fwW * eiz;
+    if (TENSOR) {   // ASPHClassicSmoothingScale second moment: WSPH^2 r r / |r|^5
+      const float ir = rsqrtf(fmaxf(rx * rx + ry * ry + rz * rz, 1.0e-30f));
+      const float ir2 = ir * ir;
+      const float w = fwW * WSPHi * (ir2 * ir2 * ir);
+      m2[0] += w * (rx * rx); m2[1] += w * (rx * ry); m2[2] += w * (rx * rz);
+      m2[3] += w * (ry * ry); m2[4] += w * (ry * rz); m2[5] += w * (rz * rz);
+    }
   }
   NodeAcc32 a;
   a.rhoSum = rhoSum; a.norm = norm;
@@ -293,12 +339,17 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   a.m0 = m0; a.m1x = m1x; a.m1y = m1y; a.m1z = m1z;
 #pragma unroll
   for (int k = 0; k < 9; ++k) { a.D[k] = D[k]; a.M[k] = M[k]; }
-  finalizeNode32(F, i, MULTI ? li : list[i], a, cnt, hp, t.herm);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.m2[k] = m2[k];
+  a.h0 = hi0;
+  a.h1 = hi1;
+  finalizeNode32<TENSOR>(F, i, MULTI ? li : list[i], a, cnt, hp, t.herm);
 }
 
 //------------------------------------------------------------------------------
 // Density sum, FP32 (computeSPHSumMassDensity.cc:15-87, gathered).
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                           Grid g, NeighborLists nl, TableDev t, HydroParams hp) {
   __shared__ float tw[kMaxTable];
@@ -326,16 +377,26 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
     const float4 pj = P.posh[j];
     float rx, ry, rz;
     relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
-    const float aj = pj.w;
-    const float eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+    float eta, Hdj;
+    if (TENSOR) {   // |H_j r| with H_j through the mirrors
+      float4 h0, h1;
+      loadTensor32(P, j, (uint32_t)dcode & mm, h0, h1);
+      eta = sqrtf(eta2Sym32(h0, h1, rx, ry, rz));
+      Hdj = h1.z;
+    } else {
+      const float aj = pj.w;
+      eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+      Hdj = aj * aj * aj;
+    }
     if (eta < extent) {
       const int i0 = 3 * min(N1, (int)(eta * invStep));
-      const float w = (aj * aj * aj) * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
+      const float w = Hdj * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
       kahanAdd(s, c, ((multi ? list[j] == li : true) ? P.velm[j].w : mi) * w);
     }
   }
   const double a = F.f[F_HINV][i];
-  const double self = F.f[F_MASS][i] * (((a * a) * a) * hp.W0);
+  const double Hdeti = TENSOR ? symDet(loadSym(F, F_HT_XX, i)) : (a * a) * a;
+  const double self = F.f[F_MASS][i] * (Hdeti * hp.W0);
   const double rho = self + kahanValue(s, c);
   F.f[F_RHO][i] = rho;
   P.thermo[i].x = (float)rho;
@@ -347,6 +408,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
 // (GenericHydro.cc:113-381, pairwise velocity limit on the same neighbour
 // data, node limits with the new density) in one pass over the lists.
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                          Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                          double maxNperh, double* __restrict__ part) {
@@ -371,33 +433,54 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
     const int N1 = hp.tableN1;
     float s = 0.f, c = 0.f, worstPair = 0.0f;
+    // the node scale of GenericHydro::dt: 1/h, the largest eigenvalue of H
+    const float lmaxi = TENSOR ? P.hten[2 * i + 1].w : pi.w;
     const int cnt = nl.count[i];
     // software pipeline: entry two slots ahead, node data one slot ahead
     uint32_t entA = 0u, entB = 0u;
-    float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA;
+    float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA, hA0 = pjA, hA1 = pjA;
     if (cnt > 0) {
       entA = nl.nbr[nbSlot(i, 0, nl.cap)];
       const int j0 = (int)(entA & kIndexMask);
       pjA = P.posh[j0]; vjA = P.velm[j0];
+      if (TENSOR) { hA0 = P.hten[2 * j0]; hA1 = P.hten[2 * j0 + 1]; }
     }
     if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
     for (int q = 0; q < cnt; ++q) {
       const uint32_t ent = entA;
       const float4 pj = pjA, vj = vjA;
+      float4 h0 = hA0, h1 = hA1;
       if (q + 1 < cnt) {
         const int jn = (int)(entB & kIndexMask);
         pjA = P.posh[jn]; vjA = P.velm[jn];
+        if (TENSOR) { hA0 = P.hten[2 * jn]; hA1 = P.hten[2 * jn + 1]; }
         entA = entB;
       }
       if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
       const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
       float rx, ry, rz;
       relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
-      const float aj = pj.w;
-      const float eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+      float eta, Hdj, lmaxj;
+      if (TENSOR) {   // |H_j r| with H_j through the mirrors
+        const uint32_t mq = (uint32_t)dcode & mm;
+        if (mq) {
+          const float sx = (mq & 3u) ? -1.f : 1.f, sy = (mq & 12u) ? -1.f : 1.f, sz = (mq & 48u) ? -1.f : 1.f;
+          h0.y *= sx * sy;
+          h0.z *= sx * sz;
+          h1.x *= sy * sz;
+        }
+        eta = sqrtf(eta2Sym32(h0, h1, rx, ry, rz));
+        Hdj = h1.z;
+        lmaxj = h1.w;
+      } else {
+        const float aj = pj.w;
+        eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+        Hdj = aj * aj * aj;
+        lmaxj = aj;
+      }
       if (eta < extent) {
         const int i0 = 3 * min(N1, (int)(eta * invStep));
-        const float w = (aj * aj * aj) * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
+        const float w = Hdj * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
         kahanAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w);
       }
       float vxj = vj.x, vyj = vj.y, vzj = vj.z;
@@ -405,12 +488,13 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
       const float dx = vi.x - vxj, dy = vi.y - vyj, dz = vi.z - vzj;
       // min over pairs of min(h_i, h_j)/|v_ij| = 1/sqrt(max over pairs of
       // (max(a_i, a_j) |v_ij|)^2): no division or root per pair
-      const float am = fmaxf(pi.w, aj);
+      const float am = fmaxf(lmaxi, lmaxj);
       worstPair = fmaxf(worstPair, (am * am) * (dx * dx + dy * dy + dz * dz));
     }
     const float bestPair = worstPair > 0.0f ? rsqrtf(worstPair) : 3.0e38f;
     const double a = F.f[F_HINV][i];
-    const double rho = F.f[F_MASS][i] * (((a * a) * a) * hp.W0) + kahanValue(s, c);
+    const double Hdeti = TENSOR ? symDet(loadSym(F, F_HT_XX, i)) : (a * a) * a;
+    const double rho = F.f[F_MASS][i] * (Hdeti * hp.W0) + kahanValue(s, c);
     F.f[F_RHO][i] = rho;
     P.thermo[i].x = (float)rho;
     // Node limits of GenericHydro::dt in FP32 (the vote only picks the
@@ -418,7 +502,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     // the sweep otherwise).
     const float tiny = (float)DBL_EPSILON;
     const NodeListParams L = hp.lists[multi ? li : list[i]];
-    const float nodeScalei = 1.0f / (pi.w * (float)L.nPerh);
+    const float nodeScalei = 1.0f / (lmaxi * (float)L.nPerh);
     float bestf = 3.0e38f;
     const float csDt = nodeScalei / (P.thermo[i].z + tiny);
     if (csDt < bestf) { bestf = csDt; reason = 0; }
@@ -455,6 +539,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
 //------------------------------------------------------------------------------
 // Grad-h correction, FP32 sums (computeSPHOmegaGradhCorrection.cc:15-116).
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl,
                                                      TableDev t, HydroParams hp) {
   __shared__ float4 ta[kMaxTable / 3];
@@ -470,6 +555,8 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
   const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
   const float4 pi = P.posh[i];
   const float ai = pi.w;
+  float4 hi0 = make_float4(0.f, 0.f, 0.f, 0.f), hi1 = hi0;
+  if (TENSOR) { hi0 = P.hten[2 * i]; hi1 = P.hten[2 * i + 1]; }
   const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
   const int N1 = hp.tableN1;
   float ws = 0.f, wc = 0.f, gs = 0.f, gc = 0.f;
@@ -493,7 +580,7 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
     const int dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
     relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
-    const float eta = ai * sqrtf(rx * rx + ry * ry + rz * rz);
+    const float eta = TENSOR ? sqrtf(eta2Sym32(hi0, hi1, rx, ry, rz)) : ai * sqrtf(rx * rx + ry * ry + rz * rz);
     float w, gr;
     lookupPacked(ta, tb, N1, invStep, eta, extent, w, gr);
     kahanAdd(ws, wc, w);
@@ -510,6 +597,7 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
 //------------------------------------------------------------------------------
 // GenericHydro::dt with the pairwise velocity limit in FP32.
 //------------------------------------------------------------------------------
+template <bool TENSOR>
 __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n, Grid g,
                                                   NeighborLists nl, HydroParams hp, double maxNperh,
                                                   double* __restrict__ part) {
@@ -524,7 +612,7 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
     unpackCell(P.cell[i], ci);
     const uint32_t mm = mirrorMask(g, ci);
     const NodeListParams L = hp.lists[list[i]];
-    const double ai = F.f[F_HINV][i];
+    const double ai = F.f[TENSOR ? F_HLMAX : F_HINV][i];   // largest eigenvalue of H
     const double nodeScalei = 1.0 / ai / L.nPerh;
     const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
     const double rhoi = F.f[F_RHO][i];
@@ -543,7 +631,7 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
       if (velDt < best) { best = velDt; reason = 4; }
     }
     const float4 vi = P.velm[i];
-    const float hi = 1.0f / P.posh[i].w;
+    const float hi = 1.0f / (TENSOR ? P.hten[2 * i + 1].w : P.posh[i].w);
     float bestPair = 3.0e38f;
     const int cnt = nl.count[i];
     for (int q = 0; q < cnt; ++q) {
@@ -554,7 +642,7 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
       float vxj = vj.x, vyj = vj.y, vzj = vj.z;
       mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
       const float dx = vi.x - vxj, dy = vi.y - vyj, dz = vi.z - vzj;
-      const float hmin = fminf(hi, 1.0f / P.posh[j].w);
+      const float hmin = fminf(hi, 1.0f / (TENSOR ? P.hten[2 * j + 1].w : P.posh[j].w));
       const float dtv = hmin / fmaxf(1.0e-30f, sqrtf(dx * dx + dy * dy + dz * dz));
       bestPair = fminf(bestPair, dtv);
     }
@@ -710,8 +798,18 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
 #define SPH_PAIR32(X, C, M, MB, PF, LQ) \
-  pairKernelFP32<X, C, M, MB, PF, LQ><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
-  if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity: one variant per path
+  pairKernelFP32<X, C, M, MB, PF, LQ, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
+#define SPH_PAIR32T(X, C, LQ) \
+  pairKernelFP32<X, C, true, 3, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
+  if (hp.asph) {   // ASPH (tensor H): pipelined, NodeList test at run time, up to 168 registers
+    if (hp.xsph) {
+      if (hp.compatible) { if (hp.limitedQ) SPH_PAIR32T(true, true, true); else SPH_PAIR32T(true, true, false); }
+      else { if (hp.limitedQ) SPH_PAIR32T(true, false, true); else SPH_PAIR32T(true, false, false); }
+    } else {
+      if (hp.compatible) { if (hp.limitedQ) SPH_PAIR32T(false, true, true); else SPH_PAIR32T(false, true, false); }
+      else { if (hp.limitedQ) SPH_PAIR32T(false, false, true); else SPH_PAIR32T(false, false, false); }
+    }
+  } else if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity: one variant per path
     if (!hp.xsph && hp.compatible && !multi) SPH_PAIR32(false, true, false, 4, true, true);
     else if (hp.xsph) {
       if (hp.compatible) SPH_PAIR32(true, true, true, 4, false, true);
@@ -740,18 +838,21 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
     else { if (multi) SPH_PAIR32(false, false, true, 5, false, false); else SPH_PAIR32(false, false, false, 5, false, false); }
   }
 #undef SPH_PAIR32
+#undef SPH_PAIR32T
   lc->add(1);
 }
 
 void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                           HydroParams hp, cudaStream_t s, LaunchCounter* lc) {
-  sumDensityKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, F32, list, n, g, nl, t, hp);
+  if (hp.asph) sumDensityKernel32<true><<<gridFor(n, 128), 128, 0, s>>>(F, F32, list, n, g, nl, t, hp);
+  else sumDensityKernel32<false><<<gridFor(n, 128), 128, 0, s>>>(F, F32, list, n, g, nl, t, hp);
   lc->add(1);
 }
 
 void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                      cudaStream_t s, LaunchCounter* lc) {
-  gradhKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  if (hp.asph) gradhKernel32<true><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  else gradhKernel32<false><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
   lc->add(1);
 }
 
@@ -760,7 +861,8 @@ void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Neigh
                   cudaStream_t s, LaunchCounter* lc) {
   (void)nScratch;
   const int nb = (int)gridFor(n, 128);
-  dtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
+  if (hp.asph) dtKernel32<true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
+  else dtKernel32<false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
 }
@@ -776,7 +878,8 @@ void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g
                          HydroParams hp, double maxNperh, double* dScratch,
                          double* dOut, cudaStream_t s, LaunchCounter* lc) {
   const int nb = (int)gridFor(n, 128);
-  densityDtKernel32<<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  if (hp.asph) densityDtKernel32<true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  else densityDtKernel32<false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
 }

@@ -1,23 +1,39 @@
 // Symmetric 3x3 tensors of the ASPH path (tensor H) on the device: loads
 // and stores in the field bank, images through reflecting walls, the
 // closed-form eigenvalues used by the reference for H's extent, a Jacobi
-// eigen-decomposition for the tensor functions (bounds, square root) and the
-// ASPH tensor DH/Dt.
+// eigen-decomposition for the tensor functions (bounds, square root), the
+// ASPH tensor DH/Dt and the ASPHClassicSmoothingScale shape of Hideal.  The
+// tensor functions are templated on the arithmetic type: FP64 for the FP64
+// mode, FP32 for the per-node tail of the mixed mode.
 #pragma once
+#include <cfloat>
 #include "fields.cuh"
 
 namespace sph {
 namespace dev {
 
-struct Sym {
-  double xx, xy, xz, yy, yz, zz;
+template <class T>
+struct SymT {
+  T xx, xy, xz, yy, yz, zz;
+};
+using Sym = SymT<double>;
+
+template <class T> struct TensorEps;
+template <> struct TensorEps<double> {
+  static constexpr double eps = DBL_EPSILON;
+  static constexpr double offStop = 1.0e-40;   // squared off-diagonal norm ending the Jacobi sweeps
+};
+template <> struct TensorEps<float> {
+  static constexpr float eps = FLT_EPSILON;
+  static constexpr float offStop = 1.0e-14f;
 };
 
 __device__ __forceinline__ Sym loadSym(const Fields& F, int first, long i) {
   return Sym{F.f[first][i], F.f[first + 1][i], F.f[first + 2][i], F.f[first + 3][i], F.f[first + 4][i],
              F.f[first + 5][i]};
 }
-__device__ __forceinline__ void storeSym(Fields& F, int first, long i, const Sym& h) {
+template <class T>
+__device__ __forceinline__ void storeSym(Fields& F, int first, long i, const SymT<T>& h) {
   F.f[first][i] = h.xx;
   F.f[first + 1][i] = h.xy;
   F.f[first + 2][i] = h.xz;
@@ -55,24 +71,29 @@ __device__ __forceinline__ double eta2ExactSym(const Sym& h, double x, double y,
   return __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
 }
 // GeomSymmetricTensor<3>::Determinant (GeomSymmetricTensorInline.hh:1740-1747)
-__device__ __forceinline__ double symDet(const Sym& h) {
+template <class T>
+__device__ __forceinline__ T symDet(const SymT<T>& h) {
   return (h.xx * h.yy * h.zz + h.xy * h.yz * h.xz + h.xz * h.xy * h.yz - h.xx * h.yz * h.yz - h.xy * h.xy * h.zz -
           h.xz * h.yy * h.xz);
 }
-__device__ __forceinline__ double symMaxAbs(const Sym& h) {
+template <class T>
+__device__ __forceinline__ T symMaxAbs(const SymT<T>& h) {
   return fmax(fabs(h.xx), fmax(fabs(h.xy), fmax(fabs(h.xz), fmax(fabs(h.yy), fmax(fabs(h.yz), fabs(h.zz))))));
 }
-__device__ __forceinline__ Sym symScale(const Sym& h, double s) {
-  return Sym{h.xx * s, h.xy * s, h.xz * s, h.yy * s, h.yz * s, h.zz * s};
+template <class T>
+__device__ __forceinline__ SymT<T> symScale(const SymT<T>& h, T s) {
+  return SymT<T>{h.xx * s, h.xy * s, h.xz * s, h.yy * s, h.yz * s, h.zz * s};
 }
-__device__ __forceinline__ Sym symDiv(const Sym& h, double s) {
-  return Sym{h.xx / s, h.xy / s, h.xz / s, h.yy / s, h.yz / s, h.zz / s};
+template <class T>
+__device__ __forceinline__ SymT<T> symDiv(const SymT<T>& h, T s) {
+  return SymT<T>{h.xx / s, h.xy / s, h.xz / s, h.yy / s, h.yz / s, h.zz / s};
 }
 // GeomSymmetricTensor<3>::Inverse (GeomSymmetricTensorInline.hh:1650-1661)
-__device__ __forceinline__ Sym symInverse(const Sym& a) {
-  const double d = symDet(a);
-  return Sym{(a.yy * a.zz - a.yz * a.yz) / d, (a.yz * a.xz - a.xy * a.zz) / d, (a.xy * a.yz - a.yy * a.xz) / d,
-             (a.xx * a.zz - a.xz * a.xz) / d, (a.xy * a.xz - a.xx * a.yz) / d, (a.xx * a.yy - a.xy * a.xy) / d};
+template <class T>
+__device__ __forceinline__ SymT<T> symInverse(const SymT<T>& a) {
+  const T d = symDet(a);
+  return SymT<T>{(a.yy * a.zz - a.yz * a.yz) / d, (a.yz * a.xz - a.xy * a.zz) / d, (a.xy * a.yz - a.yy * a.xz) / d,
+                 (a.xx * a.zz - a.xz * a.xz) / d, (a.xy * a.xz - a.xx * a.yz) / d, (a.xx * a.yy - a.xy * a.xy) / d};
 }
 
 // Closed-form eigenvalues (GeomSymmetricTensor<3>::eigenValues,
@@ -106,37 +127,38 @@ __device__ __forceinline__ void symEigenValues(const Sym& h, double ev[3]) {
 // rotations; V[r][k] is component r of eigenvector k.  Every caller applies a
 // function to the eigenvalues and rotates back (V f(lambda) V^T), which does
 // not depend on the order or signs of the pairs.
-__device__ __forceinline__ void symEigen(const Sym& h, double val[3], double V[3][3]) {
-  const double fscale = fmax(10.0 * DBL_EPSILON, symMaxAbs(h));
-  const double fi = 1.0 / fscale;
-  auto z = [](double x) { return fabs(x) < 1.0e-20 ? 0.0 : x; };
-  double a00 = z(h.xx * fi), a01 = z(h.xy * fi), a02 = z(h.xz * fi);
-  double a11 = z(h.yy * fi), a12 = z(h.yz * fi), a22 = z(h.zz * fi);
+template <class T>
+__device__ __forceinline__ void symEigen(const SymT<T>& h, T val[3], T V[3][3]) {
+  const T fscale = fmax(T(10) * TensorEps<T>::eps, symMaxAbs(h));
+  const T fi = T(1) / fscale;
+  auto z = [](T x) { return fabs(x) < T(1.0e-20) ? T(0) : x; };
+  T a00 = z(h.xx * fi), a01 = z(h.xy * fi), a02 = z(h.xz * fi);
+  T a11 = z(h.yy * fi), a12 = z(h.yz * fi), a22 = z(h.zz * fi);
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) V[r][k] = r == k ? 1.0 : 0.0;
+    for (int k = 0; k < 3; ++k) V[r][k] = r == k ? T(1) : T(0);
   // one rotation in the (p, q) plane; o is the third index
-  auto rot = [&](double& app, double& aqq, double& apq, double& aop, double& aoq, int p, int q) {
-    if (apq == 0.0) return;
-    const double theta = (aqq - app) / (2.0 * apq);
-    const double t = (theta < 0.0 ? -1.0 : 1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-    const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+  auto rot = [&](T& app, T& aqq, T& apq, T& aop, T& aoq, int p, int q) {
+    if (apq == T(0)) return;
+    const T theta = (aqq - app) / (T(2) * apq);
+    const T t = (theta < T(0) ? T(-1) : T(1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+    const T c = T(1) / sqrt(t * t + T(1)), s = t * c;
     app -= t * apq;
     aqq += t * apq;
-    apq = 0.0;
-    const double op = aop, oq = aoq;
+    apq = T(0);
+    const T op = aop, oq = aoq;
     aop = c * op - s * oq;
     aoq = s * op + c * oq;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double vp = V[k][p], vq = V[k][q];
+      const T vp = V[k][p], vq = V[k][q];
       V[k][p] = c * vp - s * vq;
       V[k][q] = s * vp + c * vq;
     }
   };
   for (int sweep = 0; sweep < 32; ++sweep) {
-    if (a01 * a01 + a02 * a02 + a12 * a12 <= 1.0e-40) break;
+    if (a01 * a01 + a02 * a02 + a12 * a12 <= TensorEps<T>::offStop) break;
     rot(a00, a11, a01, a02, a12, 0, 1);   // plane (0,1); third index 2: a20, a21
     rot(a00, a22, a02, a01, a12, 0, 2);   // plane (0,2); third index 1: a10, a12
     rot(a11, a22, a12, a01, a02, 1, 2);   // plane (1,2); third index 0: a01, a02
@@ -146,16 +168,17 @@ __device__ __forceinline__ void symEigen(const Sym& h, double val[3], double V[3
   val[2] = a22 * fscale;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double nrm = 1.0 / sqrt(V[0][k] * V[0][k] + V[1][k] * V[1][k] + V[2][k] * V[2][k]);
+    const T nrm = T(1) / sqrt(V[0][k] * V[0][k] + V[1][k] * V[1][k] + V[2][k] * V[2][k]);
 #pragma unroll
     for (int r = 0; r < 3; ++r) V[r][k] *= nrm;
   }
 }
 
 // diag(d) in the frame of the eigenvectors (rotationalTransform).
-__device__ __forceinline__ Sym symFromEigen(const double d[3], const double V[3][3]) {
+template <class T>
+__device__ __forceinline__ SymT<T> symFromEigen(const T d[3], const T V[3][3]) {
   auto el = [&](int i, int j) { return V[i][0] * d[0] * V[j][0] + V[i][1] * d[1] * V[j][1] + V[i][2] * d[2] * V[j][2]; };
-  return Sym{el(0, 0), el(0, 1), el(0, 2), el(1, 1), el(1, 2), el(2, 2)};
+  return SymT<T>{el(0, 0), el(0, 1), el(0, 2), el(1, 1), el(1, 2), el(2, 2)};
 }
 
 // min(maxv, max(minv, H)) for a SymTensor and scalar bounds: enforceMinEigenValue
@@ -185,28 +208,108 @@ __device__ __forceinline__ Sym symBound(const Sym& h, double minv, double maxv) 
 // ASPH tensor DH/Dt for Dim<3> (SmoothingScaleUtilities.hh,
 // smoothingScaleDerivative): the rate of H under DvDx (row-major 9) with the
 // frame rotation removed.
-__device__ __forceinline__ Sym smoothingScaleDerivative(const Sym& H, const double* D) {
-  const double Dxx = D[0], Dxy = D[1], Dxz = D[2], Dyx = D[3], Dyy = D[4], Dyz = D[5], Dzx = D[6], Dzy = D[7],
-               Dzz = D[8];
-  const double AA = H.xx * Dxy - H.xy * (Dxx - Dyy) + H.xz * Dzy - H.yy * Dyx - H.yz * Dzx;
-  const double BB = H.xx * Dxz + H.xy * Dyz - H.xz * (Dxx - Dzz) - H.yz * Dyx - H.zz * Dzx;
-  const double CC = H.xy * Dxz + H.yy * Dyz - H.yz * (Dyy - Dzz) - H.xz * Dxy - H.zz * Dzy;
-  const double thpt = H.yy + H.zz;
-  const double Ga = (H.xx + H.yy) * thpt - H.xz * H.xz;
-  const double Gb = (H.yy + H.zz) * H.yz + H.xy * H.xz;
-  const double Gc = (H.xx + H.zz) * thpt - H.xy * H.xy;
-  const double Gd = thpt * AA + H.xz * CC;
-  const double Ge = thpt * BB - H.xy * CC;
-  const double ack = 1.0 / (Ga * Gc - Gb * Gb);
-  const double Gdot = (Gc * Gd - Gb * Ge) * ack;
-  const double Tdot = (Gb * Gd - Ga * Ge) * ack;
-  const double Phidot = (H.xz * Gdot + H.xy * Tdot + CC) / thpt;
-  return Sym{-H.xx * Dxx + H.xy * (Gdot - Dyx) - H.xz * (Tdot + Dzx),
-             H.yy * Gdot - H.yz * Tdot - H.xx * Dxy - H.xy * Dyy - H.xz * Dzy,
-             H.yz * Gdot - H.zz * Tdot - H.xx * Dxz - H.xy * Dyz - H.xz * Dzz,
-             H.yz * (Phidot - Dzy) - H.xy * (Gdot + Dxy) - H.yy * Dyy,
-             H.xy * Tdot - H.yy * Phidot - H.xz * Dxy - H.yz * Dyy - H.zz * Dzy,
-             H.xz * (Tdot - Dxz) - H.yz * (Phidot + Dyz) - H.zz * Dzz};
+template <class T>
+__device__ __forceinline__ SymT<T> smoothingScaleDerivative(const SymT<T>& H, const T* D) {
+  const T Dxx = D[0], Dxy = D[1], Dxz = D[2], Dyx = D[3], Dyy = D[4], Dyz = D[5], Dzx = D[6], Dzy = D[7], Dzz = D[8];
+  const T AA = H.xx * Dxy - H.xy * (Dxx - Dyy) + H.xz * Dzy - H.yy * Dyx - H.yz * Dzx;
+  const T BB = H.xx * Dxz + H.xy * Dyz - H.xz * (Dxx - Dzz) - H.yz * Dyx - H.zz * Dzx;
+  const T CC = H.xy * Dxz + H.yy * Dyz - H.yz * (Dyy - Dzz) - H.xz * Dxy - H.zz * Dzy;
+  const T thpt = H.yy + H.zz;
+  const T Ga = (H.xx + H.yy) * thpt - H.xz * H.xz;
+  const T Gb = (H.yy + H.zz) * H.yz + H.xy * H.xz;
+  const T Gc = (H.xx + H.zz) * thpt - H.xy * H.xy;
+  const T Gd = thpt * AA + H.xz * CC;
+  const T Ge = thpt * BB - H.xy * CC;
+  const T ack = T(1) / (Ga * Gc - Gb * Gb);
+  const T Gdot = (Gc * Gd - Gb * Ge) * ack;
+  const T Tdot = (Gb * Gd - Ga * Ge) * ack;
+  const T Phidot = (H.xz * Gdot + H.xy * Tdot + CC) / thpt;
+  return SymT<T>{-H.xx * Dxx + H.xy * (Gdot - Dyx) - H.xz * (Tdot + Dzx),
+                 H.yy * Gdot - H.yz * Tdot - H.xx * Dxy - H.xy * Dyy - H.xz * Dzy,
+                 H.yz * Gdot - H.zz * Tdot - H.xx * Dxz - H.xy * Dyz - H.xz * Dzz,
+                 H.yz * (Phidot - Dzy) - H.xy * (Gdot + Dxy) - H.yy * Dyy,
+                 H.xy * Tdot - H.yy * Phidot - H.xz * Dxy - H.yz * Dyy - H.zz * Dzy,
+                 H.xz * (Tdot - Dxz) - H.yz * (Phidot + Dyz) - H.zz * Dzz};
+}
+
+template <class T> __device__ __forceinline__ T rootnu3T(T x) { return (x < T(0) ? T(-1) : T(1)) * pow(fabs(x), T(1) / T(3)); }
+template <> __device__ __forceinline__ double rootnu3T<double>(double x) {
+  return (x < 0.0 ? -1.0 : 1.0) * pow(fabs(x), 0.3333333333333333);
+}
+
+// Hideal of ASPHClassicSmoothingScale (ASPHClassicSmoothingScale.cc:205-288)
+// from the second moment M2 of the neighbour distribution, H, the ratio s of
+// the target to the current nodes per smoothing scale and the NodeList
+// limits: the shape from the normalised M2 (eigenvalues of psi^-1/2 floored
+// at hminratio of the largest; identity when M2 is not positive definite or
+// psiweight is zero), the size as in the SPH IdealH (or H rescaled, with
+// fixShape), then the eigenvalues bounded by 1/hmax and
+// min(1/hmin, max(1/hmax, smallest) / hminratio).
+template <class T>
+__device__ __forceinline__ SymT<T> asphClassicHideal(const SymT<T>& M2, bool m2Positive, const SymT<T>& Hi, T s,
+                                                     bool fixShape, T hminInv, T hmaxInv, T hminratio) {
+  const T tiny = T(1.0e-50);
+  const T psiweight = fmax(T(0), fmin(T(1), T(2) / s - T(1)));
+  SymT<T> Hid{T(1), T(0), T(0), T(1), T(0), T(1)};
+  T ev[3], V[3][3], d[3];
+  if (psiweight > T(0) && symDet(M2) > T(0) && m2Positive) {
+    SymT<T> psi = symDiv(M2, symMaxAbs(M2));
+    const T dp = symDet(psi);
+    if (dp > T(1.0e-10)) psi = symDiv(psi, rootnu3T(fabs(dp) + tiny));
+    else psi = SymT<T>{T(1), T(0), T(0), T(1), T(0), T(1)};
+    symEigen(psi, ev, V);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ev[k] = T(1) / sqrt(ev[k]);
+    const T psimin = fmax(ev[0], fmax(ev[1], ev[2])) * hminratio;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = fmax(psimin, ev[k]);
+    psi = symFromEigen(d, V);
+    psi = symDiv(psi, rootnu3T(symDet(psi) + tiny));
+    symEigen(psi, ev, V);   // psi^(1/2), then its inverse
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = sqrt(fmax(T(0), ev[k]));
+    Hid = symInverse(symFromEigen(d, V));
+  }
+  const T aa = s < T(1) ? T(0.4) * (T(1) + s * s) : T(0.4) * (T(1) + T(1) / (s * s * s + tiny));
+  if (fixShape) Hid = symDiv(Hi, T(1) - aa + aa * s);
+  else Hid = symScale(Hid, rootnu3T(symDet(Hi)) / (T(1) - aa + aa * s));
+  symEigen(Hid, ev, V);
+  const T hminEffInv = fmin(hminInv, fmax(hmaxInv, fmin(ev[0], fmin(ev[1], ev[2]))) / hminratio);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = fmax(hmaxInv, fmin(hminEffInv, ev[k]));
+  return symFromEigen(d, V);
+}
+
+// FP32 mirror of tensor H for the FP32 sweeps and the neighbour pre-filter:
+// (xx xy xz yy) (yz zz det(H) lambda_max).
+__device__ __forceinline__ void writeTensorMirror(const Fields& F, const Fields32& P, long i) {
+  const Sym h = loadSym(F, F_HT_XX, i);
+  P.hten[2 * i] = make_float4((float)h.xx, (float)h.xy, (float)h.xz, (float)h.yy);
+  P.hten[2 * i + 1] = make_float4((float)h.yz, (float)h.zz, (float)symDet(h), (float)F.f[F_HLMAX][i]);
+}
+// H_j of a neighbour entry from the mirror, seen through the mirror-axis bits
+// mir (dcode layout) of the entry.
+__device__ __forceinline__ void loadTensor32(const Fields32& P, int j, uint32_t mir, float4& a, float4& b) {
+  a = P.hten[2 * j];
+  b = P.hten[2 * j + 1];
+  if (mir) {
+    const float sx = (mir & 3u) ? -1.f : 1.f, sy = (mir & 12u) ? -1.f : 1.f, sz = (mir & 48u) ? -1.f : 1.f;
+    a.y *= sx * sy;
+    a.z *= sx * sz;
+    b.x *= sy * sz;
+  }
+}
+// H r in FP32 from the mirror (a = xx xy xz yy, b = yz zz . .), fixed order.
+__device__ __forceinline__ void symDot32(const float4& a, const float4& b, float x, float y, float z, float& ox,
+                                         float& oy, float& oz) {
+  ox = __fmaf_rn(a.z, z, __fmaf_rn(a.y, y, __fmul_rn(a.x, x)));
+  oy = __fmaf_rn(b.x, z, __fmaf_rn(a.w, y, __fmul_rn(a.y, x)));
+  oz = __fmaf_rn(b.y, z, __fmaf_rn(b.x, y, __fmul_rn(a.z, x)));
+}
+__device__ __forceinline__ float eta2Sym32(const float4& a, const float4& b, float x, float y, float z) {
+  float ex, ey, ez;
+  symDot32(a, b, x, y, z, ex, ey, ez);
+  return __fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex)));
 }
 
 // Derived extent of a tensor H: smallest and largest eigenvalue.
