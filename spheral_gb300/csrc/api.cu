@@ -159,7 +159,7 @@ struct sphgpu_ctx {
   int itemBound = 0;         // upper bound on the number of work items
   DBuf itemCount;            // device: number of work items
   bool capCheckPending = false, totalPending = false;
-  double cachedBounds[7] = {};   // min h^-1, min x y z, max x y z of the current state
+  double cachedBounds[kBoundsVals] = {};   // min h^-1, min x y z, max x y z, tensor extents of the current state
   bool boundsValid = false;      // cachedBounds describe the current state
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
   bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
@@ -330,10 +330,10 @@ void buildGrid(sphgpu_ctx* c) {
   Scope sc(c->prof, "bounds");
   if (!c->boundsValid) {   // the bounds of the last step's check describe a changed state
     double* d = c->small.as<double>() + 20;
-    c->scratch.ensure(7 * sizeof(double) * 4096);
-    launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, d, c->stream, &c->lc);
+    c->scratch.ensure(kBoundsVals * sizeof(double) * 4096);
+    launchBounds(c->F, c->n, c->hp.asph != 0, c->scratch.as<double>(), kBoundsVals * 4096, d, c->stream, &c->lc);
     c->check();
-    CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, d, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, d, kBoundsVals * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CUDA_OK(cudaStreamSynchronize(c->stream));
     std::memcpy(c->cachedBounds, c->hsmall + 20, sizeof(c->cachedBounds));
   }
@@ -342,9 +342,14 @@ void buildGrid(sphgpu_ctx* c) {
   const double minHinv = bnd[0];
   if (!(minHinv > 0.0) || !std::isfinite(minHinv)) throw Error(SPHGPU_E_NAN, "non-positive or non-finite H");
   const double hmax = 1.0 / minHinv;
-  // tensor H: the smallest eigenvalue comes from the closed form, good to
-  // ~1e-8 relative near degenerate pairs; the margin covers it
-  const double support = c->hp.extent * hmax * (1.0 + (c->hp.asph ? 1.0e-6 : 1.0e-9));
+  const double support = c->hp.extent * hmax * (1.0 + 1.0e-9);
+  // tensor H: every neighbour r_ij lies in ext E_i or ext E_j (E the unit
+  // ellipsoid of H), whose half-width along axis a is sqrt((H^-2)_aa): the
+  // cells follow the largest half-width per axis (with a margin for the
+  // rounding of the inverse)
+  double supportAxis[3] = {support, support, support};
+  if (c->hp.asph)
+    for (int a = 0; a < 3; ++a) supportAxis[a] = c->hp.extent * bnd[7 + a] * (1.0 + 1.0e-9);
   Grid g{};
   for (int a = 0; a < 3; ++a) {
     g.kindLo[a] = g.kindHi[a] = AXIS_OPEN;
@@ -368,6 +373,7 @@ void buildGrid(sphgpu_ctx* c) {
     const double lo = g.kindLo[a] == AXIS_OPEN ? bnd[1 + a] : g.wallLo[a];
     const double hi = g.kindHi[a] == AXIS_OPEN ? bnd[4 + a] : g.wallHi[a];
     const double L = hi - lo;
+    const double support = supportAxis[a];
     int nc = (int)std::min(1024.0, std::floor(L / support));
     if (g.kindLo[a] == AXIS_PERIODIC) {
       if (nc < 3)
@@ -620,14 +626,14 @@ void evalDerivs(sphgpu_ctx* c) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
     // trial launches leave the same results) and keep the fastest.
-    // (the tensor-H kernel has a single variant: nothing to tune)
-    if (!c->pinnedVariant && !c->hp.asph && (c->pairVariant < 0 || c->tunedN != c->n)) {
+    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n)) {
       cudaEvent_t e0, e1;
       CUDA_OK(cudaEventCreate(&e0));
       CUDA_OK(cudaEventCreate(&e1));
       float best = 1e30f;
       int bestV = 1;
-      for (int v = 0; v < kPairVariants; ++v) {
+      const int nv = c->hp.asph ? kPairVariantsTensor : kPairVariants;
+      for (int v = 0; v < nv; ++v) {
         CUDA_OK(cudaEventRecord(e0, c->stream));
         launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                        c->pacc.as<float>(), v, c->stream, &c->lc);
@@ -712,9 +718,9 @@ void checkState(sphgpu_ctx* c, const char* where) {
   CUDA_OK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
   launchCheckState(c->F, c->n, flag, c->stream, &c->lc);
   double* b = c->small.as<double>() + 20;
-  c->scratch.ensure(7 * sizeof(double) * 4096);
-  launchBounds(c->F, c->n, c->scratch.as<double>(), 7 * 4096, b, c->stream, &c->lc);
-  CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, b, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  c->scratch.ensure(kBoundsVals * sizeof(double) * 4096);
+  launchBounds(c->F, c->n, c->hp.asph != 0, c->scratch.as<double>(), kBoundsVals * 4096, b, c->stream, &c->lc);
+  CUDA_OK(cudaMemcpyAsync(c->hsmall + 20, b, kBoundsVals * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaMemcpyAsync(c->hsmall + 30, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
   int h;
@@ -757,8 +763,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   }
   const double hdt = 0.5 * dt;
   {
-    Scope sc(c->prof, "update");
-    launchSaveState0(c->F, c->n, c->hp.asph != 0, c->stream, &c->lc);
+    Scope sc(c->prof, "update");   // the half-step update also saves state0
     const Fields32 m32 = c->f32();
     launchUpdate(c->F, c->listp(), c->n, c->hp, hdt, true, c->cfg.gravity != 0, c->fp32() ? &m32 : nullptr, c->grid,
                  c->stream, &c->lc);

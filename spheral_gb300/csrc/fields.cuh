@@ -42,10 +42,10 @@ enum FieldId {
   F_NUM_FIELDS
 };
 
-// Fields a permute moves (indices into Fields::f), chosen on the host.
-struct FieldSel {
+// Fields a permute moves: up to two index ranges [first, last) of Fields::f.
+struct FieldRanges {
   int n;
-  unsigned char id[F_NUM_PERMUTED];
+  int first[2], last[2];
 };
 
 struct Fields {

@@ -18,29 +18,40 @@ namespace {
 using namespace dev;
 
 //------------------------------------------------------------------------------
-// Bounds: min hinv and bounding box (for open axes).
+// Bounds: min hinv, bounding box (for open axes) and, for tensor H, the
+// largest half-width per axis of the unit ellipsoids {r : |H r| <= 1}, i.e.
+// sqrt((H^-2)_aa) = |row a of H^-1| (the cell edge per axis).
 //------------------------------------------------------------------------------
-__global__ void boundsKernel(Fields F, long n, double* __restrict__ part) {
+__global__ void boundsKernel(Fields F, long n, int tensor, double* __restrict__ part) {
   __shared__ double sm[32];
   double ah = DBL_MAX, mnx = DBL_MAX, mny = DBL_MAX, mnz = DBL_MAX, mxx = -DBL_MAX, mxy = -DBL_MAX, mxz = -DBL_MAX;
+  double ex = 0.0, ey = 0.0, ez = 0.0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     ah = fmin(ah, F.f[F_HINV][i]);
     const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i];
     mnx = fmin(mnx, x); mny = fmin(mny, y); mnz = fmin(mnz, z);
     mxx = fmax(mxx, x); mxy = fmax(mxy, y); mxz = fmax(mxz, z);
+    if (tensor) {
+      const Sym w = symInverse(loadSym(F, F_HT_XX, i));
+      ex = fmax(ex, sqrt(w.xx * w.xx + w.xy * w.xy + w.xz * w.xz));
+      ey = fmax(ey, sqrt(w.xy * w.xy + w.yy * w.yy + w.yz * w.yz));
+      ez = fmax(ez, sqrt(w.xz * w.xz + w.yz * w.yz + w.zz * w.zz));
+    }
   }
-  const double r[7] = {blockMin(ah, sm), blockMin(mnx, sm), blockMin(mny, sm), blockMin(mnz, sm),
-                       blockMax(mxx, sm), blockMax(mxy, sm), blockMax(mxz, sm)};
+  const double r[kBoundsVals] = {blockMin(ah, sm), blockMin(mnx, sm), blockMin(mny, sm), blockMin(mnz, sm),
+                                 blockMax(mxx, sm), blockMax(mxy, sm), blockMax(mxz, sm),
+                                 blockMax(ex, sm), blockMax(ey, sm), blockMax(ez, sm)};
   if (threadIdx.x == 0)
-    for (int k = 0; k < 7; ++k) part[blockIdx.x * 7 + k] = r[k];
+    for (int k = 0; k < kBoundsVals; ++k) part[blockIdx.x * kBoundsVals + k] = r[k];
 }
 __global__ void boundsFinalKernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
   __shared__ double sm[32];
-  double v[7];
-  for (int k = 0; k < 7; ++k) v[k] = k < 4 ? DBL_MAX : -DBL_MAX;
+  double v[kBoundsVals];
+  for (int k = 0; k < kBoundsVals; ++k) v[k] = k < 4 ? DBL_MAX : -DBL_MAX;
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
-    for (int k = 0; k < 7; ++k) v[k] = k < 4 ? fmin(v[k], part[b * 7 + k]) : fmax(v[k], part[b * 7 + k]);
-  for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < kBoundsVals; ++k)
+      v[k] = k < 4 ? fmin(v[k], part[b * kBoundsVals + k]) : fmax(v[k], part[b * kBoundsVals + k]);
+  for (int k = 0; k < kBoundsVals; ++k) {
     const double r = k < 4 ? blockMin(v[k], sm) : blockMax(v[k], sm);
     if (threadIdx.x == 0) out[k] = r;
   }
@@ -71,15 +82,13 @@ __global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ k
 __global__ void permuteKernel(Fields Fin, Fields Fout, const int* __restrict__ perm, const int* __restrict__ origIn,
                               int* __restrict__ origOut, const int* __restrict__ listIn, int* __restrict__ listOut,
                               const uint32_t* __restrict__ cellIn, uint32_t* __restrict__ cellOut, long n,
-                              FieldSel sel) {
+                              FieldRanges sel) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = perm[k];
+  for (int r = 0; r < sel.n; ++r)
 #pragma unroll 4
-  for (int q = 0; q < sel.n; ++q) {
-    const int f = sel.id[q];
-    Fout.f[f][k] = Fin.f[f][p];
-  }
+    for (int f = sel.first[r]; f < sel.last[r]; ++f) Fout.f[f][k] = Fin.f[f][p];
   origOut[k] = origIn[p];
   listOut[k] = listIn[p];
   cellOut[k] = cellIn[p];
@@ -122,6 +131,16 @@ __device__ __forceinline__ float tensorBand(float lmax, float lmin, const Grid& 
   const float u = 5.9604645e-8f;
   const float C = fmaxf(g.cellf[0], fmaxf(g.cellf[1], g.cellf[2]));
   return 4.0f * u * (60.0f * C * lmax / sqrtf(g.ext2f) + 24.0f * lmax / lmin + 3.0f);
+}
+
+// The exact FP64 tensor criterion |H_i r|^2 <= ext^2 or |H_j r|^2 <= ext^2
+// (H_j through the image).  Out of line: it runs for few candidates, and
+// inlined its FP64 tensors would set the register count of the whole search.
+__device__ __noinline__ bool exactTensorCriterion(const Fields& F, const Grid& g, long i, int j, int code, double qx,
+                                                  double qy, double qz, double ext2) {
+  Sym Hj = loadSym(F, F_HT_XX, j);
+  imageSym(g, code, Hj);
+  return eta2ExactSym(loadSym(F, F_HT_XX, i), qx, qy, qz) <= ext2 || eta2ExactSym(Hj, qx, qy, qz) <= ext2;
 }
 
 // TENSOR (ASPH): h^-1 in the FP32 mirror is the smallest eigenvalue of H, so
@@ -190,11 +209,9 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const float bandHi = del < 0.5f ? e2t * (1.0f + del) : FLT_MAX;
   const uint32_t mm = mirrorMask(g, hc);
   const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
-  Sym Hi{};
   float4 hi0 = make_float4(0.f, 0.f, 0.f, 0.f), hi1 = hi0;
   float tLo = 0.f, tHi = 0.f;
   if (TENSOR && active) {
-    Hi = loadSym(F, F_HT_XX, i);
     hi0 = P.hten[2 * i];
     hi1 = P.hten[2 * i + 1];
     const float dI = tensorBand(hi1.w, pi.w, g);
@@ -292,9 +309,7 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
               const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
                            qz = __dsub_rn(F.f[F_Z][i], zjd);
               if (TENSOR) {
-                Sym Hj = loadSym(F, F_HT_XX, j);
-                imageSym(g, code, Hj);
-                inside = eta2ExactSym(Hi, qx, qy, qz) <= ext2 || eta2ExactSym(Hj, qx, qy, qz) <= ext2;
+                inside = exactTensorCriterion(F, g, i, j, code, qx, qy, qz, ext2);
               } else {
                 inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
               }
@@ -804,16 +819,6 @@ __device__ __forceinline__ void eosNode(Fields& F, long i, const NodeListParams&
   F.f[F_CS][i] = sqrt(fmax(0.0, L.gamma * (L.gamma - 1.0) * eps));
 }
 
-__global__ void saveState0Kernel(Fields F, long n, int tensor) {
-  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  F.f[F_X0][i] = F.f[F_X][i]; F.f[F_Y0][i] = F.f[F_Y][i]; F.f[F_Z0][i] = F.f[F_Z][i];
-  F.f[F_VX0][i] = F.f[F_VX][i]; F.f[F_VY0][i] = F.f[F_VY][i]; F.f[F_VZ0][i] = F.f[F_VZ][i];
-  F.f[F_RHO0][i] = F.f[F_RHO][i]; F.f[F_EPS0][i] = F.f[F_EPS][i]; F.f[F_HINV0][i] = F.f[F_HINV][i];
-  if (tensor)
-#pragma unroll
-    for (int k = 0; k < 6; ++k) F.f[F_HT0_XX + k][i] = F.f[F_HT_XX + k][i];
-}
 __global__ void restoreState0Kernel(Fields F, long n, int tensor) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -833,6 +838,18 @@ __device__ __forceinline__ void storeExtent(Fields& F, long i, const Sym& h) {
   F.f[F_HINV][i] = lmin;
   F.f[F_HLMAX][i] = lmax;
 }
+// Mixed mode: the same extents from an FP32 Jacobi decomposition (GB300's
+// FP64 transcendental sequences would dominate the update).  The smallest
+// eigenvalue only has to bound |H r| / |r| from below (neighbour pre-filter),
+// so it is lowered by a margin far above the FP32 eigenvalue error; the
+// largest feeds the FP32 dt vote.
+__device__ __forceinline__ void storeExtent32(Fields& F, long i, const Sym& h) {
+  const SymT<float> hf{(float)h.xx, (float)h.xy, (float)h.xz, (float)h.yy, (float)h.yz, (float)h.zz};
+  float val[3], V[3][3];
+  symEigen(hf, val, V);
+  F.f[F_HINV][i] = (double)fminf(val[0], fminf(val[1], val[2])) * (1.0 - 1.0e-5);
+  F.f[F_HLMAX][i] = (double)fmaxf(val[0], fmaxf(val[1], val[2]));
+}
 __global__ void tensorExtentKernel(Fields F, long n) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -843,11 +860,21 @@ __global__ void tensorExtentKernel(Fields F, long n) {
 // here as well (the prepare pass folded into the update).
 // tensor (ASPH): H is the symmetric tensor, bounded on its eigenvalues
 // (IncrementBoundedState / ReplaceBoundedState with SymTensor min/max).
+template <bool TENSOR>
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
-                             double mult, int mid, int gravity, int epsIncrement, int tensor, Fields32 P, Grid g) {
+                             double mult, int mid, int gravity, int epsIncrement, Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
+  // the half-step update first takes the beginning-of-step copy (state0)
+  if (mid) {
+    F.f[F_X0][i] = F.f[F_X][i]; F.f[F_Y0][i] = F.f[F_Y][i]; F.f[F_Z0][i] = F.f[F_Z][i];
+    F.f[F_VX0][i] = F.f[F_VX][i]; F.f[F_VY0][i] = F.f[F_VY][i]; F.f[F_VZ0][i] = F.f[F_VZ][i];
+    F.f[F_RHO0][i] = F.f[F_RHO][i]; F.f[F_EPS0][i] = F.f[F_EPS][i]; F.f[F_HINV0][i] = F.f[F_HINV][i];
+    if (TENSOR)
+#pragma unroll
+      for (int k = 0; k < 6; ++k) F.f[F_HT0_XX + k][i] = F.f[F_HT_XX + k][i];
+  }
   if (epsIncrement) F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
   const double x = F.f[F_X][i] + mult * F.f[F_DXDT_X][i];
   const double y = F.f[F_Y][i] + mult * F.f[F_DXDT_Y][i];
@@ -871,7 +898,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
   F.f[F_RHO][i] = rho;
   const double hminInv = L.hminInv, hmaxInv = L.hmaxInv;
   double h;
-  if (tensor) {
+  if (TENSOR) {
     Sym t;
     if (mid) {
       t = loadSym(F, F_HT_XX, i);
@@ -883,7 +910,8 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     }
     t = symBound(t, hmaxInv, hminInv);
     storeSym(F, F_HT_XX, i, t);
-    storeExtent(F, i, t);
+    if (P.posh) storeExtent32(F, i, t);
+    else storeExtent(F, i, t);
     h = F.f[F_HINV][i];
   } else {
     h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
@@ -913,7 +941,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     P.velm[i] = make_float4((float)vx, (float)vy, (float)vz, (float)F.f[F_MASS][i]);
     const float om = (float)F.f[F_OMEGA][i];
     P.thermo[i] = make_float4((float)rho, (float)F.f[F_P][i], (float)F.f[F_CS][i], om / (om * om + 1.0e-30f));
-    if (P.hten) writeTensorMirror(F, P, i);
+    if (TENSOR) writeTensorMirror(F, P, i);
   }
 }
 
@@ -1047,11 +1075,11 @@ inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
 //==============================================================================
 // Launchers
 //==============================================================================
-void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+void launchBounds(const Fields& F, long n, bool tensor, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
                   LaunchCounter* lc) {
-  int nb = (int)std::min<long>((n + 255) / 256, nScratch / 7);
+  int nb = (int)std::min<long>((n + 255) / 256, nScratch / kBoundsVals);
   if (nb < 1) nb = 1;
-  boundsKernel<<<nb, 256, 0, s>>>(F, n, dScratch);
+  boundsKernel<<<nb, 256, 0, s>>>(F, n, tensor ? 1 : 0, dScratch);
   boundsFinalKernel<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
 }
@@ -1089,12 +1117,12 @@ void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCoun
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
                    bool carriedOnly, bool tensor, cudaStream_t s, LaunchCounter* lc) {
-  // the tensor-H fields move only in ASPH mode
-  FieldSel sel{};
-  for (int f = 0; f < (carriedOnly ? (int)F_NUM_CARRIED : (int)F_NUM_PERMUTED); ++f) {
-    const bool isTensor = (f >= F_HT_XX && f < F_NUM_CARRIED) || f >= F_HIDEALT_XX;
-    if (tensor || !isTensor) sel.id[sel.n++] = (unsigned char)f;
-  }
+  // the tensor-H fields (the end of the carried block and of the permuted
+  // block) move only in ASPH mode
+  FieldRanges sel{};
+  auto add = [&](int a, int b) { sel.first[sel.n] = a; sel.last[sel.n] = b; ++sel.n; };
+  add(0, tensor ? (int)F_NUM_CARRIED : (int)F_HT_XX);
+  if (!carriedOnly) add(F_NUM_CARRIED, tensor ? (int)F_NUM_PERMUTED : (int)F_HIDEALT_XX);
   permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n,
                                                 sel);
   lc->add(1);
@@ -1169,10 +1197,6 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
   else energyKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, pacc, pacc32, dt);
   lc->add(1);
 }
-void launchSaveState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
-  saveState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
-  lc->add(1);
-}
 void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
   restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
   lc->add(1);
@@ -1186,8 +1210,12 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   const int epsInc = (mid || !hp.compatible) ? 1 : 0;
   Fields32 P{};
   if (mirror) P = *mirror;
-  updateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
-                                               hp.asph, P, g);
+  if (hp.asph)
+    updateKernel<true><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
+                                                       P, g);
+  else
+    updateKernel<false><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0,
+                                                        epsInc, P, g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

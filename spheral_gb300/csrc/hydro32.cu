@@ -799,9 +799,14 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
   const bool multi = hp.numLists > 1;
 #define SPH_PAIR32(X, C, M, MB, PF, LQ) \
   pairKernelFP32<X, C, M, MB, PF, LQ, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
-#define SPH_PAIR32T(X, C, LQ) \
-  pairKernelFP32<X, C, true, 3, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
-  if (hp.asph) {   // ASPH (tensor H): pipelined, NodeList test at run time, up to 168 registers
+#define SPH_PAIR32T(X, C, LQ)                                                                     \
+  do {                                                                                            \
+    if (variant & 1) pairKernelFP32<X, C, true, 4, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+    else pairKernelFP32<X, C, true, 3, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);             \
+  } while (0)
+  // ASPH (tensor H): pipelined, NodeList test at run time; odd variants cap
+  // the registers at 128 (4 blocks per SM, a few spills), even ones at 168
+  if (hp.asph) {
     if (hp.xsph) {
       if (hp.compatible) { if (hp.limitedQ) SPH_PAIR32T(true, true, true); else SPH_PAIR32T(true, true, false); }
       else { if (hp.limitedQ) SPH_PAIR32T(true, false, true); else SPH_PAIR32T(true, false, false); }

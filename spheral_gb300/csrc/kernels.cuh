@@ -24,8 +24,10 @@ struct NeighborLists {
 };
 
 // Reductions ------------------------------------------------------------------
-// out[0] = min hinv, out[1..3] = min x,y,z, out[4..6] = max x,y,z
-void launchBounds(const Fields& F, long n, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
+// out[0] = min hinv, out[1..3] = min x,y,z, out[4..6] = max x,y,z,
+// out[7..9] = (tensor H) max over nodes of sqrt((H^-2)_aa) per axis, else 0
+constexpr int kBoundsVals = 10;
+void launchBounds(const Fields& F, long n, bool tensor, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
                   LaunchCounter* lc);
 
 // Neighbour build -------------------------------------------------------------
@@ -62,6 +64,7 @@ void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroPa
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                     double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
 constexpr int kPairVariants = 6;   // autotuned variants of launchPairFP32 (common path)
+constexpr int kPairVariantsTensor = 2;   // of its tensor-H (ASPH) path
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);
@@ -85,12 +88,13 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
                             double dt, cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
                                 float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc);
-// tensor: also the tensor H (ASPH)
-void launchSaveState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
+// state0 -> state (the copy is taken by the half-step update); tensor: also
+// the tensor H (ASPH)
 void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
 // ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
-// mid == true: timeAdvanceOnly increment with multiplier; else full update (eps
+// mid == true: save the beginning-of-step copies (state0), then the
+// timeAdvanceOnly increment with multiplier; else full update (eps
 // already advanced by the compatible-energy sweep when compatible).  mirror:
 // also refresh the FP32 mirrors of the new state (mixed mode), cells of grid g.
 void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
