@@ -54,6 +54,11 @@ extern "C" {
 #define SPHGPU_VISCOSITY_MONAGHAN_GINGOLD 0          /* MonaghanGingoldViscosity        */
 #define SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD 1  /* LimitedMonaghanGingoldViscosity (the SPH() factory default) */
 
+/* HEvolutionType (src/SmoothingScale/SmoothingScaleBase.hh:26-30) */
+#define SPHGPU_H_IDEAL 0       /* IdealH: the full update replaces H by Hideal (ReplaceBoundedState) */
+#define SPHGPU_H_INTEGRATE 1   /* IntegrateH: H += dt DHDt, bounded (IncrementBoundedState)        */
+#define SPHGPU_H_FIXED 2       /* FixedH: H never changes (FixedSmoothingScale)                    */
+
 #define SPHGPU_SMOOTHING_SPH 0           /* SPHSmoothingScale: isotropic H = I/h                  */
 #define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
                                             symmetric-tensor H                                  */
@@ -97,6 +102,7 @@ typedef struct sphgpu_config {
   double eta_crit_frac, eta_fold_frac;  /* limited Q: full Q below etaCritFrac/nPerh      */
   int smoothing_scale;              /* SPHGPU_SMOOTHING_*                                  */
   int fix_shape;                    /* ASPH fixShape: Hideal keeps the shape of H          */
+  int h_update;                     /* SPHGPU_H_* (the SPH() HUpdate argument)             */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,

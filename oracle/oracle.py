@@ -48,6 +48,7 @@ class OrcConfig(ctypes.Structure):
         ("eta_fold_frac", ctypes.c_double),
         ("smoothing_scale", ctypes.c_int),
         ("fix_shape", ctypes.c_int),
+        ("h_update", ctypes.c_int),
     ]
 
 
@@ -131,6 +132,8 @@ def _ip(a):
 VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
 # smoothing-scale package: SPHSmoothingScale or ASPHClassicSmoothingScale
 SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
+# HEvolutionType
+H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
 
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
@@ -181,6 +184,7 @@ class Oracle:
         c.eta_fold_frac = cfg.get("eta_fold_frac", 0.2)
         c.smoothing_scale = SMOOTHING_SCALE[cfg.get("smoothing_scale", "sph")]
         c.fix_shape = int(cfg.get("fix_shape", False))
+        c.h_update = H_UPDATE[cfg.get("h_update", "ideal")]
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))

@@ -521,6 +521,7 @@ struct Config {
   // 0 SPHSmoothingScale, 1 ASPHClassicSmoothingScale (SPHHydros.py:130-138, ASPH="CLASSIC")
   int smoothingScale = 0;
   int fixShape = 0;          // ASPHClassicSmoothingScale fixShape
+  int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
   double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
@@ -1251,7 +1252,10 @@ struct Problem {
       vel[i] = add(vel[i], mul(multiplier, DvDt[i]));
       if (cfg.gravity) vel[i] = add(vel[i], mul(multiplier, DvDtGrav[i]));
       rho[i] = std::min(L.rhoMax, std::max(L.rhoMin, rho[i] + multiplier * DrhoDt[i]));
-      if (midStep) {
+      // H: ReplaceBoundedState (IdealH; its timeAdvanceOnly update is the
+      // increment), IncrementBoundedState (IntegrateH), no policy (FixedH)
+      if (cfg.hUpdate == 2) {
+      } else if (midStep || cfg.hUpdate == 1) {
         ST hn{H[i].xx + multiplier * DHDt[i].xx, H[i].xy + multiplier * DHDt[i].xy, H[i].xz + multiplier * DHDt[i].xz,
               H[i].yy + multiplier * DHDt[i].yy, H[i].yz + multiplier * DHDt[i].yz, H[i].zz + multiplier * DHDt[i].zz};
         H[i] = clampH(hn, 1.0 / L.hmax, 1.0 / L.hmin);
@@ -1532,7 +1536,7 @@ struct orc_config {
   double G, softening, opening, ftimestep;
   int viscosity;
   double eta_crit_frac, eta_fold_frac;
-  int smoothing_scale, fix_shape;
+  int smoothing_scale, fix_shape, h_update;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1546,7 +1550,7 @@ void* orc_create(const orc_config* c) {
   g.quadraticInExpansion = c->quadratic_in_expansion; g.dtMin = c->dt_min; g.dtMax = c->dt_max; g.dtGrowth = c->dt_growth;
   g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
   g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
-  g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape;
+  g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape; g.hUpdate = c->h_update;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;

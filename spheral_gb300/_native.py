@@ -61,6 +61,7 @@ class Config(ctypes.Structure):
         ("eta_fold_frac", ctypes.c_double),
         ("smoothing_scale", ctypes.c_int),
         ("fix_shape", ctypes.c_int),
+        ("h_update", ctypes.c_int),
     ]
 
 

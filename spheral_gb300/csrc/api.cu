@@ -307,6 +307,7 @@ void refreshParams(sphgpu_ctx* c) {
   hp.etaFold = g.eta_fold_frac / c->lists[0].nPerh;
   hp.asph = g.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? 1 : 0;
   hp.fixShape = g.fix_shape ? 1 : 0;
+  hp.hUpdate = g.h_update;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -921,6 +922,7 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->eta_fold_frac = 0.2;
   c->smoothing_scale = SPHGPU_SMOOTHING_SPH;
   c->fix_shape = 0;
+  c->h_update = SPHGPU_H_IDEAL;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -939,6 +941,8 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
     if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
+    if (cfg->h_update != SPHGPU_H_IDEAL && cfg->h_update != SPHGPU_H_INTEGRATE && cfg->h_update != SPHGPU_H_FIXED)
+      throw Error(SPHGPU_E_UNSUPPORTED, "unknown H evolution");
     CUDA_OK(cudaSetDevice(cfg->device));
     CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->prof.s = c->stream;

@@ -51,6 +51,7 @@ struct HydroParams {
   double etaCrit, etaFold;       // its full-Q distance and fold width in eta
   int asph;                      // ASPHClassicSmoothingScale: tensor H throughout
   int fixShape;                  // ASPH fixShape: Hideal keeps the shape of H
+  int hUpdate;                   // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH
 };
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,

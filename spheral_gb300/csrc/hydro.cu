@@ -860,9 +860,11 @@ __global__ void tensorExtentKernel(Fields F, long n) {
 // here as well (the prepare pass folded into the update).
 // tensor (ASPH): H is the symmetric tensor, bounded on its eigenvalues
 // (IncrementBoundedState / ReplaceBoundedState with SymTensor min/max).
+// hUpdate: HEvolutionType -- 0 IdealH (the full update replaces H by Hideal),
+// 1 IntegrateH (both updates increment H by DHDt), 2 FixedH (H never changes).
 template <bool TENSOR>
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
-                             double mult, int mid, int gravity, int epsIncrement, Fields32 P, Grid g) {
+                             double mult, int mid, int gravity, int epsIncrement, int hUpdate, Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
@@ -898,9 +900,12 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
   F.f[F_RHO][i] = rho;
   const double hminInv = L.hminInv, hmaxInv = L.hmaxInv;
   double h;
-  if (TENSOR) {
+  const bool increment = mid || hUpdate == 1;
+  if (hUpdate == 2) {
+    h = F.f[F_HINV][i];
+  } else if (TENSOR) {
     Sym t;
-    if (mid) {
+    if (increment) {
       t = loadSym(F, F_HT_XX, i);
       const Sym d = loadSym(F, F_DHDTT_XX, i);
       t = Sym{t.xx + mult * d.xx, t.xy + mult * d.xy, t.xz + mult * d.xz, t.yy + mult * d.yy, t.yz + mult * d.yz,
@@ -914,7 +919,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     else storeExtent(F, i, t);
     h = F.f[F_HINV][i];
   } else {
-    h = mid ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
+    h = increment ? F.f[F_HINV][i] + mult * F.f[F_DHDT][i] : F.f[F_HIDEAL][i];
     if (h < hmaxInv) h = hmaxInv;
     if (h > hminInv) h = hminInv;
     F.f[F_HINV][i] = h;
@@ -1212,10 +1217,10 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   if (mirror) P = *mirror;
   if (hp.asph)
     updateKernel<true><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
-                                                       P, g);
+                                                       hp.hUpdate, P, g);
   else
     updateKernel<false><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0,
-                                                        epsInc, P, g);
+                                                        epsInc, hp.hUpdate, P, g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

@@ -27,6 +27,8 @@ DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acc
 VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
 # smoothing-scale package: SPHSmoothingScale or ASPHClassicSmoothingScale
 SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
+# HEvolutionType
+H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
 
 
 def config_from_dict(cfg, precision="fp64", device=0):
@@ -36,6 +38,8 @@ def config_from_dict(cfg, precision="fp64", device=0):
             c.viscosity = VISCOSITY[v]
         elif k == "smoothing_scale" and isinstance(v, str):
             c.smoothing_scale = SMOOTHING_SCALE[v]
+        elif k == "h_update" and isinstance(v, str):
+            c.h_update = H_UPDATE[v]
         elif k in dict(N.Config._fields_):
             setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
     c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)

@@ -32,17 +32,31 @@ from .engine import Engine
 # MassDensityType (src/Hydro/HydroFieldNames / SPH densityUpdate)
 RigorousSumDensity = 0
 IntegrateDensity = 1
-# HEvolutionType
+# HEvolutionType (src/SmoothingScale/SmoothingScaleBase.hh:26-30)
 IdealH = 0
+IntegrateH = 1
+FixedH = 2
+_H_UPDATE = {IdealH: "ideal", IntegrateH: "integrate", FixedH: "fixed"}
+
+
+def _h_update(HUpdate):
+    if HUpdate not in _H_UPDATE:
+        raise NotImplementedError("unknown HEvolutionType")
+    return _H_UPDATE[HUpdate]
 
 
 class SPHSmoothingScale:
     """SPHSmoothingScale(HUpdate, W): isotropic H = I/h (the SPH() default)."""
 
     def __init__(self, HUpdate=IdealH, W=None):
-        if HUpdate != IdealH:
-            raise NotImplementedError("only IdealH is on the GPU path")
-        self._cfg = dict(smoothing_scale="sph")
+        self._cfg = dict(smoothing_scale="sph", h_update=_h_update(HUpdate))
+
+
+class FixedSmoothingScale:
+    """FixedSmoothingScale(): H never changes (HEvolutionType FixedH)."""
+
+    def __init__(self):
+        self._cfg = dict(smoothing_scale="sph", h_update="fixed")
 
 
 class ASPHClassicSmoothingScale:
@@ -52,11 +66,9 @@ class ASPHClassicSmoothingScale:
     the FP64 precision mode; radialOnly is not on the GPU path."""
 
     def __init__(self, HUpdate=IdealH, W=None, fixShape=False, radialOnly=False):
-        if HUpdate != IdealH:
-            raise NotImplementedError("only IdealH is on the GPU path")
         if radialOnly:
             raise NotImplementedError("radialOnly is not on the GPU path")
-        self._cfg = dict(smoothing_scale="asph_classic", fix_shape=bool(fixShape))
+        self._cfg = dict(smoothing_scale="asph_classic", fix_shape=bool(fixShape), h_update=_h_update(HUpdate))
 
 
 class ASPHSmoothingScale:
@@ -279,12 +291,12 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
                 smoothingScaleMethod = ASPHSmoothingScale(HUpdate, W)
         else:
             smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
-    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale)):
+    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale, FixedSmoothingScale)):
         raise NotImplementedError("unknown smoothing-scale package")
     if evolveTotalEnergy:
         raise NotImplementedError("evolveTotalEnergy is not on the GPU path")
-    if HUpdate != IdealH or (filter or 0.0) != 0.0:
-        raise NotImplementedError("only IdealH without filtering is on the GPU path")
+    if (filter or 0.0) != 0.0:
+        raise NotImplementedError("H filtering is not on the GPU path")
     if Q is None:
         Q = LimitedMonaghanGingoldViscosity(1.0, 1.0)
     return SPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,

@@ -86,6 +86,24 @@ def test_asph_step_parity(native_lib, oracle_mod, case):
     assert np.abs(H[:, [1, 2, 4]]).max() > 1e-3 * np.abs(H).max()   # the shape really is anisotropic
 
 
+@pytest.mark.parametrize("h_update", ["integrate", "fixed"])
+def test_asph_h_update_parity(native_lib, oracle_mod, h_update):
+    # IntegrateH: H += dt DHDt with the tensor DH/Dt, bounded on its eigenvalues
+    def make():
+        p = problems.stretched_box(seed=77, boundaries="reflecting")
+        p.config["h_update"] = h_update
+        return p
+    p, eng, orc = _pair(oracle_mod, make)
+    H0 = eng.field("H")
+    for _ in range(4):
+        eng.step()
+        orc.step()
+    bad = compare_fields(eng, orc, STATE_FIELDS + ["DHDt"], 1e-9)
+    assert not bad, bad
+    if h_update == "fixed":
+        assert (eng.field("H") == H0).all()
+
+
 def test_asph_conserves_and_restarts(native_lib):
     from spheral_gb300.engine import Engine
     p = problems.stretched_box(seed=74)

@@ -24,6 +24,9 @@ OPTIONS = {
     "no_velocity_gradient_correction": dict(correct_velocity_gradient=False),
     "velocity_magnitude_dt": dict(use_velocity_magnitude_for_dt=True),
     "sph_factory_defaults": dict(xsph=True, viscosity="limited_monaghan_gingold"),
+    # HUpdate of the smoothing-scale package (SmoothingScaleBase.cc:53-82)
+    "integrate_h": dict(h_update="integrate"),
+    "fixed_h": dict(h_update="fixed"),
 }
 
 
@@ -78,6 +81,21 @@ def test_separate_nodelist_density_sums(native_lib, oracle_mod):
         orc2.step()
     bad = compare_fields(eng2, orc2, STATE_FIELDS, 1e-9)
     assert not bad, bad
+
+
+@pytest.mark.parametrize("h_update", ["integrate", "fixed"])
+def test_h_update_steps_mixed(native_lib, oracle_mod, h_update):
+    """IntegrateH / FixedH over three mixed-mode steps; FixedH keeps H bitwise."""
+    p = _make(dict(h_update=h_update))
+    eng, orc = _pair(oracle_mod, p, precision="fp32")
+    H0 = eng.field("H")
+    for _ in range(3):
+        eng.step()
+        orc.step()
+    bad = compare_fields(eng, orc, ["position", "velocity", "specificThermalEnergy", "H"], 5e-5)
+    assert not bad, bad
+    if h_update == "fixed":
+        assert (eng.field("H") == H0).all()
 
 
 @pytest.mark.parametrize("opt", ["xsph", "tensile", "no_compatible_energy", "sph_factory_defaults"])

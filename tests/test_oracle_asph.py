@@ -13,6 +13,8 @@
 * fixShape scales H without changing its shape.
 * Compatible-energy steps with the ASPH H evolution conserve energy and
   momentum to rounding.
+* HUpdate: IntegrateH increments H by dt DHDt at the full update, FixedH
+  leaves it unchanged (SmoothingScaleBase.cc:53-82).
 """
 import numpy as np
 import pytest
@@ -119,3 +121,23 @@ def test_asph_steps_conserve(oracle_mod, boundaries):
     ev = np.array([np.linalg.eigvalsh(sym(h)) for h in H])
     assert np.all(ev > 0.0)
     assert np.abs(H[:, [1, 2, 4]]).max() > 0.0       # the tensor evolves with off-diagonal terms
+
+
+@pytest.mark.parametrize("h_update", ["integrate", "fixed"])
+def test_h_update_options(oracle_mod, h_update):
+    # IntegrateH: the full update increments H by dt DHDt from the midpoint
+    # derivatives (IncrementBoundedState); FixedH: H never changes
+    p = problems.stretched_box(seed=10)
+    p.config["h_update"] = h_update
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    H0 = o.field("H")
+    c0 = o.conservation()
+    dt = o.step()
+    H1 = o.field("H")
+    if h_update == "fixed":
+        assert np.array_equal(H1, H0)
+    else:
+        want = H0 + dt * o.field("DHDt")
+        assert np.allclose(H1, want, rtol=1e-12, atol=1e-12 * np.abs(H0).max())
+    assert abs(o.conservation()[7] - c0[7]) < 1e-12 * abs(c0[7])

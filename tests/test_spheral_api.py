@@ -47,6 +47,9 @@ def test_asph_classic_selects_tensor_h():
     assert S.SPH(W=W, dataBase=db)._cfg["smoothing_scale"] == "sph"
     with pytest.raises(NotImplementedError):
         S.ASPHClassicSmoothingScale(S.IdealH, W, radialOnly=True)
+    # HUpdate of the factory maps onto the package
+    assert S.SPH(W=W, dataBase=db, HUpdate=S.IntegrateH)._cfg["h_update"] == "integrate"
+    assert S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.FixedSmoothingScale())._cfg["h_update"] == "fixed"
 
 
 def test_boundary_planes_map_to_axis_specs():
