@@ -103,6 +103,7 @@ typedef struct sphgpu_config {
   int smoothing_scale;              /* SPHGPU_SMOOTHING_*                                  */
   int fix_shape;                    /* ASPH fixShape: Hideal keeps the shape of H          */
   int h_update;                     /* SPHGPU_H_* (the SPH() HUpdate argument)             */
+  int evolve_total_energy;          /* evolveTotalEnergy (exclusive with compatible_energy) */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,

@@ -49,6 +49,7 @@ class OrcConfig(ctypes.Structure):
         ("smoothing_scale", ctypes.c_int),
         ("fix_shape", ctypes.c_int),
         ("h_update", ctypes.c_int),
+        ("evolve_total_energy", ctypes.c_int),
     ]
 
 
@@ -185,6 +186,7 @@ class Oracle:
         c.smoothing_scale = SMOOTHING_SCALE[cfg.get("smoothing_scale", "sph")]
         c.fix_shape = int(cfg.get("fix_shape", False))
         c.h_update = H_UPDATE[cfg.get("h_update", "ideal")]
+        c.evolve_total_energy = int(cfg.get("evolve_total_energy", False))
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))

@@ -522,6 +522,7 @@ struct Config {
   int smoothingScale = 0;
   int fixShape = 0;          // ASPHClassicSmoothingScale fixShape
   int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
+  int evolveTotalEnergy = 0; // SPH evolveTotalEnergy (SPH.cc:105-108, 541)
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
   double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
@@ -1072,7 +1073,8 @@ struct Problem {
       gradRho[i] = {a.gradRho.x / rhoi, a.gradRho.y / rhoi, a.gradRho.z / rhoi};
       DrhoDt[i] = -rhoi * traceT(DvDxi);
       DvDt[i] = a.DvDt;
-      DepsDt[i] = a.DepsDt;
+      // evolveTotalEnergy: the total-energy rate (SPH.cc:541)
+      DepsDt[i] = cfg.evolveTotalEnergy ? mi * (dot(vi, a.DvDt) + a.DepsDt) : a.DepsDt;
       maxQ[i] = a.maxQ; effQ[i] = a.effQ;
       XSPHWeightSum[i] = a.xsphW; XSPHDeltaV[i] = a.xsphDV;
       if (XSPH) {
@@ -1242,7 +1244,17 @@ struct Problem {
   void stateUpdate(double multiplier, bool midStep) {
     // specific thermal energy
     if (midStep || !cfg.compatibleEnergy) {
-      for (int i = 0; i < nInt; ++i) eps[i] += multiplier * DepsDt[i];
+      if (cfg.evolveTotalEnergy) {
+        // SpecificFromTotalThermalEnergyPolicy::update (SpecificFromTotalThermalEnergyPolicy.cc:40-70);
+        // it fires before the velocity update (no dependencies, key order)
+        for (int i = 0; i < nInt; ++i) {
+          const double E0 = mass[i] * (0.5 * mag2(vel[i]) + eps[i]);
+          const double E1 = E0 + multiplier * DepsDt[i];
+          eps[i] = E1 / mass[i] - 0.5 * mag2(add(vel[i], mul(multiplier, DvDt[i])));
+        }
+      } else {
+        for (int i = 0; i < nInt; ++i) eps[i] += multiplier * DepsDt[i];
+      }
     } else {
       compatibleEnergyUpdate(multiplier);
     }
@@ -1536,7 +1548,7 @@ struct orc_config {
   double G, softening, opening, ftimestep;
   int viscosity;
   double eta_crit_frac, eta_fold_frac;
-  int smoothing_scale, fix_shape, h_update;
+  int smoothing_scale, fix_shape, h_update, evolve_total_energy;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1551,6 +1563,7 @@ void* orc_create(const orc_config* c) {
   g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
   g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
   g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape; g.hUpdate = c->h_update;
+  g.evolveTotalEnergy = c->evolve_total_energy;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;

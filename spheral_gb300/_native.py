@@ -62,6 +62,7 @@ class Config(ctypes.Structure):
         ("smoothing_scale", ctypes.c_int),
         ("fix_shape", ctypes.c_int),
         ("h_update", ctypes.c_int),
+        ("evolve_total_energy", ctypes.c_int),
     ]
 
 

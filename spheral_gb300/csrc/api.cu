@@ -308,6 +308,7 @@ void refreshParams(sphgpu_ctx* c) {
   hp.asph = g.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? 1 : 0;
   hp.fixShape = g.fix_shape ? 1 : 0;
   hp.hUpdate = g.h_update;
+  hp.totalEnergy = g.evolve_total_energy ? 1 : 0;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -923,6 +924,7 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->smoothing_scale = SPHGPU_SMOOTHING_SPH;
   c->fix_shape = 0;
   c->h_update = SPHGPU_H_IDEAL;
+  c->evolve_total_energy = 0;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -943,6 +945,8 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
     if (cfg->h_update != SPHGPU_H_IDEAL && cfg->h_update != SPHGPU_H_INTEGRATE && cfg->h_update != SPHGPU_H_FIXED)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown H evolution");
+    if (cfg->compatible_energy && cfg->evolve_total_energy)   // SPH.cc:97-98
+      throw Error(SPHGPU_E_ARG, "compatibleEnergyEvolution and evolveTotalEnergy cannot both be set");
     CUDA_OK(cudaSetDevice(cfg->device));
     CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->prof.s = c->stream;

@@ -238,7 +238,8 @@ __device__ __forceinline__ void finalizeHydro(Fields& F, long i, const NodeAcc& 
   F.f[F_DVDT_X][i] = a.dvx;
   F.f[F_DVDT_Y][i] = a.dvy;
   F.f[F_DVDT_Z][i] = a.dvz;
-  F.f[F_DEPSDT][i] = a.deps;
+  // evolveTotalEnergy: the total-energy rate m (v . DvDt + DepsDt) (SPH.cc:541)
+  F.f[F_DEPSDT][i] = hp.totalEnergy ? mi * ((vxi * a.dvx + vyi * a.dvy + vzi * a.dvz) + a.deps) : a.deps;
   F.f[F_MAXQ][i] = a.maxQ;
   F.f[F_EFFQ][i] = a.effQ;
   double xw = a.xw;
@@ -378,7 +379,9 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
   F.f[F_DVDT_X][i] = a.dvx;
   F.f[F_DVDT_Y][i] = a.dvy;
   F.f[F_DVDT_Z][i] = a.dvz;
-  F.f[F_DEPSDT][i] = a.deps;
+  F.f[F_DEPSDT][i] = hp.totalEnergy
+                         ? (double)mi * ((F.f[F_VX][i] * a.dvx + F.f[F_VY][i] * a.dvy + F.f[F_VZ][i] * a.dvz) + a.deps)
+                         : a.deps;
   F.f[F_MAXQ][i] = a.maxQ;
   F.f[F_EFFQ][i] = a.effQ;
   float xw = a.xw;

@@ -864,7 +864,8 @@ __global__ void tensorExtentKernel(Fields F, long n) {
 // 1 IntegrateH (both updates increment H by DHDt), 2 FixedH (H never changes).
 template <bool TENSOR>
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
-                             double mult, int mid, int gravity, int epsIncrement, int hUpdate, Fields32 P, Grid g) {
+                             double mult, int mid, int gravity, int epsIncrement, int hUpdate, int totalEnergy,
+                             Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
@@ -877,7 +878,22 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
 #pragma unroll
       for (int k = 0; k < 6; ++k) F.f[F_HT0_XX + k][i] = F.f[F_HT_XX + k][i];
   }
-  if (epsIncrement) F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
+  if (epsIncrement) {
+    if (totalEnergy) {
+      // SpecificFromTotalThermalEnergyPolicy::update: eps from the total
+      // energy m (v^2/2 + eps) advanced by DEDt, with the hydro acceleration
+      // for the new kinetic part (it fires before the velocity update)
+      const double mi = F.f[F_MASS][i];
+      const double v0x = F.f[F_VX][i], v0y = F.f[F_VY][i], v0z = F.f[F_VZ][i];
+      const double v1x = v0x + mult * F.f[F_DVDT_X][i], v1y = v0y + mult * F.f[F_DVDT_Y][i],
+                   v1z = v0z + mult * F.f[F_DVDT_Z][i];
+      const double E0 = mi * (0.5 * (v0x * v0x + v0y * v0y + v0z * v0z) + F.f[F_EPS][i]);
+      const double E1 = E0 + mult * F.f[F_DEPSDT][i];
+      F.f[F_EPS][i] = E1 / mi - 0.5 * (v1x * v1x + v1y * v1y + v1z * v1z);
+    } else {
+      F.f[F_EPS][i] += mult * F.f[F_DEPSDT][i];
+    }
+  }
   const double x = F.f[F_X][i] + mult * F.f[F_DXDT_X][i];
   const double y = F.f[F_Y][i] + mult * F.f[F_DXDT_Y][i];
   const double z = F.f[F_Z][i] + mult * F.f[F_DXDT_Z][i];
@@ -1217,10 +1233,10 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   if (mirror) P = *mirror;
   if (hp.asph)
     updateKernel<true><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
-                                                       hp.hUpdate, P, g);
+                                                       hp.hUpdate, hp.totalEnergy, P, g);
   else
     updateKernel<false><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0,
-                                                        epsInc, hp.hUpdate, P, g);
+                                                        epsInc, hp.hUpdate, hp.totalEnergy, P, g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

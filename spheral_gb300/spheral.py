@@ -254,7 +254,10 @@ class ReflectingBoundary:
 class SPHHydro:
     def __init__(self, dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
                  XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile, nTensile,
-                 smoothingScaleMethod=None):
+                 smoothingScaleMethod=None, evolveTotalEnergy=False):
+        if compatibleEnergyEvolution and evolveTotalEnergy:   # SPH.cc:97-98
+            raise ValueError("SPH error : you cannot simultaneously use both compatibleEnergyEvolution and "
+                             "evolveTotalEnergy")
         self.dataBase, self.W, self.Q = dataBase, W, Q
         self.cfl = cfl
         self._cfg = dict(num_table_points=W.numPoints, cfl=cfl,
@@ -262,7 +265,8 @@ class SPHHydro:
                          compatible_energy=compatibleEnergyEvolution, gradh_correction=gradhCorrection,
                          xsph=XSPH, correct_velocity_gradient=correctVelocityGradient,
                          sum_mass_density_over_all_nodelists=sumMassDensityOverAllNodeLists,
-                         density_update=densityUpdate, eps_tensile=epsTensile, n_tensile=nTensile)
+                         density_update=densityUpdate, eps_tensile=epsTensile, n_tensile=nTensile,
+                         evolve_total_energy=evolveTotalEnergy)
         self._cfg.update(Q._config())
         self._smoothingScaleMethod = smoothingScaleMethod or SPHSmoothingScale(IdealH, W)
         self._cfg.update(self._smoothingScaleMethod._cfg)
@@ -293,15 +297,13 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
             smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
     elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale, FixedSmoothingScale)):
         raise NotImplementedError("unknown smoothing-scale package")
-    if evolveTotalEnergy:
-        raise NotImplementedError("evolveTotalEnergy is not on the GPU path")
     if (filter or 0.0) != 0.0:
         raise NotImplementedError("H filtering is not on the GPU path")
     if Q is None:
         Q = LimitedMonaghanGingoldViscosity(1.0, 1.0)
     return SPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
                     XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile,
-                    nTensile, smoothingScaleMethod)
+                    nTensile, smoothingScaleMethod, evolveTotalEnergy)
 
 
 class OctTreeGravity:

@@ -25,6 +25,7 @@ OPTIONS = {
     "velocity_magnitude_dt": dict(use_velocity_magnitude_for_dt=True),
     "sph_factory_defaults": dict(xsph=True, viscosity="limited_monaghan_gingold"),
     # HUpdate of the smoothing-scale package (SmoothingScaleBase.cc:53-82)
+    "total_energy": dict(compatible_energy=False, evolve_total_energy=True),
     "integrate_h": dict(h_update="integrate"),
     "fixed_h": dict(h_update="fixed"),
 }
@@ -98,7 +99,7 @@ def test_h_update_steps_mixed(native_lib, oracle_mod, h_update):
         assert (eng.field("H") == H0).all()
 
 
-@pytest.mark.parametrize("opt", ["xsph", "tensile", "no_compatible_energy", "sph_factory_defaults"])
+@pytest.mark.parametrize("opt", ["xsph", "tensile", "no_compatible_energy", "sph_factory_defaults", "total_energy"])
 def test_option_mixed_mode(native_lib, oracle_mod, opt):
     p = _make(OPTIONS[opt])
     eng, orc = _pair(oracle_mod, p, precision="fp32")

@@ -25,8 +25,10 @@ def test_out_of_path_options_are_refused():
     W = S.TableKernel(S.BSplineKernel(), 1000)
     with pytest.raises(NotImplementedError):
         S.SPH(W=W, dataBase=db, ASPH=True)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError):   # SPH.cc:97-98: not with compatible energy
         S.SPH(W=W, dataBase=db, evolveTotalEnergy=True)
+    assert S.SPH(W=W, dataBase=db, evolveTotalEnergy=True,
+                 compatibleEnergyEvolution=False)._cfg["evolve_total_energy"] is True
     with pytest.raises(NotImplementedError):
         S.TableKernel(object(), 100)
     with pytest.raises(NotImplementedError):
