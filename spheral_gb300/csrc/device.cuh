@@ -106,6 +106,33 @@ __device__ __forceinline__ void relSep(const float4& pi, const float4& pj, int d
   rz = __fadd_rn(__fsub_rn(pi.z, zj), oz);
 }
 
+// The cell offset (ox, oy, oz) of each of the 64 cell-offset codes of a
+// neighbour entry, staged once per block: relSepTab then reads it with one
+// shared load instead of decoding the code per pair.
+__device__ __forceinline__ void fillCellOffsets(float4* sOff, float cx, float cy, float cz) {
+  for (int t = threadIdx.x; t < 64; t += blockDim.x) {
+    const int d0 = t & 3, d1 = (t >> 2) & 3, d2 = (t >> 4) & 3;
+    sOff[t] = make_float4(d0 == 1 ? cx : (d0 == 2 ? -cx : 0.0f), d1 == 1 ? cy : (d1 == 2 ? -cy : 0.0f),
+                          d2 == 1 ? cz : (d2 == 2 ? -cz : 0.0f), 0.0f);
+  }
+}
+// relSep with the offsets from the staged table (bitwise the same result).
+__device__ __forceinline__ void relSepTab(const float4& pi, const float4& pj, int dcode, uint32_t mm, float cx,
+                                          float cy, float cz, const float4* __restrict__ sOff, float& rx, float& ry,
+                                          float& rz) {
+  float xj = pj.x, yj = pj.y, zj = pj.z;
+  const uint32_t mir = (uint32_t)dcode & mm;
+  if (mir) {
+    if (mir & 3u) xj = cx - xj;
+    if (mir & 12u) yj = cy - yj;
+    if (mir & 48u) zj = cz - zj;
+  }
+  const float4 o = sOff[dcode];
+  rx = __fadd_rn(__fsub_rn(pi.x, xj), o.x);
+  ry = __fadd_rn(__fsub_rn(pi.y, yj), o.y);
+  rz = __fadd_rn(__fsub_rn(pi.z, zj), o.z);
+}
+
 __device__ __forceinline__ void imagePos(const Grid& g, int code, double& x, double& y, double& z) {
   if (code) {
     x = imageCoord(x, code & 3, g.kindLo[0], g.kindHi[0], g.wallLo[0], g.wallHi[0]);

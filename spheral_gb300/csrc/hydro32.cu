@@ -97,8 +97,10 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
                                                       float* __restrict__ pacc) {
   __shared__ float4 ta[kMaxTable / 3];
   __shared__ float2 tb[kMaxTable / 3];
+  __shared__ float4 sOff[64];
   const int nint = hp.tableN1 + 1;
   for (int k = threadIdx.x; k < nint; k += blockDim.x) { ta[k] = t.p32a[k]; tb[k] = t.p32b[k]; }
+  fillCellOffsets(sOff, g.cellf[0], g.cellf[1], g.cellf[2]);
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     }
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
-    relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
+    relSepTab(pi, pj, dcode, mm, cx, cy, cz, sOff, rx, ry, rz);
     float vxj = vj4.x, vyj = vj4.y, vzj = vj4.z;
     mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
     const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z, sOj = thj.w;
