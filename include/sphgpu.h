@@ -78,8 +78,8 @@ typedef struct sphgpu_ctx* sphgpu_handle;
  *                                src/ArtificialViscosity/LimitedMonaghanGingoldViscosity.cc:39-53,
  *                                defaults src/PYB11/ArtificialViscosity/LimitedMonaghanGingoldViscosity.py:31-32
  *   ASPHClassicSmoothingScale(HUpdate, W, fixShape, radialOnly)
- *                                src/SmoothingScale/ASPHClassicSmoothingScale.cc:34-46 (IdealH;
- *                                radialOnly is not on this path) */
+ *                                src/SmoothingScale/ASPHClassicSmoothingScale.cc:34-46 (radialOnly
+ *                                with the default ASPHRadialFunctor, about the origin) */
 typedef struct sphgpu_config {
   int num_table_points;             /* TableKernel(BSplineKernel3d(), numPoints)           */
   double cfl;
@@ -104,6 +104,7 @@ typedef struct sphgpu_config {
   int fix_shape;                    /* ASPH fixShape: Hideal keeps the shape of H          */
   int h_update;                     /* SPHGPU_H_* (the SPH() HUpdate argument)             */
   int evolve_total_energy;          /* evolveTotalEnergy (exclusive with compatible_energy) */
+  int radial_only;                  /* ASPH radialOnly: H reshaped radially about the origin */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,

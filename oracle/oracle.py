@@ -50,6 +50,7 @@ class OrcConfig(ctypes.Structure):
         ("fix_shape", ctypes.c_int),
         ("h_update", ctypes.c_int),
         ("evolve_total_energy", ctypes.c_int),
+        ("radial_only", ctypes.c_int),
     ]
 
 
@@ -112,6 +113,7 @@ def lib():
             "orc_set_nodelist_hminratio": (i, [vp, i, d]),
             "orc_sym_eigen": (i, [dp, dp, dp]),
             "orc_smoothing_scale_derivative": (i, [dp, dp, dp]),
+            "orc_radial_evolution": (i, [dp, dp, d, d, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -187,6 +189,7 @@ class Oracle:
         c.fix_shape = int(cfg.get("fix_shape", False))
         c.h_update = H_UPDATE[cfg.get("h_update", "ideal")]
         c.evolve_total_energy = int(cfg.get("evolve_total_energy", False))
+        c.radial_only = int(cfg.get("radial_only", False))
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))
@@ -336,4 +339,13 @@ def smoothing_scale_derivative(h6, dvdx9):
     d = np.ascontiguousarray(dvdx9, dtype=np.float64)
     out = np.zeros(6)
     lib().orc_smoothing_scale_derivative(_dp(h), _dp(d), _dp(out))
+    return out
+
+
+def radial_evolution(h6, x3, s, r0):
+    """ASPH radialOnly reshaping of one H (the oracle's radialEvolution)."""
+    h = np.ascontiguousarray(h6, dtype=np.float64)
+    x = np.ascontiguousarray(x3, dtype=np.float64)
+    out = np.zeros(6)
+    lib().orc_radial_evolution(_dp(h), _dp(x), s, r0, _dp(out))
     return out

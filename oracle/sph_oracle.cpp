@@ -257,6 +257,44 @@ static ST sqrtS(const ST& H) {
                        std::sqrt(std::max(0.0, e.val[2]))};
   return fromEigen(d, e.vec);
 }
+// rotationMatrix (src/Utilities/rotationMatrix.hh:42-61): rows are the new
+// axes, the first along runit.
+static T9 rotationMatrix3(const V3& u) {
+  const double rxy = std::sqrt(u.x * u.x + u.y * u.y);
+  if (fuzzyEqual(rxy, 0.0)) return {0.0, 0.0, u.z, 0.0, 1.0, 0.0, -u.z, 0.0, 0.0};
+  return {u.x, u.y, u.z, -u.y / rxy, u.x / rxy, 0.0, -u.x * u.z / rxy, -u.y * u.z / rxy, rxy};
+}
+// R A R^T of a symmetric tensor (GeomSymmetricTensor::rotationalTransform).
+static ST rotateS(const ST& A, const T9& R) {
+  const double a[3][3] = {{A.xx, A.xy, A.xz}, {A.xy, A.yy, A.yz}, {A.xz, A.yz, A.zz}};
+  const double r[3][3] = {{R.xx, R.xy, R.xz}, {R.yx, R.yy, R.yz}, {R.zx, R.zy, R.zz}};
+  double m[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) s += r[i][k] * a[k][l] * r[j][l];
+      m[i][j] = s;
+    }
+  return {m[0][0], m[0][1], m[0][2], m[1][1], m[1][2], m[2][2]};
+}
+static T9 transposeT(const T9& t) { return {t.xx, t.yx, t.zx, t.xy, t.yy, t.zy, t.xz, t.yz, t.zz}; }
+// radialEvolution for Dim<3> (SmoothingScaleUtilities.hh): H in the frame
+// whose first axis is nhat, the radial extent scaled by 1/s, the transverse
+// block by r0/r1 -- (1,2) and (2,1) address the same element of a
+// SymTensor, so yz is divided twice -- and back to the lab frame.
+static ST radialEvolution3(const ST& Hi, const V3& nhat, double s, double r0, double r1) {
+  const T9 Tp = rotationMatrix3(nhat);
+  ST h = rotateS(Hi, Tp);
+  const double fr = r1 * safeInvVar(r0);
+  h.xx /= s;
+  h.yy /= fr;
+  h.yz /= fr;
+  h.yz /= fr;
+  h.zz /= fr;
+  return rotateS(h, transposeT(Tp));
+}
+
 // Tensor DH/Dt of ASPH (SmoothingScaleUtilities.hh, smoothingScaleDerivative
 // for Dim<3>): the rate of H under the velocity gradient with the rotation of
 // the frame taken out.
@@ -521,6 +559,7 @@ struct Config {
   // 0 SPHSmoothingScale, 1 ASPHClassicSmoothingScale (SPHHydros.py:130-138, ASPH="CLASSIC")
   int smoothingScale = 0;
   int fixShape = 0;          // ASPHClassicSmoothingScale fixShape
+  int radialOnly = 0;        // ASPHClassicSmoothingScale radialOnly (ASPHRadialFunctor defaults: about the origin)
   int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
   int evolveTotalEnergy = 0; // SPH evolveTotalEnergy (SPH.cc:105-108, 541)
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
@@ -571,6 +610,7 @@ struct Problem {
   vector<V3> DxDt, DvDt, gradRho, XSPHDeltaV, massFirst, DvDtGrav;
   vector<T9> DvDx, localDvDx, M, localM;
   vector<ST> DHDt, Hideal, massSecond;
+  vector<double> radius0;   // radialOnly: |x| at preStepInitialize (SmoothingScaleBase.cc:104-121)
   // ArtificialViscosityVelocityGradient: the Q's copy of DvDx, a state field
   // (ArtificialViscosityHandle.cc:52,78-79; zero until the first copy)
   vector<T9> DvDxQ;
@@ -1136,6 +1176,8 @@ struct Problem {
     }
     const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s + tiny));
     if (cfg.fixShape) Hid = divS(Hi, 1.0 - aa + aa * s);
+    else if (cfg.radialOnly) Hid = radialEvolution3(Hi, unitVector(pos[i]), 1.0 - aa + aa * s,
+                                                    i < (int)radius0.size() ? radius0[i] : 0.0, mag(pos[i]));
     else Hid = scaleS(Hid, rootnu3(detS(Hi)) / (1.0 - aa + aa * s));
     const EigS he = eigenVectorsS(Hid);
     const double hminInv = safeInvVar(L.hmin), hmaxInv = safeInvVar(L.hmax);
@@ -1482,6 +1524,10 @@ struct Problem {
     computeConnectivity();
     const double t = time;
     // preStepInitialize: RigorousSumDensity
+    if (cfg.radialOnly) {   // SmoothingScaleBase::preStepInitialize
+      radius0.assign(nInt, 0.0);
+      for (int i = 0; i < nInt; ++i) radius0[i] = mag(pos[i]);
+    }
     if (cfg.densityUpdate == 0) sumMassDensity();
     // initializeDerivatives(t, 0): TreeGravity::initialize builds the tree
     if (cfg.gravity) buildTree();
@@ -1548,7 +1594,7 @@ struct orc_config {
   double G, softening, opening, ftimestep;
   int viscosity;
   double eta_crit_frac, eta_fold_frac;
-  int smoothing_scale, fix_shape, h_update, evolve_total_energy;
+  int smoothing_scale, fix_shape, h_update, evolve_total_energy, radial_only;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1563,7 +1609,7 @@ void* orc_create(const orc_config* c) {
   g.gravity = c->gravity; g.G = c->G; g.softening = c->softening; g.opening = c->opening; g.ftimestep = c->ftimestep;
   g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
   g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape; g.hUpdate = c->h_update;
-  g.evolveTotalEnergy = c->evolve_total_energy;
+  g.evolveTotalEnergy = c->evolve_total_energy; g.radialOnly = c->radial_only;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;
@@ -1593,6 +1639,15 @@ int orc_sym_eigen(const double* a, double* vals, double* vecs) {
   for (int k = 0; k < 3; ++k) vals[k] = e.val[k];
   for (int r = 0; r < 3; ++r)
     for (int k = 0; k < 3; ++k) vecs[3 * r + k] = e.vec[r][k];
+  return 0;
+}
+// radialEvolution of one H (xx xy xz yy yz zz) at position x with scale s
+// and start-of-step radius r0.
+int orc_radial_evolution(const double* h, const double* x, double s, double r0, double* out) {
+  const orc::ST H{h[0], h[1], h[2], h[3], h[4], h[5]};
+  const orc::V3 X{x[0], x[1], x[2]};
+  const orc::ST r = orc::radialEvolution3(H, orc::unitVector(X), s, r0, orc::mag(X));
+  out[0] = r.xx; out[1] = r.xy; out[2] = r.xz; out[3] = r.yy; out[4] = r.yz; out[5] = r.zz;
   return 0;
 }
 // The ASPH tensor DH/Dt for one (H, DvDx).

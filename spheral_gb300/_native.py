@@ -63,6 +63,7 @@ class Config(ctypes.Structure):
         ("fix_shape", ctypes.c_int),
         ("h_update", ctypes.c_int),
         ("evolve_total_energy", ctypes.c_int),
+        ("radial_only", ctypes.c_int),
     ]
 
 

@@ -309,6 +309,7 @@ void refreshParams(sphgpu_ctx* c) {
   hp.fixShape = g.fix_shape ? 1 : 0;
   hp.hUpdate = g.h_update;
   hp.totalEnergy = g.evolve_total_energy ? 1 : 0;
+  hp.radialOnly = g.radial_only ? 1 : 0;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -739,6 +740,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   buildNeighbors(c, true);                           // Integrator::setGhostNodes + connectivity
   bool fused = false;
   auto preStep = [&]() {
+    if (c->hp.radialOnly) launchRadius0(c->F, c->n, c->stream, &c->lc);   // SmoothingScaleBase::preStepInitialize
     if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
       if (c->fp32()) {
         Scope sc(c->prof, "density_dt");
@@ -925,6 +927,7 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->fix_shape = 0;
   c->h_update = SPHGPU_H_IDEAL;
   c->evolve_total_energy = 0;
+  c->radial_only = 0;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -945,6 +948,10 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
     if (cfg->h_update != SPHGPU_H_IDEAL && cfg->h_update != SPHGPU_H_INTEGRATE && cfg->h_update != SPHGPU_H_FIXED)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown H evolution");
+    if (cfg->fix_shape && cfg->radial_only)   // ASPHClassicSmoothingScale: not both
+      throw Error(SPHGPU_E_ARG, "fixShape and radialOnly cannot both be set");
+    if (cfg->radial_only && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
+      throw Error(SPHGPU_E_ARG, "radialOnly needs the ASPH smoothing scale");
     if (cfg->compatible_energy && cfg->evolve_total_energy)   // SPH.cc:97-98
       throw Error(SPHGPU_E_ARG, "compatibleEnergyEvolution and evolveTotalEnergy cannot both be set");
     CUDA_OK(cudaSetDevice(cfg->device));

@@ -53,6 +53,7 @@ struct HydroParams {
   int fixShape;                  // ASPH fixShape: Hideal keeps the shape of H
   int hUpdate;                   // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH
   int totalEnergy;               // evolveTotalEnergy: DepsDt is the total-energy rate
+  int radialOnly;                // ASPH radialOnly
 };
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,

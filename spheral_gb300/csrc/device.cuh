@@ -335,7 +335,8 @@ __device__ __forceinline__ void finalizeNodeASPH(Fields& F, long i, int li, cons
   symEigenValues(M2, ev);
   storeSym(F, F_HIDEALT_XX, i,
            asphClassicHideal(M2, fmin(ev[0], fmin(ev[1], ev[2])) > 0.0, Hi, s, hp.fixShape != 0, L.hminInv,
-                             L.hmaxInv, L.hminratio));
+                             L.hmaxInv, L.hminratio, hp.radialOnly != 0, F.f[F_X][i], F.f[F_Y][i], F.f[F_Z][i],
+                             F.f[F_RAD0][i]));
 }
 
 // FP32 variant of finalizeNode for the mixed mode: the per-node completion
@@ -447,7 +448,8 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
     const bool pd = M2.xx > 0.0f && M2.xx * M2.yy - M2.xy * M2.xy > 0.0f && symDet(M2) > 0.0f;
     storeSym(F, F_HIDEALT_XX, i,
              asphClassicHideal(M2, pd, Hi, s, hp.fixShape != 0, (float)L.hminInv, (float)L.hmaxInv,
-                               (float)L.hminratio));
+                               (float)L.hminratio, hp.radialOnly != 0, (float)F.f[F_X][i], (float)F.f[F_Y][i],
+                               (float)F.f[F_Z][i], (float)F.f[F_RAD0][i]));
     return;
   }
   // FP32 forms of DHDt = -(H/3) tr(DvDx) and of the IdealH clamp

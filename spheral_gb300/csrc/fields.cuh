@@ -35,6 +35,7 @@ enum FieldId {
   // ASPH only: tensor Hideal and the second moment of the neighbour distribution
   F_HIDEALT_XX, F_HIDEALT_XY, F_HIDEALT_XZ, F_HIDEALT_YY, F_HIDEALT_YZ, F_HIDEALT_ZZ,
   F_M2_XX, F_M2_XY, F_M2_XZ, F_M2_YY, F_M2_YZ, F_M2_ZZ,
+  F_RAD0,          // ASPH radialOnly: |x| at the start of the step
   F_NUM_PERMUTED,
   // beginning-of-step copies (not permuted: written after the sort)
   F_X0 = F_NUM_PERMUTED, F_Y0, F_Z0, F_VX0, F_VY0, F_VZ0, F_RHO0, F_EPS0, F_HINV0,

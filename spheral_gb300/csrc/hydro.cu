@@ -850,6 +850,14 @@ __device__ __forceinline__ void storeExtent32(Fields& F, long i, const Sym& h) {
   F.f[F_HINV][i] = (double)fminf(val[0], fminf(val[1], val[2])) * (1.0 - 1.0e-5);
   F.f[F_HLMAX][i] = (double)fmaxf(val[0], fmaxf(val[1], val[2]));
 }
+// ASPH radialOnly: the radius of every node at the start of the step
+// (SmoothingScaleBase::preStepInitialize).
+__global__ void radius0Kernel(Fields F, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i];
+  F.f[F_RAD0][i] = sqrt(x * x + y * y + z * z);
+}
 __global__ void tensorExtentKernel(Fields F, long n) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1220,6 +1228,10 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
 }
 void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
   restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
+  lc->add(1);
+}
+void launchRadius0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
+  radius0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n);
   lc->add(1);
 }
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {

@@ -93,6 +93,8 @@ void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, cons
 void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
 // ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
+// ASPH radialOnly: F_RAD0 <- |x|
+void launchRadius0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // mid == true: save the beginning-of-step copies (state0), then the
 // timeAdvanceOnly increment with multiplier; else full update (eps
 // already advanced by the compatible-energy sweep when compatible).  mirror:

@@ -237,6 +237,61 @@ template <> __device__ __forceinline__ double rootnu3T<double>(double x) {
   return (x < 0.0 ? -1.0 : 1.0) * pow(fabs(x), 0.3333333333333333);
 }
 
+// rotationMatrix (src/Utilities/rotationMatrix.hh:42-61) of the unit vector
+// (ux, uy, uz): rows are the new axes, the first along u.
+template <class T>
+__device__ __forceinline__ void rotationMatrix3(T ux, T uy, T uz, T R[3][3]) {
+  const T rxy = sqrt(ux * ux + uy * uy);
+  if (fabs(rxy - T(0)) <= T(1.0e-15) * fmax(T(1), fabs(rxy))) {
+    R[0][0] = 0; R[0][1] = 0; R[0][2] = uz;
+    R[1][0] = 0; R[1][1] = 1; R[1][2] = 0;
+    R[2][0] = -uz; R[2][1] = 0; R[2][2] = 0;
+  } else {
+    R[0][0] = ux; R[0][1] = uy; R[0][2] = uz;
+    R[1][0] = -uy / rxy; R[1][1] = ux / rxy; R[1][2] = 0;
+    R[2][0] = -ux * uz / rxy; R[2][1] = -uy * uz / rxy; R[2][2] = rxy;
+  }
+}
+// R A R^T (transpose = false) or R^T A R (true) of a symmetric tensor.
+template <class T>
+__device__ __forceinline__ SymT<T> symRotate(const SymT<T>& A, const T R[3][3], bool transpose) {
+  const T a[3][3] = {{A.xx, A.xy, A.xz}, {A.xy, A.yy, A.yz}, {A.xz, A.yz, A.zz}};
+  T m[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+          s += (transpose ? R[k][i] : R[i][k]) * a[k][l] * (transpose ? R[l][j] : R[j][l]);
+      m[i][j] = s;
+    }
+  return SymT<T>{m[0][0], m[0][1], m[0][2], m[1][1], m[1][2], m[2][2]};
+}
+// radialEvolution for Dim<3> (SmoothingScaleUtilities.hh): H in the frame
+// whose first axis is the radial direction, the radial extent scaled by 1/s,
+// the transverse block by r0/r1 -- (1,2) and (2,1) address one element of a
+// SymTensor there, so yz is divided twice -- and back to the lab frame.
+template <class T>
+__device__ __forceinline__ SymT<T> radialEvolution(const SymT<T>& Hi, T x, T y, T z, T s, T r0) {
+  const T r1 = sqrt(x * x + y * y + z * z);
+  T ux = T(1), uy = T(0), uz = T(0);   // GeomVector::unitVector
+  if (r1 > T(1.0e-50)) { ux = x / r1; uy = y / r1; uz = z / r1; }
+  T R[3][3];
+  rotationMatrix3(ux, uy, uz, R);
+  SymT<T> h = symRotate(Hi, R, false);
+  const T fr = r1 * ((r0 < T(0) ? T(-1) : T(1)) / fmax(T(1.0e-30), fabs(r0)));
+  h.xx /= s;
+  h.yy /= fr;
+  h.yz /= fr;
+  h.yz /= fr;
+  h.zz /= fr;
+  return symRotate(h, R, true);
+}
+
 // Hideal of ASPHClassicSmoothingScale (ASPHClassicSmoothingScale.cc:205-288)
 // from the second moment M2 of the neighbour distribution, H, the ratio s of
 // the target to the current nodes per smoothing scale and the NodeList
@@ -245,9 +300,14 @@ template <> __device__ __forceinline__ double rootnu3T<double>(double x) {
 // psiweight is zero), the size as in the SPH IdealH (or H rescaled, with
 // fixShape), then the eigenvalues bounded by 1/hmax and
 // min(1/hmin, max(1/hmax, smallest) / hminratio).
+// radialOnly: H reshaped along the radial direction of x about the origin
+// (radialEvolution, the default ASPHRadialFunctor) with r0 its start-of-step
+// radius.
 template <class T>
 __device__ __forceinline__ SymT<T> asphClassicHideal(const SymT<T>& M2, bool m2Positive, const SymT<T>& Hi, T s,
-                                                     bool fixShape, T hminInv, T hmaxInv, T hminratio) {
+                                                     bool fixShape, T hminInv, T hmaxInv, T hminratio,
+                                                     bool radialOnly = false, T x = T(0), T y = T(0), T z = T(0),
+                                                     T r0 = T(0)) {
   const T tiny = T(1.0e-50);
   const T psiweight = fmax(T(0), fmin(T(1), T(2) / s - T(1)));
   SymT<T> Hid{T(1), T(0), T(0), T(1), T(0), T(1)};
@@ -272,6 +332,7 @@ __device__ __forceinline__ SymT<T> asphClassicHideal(const SymT<T>& M2, bool m2P
   }
   const T aa = s < T(1) ? T(0.4) * (T(1) + s * s) : T(0.4) * (T(1) + T(1) / (s * s * s + tiny));
   if (fixShape) Hid = symDiv(Hi, T(1) - aa + aa * s);
+  else if (radialOnly) Hid = radialEvolution(Hi, x, y, z, T(1) - aa + aa * s, r0);
   else Hid = symScale(Hid, rootnu3T(symDet(Hi)) / (T(1) - aa + aa * s));
   symEigen(Hid, ev, V);
   const T hminEffInv = fmin(hminInv, fmax(hmaxInv, fmin(ev[0], fmin(ev[1], ev[2]))) / hminratio);

@@ -62,13 +62,15 @@ class FixedSmoothingScale:
 class ASPHClassicSmoothingScale:
     """ASPHClassicSmoothingScale(HUpdate, W, fixShape=False, radialOnly=False):
     symmetric-tensor H shaped by the second moment of the neighbour
-    distribution (src/SmoothingScale/ASPHClassicSmoothingScale.cc).  Runs in
-    the FP64 precision mode; radialOnly is not on the GPU path."""
+    distribution (src/SmoothingScale/ASPHClassicSmoothingScale.cc); radialOnly
+    reshapes H along the radial direction about the origin (the default
+    ASPHRadialFunctor)."""
 
     def __init__(self, HUpdate=IdealH, W=None, fixShape=False, radialOnly=False):
-        if radialOnly:
-            raise NotImplementedError("radialOnly is not on the GPU path")
-        self._cfg = dict(smoothing_scale="asph_classic", fix_shape=bool(fixShape), h_update=_h_update(HUpdate))
+        if fixShape and radialOnly:
+            raise ValueError("fixShape and radialOnly cannot both be set")
+        self._cfg = dict(smoothing_scale="asph_classic", fix_shape=bool(fixShape), radial_only=bool(radialOnly),
+                         h_update=_h_update(HUpdate))
 
 
 class ASPHSmoothingScale:

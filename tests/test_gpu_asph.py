@@ -25,8 +25,15 @@ from _parity import DERIV_FIELDS, STATE_FIELDS, compare_fields, ordered_pairs_fr
 
 pytestmark = pytest.mark.gpu
 
+def _radial():
+    p = problems.stretched_box(seed=78, boundaries="reflecting")
+    p.config["radial_only"] = True
+    return p
+
+
 CASES = {
     "periodic": lambda: problems.stretched_box(seed=71, boundaries="periodic"),
+    "radial_only": _radial,
     "reflecting": lambda: problems.stretched_box(seed=72, boundaries="reflecting"),
     "fix_shape": lambda: problems.stretched_box(seed=73, boundaries="periodic", fix_shape=True),
 }

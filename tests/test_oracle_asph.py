@@ -15,6 +15,9 @@
   momentum to rounding.
 * HUpdate: IntegrateH increments H by dt DHDt at the full update, FixedH
   leaves it unchanged (SmoothingScaleBase.cc:53-82).
+* radialOnly (radialEvolution): the identity for s = 1 and an unchanged
+  radius; for isotropic H the radial eigenvalue scales by 1/s and the
+  transverse ones by r0/r1.
 """
 import numpy as np
 import pytest
@@ -140,4 +143,32 @@ def test_h_update_options(oracle_mod, h_update):
     else:
         want = H0 + dt * o.field("DHDt")
         assert np.allclose(H1, want, rtol=1e-12, atol=1e-12 * np.abs(H0).max())
+    assert abs(o.conservation()[7] - c0[7]) < 1e-12 * abs(c0[7])
+
+
+def test_radial_evolution(oracle_mod):
+    rng = np.random.default_rng(12)
+    for _ in range(5):
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        H = q @ np.diag(rng.uniform(5.0, 20.0, 3)) @ q.T
+        x = rng.normal(size=3)
+        got = sym(oracle_mod.radial_evolution(six(H), x, 1.0, np.linalg.norm(x)))
+        assert np.allclose(got, H, rtol=1e-12, atol=1e-12 * np.abs(H).max())
+        a, s, fr = 10.0, 1.3, 1.1
+        got = sym(oracle_mod.radial_evolution(six(a * np.eye(3)), x, s, np.linalg.norm(x) / fr))
+        nh = x / np.linalg.norm(x)
+        assert abs(nh @ got @ nh - a / s) < 1e-12 * a
+        t = np.cross(nh, [0.3, -0.2, 0.9])
+        t /= np.linalg.norm(t)
+        assert abs(t @ got @ t - a / fr) < 1e-12 * a
+
+
+def test_radial_only_steps_conserve(oracle_mod):
+    p = problems.stretched_box(seed=11)
+    p.config["radial_only"] = True
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    c0 = o.conservation()
+    for _ in range(3):
+        o.step()
     assert abs(o.conservation()[7] - c0[7]) < 1e-12 * abs(c0[7])

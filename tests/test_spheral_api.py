@@ -47,8 +47,9 @@ def test_asph_classic_selects_tensor_h():
     fixed = S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.ASPHClassicSmoothingScale(S.IdealH, W, fixShape=True))
     assert fixed._cfg["fix_shape"] is True
     assert S.SPH(W=W, dataBase=db)._cfg["smoothing_scale"] == "sph"
-    with pytest.raises(NotImplementedError):
-        S.ASPHClassicSmoothingScale(S.IdealH, W, radialOnly=True)
+    assert S.ASPHClassicSmoothingScale(S.IdealH, W, radialOnly=True)._cfg["radial_only"] is True
+    with pytest.raises(ValueError):
+        S.ASPHClassicSmoothingScale(S.IdealH, W, fixShape=True, radialOnly=True)
     # HUpdate of the factory maps onto the package
     assert S.SPH(W=W, dataBase=db, HUpdate=S.IntegrateH)._cfg["h_update"] == "integrate"
     assert S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.FixedSmoothingScale())._cfg["h_update"] == "fixed"
