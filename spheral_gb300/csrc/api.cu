@@ -372,12 +372,11 @@ void buildGrid(sphgpu_ctx* c) {
       g.wallLo[b.axis] = b.lo;
     }
   }
+  int ncA[3];
   for (int a = 0; a < 3; ++a) {
     const double lo = g.kindLo[a] == AXIS_OPEN ? bnd[1 + a] : g.wallLo[a];
     const double hi = g.kindHi[a] == AXIS_OPEN ? bnd[4 + a] : g.wallHi[a];
-    const double L = hi - lo;
-    const double support = supportAxis[a];
-    int nc = (int)std::min(1024.0, std::floor(L / support));
+    int nc = (int)std::min(1024.0, std::floor((hi - lo) / supportAxis[a]));
     if (g.kindLo[a] == AXIS_PERIODIC) {
       if (nc < 3)
         throw Error(SPHGPU_E_UNSUPPORTED,
@@ -385,6 +384,29 @@ void buildGrid(sphgpu_ctx* c) {
     } else {
       nc = std::max(1, nc);
     }
+    ncA[a] = nc;
+  }
+  // A sparse or spread-out node set would ask for far more cells than nodes
+  // (and cell tables as large as the key space): coarsen the widest axis
+  // until the cells number at most max(4096, 8 n).  Larger cells only add
+  // candidates; periodic axes keep at least three.
+  const double cellCap = std::max(4096.0, 8.0 * (double)c->n);
+  while ((double)ncA[0] * ncA[1] * ncA[2] > cellCap) {
+    int a = -1;
+    for (int b = 0; b < 3; ++b) {
+      const int minNc = g.kindLo[b] == AXIS_PERIODIC ? 3 : 1;
+      if (ncA[b] > minNc && (a < 0 || ncA[b] > ncA[a])) a = b;
+    }
+    if (a < 0) break;
+    const int minNc = g.kindLo[a] == AXIS_PERIODIC ? 3 : 1;
+    ncA[a] = std::max(minNc, (int)(ncA[a] * 0.8));
+  }
+  for (int a = 0; a < 3; ++a) {
+    const double lo = g.kindLo[a] == AXIS_OPEN ? bnd[1 + a] : g.wallLo[a];
+    const double hi = g.kindHi[a] == AXIS_OPEN ? bnd[4 + a] : g.wallHi[a];
+    const double L = hi - lo;
+    const double support = supportAxis[a];
+    const int nc = ncA[a];
     // cell >= support: every interacting pair sits in adjacent cells
     const double cell = std::max(L / nc, support);
     g.lo[a] = lo;
