@@ -162,6 +162,7 @@ struct sphgpu_ctx {
   double cachedBounds[kBoundsVals] = {};   // min h^-1, min x y z, max x y z, tensor extents of the current state
   bool boundsValid = false;      // cachedBounds describe the current state
   int pairVariant = -1;      // autotuned FP32 pair-kernel variant (-1: not tuned yet)
+  bool omegaStale = false;   // the end-of-step grad-h correction is owed (computed on first read)
   bool pinnedVariant = false;  // set by sphgpu_set_pair_variant
   long tunedN = 0;
 
@@ -640,6 +641,12 @@ void gradh(sphgpu_ctx* c) {
     launchGradh(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
   c->check();
 }
+void settleOmega(sphgpu_ctx* c) {
+  if (!c->omegaStale) return;
+  gradh(c);
+  c->omegaStale = false;
+}
+
 void evalDerivs(sphgpu_ctx* c) {
   ensurePacc(c);
   if (c->fp32() && c->hp.limitedQ) {   // FP32 mirror of the Q's DvDx in the current node order
@@ -798,6 +805,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   c->time = t + hdt;
   copyQGradient(c);                                  // postStateUpdate (mid): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
+  c->omegaStale = false;
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
   {
     Scope sc(c->prof, "update");
@@ -822,7 +830,20 @@ double step(sphgpu_ctx* c, double maxTime) {
   c->check();
   c->time = t + dt;
   copyQGradient(c);                                  // postStateUpdate (end): the Q's DvDx
-  if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (end)
+  // postStateUpdate (end): the grad-h correction of the new state.  Nothing
+  // of the next step reads it before the half-step postStateUpdate computes
+  // it again (the density sum, the dt vote and the half-step update do not
+  // use it), so it is owed rather than computed: every read of the state
+  // outside a step (fields, derivatives, checkpoints, a refresh of the FP32
+  // mirror) settles it first on these same lists.  The FP32 sweep reads only
+  // the mirror this update wrote, which the boundary enforcement below leaves
+  // alone, so the settled values are those of an eager evaluation; the FP64
+  // sweep reads the FP64 positions, so it is owed only when no wall or period
+  // can move a node after it.
+  if (c->cfg.gradh_correction) {
+    if (c->fp32() || c->bcs.empty()) c->omegaStale = true;
+    else gradh(c);
+  }
   {
     Scope sc(c->prof, "enforce");
     launchEnforce(c->F, c->n, c->grid, c->hp.asph != 0, c->stream, &c->lc);
@@ -1137,6 +1158,7 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   CUDA_OK(cudaMemcpy(c->list[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   c->haveNeighbors = false;
   c->initialized = false;
+  c->omegaStale = false;
   refreshParams(c);
   API_END(c)
 }
@@ -1159,6 +1181,7 @@ int sphgpu_checkpoint_size(sphgpu_handle c, size_t* bytes) {
 int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
   API_BEGIN(c)
   requireState(c);
+  settleOmega(c);
   if (!buffer || bytes < checkpointBytes(c->n)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
   const long n = c->n;
   CheckpointHeader h{};
@@ -1232,6 +1255,7 @@ int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
   c->nbCapNext = 0;
   c->haveNeighbors = false;
   c->initialized = true;
+  c->omegaStale = false;
   refreshParams(c);
   API_END(c)
 }
@@ -1244,6 +1268,7 @@ int sphgpu_initialize(sphgpu_handle c) {
   c->check();
   buildNeighbors(c);
   if (c->cfg.gradh_correction) gradh(c);
+  c->omegaStale = false;
   CUDA_OK(cudaStreamSynchronize(c->stream));
   c->initialized = true;
   API_END(c)
@@ -1253,6 +1278,7 @@ int sphgpu_connectivity(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
   refreshParams(c);
+  settleOmega(c);   // on the lists the owed correction belongs to
   buildNeighbors(c);
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
@@ -1261,6 +1287,7 @@ int sphgpu_connectivity(sphgpu_handle c) {
 int sphgpu_sum_density(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
+  settleOmega(c);
   if (!c->haveNeighbors) buildNeighbors(c);
   prepare32(c);
   sumDensity(c);
@@ -1274,6 +1301,7 @@ int sphgpu_gradh(sphgpu_handle c) {
   if (!c->haveNeighbors) buildNeighbors(c);
   prepare32(c);
   gradh(c);
+  c->omegaStale = false;
   CUDA_OK(cudaStreamSynchronize(c->stream));
   API_END(c)
 }
@@ -1282,6 +1310,7 @@ int sphgpu_evaluate_derivatives(sphgpu_handle c) {
   API_BEGIN(c)
   requireState(c);
   refreshParams(c);
+  settleOmega(c);
   if (!c->haveNeighbors) buildNeighbors(c);
   prepare32(c);
   evalDerivs(c);
@@ -1292,6 +1321,7 @@ int sphgpu_evaluate_derivatives(sphgpu_handle c) {
 int sphgpu_dt(sphgpu_handle c, double* dt, int* reason) {
   API_BEGIN(c)
   requireState(c);
+  settleOmega(c);
   refreshParams(c);
   if (!c->haveNeighbors) buildNeighbors(c);
   prepare32(c);
@@ -1397,6 +1427,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   if (ncomp) *ncomp = fs.ncomp;
   if (!out) return SPHGPU_OK;
   requireState(c);
+  settleOmega(c);
   const long n = c->n;
   c->stage.ensure((size_t)n * fs.ncomp * sizeof(double));
   double* st = c->stage.as<double>();
@@ -1416,6 +1447,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
 
 int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   API_BEGIN(c)
+  if (c->n > 0 && c->haveTable) settleOmega(c);   // the state it belongs to is about to change
   c->boundsValid = false;   // the state changes: bounds are measured again
   if (!name || !in) throw Error(SPHGPU_E_ARG, "null argument");
   FieldSpec fs;
@@ -1439,6 +1471,7 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
 int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, const double* mass, const double* rho,
                         const double* eps, const double* H) {
   API_BEGIN(c)
+  if (c->n > 0 && c->haveTable) settleOmega(c);   // the state it belongs to is about to change
   c->boundsValid = false;   // the state changes: bounds are measured again
   requireState(c);
   const long n = c->n;
