@@ -278,7 +278,79 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
       const int nval = min(W, e - base);
       // the home cell's own batch contains node i itself
       const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
-      if (active) {
+      if (!TENSOR && active) {
+        // Isotropic H.  The common path takes no branch per candidate: a
+        // candidate below the band is a neighbour outright, one inside the
+        // band only raises a flag, and the (rare) flagged batches are
+        // rescanned with the exact FP64 criterion afterwards, their
+        // neighbours appended behind the batch's others.  The capacity is
+        // checked once per batch unless the batch could overflow it, and
+        // the self test runs only in the group's own batch of the home cell.
+        const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
+        const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
+        const bool own = dcode == 0 && base == k0;   // group-uniform: here candidate `lane` is node i
+        bool amb = false;
+        if (!WRITE || cnt + nval <= cap) {
+          uint32_t* o = WRITE ? out + (size_t)cnt * 32 : nullptr;
+          int c = 0;
+          if (!own) {
+#pragma unroll 4
+            for (int u = 0; u < nval; ++u) {
+              const float4 cq = stage[wib][u];
+              const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+              const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+              amb |= (e2 >= bandLo) & (e2 <= bandHi);
+              if (e2 < bandLo) {
+                if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
+                ++c;
+              }
+            }
+          } else {
+#pragma unroll 4
+            for (int u = 0; u < nval; ++u) {
+              const float4 cq = stage[wib][u];
+              const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+              const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+              amb |= (e2 >= bandLo) & (e2 <= bandHi);
+              if ((e2 < bandLo) & (u != lane)) {
+                if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
+                ++c;
+              }
+            }
+          }
+          cnt += c;
+        } else {   // this batch may reach the capacity: count past it, store below it
+          for (int u = 0; u < nval; ++u) {
+            const float4 cq = stage[wib][u];
+            const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+            const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+            amb |= (e2 >= bandLo) & (e2 <= bandHi);
+            if ((e2 < bandLo) & (u != self)) {
+              if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
+              ++cnt;
+            }
+          }
+        }
+        if (amb) {   // guard band: the exact FP64 criterion for the flagged candidates
+          for (int u = 0; u < nval; ++u) {
+            const float4 cq = stage[wib][u];
+            const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+            const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+            if (e2 >= bandLo && e2 <= bandHi && u != self) {
+              const int j = base + u;
+              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+              imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
+              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                           qz = __dsub_rn(F.f[F_Z][i], zjd);
+              if (eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2) {
+                if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
+                ++cnt;
+              }
+            }
+          }
+        }
+      }
+      if (TENSOR && active) {
         const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
         // this node shifted by the cell offset: r = (x_i + o) - x_j
         const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
