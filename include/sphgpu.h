@@ -239,13 +239,19 @@ int sphgpu_set_field(sphgpu_handle h, const char* name, const double* in);
  * (any pointer may be NULL to keep that field).  The package's derivative
  * fields stay on the device, as SPHBase owns its derivative FieldLists
  * (src/SPH/SPHBase.hh:223-253) while the NodeLists own the state.
+ * Arrays in page-locked (pinned) host memory are read in place by the
+ * device over the host link, in stream order: keep them unchanged until the
+ * next call that synchronises (step, download_state, synchronize).  Pageable
+ * arrays are copied through a device staging buffer.
  * Replaces: the State field references handed to Physics::evaluateDerivatives
  * (src/Physics/Physics.hh:49-60) when the host owns the FieldLists. */
 int sphgpu_upload_state(sphgpu_handle h, const double* pos, const double* vel, const double* mass, const double* rho,
                         const double* eps, const double* H);
 
 /* Copy the evolved state back to host arrays in caller order (NULL skips a
- * field).  Replaces: reading the NodeList FieldLists after Integrator::step. */
+ * field); pinned arrays are written in place by the device.  Returns when
+ * the arrays hold the state.
+ * Replaces: reading the NodeList FieldLists after Integrator::step. */
 int sphgpu_download_state(sphgpu_handle h, double* pos, double* vel, double* rho, double* eps, double* H);
 
 /* Ordered neighbour pairs (i, j, image) in caller node indices; image packs

@@ -130,6 +130,9 @@ struct sphgpu_ctx {
   DBuf bankA, bankB;   // F_NUM_FIELDS * cap doubles each
   Fields F{}, Falt{};
   DBuf orig[2], list[2], cellc[2];
+  DBuf inv;                  // internal index of each caller index (in-place host transfers)
+  long permVersion = 0;      // bumped whenever the internal order changes
+  long invVersion = -1;      // permVersion the inverse was built for
   DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
   DBuf hten;                 // ASPH: FP32 mirror of tensor H (2 float4 per node)
   DBuf stage;                // host <-> device staging for caller-order transfers
@@ -499,6 +502,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     std::swap(c->bankA, c->bankB);
     std::swap(c->F, c->Falt);
     c->cur = nx;
+    ++c->permVersion;
   }
   c->check();
   const size_t space = (size_t)1 << keyBits;
@@ -1154,6 +1158,7 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   std::vector<int> ids(n);
   for (long i = 0; i < n; ++i) ids[i] = (int)i;
   CUDA_OK(cudaMemcpy(c->orig[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  ++c->permVersion;
   for (long i = 0; i < n; ++i) ids[i] = nodelist ? nodelist[i] : 0;
   CUDA_OK(cudaMemcpy(c->list[0].p, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   c->haveNeighbors = false;
@@ -1239,6 +1244,7 @@ int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
   for (int f = 0; f < F_NUM_PERMUTED; ++f, in += n * sizeof(double))
     CUDA_OK(cudaMemcpyAsync(c->F.f[f], in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_OK(cudaMemcpyAsync(c->orig[0].p, in, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  ++c->permVersion;
   in += n * sizeof(int);
   CUDA_OK(cudaMemcpyAsync(c->list[0].p, in, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CUDA_OK(cudaStreamSynchronize(c->stream));
@@ -1468,6 +1474,32 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   API_END(c)
 }
 
+// The internal index of each caller index, rebuilt after a reordering.
+const int* invOrder(sphgpu_ctx* c) {
+  if (c->invVersion != c->permVersion) {
+    c->inv.ensure((size_t)c->n * sizeof(int));
+    launchInverseOrder(c->origp(), c->inv.as<int>(), c->n, c->stream, &c->lc);
+    c->invVersion = c->permVersion;
+  }
+  return c->inv.as<int>();
+}
+// The device address of a host array of `bytes` bytes when it lies in
+// page-locked memory the device can address (both ends checked); nullptr for
+// pageable memory, which takes the staged copy instead.  Kernels then read or
+// write the pinned array in place over the host link.
+void* mappedHost(const void* p, size_t bytes) {
+  if (!p || bytes == 0) return nullptr;
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  const char* last = static_cast<const char*>(p) + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (b.type != cudaMemoryTypeHost || !b.devicePointer) return nullptr;
+  if (static_cast<char*>(b.devicePointer) - static_cast<char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a.devicePointer;
+}
+
 int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, const double* mass, const double* rho,
                         const double* eps, const double* H) {
   API_BEGIN(c)
@@ -1484,14 +1516,20 @@ int sphgpu_upload_state(sphgpu_handle c, const double* pos, const double* vel, c
   size_t off = 0;
   for (const auto& it : items) {
     if (!it.p) continue;
-    CUDA_OK(cudaMemcpyAsync(st + off, it.p, (size_t)n * it.stride * sizeof(double), cudaMemcpyHostToDevice,
-                            c->stream));
+    const size_t bytes = (size_t)n * it.stride * sizeof(double);
+    if (const void* dp = mappedHost(it.p, bytes)) {   // pinned: read in place, caller order
+      launchScatterInHost(c->F, invOrder(c), static_cast<const double*>(dp), it.first, it.ncomp, it.stride, n,
+                          c->stream, &c->lc);
+      continue;
+    }
+    CUDA_OK(cudaMemcpyAsync(st + off, it.p, bytes, cudaMemcpyHostToDevice, c->stream));
     launchScatterIn(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
     off += (size_t)n * it.stride;
   }
   if (asph && H) launchTensorExtent(c->F, n, c->stream, &c->lc);
   c->check();
-  if (c->haveNeighbors) prepare32(c);
+  // The FP32 mirror is not refreshed here: the step rebuilds it with the
+  // lists, and every other entry that sweeps it refreshes it first.
   API_END(c)
 }
 
@@ -1508,6 +1546,12 @@ int sphgpu_download_state(sphgpu_handle c, double* pos, double* vel, double* rho
   size_t off = 0;
   for (const auto& it : items) {
     if (!it.p) continue;
+    const size_t bytes = (size_t)n * it.stride * sizeof(double);
+    if (void* dp = mappedHost(it.p, bytes)) {   // pinned: written in place, caller order
+      launchGatherOutHost(c->F, invOrder(c), static_cast<double*>(dp), it.first, it.ncomp, it.stride,
+                          it.first == F_HINV && !asph, n, c->stream, &c->lc);
+      continue;
+    }
     if (it.first == F_HINV && !asph) launchGatherOutH(c->F, c->origp(), st + off, F_HINV, n, c->stream, &c->lc);
     else launchGatherOut(c->F, c->origp(), st + off, it.first, it.ncomp, it.stride, n, c->stream, &c->lc);
     CUDA_OK(cudaMemcpyAsync(it.p, st + off, (size_t)n * it.stride * sizeof(double), cudaMemcpyDeviceToHost,

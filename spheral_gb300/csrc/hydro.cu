@@ -351,42 +351,53 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         }
       }
       if (TENSOR && active) {
+        // Tensor H: the scalar pre-filter (h^-1 the smallest eigenvalue)
+        // rejects the far candidates, the rest take the FP32 tensor test on
+        // each side with its own band; candidates inside a band only raise a
+        // flag, and flagged batches are rescanned with the exact FP64 tensor
+        // criterion afterwards (their neighbours appended behind the rest).
         const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
         // this node shifted by the cell offset: r = (x_i + o) - x_j
         const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
+        bool amb = false;
 #pragma unroll 4
         for (int u = 0; u < nval; ++u) {
           const float4 cq = stage[wib][u];
           const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          const float e2 = fminf(ai2, cq.w) * r2;
+          const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
           if (e2 <= bandHi) {
-            bool inside = true;
-            bool exact = !TENSOR && e2 >= bandLo;
-            if (TENSOR) {   // FP32 tensor test, each side with its own band
-              const float4 h0 = stageH[wib][2 * u], h1 = stageH[wib][2 * u + 1];
-              const float e2i = eta2Sym32(hi0, hi1, rx, ry, rz);
-              const float e2j = eta2Sym32(h0, h1, rx, ry, rz);
-              const float jLo = h1.z < 0.5f ? e2t * (1.0f - h1.z) : -1.0f;
-              const float jHi = h1.z < 0.5f ? e2t * (1.0f + h1.z) : FLT_MAX;
-              if (e2i <= tLo || e2j <= jLo) inside = true;
-              else if (e2i >= tHi && e2j >= jHi) inside = false;
-              else exact = true;
+            const float4 h0 = stageH[wib][2 * u], h1 = stageH[wib][2 * u + 1];
+            const float e2i = eta2Sym32(hi0, hi1, rx, ry, rz);
+            const float e2j = eta2Sym32(h0, h1, rx, ry, rz);
+            const float jLo = h1.z < 0.5f ? e2t * (1.0f - h1.z) : -1.0f;
+            const float jHi = h1.z < 0.5f ? e2t * (1.0f + h1.z) : FLT_MAX;
+            const bool in = (e2i <= tLo) | (e2j <= jLo);
+            amb |= !in & !((e2i >= tHi) & (e2j >= jHi));
+            if (in & (u != self)) {
+              if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
+              ++cnt;
             }
-            if (exact) {   // guard band: the exact FP64 criterion (rare)
-              const int j = base + u;
-              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-              const int code = imageCode(g, hc, dcode);
-              imagePos(g, code, xjd, yjd, zjd);
-              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
-                           qz = __dsub_rn(F.f[F_Z][i], zjd);
-              if (TENSOR) {
-                inside = exactTensorCriterion(F, g, i, j, code, qx, qy, qz, ext2);
-              } else {
-                inside = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
-              }
-            }
-            if (inside && u != self) {
+          }
+        }
+        if (amb) {   // guard band: the exact FP64 tensor criterion for the flagged candidates
+          const int code = imageCode(g, hc, dcode);
+          for (int u = 0; u < nval; ++u) {
+            const float4 cq = stage[wib][u];
+            const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+            const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+            if (e2 > bandHi || u == self) continue;
+            const float4 h0 = stageH[wib][2 * u], h1 = stageH[wib][2 * u + 1];
+            const float e2i = eta2Sym32(hi0, hi1, rx, ry, rz);
+            const float e2j = eta2Sym32(h0, h1, rx, ry, rz);
+            const float jLo = h1.z < 0.5f ? e2t * (1.0f - h1.z) : -1.0f;
+            const float jHi = h1.z < 0.5f ? e2t * (1.0f + h1.z) : FLT_MAX;
+            if ((e2i <= tLo) | (e2j <= jLo) | ((e2i >= tHi) & (e2j >= jHi))) continue;   // settled in FP32
+            const int j = base + u;
+            double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+            imagePos(g, code, xjd, yjd, zjd);
+            const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                         qz = __dsub_rn(F.f[F_Z][i], zjd);
+            if (exactTensorCriterion(F, g, i, j, code, qx, qy, qz, ext2)) {
               if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
               ++cnt;
             }
@@ -1153,6 +1164,35 @@ __global__ void scatterInKernel(Fields F, const int* __restrict__ orig, const do
   const long o = (long)orig[k] * stride;
   for (int c = 0; c < ncomp; ++c) F.f[first + c][k] = stage[o + c];
 }
+// Caller-order transfers that address a pinned host array in place: the
+// threads walk the flat host array (n records of `stride` doubles), so the
+// host link sees contiguous reads (writes), and the permutation to the
+// internal order (inv: caller index -> internal index) lands on the device
+// side.  Components past ncomp are skipped on the way in; on the way out an
+// isotropic H (isoH) is written as the SymTensor (a, 0, 0, a, 0, a).
+__global__ void inverseOrderKernel(const int* __restrict__ orig, int* __restrict__ inv, long n) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k < n) inv[orig[k]] = (int)k;
+}
+__global__ void scatterInHostKernel(Fields F, const int* __restrict__ inv, const double* __restrict__ src, int first,
+                                    int ncomp, int stride, long n) {
+  const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e >= n * stride) return;
+  const long m = e / stride;
+  const int c = (int)(e - m * stride);
+  if (c < ncomp) F.f[first + c][inv[m]] = src[e];
+}
+__global__ void gatherOutHostKernel(Fields F, const int* __restrict__ inv, double* __restrict__ dst, int first,
+                                    int ncomp, int stride, int isoH, long n) {
+  const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e >= n * stride) return;
+  const long m = e / stride;
+  const int c = (int)(e - m * stride);
+  double v;
+  if (isoH) v = (c == 0 || c == 3 || c == 5) ? F.f[first][inv[m]] : 0.0;
+  else v = c < ncomp ? F.f[first + c][inv[m]] : 0.0;
+  dst[e] = v;
+}
 // H as SymTensor (xx, xy, xz, yy, yz, zz) <-> isotropic hinv.
 __global__ void gatherOutHKernel(Fields F, const int* __restrict__ orig, double* __restrict__ stage, int field,
                                  long n) {
@@ -1352,6 +1392,20 @@ void launchGatherOut(Fields F, const int* orig, double* stage, int first, int nc
 void launchScatterIn(Fields F, const int* orig, const double* stage, int first, int ncomp, int stride, long n,
                      cudaStream_t s, LaunchCounter* lc) {
   scatterInKernel<<<gridFor(n, 256), 256, 0, s>>>(F, orig, stage, first, ncomp, stride, n);
+  lc->add(1);
+}
+void launchInverseOrder(const int* orig, int* inv, long n, cudaStream_t s, LaunchCounter* lc) {
+  inverseOrderKernel<<<gridFor(n, 256), 256, 0, s>>>(orig, inv, n);
+  lc->add(1);
+}
+void launchScatterInHost(Fields F, const int* inv, const double* src, int first, int ncomp, int stride, long n,
+                         cudaStream_t s, LaunchCounter* lc) {
+  scatterInHostKernel<<<gridFor(n * stride, 256), 256, 0, s>>>(F, inv, src, first, ncomp, stride, n);
+  lc->add(1);
+}
+void launchGatherOutHost(Fields F, const int* inv, double* dst, int first, int ncomp, int stride, bool isoH, long n,
+                         cudaStream_t s, LaunchCounter* lc) {
+  gatherOutHostKernel<<<gridFor(n * stride, 256), 256, 0, s>>>(F, inv, dst, first, ncomp, stride, isoH ? 1 : 0, n);
   lc->add(1);
 }
 void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long n, cudaStream_t s, LaunchCounter* lc) {

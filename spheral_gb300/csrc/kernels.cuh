@@ -113,6 +113,13 @@ void launchGatherOut(Fields F, const int* orig, double* stage, int first, int nc
 void launchScatterIn(Fields F, const int* orig, const double* stage, int first, int ncomp, int stride, long n,
                      cudaStream_t s, LaunchCounter* lc);
 void launchGatherOutH(Fields F, const int* orig, double* stage, int field, long n, cudaStream_t s, LaunchCounter* lc);
+// caller-order transfers on pinned host arrays addressed in place (inv: the
+// internal index of each caller index)
+void launchInverseOrder(const int* orig, int* inv, long n, cudaStream_t s, LaunchCounter* lc);
+void launchScatterInHost(Fields F, const int* inv, const double* src, int first, int ncomp, int stride, long n,
+                         cudaStream_t s, LaunchCounter* lc);
+void launchGatherOutHost(Fields F, const int* inv, double* dst, int first, int ncomp, int stride, bool isoH, long n,
+                         cudaStream_t s, LaunchCounter* lc);
 void launchCountsOut(const int* counts, const int* orig, double* stage, long n, cudaStream_t s, LaunchCounter* lc);
 // check finite / positive state: writes a flag
 void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc);
