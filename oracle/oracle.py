@@ -51,6 +51,8 @@ class OrcConfig(ctypes.Structure):
         ("h_update", ctypes.c_int),
         ("evolve_total_energy", ctypes.c_int),
         ("radial_only", ctypes.c_int),
+        ("hydro", ctypes.c_int),
+        ("rk_volume", ctypes.c_int),
     ]
 
 
@@ -114,6 +116,8 @@ def lib():
             "orc_sym_eigen": (i, [dp, dp, dp]),
             "orc_smoothing_scale_derivative": (i, [dp, dp, dp]),
             "orc_radial_evolution": (i, [dp, dp, d, d, dp]),
+            "orc_rk_volumes": (i, [vp]),
+            "orc_rk_corrections": (i, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -137,6 +141,10 @@ VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
 SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
 # HEvolutionType
 H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
+# hydro package: SPH or CRKSPH (LinearOrder)
+HYDRO = {"sph": 0, "crksph": 1}
+# RKVolumeType (RKCorrectionParams.hh): the volume types without a tessellation
+RK_VOLUME = {"mass_over_density": 0, "sum": 1, "h": 4}
 
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
@@ -145,6 +153,7 @@ FIELD_NCOMP = {
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
     "DepsDtCompatible": 1, "ArtificialViscosityVelocityGradient": 9, "massSecondMoment": 6,
+    "volume": 1, "rkCorrections": 16,
 }
 
 
@@ -190,6 +199,8 @@ class Oracle:
         c.h_update = H_UPDATE[cfg.get("h_update", "ideal")]
         c.evolve_total_energy = int(cfg.get("evolve_total_energy", False))
         c.radial_only = int(cfg.get("radial_only", False))
+        c.hydro = HYDRO[cfg.get("hydro", "sph")]
+        c.rk_volume = RK_VOLUME[cfg.get("rk_volume", "sum")]
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))
@@ -229,6 +240,12 @@ class Oracle:
 
     def gradh(self):
         self.L.orc_gradh(self.h)
+
+    def rk_volumes(self):
+        self.L.orc_rk_volumes(self.h)
+
+    def rk_corrections(self):
+        self.L.orc_rk_corrections(self.h)
 
     def apply_ghosts(self):
         self.L.orc_apply_ghosts(self.h)

@@ -40,6 +40,11 @@
 //   src/Geometry/GeomSymmetricTensorInline.hh:1650-1747,2230-2260
 //   src/Geometry/GeomTensorInline.hh:1885-1972
 //   src/Gravity/TreeGravity.cc:55-82,146-480,819-932, TreeGravityInline.hh:38-165
+//   CRKSPH: src/CRKSPH/CRKSPH.cc:143-380, CRKSPHBase.cc:190-225,
+//   src/CRKSPH/computeCRKSPHSumMassDensity.cc:15-110, src/RK/RKCorrections.cc:300-420,
+//   src/RK/RKUtilities.cc:66-80,181-206,250-491, RKUtilitiesInline.hh:155-163,345-351,
+//   src/RK/computeRKVolumes.cc:20-70, computeRKSumVolume.cc:30-110, computeHVolumes.cc:25-60,
+//   src/RK/ContinuityVolumePolicy.cc:40-75, src/Boundary/ReflectingBoundary.cc:402-432
 //
 // Third-party arithmetic: the reference fits each quadratic table interval
 // with Eigen's 3x3 inverse and solves the Hermite knot system with Eigen's
@@ -48,6 +53,7 @@
 // coefficients agree with the reference to rounding, bit parity is unpinned.
 // =============================================================================
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -486,6 +492,7 @@ struct TableKernel {
   int numPoints = 0;
   double kernelValueSPH(double eta) const { return eta < extent ? std::fabs(gW(eta)) : 0.0; }
   double kernelValue(double eta, double Hdet) const { return eta < extent ? Hdet * W(eta) : 0.0; }
+  double gradValue(double eta, double Hdet) const { return eta < extent ? Hdet * gW(eta) : 0.0; }
   void kernelAndGradValue(double eta, double Hdet, double& w, double& g) const {
     if (eta < extent) { const size_t i0 = W.lowerBound(eta); w = Hdet * W.at(eta, i0); g = Hdet * gW.at(eta, i0); }
     else { w = 0.0; g = 0.0; }
@@ -562,6 +569,8 @@ struct Config {
   int radialOnly = 0;        // ASPHClassicSmoothingScale radialOnly (ASPHRadialFunctor defaults: about the origin)
   int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
   int evolveTotalEnergy = 0; // SPH evolveTotalEnergy (SPH.cc:105-108, 541)
+  int hydro = 0;             // 0 SPH, 1 CRKSPH (CRKSPHHydros.py:9-110, LinearOrder)
+  int rkVolume = 1;          // RKVolumeType: 0 RKMassOverDensity, 1 RKSumVolume, 4 HVolume
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
   double G = 1.0, softening = 0.01, opening = 0.5, ftimestep = 0.1;
@@ -595,6 +604,11 @@ struct Problem {
   vector<V3> pos, vel;
   vector<double> mass, rho, eps, P, cs, omega;
   vector<ST> H;
+  // CRKSPH: the RK volume and the LinearOrder corrections (C_0..3, then
+  // dC/dx, dC/dy, dC/dz, 4 each: RKUtilities offsetGradC)
+  typedef std::array<double, 16> RKC;
+  vector<double> vol;
+  vector<RKC> rkc;
   vector<int> list;
   // ghost transform bookkeeping: for each ghost: control index and per-axis code
   vector<int> ctrl;      // flat control index (ultimately an internal node)
@@ -621,7 +635,7 @@ struct Problem {
 
   void resizeAll(int n) {
     pos.resize(n); vel.resize(n); mass.resize(n); rho.resize(n); eps.resize(n); P.resize(n); cs.resize(n);
-    omega.resize(n, 1.0); H.resize(n); list.resize(n);
+    omega.resize(n, 1.0); H.resize(n); list.resize(n); vol.resize(n, 0.0); rkc.resize(n, RKC{});
   }
   void resizeDerivs() {
     const int n = nTot;
@@ -719,7 +733,7 @@ struct Problem {
             const int g = nTot++;
             pos.push_back(pos[c]); vel.push_back(vel[c]); mass.push_back(mass[c]); rho.push_back(rho[c]);
             eps.push_back(eps[c]); P.push_back(P[c]); cs.push_back(cs[c]); omega.push_back(omega[c]);
-            H.push_back(H[c]); list.push_back(list[c]);
+            H.push_back(H[c]); list.push_back(list[c]); vol.push_back(vol[c]); rkc.push_back(rkc[c]);
             const int root = ctrl[c] < 0 ? c : ctrl[c];
             ctrl.push_back(root);
             const int code = (b.type == 0 ? (sub == 0 ? 1 : 2) : (b.wallHigh ? 2 : 1));
@@ -758,6 +772,7 @@ struct Problem {
           comp(pos[g], b.axis) = mapCoord(compc(pos[c], b.axis), wEx, sEx, wEn, sEn);
           H[g] = H[c]; mass[g] = mass[c]; rho[g] = rho[c]; eps[g] = eps[c]; P[g] = P[c]; cs[g] = cs[c];
           omega[g] = omega[c]; vel[g] = vel[c];
+          if (cfg.hydro == 1) vol[g] = vol[c];
           if (b.type == 1) {
             comp(vel[g], b.axis) = -compc(vel[c], b.axis);
             // (R H R).Symmetric(): flips the off-diagonal terms that touch the axis
@@ -1187,6 +1202,292 @@ struct Problem {
     Hideal[i] = fromEigen(d, he.vec);
   }
 
+  //============================================================================
+  // CRKSPH with LinearOrder reproducing kernels.
+  //============================================================================
+  // ReflectingBoundary::applyGhostBoundary for RKCoefficients
+  // (ReflectingBoundary.cc:402-432) with the reflection operator of
+  // RKUtilities::getTransformationMatrix: for a wall normal to axis a an entry
+  // changes sign once per index equal to a (C_{1+a}; dC_a[0]; dC_a[1+k] and
+  // dC_k[1+a] for k != a; dC_a[1+a] keeps its sign).
+  static void reflectRKC(RKC& c, int a) {
+    c[1 + a] = -c[1 + a];
+    for (int d = 0; d < 3; ++d)
+      for (int k = 0; k < 4; ++k) {
+        const int flips = (d == a ? 1 : 0) + ((k >= 1 && k - 1 == a) ? 1 : 0);
+        if (flips == 1) c[4 + 4 * d + k] = -c[4 + 4 * d + k];
+      }
+  }
+  void applyGhostRKC() { applyGhostField(rkc, [](RKC& c, int a) { reflectRKC(c, a); }); }
+
+  // computeRKVolumes (computeRKVolumes.cc:20-70) for the volume types that
+  // need no tessellation: RKMassOverDensity, RKSumVolume
+  // (computeRKSumVolume.cc:30-110), HVolume (computeHVolumes.cc:25-60, with
+  // the first NodeList's nPerh).
+  void computeRKVolumes() {
+    vol.resize(nTot);
+    if (cfg.rkVolume == 0) {
+      for (int i = 0; i < nInt; ++i) vol[i] = mass[i] / rho[i];
+    } else if (cfg.rkVolume == 4) {
+      const double nPerh = lists[0].nPerh;
+      for (int i = 0; i < nInt; ++i) vol[i] = 0.125 * 4.0 / 3.0 * M_PI / detS(scaleS(nPerh, H[i]));
+    } else {
+      const double etaVolMax = std::pow(0.5 * W.extent, 3) * (4.0 / 3.0 * M_PI);
+      const double W0 = W.kernelValue(0.0, 1.0);
+      vector<double> acc(nTot, 0.0);
+      pairSweep(pairs.size(), acc, nTot, [&](long kk, vector<double>& p) {
+        const int i = pairs[kk].first, j = pairs[kk].second;
+        const V3 rij = sub(pos[i], pos[j]);
+        p[i] += W.kernelValue(mag(dotSV(H[i], rij)), detS(H[i]));
+        p[j] += W.kernelValue(mag(dotSV(H[j], rij)), detS(H[j]));
+      });
+      for (int i = 0; i < nInt; ++i) {
+        const double Hdeti = detS(H[i]);
+        const double v = acc[i] + Hdeti * W0;
+        vol[i] = std::min(etaVolMax / Hdeti, 1.0 / v);
+      }
+    }
+    applyGhostScalar(vol);
+  }
+
+  // computeCRKSPHSumMassDensity (computeCRKSPHSumMassDensity.cc:15-110):
+  // pairs of the same NodeList, plain kernel of each side's own H.
+  void crkSumMassDensity() {
+    struct Acc { double wsum = 0, rho = 0, vol1 = 0;
+                 Acc& operator+=(const Acc& o) { wsum += o.wsum; rho += o.rho; vol1 += o.vol1; return *this; } };
+    vector<Acc> acc(nTot);
+    pairSweep(pairs.size(), acc, nTot, [&](long kk, vector<Acc>& p) {
+      const int i = pairs[kk].first, j = pairs[kk].second;
+      if (list[i] != list[j]) return;
+      const V3 rij = sub(pos[i], pos[j]);
+      const double Wi = W.kernelValue(mag(dotSV(H[i], rij)), detS(H[i]));
+      const double Wj = W.kernelValue(mag(dotSV(H[j], rij)), detS(H[j]));
+      const double Vi = vol[i], Vj = vol[j];
+      p[i].wsum += Vj * Wj; p[j].wsum += Vi * Wi;
+      p[i].rho += mass[j] * Vj * Wj; p[j].rho += mass[i] * Vi * Wi;
+      p[i].vol1 += Vj * Vj * Wj; p[j].vol1 += Vi * Vi * Wi;
+    });
+    const double W0 = W.kernelValue(0.0, 1.0);
+    for (int i = 0; i < nInt; ++i) {
+      const auto& L = lists[list[i]];
+      const double mi = mass[i], Vi = vol[i], Hdeti = detS(H[i]);
+      const double wsum = acc[i].wsum + Vi * Hdeti * W0;
+      const double vol1 = (acc[i].vol1 + Vi * Vi * Hdeti * W0) / wsum;
+      rho[i] = std::max(std::max(L.rhoMin, 0.1 * mi * Hdeti),
+                        std::min(L.rhoMax, (acc[i].rho + mi * Vi * Hdeti * W0) / (wsum * vol1)));
+    }
+    applyGhostScalar(rho);
+  }
+
+  // RKUtilities::evaluateBaseKernelAndGradient (RKUtilities.cc:66-80)
+  void rkBase(const V3& x, const ST& Hm, double& w, V3& dw) const {
+    const V3 eta = dotSV(Hm, x);
+    const double etaMag = mag(eta);
+    const V3 etaUnit = unitVector(eta);
+    const double Hdet = detS(Hm);
+    w = W.kernelValue(etaMag, Hdet);
+    const double dk = W.gradValue(etaMag, Hdet);
+    dw = mul(dotSV(Hm, etaUnit), dk);
+  }
+  // RKUtilities::evaluateKernelAndGradient (RKUtilities.cc:181-206), LinearOrder:
+  // P = (1, x, y, z), dP/dx_d = e_{1+d}; inner products summed from index 0.
+  void rkKernelAndGradient(const V3& x, const ST& Hm, const RKC& c, double& WR, V3& gradWR) const {
+    double w; V3 dw;
+    rkBase(x, Hm, w, dw);
+    const double P[4] = {1.0, x.x, x.y, x.z};
+    double CP = 0.0;
+    for (int k = 0; k < 4; ++k) CP += c[k] * P[k];
+    double g[3];
+    for (int d = 0; d < 3; ++d) {
+      const double CdP = c[1 + d];
+      double dCP = 0.0;
+      for (int k = 0; k < 4; ++k) dCP += c[4 + 4 * d + k] * P[k];
+      g[d] = (CdP + dCP) * w + CP * compc(dw, d);
+    }
+    WR = CP * w;
+    gradWR = {g[0], g[1], g[2]};
+  }
+  // 4x4 solve by Gaussian elimination with partial pivoting (the reference
+  // uses Eigen's colPivHouseholderQr; any accurate solver gives the same
+  // corrections to rounding).  A is overwritten by its LU factors; piv
+  // records the row order.
+  static void lu4(double A[4][4], int piv[4]) {
+    for (int k = 0; k < 4; ++k) piv[k] = k;
+    for (int k = 0; k < 4; ++k) {
+      int p = k;
+      for (int r = k + 1; r < 4; ++r) if (std::fabs(A[r][k]) > std::fabs(A[p][k])) p = r;
+      if (p != k) { for (int c = 0; c < 4; ++c) std::swap(A[k][c], A[p][c]); std::swap(piv[k], piv[p]); }
+      const double inv = 1.0 / A[k][k];
+      for (int r = k + 1; r < 4; ++r) {
+        const double f = A[r][k] * inv;
+        A[r][k] = f;
+        for (int c = k + 1; c < 4; ++c) A[r][c] -= f * A[k][c];
+      }
+    }
+  }
+  static void solve4(const double LU[4][4], const int piv[4], const double b[4], double x[4]) {
+    double y[4];
+    for (int r = 0; r < 4; ++r) {
+      double v = b[piv[r]];
+      for (int c = 0; c < r; ++c) v -= LU[r][c] * y[c];
+      y[r] = v;
+    }
+    for (int r = 3; r >= 0; --r) {
+      double v = y[r];
+      for (int c = r + 1; c < 4; ++c) v -= LU[r][c] * x[c];
+      x[r] = v / LU[r][r];
+    }
+  }
+  // RKUtilities::computeCorrections (RKUtilities.cc:250-491), LinearOrder, no
+  // Hessian: moments over the neighbours of i and i itself with the
+  // scatter kernel W(x_ij, H_j), then C = M^-1 e_0, dC_d = -M^-1 (dM_d C);
+  // ghost values follow (RKCorrections::initialize returns true, so the
+  // integrator applies the ghost boundaries after it).
+  void computeRKCorrections() {
+    rkc.resize(nTot);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nInt; ++i) {
+      double M[4][4] = {}, dM[3][4][4] = {};
+      auto addTo = [&](int j) {
+        const V3 xij = sub(pos[i], pos[j]);
+        double w; V3 dw;
+        rkBase(xij, H[j], w, dw);
+        const double vj = vol[j];
+        const double p[4] = {1.0, xij.x, xij.y, xij.z};
+        for (int k = 0; k < 4; ++k)
+          for (int l = k; l < 4; ++l) M[k][l] += vj * p[k] * p[l] * w;
+        for (int d = 0; d < 3; ++d)
+          for (int k = 0; k < 4; ++k)
+            for (int l = k; l < 4; ++l) {
+              const double dpk = (k == 1 + d) ? 1.0 : 0.0, dpl = (l == 1 + d) ? 1.0 : 0.0;
+              dM[d][k][l] += vj * ((dpk * p[l] + p[k] * dpl) * w + p[k] * p[l] * compc(dw, d));
+            }
+      };
+      for (int j : neighbors[i]) addTo(j);
+      addTo(i);
+      for (int k = 0; k < 4; ++k)
+        for (int l = 0; l < k; ++l) {
+          M[k][l] = M[l][k];
+          for (int d = 0; d < 3; ++d) dM[d][k][l] = dM[d][l][k];
+        }
+      int piv[4];
+      lu4(M, piv);
+      const double e0[4] = {1.0, 0.0, 0.0, 0.0};
+      double C[4];
+      solve4(M, piv, e0, C);
+      RKC out{};
+      for (int k = 0; k < 4; ++k) out[k] = C[k];
+      for (int d = 0; d < 3; ++d) {
+        double rhs[4], dC[4];
+        for (int k = 0; k < 4; ++k) {
+          double v = 0.0;
+          for (int l = 0; l < 4; ++l) v += dM[d][k][l] * C[l];
+          rhs[k] = -v;
+        }
+        solve4(M, piv, rhs, dC);
+        for (int k = 0; k < 4; ++k) out[4 + 4 * d + k] = dC[k];
+      }
+      rkc[i] = out;
+    }
+    applyGhostRKC();
+  }
+
+  // CRKSPH::evaluateDerivativesImpl (CRKSPH.cc:180-380) with the
+  // SPHSmoothingScale moments (SPHSmoothingScale.cc:150-275).
+  struct CrkAcc {
+    double DepsDt = 0, maxQ = 0, effQ = 0, m0 = 0;
+    V3 DvDt, xsphDV, m1;
+    T9 DvDx, localDvDx;
+    CrkAcc& operator+=(const CrkAcc& o) {
+      DepsDt += o.DepsDt; maxQ = std::max(maxQ, o.maxQ); effQ += o.effQ; m0 += o.m0;
+      DvDt = add(DvDt, o.DvDt); xsphDV = add(xsphDV, o.xsphDV); m1 = add(m1, o.m1);
+      addT(DvDx, o.DvDx); addT(localDvDx, o.localDvDx);
+      return *this;
+    }
+  };
+  void evaluateDerivativesCRK() {
+    const bool compatible = cfg.compatibleEnergy != 0, XSPH = cfg.XSPH != 0;
+    vector<CrkAcc> acc(nTot);
+    pairAccel.assign(pairs.size(), V3{});
+    pairSweep(pairs.size(), acc, nTot, [&](long kk, vector<CrkAcc>& p) {
+      const int i = pairs[kk].first, j = pairs[kk].second;
+      const V3 ri = pos[i], vi = vel[i]; const double mi = mass[i], rhoi = rho[i], Pi = P[i], ci = cs[i];
+      const V3 rj = pos[j], vj = vel[j]; const double mj = mass[j], rhoj = rho[j], Pj = P[j], cj = cs[j];
+      const ST Hi = H[i], Hj = H[j];
+      const double weighti = vol[i], weightj = vol[j];
+      auto& ai = p[i]; auto& aj = p[j];
+      const V3 rij = sub(ri, rj), vij = sub(vi, vj);
+      const V3 etai = dotSV(Hi, rij), etaj = dotSV(Hj, rij);
+      double Wi, Wj; V3 gradWi, gradWj;
+      rkKernelAndGradient(rij, Hj, rkc[i], Wj, gradWj);
+      rkKernelAndGradient(mul(-1.0, rij), Hi, rkc[j], Wi, gradWi);
+      const V3 deltagrad = sub(gradWj, gradWi);
+      double QPiij_, QPiji_, Qi, Qj;
+      QPiij(QPiij_, QPiji_, Qi, Qj, ri, etai, vi, rhoi, ci, rj, etaj, vj, rhoj, cj, DvDxQ[i], DvDxQ[j]);
+      const V3 Qaccij = mul(rhoi * rhoi * QPiij_ + rhoj * rhoj * QPiji_, deltagrad);
+      const double workQi = dot(mul(rhoj * rhoj * QPiji_, vij), deltagrad);
+      const double workQj = dot(mul(rhoi * rhoi * QPiij_, vij), deltagrad);
+      ai.maxQ = std::max(ai.maxQ, 4.0 * Qi); aj.maxQ = std::max(aj.maxQ, 4.0 * Qj);
+      ai.effQ += weightj * Qi * Wj; aj.effQ += weighti * Qj * Wi;
+      const T9 dDi = scaleT(weightj, dyad(vij, gradWj)), dDj = scaleT(weighti, dyad(vij, gradWi));
+      subT(ai.DvDx, dDi); addT(aj.DvDx, dDj);
+      if (list[i] == list[j]) { subT(ai.localDvDx, dDi); addT(aj.localDvDx, dDj); }
+      const V3 force = mul(0.5 * weighti * weightj, add(mul(Pi + Pj, deltagrad), Qaccij));
+      ai.DvDt = sub(ai.DvDt, mul(force, 1.0 / mi));
+      aj.DvDt = add(aj.DvDt, mul(force, 1.0 / mj));
+      if (compatible) pairAccel[kk] = mul(force, -1.0 / mi);
+      ai.DepsDt += 0.5 * weighti * weightj * (Pj * dot(vij, deltagrad) + workQi) / mi;
+      aj.DepsDt += 0.5 * weighti * weightj * (Pi * dot(vij, deltagrad) + workQj) / mj;
+      if (XSPH && list[i] == list[j]) {
+        ai.xsphDV = sub(ai.xsphDV, mul(weightj * Wj, vij));
+        aj.xsphDV = add(aj.xsphDV, mul(weighti * Wi, vij));
+      }
+      // SPHSmoothingScale moments
+      const double fweightij = (list[i] != list[j]) ? mj * rhoi / (mi * rhoj) : 1.0;
+      const double WSPHi = W.kernelValueSPH(mag(etai)), WSPHj = W.kernelValueSPH(mag(etaj));
+      ai.m0 += fweightij * WSPHi; aj.m0 += 1.0 / fweightij * WSPHj;
+      ai.m1 = sub(ai.m1, mul(fweightij * WSPHi, etai)); aj.m1 = add(aj.m1, mul(1.0 / fweightij * WSPHj, etaj));
+    });
+    for (int i = 0; i < nInt; ++i) {
+      auto& a = acc[i];
+      const double mi = mass[i], rhoi = rho[i]; const V3 vi = vel[i];
+      DvDx[i] = a.DvDx; localDvDx[i] = a.localDvDx;
+      M[i] = T9{}; localM[i] = T9{}; gradRho[i] = V3{}; rhoSum[i] = 0.0; normalization[i] = 0.0;
+      XSPHWeightSum[i] = 0.0;
+      XSPHDeltaV[i] = a.xsphDV;
+      DxDt[i] = XSPH ? add(vi, a.xsphDV) : vi;
+      DrhoDt[i] = -rhoi * traceT(a.DvDx);
+      DvDt[i] = a.DvDt;
+      DepsDt[i] = cfg.evolveTotalEnergy ? mi * (dot(vi, a.DvDt) + a.DepsDt) : a.DepsDt;
+      maxQ[i] = a.maxQ; effQ[i] = a.effQ;
+      // SPHSmoothingScale finalize (SPHSmoothingScale.cc:232-272)
+      const auto& L = lists[list[i]];
+      const double m0 = rootnu3(std::max(0.0, a.m0));
+      massZeroth[i] = m0; massFirst[i] = a.m1;
+      const double tr = traceT(a.DvDx);
+      DHDt[i] = ST{-H[i].xx / 3 * tr, -H[i].xy / 3 * tr, -H[i].xz / 3 * tr, -H[i].yy / 3 * tr, -H[i].yz / 3 * tr,
+                   -H[i].zz / 3 * tr};
+      const double cur = fuzzyEqual(m0, 0.0) ? 0.5 * L.nPerh : W.equivalentNodesPerSmoothingScale(m0);
+      const double s = std::min(4.0, std::max(0.25, L.nPerh / (cur + 1.0e-30)));
+      const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
+      const double hi0 = 1.0 / H[i].xx;
+      const double hi1 = std::min(L.hmax, std::max(L.hmin, hi0 * (1.0 - aa + aa * s)));
+      const double hinv = 1.0 / hi1;
+      Hideal[i] = ST{hinv, 0.0, 0.0, hinv, 0.0, hinv};
+    }
+  }
+
+  // ContinuityVolumePolicy::update (ContinuityVolumePolicy.cc:40-75): fires
+  // after the mass density (its dependency), so it sees the updated rho and H.
+  void volumeUpdate(double multiplier) {
+    for (int i = 0; i < nInt; ++i) {
+      const double volMin = 0.5 * mass[i] * safeInvVar(rho[i]);
+      const double volMax = 4.0 * M_PI / (3.0 * detS(H[i]));
+      const double dVdt = -mass[i] * safeInvVar(rho[i] * rho[i]) * DrhoDt[i];
+      vol[i] = std::max(volMin, std::min(volMax, vol[i] + multiplier * dVdt));
+    }
+  }
+
   // SPHBase::finalizeDerivatives: ghost values of DvDt and DepsDt.
   void finalizeDerivatives() {
     if (cfg.compatibleEnergy) { applyGhostVector(DvDt); applyGhostScalar(DepsDt); }
@@ -1317,6 +1618,7 @@ struct Problem {
         H[i] = clampH(Hideal[i], 1.0 / L.hmax, 1.0 / L.hmin);
       }
     }
+    if (cfg.hydro == 1) volumeUpdate(multiplier);
     updateEOS(nInt);
   }
 
@@ -1511,6 +1813,12 @@ struct Problem {
     applyGhostState();
     updateEOS(nTot);
     applyGhostState();
+    if (cfg.hydro == 1) {
+      // RKCorrections::initializeProblemStartupDependencies (RKCorrections.cc:85-150)
+      computeRKVolumes();
+      computeRKCorrections();
+      return;
+    }
     if (cfg.gradhCorrection) omegaGradh();
   }
 
@@ -1528,14 +1836,23 @@ struct Problem {
       radius0.assign(nInt, 0.0);
       for (int i = 0; i < nInt; ++i) radius0[i] = mag(pos[i]);
     }
-    if (cfg.densityUpdate == 0) sumMassDensity();
+    if (cfg.hydro == 1) {
+      // RKCorrections::preStepInitialize (volumes), then
+      // CRKSPHBase::preStepInitialize (CRKSPHBase.cc:190-225, the CRK sum).
+      // The corrections RKCorrections::initialize computes at t are
+      // recomputed at t + dt/2 before anything reads them.
+      computeRKVolumes();
+      if (cfg.densityUpdate == 0) crkSumMassDensity();
+    } else if (cfg.densityUpdate == 0) {
+      sumMassDensity();
+    }
     // initializeDerivatives(t, 0): TreeGravity::initialize builds the tree
     if (cfg.gravity) buildTree();
     const double dt = selectDt(std::min(cfg.dtMin, maxTime - t), std::min(cfg.dtMax, maxTime - t));
     const double hdt = 0.5 * dt;
     // state0 copy (internal + ghost values)
     const auto pos0 = pos; const auto vel0 = vel; const auto rho0 = rho; const auto eps0 = eps;
-    const auto H0 = H; const auto P0 = P; const auto cs0 = cs; const auto omega0 = omega;
+    const auto H0 = H; const auto P0 = P; const auto cs0 = cs; const auto omega0 = omega; const auto vol0 = vol;
     // mid-step: timeAdvanceOnly update with the previous derivatives
     stateUpdate(hdt, true);
     time = t + hdt;
@@ -1544,11 +1861,16 @@ struct Problem {
     if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
     // derivatives at the midpoint
     if (cfg.gravity) buildTree();
-    evaluateDerivatives();
+    if (cfg.hydro == 1) {
+      computeRKCorrections();   // RKCorrections::initialize(t + dt/2)
+      evaluateDerivativesCRK();
+    } else {
+      evaluateDerivatives();
+    }
     if (cfg.gravity) applyTreeForces();
     finalizeDerivatives();
     // full step from state0
-    pos = pos0; vel = vel0; rho = rho0; eps = eps0; H = H0; P = P0; cs = cs0; omega = omega0;
+    pos = pos0; vel = vel0; rho = rho0; eps = eps0; H = H0; P = P0; cs = cs0; omega = omega0; vol = vol0;
     stateUpdate(dt, false);
     time = t + dt;
     applyGhostState();
@@ -1595,6 +1917,7 @@ struct orc_config {
   int viscosity;
   double eta_crit_frac, eta_fold_frac;
   int smoothing_scale, fix_shape, h_update, evolve_total_energy, radial_only;
+  int hydro, rk_volume;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1610,6 +1933,7 @@ void* orc_create(const orc_config* c) {
   g.viscosity = c->viscosity; g.etaCritFrac = c->eta_crit_frac; g.etaFoldFrac = c->eta_fold_frac;
   g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape; g.hUpdate = c->h_update;
   g.evolveTotalEnergy = c->evolve_total_energy; g.radialOnly = c->radial_only;
+  g.hydro = c->hydro; g.rkVolume = c->rk_volume;
   p->lastDt = c->last_dt; p->time = c->time;
   p->W.build(c->num_table_points);
   return p;
@@ -1693,12 +2017,20 @@ int orc_connectivity(void* h) {
   return 0;
 }
 int orc_update_eos(void* h) { auto* p = static_cast<Problem*>(h); p->updateEOS(p->nTot); return 0; }
-int orc_sum_density(void* h) { static_cast<Problem*>(h)->sumMassDensity(); return 0; }
+int orc_sum_density(void* h) {
+  auto* p = static_cast<Problem*>(h);
+  if (p->cfg.hydro == 1) p->crkSumMassDensity(); else p->sumMassDensity();
+  return 0;
+}
+// CRKSPH: the RK volumes (RKCorrections::preStepInitialize) and the
+// corrections (RKCorrections::initialize) of the current state
+int orc_rk_volumes(void* h) { static_cast<Problem*>(h)->computeRKVolumes(); return 0; }
+int orc_rk_corrections(void* h) { static_cast<Problem*>(h)->computeRKCorrections(); return 0; }
 int orc_gradh(void* h) { auto* p = static_cast<Problem*>(h); p->omegaGradh(); return 0; }
 int orc_apply_ghosts(void* h) { static_cast<Problem*>(h)->applyGhostState(); return 0; }
 int orc_eval_derivs(void* h) {
   auto* p = static_cast<Problem*>(h);
-  p->evaluateDerivatives();
+  if (p->cfg.hydro == 1) p->evaluateDerivativesCRK(); else p->evaluateDerivatives();
   p->finalizeDerivatives();
   return 0;
 }
@@ -1791,6 +2123,12 @@ int orc_get_field(void* h, const char* name, double* out) {
   if (s == "DvDtGravity") return v3(p->DvDtGrav);
   if (s == "potential") return sc(p->potential);
   if (s == "DepsDtCompatible") return sc(p->DepsDtCompat);
+  if (s == "volume") return sc(p->vol);
+  if (s == "rkCorrections") {
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 16; ++k) out[16 * i + k] = p->rkc[i][k];
+    return 16;
+  }
   return -1;
 }
 // Overwrite a state field (internal nodes) by name.

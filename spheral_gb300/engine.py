@@ -18,6 +18,7 @@ FIELD_NCOMP = {
     "maxViscousPressure": 1, "effViscousPressure": 1, "XSPHWeightSum": 1, "XSPHDeltaV": 3, "DHDt": 6,
     "Hideal": 6, "massZerothMoment": 1, "massFirstMoment": 3, "DvDtGravity": 3, "potential": 1,
     "DepsDtCompatible": 1, "numNeighbors": 1, "ArtificialViscosityVelocityGradient": 9, "massSecondMoment": 6,
+    "volume": 1, "rkCorrections": 16,
 }
 
 DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acceleration", "velocity magnitude",

@@ -1,0 +1,102 @@
+"""CPU checks of the oracle's CRKSPH restatement (src/CRKSPH/CRKSPH.cc,
+src/RK/RKUtilities.cc LinearOrder, computeCRKSPHSumMassDensity.cc,
+computeRKVolumes.cc, ContinuityVolumePolicy.cc).
+
+* Linear reproduction, the defining property of the LinearOrder corrections:
+  for v = A x the CRK velocity gradient is A at every node, free surfaces
+  included (open boundaries), for each volume type.
+* The corrections of a mirror image follow the reflection operator of the
+  coefficients: a reflecting box and its periodic twin give the same
+  interior derivatives only through that transform, so the wall case is
+  checked for conservation instead.
+* Compatible-energy CRKSPH steps conserve momentum (periodic) and energy to
+  rounding; the volume stays within the ContinuityVolumePolicy bounds.
+* The CRK mass density of a uniform lattice with V = m / rho is rho.
+"""
+import numpy as np
+import pytest
+
+from spheral_gb300 import problems
+
+
+@pytest.mark.parametrize("rk_volume", ["sum", "mass_over_density", "h"])
+def test_linear_velocity_gradient_reproduced(oracle_mod, rk_volume):
+    A = np.array([[0.3, -0.2, 0.1], [0.05, -0.4, 0.25], [0.15, 0.2, 0.35]])
+    p = problems.crksph_box(n_side=8, seed=31, boundaries="open", rk_volume=rk_volume, linear_velocity=A)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    o.rk_corrections()
+    o.evaluate_derivatives()
+    D = o.field("DvDx").reshape(-1, 3, 3)
+    err = np.abs(D - A[None]).max()
+    assert err < 1e-10, err
+    assert o.field("volume").min() > 0.0
+
+
+def _reflect_rkc(c, a):
+    """The reflection operator of the LinearOrder coefficients for a plane
+    normal to axis a: an entry flips once per index equal to a."""
+    c = c.copy()
+    c[..., 1 + a] *= -1.0
+    for d in range(3):
+        for k in range(4):
+            flips = (d == a) + (k >= 1 and k - 1 == a)
+            if flips == 1:
+                c[..., 4 + 4 * d + k] *= -1.0
+    return c
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_corrections_follow_the_reflection_operator(oracle_mod, axis):
+    # a periodic node set symmetric under x_a -> 1 - x_a: the corrections of
+    # mirror partners are related by the operator the ghosts of a
+    # reflecting wall apply (ReflectingBoundary.cc:402-432)
+    rng = np.random.default_rng(40 + axis)
+    half = problems._lattice(8, 8, 8, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    half = half[half[:, axis] < 0.5]
+    half = half + rng.normal(0.0, 0.02 / 8, half.shape)
+    mirror = half.copy()
+    mirror[:, axis] = 1.0 - mirror[:, axis]
+    p = problems.crksph_box(n_side=8, seed=41, boundaries="periodic", vel_scale=0.0)
+    pos = np.vstack([half, mirror])
+    n = len(pos)
+    h = np.concatenate([1.51 / 8 * (1 + 0.05 * rng.uniform(-1, 1, len(half)))] * 2)
+    m = np.concatenate([p.mass[:len(half)]] * 2)
+    p = problems.Problem("mirror_pairs", pos, np.zeros((n, 3)), m, np.ones(n), np.ones(n), h, None,
+                         p.nodelists, p.boundaries, p.config)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    c = o.field("rkCorrections")
+    k = len(half)
+    want = _reflect_rkc(c[:k], axis)
+    assert np.allclose(c[k:], want, rtol=1e-9, atol=1e-9 * np.abs(c).max())
+    assert np.abs(c[:k, 1 + axis]).max() > 1e-6 * np.abs(c[:k, 0]).max()   # the odd entries are not all zero
+
+
+@pytest.mark.parametrize("boundaries", ["periodic", "reflecting", "open"])
+def test_crksph_steps_conserve(oracle_mod, boundaries):
+    p = problems.crksph_box(n_side=8, seed=35, boundaries=boundaries, vel_scale=0.2)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    c0 = o.conservation()
+    for _ in range(4):
+        o.step()
+    c1 = o.conservation()
+    assert abs(c1[7] - c0[7]) < 1e-12 * abs(c0[7])
+    if boundaries != "reflecting":
+        assert np.abs(c1[1:4] - c0[1:4]).max() < 1e-12 * np.sqrt(2.0 * c0[0] * c0[4])
+    vol = o.field("volume")
+    m, rho, H = o.field("mass"), o.field("massDensity"), o.field("H")
+    assert np.all(vol >= 0.5 * m / rho * (1 - 1e-12))
+    assert np.all(vol <= 4.0 * np.pi / (3.0 * H[:, 0] ** 3) * (1 + 1e-12))
+
+
+def test_crk_density_of_uniform_lattice(oracle_mod):
+    p = problems.crksph_box(n_side=10, seed=37, boundaries="periodic", rk_volume="mass_over_density",
+                            vel_scale=0.0, jitter=0.0)
+    p.rho[:] = 1.3
+    p.mass[:] = 1.3 / 1000.0
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    o.sum_density()
+    assert np.allclose(o.field("massDensity"), 1.3, rtol=1e-12)
