@@ -63,6 +63,18 @@ extern "C" {
 #define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
                                             symmetric-tensor H                                  */
 
+/* Hydro package (cfg.hydro). */
+#define SPHGPU_HYDRO_SPH 0     /* SPH (src/SPH/SPH.cc)                                              */
+#define SPHGPU_HYDRO_CRKSPH 1  /* CRKSPH with LinearOrder reproducing kernels (src/CRKSPH/CRKSPH.cc,
+                                  RKCorrections): FP64 precision, isotropic H, no grad-h          */
+
+/* RK volume weighting of CRKSPH (cfg.rk_volume, RKVolumeType of
+ * src/RK/RKCorrectionParams.hh; RKVoronoiVolume and RKHullVolume need a
+ * tessellation and are not built). */
+#define SPHGPU_RK_VOLUME_MASS_OVER_DENSITY 0  /* RKMassOverDensity: V = m / rho             */
+#define SPHGPU_RK_VOLUME_SUM 1                /* RKSumVolume: V = 1 / sum_j W_ij            */
+#define SPHGPU_RK_VOLUME_H 4                  /* HVolume: V = (pi / 6) / det(nPerh H)       */
+
 typedef struct sphgpu_ctx* sphgpu_handle;
 
 /* Package, artificial-viscosity, integrator and gravity settings.  Field
@@ -105,6 +117,8 @@ typedef struct sphgpu_config {
   int h_update;                     /* SPHGPU_H_* (the SPH() HUpdate argument)             */
   int evolve_total_energy;          /* evolveTotalEnergy (exclusive with compatible_energy) */
   int radial_only;                  /* ASPH radialOnly: H reshaped radially about the origin */
+  int hydro;                        /* SPHGPU_HYDRO_* (CRKSPH(...) factory: CRKSPHHydros.py:9-110) */
+  int rk_volume;                    /* SPHGPU_RK_VOLUME_* (SpheralController volumeType)    */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,

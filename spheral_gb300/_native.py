@@ -64,6 +64,8 @@ class Config(ctypes.Structure):
         ("h_update", ctypes.c_int),
         ("evolve_total_energy", ctypes.c_int),
         ("radial_only", ctypes.c_int),
+        ("hydro", ctypes.c_int),
+        ("rk_volume", ctypes.c_int),
     ]
 
 

@@ -314,6 +314,8 @@ void refreshParams(sphgpu_ctx* c) {
   hp.hUpdate = g.h_update;
   hp.totalEnergy = g.evolve_total_energy ? 1 : 0;
   hp.radialOnly = g.radial_only ? 1 : 0;
+  hp.crk = g.hydro == SPHGPU_HYDRO_CRKSPH ? 1 : 0;
+  hp.rkVolume = g.rk_volume;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -498,7 +500,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     const int nx = 1 - c->cur;
     launchPermute(c->F, c->Falt, v, c->orig[c->cur].as<int>(), c->orig[nx].as<int>(), c->list[c->cur].as<int>(),
                   c->list[nx].as<int>(), c->cellc[c->cur].as<uint32_t>(), c->cellc[nx].as<uint32_t>(), n,
-                  inStep, c->hp.asph != 0, c->stream, &c->lc);
+                  inStep, c->hp.asph != 0, c->hp.crk != 0, c->stream, &c->lc);
     std::swap(c->bankA, c->bankB);
     std::swap(c->F, c->Falt);
     c->cur = nx;
@@ -631,7 +633,9 @@ void prepare32(sphgpu_ctx* c) {
 }
 void sumDensity(sphgpu_ctx* c) {
   Scope sc(c->prof, "sum_density");
-  if (c->fp32())
+  if (c->hp.crk)   // computeCRKSPHSumMassDensity with the current RK volumes
+    launchCRKDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  else if (c->fp32())
     launchSumDensityFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
   else
     launchSumDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
@@ -688,6 +692,16 @@ void evalDerivs(sphgpu_ctx* c) {
     Scope sc(c->prof, "pair_fp32");
     launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                    c->pacc.as<float>(), c->pairVariant, c->stream, &c->lc);
+  } else if (c->hp.crk) {
+    // RKCorrections::initialize (the integrator's initializeDerivatives) on
+    // the state being evaluated, then CRKSPH::evaluateDerivatives
+    {
+      Scope sc(c->prof, "rk_corrections");
+      launchRKCorrections(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    }
+    Scope sc(c->prof, "pair_crk");
+    launchPairCRK(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->pacc.as<double>(), c->stream,
+                  &c->lc);
   } else {
     Scope sc(c->prof, "pair_fp64");
     launchPairFP64(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->pacc.as<double>(),
@@ -774,6 +788,10 @@ double step(sphgpu_ctx* c, double maxTime) {
   bool fused = false;
   auto preStep = [&]() {
     if (c->hp.radialOnly) launchRadius0(c->F, c->n, c->stream, &c->lc);   // SmoothingScaleBase::preStepInitialize
+    if (c->hp.crk) {   // RKCorrections::preStepInitialize: the RK volumes
+      Scope sc(c->prof, "rk_volume");
+      launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    }
     if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
       if (c->fp32()) {
         Scope sc(c->prof, "density_dt");
@@ -813,7 +831,7 @@ double step(sphgpu_ctx* c, double maxTime) {
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
   {
     Scope sc(c->prof, "update");
-    launchRestoreState0(c->F, c->n, c->hp.asph != 0, c->stream, &c->lc);
+    launchRestoreState0(c->F, c->n, c->hp.asph != 0, c->hp.crk != 0, c->stream, &c->lc);
   }
   if (c->cfg.compatible_energy) {
     Scope sc(c->prof, "energy");
@@ -864,9 +882,13 @@ struct FieldSpec {
   int ncomp;
 };
 // asph: H, Hideal and DHDt are the tensor fields (and massSecondMoment exists).
-bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb, bool asph) {
+bool fieldSpec(const std::string& s, FieldSpec& fs, bool& isH, bool& isNumNb, bool asph, bool crk) {
   isH = false;
   isNumNb = false;
+  if (crk && (s == "volume" || s == "rkCorrections")) {   // RKCorrections state (LinearOrder)
+    fs = {s == "volume" ? F_VOL : F_RKC_0, s == "volume" ? 1 : 16};
+    return true;
+  }
   static const std::map<std::string, FieldSpec> m = {
       {"position", {F_X, 3}}, {"velocity", {F_VX, 3}}, {"mass", {F_MASS, 1}}, {"massDensity", {F_RHO, 1}},
       {"specificThermalEnergy", {F_EPS, 1}}, {"pressure", {F_P, 1}}, {"soundSpeed", {F_CS, 1}},
@@ -975,6 +997,8 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->h_update = SPHGPU_H_IDEAL;
   c->evolve_total_energy = 0;
   c->radial_only = 0;
+  c->hydro = SPHGPU_HYDRO_SPH;
+  c->rk_volume = SPHGPU_RK_VOLUME_SUM;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -1001,6 +1025,19 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_ARG, "radialOnly needs the ASPH smoothing scale");
     if (cfg->compatible_energy && cfg->evolve_total_energy)   // SPH.cc:97-98
       throw Error(SPHGPU_E_ARG, "compatibleEnergyEvolution and evolveTotalEnergy cannot both be set");
+    if (cfg->hydro != SPHGPU_HYDRO_SPH && cfg->hydro != SPHGPU_HYDRO_CRKSPH)
+      throw Error(SPHGPU_E_UNSUPPORTED, "unknown hydro package");
+    if (cfg->hydro == SPHGPU_HYDRO_CRKSPH) {
+      if (cfg->rk_volume != SPHGPU_RK_VOLUME_MASS_OVER_DENSITY && cfg->rk_volume != SPHGPU_RK_VOLUME_SUM &&
+          cfg->rk_volume != SPHGPU_RK_VOLUME_H)
+        throw Error(SPHGPU_E_UNSUPPORTED, "RK volume types with a tessellation are not built");
+      if (cfg->precision != SPHGPU_PRECISION_FP64)
+        throw Error(SPHGPU_E_UNSUPPORTED, "CRKSPH runs in FP64 precision");
+      if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH)
+        throw Error(SPHGPU_E_UNSUPPORTED, "CRKSPH runs with the SPH smoothing scale (isotropic H)");
+      if (cfg->gradh_correction)
+        throw Error(SPHGPU_E_ARG, "CRKSPH has no grad-h correction");
+    }
     CUDA_OK(cudaSetDevice(cfg->device));
     CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->prof.s = c->stream;
@@ -1275,6 +1312,13 @@ int sphgpu_initialize(sphgpu_handle c) {
   buildNeighbors(c);
   if (c->cfg.gradh_correction) gradh(c);
   c->omegaStale = false;
+  if (c->hp.crk) {
+    // RKCorrections::initializeProblemStartupDependencies
+    // (src/RK/RKCorrections.cc:85-150): volumes, then corrections
+    launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    launchRKCorrections(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    c->check();
+  }
   CUDA_OK(cudaStreamSynchronize(c->stream));
   c->initialized = true;
   API_END(c)
@@ -1427,7 +1471,7 @@ int sphgpu_get_field(sphgpu_handle c, const char* name, double* out, int* ncomp)
   if (!name) throw Error(SPHGPU_E_ARG, "null field name");
   FieldSpec fs;
   bool isH, isNb;
-  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
+  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0, c->hp.crk != 0)) throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
   if (fs.first == F_DVDXQ_XX && !c->hp.limitedQ)
     throw Error(SPHGPU_E_STATE, "ArtificialViscosityVelocityGradient exists only with the limited Q");
   if (ncomp) *ncomp = fs.ncomp;
@@ -1458,7 +1502,7 @@ int sphgpu_set_field(sphgpu_handle c, const char* name, const double* in) {
   if (!name || !in) throw Error(SPHGPU_E_ARG, "null argument");
   FieldSpec fs;
   bool isH, isNb;
-  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0) || isNb)
+  if (!fieldSpec(name, fs, isH, isNb, c->hp.asph != 0, c->hp.crk != 0) || isNb)
     throw Error(SPHGPU_E_ARG, std::string("unknown field ") + name);
   requireState(c);
   const long n = c->n;

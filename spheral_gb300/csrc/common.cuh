@@ -54,7 +54,12 @@ struct HydroParams {
   int hUpdate;                   // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH
   int totalEnergy;               // evolveTotalEnergy: DepsDt is the total-energy rate
   int radialOnly;                // ASPH radialOnly
+  int crk;                       // CRKSPH (LinearOrder reproducing kernels) instead of SPH
+  int rkVolume;                  // RKVolumeType: 0 m/rho, 1 RKSumVolume, 4 HVolume
 };
+
+// safeInvVar (src/Utilities/safeInv.hh): sgn(x) / max(fuzz, |x|), fuzz 1e-30
+__device__ __forceinline__ double safeInvVarD(double x) { return (x < 0.0 ? -1.0 : 1.0) / fmax(1.0e-30, fabs(x)); }
 
 // Image of coordinate p under the per-axis code (reference ghost mapping,
 // PlanarBoundary::mapPosition -> mapPositionThroughPlanes, with

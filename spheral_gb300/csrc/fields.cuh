@@ -36,17 +36,23 @@ enum FieldId {
   F_HIDEALT_XX, F_HIDEALT_XY, F_HIDEALT_XZ, F_HIDEALT_YY, F_HIDEALT_YZ, F_HIDEALT_ZZ,
   F_M2_XX, F_M2_XY, F_M2_XZ, F_M2_YY, F_M2_YZ, F_M2_ZZ,
   F_RAD0,          // ASPH radialOnly: |x| at the start of the step
+  // CRKSPH only: the RK volume and the LinearOrder corrections (C_0..3, then
+  // dC/dx, dC/dy, dC/dz with 4 entries each).  Permuted only in CRKSPH mode.
+  F_VOL,
+  F_RKC_0, F_RKC_1, F_RKC_2, F_RKC_3, F_RKC_4, F_RKC_5, F_RKC_6, F_RKC_7,
+  F_RKC_8, F_RKC_9, F_RKC_10, F_RKC_11, F_RKC_12, F_RKC_13, F_RKC_14, F_RKC_15,
   F_NUM_PERMUTED,
   // beginning-of-step copies (not permuted: written after the sort)
   F_X0 = F_NUM_PERMUTED, F_Y0, F_Z0, F_VX0, F_VY0, F_VZ0, F_RHO0, F_EPS0, F_HINV0,
   F_HT0_XX, F_HT0_XY, F_HT0_XZ, F_HT0_YY, F_HT0_YZ, F_HT0_ZZ,
+  F_VOL0,
   F_NUM_FIELDS
 };
 
-// Fields a permute moves: up to two index ranges [first, last) of Fields::f.
+// Fields a permute moves: up to three index ranges [first, last) of Fields::f.
 struct FieldRanges {
   int n;
-  int first[2], last[2];
+  int first[3], last[3];
 };
 
 struct Fields {

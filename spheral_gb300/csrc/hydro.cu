@@ -902,7 +902,7 @@ __device__ __forceinline__ void eosNode(Fields& F, long i, const NodeListParams&
   F.f[F_CS][i] = sqrt(fmax(0.0, L.gamma * (L.gamma - 1.0) * eps));
 }
 
-__global__ void restoreState0Kernel(Fields F, long n, int tensor) {
+__global__ void restoreState0Kernel(Fields F, long n, int tensor, int crk) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   F.f[F_X][i] = F.f[F_X0][i]; F.f[F_Y][i] = F.f[F_Y0][i]; F.f[F_Z][i] = F.f[F_Z0][i];
@@ -911,6 +911,7 @@ __global__ void restoreState0Kernel(Fields F, long n, int tensor) {
   if (tensor)
 #pragma unroll
     for (int k = 0; k < 6; ++k) F.f[F_HT_XX + k][i] = F.f[F_HT0_XX + k][i];
+  if (crk) F.f[F_VOL][i] = F.f[F_VOL0][i];
 }
 
 // Extent of tensor H (ASPH): smallest eigenvalue -> F_HINV (cell size,
@@ -956,7 +957,7 @@ __global__ void tensorExtentKernel(Fields F, long n) {
 template <bool TENSOR>
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
                              double mult, int mid, int gravity, int epsIncrement, int hUpdate, int totalEnergy,
-                             Fields32 P, Grid g) {
+                             int crk, Fields32 P, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
@@ -968,6 +969,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     if (TENSOR)
 #pragma unroll
       for (int k = 0; k < 6; ++k) F.f[F_HT0_XX + k][i] = F.f[F_HT_XX + k][i];
+    if (crk) F.f[F_VOL0][i] = F.f[F_VOL][i];
   }
   if (epsIncrement) {
     if (totalEnergy) {
@@ -1030,6 +1032,15 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     if (h < hmaxInv) h = hmaxInv;
     if (h > hminInv) h = hminInv;
     F.f[F_HINV][i] = h;
+  }
+  if (crk) {
+    // ContinuityVolumePolicy::update (src/RK/ContinuityVolumePolicy.cc:40-75):
+    // it depends on the mass density, so it sees the updated rho and H
+    const double mi = F.f[F_MASS][i];
+    const double volMin = 0.5 * mi * safeInvVarD(rho);
+    const double volMax = 4.0 * 3.141592653589793 / (3.0 * ((h * h) * h));
+    const double dVdt = -mi * safeInvVarD(rho * rho) * F.f[F_DRHODT][i];
+    F.f[F_VOL][i] = fmax(volMin, fmin(volMax, F.f[F_VOL][i] + mult * dVdt));
   }
   if (P.posh) {
     // Mixed mode: the sound speed feeds only FP32 sweeps (Q, dt vote), so it
@@ -1257,13 +1268,17 @@ void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCoun
 }
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool carriedOnly, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+                   bool carriedOnly, bool tensor, bool crk, cudaStream_t s, LaunchCounter* lc) {
   // the tensor-H fields (the end of the carried block and of the permuted
-  // block) move only in ASPH mode
+  // block) move only in ASPH mode, the RK volume and corrections (the end of
+  // the permuted block) only in CRKSPH mode
   FieldRanges sel{};
   auto add = [&](int a, int b) { sel.first[sel.n] = a; sel.last[sel.n] = b; ++sel.n; };
   add(0, tensor ? (int)F_NUM_CARRIED : (int)F_HT_XX);
-  if (!carriedOnly) add(F_NUM_CARRIED, tensor ? (int)F_NUM_PERMUTED : (int)F_HIDEALT_XX);
+  if (!carriedOnly) {
+    add(F_NUM_CARRIED, tensor ? (int)F_VOL : (int)F_HIDEALT_XX);
+    if (crk) add(F_VOL, F_NUM_PERMUTED);
+  }
   permuteKernel<<<gridFor(n, 256), 256, 0, s>>>(Fin, Fout, perm, origIn, origOut, listIn, listOut, cellIn, cellOut, n,
                                                 sel);
   lc->add(1);
@@ -1338,8 +1353,8 @@ void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const do
   else energyKernel<false><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, pacc, pacc32, dt);
   lc->add(1);
 }
-void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc) {
-  restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0);
+void launchRestoreState0(Fields F, long n, bool tensor, bool crk, cudaStream_t s, LaunchCounter* lc) {
+  restoreState0Kernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, tensor ? 1 : 0, crk ? 1 : 0);
   lc->add(1);
 }
 void launchRadius0(Fields F, long n, cudaStream_t s, LaunchCounter* lc) {
@@ -1357,10 +1372,10 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   if (mirror) P = *mirror;
   if (hp.asph)
     updateKernel<true><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
-                                                       hp.hUpdate, hp.totalEnergy, P, g);
+                                                       hp.hUpdate, hp.totalEnergy, 0, P, g);
   else
     updateKernel<false><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0,
-                                                        epsInc, hp.hUpdate, hp.totalEnergy, P, g);
+                                                        epsInc, hp.hUpdate, hp.totalEnergy, hp.crk, P, g);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

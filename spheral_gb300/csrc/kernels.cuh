@@ -38,7 +38,7 @@ void launchCellKeys(const Fields& F, long n, Grid g, uint32_t* keys, int* vals, 
 // returns); otherwise every permuted field.
 void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* origIn, int* origOut,
                    const int* listIn, int* listOut, const uint32_t* cellIn, uint32_t* cellOut, long n,
-                   bool carriedOnly, bool tensor, cudaStream_t s, LaunchCounter* lc);
+                   bool carriedOnly, bool tensor, bool crk, cudaStream_t s, LaunchCounter* lc);
 // The limited Q's DvDx <- the hydro DvDx; and its FP32 mirror (3 float4 per node).
 void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc);
@@ -90,7 +90,19 @@ void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, cons
                                 float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc);
 // state0 -> state (the copy is taken by the half-step update); tensor: also
 // the tensor H (ASPH)
-void launchRestoreState0(Fields F, long n, bool tensor, cudaStream_t s, LaunchCounter* lc);
+void launchRestoreState0(Fields F, long n, bool tensor, bool crk, cudaStream_t s, LaunchCounter* lc);
+// CRKSPH (crk.cu): the RK volumes (RKCorrections::preStepInitialize), the CRK
+// mass density sum (CRKSPHBase::preStepInitialize), the LinearOrder
+// corrections (RKCorrections::initialize) and the CRKSPH pair loop with the
+// SPHSmoothingScale moments and node finalize (FP64).
+void launchRKVolumes(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
+                     LaunchCounter* lc);
+void launchCRKDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                      cudaStream_t s, LaunchCounter* lc);
+void launchRKCorrections(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp, cudaStream_t s,
+                         LaunchCounter* lc);
+void launchPairCRK(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                   double* pacc, cudaStream_t s, LaunchCounter* lc);
 // ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // ASPH radialOnly: F_RAD0 <- |x|

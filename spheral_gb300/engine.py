@@ -30,6 +30,9 @@ VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
 SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
 # HEvolutionType
 H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
+# hydro package and the RK volume type of CRKSPH (RKVolumeType)
+HYDRO = {"sph": 0, "crksph": 1}
+RK_VOLUME = {"mass_over_density": 0, "sum": 1, "h": 4}
 
 
 def config_from_dict(cfg, precision="fp64", device=0):
@@ -41,6 +44,10 @@ def config_from_dict(cfg, precision="fp64", device=0):
             c.smoothing_scale = SMOOTHING_SCALE[v]
         elif k == "h_update" and isinstance(v, str):
             c.h_update = H_UPDATE[v]
+        elif k == "hydro" and isinstance(v, str):
+            c.hydro = HYDRO[v]
+        elif k == "rk_volume" and isinstance(v, str):
+            c.rk_volume = RK_VOLUME[v]
         elif k in dict(N.Config._fields_):
             setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
     c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)
