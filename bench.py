@@ -138,7 +138,8 @@ def max_over_ranks(dist, v):
 
 def make_workload_name(args):
     return None, {"kh": "kelvin_helmholtz_3d", "sweep": "sweep_box", "sod": "sod_planar_3d",
-                  "evrard": "evrard_collapse_3d", "asph": "asph_stretched_lattice_3d"}[args.workload]
+                  "evrard": "evrard_collapse_3d", "asph": "asph_stretched_lattice_3d",
+                  "crksph": "kelvin_helmholtz_3d_crksph"}[args.workload]
 
 
 def asph_box(n1, seed=13):
@@ -146,6 +147,17 @@ def asph_box(n1, seed=13):
     (spacings 1 : 1.25 : 1.6 across x y z) with rotated tensor H."""
     from spheral_gb300 import problems
     return problems.stretched_box(nx=int(round(1.25 * n1)), ny=n1, nz=int(round(0.8 * n1)), seed=seed)
+
+
+def crksph_kh(n1):
+    """The Kelvin-Helmholtz slab run with the CRKSPH() factory defaults
+    (CRKSPHHydros.py:9-110: XSPH, limited Q with Cl = 1, Cq = 0.25, no grad-h)
+    and RKSumVolume."""
+    from spheral_gb300 import problems
+    p = problems.kelvin_helmholtz(n1=n1)
+    p.config.update(hydro="crksph", rk_volume="sum", xsph=True, gradh_correction=False,
+                    viscosity="limited_monaghan_gingold", Cl=1.0, Cq=0.25)
+    return p
 
 
 def make_workload(args):
@@ -160,6 +172,8 @@ def make_workload(args):
         return problems.evrard(n=args.n_evrard), "evrard_collapse_3d"
     if args.workload == "asph":
         return asph_box(args.n1), "asph_stretched_lattice_3d"
+    if args.workload == "crksph":
+        return crksph_kh(args.n1), "kelvin_helmholtz_3d_crksph"
     raise SystemExit("unknown workload")
 
 
@@ -177,6 +191,8 @@ def cpu_baseline(args, steps=None, warmup=1):
         p = problems.evrard(n=65536)
     elif args.workload == "asph":
         p = asph_box(args.cpu_n1)
+    elif args.workload == "crksph":
+        p = crksph_kh(args.cpu_n1)
     else:
         p = problems.sod(nx1=args.cpu_n1)
     o = orc.Oracle(p)
@@ -237,8 +253,8 @@ def run_ours(args, ws, rank, local, dist):
     for _ in range(args.warmup):
         eng.step()
     e0 = eng.conservation()
-    pair_kernel = "pair_fp32" if args.precision == "fp32" else "pair_fp64"
-    names = [pair_kernel, "gravity", "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt",
+    pair_kernel = "pair_crk" if args.workload == "crksph" else ("pair_fp32" if args.precision == "fp32" else "pair_fp64")
+    names = [pair_kernel, "rk_corrections", "rk_volume", "gravity", "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt",
              "energy",
              "gradh", "radix_sort",
              "permute", "update", "prepare_fp32", "enforce", "cell_keys", "bounds", "cell_ranges"]
@@ -519,7 +535,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard", "asph"])
+    ap.add_argument("--workload", default="kh", choices=["kh", "sweep", "sod", "ensemble", "evrard", "asph", "crksph"])
     ap.add_argument("--n-evrard", type=int, default=1048576)
     ap.add_argument("--validate", action="store_true", help="evrard: integrate to --goal-time and compare profiles")
     ap.add_argument("--goal-time", type=float, default=0.8)
@@ -536,6 +552,8 @@ def main():
     ap.add_argument("--cpu-n1", type=int, default=56)
     ap.add_argument("--cpu-steps", type=int, default=6)
     args = ap.parse_args()
+    if args.workload == "crksph":
+        args.precision = "fp64"   # the CRKSPH path runs in FP64
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank, dist)

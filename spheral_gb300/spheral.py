@@ -39,6 +39,21 @@ FixedH = 2
 _H_UPDATE = {IdealH: "ideal", IntegrateH: "integrate", FixedH: "fixed"}
 
 
+class RKOrder:
+    """src/RK/RKCorrectionParams.hh: correction order of the reproducing kernels."""
+    ZerothOrder, LinearOrder, QuadraticOrder, CubicOrder = 0, 1, 2, 3
+    QuarticOrder, QuinticOrder, SexticOrder, SepticOrder = 4, 5, 6, 7
+
+
+class RKVolumeType:
+    """src/RK/RKCorrectionParams.hh: RK volume weighting."""
+    RKMassOverDensity, RKSumVolume, RKVoronoiVolume, RKHullVolume, HVolume = 0, 1, 2, 3, 4
+
+
+RKMassOverDensity, RKSumVolume, RKVoronoiVolume, RKHullVolume, HVolume = 0, 1, 2, 3, 4
+_RK_VOLUME = {RKMassOverDensity: "mass_over_density", RKSumVolume: "sum", HVolume: "h"}
+
+
 def _h_update(HUpdate):
     if HUpdate not in _H_UPDATE:
         raise NotImplementedError("unknown HEvolutionType")
@@ -306,6 +321,50 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
     return SPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
                     XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile,
                     nTensile, smoothingScaleMethod, evolveTotalEnergy)
+
+
+class CRKSPHHydro(SPHHydro):
+    """CRKSPH package (src/CRKSPH/CRKSPH.cc) with its RKCorrections companion
+    (src/RK/RKCorrections.cc) at LinearOrder, in FP64."""
+
+    def __init__(self, dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, evolveTotalEnergy,
+                 XSPH, densityUpdate, epsTensile, nTensile, smoothingScaleMethod, volumeType):
+        if compatibleEnergyEvolution and evolveTotalEnergy:   # CRKSPH.cc:99-101
+            raise ValueError("CRKSPH error : you cannot simultaneously use both compatibleEnergyEvolution and "
+                             "evolveTotalEnergy")
+        if volumeType not in _RK_VOLUME:
+            raise NotImplementedError("RKVoronoiVolume and RKHullVolume need a tessellation and are not on the "
+                                      "GPU path")
+        super().__init__(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, False, XSPH,
+                         False, True, densityUpdate, epsTensile, nTensile, smoothingScaleMethod, evolveTotalEnergy)
+        self._cfg.update(hydro="crksph", rk_volume=_RK_VOLUME[volumeType])
+
+
+def CRKSPH(dataBase, W, Q=None, order=RKOrder.LinearOrder, filter=0.0, cfl=0.25, useVelocityMagnitudeForDt=False,
+           compatibleEnergyEvolution=True, evolveTotalEnergy=False, XSPH=True, densityUpdate=RigorousSumDensity,
+           HUpdate=IdealH, epsTensile=0.0, nTensile=4.0, damageRelieveRubble=False, ASPH=False, etaMinAxis=0.1,
+           crktype="default", smoothingScaleMethod=None, volumeType=RKSumVolume):
+    """The CRKSPH() factory (src/CRKSPH/CRKSPHHydros.py:9-110) with its
+    defaults: the default Q is LimitedMonaghanGingoldViscosity with
+    Cl = 2 (extent/4) and Cq = (extent/4)^2.  The reference hands the RK
+    volume type to SpheralController (default RKVoronoiVolume, which needs a
+    tessellation); here it is the volumeType argument, RKSumVolume by default.
+    LinearOrder, the default crktype and SPHSmoothingScale are on this path."""
+    if order != RKOrder.LinearOrder:
+        raise NotImplementedError("only LinearOrder reproducing kernels are on the GPU path")
+    if crktype.lower() != "default":
+        raise NotImplementedError("CRKSPHVariant is not on the GPU path")
+    if ASPH:
+        raise NotImplementedError("ACRKSPH is not on the GPU path")
+    if smoothingScaleMethod is None:
+        smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
+    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, FixedSmoothingScale)):
+        raise NotImplementedError("CRKSPH runs with SPHSmoothingScale on the GPU path")
+    if Q is None:
+        e = W.kernelExtent / 4.0
+        Q = LimitedMonaghanGingoldViscosity(2.0 * e, e * e)
+    return CRKSPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, evolveTotalEnergy,
+                       XSPH, densityUpdate, epsTensile, nTensile, smoothingScaleMethod, volumeType)
 
 
 class OctTreeGravity:

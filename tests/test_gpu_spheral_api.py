@@ -95,3 +95,38 @@ def test_spheral_style_asph_classic_matches_engine(native_lib):
         eng.step()
     assert np.array_equal(nodes.Hfield(), eng.field("H"))
     assert np.array_equal(nodes.positions(), eng.field("position"))
+
+
+def test_spheral_style_crksph_matches_engine(native_lib):
+    # CRKSPH() with its factory defaults runs the same FP64 CRK step as the engine
+    from spheral_gb300.engine import Engine
+    ref = problems.crksph_box(n_side=12, seed=57, boundaries="periodic")
+    W = S.TableKernel(S.BSplineKernel(), 1000)
+    nl = ref.nodelists[0]
+    nodes = S.makeFluidNodeList("fluid", S.GammaLawGas(5.0 / 3.0), hmin=nl["hmin"], hmax=nl["hmax"],
+                                nPerh=nl["nPerh"])
+    nodes.resize(ref.n)
+    nodes.positions()[:] = ref.pos
+    nodes.velocity()[:] = ref.vel
+    nodes.mass()[:] = ref.mass
+    nodes.massDensity()[:] = ref.rho
+    nodes.specificThermalEnergy()[:] = ref.eps
+    nodes.Hfield()[:] = ref.H
+    db = S.DataBase()
+    db.appendNodeList(nodes)
+    hydro = S.CRKSPH(dataBase=db, W=W)
+    for a in range(3):
+        lo, hi, nrm, nrm2 = [0.0] * 3, [0.0] * 3, [0.0] * 3, [0.0] * 3
+        hi[a], nrm[a], nrm2[a] = 1.0, 1.0, -1.0
+        hydro.appendBoundary(S.PeriodicBoundary(S.Plane(lo, nrm), S.Plane(hi, nrm2)))
+    integrator = S.CheapSynchronousRK2Integrator(db, dtMin=0.0, dtMax=0.1, dtGrowth=2.0)
+    integrator.lastDt = 1e-3
+    integrator.appendPhysicsPackage(hydro)
+    for _ in range(3):
+        integrator.step()
+    eng = Engine.from_problem(ref)
+    eng.initialize()
+    for _ in range(3):
+        eng.step()
+    assert np.array_equal(nodes.positions(), eng.field("position"))
+    assert np.array_equal(nodes.specificThermalEnergy(), eng.field("specificThermalEnergy"))

@@ -69,3 +69,21 @@ def test_nodelist_fields_before_the_first_step():
     nodes.resize(10)
     nodes.positions()[:] = np.arange(30).reshape(10, 3)
     assert nodes.positions()[3, 1] == 10.0 and nodes.numInternalNodes == 10
+
+
+def test_crksph_factory_defaults_follow_the_reference():
+    # CRKSPHHydros.py:9-110: XSPH on, compatible energy, LimitedMonaghanGingold
+    # with Cl = 2 (extent/4), Cq = (extent/4)^2, no grad-h
+    W = S.TableKernel(S.BSplineKernel(), 1000)
+    h = S.CRKSPH(dataBase=S.DataBase(), W=W)
+    c = h._cfg
+    assert c["hydro"] == "crksph" and c["rk_volume"] == "sum"
+    assert c["xsph"] and c["compatible_energy"] and not c["gradh_correction"]
+    assert c["viscosity"] == "limited_monaghan_gingold" and c["Cl"] == 1.0 and c["Cq"] == 0.25
+    assert S.CRKSPH(dataBase=S.DataBase(), W=W, volumeType=S.RKMassOverDensity)._cfg["rk_volume"] == "mass_over_density"
+    for bad in (dict(order=S.RKOrder.QuadraticOrder), dict(crktype="variant"), dict(ASPH=True),
+                dict(volumeType=S.RKVoronoiVolume)):
+        with pytest.raises(NotImplementedError):
+            S.CRKSPH(dataBase=S.DataBase(), W=W, **bad)
+    with pytest.raises(ValueError):
+        S.CRKSPH(dataBase=S.DataBase(), W=W, evolveTotalEnergy=True)
