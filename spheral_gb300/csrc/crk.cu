@@ -22,13 +22,14 @@ inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
 // RKUtilities::evaluateBaseKernelAndGradient (RKUtilities.cc:66-80) for H = a I:
 // eta = a x, w = Hdet W(|eta|), grad = (H eta^) Hdet dW(|eta|); a zero eta
 // takes the unit vector (1, 0, 0) (GeomVector::unitVector).
-__device__ __forceinline__ void rkBase(const double* __restrict__ tw, const double* __restrict__ tg,
-                                       const HydroParams& hp, double a, double x, double y, double z, double& w,
-                                       double& dwx, double& dwy, double& dwz) {
-  const double ex = a * x, ey = a * y, ez = a * z;
-  const double em = sqrt(ex * ex + ey * ey + ez * ez);
+__device__ __forceinline__ void rkBaseEta(const double* __restrict__ tw, const double* __restrict__ tg,
+                                          const HydroParams& hp, double a, double ex, double ey, double ez, double em,
+                                          double& w, double& dwx, double& dwy, double& dwz) {
   double ux = 1.0, uy = 0.0, uz = 0.0;
-  if (em > 1.0e-50) { ux = ex / em; uy = ey / em; uz = ez / em; }
+  if (em > 1.0e-50) {
+    const double ie = 1.0 / em;
+    ux = ex * ie; uy = ey * ie; uz = ez * ie;
+  }
   const double Hdet = (a * a) * a;
   double k = 0.0, dk = 0.0;
   if (em < hp.extent) {
@@ -40,6 +41,12 @@ __device__ __forceinline__ void rkBase(const double* __restrict__ tw, const doub
   dwx = (a * ux) * dk;
   dwy = (a * uy) * dk;
   dwz = (a * uz) * dk;
+}
+__device__ __forceinline__ void rkBase(const double* __restrict__ tw, const double* __restrict__ tg,
+                                       const HydroParams& hp, double a, double x, double y, double z, double& w,
+                                       double& dwx, double& dwy, double& dwz) {
+  const double ex = a * x, ey = a * y, ez = a * z;
+  rkBaseEta(tw, tg, hp, a, ex, ey, ez, sqrt(ex * ex + ey * ey + ez * ez), w, dwx, dwy, dwz);
 }
 
 // RKUtilities::evaluateKernelAndGradient (RKUtilities.cc:181-206), LinearOrder:
@@ -183,17 +190,23 @@ __device__ __forceinline__ int symIdx(int k, int l) {   // upper triangle of 4x4
 
 __device__ __forceinline__ void addMoments(double* M, double (*dM)[10], double vj, double x, double y, double z,
                                            double w, double dwx, double dwy, double dwz) {
+  // M_kl += V_j p_k p_l W; dM_d,kl += V_j ((dp_dk p_l + p_k dp_dl) W + p_k p_l dW_d)
+  // with dp_dk = [k == 1 + d]: the products p_k p_l and V_j W, V_j dW_d are shared
   const double p[4] = {1.0, x, y, z};
-  const double dw[3] = {dwx, dwy, dwz};
+  const double vw = vj * w;
+  const double vd[3] = {vj * dwx, vj * dwy, vj * dwz};
 #pragma unroll
   for (int k = 0; k < 4; ++k)
 #pragma unroll
     for (int l = k; l < 4; ++l) {
-      M[symIdx(k, l)] += vj * p[k] * p[l] * w;
+      const double pp = p[k] * p[l];
+      M[symIdx(k, l)] += vw * pp;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const double dpk = (k == 1 + d) ? 1.0 : 0.0, dpl = (l == 1 + d) ? 1.0 : 0.0;
-        dM[d][symIdx(k, l)] += vj * ((dpk * p[l] + p[k] * dpl) * w + p[k] * p[l] * dw[d]);
+        double t = vd[d] * pp;
+        if (k == 1 + d) t += vw * p[l];
+        if (l == 1 + d) t += vw * p[k];
+        dM[d][symIdx(k, l)] += t;
       }
     }
 }
@@ -319,6 +332,7 @@ __global__ void __launch_bounds__(128) pairKernelCRK(Fields F, const int* __rest
   const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
   const double mi = F.f[F_MASS][i], rhoi = F.f[F_RHO][i], Pi = F.f[F_P][i], ci = F.f[F_CS][i];
   const double ai = F.f[F_HINV][i], Vi = F.f[F_VOL][i];
+  const double invMi = 1.0 / mi;   // the reference forms force / m_i as force * (1 / m_i)
   const int li = list[i];
   double Ci[16];
 #pragma unroll
@@ -354,21 +368,22 @@ __global__ void __launch_bounds__(128) pairKernelCRK(Fields F, const int* __rest
 
     const double rx = xi - xj, ry = yi - yj, rz = zi - zj;
     const double vijx = vxi - vxj, vijy = vyi - vyj, vijz = vzi - vzj;
-    // corrected kernels: W_j with H_j and C_i, W_i with H_i and C_j at -r_ij
-    double w, dwx, dwy, dwz, Wj, gjx, gjy, gjz, Wi, gix, giy, giz;
-    rkBase(tw, tg, hp, aj, rx, ry, rz, w, dwx, dwy, dwz);
-    rkEval(Ci, rx, ry, rz, w, dwx, dwy, dwz, Wj, gjx, gjy, gjz);
-    rkBase(tw, tg, hp, ai, -rx, -ry, -rz, w, dwx, dwy, dwz);
-    rkEval(Cj, -rx, -ry, -rz, w, dwx, dwy, dwz, Wi, gix, giy, giz);
-    const double dgx = gjx - gix, dgy = gjy - giy, dgz = gjz - giz;
-
-    // Monaghan-Gingold Q on eta_i = H_i r_ij, eta_j = H_j r_ij (the limited
-    // form first corrects the two velocities along the pair with the Q's DvDx)
+    // eta_i = H_i r_ij, eta_j = H_j r_ij (the base kernel of W_i at -r_ij sees -eta_i)
     const double eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
     const double ejx = aj * rx, ejy = aj * ry, ejz = aj * rz;
     const double etaMag2i = eix * eix + eiy * eiy + eiz * eiz;
     const double etaMag2j = ejx * ejx + ejy * ejy + ejz * ejz;
     const double etaMagi = sqrt(etaMag2i), etaMagj = sqrt(etaMag2j);
+    // corrected kernels: W_j with H_j and C_i, W_i with H_i and C_j at -r_ij
+    double w, dwx, dwy, dwz, Wj, gjx, gjy, gjz, Wi, gix, giy, giz;
+    rkBaseEta(tw, tg, hp, aj, ejx, ejy, ejz, etaMagj, w, dwx, dwy, dwz);
+    rkEval(Ci, rx, ry, rz, w, dwx, dwy, dwz, Wj, gjx, gjy, gjz);
+    rkBaseEta(tw, tg, hp, ai, -eix, -eiy, -eiz, etaMagi, w, dwx, dwy, dwz);
+    rkEval(Cj, -rx, -ry, -rz, w, dwx, dwy, dwz, Wi, gix, giy, giz);
+    const double dgx = gjx - gix, dgy = gjy - giy, dgz = gjz - giz;
+
+    // Monaghan-Gingold Q (the limited form first corrects the two velocities
+    // along the pair with the Q's DvDx)
     double vqx = vijx, vqy = vijy, vqz = vijz;
     if (hp.limitedQ) {
       double Dj[9];
@@ -405,12 +420,11 @@ __global__ void __launch_bounds__(128) pairKernelCRK(Fields F, const int* __rest
     const double qmj = hp.quadraticInExpansion ? -(muj < 0.0 ? -1.0 : 1.0) * muj * muj : fmin(0.0, muj) * fmin(0.0, muj);
     const double ei = -Clij * ci * lmi + Cqij * qmi;
     const double ej = -Clij * cj * lmj + Cqij * qmj;
-    const double QPiij = ei / rhoi, QPiji = ej / rhoj;
+    // rho^2 QPi = rho e (QPi_ij = e_i / rho_i): no division
     const double Qi = rhoi * ei;
-
-    const double qs = rhoi * rhoi * QPiij + rhoj * rhoj * QPiji;
+    const double qj = rhoj * ej;
+    const double qs = Qi + qj;
     const double Qax = qs * dgx, Qay = qs * dgy, Qaz = qs * dgz;
-    const double qj = rhoj * rhoj * QPiji;
     const double workQi = (qj * vijx) * dgx + (qj * vijy) * dgy + (qj * vijz) * dgz;
     maxQ = fmax(maxQ, 4.0 * Qi);
     effQ += Vj * Qi * Wj;
@@ -424,15 +438,16 @@ __global__ void __launch_bounds__(128) pairKernelCRK(Fields F, const int* __rest
     const double f = 0.5 * (Vi * Vj);
     const double PP = Pi + Pj;
     const double fx = f * (PP * dgx + Qax), fy = f * (PP * dgy + Qay), fz = f * (PP * dgz + Qaz);
-    dvx -= fx / mi;
-    dvy -= fy / mi;
-    dvz -= fz / mi;
+    const double ax = fx * invMi, ay = fy * invMi, az = fz * invMi;
+    dvx -= ax;
+    dvy -= ay;
+    dvz -= az;
     if (COMPAT) {
-      pacc[3 * slot] = -fx / mi;
-      pacc[3 * slot + 1] = -fy / mi;
-      pacc[3 * slot + 2] = -fz / mi;
+      pacc[3 * slot] = -ax;
+      pacc[3 * slot + 1] = -ay;
+      pacc[3 * slot + 2] = -az;
     }
-    deps += f * (Pj * (vijx * dgx + vijy * dgy + vijz * dgz) + workQi) / mi;
+    deps += f * (Pj * (vijx * dgx + vijy * dgy + vijz * dgz) + workQi) * invMi;
     if (XSPH && lj == li) {
       const double xw = Vj * Wj;
       xdx -= xw * vijx; xdy -= xw * vijy; xdz -= xw * vijz;
