@@ -552,8 +552,6 @@ def main():
     ap.add_argument("--cpu-n1", type=int, default=56)
     ap.add_argument("--cpu-steps", type=int, default=6)
     args = ap.parse_args()
-    if args.workload == "crksph":
-        args.precision = "fp64"   # the CRKSPH path runs in FP64
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank, dist)

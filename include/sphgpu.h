@@ -66,7 +66,7 @@ extern "C" {
 /* Hydro package (cfg.hydro). */
 #define SPHGPU_HYDRO_SPH 0     /* SPH (src/SPH/SPH.cc)                                              */
 #define SPHGPU_HYDRO_CRKSPH 1  /* CRKSPH with LinearOrder reproducing kernels (src/CRKSPH/CRKSPH.cc,
-                                  RKCorrections): FP64 precision, isotropic H, no grad-h          */
+                                  RKCorrections): both precision modes, isotropic H, no grad-h    */
 
 /* RK volume weighting of CRKSPH (cfg.rk_volume, RKVolumeType of
  * src/RK/RKCorrectionParams.hh; RKVoronoiVolume and RKHullVolume need a

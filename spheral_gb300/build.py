@@ -15,7 +15,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsphgpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-CUDA_SOURCES = ["sort.cu", "hydro.cu", "hydro32.cu", "crk.cu", "gravity.cu", "api.cu", "noalloc.cu"]
+CUDA_SOURCES = ["sort.cu", "hydro.cu", "hydro32.cu", "crk.cu", "crk32.cu", "gravity.cu", "api.cu", "noalloc.cu"]
 HOST_SOURCES = ["table.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off: host arithmetic (kernel-table build) is identical on x86-64 and aarch64

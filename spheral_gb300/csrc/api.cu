@@ -135,6 +135,7 @@ struct sphgpu_ctx {
   long invVersion = -1;      // permVersion the inverse was built for
   DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
   DBuf hten;                 // ASPH: FP32 mirror of tensor H (2 float4 per node)
+  DBuf vol32, rkc32;         // CRKSPH, mixed mode: FP32 mirrors of the RK volume and corrections
   DBuf stage;                // host <-> device staging for caller-order transfers
   DBuf v12;                  // half-step velocities + DepsDt0 of the mixed-mode energy sweep
   int cur = 0;
@@ -206,6 +207,8 @@ struct sphgpu_ctx {
     p.cell = cellp();
     p.dvq = dvq.p ? dvq.as<float4>() : nullptr;
     p.hten = cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? hten.as<float4>() : nullptr;
+    p.vol = vol32.p ? vol32.as<float>() : nullptr;
+    p.rkc = rkc32.p ? rkc32.as<float4>() : nullptr;
     return p;
   }
   bool fp32() const { return cfg.precision == SPHGPU_PRECISION_FP32; }
@@ -227,6 +230,12 @@ void ensureCapacity(sphgpu_ctx* c, long n) {
   c->thermo.release(); c->thermo.ensure(n * sizeof(float4));
   c->hten.release();
   if (c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC) c->hten.ensure(2 * n * sizeof(float4));
+  c->vol32.release();
+  c->rkc32.release();
+  if (c->cfg.hydro == SPHGPU_HYDRO_CRKSPH && c->cfg.precision == SPHGPU_PRECISION_FP32) {
+    c->vol32.ensure(n * sizeof(float));
+    c->rkc32.ensure(4 * n * sizeof(float4));
+  }
   for (int k = 0; k < 2; ++k) {
     c->orig[k].release(); c->orig[k].ensure(n * sizeof(int));
     c->list[k].release(); c->list[k].ensure(n * sizeof(int));
@@ -633,7 +642,9 @@ void prepare32(sphgpu_ctx* c) {
 }
 void sumDensity(sphgpu_ctx* c) {
   Scope sc(c->prof, "sum_density");
-  if (c->hp.crk)   // computeCRKSPHSumMassDensity with the current RK volumes
+  if (c->hp.crk && c->fp32())   // computeCRKSPHSumMassDensity with the current RK volumes
+    launchCRKDensityFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+  else if (c->hp.crk)
     launchCRKDensity(c->F, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
   else if (c->fp32())
     launchSumDensityFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
@@ -662,7 +673,16 @@ void evalDerivs(sphgpu_ctx* c) {
     launchQGradient32(c->F, c->dvq.as<float4>(), c->n, c->stream, &c->lc);
     c->check();
   }
-  if (c->fp32()) {
+  if (c->hp.crk && c->fp32()) {
+    // RKCorrections::initialize, then CRKSPH::evaluateDerivatives, FP32 sweeps
+    {
+      Scope sc(c->prof, "rk_corrections");
+      launchRKCorrectionsFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    }
+    Scope sc(c->prof, "pair_crk");
+    launchPairCRKFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
+                      c->pacc.as<float>(), c->stream, &c->lc);
+  } else if (c->fp32()) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
     // trial launches leave the same results) and keep the fastest.
@@ -790,10 +810,13 @@ double step(sphgpu_ctx* c, double maxTime) {
     if (c->hp.radialOnly) launchRadius0(c->F, c->n, c->stream, &c->lc);   // SmoothingScaleBase::preStepInitialize
     if (c->hp.crk) {   // RKCorrections::preStepInitialize: the RK volumes
       Scope sc(c->prof, "rk_volume");
-      launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+      if (c->fp32())
+        launchRKVolumesFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+      else
+        launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
     }
-    if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed)
-      if (c->fp32()) {
+    if (c->cfg.density_update == SPHGPU_DENSITY_RIGOROUS_SUM) {   // preStepInitialize (+ dt vote when mixed SPH)
+      if (c->fp32() && !c->hp.crk) {
         Scope sc(c->prof, "density_dt");
         const long nb = (c->n + 127) / 128;
         c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
@@ -1031,8 +1054,6 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       if (cfg->rk_volume != SPHGPU_RK_VOLUME_MASS_OVER_DENSITY && cfg->rk_volume != SPHGPU_RK_VOLUME_SUM &&
           cfg->rk_volume != SPHGPU_RK_VOLUME_H)
         throw Error(SPHGPU_E_UNSUPPORTED, "RK volume types with a tessellation are not built");
-      if (cfg->precision != SPHGPU_PRECISION_FP64)
-        throw Error(SPHGPU_E_UNSUPPORTED, "CRKSPH runs in FP64 precision");
       if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH)
         throw Error(SPHGPU_E_UNSUPPORTED, "CRKSPH runs with the SPH smoothing scale (isotropic H)");
       if (cfg->gradh_correction)
@@ -1315,8 +1336,13 @@ int sphgpu_initialize(sphgpu_handle c) {
   if (c->hp.crk) {
     // RKCorrections::initializeProblemStartupDependencies
     // (src/RK/RKCorrections.cc:85-150): volumes, then corrections
-    launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
-    launchRKCorrections(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    if (c->fp32()) {
+      launchRKVolumesFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+      launchRKCorrectionsFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    } else {
+      launchRKVolumes(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+      launchRKCorrections(c->F, c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
+    }
     c->check();
   }
   CUDA_OK(cudaStreamSynchronize(c->stream));

@@ -67,6 +67,8 @@ struct Fields32 {
   uint32_t* cell;   // packed cell coordinates (10 bits per axis)
   float4* dvq;      // limited Q: DvDx of the Q as 3 float4 per node (xx xy xz yx | yy yz zx zy | zz - - -)
   float4* hten;     // ASPH: tensor H as 2 float4 per node (xx xy xz yy | yz zz det(H) lambda_max)
+  float* vol;       // CRKSPH: RK volume
+  float4* rkc;      // CRKSPH: LinearOrder corrections, 4 float4 per node (C | dC/dx | dC/dy | dC/dz)
 };
 
 }  // namespace sph

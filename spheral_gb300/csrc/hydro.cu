@@ -1065,6 +1065,7 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     const float om = (float)F.f[F_OMEGA][i];
     P.thermo[i] = make_float4((float)rho, (float)F.f[F_P][i], (float)F.f[F_CS][i], om / (om * om + 1.0e-30f));
     if (TENSOR) writeTensorMirror(F, P, i);
+    if (crk && P.vol) P.vol[i] = (float)F.f[F_VOL][i];
   }
 }
 

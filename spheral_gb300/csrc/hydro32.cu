@@ -51,6 +51,7 @@ __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   P.thermo[i] = make_float4((float)F.f[F_RHO][i], (float)F.f[F_P][i], (float)F.f[F_CS][i],
                             (float)(om / (om * om + 1.0e-30)));
   if (P.hten) writeTensorMirror(F, P, i);
+  if (P.vol) P.vol[i] = (float)F.f[F_VOL][i];
 }
 
 __device__ __forceinline__ void lookup32(const float* __restrict__ tw, const float* __restrict__ tg, int N1,

@@ -103,6 +103,16 @@ void launchRKCorrections(Fields F, long n, Grid g, NeighborLists nl, TableDev t,
                          LaunchCounter* lc);
 void launchPairCRK(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                    double* pacc, cudaStream_t s, LaunchCounter* lc);
+// Mixed-precision CRKSPH (crk32.cu): FP32 sweeps on the FP32 mirror, FP64
+// per-node completions; the volume and correction mirrors are written too.
+void launchRKVolumesFP32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                         cudaStream_t s, LaunchCounter* lc);
+void launchCRKDensityFP32(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                          HydroParams hp, cudaStream_t s, LaunchCounter* lc);
+void launchRKCorrectionsFP32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
+                             cudaStream_t s, LaunchCounter* lc);
+void launchPairCRKFP32(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                       HydroParams hp, float* pacc, cudaStream_t s, LaunchCounter* lc);
 // ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // ASPH radialOnly: F_RAD0 <- |x|

@@ -11,7 +11,15 @@ RKSumVolume, RKMassOverDensity and HVolume; the CRKSPH factory defaults
 Tolerances (FP64): neighbour-independent fields after initialize and one
 evaluation <= 1e-12 normwise (the 4x4 moment solves use the same LU order
 on both sides); one step <= 1e-11, five steps <= 1e-9; linear velocity
-fields reproduced to 1e-10; energy conserved to 1e-12."""
+fields reproduced to 1e-10; energy conserved to 1e-12.
+
+Mixed mode (FP32 sweeps on the cell-relative mirror, correction moments in
+the eta units of each node, FP64 4x4 solves and node completions): volumes,
+corrections, density and derivatives <= 1e-5 of the FP64 oracle (measured
+<= 2e-6), three steps <= 1e-5 (measured <= 1e-6), dt <= 1e-6, linear
+fields reproduced to 1e-5 (measured 3e-7), energy conserved to 1e-9 and
+momentum to 1e-9 over five steps (the FP32 pair force is bitwise
+antisymmetric; measured ~1e-10)."""
 import numpy as np
 import pytest
 
@@ -108,12 +116,69 @@ def test_crk_conserves_and_restarts(native_lib, boundaries):
         assert np.array_equal(again.field(f), eng.field(f)), f
 
 
+def _pair_mixed(oracle_mod, boundaries, rk_volume, seed=51, **kw):
+    from spheral_gb300.engine import Engine
+    p = problems.crksph_box(n_side=12, seed=seed, boundaries=boundaries, rk_volume=rk_volume, **kw)
+    eng = Engine.from_problem(p, precision="fp32")
+    orc = oracle_mod.Oracle(p)
+    eng.initialize()
+    orc.initialize()
+    return p, eng, orc
+
+
+@pytest.mark.parametrize("boundaries,rk_volume", CASES)
+def test_crk_mixed_evaluation_close(native_lib, oracle_mod, boundaries, rk_volume):
+    p, eng, orc = _pair_mixed(oracle_mod, boundaries, rk_volume)
+    bad = compare_fields(eng, orc, ["volume", "rkCorrections"], 1e-5)
+    assert not bad, bad
+    eng.sum_density()
+    orc.sum_density()
+    bad = compare_fields(eng, orc, ["massDensity"], 1e-5)
+    assert not bad, bad
+    eng.evaluate_derivatives()
+    orc.rk_corrections()
+    orc.evaluate_derivatives()
+    bad = compare_fields(eng, orc, DERIVS + ["rkCorrections"], 1e-5)
+    assert not bad, bad
+    dg, _ = eng.dt()
+    assert abs(dg - orc.hydro_dt()) <= 1e-6 * dg
+
+
+@pytest.mark.parametrize("boundaries,rk_volume", CASES)
+def test_crk_mixed_steps_close(native_lib, oracle_mod, boundaries, rk_volume):
+    p, eng, orc = _pair_mixed(oracle_mod, boundaries, rk_volume)
+    for _ in range(3):
+        eng.step()
+        orc.step()
+    bad = compare_fields(eng, orc, STATE + ["DvDt", "DepsDt"], 1e-5)
+    assert not bad, bad
+
+
+def test_crk_mixed_reproduces_linear_velocity(native_lib, oracle_mod):
+    A = np.array([[0.3, -0.2, 0.1], [0.05, -0.4, 0.25], [0.15, 0.2, 0.35]])
+    p, eng, orc = _pair_mixed(oracle_mod, "open", "sum", seed=53, linear_velocity=A)
+    eng.evaluate_derivatives()
+    assert np.abs(eng.field("DvDx").reshape(-1, 3, 3) - A[None]).max() < 1e-5
+
+
+def test_crk_mixed_conserves(native_lib):
+    from spheral_gb300.engine import Engine
+    p = problems.crksph_box(n_side=12, seed=76, vel_scale=0.1)
+    eng = Engine.from_problem(p, precision="fp32")
+    eng.initialize()
+    c0 = eng.conservation()
+    eng.advance(5)
+    c1 = eng.conservation()
+    assert abs(c1[7] - c0[7]) <= 1e-9 * abs(c0[7])
+    assert np.abs(c1[1:4] - c0[1:4]).max() <= 1e-9 * np.sqrt(2.0 * c0[0] * c0[4])
+
+
 def test_crk_unsupported_settings(native_lib):
     from spheral_gb300 import _native as N
     from spheral_gb300.engine import Engine
     base = problems.crksph_box(n_side=4).config
     with pytest.raises(N.SphGpuError) as e:
-        Engine(base, precision="fp32")
+        Engine(dict(base, smoothing_scale="asph_classic"), precision="fp64")
     assert e.value.code == 3   # SPHGPU_E_UNSUPPORTED
     with pytest.raises(N.SphGpuError) as e:
         Engine(dict(base, gradh_correction=True), precision="fp64")
