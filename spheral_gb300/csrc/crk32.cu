@@ -512,20 +512,23 @@ __global__ void __launch_bounds__(128) pairKernelCRK32(Fields F, Fields32 P, con
     m0 += fwW;
     m1x -= fwW * eix; m1y -= fwW * eiy; m1z -= fwW * eiz;
   }
-  // node finalize (FP64 stores)
-  const double vxi = F.f[F_VX][i], vyi = F.f[F_VY][i], vzi = F.f[F_VZ][i];
-  const double rhoid = F.f[F_RHO][i], mid = F.f[F_MASS][i], aid = F.f[F_HINV][i];
-  double Dd[9];
+  // node finalize: the sums leave as FP64 values, the per-node arithmetic is
+  // FP32 (GB300's FP64 rate would make it visible next to the pair loop)
+  const float trace = D[0] + D[4] + D[8];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) { Dd[k] = D[k]; F.f[F_DVDX_XX + k][i] = Dd[k]; F.f[F_M_XX + k][i] = 0.0; }
-  const double trace = Dd[0] + Dd[4] + Dd[8];
+  for (int k = 0; k < 9; ++k) { F.f[F_DVDX_XX + k][i] = D[k]; F.f[F_M_XX + k][i] = 0.0; }
   const double dvx = kahanValue(sdx, cdx), dvy = kahanValue(sdy, cdy), dvz = kahanValue(sdz, cdz);
   const double deps = kahanValue(se, ce);
-  F.f[F_DRHODT][i] = -rhoid * trace;
+  F.f[F_DRHODT][i] = (double)(-rhoi * trace);
   F.f[F_DVDT_X][i] = dvx;
   F.f[F_DVDT_Y][i] = dvy;
   F.f[F_DVDT_Z][i] = dvz;
-  F.f[F_DEPSDT][i] = hp.totalEnergy ? mid * ((vxi * dvx + vyi * dvy + vzi * dvz) + deps) : deps;
+  if (hp.totalEnergy) {
+    const double vxd = F.f[F_VX][i], vyd = F.f[F_VY][i], vzd = F.f[F_VZ][i];
+    F.f[F_DEPSDT][i] = F.f[F_MASS][i] * ((vxd * dvx + vyd * dvy + vzd * dvz) + deps);
+  } else {
+    F.f[F_DEPSDT][i] = deps;
+  }
   F.f[F_MAXQ][i] = maxQ;
   F.f[F_EFFQ][i] = effQ;
   F.f[F_RHOSUM][i] = 0.0;
@@ -535,22 +538,30 @@ __global__ void __launch_bounds__(128) pairKernelCRK32(Fields F, Fields32 P, con
   F.f[F_XSPHDV_X][i] = xdx;
   F.f[F_XSPHDV_Y][i] = xdy;
   F.f[F_XSPHDV_Z][i] = xdz;
-  F.f[F_DXDT_X][i] = XSPH ? vxi + xdx : vxi;
-  F.f[F_DXDT_Y][i] = XSPH ? vyi + xdy : vyi;
-  F.f[F_DXDT_Z][i] = XSPH ? vzi + xdz : vzi;
+  if (XSPH) {
+    F.f[F_DXDT_X][i] = F.f[F_VX][i] + xdx;
+    F.f[F_DXDT_Y][i] = F.f[F_VY][i] + xdy;
+    F.f[F_DXDT_Z][i] = F.f[F_VZ][i] + xdz;
+  } else {
+    F.f[F_DXDT_X][i] = F.f[F_VX][i];
+    F.f[F_DXDT_Y][i] = F.f[F_VY][i];
+    F.f[F_DXDT_Z][i] = F.f[F_VZ][i];
+  }
+  // SPHSmoothingScale finalize in FP32: DHDt = -(H/3) tr(DvDx), Hideal =
+  // clamp(H / f, 1/hmax, 1/hmin)
   const NodeListParams L = hp.lists[li];
-  const double m0r = pow(fmax(0.0, (double)m0), 0.3333333333333333);
+  const float m0r = cbrtf(fmaxf(0.0f, m0));
   F.f[F_M0][i] = m0r;
   F.f[F_M1_X][i] = m1x;
   F.f[F_M1_Y][i] = m1y;
   F.f[F_M1_Z][i] = m1z;
-  F.f[F_DHDT][i] = ((-aid) / 3.0) * trace;
-  const bool isolated = fabs(m0r) <= 1.0e-15 * fmax(1.0, fabs(m0r));
-  const double cur = isolated ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(t.herm, hp, m0r));
-  const double sr = fmin(4.0, fmax(0.25, L.nPerh / (cur + 1.0e-30)));
-  const double aa = sr < 1.0 ? 0.4 * (1.0 + sr * sr) : 0.4 * (1.0 + 1.0 / (sr * sr * sr));
-  const double hi1 = fmin(L.hmax, fmax(L.hmin, (1.0 / aid) * (1.0 - aa + aa * sr)));
-  F.f[F_HIDEAL][i] = 1.0 / hi1;
+  F.f[F_DHDT][i] = (double)(-(ai * (1.0f / 3.0f)) * trace);
+  const float nPerh = (float)L.nPerh;
+  const bool isolated = fabsf(m0r) <= 1.0e-15f * fmaxf(1.0f, fabsf(m0r));
+  const float cur = isolated ? 0.5f * nPerh : fmaxf(0.0f, hermiteLookup32(t.herm, hp, m0r));
+  const float sr = fminf(4.0f, fmaxf(0.25f, nPerh / (cur + 1.0e-30f)));
+  const float aa = sr < 1.0f ? 0.4f * (1.0f + sr * sr) : 0.4f * (1.0f + 1.0f / (sr * sr * sr));
+  F.f[F_HIDEAL][i] = fmin(L.hminInv, fmax(L.hmaxInv, (double)(ai / (1.0f - aa + aa * sr))));
 }
 
 __global__ void volumeMirrorKernel(Fields F, Fields32 P, long n) {
