@@ -327,12 +327,13 @@ def stretched_box(nx=24, ny=18, nz=14, seed=13, nPerh=1.51, jitter=0.15, vel_sca
 
 
 def crksph_box(n_side=10, seed=21, boundaries="periodic", rk_volume="sum", vel_scale=0.3, linear_velocity=None,
-               jitter=0.2):
+               jitter=0.2, two_lists=False):
     """random_box set up for CRKSPH (CRKSPHHydros.py:9-110 defaults): XSPH on,
     LimitedMonaghanGingoldViscosity with Cl = 2 (extent/4) = 1 and
     Cq = (extent/4)^2 = 0.25, no grad-h, compatible energy, IdealH.
     linear_velocity: a 3x3 matrix A to set v = A x (open boundaries)."""
-    p = random_box(n_side=n_side, seed=seed, boundaries=boundaries, vel_scale=vel_scale, jitter=jitter)
+    p = random_box(n_side=n_side, seed=seed, boundaries=boundaries, vel_scale=vel_scale, jitter=jitter,
+                   two_lists=two_lists)
     if linear_velocity is not None:
         p.vel = np.ascontiguousarray(p.pos @ np.asarray(linear_velocity, dtype=np.float64).T)
     p.config.update(hydro="crksph", rk_volume=rk_volume, xsph=True, gradh_correction=False,

@@ -83,6 +83,32 @@ def test_crk_step_parity(native_lib, oracle_mod, boundaries, rk_volume):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_crk_two_nodelists(native_lib, oracle_mod, precision):
+    # two NodeLists: the CRK density sums only the node's own list, XSPH and
+    # the moments weight other lists (fweight) as the reference does
+    from spheral_gb300.engine import Engine
+    p = problems.crksph_box(n_side=12, seed=59, boundaries="periodic", two_lists=True)
+    eng = Engine.from_problem(p, precision=precision)
+    orc = oracle_mod.Oracle(p)
+    eng.initialize()
+    orc.initialize()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    eng.sum_density()
+    orc.sum_density()
+    eng.evaluate_derivatives()
+    orc.rk_corrections()
+    orc.evaluate_derivatives()
+    bad = compare_fields(eng, orc, ["massDensity", "DvDt", "DepsDt", "DvDx", "XSPHDeltaV", "Hideal",
+                                    "massZerothMoment", "massFirstMoment"], tol)
+    assert not bad, bad
+    for _ in range(3):
+        eng.step()
+        orc.step()
+    bad = compare_fields(eng, orc, STATE, 1e-10 if precision == "fp64" else 1e-5)
+    assert not bad, bad
+
+
 def test_crk_reproduces_linear_velocity(native_lib, oracle_mod):
     A = np.array([[0.3, -0.2, 0.1], [0.05, -0.4, 0.25], [0.15, 0.2, 0.35]])
     p, eng, orc = _pair(oracle_mod, "open", "sum", seed=53, linear_velocity=A)
