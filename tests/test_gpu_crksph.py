@@ -212,3 +212,32 @@ def test_crk_unsupported_settings(native_lib):
     with pytest.raises(N.SphGpuError) as e:
         Engine(dict(base, rk_volume=2), precision="fp64")
     assert e.value.code == 3   # SPHGPU_E_UNSUPPORTED
+
+
+OPTIONS = {
+    "integrate_density": dict(density_update=1),
+    "total_energy": dict(compatible_energy=False, evolve_total_energy=True),
+    "no_xsph": dict(xsph=False),
+    "mg_q": dict(viscosity="monaghan_gingold", Cl=1.0, Cq=1.0),
+    "integrate_h": dict(h_update="integrate"),
+    "fixed_h": dict(h_update="fixed"),
+}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("option", list(OPTIONS))
+def test_crk_options(native_lib, oracle_mod, option, precision):
+    # the CRKSPH() options on the path: each against the oracle over three steps
+    from spheral_gb300.engine import Engine
+    p = problems.crksph_box(n_side=12, seed=61, boundaries="reflecting")
+    p.config.update(OPTIONS[option])
+    eng = Engine.from_problem(p, precision=precision)
+    orc = oracle_mod.Oracle(p)
+    eng.initialize()
+    orc.initialize()
+    for _ in range(3):
+        eng.step()
+        orc.step()
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    bad = compare_fields(eng, orc, STATE + ["DvDt", "DepsDt"], tol)
+    assert not bad, bad
