@@ -63,6 +63,10 @@ extern "C" {
 #define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
                                             symmetric-tensor H                                  */
 
+/* Base kernel of the TableKernel (cfg.kernel, cfg.kernel_order). */
+#define SPHGPU_KERNEL_BSPLINE 0   /* BSplineKernel (cubic, extent 2), the default            */
+#define SPHGPU_KERNEL_NBSPLINE 1  /* NBSplineKernel(order), order 2..9, extent (order+1)/2    */
+
 /* Hydro package (cfg.hydro). */
 #define SPHGPU_HYDRO_SPH 0     /* SPH (src/SPH/SPH.cc)                                              */
 #define SPHGPU_HYDRO_CRKSPH 1  /* CRKSPH with LinearOrder reproducing kernels (src/CRKSPH/CRKSPH.cc,
@@ -119,6 +123,8 @@ typedef struct sphgpu_config {
   int radial_only;                  /* ASPH radialOnly: H reshaped radially about the origin */
   int hydro;                        /* SPHGPU_HYDRO_* (CRKSPH(...) factory: CRKSPHHydros.py:9-110) */
   int rk_volume;                    /* SPHGPU_RK_VOLUME_* (SpheralController volumeType)    */
+  int kernel;                       /* SPHGPU_KERNEL_*: base kernel of the built-in table    */
+  int kernel_order;                 /* NBSplineKernel order                                  */
 } sphgpu_config;
 
 /* Fill *cfg with the reference defaults of the SPH() factory (cfl 0.25,
@@ -142,6 +148,14 @@ const char* sphgpu_last_error(sphgpu_handle h);
  * Replaces: TableKernel<Dim<3>>::TableKernel (src/Kernel/TableKernel.cc:169-209). */
 int sphgpu_build_bspline_table(int num_points, double* w, double* grad, double* grad2,
                                double* nperh, double* wsum, double* meta);
+
+/* The TableKernel of a base kernel (kernel = SPHGPU_KERNEL_*, order for
+ * NBSplineKernel): the layouts of sphgpu_build_bspline_table, and meta[9]
+ * receives the kernel extent (meta has 10 entries).
+ * Replaces: TableKernel<Dim<3>>::TableKernel(NBSplineKernel(order), numPoints)
+ * (src/Kernel/TableKernel.cc:169-209, src/Kernel/NBSplineKernel.cc:20-118). */
+int sphgpu_build_kernel_table(int kernel, int order, int num_points, double* w, double* grad, double* grad2,
+                              double* nperh, double* wsum, double* meta);
 
 /* Install a kernel table (the product of a reference TableKernel or of
  * sphgpu_build_bspline_table; same layouts).  Replaces: the TableKernelView

@@ -53,6 +53,8 @@ class OrcConfig(ctypes.Structure):
         ("radial_only", ctypes.c_int),
         ("hydro", ctypes.c_int),
         ("rk_volume", ctypes.c_int),
+        ("kernel", ctypes.c_int),
+        ("kernel_order", ctypes.c_int),
     ]
 
 
@@ -117,6 +119,8 @@ def lib():
             "orc_smoothing_scale_derivative": (i, [dp, dp, dp]),
             "orc_radial_evolution": (i, [dp, dp, d, d, dp]),
             "orc_rk_volumes": (i, [vp]),
+            "orc_nbspline_value": (d, [i, d]),
+            "orc_nbspline_grad": (d, [i, d]),
             "orc_rk_corrections": (i, [vp]),
         }
         for name, (res, args) in sig.items():
@@ -145,6 +149,8 @@ H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
 HYDRO = {"sph": 0, "crksph": 1}
 # RKVolumeType (RKCorrectionParams.hh): the volume types without a tessellation
 RK_VOLUME = {"mass_over_density": 0, "sum": 1, "h": 4}
+# base kernel of the TableKernel
+KERNEL = {"bspline": 0, "nbspline": 1}
 
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,
@@ -201,6 +207,8 @@ class Oracle:
         c.radial_only = int(cfg.get("radial_only", False))
         c.hydro = HYDRO[cfg.get("hydro", "sph")]
         c.rk_volume = RK_VOLUME[cfg.get("rk_volume", "sum")]
+        c.kernel = KERNEL[cfg.get("kernel", "bspline")]
+        c.kernel_order = int(cfg.get("kernel_order", 3))
         self._cfg = c
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(c))
@@ -310,7 +318,7 @@ class Oracle:
         nq = npts + (1 if npts % 2 == 0 else 0)
         ncoef = 3 * ((nq - 1) // 2)
         w = np.zeros(ncoef); g = np.zeros(ncoef); g2 = np.zeros(ncoef)
-        nh = np.zeros(2 * npts); ws = np.zeros(2 * npts); meta = np.zeros(9)
+        nh = np.zeros(2 * npts); ws = np.zeros(2 * npts); meta = np.zeros(10)
         self.L.orc_table(self.h, _dp(w), _dp(g), _dp(g2), _dp(nh), _dp(ws), _dp(meta))
         return dict(W=w, gradW=g, grad2W=g2, nperh=nh, wsum=ws, meta=meta)
 
@@ -366,3 +374,12 @@ def radial_evolution(h6, x3, s, r0):
     out = np.zeros(6)
     lib().orc_radial_evolution(_dp(h), _dp(x), s, r0, _dp(out))
     return out
+
+
+def nbspline_value(order, eta):
+    """The analytic NBSplineKernel(order) value at eta (Hdet = 1)."""
+    return lib().orc_nbspline_value(order, eta)
+
+
+def nbspline_grad(order, eta):
+    return lib().orc_nbspline_grad(order, eta)

@@ -483,6 +483,66 @@ static double bisectRoot(const F& f, double xmin, double xmax, double xacc = 1.0
 }
 
 //------------------------------------------------------------------------------
+// NBSplineKernel<Dim<3>> (src/Kernel/NBSplineKernel.cc:20-118,
+// NBSplineKernelInline.hh:40-99): the centred cardinal B-spline of the given
+// order, sum_i (-1)^i C(k, i) (eta - i + k/2)_+^(k-1) / (k-1)! with
+// k = order + 1, extent (order + 1) / 2 (integer division) and the volume
+// normalisation from Simpson's rule (10,000 bins) of 4 pi r^2 W(r)
+// (VolumeIntegrationFunctions.cc, simpsonsIntegration.hh:19-50).
+//------------------------------------------------------------------------------
+struct NBSpline3 {
+  int order = 3;
+  double A = 1.0;
+  double extent = 2.0;
+  static int factorial(int n) {
+    if (n < 0) return std::numeric_limits<int>::max();
+    int r = 1;
+    for (int i = 1; i < n + 1; ++i) r *= i;
+    return r;
+  }
+  static int binomial(int n, int m) { return factorial(n) / (factorial(n - m) * factorial(m)); }
+  static double oneSided(double x, int e) { return x >= 0.0 ? std::pow(x, e) : 0.0; }
+  double series(double eta, int e) const {
+    const int k = order + 1;
+    const double halfk = 0.5 * k;
+    double r = 0.0;
+    for (int i = 0; i <= k; ++i) r += std::pow(-1.0, i) * binomial(k, i) * oneSided(eta - i + halfk, e);
+    return r;
+  }
+  explicit NBSpline3(int o) : order(o) {
+    extent = (double)((order + 1) / 2);
+    A = 1.0;
+    const int nb = 10000;
+    const double dx = (extent - 0.0) / nb;
+    double sum = 0.0;
+    for (int i = 0; i < nb + 1; ++i) {
+      const double r = 0.0 + i * dx;
+      const double f = 4.0 * M_PI * r * r * value(r, 1.0);
+      if (i == 0 || i == nb) sum += f;
+      else if (i % 2 == 0) sum += 2.0 * f;
+      else sum += 4.0 * f;
+    }
+    sum *= dx / 3.0;
+    A = 1.0 / sum;
+  }
+  double value(double eta, double Hdet) const {
+    if (eta >= extent) return 0.0;
+    const int k1 = std::max(0, order);
+    return series(eta, k1) * (A * Hdet / factorial(k1));
+  }
+  double grad(double eta, double Hdet) const {
+    if (eta >= extent) return 0.0;
+    const int k2 = std::max(-1, order - 1);
+    return series(eta, k2) * (A * Hdet / factorial(k2));
+  }
+  double grad2(double eta, double Hdet) const {
+    if (eta >= extent) return 0.0;
+    const int k3 = std::max(-2, order - 2);
+    return series(eta, k3) * (A * Hdet / factorial(k3));
+  }
+};
+
+//------------------------------------------------------------------------------
 // TableKernel<Dim<3>> (TableKernel.cc:169-209).
 //------------------------------------------------------------------------------
 struct TableKernel {
@@ -508,7 +568,10 @@ struct TableKernel {
     return std::pow(result, 1.0 / 3.0);
   }
   void build(int nPoints, double minNperh_ = 0.25, double maxNperh_ = 64.0) {
-    BSpline3 k;
+    buildFrom(BSpline3(), nPoints, minNperh_, maxNperh_);
+  }
+  template <class K>
+  void buildFrom(const K& k, int nPoints, double minNperh_ = 0.25, double maxNperh_ = 64.0) {
     numPoints = nPoints;
     extent = k.extent;
     W.initialize(0.0, k.extent, nPoints, [&](double x) { return k.value(x, 1.0); });
@@ -570,6 +633,8 @@ struct Config {
   int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
   int evolveTotalEnergy = 0; // SPH evolveTotalEnergy (SPH.cc:105-108, 541)
   int hydro = 0;             // 0 SPH, 1 CRKSPH (CRKSPHHydros.py:9-110, LinearOrder)
+  int kernel = 0;            // base kernel of the TableKernel: 0 BSplineKernel, 1 NBSplineKernel(kernelOrder)
+  int kernelOrder = 3;
   int rkVolume = 1;          // RKVolumeType: 0 RKMassOverDensity, 1 RKSumVolume, 4 HVolume
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
   int gravity = 0;
@@ -1918,6 +1983,7 @@ struct orc_config {
   double eta_crit_frac, eta_fold_frac;
   int smoothing_scale, fix_shape, h_update, evolve_total_energy, radial_only;
   int hydro, rk_volume;
+  int kernel, kernel_order;
 };
 
 void* orc_create(const orc_config* c) {
@@ -1934,8 +2000,10 @@ void* orc_create(const orc_config* c) {
   g.smoothingScale = c->smoothing_scale; g.fixShape = c->fix_shape; g.hUpdate = c->h_update;
   g.evolveTotalEnergy = c->evolve_total_energy; g.radialOnly = c->radial_only;
   g.hydro = c->hydro; g.rkVolume = c->rk_volume;
+  g.kernel = c->kernel; g.kernelOrder = c->kernel_order;
   p->lastDt = c->last_dt; p->time = c->time;
-  p->W.build(c->num_table_points);
+  if (g.kernel == 1) p->W.buildFrom(orc::NBSpline3(g.kernelOrder), c->num_table_points);
+  else p->W.build(c->num_table_points);
   return p;
 }
 void orc_destroy(void* h) { delete static_cast<Problem*>(h); }
@@ -2153,9 +2221,17 @@ int orc_table(void* h, double* w, double* g, double* g2, double* nperh, double* 
   for (size_t k = 0; k < W.nperhLookup.v.size(); ++k) { nperh[k] = W.nperhLookup.v[k]; wsum[k] = W.wsumLookup.v[k]; }
   meta[0] = (double)W.W.N1; meta[1] = W.W.xstep; meta[2] = (double)W.nperhLookup.N;
   meta[3] = W.nperhLookup.xmin; meta[4] = W.nperhLookup.xmax; meta[5] = W.wsumLookup.xmin; meta[6] = W.wsumLookup.xmax;
-  meta[7] = W.minNperh; meta[8] = W.maxNperh;
+  meta[7] = W.minNperh; meta[8] = W.maxNperh; meta[9] = W.extent;
   return 0;
 }
+static const orc::NBSpline3& nbsplineOf(int order) {   // one normalised kernel per order (orders 1..15)
+  static orc::NBSpline3* cache[16] = {nullptr};
+  const int o = std::min(15, std::max(1, order));
+  if (!cache[o]) cache[o] = new orc::NBSpline3(o);
+  return *cache[o];
+}
+double orc_nbspline_value(int order, double eta) { return nbsplineOf(order).value(eta, 1.0); }
+double orc_nbspline_grad(int order, double eta) { return nbsplineOf(order).grad(eta, 1.0); }
 double orc_kernel_value(void* h, double eta, double Hdet) { return static_cast<Problem*>(h)->W.kernelValue(eta, Hdet); }
 double orc_grad_value(void* h, double eta, double Hdet) {
   double w, g; static_cast<Problem*>(h)->W.kernelAndGradValue(eta, Hdet, w, g); return g;

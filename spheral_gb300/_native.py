@@ -66,6 +66,8 @@ class Config(ctypes.Structure):
         ("radial_only", ctypes.c_int),
         ("hydro", ctypes.c_int),
         ("rk_volume", ctypes.c_int),
+        ("kernel", ctypes.c_int),
+        ("kernel_order", ctypes.c_int),
     ]
 
 
@@ -86,6 +88,7 @@ SIGNATURES = {
     "sphgpu_destroy": (_i, [_vp]),
     "sphgpu_last_error": (_cp, [_vp]),
     "sphgpu_build_bspline_table": (_i, [_i, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "sphgpu_build_kernel_table": (_i, [_i, _i, _i, _dp, _dp, _dp, _dp, _dp, _dp]),
     "sphgpu_set_kernel_table": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "sphgpu_set_nodelist": (_i, [_vp, _i, _d, _d, _d, _d, _d, _d]),
     "sphgpu_set_nodelist_hminratio": (_i, [_vp, _i, _d]),
@@ -174,4 +177,21 @@ def build_bspline_table(num_points=1000):
     rc = lib().sphgpu_build_bspline_table(num_points, dptr(w), dptr(g), dptr(g2), dptr(nh), dptr(ws), dptr(meta))
     if rc != SPHGPU_OK:
         raise SphGpuError(rc, "build_bspline_table")
+    return dict(W=w, gradW=g, grad2W=g2, nperh=nh, wsum=ws, meta=meta)
+
+
+KERNELS = {"bspline": 0, "nbspline": 1}
+
+
+def build_kernel_table(num_points=1000, kernel="bspline", order=3):
+    """Host-side TableKernel of a base kernel (BSplineKernel or
+    NBSplineKernel(order)); meta[9] is the kernel extent."""
+    nq = num_points | 1
+    ncoef = 3 * ((nq - 1) // 2)
+    w, g, g2 = np.zeros(ncoef), np.zeros(ncoef), np.zeros(ncoef)
+    nh, ws, meta = np.zeros(2 * num_points), np.zeros(2 * num_points), np.zeros(10)
+    rc = lib().sphgpu_build_kernel_table(KERNELS[kernel] if isinstance(kernel, str) else int(kernel), int(order),
+                                         num_points, dptr(w), dptr(g), dptr(g2), dptr(nh), dptr(ws), dptr(meta))
+    if rc != SPHGPU_OK:
+        raise SphGpuError(rc, "build_kernel_table")
     return dict(W=w, gradW=g, grad2W=g2, nperh=nh, wsum=ws, meta=meta)

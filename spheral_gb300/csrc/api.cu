@@ -17,6 +17,9 @@
 namespace sph {
 namespace table {
 int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* nperh, double* wsum, double* meta);
+int buildKernelTable(int kernel, int order, int numPoints, double* w, double* g, double* g2, double* nperh,
+                     double* wsum, double* meta);
+double kernelExtent(int kernel, int order);
 }
 
 struct Error : std::runtime_error {
@@ -136,6 +139,7 @@ struct sphgpu_ctx {
   DBuf posh, velm, thermo;   // FP32 mirrors of the pair-loop inputs
   DBuf hten;                 // ASPH: FP32 mirror of tensor H (2 float4 per node)
   DBuf vol32, rkc32;         // CRKSPH, mixed mode: FP32 mirrors of the RK volume and corrections
+  double kernelExtent = 2.0; // extent of the configured base kernel (BSpline 2, NBSpline (order+1)/2)
   DBuf stage;                // host <-> device staging for caller-order transfers
   DBuf v12;                  // half-step velocities + DepsDt0 of the mixed-mode energy sweep
   int cur = 0;
@@ -279,7 +283,7 @@ void setTable(sphgpu_ctx* c, const double* w, const double* g, const double* g2,
   auto& hp = c->hp;
   hp.tableN1 = N1;
   hp.tableXstep = meta[1];
-  hp.extent = 2.0;
+  hp.extent = c->kernelExtent;
   hp.W0 = 1.0 * (c->tw[0] + (c->tw[1] + c->tw[2] * 0.0) * 0.0);
   hp.hermN = nh;
   hp.hermXmin = meta[3];
@@ -1022,6 +1026,8 @@ void sphgpu_default_config(sphgpu_config* c) {
   c->radial_only = 0;
   c->hydro = SPHGPU_HYDRO_SPH;
   c->rk_volume = SPHGPU_RK_VOLUME_SUM;
+  c->kernel = SPHGPU_KERNEL_BSPLINE;
+  c->kernel_order = 3;
 }
 
 int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
@@ -1070,12 +1076,19 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       c->lists[k] = NodeListParams{1.51, 1e-20, 1e20, 1e-10, 1e10, 5.0 / 3.0, -1.79e308, 1.79e308, 1e20, 1e-20, 0.1};
     c->numLists = 0;
     if (cfg->gravity) c->grav = gravityCreate();
-    // Build the default cubic B-spline table.
+    // Build the table of the configured base kernel (TableKernel(BSplineKernel(), n)
+    // by default, or TableKernel(NBSplineKernel(order), n)).
+    if (cfg->kernel != SPHGPU_KERNEL_BSPLINE && cfg->kernel != SPHGPU_KERNEL_NBSPLINE)
+      throw Error(SPHGPU_E_UNSUPPORTED, "unknown base kernel");
+    if (cfg->kernel == SPHGPU_KERNEL_NBSPLINE && (cfg->kernel_order < 2 || cfg->kernel_order > 9))
+      throw Error(SPHGPU_E_ARG, "NBSplineKernel order must be 2..9");
     const int np = cfg->num_table_points > 0 ? cfg->num_table_points : 1000;
     const int nq = np | 1;
-    std::vector<double> w(3 * ((nq - 1) / 2)), g(w.size()), g2(w.size()), nh(2 * np), ws(2 * np), meta(9);
-    if (table::buildBSplineTable(np, w.data(), g.data(), g2.data(), nh.data(), ws.data(), meta.data()) != 0)
+    std::vector<double> w(3 * ((nq - 1) / 2)), g(w.size()), g2(w.size()), nh(2 * np), ws(2 * np), meta(10);
+    if (table::buildKernelTable(cfg->kernel, cfg->kernel_order, np, w.data(), g.data(), g2.data(), nh.data(),
+                                ws.data(), meta.data()) != 0)
       throw Error(SPHGPU_E_ARG, "bad num_table_points");
+    c->kernelExtent = meta[9];
     setTable(c, w.data(), g.data(), g2.data(), nh.data(), ws.data(), meta.data());
     refreshParams(c);
   } catch (const Error& e) {
@@ -1118,6 +1131,14 @@ int sphgpu_build_bspline_table(int num_points, double* w, double* grad, double* 
   if (!w || !grad || !grad2 || !nperh || !wsum || !meta) return SPHGPU_E_ARG;
   return sph::table::buildBSplineTable(num_points, w, grad, grad2, nperh, wsum, meta) == 0 ? SPHGPU_OK
                                                                                            : SPHGPU_E_ARG;
+}
+
+int sphgpu_build_kernel_table(int kernel, int order, int num_points, double* w, double* grad, double* grad2,
+                              double* nperh, double* wsum, double* meta) {
+  if (!w || !grad || !grad2 || !nperh || !wsum || !meta) return SPHGPU_E_ARG;
+  return sph::table::buildKernelTable(kernel, order, num_points, w, grad, grad2, nperh, wsum, meta) == 0
+             ? SPHGPU_OK
+             : SPHGPU_E_ARG;
 }
 
 int sphgpu_set_kernel_table(sphgpu_handle c, const double* w, const double* grad, const double* grad2,

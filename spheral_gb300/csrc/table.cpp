@@ -2,6 +2,8 @@
 // pair loops (product restatement of the reference table build).
 //
 //  BSplineKernel<Dim<3>> values/gradients   src/Kernel/BSplineKernelInline.hh:28-93
+//  NBSplineKernel<Dim<3>>                    src/Kernel/NBSplineKernel.cc:20-118, NBSplineKernelInline.hh:40-99
+//  its volume normalisation                  src/Kernel/VolumeIntegrationFunctions.cc, simpsonsIntegration.hh:19-50
 //  TableKernel<Dim<3>> constructor           src/Kernel/TableKernel.cc:169-209
 //  sumKernelValues (3-D)                     src/Kernel/TableKernel.cc:53-66
 //  QuadraticInterpolator::initialize         src/Utilities/QuadraticInterpolator.cc:60-100
@@ -149,15 +151,66 @@ double bisect(F f, double xmin, double xmax) {
   }
   return 0.0;
 }
-}  // namespace
 
-// Returns 0 on success.  Layouts as documented for sphgpu_build_bspline_table.
-int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* nperh, double* wsum, double* meta) {
+// The centred cardinal B-spline of a given order (Spheral's NBSplineKernel):
+// sum_i (-1)^i C(k, i) (eta - i + k/2)_+^e / e!, k = order + 1, with e = order
+// for W, order - 1 for dW/deta and order - 2 for the second derivative;
+// extent (order + 1) / 2 (integer division); 3-D volume normalisation by
+// Simpson's rule over 10,000 bins of 4 pi r^2 W(r).
+struct NBSpline {
+  int order;
+  double A = 1.0, extent;
+  static int factorial(int n) {
+    if (n < 0) return 2147483647;
+    int r = 1;
+    for (int i = 1; i < n + 1; ++i) r *= i;
+    return r;
+  }
+  static int binomial(int n, int m) { return factorial(n) / (factorial(n - m) * factorial(m)); }
+  double series(double eta, int e) const {
+    const int k = order + 1;
+    const double halfk = 0.5 * k;
+    double r = 0.0;
+    for (int i = 0; i <= k; ++i) {
+      const double x = eta - i + halfk;
+      r += std::pow(-1.0, i) * binomial(k, i) * (x >= 0.0 ? std::pow(x, e) : 0.0);
+    }
+    return r;
+  }
+  double term(double eta, int e) const {
+    if (eta >= extent) return 0.0;
+    return series(eta, e) * (A * 1.0 / factorial(e));
+  }
+  double W(double eta) const { return term(eta, std::max(0, order)); }
+  double G(double eta) const { return term(eta, std::max(-1, order - 1)); }
+  double G2(double eta) const { return term(eta, std::max(-2, order - 2)); }
+  explicit NBSpline(int o) : order(o), extent((double)((o + 1) / 2)) {
+    const int nb = 10000;
+    const double dx = (extent - 0.0) / nb;
+    double sum = 0.0;
+    for (int i = 0; i < nb + 1; ++i) {
+      const double r = 0.0 + i * dx;
+      const double f = 4.0 * M_PI * r * r * W(r);
+      if (i == 0 || i == nb) sum += f;
+      else if (i % 2 == 0) sum += 2.0 * f;
+      else sum += 4.0 * f;
+    }
+    sum *= dx / 3.0;
+    A = 1.0 / sum;
+  }
+};
+
+// TableKernel construction from a base kernel (W, dW/deta, d2W/deta2 at
+// Hdet = 1 and its extent).
+template <class FW, class FG, class FG2>
+int buildTable(double extent, FW fw, FG fg, FG2 fg2, int numPoints, double* w, double* g, double* g2, double* nperh,
+               double* wsum, double* meta) {
   if (numPoints < 3) return 2;
+  const double kExtent = extent;
   Quad qw, qg, qg2;
-  qw.fit(0.0, kExtent, (size_t)numPoints, bsW);
-  qg.fit(0.0, kExtent, (size_t)numPoints, bsG);
-  qg2.fit(0.0, kExtent, (size_t)numPoints, bsG2);
+  qw.fit(0.0, kExtent, (size_t)numPoints, fw);
+  qg.fit(0.0, kExtent, (size_t)numPoints, fg);
+  qg2.fit(0.0, kExtent, (size_t)numPoints, fg2);
   const double minNperh = std::max(0.25, 1.1 / kExtent);
   double maxNperh = 64.0;
   if (maxNperh <= minNperh) maxNperh = 4.0 * minNperh;
@@ -185,6 +238,31 @@ int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* n
   meta[7] = minNperh; meta[8] = maxNperh;
   return 0;
 }
+}  // namespace
+
+// Returns 0 on success.  Layouts as documented for sphgpu_build_bspline_table.
+int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* nperh, double* wsum, double* meta) {
+  return buildTable(kExtent, bsW, bsG, bsG2, numPoints, w, g, g2, nperh, wsum, meta);
+}
+
+// kernel 0: BSplineKernel (order ignored); 1: NBSplineKernel(order), order
+// 2..9.  meta[9] receives the kernel extent.
+int buildKernelTable(int kernel, int order, int numPoints, double* w, double* g, double* g2, double* nperh,
+                     double* wsum, double* meta) {
+  if (kernel == 0) {
+    const int rc = buildBSplineTable(numPoints, w, g, g2, nperh, wsum, meta);
+    meta[9] = kExtent;
+    return rc;
+  }
+  if (kernel != 1 || order < 2 || order > 9) return 2;
+  const NBSpline k(order);
+  const int rc = buildTable(
+      k.extent, [&](double x) { return k.W(x); }, [&](double x) { return k.G(x); }, [&](double x) { return k.G2(x); },
+      numPoints, w, g, g2, nperh, wsum, meta);
+  meta[9] = k.extent;
+  return rc;
+}
+double kernelExtent(int kernel, int order) { return kernel == 1 ? (double)((order + 1) / 2) : kExtent; }
 
 }  // namespace table
 }  // namespace sph

@@ -48,6 +48,8 @@ def config_from_dict(cfg, precision="fp64", device=0):
             c.hydro = HYDRO[v]
         elif k == "rk_volume" and isinstance(v, str):
             c.rk_volume = RK_VOLUME[v]
+        elif k == "kernel" and isinstance(v, str):
+            c.kernel = N.KERNELS[v]
         elif k in dict(N.Config._fields_):
             setattr(c, k, type(getattr(c, k))(v) if not isinstance(v, bool) else int(v))
     c.precision = N.PRECISION[precision] if isinstance(precision, str) else int(precision)

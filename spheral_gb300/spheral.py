@@ -101,12 +101,27 @@ class ASPHSmoothingScale:
 class BSplineKernel:
     """The cubic B-spline (src/Kernel/BSplineKernelInline.hh:28-93)."""
     kernelExtent = 2.0
+    _cfg = dict(kernel="bspline", kernel_order=3)
+
+
+class NBSplineKernel:
+    """The centred cardinal B-spline of a given order
+    (src/Kernel/NBSplineKernel.cc:20-118): extent (order + 1) / 2 with the
+    reference's integer division, volume normalisation by Simpson's rule."""
+
+    def __init__(self, order):
+        order = int(order)
+        if not 2 <= order <= 9:
+            raise NotImplementedError("NBSplineKernel orders 2..9 are on the GPU path")
+        self.order = order
+        self.kernelExtent = float((order + 1) // 2)
+        self._cfg = dict(kernel="nbspline", kernel_order=order)
 
 
 class TableKernel:
     def __init__(self, kernel, numPoints=1000):
-        if not isinstance(kernel, BSplineKernel):
-            raise NotImplementedError("only TableKernel(BSplineKernel(), n) is on the GPU path")
+        if not isinstance(kernel, (BSplineKernel, NBSplineKernel)):
+            raise NotImplementedError("TableKernel of BSplineKernel or NBSplineKernel is on the GPU path")
         self.kernel = kernel
         self.numPoints = int(numPoints)
         self.kernelExtent = kernel.kernelExtent
@@ -284,6 +299,7 @@ class SPHHydro:
                          sum_mass_density_over_all_nodelists=sumMassDensityOverAllNodeLists,
                          density_update=densityUpdate, eps_tensile=epsTensile, n_tensile=nTensile,
                          evolve_total_energy=evolveTotalEnergy)
+        self._cfg.update(W.kernel._cfg)
         self._cfg.update(Q._config())
         self._smoothingScaleMethod = smoothingScaleMethod or SPHSmoothingScale(IdealH, W)
         self._cfg.update(self._smoothingScaleMethod._cfg)

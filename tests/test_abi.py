@@ -28,10 +28,13 @@ def test_library_exports_every_declared_symbol(native_lib):
         assert hasattr(native_lib, n), n
 
 
-def test_host_table_matches_oracle(native_lib, oracle_mod):
+@pytest.mark.parametrize("kernel,order", [("bspline", 3), ("nbspline", 3), ("nbspline", 5), ("nbspline", 7)])
+def test_host_table_matches_oracle(native_lib, oracle_mod, kernel, order):
     from spheral_gb300 import _native, problems
-    t = _native.build_bspline_table(1000)
-    o = oracle_mod.Oracle(problems.random_box(n_side=12))
+    t = _native.build_kernel_table(1000, kernel, order)
+    p = problems.random_box(n_side=12)
+    p.config.update(kernel=kernel, kernel_order=order)
+    o = oracle_mod.Oracle(p)
     r = o.table()
     for k in ("W", "gradW", "grad2W", "nperh", "wsum", "meta"):
         a, b = t[k], r[k]

@@ -87,3 +87,14 @@ def test_crksph_factory_defaults_follow_the_reference():
             S.CRKSPH(dataBase=S.DataBase(), W=W, **bad)
     with pytest.raises(ValueError):
         S.CRKSPH(dataBase=S.DataBase(), W=W, evolveTotalEnergy=True)
+
+
+def test_nbspline_table_kernel_configures_the_package():
+    W = S.TableKernel(S.NBSplineKernel(5), 1000)
+    assert W.kernelExtent == 3.0
+    h = S.SPH(W=W, dataBase=S.DataBase())
+    assert h._cfg["kernel"] == "nbspline" and h._cfg["kernel_order"] == 5
+    c = S.CRKSPH(dataBase=S.DataBase(), W=W)
+    assert c._cfg["Cl"] == 2.0 * 0.75 and c._cfg["Cq"] == 0.75 ** 2   # Cl = 2 (extent/4), Cq = (extent/4)^2
+    with pytest.raises(NotImplementedError):
+        S.NBSplineKernel(12)
