@@ -66,6 +66,8 @@ extern "C" {
 /* Base kernel of the TableKernel (cfg.kernel, cfg.kernel_order). */
 #define SPHGPU_KERNEL_BSPLINE 0   /* BSplineKernel (cubic, extent 2), the default            */
 #define SPHGPU_KERNEL_NBSPLINE 1  /* NBSplineKernel(order), order 2..9, extent (order+1)/2    */
+#define SPHGPU_KERNEL_WENDLAND_C2 2  /* WendlandC2Kernel (3-D form), extent 1                */
+#define SPHGPU_KERNEL_WENDLAND_C4 3  /* WendlandC4Kernel (3-D form), extent 1                */
 
 /* Hydro package (cfg.hydro). */
 #define SPHGPU_HYDRO_SPH 0     /* SPH (src/SPH/SPH.cc)                                              */

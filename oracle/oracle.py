@@ -150,7 +150,7 @@ HYDRO = {"sph": 0, "crksph": 1}
 # RKVolumeType (RKCorrectionParams.hh): the volume types without a tessellation
 RK_VOLUME = {"mass_over_density": 0, "sum": 1, "h": 4}
 # base kernel of the TableKernel
-KERNEL = {"bspline": 0, "nbspline": 1}
+KERNEL = {"bspline": 0, "nbspline": 1, "wendland_c2": 2, "wendland_c4": 3}
 
 FIELD_NCOMP = {
     "position": 3, "velocity": 3, "mass": 1, "massDensity": 1, "specificThermalEnergy": 1, "H": 6,

@@ -543,6 +543,29 @@ struct NBSpline3 {
 };
 
 //------------------------------------------------------------------------------
+// WendlandC2Kernel / WendlandC4Kernel, 3-D forms
+// (src/Kernel/WendlandC2KernelInline.hh:40-90, WendlandC4KernelInline.hh:28-90).
+//------------------------------------------------------------------------------
+struct WendlandC2_3 {
+  double A = 21.0 / (2.0 * M_PI), extent = 1.0;
+  double value(double e, double Hdet) const { return A * Hdet * (std::pow(1.0 - e, 4) * (1.0 + 4.0 * e)) * (e < 1.0 ? 1.0 : 0.0); }
+  double grad(double e, double Hdet) const { return A * Hdet * (20.0 * std::pow(e - 1.0, 3) * e) * (e < 1.0 ? 1.0 : 0.0); }
+  double grad2(double e, double Hdet) const { return A * Hdet * (20.0 * std::pow(e - 1.0, 2) * (4.0 * e - 1.0)) * (e < 1.0 ? 1.0 : 0.0); }
+};
+struct WendlandC4_3 {
+  double A = 495.0 / (32.0 * M_PI), extent = 1.0;
+  double value(double e, double Hdet) const {
+    return A * Hdet * (std::pow(1.0 - e, 6) * (1.0 + 6.0 * e + (35.0 / 3.0) * (e * e))) * (e < 1.0 ? 1.0 : 0.0);
+  }
+  double grad(double e, double Hdet) const {
+    return A * Hdet * ((56.0 / 3.0) * std::pow(e - 1.0, 5) * e * (5.0 * e + 1.0)) * (e < 1.0 ? 1.0 : 0.0);
+  }
+  double grad2(double e, double Hdet) const {
+    return A * Hdet * ((56.0 / 3.0) * std::pow(e - 1.0, 4) * (35.0 * (e * e) - 4.0 * e - 1.0)) * (e < 1.0 ? 1.0 : 0.0);
+  }
+};
+
+//------------------------------------------------------------------------------
 // TableKernel<Dim<3>> (TableKernel.cc:169-209).
 //------------------------------------------------------------------------------
 struct TableKernel {
@@ -633,7 +656,8 @@ struct Config {
   int hUpdate = 0;           // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH (SmoothingScaleBase.cc:53-82)
   int evolveTotalEnergy = 0; // SPH evolveTotalEnergy (SPH.cc:105-108, 541)
   int hydro = 0;             // 0 SPH, 1 CRKSPH (CRKSPHHydros.py:9-110, LinearOrder)
-  int kernel = 0;            // base kernel of the TableKernel: 0 BSplineKernel, 1 NBSplineKernel(kernelOrder)
+  int kernel = 0;            // base kernel of the TableKernel: 0 BSplineKernel, 1 NBSplineKernel(kernelOrder),
+                             // 2 WendlandC2Kernel, 3 WendlandC4Kernel
   int kernelOrder = 3;
   int rkVolume = 1;          // RKVolumeType: 0 RKMassOverDensity, 1 RKSumVolume, 4 HVolume
   double dtMin = 0.0, dtMax = std::numeric_limits<double>::max(), dtGrowth = 2.0;
@@ -2003,6 +2027,8 @@ void* orc_create(const orc_config* c) {
   g.kernel = c->kernel; g.kernelOrder = c->kernel_order;
   p->lastDt = c->last_dt; p->time = c->time;
   if (g.kernel == 1) p->W.buildFrom(orc::NBSpline3(g.kernelOrder), c->num_table_points);
+  else if (g.kernel == 2) p->W.buildFrom(orc::WendlandC2_3(), c->num_table_points);
+  else if (g.kernel == 3) p->W.buildFrom(orc::WendlandC4_3(), c->num_table_points);
   else p->W.build(c->num_table_points);
   return p;
 }

@@ -180,7 +180,7 @@ def build_bspline_table(num_points=1000):
     return dict(W=w, gradW=g, grad2W=g2, nperh=nh, wsum=ws, meta=meta)
 
 
-KERNELS = {"bspline": 0, "nbspline": 1}
+KERNELS = {"bspline": 0, "nbspline": 1, "wendland_c2": 2, "wendland_c4": 3}
 
 
 def build_kernel_table(num_points=1000, kernel="bspline", order=3):

@@ -1078,7 +1078,8 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
     if (cfg->gravity) c->grav = gravityCreate();
     // Build the table of the configured base kernel (TableKernel(BSplineKernel(), n)
     // by default, or TableKernel(NBSplineKernel(order), n)).
-    if (cfg->kernel != SPHGPU_KERNEL_BSPLINE && cfg->kernel != SPHGPU_KERNEL_NBSPLINE)
+    if (cfg->kernel != SPHGPU_KERNEL_BSPLINE && cfg->kernel != SPHGPU_KERNEL_NBSPLINE &&
+        cfg->kernel != SPHGPU_KERNEL_WENDLAND_C2 && cfg->kernel != SPHGPU_KERNEL_WENDLAND_C4)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown base kernel");
     if (cfg->kernel == SPHGPU_KERNEL_NBSPLINE && (cfg->kernel_order < 2 || cfg->kernel_order > 9))
       throw Error(SPHGPU_E_ARG, "NBSplineKernel order must be 2..9");

@@ -200,6 +200,24 @@ struct NBSpline {
   }
 };
 
+// Wendland kernels, 3-D forms (src/Kernel/WendlandC2KernelInline.hh,
+// WendlandC4KernelInline.hh): extent 1, W(1) = 0.
+double wc2W(double e) { const double A = 21.0 / (2.0 * M_PI); return A * 1.0 * (std::pow(1.0 - e, 4) * (1.0 + 4.0 * e)) * (e < 1.0 ? 1.0 : 0.0); }
+double wc2G(double e) { const double A = 21.0 / (2.0 * M_PI); return A * 1.0 * (20.0 * std::pow(e - 1.0, 3) * e) * (e < 1.0 ? 1.0 : 0.0); }
+double wc2G2(double e) { const double A = 21.0 / (2.0 * M_PI); return A * 1.0 * (20.0 * std::pow(e - 1.0, 2) * (4.0 * e - 1.0)) * (e < 1.0 ? 1.0 : 0.0); }
+double wc4W(double e) {
+  const double A = 495.0 / (32.0 * M_PI);
+  return A * 1.0 * (std::pow(1.0 - e, 6) * (1.0 + 6.0 * e + (35.0 / 3.0) * (e * e))) * (e < 1.0 ? 1.0 : 0.0);
+}
+double wc4G(double e) {
+  const double A = 495.0 / (32.0 * M_PI);
+  return A * 1.0 * ((56.0 / 3.0) * std::pow(e - 1.0, 5) * e * (5.0 * e + 1.0)) * (e < 1.0 ? 1.0 : 0.0);
+}
+double wc4G2(double e) {
+  const double A = 495.0 / (32.0 * M_PI);
+  return A * 1.0 * ((56.0 / 3.0) * std::pow(e - 1.0, 4) * (35.0 * (e * e) - 4.0 * e - 1.0)) * (e < 1.0 ? 1.0 : 0.0);
+}
+
 // TableKernel construction from a base kernel (W, dW/deta, d2W/deta2 at
 // Hdet = 1 and its extent).
 template <class FW, class FG, class FG2>
@@ -246,12 +264,19 @@ int buildBSplineTable(int numPoints, double* w, double* g, double* g2, double* n
 }
 
 // kernel 0: BSplineKernel (order ignored); 1: NBSplineKernel(order), order
-// 2..9.  meta[9] receives the kernel extent.
+// 2..9; 2: WendlandC2Kernel; 3: WendlandC4Kernel.  meta[9] receives the
+// kernel extent.
 int buildKernelTable(int kernel, int order, int numPoints, double* w, double* g, double* g2, double* nperh,
                      double* wsum, double* meta) {
   if (kernel == 0) {
     const int rc = buildBSplineTable(numPoints, w, g, g2, nperh, wsum, meta);
     meta[9] = kExtent;
+    return rc;
+  }
+  if (kernel == 2 || kernel == 3) {
+    const int rc = kernel == 2 ? buildTable(1.0, wc2W, wc2G, wc2G2, numPoints, w, g, g2, nperh, wsum, meta)
+                               : buildTable(1.0, wc4W, wc4G, wc4G2, numPoints, w, g, g2, nperh, wsum, meta);
+    meta[9] = 1.0;
     return rc;
   }
   if (kernel != 1 || order < 2 || order > 9) return 2;
@@ -262,7 +287,9 @@ int buildKernelTable(int kernel, int order, int numPoints, double* w, double* g,
   meta[9] = k.extent;
   return rc;
 }
-double kernelExtent(int kernel, int order) { return kernel == 1 ? (double)((order + 1) / 2) : kExtent; }
+double kernelExtent(int kernel, int order) {
+  return kernel == 1 ? (double)((order + 1) / 2) : (kernel == 2 || kernel == 3 ? 1.0 : kExtent);
+}
 
 }  // namespace table
 }  // namespace sph

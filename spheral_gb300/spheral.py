@@ -118,10 +118,23 @@ class NBSplineKernel:
         self._cfg = dict(kernel="nbspline", kernel_order=order)
 
 
+class WendlandC2Kernel:
+    """Wendland C2, 3-D form (src/Kernel/WendlandC2KernelInline.hh), extent 1."""
+    kernelExtent = 1.0
+    _cfg = dict(kernel="wendland_c2", kernel_order=0)
+
+
+class WendlandC4Kernel:
+    """Wendland C4, 3-D form (src/Kernel/WendlandC4KernelInline.hh), extent 1."""
+    kernelExtent = 1.0
+    _cfg = dict(kernel="wendland_c4", kernel_order=0)
+
+
 class TableKernel:
     def __init__(self, kernel, numPoints=1000):
-        if not isinstance(kernel, (BSplineKernel, NBSplineKernel)):
-            raise NotImplementedError("TableKernel of BSplineKernel or NBSplineKernel is on the GPU path")
+        if not isinstance(kernel, (BSplineKernel, NBSplineKernel, WendlandC2Kernel, WendlandC4Kernel)):
+            raise NotImplementedError("TableKernel of BSplineKernel, NBSplineKernel or WendlandC2/C4Kernel is on "
+                                      "the GPU path")
         self.kernel = kernel
         self.numPoints = int(numPoints)
         self.kernelExtent = kernel.kernelExtent

@@ -28,7 +28,8 @@ def test_library_exports_every_declared_symbol(native_lib):
         assert hasattr(native_lib, n), n
 
 
-@pytest.mark.parametrize("kernel,order", [("bspline", 3), ("nbspline", 3), ("nbspline", 5), ("nbspline", 7)])
+@pytest.mark.parametrize("kernel,order", [("bspline", 3), ("nbspline", 3), ("nbspline", 5), ("nbspline", 7),
+                                          ("wendland_c2", 0), ("wendland_c4", 0)])
 def test_host_table_matches_oracle(native_lib, oracle_mod, kernel, order):
     from spheral_gb300 import _native, problems
     t = _native.build_kernel_table(1000, kernel, order)

@@ -60,3 +60,15 @@ def test_even_orders_truncated_at_the_integer_extent(oracle_mod, order):
     ext = (order + 1) // 2
     assert oracle_mod.nbspline_value(order, ext - 1e-9) > 1e-4
     assert oracle_mod.nbspline_value(order, float(ext)) == 0.0
+
+
+@pytest.mark.parametrize("kernel", ["wendland_c2", "wendland_c4"])
+def test_wendland_tables_normalised(oracle_mod, kernel):
+    # WendlandC2 / C4 (3-D forms, extent 1): the tabulated kernel integrates
+    # to one and vanishes at the extent
+    p = problems.random_box(n_side=12)
+    p.config.update(kernel=kernel)
+    o = oracle_mod.Oracle(p)
+    val, _ = integrate.quad(lambda r: 4 * np.pi * r * r * o.kernel_value(r), 0.0, 1.0, limit=400)
+    assert abs(val - 1.0) < 1e-6
+    assert o.kernel_value(1.0) == 0.0 and o.kernel_value(0.0) > 0.0
