@@ -23,21 +23,6 @@ using namespace dev;
 
 inline unsigned gridFor(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-__device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
-  const float y = __fsub_rn(x, c);
-  const float t = __fadd_rn(s, y);
-  c = __fsub_rn(__fsub_rn(t, s), y);
-  s = t;
-}
-__device__ __forceinline__ double kahanValue(float s, float c) { return (double)s - (double)c; }
-
-__device__ __forceinline__ void mirrorVel(uint32_t mir, float& vx, float& vy, float& vz) {
-  if (mir) {
-    if (mir & 3u) vx = -vx;
-    if (mir & 12u) vy = -vy;
-    if (mir & 48u) vz = -vz;
-  }
-}
 
 // Packed table lookup: W and dW/deta at eta (zero beyond the extent).
 __device__ __forceinline__ void lookup(const float4* __restrict__ ta, const float2* __restrict__ tb, int N1,

@@ -9,6 +9,26 @@ namespace dev {
 
 constexpr double kTiny30 = 1.0e-30;
 
+// Kahan-compensated FP32 accumulation (explicit round-to-nearest so the
+// compensation survives contraction); the pair leaves as the FP64 value s - c.
+__device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+__device__ __forceinline__ double kahanValue(float s, float c) { return (double)s - (double)c; }
+
+// Velocity of a mirror image: the components along the mirrored axes flip
+// (mir: per-axis bits of the entry's cell-offset code that cross a wall).
+__device__ __forceinline__ void mirrorVel(uint32_t mir, float& vx, float& vy, float& vz) {
+  if (mir) {
+    if (mir & 3u) vx = -vx;
+    if (mir & 12u) vy = -vy;
+    if (mir & 48u) vz = -vz;
+  }
+}
+
 // Warp-interleaved neighbour storage: slot q of node i lives at
 // ((i / 32) * cap + q) * 32 + i % 32, so a warp reading slot q of its 32 nodes
 // touches one contiguous 128-byte line.

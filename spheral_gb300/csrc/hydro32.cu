@@ -20,21 +20,6 @@ namespace sph {
 namespace {
 using namespace dev;
 
-__device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
-  const float y = __fsub_rn(x, c);
-  const float t = __fadd_rn(s, y);
-  c = __fsub_rn(__fsub_rn(t, s), y);
-  s = t;
-}
-__device__ __forceinline__ double kahanValue(float s, float c) { return (double)s - (double)c; }
-
-__device__ __forceinline__ void mirrorVel(uint32_t mir, float& vx, float& vy, float& vz) {
-  if (mir) {
-    if (mir & 3u) vx = -vx;
-    if (mir & 12u) vy = -vy;
-    if (mir & 48u) vz = -vz;
-  }
-}
 
 __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
