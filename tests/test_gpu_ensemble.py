@@ -65,3 +65,31 @@ def test_ensemble_rejects_repeated_handle(native_lib):
     arr = (ctypes.c_void_p * 2)(e.h, e.h)
     assert L.sphgpu_ensemble_advance(arr, 2, 1, 1e300, 1, None) == 2
     e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mixed_method_ensemble_equals_single_runs(native_lib, precision):
+    """Boxes with different hydro methods and kernels in one call: CRKSPH
+    (summed and mass-over-density volumes, the two-list variant) beside SPH
+    boxes with the BSpline and the fifth-order NBSpline tables."""
+    from spheral_gb300.engine import Engine
+    probs = [problems.crksph_box(12, 3), problems.turbulent_box(12, 7),
+             problems.crksph_box(12, 5, rk_volume="mass_over_density"),
+             problems.crksph_box(12, 9, two_lists=True)]
+    nb = problems.random_box(n_side=16, seed=11, boundaries="periodic")
+    nb.config.update(kernel="nbspline", kernel_order=5)
+    probs.append(nb)
+    ens = [Engine.from_problem(p, precision=precision) for p in probs]
+    for e in ens:
+        e.initialize()
+    Engine.ensemble_advance(ens, 3, nthreads=3)
+    for p, e in zip(probs, ens):
+        ref = Engine.from_problem(p, precision=precision)
+        ref.initialize()
+        ref.advance(3)
+        assert e.time == ref.time
+        for f in FIELDS:
+            assert np.array_equal(e.field(f), ref.field(f)), (p.name, f)
+        ref.close()
+    for e in ens:
+        e.close()
