@@ -330,8 +330,10 @@ int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
  * with the same configuration, NodeLists and boundaries (no set_particles
  * needed).  The image keeps the library's internal node order and kernel
  * variant, so a restored run continues bitwise as the uninterrupted one.
- * SPHGPU_E_ARG for a buffer that is not such an image, SPHGPU_E_STATE for an
- * image of another precision mode, viscosity or NodeList set. */
+ * SPHGPU_E_ARG for a buffer that is not such an image (wrong tag or version,
+ * short, a node order that is not a permutation, NodeList ids out of range),
+ * SPHGPU_E_STATE for an image of another precision mode, viscosity, smoothing
+ * scale, hydro package, RK volume type, kernel table or NodeList set. */
 int sphgpu_checkpoint_size(sphgpu_handle h, size_t* bytes);
 int sphgpu_checkpoint(sphgpu_handle h, void* buffer, size_t bytes);
 int sphgpu_restore(sphgpu_handle h, const void* buffer, size_t bytes);

@@ -978,7 +978,25 @@ struct CheckpointHeader {
   int64_t n, cycle;
   double time, lastDt, dtMultiplier, dtMinAcc, extraEnergy;
   int32_t precision, numLists, pairVariant, viscosity, smoothingScale, fixShape;
+  // version 3: the package and kernel the image belongs to
+  int32_t hydro, rkVolume, radialOnly, pad;
+  uint64_t tableHash;   // FNV-1a of the W and grad W table coefficients
 };
+constexpr int32_t kCheckpointVersion = 3;
+
+// FNV-1a over the bytes of the kernel table the handle evaluates, so an image
+// written with another TableKernel (base kernel, order or number of points,
+// or a table set by the caller) is told apart from this handle's.
+uint64_t tableHash(const sphgpu_ctx* c) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p, size_t bytes) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t k = 0; k < bytes; ++k) { h ^= b[k]; h *= 1099511628211ull; }
+  };
+  mix(c->tw.data(), c->tw.size() * sizeof(double));
+  mix(c->tg.data(), c->tg.size() * sizeof(double));
+  return h;
+}
 constexpr char kCheckpointMagic[8] = {'S', 'P', 'H', 'G', 'P', 'U', 'C', 'K'};
 size_t checkpointBytes(long n) {
   return sizeof(CheckpointHeader) + (size_t)F_NUM_PERMUTED * n * sizeof(double) + 2 * (size_t)n * sizeof(int);
@@ -1271,7 +1289,7 @@ int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
   const long n = c->n;
   CheckpointHeader h{};
   std::memcpy(h.magic, kCheckpointMagic, 8);
-  h.version = 2;
+  h.version = kCheckpointVersion;
   h.nfields = F_NUM_PERMUTED;
   h.n = n;
   h.cycle = c->cycle;
@@ -1286,6 +1304,10 @@ int sphgpu_checkpoint(sphgpu_handle c, void* buffer, size_t bytes) {
   h.viscosity = c->cfg.viscosity;
   h.smoothingScale = c->cfg.smoothing_scale;
   h.fixShape = c->cfg.fix_shape;
+  h.hydro = c->cfg.hydro;
+  h.rkVolume = c->cfg.rk_volume;
+  h.radialOnly = c->cfg.radial_only;
+  h.tableHash = tableHash(c);
   char* out = static_cast<char*>(buffer);
   std::memcpy(out, &h, sizeof(h));
   out += sizeof(h);
@@ -1304,16 +1326,38 @@ int sphgpu_restore(sphgpu_handle c, const void* buffer, size_t bytes) {
   if (!buffer || bytes < sizeof(CheckpointHeader)) throw Error(SPHGPU_E_ARG, "checkpoint buffer too small");
   CheckpointHeader h;
   std::memcpy(&h, buffer, sizeof(h));
-  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 2 || h.nfields != F_NUM_PERMUTED)
+  if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != kCheckpointVersion ||
+      h.nfields != F_NUM_PERMUTED)
     throw Error(SPHGPU_E_ARG, "not a checkpoint of this library version");
   if (h.n <= 0 || h.n >= kMaxNodes || bytes < checkpointBytes((long)h.n))
     throw Error(SPHGPU_E_ARG, "checkpoint size does not match its node count");
   if (h.precision != c->cfg.precision || h.viscosity != c->cfg.viscosity ||
-      h.smoothingScale != c->cfg.smoothing_scale || h.fixShape != c->cfg.fix_shape)
+      h.smoothingScale != c->cfg.smoothing_scale || h.fixShape != c->cfg.fix_shape ||
+      h.radialOnly != c->cfg.radial_only)
     throw Error(SPHGPU_E_STATE, "checkpoint written with another precision mode, viscosity or smoothing scale");
-  if (h.numLists > std::max(1, c->numLists))
+  if (h.hydro != c->cfg.hydro || (c->cfg.hydro == SPHGPU_HYDRO_CRKSPH && h.rkVolume != c->cfg.rk_volume))
+    throw Error(SPHGPU_E_STATE, "checkpoint written by another hydro package or RK volume type");
+  if (h.tableHash != tableHash(c))
+    throw Error(SPHGPU_E_STATE, "checkpoint written with another kernel table");
+  if (h.numLists < 1 || h.numLists > std::max(1, c->numLists))
     throw Error(SPHGPU_E_STATE, "checkpoint uses NodeLists that are not set on this handle");
   const long n = (long)h.n;
+  {
+    // The caller-order map must be a permutation of 0..n-1 and every NodeList
+    // id must name a NodeList of the image: both index device tables and
+    // caller arrays, so a truncated or corrupted image is refused here.
+    const char* tail = static_cast<const char*>(buffer) + sizeof(h) + (size_t)F_NUM_PERMUTED * n * sizeof(double);
+    std::vector<int> orig((size_t)n), ids((size_t)n);
+    std::memcpy(orig.data(), tail, n * sizeof(int));
+    std::memcpy(ids.data(), tail + n * sizeof(int), n * sizeof(int));
+    std::vector<unsigned char> seen((size_t)n, 0);
+    for (long k = 0; k < n; ++k) {
+      const int o = orig[k];
+      if (o < 0 || o >= n || seen[o]) throw Error(SPHGPU_E_ARG, "checkpoint node order is not a permutation");
+      seen[o] = 1;
+      if (ids[k] < 0 || ids[k] >= h.numLists) throw Error(SPHGPU_E_ARG, "checkpoint NodeList id out of range");
+    }
+  }
   ensureCapacity(c, n);
   c->n = n;
   c->cur = 0;

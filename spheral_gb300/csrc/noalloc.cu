@@ -108,8 +108,18 @@ extern "C" int sphgpu_conservation_noalloc(const double* mass, const double* vel
   long nb = (n + kNoAllocThreads - 1) / kNoAllocThreads;
   if (nb > kNoAllocBlocks) nb = kNoAllocBlocks;
   // Every block overwrites its own partials and the final pass reads only
-  // those nb sets, so nothing from an earlier call needs clearing.
-  noallocPartialKernel<<<(unsigned)nb, kNoAllocThreads, 0, s>>>(mass, vel, eps, pot, n, partials);
-  noallocFinalKernel<<<1, kNoAllocThreads, 0, s>>>(partials, (int)nb, out);
-  return cudaGetLastError() == cudaSuccess ? SPHGPU_OK : SPHGPU_E_CUDA;
+  // those nb sets, so nothing from an earlier call needs clearing.  The
+  // launches go through cudaLaunchKernel, whose return code is this launch's
+  // own: an error left pending by some earlier, unrelated launch on the
+  // thread is neither reported as this call's failure nor cleared by it.
+  int nbi = (int)nb;
+  void* partialArgs[] = {(void*)&mass, (void*)&vel, (void*)&eps, (void*)&pot, (void*)&n, (void*)&partials};
+  if (cudaLaunchKernel((const void*)noallocPartialKernel, dim3((unsigned)nb), dim3(kNoAllocThreads), partialArgs,
+                       0, s) != cudaSuccess)
+    return SPHGPU_E_CUDA;
+  void* finalArgs[] = {(void*)&partials, (void*)&nbi, (void*)&out};
+  if (cudaLaunchKernel((const void*)noallocFinalKernel, dim3(1), dim3(kNoAllocThreads), finalArgs, 0, s) !=
+      cudaSuccess)
+    return SPHGPU_E_CUDA;
+  return SPHGPU_OK;
 }

@@ -156,9 +156,10 @@ class FluidNodeList:
     """The per-NodeList parameters and initial fields of one fluid."""
 
     def __init__(self, name, eos, numInternal=0, hmin=1.0e-20, hmax=1.0e20, hminratio=0.1, nPerh=2.01,
-                 maxNumNeighbors=500, rhoMin=1.0e-10, rhoMax=1e10):
+                 maxNumNeighbors=500, rhoMin=1.0e-10, rhoMax=1e10, kernelExtent=2.0):
         self.name = name
         self.eos = eos
+        self.kernelExtent = float(kernelExtent)   # the NodeList's neighbour-search extent
         self.hmin, self.hmax, self.hminratio = float(hmin), float(hmax), float(hminratio)
         self.nPerh = float(nPerh)
         self.rhoMin, self.rhoMax = float(rhoMin), float(rhoMax)
@@ -212,11 +213,12 @@ class FluidNodeList:
 
 def makeFluidNodeList(name, eos, numInternal=0, numGhost=0, hmin=1.0e-20, hmax=1.0e20, hminratio=0.1, nPerh=2.01,
                       maxNumNeighbors=500, rhoMin=1.0e-10, rhoMax=1e10, kernelExtent=2.0, **ignored):
-    """src/NodeList/FluidNodeLists.py:15-47 (neighbour-object arguments are
-    accepted and ignored: the GPU package builds its own cell lists)."""
-    if kernelExtent != 2.0:
-        raise NotImplementedError("the GPU path uses the B-spline extent 2")
-    return FluidNodeList(name, eos, numInternal, hmin, hmax, hminratio, nPerh, maxNumNeighbors, rhoMin, rhoMax)
+    """src/NodeList/FluidNodeLists.py:15-47.  kernelExtent (default 2) is kept:
+    DataBase.maxKernelExtent, and through it the SPH()/CRKSPH() default Q,
+    depend on it as in the reference.  The other neighbour-object arguments
+    are accepted and ignored: the GPU package builds its own cell lists."""
+    return FluidNodeList(name, eos, numInternal, hmin, hmax, hminratio, nPerh, maxNumNeighbors, rhoMin, rhoMax,
+                         kernelExtent)
 
 
 class DataBase:
@@ -231,6 +233,12 @@ class DataBase:
     @property
     def numNodeLists(self):
         return len(self.nodeLists)
+
+    @property
+    def maxKernelExtent(self):
+        """The largest neighbour-search extent of the NodeLists, 0 with none
+        (src/DataBase/DataBase.cc:1742-1748)."""
+        return max([nl.kernelExtent for nl in self.nodeLists], default=0.0)
 
     numFluidNodeLists = numNodeLists
 
@@ -330,7 +338,9 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
         HUpdate=IdealH, epsTensile=0.0, nTensile=4.0, damageRelieveRubble=False, strengthInDamage=False,
         xmin=None, xmax=None, etaMinAxis=0.1, ASPH=False, smoothingScaleMethod=None):
     """The SPH() factory (src/SPH/SPHHydros.py:9-156) with its defaults; the
-    default Q is LimitedMonaghanGingoldViscosity(1, 1) as in the factory.
+    default Q is LimitedMonaghanGingoldViscosity with Cl = 2 (e/2) and
+    Cq = 2 (e/2)^2, e = dataBase.maxKernelExtent (SPHHydros.py:86-94): 2 and 2
+    for NodeLists of the default extent 2, 3 and 4.5 for extent 3.
     ASPH="CLASSIC" selects ASPHClassicSmoothingScale (SPHHydros.py:130-138);
     ASPH=True (the Voronoi-based ASPHSmoothingScale) is not on this path."""
     if smoothingScaleMethod is None:
@@ -345,8 +355,9 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
         raise NotImplementedError("unknown smoothing-scale package")
     if (filter or 0.0) != 0.0:
         raise NotImplementedError("H filtering is not on the GPU path")
-    if Q is None:
-        Q = LimitedMonaghanGingoldViscosity(1.0, 1.0)
+    if not Q:
+        e = dataBase.maxKernelExtent / 2.0
+        Q = LimitedMonaghanGingoldViscosity(2.0 * e, 2.0 * e * e)
     return SPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, gradhCorrection,
                     XSPH, correctVelocityGradient, sumMassDensityOverAllNodeLists, densityUpdate, epsTensile,
                     nTensile, smoothingScaleMethod, evolveTotalEnergy)
@@ -375,7 +386,8 @@ def CRKSPH(dataBase, W, Q=None, order=RKOrder.LinearOrder, filter=0.0, cfl=0.25,
            crktype="default", smoothingScaleMethod=None, volumeType=RKSumVolume):
     """The CRKSPH() factory (src/CRKSPH/CRKSPHHydros.py:9-110) with its
     defaults: the default Q is LimitedMonaghanGingoldViscosity with
-    Cl = 2 (extent/4) and Cq = (extent/4)^2.  The reference hands the RK
+    Cl = 2 (e/4) and Cq = (e/4)^2, e = dataBase.maxKernelExtent
+    (CRKSPHHydros.py:64-68).  The reference hands the RK
     volume type to SpheralController (default RKVoronoiVolume, which needs a
     tessellation); here it is the volumeType argument, RKSumVolume by default.
     LinearOrder, the default crktype and SPHSmoothingScale are on this path."""
@@ -389,8 +401,8 @@ def CRKSPH(dataBase, W, Q=None, order=RKOrder.LinearOrder, filter=0.0, cfl=0.25,
         smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
     elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, FixedSmoothingScale)):
         raise NotImplementedError("CRKSPH runs with SPHSmoothingScale on the GPU path")
-    if Q is None:
-        e = W.kernelExtent / 4.0
+    if not Q:
+        e = dataBase.maxKernelExtent / 4.0
         Q = LimitedMonaghanGingoldViscosity(2.0 * e, e * e)
     return CRKSPHHydro(dataBase, W, Q, cfl, useVelocityMagnitudeForDt, compatibleEnergyEvolution, evolveTotalEnergy,
                        XSPH, densityUpdate, epsTensile, nTensile, smoothingScaleMethod, volumeType)
@@ -433,6 +445,12 @@ class CheapSynchronousRK2Integrator:
         lists = self.dataBase.nodeLists
         if not lists:
             raise RuntimeError("the DataBase has no NodeLists")
+        for nl in lists:
+            # the GPU neighbour build takes its extent from the TableKernel; the
+            # reference takes the NodeLists' (ConnectivityMap.cc:779-786)
+            if nl.kernelExtent != hydro.W.kernelExtent:
+                raise NotImplementedError(f"NodeList {nl.name!r} has kernelExtent {nl.kernelExtent}, the TableKernel "
+                                          f"{hydro.W.kernelExtent}: the GPU path needs them equal")
         pieces = [nl._state for nl in lists]
         cat = lambda k: np.concatenate([p[k] for p in pieces])
         H = cat("H")
@@ -443,6 +461,7 @@ class CheapSynchronousRK2Integrator:
                                 cat("specificThermalEnergy"), 1.0 / H[:, 0], nodelist if len(lists) > 1 else None,
                                 nls, [b._spec for b in hydro.boundaries], cfg)
         prob.H = np.ascontiguousarray(H)
+        self._problem = prob
         self._engine = Engine.from_problem(prob, precision=self.precision)
         self._engine.initialize()
         lo = 0

@@ -1,6 +1,7 @@
 """Generate the golden fixtures from the reference's own test data.
 
-Runs only where the reference source tree is available: it imports
+Runs only where the reference source tree is available (its root is the
+first argument, or SPHERAL_REFERENCE_ROOT): it imports
 tests/functional/Hydro/Sod/SodAnalyticSolution.py (a pure-Python module) for
 sod_analytic.npz, and reads the Evrard collapse comparison profiles of
 tests/functional/EvrardSphericalCollapse/{rho,vel,entropy}.dat for
@@ -12,16 +13,22 @@ Configuration: the 3-D planar Sod tube of spheral_gb300.problems.sod (x in
 of density, velocity, specific energy and pressure at t = 0.05, 0.10, 0.15
 on 401 points.
 """
+import argparse
 import os
 import sys
 
 import numpy as np
 
-REF = "/root/reference/tests/functional/Hydro/Sod"
-EVRARD = "/root/reference/tests/functional/EvrardSphericalCollapse"
+
+def _paths(root):
+    """Directories of the reference's Sod and Evrard test data under the
+    root of a Spheral source tree."""
+    return (os.path.join(root, "tests", "functional", "Hydro", "Sod"),
+            os.path.join(root, "tests", "functional", "EvrardSphericalCollapse"))
 
 
-def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analytic.npz")):
+def main(root, out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analytic.npz")):
+    REF, EVRARD = _paths(root)
     sys.path.insert(0, REF)
     from SodAnalyticSolution import SodSolutionGasGas
     g = 5.0 / 3.0
@@ -38,10 +45,10 @@ def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sod_analy
         data[key + "_P"] = np.array(P)
     np.savez(out, **data)
     print("wrote", out)
-    evrard()
+    evrard(EVRARD)
 
 
-def evrard(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "evrard_profiles.npz")):
+def evrard(EVRARD, out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "evrard_profiles.npz")):
     """Radial profiles at t = 0.8 of the Evrard collapse (columns r, value)."""
     data = {}
     for name in ("rho", "vel", "entropy"):
@@ -53,4 +60,10 @@ def evrard(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "evrard_
 
 
 if __name__ == "__main__":
-    main()
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("reference_root", nargs="?", default=os.environ.get("SPHERAL_REFERENCE_ROOT"),
+                    help="root of the Spheral source tree (default: $SPHERAL_REFERENCE_ROOT)")
+    a = ap.parse_args()
+    if not a.reference_root:
+        ap.error("give the Spheral source root as an argument or in SPHERAL_REFERENCE_ROOT")
+    main(a.reference_root)

@@ -8,16 +8,52 @@ from spheral_gb300 import spheral as S
 
 def test_factory_defaults_follow_the_reference():
     # SPH() defaults (src/SPH/SPHHydros.py:9-33): XSPH on, compatible energy,
-    # grad-h, RigorousSumDensity, and LimitedMonaghanGingoldViscosity(1, 1)
+    # grad-h, RigorousSumDensity, and LimitedMonaghanGingoldViscosity with
+    # Cl = 2 (e/2), Cq = 2 (e/2)^2 for e = dataBase.maxKernelExtent (:86-94)
     db = S.DataBase()
+    nodes = S.makeFluidNodeList("fluid", S.GammaLawGasMKS(5.0 / 3.0, 1.0))
+    assert nodes.nodesPerSmoothingScale() == 2.01 and nodes.hmin == 1e-20 and nodes.rhoMin == 1e-10
+    assert nodes.kernelExtent == 2.0
+    db.appendNodeList(nodes)
+    assert db.maxKernelExtent == 2.0
     W = S.TableKernel(S.BSplineKernel(), 1000)
     hydro = S.SPH(W=W, dataBase=db)
     assert isinstance(hydro.Q, S.LimitedMonaghanGingoldViscosity)
     c = hydro._cfg
     assert c["xsph"] and c["compatible_energy"] and c["gradh_correction"] and c["density_update"] == 0
     assert c["viscosity"] == "limited_monaghan_gingold" and c["eta_crit_frac"] == 1.0 and c["eta_fold_frac"] == 0.2
-    nodes = S.makeFluidNodeList("fluid", S.GammaLawGasMKS(5.0 / 3.0, 1.0))
-    assert nodes.nodesPerSmoothingScale() == 2.01 and nodes.hmin == 1e-20 and nodes.rhoMin == 1e-10
+    assert c["Cl"] == 2.0 and c["Cq"] == 2.0
+
+
+def test_default_q_follows_the_nodelist_extent():
+    # extent 3 (an NBSpline(5) script passes kernelExtent = W.kernelExtent): Cl = 3, Cq = 4.5
+    db = S.DataBase()
+    db.appendNodeList(S.makeFluidNodeList("a", S.GammaLawGas(5.0 / 3.0), kernelExtent=3.0))
+    db.appendNodeList(S.makeFluidNodeList("b", S.GammaLawGas(5.0 / 3.0)))
+    assert db.maxKernelExtent == 3.0
+    c = S.SPH(W=S.TableKernel(S.NBSplineKernel(5), 1000), dataBase=db)._cfg
+    assert c["Cl"] == 3.0 and c["Cq"] == 4.5
+    # an empty DataBase has extent 0, so the reference's default Q has no strength
+    assert S.DataBase().maxKernelExtent == 0.0
+    c0 = S.SPH(W=S.TableKernel(S.BSplineKernel(), 1000), dataBase=S.DataBase())._cfg
+    assert c0["Cl"] == 0.0 and c0["Cq"] == 0.0
+    # an explicit Q is kept
+    q = S.MonaghanGingoldViscosity(1.0, 0.5)
+    assert S.SPH(W=S.TableKernel(S.BSplineKernel(), 1000), dataBase=db, Q=q)._cfg["Cq"] == 0.5
+
+
+def test_nodelist_extent_must_match_the_table_kernel():
+    # the GPU neighbour build uses the TableKernel's extent: a NodeList with a
+    # different neighbour extent is refused when the integrator starts
+    db = S.DataBase()
+    nodes = S.makeFluidNodeList("fluid", S.GammaLawGas(5.0 / 3.0), kernelExtent=2.0)
+    nodes.resize(8)
+    db.appendNodeList(nodes)
+    hydro = S.SPH(W=S.TableKernel(S.NBSplineKernel(5), 1000), dataBase=db)
+    integ = S.CheapSynchronousRK2Integrator(db)
+    integ.appendPhysicsPackage(hydro)
+    with pytest.raises(NotImplementedError):
+        integ.step()
 
 
 def test_out_of_path_options_are_refused():
@@ -73,9 +109,11 @@ def test_nodelist_fields_before_the_first_step():
 
 def test_crksph_factory_defaults_follow_the_reference():
     # CRKSPHHydros.py:9-110: XSPH on, compatible energy, LimitedMonaghanGingold
-    # with Cl = 2 (extent/4), Cq = (extent/4)^2, no grad-h
+    # with Cl = 2 (e/4), Cq = (e/4)^2 for e = dataBase.maxKernelExtent, no grad-h
     W = S.TableKernel(S.BSplineKernel(), 1000)
-    h = S.CRKSPH(dataBase=S.DataBase(), W=W)
+    db = S.DataBase()
+    db.appendNodeList(S.makeFluidNodeList("fluid", S.GammaLawGas(5.0 / 3.0)))
+    h = S.CRKSPH(dataBase=db, W=W)
     c = h._cfg
     assert c["hydro"] == "crksph" and c["rk_volume"] == "sum"
     assert c["xsph"] and c["compatible_energy"] and not c["gradh_correction"]
@@ -92,9 +130,11 @@ def test_crksph_factory_defaults_follow_the_reference():
 def test_nbspline_table_kernel_configures_the_package():
     W = S.TableKernel(S.NBSplineKernel(5), 1000)
     assert W.kernelExtent == 3.0
-    h = S.SPH(W=W, dataBase=S.DataBase())
+    db = S.DataBase()
+    db.appendNodeList(S.makeFluidNodeList("fluid", S.GammaLawGas(5.0 / 3.0), kernelExtent=W.kernelExtent))
+    h = S.SPH(W=W, dataBase=db)
     assert h._cfg["kernel"] == "nbspline" and h._cfg["kernel_order"] == 5
-    c = S.CRKSPH(dataBase=S.DataBase(), W=W)
+    c = S.CRKSPH(dataBase=db, W=W)
     assert c._cfg["Cl"] == 2.0 * 0.75 and c._cfg["Cq"] == 0.75 ** 2   # Cl = 2 (extent/4), Cq = (extent/4)^2
     with pytest.raises(NotImplementedError):
         S.NBSplineKernel(12)

@@ -51,6 +51,35 @@ def test_conservation_noalloc_matches_handle(native_lib):
             assert abs(got[k] - want[k]) <= 1e-12 * max(scale, 1e-300), (k, got[k], want[k])
 
 
+def test_conservation_noalloc_with_gravity_potential(native_lib):
+    # a self-gravitating box: the potential passed as pot gives the 1/2 sum m phi
+    # term and the total of the handle's own tally (TreeGravity's extra energy)
+    import torch
+    from spheral_gb300 import problems
+    from spheral_gb300.engine import Engine
+    p = problems.random_box(n_side=10, seed=31, boundaries="open", gravity=True)
+    eng = Engine.from_problem(p, precision="fp64")
+    eng.initialize()
+    eng.advance(2)
+    want = eng.conservation()
+    assert want[6] != 0.0
+    dev = torch.device("cuda", 0)
+    mass = torch.tensor(eng.field("mass"), dtype=torch.float64, device=dev)
+    vel = torch.tensor(eng.field("velocity").ravel(), dtype=torch.float64, device=dev)
+    eps = torch.tensor(eng.field("specificThermalEnergy"), dtype=torch.float64, device=dev)
+    pot = torch.tensor(eng.field("potential"), dtype=torch.float64, device=dev)
+    out = torch.empty(8, dtype=torch.float64, device=dev)
+    f = _entry(native_lib)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for _ in range(2):
+        out.fill_(np.nan)
+        assert f(mass.data_ptr(), vel.data_ptr(), eps.data_ptr(), pot.data_ptr(), p.n, out.data_ptr(), stream) == 0
+        torch.cuda.synchronize(dev)
+        got = out.cpu().numpy()
+        for k in (0, 4, 5, 6, 7):
+            assert abs(got[k] - want[k]) <= 1e-12 * abs(want[k]), (k, got[k], want[k])
+
+
 def test_conservation_noalloc_rejects_sizes(native_lib):
     import torch
     f = _entry(native_lib)
