@@ -42,6 +42,7 @@ VALUES_PER_NODE = 63       # per-node state read + derivatives written by the pa
 # kelvin_helmholtz(n1=64) (862 MB for 21.76 M pairs); traffic grows in
 # proportion to the pairs, so it is scaled by the pairs of the launch.
 TRAFFIC_BYTES_PER_PAIR = {"fp32": 39.6}
+TRAFFIC_SOURCE = "ncu capture at n1=64 scaled by pairs per launch"
 
 
 def peaks():
@@ -177,24 +178,27 @@ def make_workload(args):
     raise SystemExit("unknown workload")
 
 
-def cpu_baseline(args, steps=None, warmup=1):
+def cpu_baseline(args, steps=None, warmup=1, n1=None, threads=0):
     """Oracle CheapRK2 steps on a bounded sample of the workload (same
-    generator, smaller lattice); returns pairs/s and the sample description."""
+    generator, smaller lattice); returns pairs/s and the sample description.
+    threads = 0 uses every host thread, 1 a single core."""
     from oracle import oracle as orc
     from spheral_gb300 import problems
     orc.build()
+    n1 = args.cpu_n1 if n1 is None else n1
+    orc.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
     if args.workload == "kh":
-        p = problems.kelvin_helmholtz(n1=args.cpu_n1)
+        p = problems.kelvin_helmholtz(n1=n1)
     elif args.workload == "sweep":
-        p = problems.sweep_box(n_side=args.cpu_n1, neighbors=args.neighbors)
+        p = problems.sweep_box(n_side=n1, neighbors=args.neighbors)
     elif args.workload == "evrard":
-        p = problems.evrard(n=65536)
+        p = problems.evrard(n=65536 if threads != 1 else 8192)
     elif args.workload == "asph":
-        p = asph_box(args.cpu_n1)
+        p = asph_box(n1)
     elif args.workload == "crksph":
-        p = crksph_kh(args.cpu_n1)
+        p = crksph_kh(n1)
     else:
-        p = problems.sod(nx1=args.cpu_n1)
+        p = problems.sod(nx1=n1)
     o = orc.Oracle(p)
     o.initialize()
     for _ in range(max(1, warmup)):   # the first step allocates
@@ -206,8 +210,10 @@ def cpu_baseline(args, steps=None, warmup=1):
         o.step()
         pairs += o.L.orc_num_pairs(o.h)
     dt = time.perf_counter() - t0
-    return pairs / dt, dict(n=p.n, steps=steps, seconds=dt, pairs_per_step=pairs / steps,
-                            cores=orc.num_threads(), kind="port")
+    cores = orc.num_threads()
+    orc.set_threads(os.cpu_count() or 1)
+    return pairs / dt, dict(n=p.n, n1=n1, steps=steps, seconds=dt, pairs_per_step=pairs / steps,
+                            cores=cores, kind="port")
 
 
 def run_reference(args, ws, rank, dist):
@@ -242,6 +248,150 @@ def time_steps(eng, steps, prof_names=()):
     launches = eng.launch_count() - l0
     prof = {n: eng.profile_get(n) for n in prof_names}
     return ms, pairs, launches, prof
+
+
+def kh_mode_amplitude(pos, vel, mass):
+    """Amplitude of the vy mode at the seeded wavenumber 4 pi along x at the
+    two shear layers y = 0.25 and 0.75 (the growth diagnostic of McNally,
+    Lyra and Passy 2012, ApJS 201:18, eqs. 10-13): s, c and d are sums over
+    nodes of vy sin(4 pi x) e, vy cos(4 pi x) e and e, with the weight
+    e = exp(-4 pi |y - 0.25|) below y = 0.5 and exp(-4 pi |(1 - y) - 0.25|)
+    above; the amplitude is 2 sqrt((s/d)^2 + (c/d)^2)."""
+    x, y, vy = pos[:, 0], pos[:, 1], vel[:, 1]
+    e = np.where(y < 0.5, np.exp(-4.0 * math.pi * np.abs(y - 0.25)), np.exp(-4.0 * math.pi * np.abs(0.75 - y)))
+    w = mass * e
+    d = np.sum(w)
+    s_ = np.sum(w * vy * np.sin(4.0 * math.pi * x)) / d
+    c_ = np.sum(w * vy * np.cos(4.0 * math.pi * x)) / d
+    return float(2.0 * math.sqrt(s_ * s_ + c_ * c_))
+
+
+def fp32_vs_fp64(args, local):
+    """The mixed mode against an all-FP64 run of the same Kelvin-Helmholtz
+    problem at the same physical time.  The FP64 run takes
+    args.fp64_compare_steps steps and defines the goal time T; the mixed run
+    and a control FP64 run whose initial positions are moved by one ulp are
+    advanced to T exactly (the last step is cut at T).  Node-by-node L1 and
+    L2 relative differences of rho, eps and v (nodes in the caller's order,
+    so the comparison is Lagrangian) and the shear-layer mode amplitude are
+    reported for mixed vs FP64 and for the control vs FP64: KH is chaotic, and
+    the control measures how far two FP64 runs drift apart from a rounding-
+    level change of the initial state."""
+    from spheral_gb300.engine import Engine
+    prob = crksph_kh(args.compare_n1) if args.workload == "crksph" else None
+    if prob is None:
+        from spheral_gb300 import problems
+        prob = problems.kelvin_helmholtz(n1=args.compare_n1)
+
+    def run(p, precision, goal=None):
+        e = Engine.from_problem(p, precision=precision, device=local)
+        e.initialize()
+        c0 = e.conservation()
+        t0 = time.perf_counter()
+        steps = 0
+        if goal is None:
+            e.advance(args.fp64_compare_steps)
+            steps = args.fp64_compare_steps
+        else:
+            while e.time < goal * (1.0 - 1e-15) and steps < 20 * args.fp64_compare_steps:
+                e.step(goal)
+                steps += 1
+        e.synchronize()
+        wall = time.perf_counter() - t0
+        c1 = e.conservation()
+        out = dict(rho=e.field("massDensity"), eps=e.field("specificThermalEnergy"), vel=e.field("velocity"),
+                   pos=e.field("position"), t=e.time, steps=steps, wall=wall,
+                   err=abs(c1[7] - c0[7]) / abs(c0[7]))
+        e.close()
+        return out
+
+    ref = run(prob, "fp64")
+    goal = ref["t"]
+    mixed = run(prob, "fp32", goal)
+    import copy
+    pert = copy.copy(prob)
+    pert.pos = np.ascontiguousarray(np.nextafter(prob.pos, np.inf))
+    ctrl = run(pert, "fp64", goal)
+
+    def diffs(a, b):
+        out = {}
+        for k in ("rho", "eps", "vel"):
+            x, y = a[k].ravel(), b[k].ravel()
+            out["L1_" + k] = float(np.sum(np.abs(x - y)) / np.sum(np.abs(y)))
+            out["L2_" + k] = float(math.sqrt(np.sum((x - y) ** 2) / np.sum(y * y)))
+            out["max_" + k] = float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+        return out
+
+    amp = {name: kh_mode_amplitude(r["pos"], r["vel"], prob.mass) for name, r in
+           (("fp64", ref), ("mixed", mixed), ("control", ctrl))}
+    amp0 = kh_mode_amplitude(prob.pos, prob.vel, prob.mass)
+    return {"workload": ("kelvin_helmholtz_3d_crksph" if args.workload == "crksph" else "kelvin_helmholtz_3d"),
+            "n1": args.compare_n1, "n": prob.n, "goal_time": goal, "steps_fp64": ref["steps"],
+            "steps_mixed": mixed["steps"], "steps_control": ctrl["steps"],
+            "time_mixed": mixed["t"], "time_control": ctrl["t"],
+            "energy_error_fp64": ref["err"], "energy_error_mixed": mixed["err"], "energy_error_control": ctrl["err"],
+            "mixed_vs_fp64": diffs(mixed, ref), "control_vs_fp64": diffs(ctrl, ref),
+            "mode_amplitude": dict(amp, initial=amp0),
+            "mode_amplitude_rel_diff_mixed": abs(amp["mixed"] - amp["fp64"]) / amp["fp64"],
+            "mode_amplitude_rel_diff_control": abs(amp["control"] - amp["fp64"]) / amp["fp64"],
+            "control": "FP64 run with every initial position moved by one ulp (numpy nextafter toward +inf)",
+            "wall_s": {"fp64": ref["wall"], "mixed": mixed["wall"], "control": ctrl["wall"]}}
+
+
+def ensemble_record(args, local, nboxes, steps, warmup=2):
+    """Batched-ensemble throughput against one large box of about the same
+    total size: nboxes turbulent boxes (counts log-uniform 4,096..262,144,
+    seeded) advanced together by sphgpu_ensemble_advance, then one box alone."""
+    from spheral_gb300.engine import Engine
+    from spheral_gb300 import problems
+    import torch
+    probs = problems.ensemble(nboxes)
+    engines = [Engine.from_problem(p, precision=args.precision, device=local) for p in probs]
+    for e in engines:
+        e.initialize()
+    Engine.ensemble_advance(engines, warmup, nthreads=args.threads)
+    e0 = [e.conservation()[7] for e in engines]
+    before = sum(e.neighbor_entries() // 2 for e in engines)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Engine.ensemble_advance(engines, steps, nthreads=args.threads)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    after = sum(e.neighbor_entries() // 2 for e in engines)
+    pairs = 0.5 * (before + after) * steps
+    value = pairs / wall
+    errs = [abs(e.conservation()[7] - a) / abs(a) for e, a in zip(engines, e0)]
+    ntot = sum(p.n for p in probs)
+    nmin, nmax = min(p.n for p in probs), max(p.n for p in probs)
+    for e in engines:
+        e.close()
+    side = int(round(ntot ** (1.0 / 3.0)))
+    big = Engine.from_problem(problems.turbulent_box(side, 1), precision=args.precision, device=local)
+    big.initialize()
+    big.advance(warmup)
+    torch.cuda.synchronize()
+    bsteps = max(3, min(steps, 30))
+    b_before = big.neighbor_entries() // 2
+    t0 = time.perf_counter()
+    big.advance(bsteps)
+    torch.cuda.synchronize()
+    bwall = time.perf_counter() - t0
+    b_pairs = 0.5 * (b_before + big.neighbor_entries() // 2) * bsteps
+    single = b_pairs / bwall
+    big.close()
+    return {"boxes": nboxes, "n_total": ntot, "n_min": nmin, "n_max": nmax, "steps": steps, "value": value,
+            "unit": UNIT, "wall_s": wall, "energy_error_max_over_boxes": max(errs),
+            "single_large_run": {"n": side ** 3, "value": single, "unit": UNIT, "steps": bsteps},
+            "ensemble_over_single": value / single,
+            "timer": "host wall clock, device synchronised on both sides"}
+
+
+def pipe_peak_tflops(precision, sm_count, sm_mhz):
+    """Nominal non-tensor FMA peak: FP32 128 lanes per SM, FP64 at GB300's
+    nominal 1.25 TFLOP/s for 152 SMs at 2,070 MHz (about 2 FP64 lanes per SM),
+    each lane 2 FLOP per clock, scaled by the device's SM count and max clock."""
+    lanes = 128.0 if precision == "fp32" else 1.25e12 / (152 * 2 * 2070e6)
+    return sm_count * lanes * 2.0 * sm_mhz * 1e6 / 1e12
 
 
 def run_ours(args, ws, rank, local, dist):
@@ -296,10 +446,16 @@ def run_ours(args, ws, rank, local, dist):
     if args.precision == "fp32" and args.fp64_steps > 0:
         e64 = Engine.from_problem(prob, precision="fp64", device=local)
         e64.initialize()
-        e64.step()
-        ms64, pairs64, _, _ = time_steps(e64, args.fp64_steps)
+        for _ in range(args.warmup):
+            e64.step()
+        names64 = ["pair_crk" if args.workload == "crksph" else "pair_fp64"]
+        e64.profile(True)
+        ms64, pairs64, _, prof64 = time_steps(e64, args.fp64_steps, names64)
+        e64.profile(False)
+        n64, t64 = prof64[names64[0]]
         fp64 = {"value": pairs64 / (ms64 / 1e3), "unit": UNIT, "steps": args.fp64_steps,
-                "ms_per_step": ms64 / args.fp64_steps}
+                "ms_per_step": ms64 / args.fp64_steps, "pair_kernel_ms": t64 / max(1, n64),
+                "pairs_per_launch": pairs64 / args.fp64_steps}
         e64.close()
 
     # Energy-conservation error of the mixed-precision run over a long run:
@@ -311,26 +467,15 @@ def run_ours(args, ws, rank, local, dist):
     long_steps = max(done, args.energy_steps)
     long_err = abs(e_end[7] - e0[7]) / abs(e0[7])
 
-    # Optional accuracy comparison: fresh FP32 and FP64 runs of the same
-    # problem for the same number of steps.
+    # Accuracy of the mixed mode against an all-FP64 run of the same problem
+    # at the same physical time, with an FP64 chaos control.
     compare = None
-    if args.fp64_compare_steps > 0 and args.precision == "fp32":
-        runs = {}
-        for prec in ("fp32", "fp64"):
-            e = Engine.from_problem(prob, precision=prec, device=local)
-            e.initialize()
-            c0 = e.conservation()
-            e.advance(args.fp64_compare_steps)
-            c1 = e.conservation()
-            runs[prec] = dict(rho=e.field("massDensity"), eps=e.field("specificThermalEnergy"),
-                              vel=e.field("velocity"), t=e.time, err=abs(c1[7] - c0[7]) / abs(c0[7]))
-            e.close()
-        a, b = runs["fp32"], runs["fp64"]
-        rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
-        compare = {"steps": args.fp64_compare_steps, "time_fp32": a["t"], "time_fp64": b["t"],
-                   "energy_error_fp32": a["err"], "energy_error_fp64": b["err"],
-                   "max_rel_diff_rho": rel(a["rho"], b["rho"]), "max_rel_diff_eps": rel(a["eps"], b["eps"]),
-                   "max_rel_diff_vel": rel(a["vel"], b["vel"])}
+    if args.fp64_compare_steps > 0 and args.precision == "fp32" and args.workload in ("kh", "crksph"):
+        compare = fp32_vs_fp64(args, local)
+
+    ens = None
+    if args.ens_boxes > 0 and args.workload == "kh":
+        ens = ensemble_record(args, local, args.ens_boxes, args.ens_steps)
 
     if rank != 0:
         return
@@ -343,13 +488,25 @@ def run_ours(args, ws, rank, local, dist):
     achieved_gbs = b_pair * pairs_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     tflops = FLOP_PER_PAIR * pairs_per_launch / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else None
     clocks = clk.summary()
-    fp32_peak = 152 * 128 * 2 * (clocks["sm_max_mhz"] or 2070.0) * 1e6 / 1e12
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    pipe_peak = pipe_peak_tflops(args.precision, sm_count, clocks["sm_max_mhz"] or 2070.0)
+    if fp64 is not None and fp64["pair_kernel_ms"] > 0:
+        fp64["pair_kernel_tflops"] = FLOP_PER_PAIR * fp64["pairs_per_launch"] / (fp64["pair_kernel_ms"] / 1e3) / 1e12
+        fp64["fp64_pipe_peak_tflops"] = pipe_peak_tflops("fp64", sm_count, clocks["sm_max_mhz"] or 2070.0)
+        fp64["fp64_pipe_frac"] = fp64["pair_kernel_tflops"] / fp64["fp64_pipe_peak_tflops"]
     cpu = None
     if args.cpu_steps > 0:
         cval, cinfo = cpu_baseline(args)
         cpu = {"value": cval, "unit": UNIT, "cores": cinfo["cores"], "kind": "port",
-               "sample": (f"{cinfo['steps']} steps of the same generator at n1={args.cpu_n1} ({cinfo['n']} nodes), "
-                          f"{cinfo['seconds']:.1f} s, FP64 oracle, OpenMP")}
+               "sample": (f"{cinfo['steps']} steps of the same generator at n1={cinfo['n1']} ({cinfo['n']} nodes), "
+                          f"{cinfo['seconds']:.1f} s, FP64 oracle, OpenMP on every host thread"),
+               "build": "g++ -O3 -fopenmp -ffp-contract=off (no -march=native: the oracle must give the same "
+                        "results on the x86-64 and aarch64 hosts)"}
+        if args.cpu1_steps > 0:
+            v1, i1 = cpu_baseline(args, steps=args.cpu1_steps, n1=args.cpu1_n1, threads=1)
+            cpu["one_core"] = {"value": v1, "unit": UNIT, "cores": i1["cores"],
+                               "sample": (f"{i1['steps']} steps at n1={i1['n1']} ({i1['n']} nodes), "
+                                          f"{i1['seconds']:.1f} s, one thread")}
     line = {
         "metric": METRIC,
         "value": value,
@@ -378,20 +535,24 @@ def run_ours(args, ws, rank, local, dist):
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
         "pair_variant": pair_variant,
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved_gbs / hbm) if achieved_gbs else None,
+        "roofline": {"bound": f"{args.precision}_pipe", "achieved": tflops, "peak": pipe_peak, "unit": "TFLOP/s",
+                     "frac": (tflops / pipe_peak) if tflops else None,
                      "traffic": (TRAFFIC_BYTES_PER_PAIR[args.precision] * pairs_per_launch
                                  if args.precision in TRAFFIC_BYTES_PER_PAIR else None),
-                     "traffic_source": "ncu capture at n1=64 scaled by pairs per launch",
-                     "peak_kind": peak_kind, "kernel": pair_kernel,
-                     "algorithmic_bytes_per_pair": b_pair, "pairs_per_launch": pairs_per_launch,
-                     "avg_launch_ms": avg_ms},
-        "roofline_pipe": {"unit": "TFLOP/s", "achieved": tflops, "flop_per_pair": FLOP_PER_PAIR,
-                          "peak": fp32_peak if args.precision == "fp32" else None,
-                          "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)",
-                          "frac": (tflops / fp32_peak) if (tflops and args.precision == "fp32") else None},
+                     "traffic_source": TRAFFIC_SOURCE,
+                     "peak_kind": (f"nominal non-tensor {args.precision.upper()} FMA rate: {sm_count} SMs (queried) x "
+                                   f"{'128' if args.precision == 'fp32' else '~2'} lanes x 2 FLOP x max SM clock; no "
+                                   "FP32/FP64 pipe figure is in the measured peaks"),
+                     "kernel": pair_kernel, "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs_per_launch,
+                     "avg_launch_ms": avg_ms, "sm_count": sm_count,
+                     "why": ("pairs/s roof = min(pipe / 456 FLOP, HBM / B_pair); the pipe roof is the lower one for "
+                             "this mode, so it binds"),
+                     "hbm": {"achieved": achieved_gbs, "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind,
+                             "frac": (achieved_gbs / hbm) if achieved_gbs else None,
+                             "algorithmic_bytes_per_pair": b_pair}},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in prof.items() if v[0] > 0},
         "fp64_gpu": fp64,
+        "ensemble": ens,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -546,11 +707,17 @@ def main():
     ap.add_argument("--n1", type=int, default=112)
     ap.add_argument("--neighbors", type=int, default=64)
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--energy-steps", type=int, default=1000)
-    ap.add_argument("--fp64-compare-steps", type=int, default=0)
+    ap.add_argument("--fp64-compare-steps", type=int, default=1000,
+                    help="steps of the FP64 run that sets the goal time of the mixed-vs-FP64 comparison (0: skip)")
+    ap.add_argument("--compare-n1", type=int, default=56, help="lattice of the mixed-vs-FP64 comparison")
+    ap.add_argument("--ens-boxes", type=int, default=64, help="boxes of the ensemble sub-record (0: skip)")
+    ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--cpu-n1", type=int, default=56)
     ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--cpu1-n1", type=int, default=28, help="lattice of the one-core CPU sample")
+    ap.add_argument("--cpu1-steps", type=int, default=2)
     args = ap.parse_args()
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":

@@ -114,6 +114,7 @@ def lib():
             "orc_bspline_value": (d, [d]),
             "orc_bspline_grad": (d, [d]),
             "orc_num_threads": (i, []),
+            "orc_set_threads": (i, [i]),
             "orc_set_nodelist_hminratio": (i, [vp, i, d]),
             "orc_sym_eigen": (i, [dp, dp, dp]),
             "orc_smoothing_scale_derivative": (i, [dp, dp, dp]),
@@ -345,6 +346,11 @@ def bspline_grad(eta):
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def set_threads(n):
+    """OpenMP threads of the oracle's loops from now on; returns the count."""
+    return lib().orc_set_threads(int(n))
 
 
 def sym_eigen(a6):

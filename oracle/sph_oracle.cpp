@@ -2266,6 +2266,18 @@ double orc_nperh_lookup(void* h, double wsum) { return static_cast<Problem*>(h)-
 double orc_wsum_lookup(void* h, double nperh) { return static_cast<Problem*>(h)->W.equivalentWsum(nperh); }
 double orc_bspline_value(double eta) { return orc::BSpline3().value(eta, 1.0); }
 double orc_bspline_grad(double eta) { return orc::BSpline3().grad(eta, 1.0); }
+// Thread count of the OpenMP loops that follow (the CPU baseline times the
+// same sample on all host threads and on one).
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n >= 1) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -1,0 +1,109 @@
+"""Parity at the sizes the benchmarks run, not only on small boxes.
+
+The GPU paths that only appear at size — multi-block reductions, 16- and
+32-lane neighbour-search groups in dense cells, grid capping, neighbour list
+capacities near their maximum, the FP32 band test at the Kelvin-Helmholtz
+density contrast, and the pair-kernel variant the autotuner picks for a
+large node set — are compared with the CPU oracle on:
+
+  * the bench's own CPU sample, kelvin_helmholtz(n1=56): 259,308 nodes;
+  * sweep_box(n_side=48, neighbors=128): 110,592 nodes at k = 128;
+  * the largest box of the 256-box ensemble (box 156, 64^3 = 262,144 nodes).
+
+Tolerances as in the small-box parity tests: neighbour sets exact (compared
+as sorted 64-bit keys of (node, neighbour, image code)); FP64 derivative
+fields after one evaluation <= 1e-12 normwise; one full step <= 1e-11;
+mixed mode (autotuned pair variant) derivatives <= 2e-5 normwise.
+"""
+import numpy as np
+import pytest
+
+from spheral_gb300 import problems
+
+from _parity import DERIV_FIELDS, STATE_FIELDS, compare_fields, periodic_axes
+
+pytestmark = pytest.mark.gpu
+
+FP32_DERIVS = ["massDensitySum", "DvDt", "DepsDt", "DvDx", "gradRho", "M", "maxViscousPressure", "DHDt", "Hideal",
+               "massZerothMoment"]
+
+CASES = {
+    "kh_n1_56": lambda: problems.kelvin_helmholtz(n1=56),
+    "sweep_k128": lambda: problems.sweep_box(n_side=48, neighbors=128),
+    "ensemble_box_156": lambda: problems.turbulent_box(problems.ensemble_sizes(256)[156], 4 + 156),
+}
+
+
+def _pair_keys(i, j, im, n):
+    return (i.astype(np.int64) * n + j.astype(np.int64)) * 64 + im.astype(np.int64)
+
+
+def _oracle_ordered_keys(orc, axes, n):
+    """Both orientations of the oracle's unordered pairs, with the image code
+    of (j, i) mirrored on periodic axes (code 1 <-> 2)."""
+    i, j, im = orc.pairs()
+    inv = np.zeros_like(im)
+    for ax in range(3):
+        code = (im >> (2 * ax)) & 3
+        if ax in axes:
+            code = np.where(code != 0, 3 - code, 0)
+        inv |= code << (2 * ax)
+    keys = np.concatenate([_pair_keys(i, j, im, n), _pair_keys(j, i, inv, n)])
+    return np.sort(keys)
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def case(request, native_lib, oracle_mod):
+    # initialised and evaluated once per case; evaluation leaves the state alone
+    p = CASES[request.param]()
+    orc = oracle_mod.Oracle(p)
+    orc.initialize()
+    orc.evaluate_derivatives()
+    return request.param, p, orc
+
+
+def test_neighbor_sets_exact_at_size(case):
+    from spheral_gb300.engine import Engine
+    name, p, orc = case
+    eng = Engine.from_problem(p)
+    eng.initialize()
+    i, j, im = eng.pairs()
+    got = np.sort(_pair_keys(i, j, im, p.n))
+    assert np.all(np.diff(got) > 0), "duplicate neighbour entries"
+    want = _oracle_ordered_keys(orc, periodic_axes(p), p.n)
+    assert got.size == want.size and np.array_equal(got, want), (name, got.size, want.size)
+    assert np.array_equal(eng.field("numNeighbors").astype(np.int64), orc.num_neighbors().astype(np.int64))
+    eng.close()
+
+
+def test_derivatives_and_step_at_size(case, oracle_mod):
+    from spheral_gb300.engine import Engine
+    name, p, orc = case
+    eng = Engine.from_problem(p)
+    eng.initialize()
+    eng.evaluate_derivatives()
+    bad = compare_fields(eng, orc, DERIV_FIELDS, 1e-12)
+    assert not bad, (name, bad)
+    o = oracle_mod.Oracle(p)
+    o.initialize()
+    dg, do = eng.step(), o.step()
+    assert abs(dg - do) <= 1e-12 * do
+    bad = compare_fields(eng, o, STATE_FIELDS, 1e-11)
+    assert not bad, (name, bad)
+    eng.close()
+
+
+def test_mixed_mode_at_size(case, oracle_mod):
+    from spheral_gb300.engine import Engine
+    name, p, orc = case
+    eng = Engine.from_problem(p, precision="fp32")
+    eng.initialize()
+    eng.evaluate_derivatives()   # the autotuner picks the pair variant here, at this size
+    variant, nvariants = eng.pair_variant()
+    assert 0 <= variant < nvariants
+    # the FP32 pre-filter with its guard band still gives the exact neighbour sets
+    i, j, im = eng.pairs()
+    assert np.array_equal(np.sort(_pair_keys(i, j, im, p.n)), _oracle_ordered_keys(orc, periodic_axes(p), p.n))
+    bad = compare_fields(eng, orc, FP32_DERIVS, 2e-5)
+    assert not bad, (name, variant, bad)
+    eng.close()
