@@ -312,6 +312,11 @@ def fp32_vs_fp64(args, local):
     pert = copy.copy(prob)
     pert.pos = np.ascontiguousarray(np.nextafter(prob.pos, np.inf))
     ctrl = run(pert, "fp64", goal)
+    # second control: the FP64 run from initial positions rounded to FP32, a
+    # perturbation of the size the mixed mode's FP32 sweeps make at each step
+    r32 = copy.copy(prob)
+    r32.pos = np.ascontiguousarray(prob.pos.astype(np.float32).astype(np.float64))
+    ctrl32 = run(r32, "fp64", goal)
 
     def diffs(a, b):
         out = {}
@@ -323,19 +328,24 @@ def fp32_vs_fp64(args, local):
         return out
 
     amp = {name: kh_mode_amplitude(r["pos"], r["vel"], prob.mass) for name, r in
-           (("fp64", ref), ("mixed", mixed), ("control", ctrl))}
+           (("fp64", ref), ("mixed", mixed), ("control", ctrl), ("control_fp32_start", ctrl32))}
     amp0 = kh_mode_amplitude(prob.pos, prob.vel, prob.mass)
     return {"workload": ("kelvin_helmholtz_3d_crksph" if args.workload == "crksph" else "kelvin_helmholtz_3d"),
             "n1": args.compare_n1, "n": prob.n, "goal_time": goal, "steps_fp64": ref["steps"],
-            "steps_mixed": mixed["steps"], "steps_control": ctrl["steps"],
-            "time_mixed": mixed["t"], "time_control": ctrl["t"],
+            "steps_mixed": mixed["steps"], "steps_control": ctrl["steps"], "steps_control_fp32_start": ctrl32["steps"],
+            "time_mixed": mixed["t"], "time_control": ctrl["t"], "time_control_fp32_start": ctrl32["t"],
             "energy_error_fp64": ref["err"], "energy_error_mixed": mixed["err"], "energy_error_control": ctrl["err"],
             "mixed_vs_fp64": diffs(mixed, ref), "control_vs_fp64": diffs(ctrl, ref),
+            "control_fp32_start_vs_fp64": diffs(ctrl32, ref),
             "mode_amplitude": dict(amp, initial=amp0),
             "mode_amplitude_rel_diff_mixed": abs(amp["mixed"] - amp["fp64"]) / amp["fp64"],
             "mode_amplitude_rel_diff_control": abs(amp["control"] - amp["fp64"]) / amp["fp64"],
+            "mode_amplitude_rel_diff_control_fp32_start":
+                abs(amp["control_fp32_start"] - amp["fp64"]) / amp["fp64"],
             "control": "FP64 run with every initial position moved by one ulp (numpy nextafter toward +inf)",
-            "wall_s": {"fp64": ref["wall"], "mixed": mixed["wall"], "control": ctrl["wall"]}}
+            "control_fp32_start": "FP64 run with the initial positions rounded to FP32",
+            "wall_s": {"fp64": ref["wall"], "mixed": mixed["wall"], "control": ctrl["wall"],
+                       "control_fp32_start": ctrl32["wall"]}}
 
 
 def ensemble_record(args, local, nboxes, steps, warmup=2):
