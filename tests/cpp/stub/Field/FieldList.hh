@@ -1,0 +1,2 @@
+// stand-in: see spheral_stub.hh
+#include "../spheral_stub.hh"
