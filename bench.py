@@ -413,7 +413,8 @@ def run_ours(args, ws, rank, local, dist):
     for _ in range(args.warmup):
         eng.step()
     e0 = eng.conservation()
-    pair_kernel = "pair_crk" if args.workload == "crksph" else ("pair_fp32" if args.precision == "fp32" else "pair_fp64")
+    f32 = args.precision in ("fp32", "fp32_plain")
+    pair_kernel = "pair_crk" if args.workload == "crksph" else ("pair_fp32" if f32 else "pair_fp64")
     names = [pair_kernel, "rk_corrections", "rk_volume", "gravity", "neighbor_count", "neighbors", "neighbor_items", "sum_density", "density_dt", "dt",
              "energy",
              "gradh", "radix_sort",
@@ -424,9 +425,11 @@ def run_ours(args, ws, rank, local, dist):
         ms, pairs, launches, prof = time_steps(eng, args.steps, names)
     eng.profile(False)
     ms = max_over_ranks(dist, ms)
-    pair_variant = eng.pair_variant()[0] if args.precision == "fp32" else None
+    pair_variant = eng.pair_variant()[0] if f32 else None
     e1 = eng.conservation()
     energy_err = abs(e1[7] - e0[7]) / abs(e0[7])
+    p_scale = float(np.sum(prob.mass * np.linalg.norm(prob.vel, axis=1)))   # sum m |v| of the initial state
+    mom_err = float(np.linalg.norm(e1[1:4] - e0[1:4]) / p_scale) if p_scale > 0 else None
     value = ws * pairs / (ms / 1e3)
     k_mean = 2.0 * pairs / args.steps / n
 
@@ -476,6 +479,7 @@ def run_ours(args, ws, rank, local, dist):
     e_end = eng.conservation()
     long_steps = max(done, args.energy_steps)
     long_err = abs(e_end[7] - e0[7]) / abs(e0[7])
+    long_mom = float(np.linalg.norm(e_end[1:4] - e0[1:4]) / p_scale) if p_scale > 0 else None
 
     # Accuracy of the mixed mode against an all-FP64 run of the same problem
     # at the same physical time, with an FP64 chaos control.
@@ -493,13 +497,14 @@ def run_ours(args, ws, rank, local, dist):
     nl, tl = prof.get(pair_kernel, (0, 0.0))
     avg_ms = tl / max(1, nl)
     pairs_per_launch = pairs / max(1, args.steps)
-    elem = 4 if args.precision == "fp32" else 8
+    elem = 4 if f32 else 8
     b_pair = elem * VALUES_PER_NODE / (k_mean / 2.0) + 6 * elem
     achieved_gbs = b_pair * pairs_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     tflops = FLOP_PER_PAIR * pairs_per_launch / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else None
     clocks = clk.summary()
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    pipe_peak = pipe_peak_tflops(args.precision, sm_count, clocks["sm_max_mhz"] or 2070.0)
+    pipe = "fp32" if f32 else "fp64"
+    pipe_peak = pipe_peak_tflops(pipe, sm_count, clocks["sm_max_mhz"] or 2070.0)
     if fp64 is not None and fp64["pair_kernel_ms"] > 0:
         fp64["pair_kernel_tflops"] = FLOP_PER_PAIR * fp64["pairs_per_launch"] / (fp64["pair_kernel_ms"] / 1e3) / 1e12
         fp64["fp64_pipe_peak_tflops"] = pipe_peak_tflops("fp64", sm_count, clocks["sm_max_mhz"] or 2070.0)
@@ -528,14 +533,19 @@ def run_ours(args, ws, rank, local, dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32" if args.precision == "fp32" else "f64",
-        "precision": ("FP32 pair sweeps on cell-relative positions with compensated sums; FP64 neighbour "
-                      "criterion, integration, compatible energy and tallies") if args.precision == "fp32"
-        else "FP64 throughout",
+        "dtype": "fp32" if f32 else "f64",
+        "precision": {"fp32": ("FP32 pair sweeps on cell-relative positions with compensated sums; FP64 neighbour "
+                               "criterion, integration, compatible energy and tallies"),
+                      "fp32_plain": ("FP32-relative: FP32 pair sweeps on cell-relative positions with plain "
+                                     "(uncompensated) sums; FP64 neighbour criterion, integration and tallies"),
+                      "fp64": "FP64 throughout"}[args.precision],
         "data": "synthetic (seeded generator, no external data)",
         "energy_error": long_err,
         "energy_error_steps": long_steps,
         "energy_error_timed_steps": energy_err,
+        "momentum_error": long_mom,
+        "momentum_error_timed_steps": mom_err,
+        "momentum_error_definition": "|P(t) - P(0)| / sum m |v(0)|",
         "fp32_vs_fp64": compare,
         "config": {"workload": wname, "n": n, "n1": prob.meta.get("n1"), "n2": prob.meta.get("n2"),
                    "mean_neighbors": k_mean, "pairs_per_step": pairs / args.steps,
@@ -545,13 +555,13 @@ def run_ours(args, ws, rank, local, dist):
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
         "pair_variant": pair_variant,
-        "roofline": {"bound": f"{args.precision}_pipe", "achieved": tflops, "peak": pipe_peak, "unit": "TFLOP/s",
+        "roofline": {"bound": f"{pipe}_pipe", "achieved": tflops, "peak": pipe_peak, "unit": "TFLOP/s",
                      "frac": (tflops / pipe_peak) if tflops else None,
-                     "traffic": (TRAFFIC_BYTES_PER_PAIR[args.precision] * pairs_per_launch
-                                 if args.precision in TRAFFIC_BYTES_PER_PAIR else None),
+                     "traffic": (TRAFFIC_BYTES_PER_PAIR[pipe] * pairs_per_launch
+                                 if pipe in TRAFFIC_BYTES_PER_PAIR else None),
                      "traffic_source": TRAFFIC_SOURCE,
-                     "peak_kind": (f"nominal non-tensor {args.precision.upper()} FMA rate: {sm_count} SMs (queried) x "
-                                   f"{'128' if args.precision == 'fp32' else '~2'} lanes x 2 FLOP x max SM clock; no "
+                     "peak_kind": (f"nominal non-tensor {pipe.upper()} FMA rate: {sm_count} SMs (queried) x "
+                                   f"{'128' if f32 else '~2'} lanes x 2 FLOP x max SM clock; no "
                                    "FP32/FP64 pipe figure is in the measured peaks"),
                      "kernel": pair_kernel, "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs_per_launch,
                      "avg_launch_ms": avg_ms, "sm_count": sm_count,
@@ -713,7 +723,7 @@ def main():
     ap.add_argument("--max-steps", type=int, default=100000)
     ap.add_argument("--boxes", type=int, default=256)
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32_plain", "fp64"])
     ap.add_argument("--n1", type=int, default=112)
     ap.add_argument("--neighbors", type=int, default=64)
     ap.add_argument("--e2e-steps", type=int, default=5)

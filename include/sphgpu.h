@@ -44,6 +44,9 @@ extern "C" {
 
 #define SPHGPU_PRECISION_FP64 0   /* every pair sum in FP64                               */
 #define SPHGPU_PRECISION_FP32 1   /* FP32 pair loop on cell-relative positions, compensated sums */
+#define SPHGPU_PRECISION_FP32_PLAIN 2  /* the same FP32 sweeps with plain (uncompensated) FP32 sums: the
+                                          "FP32-relative" mode of the throughput sweep, kept to measure
+                                          what compensation costs and buys (momentum drifts at ~1e-7) */
 
 #define SPHGPU_BOUNDARY_PERIODIC 0
 #define SPHGPU_BOUNDARY_REFLECTING 1

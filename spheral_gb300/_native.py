@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_HERE, "libsphgpu.so")
 
 SPHGPU_OK = 0
 ERRORS = {1: "E_CUDA", 2: "E_ARG", 3: "E_UNSUPPORTED", 4: "E_OVERFLOW", 5: "E_NAN", 6: "E_TIMEOUT", 7: "E_STATE"}
-PRECISION = {"fp64": 0, "fp32": 1}
+PRECISION = {"fp64": 0, "fp32": 1, "fp32_plain": 2}
 BOUNDARY_PERIODIC = 0
 BOUNDARY_REFLECTING = 1
 

@@ -215,7 +215,7 @@ struct sphgpu_ctx {
     p.rkc = rkc32.p ? rkc32.as<float4>() : nullptr;
     return p;
   }
-  bool fp32() const { return cfg.precision == SPHGPU_PRECISION_FP32; }
+  bool fp32() const { return cfg.precision != SPHGPU_PRECISION_FP64; }   // FP32 sweeps (compensated or plain)
   void check() { CUDA_OK(cudaGetLastError()); }
 };
 
@@ -236,7 +236,7 @@ void ensureCapacity(sphgpu_ctx* c, long n) {
   if (c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC) c->hten.ensure(2 * n * sizeof(float4));
   c->vol32.release();
   c->rkc32.release();
-  if (c->cfg.hydro == SPHGPU_HYDRO_CRKSPH && c->cfg.precision == SPHGPU_PRECISION_FP32) {
+  if (c->cfg.hydro == SPHGPU_HYDRO_CRKSPH && c->fp32()) {
     c->vol32.ensure(n * sizeof(float));
     c->rkc32.ensure(4 * n * sizeof(float4));
   }
@@ -329,6 +329,7 @@ void refreshParams(sphgpu_ctx* c) {
   hp.radialOnly = g.radial_only ? 1 : 0;
   hp.crk = g.hydro == SPHGPU_HYDRO_CRKSPH ? 1 : 0;
   hp.rkVolume = g.rk_volume;
+  hp.plainSums = g.precision == SPHGPU_PRECISION_FP32_PLAIN ? 1 : 0;
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
@@ -625,7 +626,7 @@ bool resolveNeighbors(sphgpu_ctx* c) {
 }
 
 void ensurePacc(sphgpu_ctx* c) {
-  const size_t per = c->cfg.precision == SPHGPU_PRECISION_FP32 ? sizeof(float) : sizeof(double);
+  const size_t per = c->fp32() ? sizeof(float) : sizeof(double);
   c->pacc.ensure(std::max<size_t>(1, c->nbSlots()) * 3 * per);
 }
 
@@ -1054,8 +1055,11 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
   auto* c = new sphgpu_ctx();
   try {
     c->cfg = *cfg;
-    if (cfg->precision != SPHGPU_PRECISION_FP64 && cfg->precision != SPHGPU_PRECISION_FP32)
+    if (cfg->precision != SPHGPU_PRECISION_FP64 && cfg->precision != SPHGPU_PRECISION_FP32 &&
+        cfg->precision != SPHGPU_PRECISION_FP32_PLAIN)
       throw Error(SPHGPU_E_ARG, "unknown precision mode");
+    if (cfg->precision == SPHGPU_PRECISION_FP32_PLAIN && cfg->hydro == SPHGPU_HYDRO_CRKSPH)
+      throw Error(SPHGPU_E_UNSUPPORTED, "the plain-sum FP32 mode covers the SPH sweeps");
     if (cfg->viscosity != SPHGPU_VISCOSITY_MONAGHAN_GINGOLD && cfg->viscosity != SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown artificial viscosity");
     if (cfg->viscosity == SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD && !(cfg->eta_fold_frac > 0.0))

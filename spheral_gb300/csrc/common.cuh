@@ -56,6 +56,7 @@ struct HydroParams {
   int radialOnly;                // ASPH radialOnly
   int crk;                       // CRKSPH (LinearOrder reproducing kernels) instead of SPH
   int rkVolume;                  // RKVolumeType: 0 m/rho, 1 RKSumVolume, 4 HVolume
+  int plainSums;                 // FP32 sweeps add plainly instead of compensated (FP32_PLAIN mode)
 };
 
 // safeInvVar (src/Utilities/safeInv.hh): sgn(x) / max(fuzz, |x|), fuzz 1e-30

@@ -18,6 +18,11 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
   s = t;
 }
 __device__ __forceinline__ double kahanValue(float s, float c) { return (double)s - (double)c; }
+// The same accumulation, or a plain FP32 sum when `plain` (uniform per launch).
+__device__ __forceinline__ void sumAdd(float& s, float& c, float x, int plain) {
+  if (plain) s = __fadd_rn(s, x);
+  else kahanAdd(s, c, x);
+}
 
 // Velocity of a mirror image: the components along the mirrored axes flip
 // (mir: per-axis bits of the entry's cell-offset code that cross a wall).

@@ -281,16 +281,16 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     const float ddy = __fadd_rn(__fmul_rn(ci_, gwiy), __fmul_rn(cj_, gwjy));
     const float ddz = __fadd_rn(__fmul_rn(ci_, gwiz), __fmul_rn(cj_, gwjz));
     const float pax = __fmul_rn(-mj, ddx), pay = __fmul_rn(-mj, ddy), paz = __fmul_rn(-mj, ddz);
-    kahanAdd(sdx, cdx, pax);
-    kahanAdd(sdy, cdy, pay);
-    kahanAdd(sdz, cdz, paz);
+    sumAdd(sdx, cdx, pax, hp.plainSums);
+    sumAdd(sdy, cdy, pay, hp.plainSums);
+    sumAdd(sdz, cdz, paz, hp.plainSums);
     if (COMPAT) {
       pacc[3 * k] = pax;
       pacc[3 * k + 1] = pay;
       pacc[3 * k + 2] = paz;
     }
     const float vg = vx * gwix + vy * gwiy + vz * gwiz;
-    kahanAdd(se, ce, mj * (Prhoi + qai) * vg);
+    sumAdd(se, ce, mj * (Prhoi + qai) * vg, hp.plainSums);
     const float mvx = mj * vx, mvy = mj * vy, mvz = mj * vz;
     D[0] -= mvx * gwix; D[1] -= mvx * gwiy; D[2] -= mvx * gwiz;
     D[3] -= mvy * gwix; D[4] -= mvy * gwiy; D[5] -= mvy * gwiz;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
     if (eta < extent) {
       const int i0 = 3 * min(N1, (int)(eta * invStep));
       const float w = Hdj * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
-      kahanAdd(s, c, ((multi ? list[j] == li : true) ? P.velm[j].w : mi) * w);
+      sumAdd(s, c, ((multi ? list[j] == li : true) ? P.velm[j].w : mi) * w, hp.plainSums);
     }
   }
   const double a = F.f[F_HINV][i];
@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
       if (eta < extent) {
         const int i0 = 3 * min(N1, (int)(eta * invStep));
         const float w = Hdj * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
-        kahanAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w);
+        sumAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w, hp.plainSums);
       }
       float vxj = vj.x, vyj = vj.y, vzj = vj.z;
       mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
@@ -571,8 +571,8 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
     const float eta = TENSOR ? sqrtf(eta2Sym32(hi0, hi1, rx, ry, rz)) : ai * sqrtf(rx * rx + ry * ry + rz * rz);
     float w, gr;
     lookupPacked(ta, tb, N1, invStep, eta, extent, w, gr);
-    kahanAdd(ws, wc, w);
-    kahanAdd(gs, gc, eta * gr);
+    sumAdd(ws, wc, w, hp.plainSums);
+    sumAdd(gs, gc, eta * gr, hp.plainSums);
   }
   // Omega = -sum eta dW/deta / (3 (sum W + W0)) (Hdet cancels), in FP32 from
   // the compensated sums

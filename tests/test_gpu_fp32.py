@@ -100,3 +100,23 @@ def test_fp32_step_dt_close(native_lib, oracle_mod, case):
         dg = eng.step()
         do = orc.step()
         assert abs(dg - do) <= 1e-5 * do, (dg, do)
+
+
+@pytest.mark.parametrize("case", ["periodic", "kh"])
+def test_fp32_plain_sums_close(native_lib, oracle_mod, case):
+    # the FP32-relative mode of the throughput sweep (SPHGPU_PRECISION_FP32_PLAIN):
+    # the same FP32 sweeps with plain sums, same neighbour sets, derivatives
+    # within the mixed mode's 2e-5 of the FP64 oracle
+    from spheral_gb300.engine import Engine
+    p = CASES[case]()
+    eng = Engine.from_problem(p, precision="fp32_plain")
+    orc = oracle_mod.Oracle(p)
+    eng.initialize()
+    orc.initialize()
+    i, j, im = eng.pairs()
+    assert set(zip(i.tolist(), j.tolist(), im.tolist())) == ordered_pairs_from_oracle(orc, periodic_axes(p))
+    eng.evaluate_derivatives()
+    orc.evaluate_derivatives()
+    bad = compare_fields(eng, orc, FP32_DERIVS, 2e-5)
+    assert not bad, bad
+    eng.advance(3)
