@@ -363,6 +363,51 @@ int sphgpu_synchronize(sphgpu_handle h);
 int sphgpu_conservation_noalloc(const double* mass, const double* vel, const double* eps, const double* pot, long n,
                                 double* out, void* stream);
 
+/* Domain decomposition (the halo exchange of a single run spread over
+ * several handles, one per domain, each on its own GPU or sharing one).
+ * A domain's handle holds its owned nodes first (caller indices
+ * 0..n-n_ghost-1) and then n_ghost halo copies of other domains' nodes that
+ * lie within a kernel support of it; the caller builds that node set (for
+ * instance from sphgpu_checkpoint images, whose rows sphgpu_image_layout
+ * describes) and registers it with sphgpu_set_domain.  Halo copies are read
+ * as neighbours by every sweep, take no part in the time-step vote, and are
+ * refreshed during sphgpu_step through `fn`, called once per step at each of
+ * these points, in this order, on every domain:
+ *   SPHGPU_EXCHANGE_DENSITY  after the start-of-step density sum: mass density
+ *   SPHGPU_EXCHANGE_DT       *dt holds this domain's vote; fn stores the
+ *                            smallest vote of all domains there
+ *   SPHGPU_EXCHANGE_OMEGA    after the mid-step grad-h correction (when on)
+ *   SPHGPU_EXCHANGE_DERIVS   after the mid-step derivatives: DvDt (3), DepsDt
+ * At a row point fn gathers, with sphgpu_exchange_get, the rows of the owned
+ * nodes other domains hold as halo copies, sends them, and stores the rows
+ * of its own halo (in halo caller order) with sphgpu_exchange_put.  fn
+ * returns 0, or non-zero to fail the step with SPHGPU_E_STATE.  Everything
+ * else a halo copy needs during the step it computes itself, bitwise as its
+ * owner does, from the rows it started the step with.  n_ghost = 0 and
+ * fn = NULL end the decomposition.  Gravity and CRKSPH are not covered
+ * (SPHGPU_E_UNSUPPORTED).
+ * Replaces: DistributedBoundary (src/Distributed/DistributedBoundary.cc:
+ * setControlAndGhostNodes, applyGhostBoundaries, finalizeGhostBoundary) and
+ * the global time-step minimum of Integrator::selectDt
+ * (src/Integrator/Integrator.cc:152-153). */
+#define SPHGPU_EXCHANGE_DENSITY 1
+#define SPHGPU_EXCHANGE_DT 2
+#define SPHGPU_EXCHANGE_OMEGA 3
+#define SPHGPU_EXCHANGE_DERIVS 4
+typedef int (*sphgpu_exchange_fn)(void* user, int point, double* dt);
+int sphgpu_set_domain(sphgpu_handle h, long n_ghost, sphgpu_exchange_fn fn, void* user);
+/* Values per node exchanged at `point` (0 for SPHGPU_EXCHANGE_DT). */
+int sphgpu_exchange_width(sphgpu_handle h, int point, int* width);
+/* Rows (width values each) of the owned nodes idx[0..count) into out. */
+int sphgpu_exchange_get(sphgpu_handle h, int point, const int* idx, long count, double* out);
+/* Rows of the n_ghost halo copies, in halo caller order, from in. */
+int sphgpu_exchange_put(sphgpu_handle h, int point, const double* in);
+/* Layout of a checkpoint image: header bytes, then nrows rows of n doubles
+ * (one per carried field, internal node order), then n ints of caller index
+ * and n ints of NodeList id.  *row (if field is not NULL) is the first row of
+ * the named field (e.g. "position": rows row..row+2 hold x, y, z). */
+int sphgpu_image_layout(sphgpu_handle h, const char* field, size_t* header_bytes, int* row, int* nrows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,7 +124,16 @@ SIGNATURES = {
     "sphgpu_timer_start": (_i, [_vp]),
     "sphgpu_timer_stop": (_i, [_vp, _dp]),
     "sphgpu_neighbor_count": (_i, [_vp, _lp]),
+    "sphgpu_set_domain": (_i, [_vp, _l, _vp, _vp]),
+    "sphgpu_exchange_width": (_i, [_vp, _i, _ip]),
+    "sphgpu_exchange_get": (_i, [_vp, _i, _ip, _l, _dp]),
+    "sphgpu_exchange_put": (_i, [_vp, _i, _dp]),
+    "sphgpu_image_layout": (_i, [_vp, _cp, ctypes.POINTER(ctypes.c_size_t), _ip, _ip]),
 }
+
+# Exchange points of sphgpu_set_domain and the callback type.
+EXCHANGE_DENSITY, EXCHANGE_DT, EXCHANGE_OMEGA, EXCHANGE_DERIVS = 1, 2, 3, 4
+EXCHANGE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double))
 
 
 def lib():

@@ -141,6 +141,12 @@ struct sphgpu_ctx {
   DBuf vol32, rkc32;         // CRKSPH, mixed mode: FP32 mirrors of the RK volume and corrections
   double kernelExtent = 2.0; // extent of the configured base kernel (BSpline 2, NBSpline (order+1)/2)
   DBuf stage;                // host <-> device staging for caller-order transfers
+  // domain decomposition: the last nGhost caller indices are halo copies of
+  // other domains' nodes; xfn is called at the step's exchange points
+  long nGhost = 0;
+  sphgpu_exchange_fn xfn = nullptr;
+  void* xuser = nullptr;
+  DBuf xstage, xidx;         // exchange rows and caller indices
   DBuf v12;                  // half-step velocities + DepsDt0 of the mixed-mode energy sweep
   int cur = 0;
   long cap = 0;
@@ -750,8 +756,16 @@ void evalDerivs(sphgpu_ctx* c) {
 
 // Integrator::selectDt (src/Integrator/Integrator.cc:116-169).
 // fusedDone: the mixed-mode density sweep already left the dt vote in small[0..1].
+// Halo copies take no part in the dt vote: the vote kernels read the caller
+// index of each sorted node (the current bank) and the owned count.
+void setGhostParams(sphgpu_ctx* c) {
+  c->hp.ghostOrig = c->nGhost > 0 ? c->origp() : nullptr;
+  c->hp.nOwn = c->n - c->nGhost;
+}
+
 double packageDt(sphgpu_ctx* c, int* reason, bool fusedDone = false) {
   Scope sc(c->prof, "dt");
+  setGhostParams(c);
   const long nb = (c->n + 127) / 128;
   c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
   double* d = c->small.as<double>();
@@ -805,6 +819,17 @@ void checkState(sphgpu_ctx* c, const char* where) {
   c->boundsValid = true;
 }
 
+// Domain decomposition (DistributedBoundary::applyGhostBoundaries,
+// src/Distributed/DistributedBoundary.cc): the caller's exchange function
+// refreshes the halo copies at the points of the step where a neighbour sum
+// has changed a field they are read for.  Every domain reaches the same
+// points in the same order once per step.
+void exchangePoint(sphgpu_ctx* c, int point, double* dt = nullptr) {
+  if (!c->xfn) return;
+  const int rc = c->xfn(c->xuser, point, dt);
+  if (rc != 0) throw Error(SPHGPU_E_STATE, "the domain exchange function failed at point " + std::to_string(point));
+}
+
 // CheapSynchronousRK2::step (src/Integrator/CheapSynchronousRK2.cc:40-132).
 double step(sphgpu_ctx* c, double maxTime) {
   requireState(c);
@@ -825,6 +850,7 @@ double step(sphgpu_ctx* c, double maxTime) {
         Scope sc(c->prof, "density_dt");
         const long nb = (c->n + 127) / 128;
         c->scratch.ensure(std::max<size_t>(2 * nb * sizeof(double), 7 * sizeof(double) * 4096));
+        setGhostParams(c);
         launchDensityDtFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
                             c->maxNperh(), c->scratch.as<double>(), c->small.as<double>(), c->stream, &c->lc);
         c->check();
@@ -844,6 +870,11 @@ double step(sphgpu_ctx* c, double maxTime) {
     preStep();
     dt = selectDt(c, std::min(c->cfg.dt_min, maxTime - t), std::min(c->cfg.dt_max, maxTime - t), fused);
   }
+  if (c->xfn) {
+    exchangePoint(c, SPHGPU_EXCHANGE_DENSITY);   // the halo's summed densities
+    exchangePoint(c, SPHGPU_EXCHANGE_DT, &dt);   // the smallest vote of all domains
+    if (!(dt > 0.0) || !std::isfinite(dt)) throw Error(SPHGPU_E_STATE, "the domain exchange returned a bad dt");
+  }
   const double hdt = 0.5 * dt;
   {
     Scope sc(c->prof, "update");   // the half-step update also saves state0
@@ -856,7 +887,9 @@ double step(sphgpu_ctx* c, double maxTime) {
   copyQGradient(c);                                  // postStateUpdate (mid): the Q's DvDx
   if (c->cfg.gradh_correction) gradh(c);             // postStateUpdate (mid)
   c->omegaStale = false;
+  if (c->cfg.gradh_correction) exchangePoint(c, SPHGPU_EXCHANGE_OMEGA);
   evalDerivs(c);                                     // derivs.Zero(); evaluateDerivatives(t + dt/2)
+  exchangePoint(c, SPHGPU_EXCHANGE_DERIVS);          // the halo's accelerations and energy rates
   {
     Scope sc(c->prof, "update");
     launchRestoreState0(c->F, c->n, c->hp.asph != 0, c->hp.crk != 0, c->stream, &c->lc);
@@ -960,6 +993,7 @@ int failStd(sphgpu_ctx* c, const std::exception& e) {
 #define API_BEGIN(h) \
   if (!(h)) return SPHGPU_E_ARG; \
   try {
+#define API_RETURN_OK(h) return SPHGPU_OK
 #define API_END(h)                        \
   }                                       \
   catch (const Error& e) {                \
@@ -1737,6 +1771,95 @@ int sphgpu_get_pairs(sphgpu_handle c, int* i_out, int* j_out, int* image, long* 
         image[k] = code;
       }
     }
+  API_END(c)
+}
+
+namespace {
+ExchangeFields exchangeFields(int point) {
+  ExchangeFields ef{};
+  if (point == SPHGPU_EXCHANGE_DENSITY) {
+    ef.w = 1; ef.mirror = 1; ef.ids[0] = F_RHO;
+  } else if (point == SPHGPU_EXCHANGE_OMEGA) {
+    ef.w = 1; ef.mirror = 2; ef.ids[0] = F_OMEGA;
+  } else if (point == SPHGPU_EXCHANGE_DERIVS) {
+    ef.w = 4; ef.mirror = 0;
+    ef.ids[0] = F_DVDT_X; ef.ids[1] = F_DVDT_Y; ef.ids[2] = F_DVDT_Z; ef.ids[3] = F_DEPSDT;
+  } else {
+    throw Error(SPHGPU_E_ARG, "not a row exchange point");
+  }
+  return ef;
+}
+}  // namespace
+
+int sphgpu_set_domain(sphgpu_handle c, long n_ghost, sphgpu_exchange_fn fn, void* user) {
+  API_BEGIN(c)
+  requireState(c);
+  if (n_ghost < 0 || n_ghost >= c->n) throw Error(SPHGPU_E_ARG, "halo count out of range");
+  if (n_ghost > 0 && !fn) throw Error(SPHGPU_E_ARG, "a halo needs an exchange function");
+  if (fn && (c->cfg.gravity || c->hp.crk))
+    throw Error(SPHGPU_E_UNSUPPORTED, "domain decomposition covers the SPH hydro step without gravity");
+  c->nGhost = n_ghost;
+  c->xfn = fn;
+  c->xuser = user;
+  API_END(c)
+}
+
+int sphgpu_exchange_width(sphgpu_handle c, int point, int* width) {
+  API_BEGIN(c)
+  if (!width) throw Error(SPHGPU_E_ARG, "null width");
+  *width = point == SPHGPU_EXCHANGE_DT ? 0 : exchangeFields(point).w;
+  API_END(c)
+}
+
+int sphgpu_exchange_get(sphgpu_handle c, int point, const int* idx, long count, double* out) {
+  API_BEGIN(c)
+  requireState(c);
+  const ExchangeFields ef = exchangeFields(point);
+  if (count < 0 || (count > 0 && (!idx || !out))) throw Error(SPHGPU_E_ARG, "bad exchange rows");
+  if (count == 0) API_RETURN_OK(c);
+  for (long r = 0; r < count; ++r)
+    if (idx[r] < 0 || idx[r] >= c->n - c->nGhost) throw Error(SPHGPU_E_ARG, "exchange row is not an owned node");
+  c->xidx.ensure((size_t)count * sizeof(int));
+  c->xstage.ensure((size_t)count * ef.w * sizeof(double));
+  CUDA_OK(cudaMemcpyAsync(c->xidx.p, idx, (size_t)count * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  launchExchangeGet(c->F, invOrder(c), c->xidx.as<int>(), count, ef, c->xstage.as<double>(), c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaMemcpyAsync(out, c->xstage.p, (size_t)count * ef.w * sizeof(double), cudaMemcpyDeviceToHost,
+                          c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_exchange_put(sphgpu_handle c, int point, const double* in) {
+  API_BEGIN(c)
+  requireState(c);
+  const ExchangeFields ef = exchangeFields(point);
+  const long count = c->nGhost;
+  if (count == 0) API_RETURN_OK(c);
+  if (!in) throw Error(SPHGPU_E_ARG, "null exchange rows");
+  c->xstage.ensure((size_t)count * ef.w * sizeof(double));
+  CUDA_OK(cudaMemcpyAsync(c->xstage.p, in, (size_t)count * ef.w * sizeof(double), cudaMemcpyHostToDevice,
+                          c->stream));
+  Fields32 m32{};
+  if (c->fp32()) m32 = c->f32();
+  launchExchangePut(c->F, m32, invOrder(c), c->n - count, count, ef, c->xstage.as<double>(), c->stream, &c->lc);
+  c->check();
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  API_END(c)
+}
+
+int sphgpu_image_layout(sphgpu_handle c, const char* field, size_t* header_bytes, int* row, int* nrows) {
+  API_BEGIN(c)
+  if (header_bytes) *header_bytes = sizeof(CheckpointHeader);
+  if (nrows) *nrows = F_NUM_PERMUTED;
+  if (row) {
+    if (!field) throw Error(SPHGPU_E_ARG, "null field name");
+    FieldSpec fs;
+    bool isH, isNumNb;
+    if (!fieldSpec(field, fs, isH, isNumNb, c->hp.asph != 0, c->hp.crk != 0) || isNumNb || fs.first >= F_NUM_PERMUTED)
+      throw Error(SPHGPU_E_ARG, std::string("no image row for ") + field);
+    *row = fs.first;
+  }
   API_END(c)
 }
 

@@ -57,7 +57,16 @@ struct HydroParams {
   int crk;                       // CRKSPH (LinearOrder reproducing kernels) instead of SPH
   int rkVolume;                  // RKVolumeType: 0 m/rho, 1 RKSumVolume, 4 HVolume
   int plainSums;                 // FP32 sweeps add plainly instead of compensated (FP32_PLAIN mode)
+  // Domain decomposition: caller index of every (sorted) node and the count
+  // of owned nodes; caller indices >= nOwn are halo copies of another
+  // domain's nodes and take no part in the time-step vote.  Null without a
+  // decomposition.  Set by the host just before the dt launches.
+  const int* ghostOrig;
+  long nOwn;
 };
+__device__ __forceinline__ bool isGhost(const HydroParams& hp, long i) {
+  return hp.ghostOrig != nullptr && hp.ghostOrig[i] >= hp.nOwn;
+}
 
 // safeInvVar (src/Utilities/safeInv.hh): sgn(x) / max(fuzz, |x|), fuzz 1e-30
 __device__ __forceinline__ double safeInvVarD(double x) { return (x < 0.0 ? -1.0 : 1.0) / fmax(1.0e-30, fabs(x)); }

@@ -770,7 +770,7 @@ __global__ void __launch_bounds__(128) dtKernel(Fields F, const int* __restrict_
   const double tiny = DBL_EPSILON;
   double best = DBL_MAX;
   int reason = -1;
-  if (i < n) {
+  if (i < n && !isGhost(hp, i)) {
     int hc[3];
     unpackCell(nl.cell[i], hc);
     const NodeListParams L = hp.lists[list[i]];
@@ -1169,6 +1169,33 @@ __global__ void gatherOutKernel(Fields F, const int* __restrict__ orig, double* 
   const long o = (long)orig[k] * stride;
   for (int c = 0; c < ncomp; ++c) stage[o + c] = F.f[first + c][k];
 }
+// Domain-decomposition exchange: rows of `w` values of the fields ids[0..w)
+// for caller indices idx (get), or for the halo nodes, caller indices
+// nOwn..nOwn+count-1 in order (put).  inv: internal index of each caller index.
+__global__ void exchangeGetKernel(Fields F, const int* __restrict__ inv, const int* __restrict__ idx, long count,
+                                  ExchangeFields ef, double* __restrict__ out) {
+  const long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (r >= count) return;
+  const long k = inv[idx[r]];
+  for (int c = 0; c < ef.w; ++c) out[r * ef.w + c] = F.f[ef.ids[c]][k];
+}
+__global__ void exchangePutKernel(Fields F, Fields32 P, const int* __restrict__ inv, long nOwn, long count,
+                                  ExchangeFields ef, const double* __restrict__ in) {
+  const long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (r >= count) return;
+  const long k = inv[nOwn + r];
+  for (int c = 0; c < ef.w; ++c) F.f[ef.ids[c]][k] = in[r * ef.w + c];
+  // the FP32 mirror entries the sweeps read next, written as their own
+  // kernels write them for owned nodes
+  if (P.thermo) {
+    if (ef.mirror == 1) P.thermo[k].x = (float)F.f[F_RHO][k];
+    if (ef.mirror == 2) {
+      const float om = (float)F.f[F_OMEGA][k];
+      P.thermo[k].w = om / (om * om + 1.0e-30f);
+    }
+  }
+}
+
 __global__ void scatterInKernel(Fields F, const int* __restrict__ orig, const double* __restrict__ stage, int first,
                                 int ncomp, int stride, long n) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -1397,6 +1424,19 @@ void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nS
 }
 void launchCheckState(Fields F, long n, int* dFlag, cudaStream_t s, LaunchCounter* lc) {
   checkStateKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, dFlag);
+  lc->add(1);
+}
+
+void launchExchangeGet(Fields F, const int* inv, const int* idx, long count, ExchangeFields ef, double* out,
+                       cudaStream_t s, LaunchCounter* lc) {
+  if (count <= 0) return;
+  exchangeGetKernel<<<gridFor(count, 256), 256, 0, s>>>(F, inv, idx, count, ef, out);
+  lc->add(1);
+}
+void launchExchangePut(Fields F, Fields32 P, const int* inv, long nOwn, long count, ExchangeFields ef,
+                       const double* in, cudaStream_t s, LaunchCounter* lc) {
+  if (count <= 0) return;
+  exchangePutKernel<<<gridFor(count, 256), 256, 0, s>>>(F, P, inv, nOwn, count, ef, in);
   lc->add(1);
 }
 

@@ -509,7 +509,8 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     }
     const float pairDt = bestPair / (float)maxNperh;
     if (pairDt < bestf) { bestf = pairDt; reason = 5; }
-    best = (double)bestf;
+    best = isGhost(hp, i) ? DBL_MAX : (double)bestf;   // halo copies do not vote
+    if (isGhost(hp, i)) reason = -1;
   }
   sv[threadIdx.x] = best;
   sr[threadIdx.x] = reason;
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(128) dtKernel32(Fields F, Fields32 P, const in
   const double tiny = DBL_EPSILON;
   double best = DBL_MAX;
   int reason = -1;
-  if (i < n) {
+  if (i < n && !isGhost(hp, i)) {
     int ci[3];
     unpackCell(P.cell[i], ci);
     const uint32_t mm = mirrorMask(g, ci);

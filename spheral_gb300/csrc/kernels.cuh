@@ -129,6 +129,16 @@ void launchEnforce(Fields F, long n, Grid g, bool tensor, cudaStream_t s, Launch
 // out[0..7] conservation totals
 void launchConservation(Fields F, long n, bool gravity, double* dScratch, int nScratch, double* dOut, cudaStream_t s,
                         LaunchCounter* lc);
+// Domain-decomposition exchange rows: w field ids; mirror 1 refreshes the FP32
+// density mirror, 2 the FP32 grad-h mirror of the halo nodes after a put.
+struct ExchangeFields {
+  int w, mirror;
+  int ids[8];
+};
+void launchExchangeGet(Fields F, const int* inv, const int* idx, long count, ExchangeFields ef, double* out,
+                       cudaStream_t s, LaunchCounter* lc);
+void launchExchangePut(Fields F, Fields32 P, const int* inv, long nOwn, long count, ExchangeFields ef,
+                       const double* in, cudaStream_t s, LaunchCounter* lc);
 // caller-order transfers through a device staging buffer (stride doubles per node)
 void launchGatherOut(Fields F, const int* orig, double* stage, int first, int ncomp, int stride, long n,
                      cudaStream_t s, LaunchCounter* lc);

@@ -147,7 +147,11 @@ class Engine:
 
     def step(self, max_time=1.0e300):
         d = ctypes.c_double()
-        self._chk(self.L.sphgpu_step(self.h, max_time, ctypes.byref(d)))
+        rc = self.L.sphgpu_step(self.h, max_time, ctypes.byref(d))
+        if rc != N.SPHGPU_OK and getattr(self, "_xerr", None) is not None:
+            err, self._xerr = self._xerr, None
+            raise N.SphGpuError(rc, "the domain exchange failed: %r" % (err,)) from err
+        self._chk(rc)
         return d.value
 
     def advance(self, nsteps, max_time=1.0e300):
@@ -261,6 +265,59 @@ class Engine:
     def download_state(self, pos=None, vel=None, rho=None, eps=None, H=None):
         ptr = lambda a: None if a is None else N.dptr(a)
         self._chk(self.L.sphgpu_download_state(self.h, ptr(pos), ptr(vel), ptr(rho), ptr(eps), ptr(H)))
+
+    # -- domain decomposition -------------------------------------------------
+    def set_domain(self, n_ghost, exchange=None):
+        """Mark the last n_ghost nodes as halo copies and register
+        exchange(point, dt) -> new dt or None, called inside step() at each
+        exchange point (see sphgpu_set_domain).  An exception in exchange
+        fails the step."""
+        if exchange is None:
+            self._xcb = None
+            self._chk(self.L.sphgpu_set_domain(self.h, int(n_ghost), None, None))
+            return
+
+        def cb(user, point, dtp):
+            try:
+                if point == N.EXCHANGE_DT:
+                    dtp[0] = float(exchange(point, float(dtp[0])))
+                else:
+                    exchange(point, None)
+                return 0
+            except Exception as e:   # reported through the step's status
+                self._xerr = e
+                return 1
+
+        self._xerr = None
+        self._xcb = N.EXCHANGE_FN(cb)   # kept alive while registered
+        self._chk(self.L.sphgpu_set_domain(self.h, int(n_ghost), ctypes.cast(self._xcb, ctypes.c_void_p), None))
+
+    def exchange_width(self, point):
+        w = ctypes.c_int()
+        self._chk(self.L.sphgpu_exchange_width(self.h, int(point), ctypes.byref(w)))
+        return w.value
+
+    def exchange_get(self, point, idx):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        w = self.exchange_width(point)
+        out = np.zeros((len(idx), w))
+        if len(idx):
+            self._chk(self.L.sphgpu_exchange_get(self.h, int(point), N.iptr(idx), len(idx), N.dptr(out)))
+        return out
+
+    def exchange_put(self, point, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        self._chk(self.L.sphgpu_exchange_put(self.h, int(point), N.dptr(rows)))
+
+    def image_layout(self, field=None):
+        """(header bytes, first row of `field` or None, number of rows) of a
+        checkpoint image."""
+        hb = ctypes.c_size_t()
+        row = ctypes.c_int(-1)
+        nrows = ctypes.c_int()
+        self._chk(self.L.sphgpu_image_layout(self.h, field.encode() if field else None, ctypes.byref(hb),
+                                             ctypes.byref(row) if field else None, ctypes.byref(nrows)))
+        return hb.value, (row.value if field else None), nrows.value
 
     def launch_count(self):
         n = ctypes.c_long()
