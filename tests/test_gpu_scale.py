@@ -85,8 +85,15 @@ def test_derivatives_and_step_at_size(case, oracle_mod):
     eng = Engine.from_problem(p)
     eng.initialize()
     eng.evaluate_derivatives()
-    bad = compare_fields(eng, orc, DERIV_FIELDS, 1e-12)
+    # on an unjittered lattice (the ensemble's boxes) the first moment cancels
+    # to rounding noise: it is compared against the zeroth moment's scale
+    lattice = name.startswith("ensemble")
+    fields = [f for f in DERIV_FIELDS if not (lattice and f == "massFirstMoment")]
+    bad = compare_fields(eng, orc, fields, 1e-12)
     assert not bad, (name, bad)
+    if lattice:
+        m1 = np.abs(eng.field("massFirstMoment") - orc.field("massFirstMoment"))
+        assert np.max(m1) <= 1e-12 * np.max(np.abs(orc.field("massZerothMoment")))
     eng.close()
     # the step from fresh handles on both sides: CheapSynchronousRK2's first
     # half-step uses the derivatives the state already holds
