@@ -65,6 +65,10 @@ extern "C" {
 #define SPHGPU_SMOOTHING_SPH 0           /* SPHSmoothingScale: isotropic H = I/h                  */
 #define SPHGPU_SMOOTHING_ASPH_CLASSIC 1  /* ASPHClassicSmoothingScale (SPH(..., ASPH="CLASSIC")):
                                             symmetric-tensor H                                  */
+#define SPHGPU_SMOOTHING_ASPH 2          /* ASPHSmoothingScale (SPH(..., ASPH=True)) with fix_shape or
+                                            radial_only: H integrated with DH/Dt in the step
+                                            (IncrementASPHHtensor) and reset from the zeroth moment
+                                            at its end; the Voronoi-shaped form is not built      */
 
 /* Base kernel of the TableKernel (cfg.kernel, cfg.kernel_order). */
 #define SPHGPU_KERNEL_BSPLINE 0   /* BSplineKernel (cubic, extent 2), the default            */

@@ -1229,6 +1229,12 @@ struct Problem {
         DxDt[i] = vi;
       }
       if (cfg.smoothingScale == 1) { asphClassicFinalize(i, a, DvDxi); continue; }
+      if (cfg.smoothingScale == 2) {
+        // ASPHSmoothingScale::evaluateDerivatives (ASPHSmoothingScale.cc:105-149):
+        // only the tensor rate; the ideal H comes at the end of the step
+        DHDt[i] = smoothingScaleDerivative3(H[i], DvDxi);
+        continue;
+      }
       // SPHSmoothingScale finalize
       const auto& L = lists[list[i]];
       double m0 = rootnu3(std::max(0.0, a.m0));
@@ -1661,6 +1667,78 @@ struct Problem {
   // the previous derivatives (CheapSynchronousRK2.cc:75-80); otherwise the full
   // update from state0 (CheapSynchronousRK2.cc:105-110).
   //----------------------------------------------------------------------------
+  // The eigenvalue limits of the ASPH smoothing scales: every eigenvalue of
+  // H within [1/hmax, min(1/hmin, max(1/hmax, smallest)/hminratio)]
+  // (constructSymTensorWithBoundedDiagonal + rotationalTransform,
+  // IncrementASPHHtensor.cc:88-92, ASPHSmoothingScale.cc:355-359).
+  static ST limitASPH(const ST& h, const NodeListParams& L) {
+    const EigS he = eigenVectorsS(h);
+    const double hminInv = 1.0 / L.hmin, hmaxInv = 1.0 / L.hmax;
+    const double hminEffInv =
+        std::min(hminInv, std::max(hmaxInv, std::min(he.val[0], std::min(he.val[1], he.val[2]))) / L.hminratio);
+    double d[3];
+    for (int k = 0; k < 3; ++k) d[k] = std::max(hmaxInv, std::min(hminEffInv, he.val[k]));
+    return fromEigen(d, he.vec);
+  }
+  // IncrementASPHHtensor::update (src/SmoothingScale/IncrementASPHHtensor.cc:37-100):
+  // fixShape scales H by the cube root of the determinant ratio of the plain
+  // increment; radialOnly increments only the radial diagonal element in the
+  // frame whose first axis is the radial direction (about the origin, at the
+  // position before this update); otherwise H += m DH/Dt; then the limits.
+  ST incrementASPHHtensor(const ST& Hi, const ST& D, double m, const V3& xi, const NodeListParams& L) const {
+    ST h = Hi;
+    if (cfg.fixShape) {
+      const ST hp{Hi.xx + m * D.xx, Hi.xy + m * D.xy, Hi.xz + m * D.xz, Hi.yy + m * D.yy, Hi.yz + m * D.yz,
+                  Hi.zz + m * D.zz};
+      h = scaleS(Hi, rootnu3(detS(hp) / detS(Hi)));
+    } else if (cfg.radialOnly) {
+      const T9 T = rotationMatrix3(unitVector(xi));
+      h = rotateS(Hi, T);
+      const ST d = rotateS(D, T);
+      h.xx += m * d.xx;
+      h = rotateS(h, transposeT(T));
+    } else {
+      h = ST{Hi.xx + m * D.xx, Hi.xy + m * D.xy, Hi.xz + m * D.xz, Hi.yy + m * D.yy, Hi.yz + m * D.yz,
+             Hi.zz + m * D.zz};
+    }
+    return limitASPH(h, L);
+  }
+  // ASPHSmoothingScale::finalize (ASPHSmoothingScale.cc:157-380) in its
+  // fixShape and radialOnly forms (no Voronoi second moment): the zeroth
+  // moment of the end-of-step state over the step's pairs, the IdealH size
+  // ratio, H scaled (fixShape) or reshaped radially (radialOnly), the limits.
+  // With IntegrateH or FixedH only the limits are applied.
+  void asphFinalize() {
+    if (cfg.hUpdate != 0) {
+      for (int i = 0; i < nInt; ++i) H[i] = limitASPH(H[i], lists[list[i]]);
+      return;
+    }
+    vector<double> m0(nTot, 0.0);
+    pairSweep(pairs.size(), m0, nTot, [&](long kk, vector<double>& p) {
+      const int i = pairs[kk].first, j = pairs[kk].second;
+      const V3 rij = sub(pos[i], pos[j]);
+      const double WSPHi = W.kernelValueSPH(mag(dotSV(H[i], rij))), WSPHj = W.kernelValueSPH(mag(dotSV(H[j], rij)));
+      const double fweightij = (list[i] != list[j]) ? mass[j] * rho[i] / (mass[i] * rho[j]) : 1.0;
+      p[i] += fweightij * WSPHi;
+      p[j] += 1.0 / fweightij * WSPHj;
+    });
+    for (int i = 0; i < nInt; ++i) {
+      const auto& L = lists[list[i]];
+      const double mz = rootnu3(std::max(0.0, m0[i]));
+      massZeroth[i] = mz;
+      const double cur = fuzzyEqual(mz, 0.0) ? 0.5 * L.nPerh : W.equivalentNodesPerSmoothingScale(mz);
+      const double s = std::min(4.0, std::max(0.25, L.nPerh / (cur + 1.0e-30)));
+      const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
+      ST Hid;
+      if (cfg.fixShape) Hid = divS(H[i], 1.0 - aa + aa * s);
+      else Hid = radialEvolution3(H[i], unitVector(pos[i]), 1.0 - aa + aa * s,
+                                  i < (int)radius0.size() ? radius0[i] : 0.0, mag(pos[i]));
+      Hid = limitASPH(Hid, L);
+      Hideal[i] = Hid;
+      H[i] = Hid;
+    }
+  }
+
   static ST clampH(const ST& h, double minv, double maxv) {
     // min(maxv, max(minv, H)): SymTensor min/max with a scalar bound the
     // eigenvalues (GeomSymmetricTensorInline.hh:2745-2772); the isotropic
@@ -1692,13 +1770,17 @@ struct Problem {
     }
     for (int i = 0; i < nInt; ++i) {
       const auto& L = lists[list[i]];
+      const V3 pos0i = pos[i];   // State::update applies the "H" policy before "position" (key order)
       pos[i] = add(pos[i], mul(multiplier, DxDt[i]));
       vel[i] = add(vel[i], mul(multiplier, DvDt[i]));
       if (cfg.gravity) vel[i] = add(vel[i], mul(multiplier, DvDtGrav[i]));
       rho[i] = std::min(L.rhoMax, std::max(L.rhoMin, rho[i] + multiplier * DrhoDt[i]));
       // H: ReplaceBoundedState (IdealH; its timeAdvanceOnly update is the
-      // increment), IncrementBoundedState (IntegrateH), no policy (FixedH)
-      if (cfg.hUpdate == 2) {
+      // increment), IncrementBoundedState (IntegrateH), no policy (FixedH);
+      // ASPHSmoothingScale: IncrementASPHHtensor for IdealH and IntegrateH
+      if (cfg.smoothingScale == 2) {
+        if (cfg.hUpdate != 2) H[i] = incrementASPHHtensor(H[i], DHDt[i], multiplier, pos0i, L);
+      } else if (cfg.hUpdate == 2) {
       } else if (midStep || cfg.hUpdate == 1) {
         ST hn{H[i].xx + multiplier * DHDt[i].xx, H[i].xy + multiplier * DHDt[i].xy, H[i].xz + multiplier * DHDt[i].xz,
               H[i].yy + multiplier * DHDt[i].yy, H[i].yz + multiplier * DHDt[i].yz, H[i].zz + multiplier * DHDt[i].zz};
@@ -1965,6 +2047,8 @@ struct Problem {
     applyGhostState();
     copyQVelocityGradient();
     if (cfg.gradhCorrection) { omegaGradh(); applyGhostState(); }
+    // postStepFinalize: the ASPHSmoothingScale end-of-step H
+    if (cfg.smoothingScale == 2) asphFinalize();
     enforceBoundaries();
     ++cycle;
     lastDt = dt;

@@ -216,7 +216,7 @@ struct sphgpu_ctx {
     p.thermo = thermo.as<float4>();
     p.cell = cellp();
     p.dvq = dvq.p ? dvq.as<float4>() : nullptr;
-    p.hten = cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? hten.as<float4>() : nullptr;
+    p.hten = cfg.smoothing_scale != SPHGPU_SMOOTHING_SPH ? hten.as<float4>() : nullptr;
     p.vol = vol32.p ? vol32.as<float>() : nullptr;
     p.rkc = rkc32.p ? rkc32.as<float4>() : nullptr;
     return p;
@@ -239,7 +239,7 @@ void ensureCapacity(sphgpu_ctx* c, long n) {
   c->velm.release(); c->velm.ensure(n * sizeof(float4));
   c->thermo.release(); c->thermo.ensure(n * sizeof(float4));
   c->hten.release();
-  if (c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC) c->hten.ensure(2 * n * sizeof(float4));
+  if (c->cfg.smoothing_scale != SPHGPU_SMOOTHING_SPH) c->hten.ensure(2 * n * sizeof(float4));
   c->vol32.release();
   c->rkc32.release();
   if (c->cfg.hydro == SPHGPU_HYDRO_CRKSPH && c->fp32()) {
@@ -328,7 +328,8 @@ void refreshParams(sphgpu_ctx* c) {
   hp.limitedQ = g.viscosity == SPHGPU_VISCOSITY_LIMITED_MONAGHAN_GINGOLD ? 1 : 0;
   hp.etaCrit = g.eta_crit_frac / c->lists[0].nPerh;
   hp.etaFold = g.eta_fold_frac / c->lists[0].nPerh;
-  hp.asph = g.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC ? 1 : 0;
+  hp.asph = g.smoothing_scale != SPHGPU_SMOOTHING_SPH ? 1 : 0;   // tensor H
+  hp.asphEnd = g.smoothing_scale == SPHGPU_SMOOTHING_ASPH ? 1 : 0;
   hp.fixShape = g.fix_shape ? 1 : 0;
   hp.hUpdate = g.h_update;
   hp.totalEnergy = g.evolve_total_energy ? 1 : 0;
@@ -924,8 +925,16 @@ double step(sphgpu_ctx* c, double maxTime) {
   // sweep reads the FP64 positions, so it is owed only when no wall or period
   // can move a node after it.
   if (c->cfg.gradh_correction) {
-    if (c->fp32() || c->bcs.empty()) c->omegaStale = true;
+    // ASPHSmoothingScale changes H after this point: its Omega is the one of
+    // the H before that change, so it is computed now
+    if ((c->fp32() || c->bcs.empty()) && !c->hp.asphEnd) c->omegaStale = true;
     else gradh(c);
+  }
+  if (c->hp.asphEnd) {   // postStepFinalize: ASPHSmoothingScale::finalize
+    Scope sc(c->prof, "asph_end");
+    launchASPHEnd(c->F, c->fp32() ? c->f32() : Fields32{}, c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
+                  c->stream, &c->lc);
+    c->check();
   }
   {
     Scope sc(c->prof, "enforce");
@@ -1100,13 +1109,17 @@ int sphgpu_create(const sphgpu_config* cfg, sphgpu_handle* out) {
       throw Error(SPHGPU_E_ARG, "etaFoldFrac must be positive");
     if (cfg->density_update != SPHGPU_DENSITY_RIGOROUS_SUM && cfg->density_update != SPHGPU_DENSITY_INTEGRATE)
       throw Error(SPHGPU_E_UNSUPPORTED, "only RigorousSumDensity and IntegrateDensity are on this path");
-    if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
+    if (cfg->smoothing_scale != SPHGPU_SMOOTHING_SPH && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC &&
+        cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown smoothing-scale package");
+    if (cfg->smoothing_scale == SPHGPU_SMOOTHING_ASPH && !cfg->fix_shape && !cfg->radial_only)
+      throw Error(SPHGPU_E_UNSUPPORTED, "ASPHSmoothingScale without fixShape or radialOnly shapes H from Voronoi "
+                                        "cells, which are not built");
     if (cfg->h_update != SPHGPU_H_IDEAL && cfg->h_update != SPHGPU_H_INTEGRATE && cfg->h_update != SPHGPU_H_FIXED)
       throw Error(SPHGPU_E_UNSUPPORTED, "unknown H evolution");
     if (cfg->fix_shape && cfg->radial_only)   // ASPHClassicSmoothingScale: not both
       throw Error(SPHGPU_E_ARG, "fixShape and radialOnly cannot both be set");
-    if (cfg->radial_only && cfg->smoothing_scale != SPHGPU_SMOOTHING_ASPH_CLASSIC)
+    if (cfg->radial_only && cfg->smoothing_scale == SPHGPU_SMOOTHING_SPH)
       throw Error(SPHGPU_E_ARG, "radialOnly needs the ASPH smoothing scale");
     if (cfg->compatible_energy && cfg->evolve_total_energy)   // SPH.cc:97-98
       throw Error(SPHGPU_E_ARG, "compatibleEnergyEvolution and evolveTotalEnergy cannot both be set");
@@ -1248,7 +1261,7 @@ int sphgpu_set_particles(sphgpu_handle c, long n, const double* pos, const doubl
   if (n <= 0 || n >= kMaxNodes) throw Error(SPHGPU_E_ARG, "particle count out of range");
   if (!pos || !vel || !mass || !rho || !eps || !H) throw Error(SPHGPU_E_ARG, "null particle array");
   if (c->numLists == 0) c->numLists = 1;
-  const bool asph = c->cfg.smoothing_scale == SPHGPU_SMOOTHING_ASPH_CLASSIC;
+  const bool asph = c->cfg.smoothing_scale != SPHGPU_SMOOTHING_SPH;
   for (long i = 0; i < n; ++i) {
     const double* h = H + 6 * i;
     if (asph) {   // symmetric positive definite: leading minors positive (Sylvester)

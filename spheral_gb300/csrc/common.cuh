@@ -49,7 +49,8 @@ struct HydroParams {
   const NodeListParams* lists;   // device table of the NodeLists (kMaxNodeLists entries)
   int limitedQ;                  // LimitedMonaghanGingoldViscosity instead of MonaghanGingoldViscosity
   double etaCrit, etaFold;       // its full-Q distance and fold width in eta
-  int asph;                      // ASPHClassicSmoothingScale: tensor H throughout
+  int asph;                      // an ASPH smoothing scale: tensor H throughout
+  int asphEnd;                   // ASPHSmoothingScale: H integrated in the step, reset at its end
   int fixShape;                  // ASPH fixShape: Hideal keeps the shape of H
   int hUpdate;                   // HEvolutionType: 0 IdealH, 1 IntegrateH, 2 FixedH
   int totalEnergy;               // evolveTotalEnergy: DepsDt is the total-energy rate

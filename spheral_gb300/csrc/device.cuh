@@ -346,6 +346,7 @@ __device__ __forceinline__ void finalizeNodeASPH(Fields& F, long i, int li, cons
   finalizeHydro(F, i, a, mi, rhoi, vxi, vyi, vzi, symDet(Hi), numNb, hp, D);
   const NodeListParams L = hp.lists[li];
   storeSym(F, F_DHDTT_XX, i, smoothingScaleDerivative(Hi, D));
+  if (hp.asphEnd) return;   // ASPHSmoothingScale: the ideal H comes at the end of the step
   const double m0 = rootnu3T(fmax(0.0, a.m0));
   F.f[F_M0][i] = m0;
   F.f[F_M1_X][i] = a.m1x;
@@ -456,13 +457,16 @@ __device__ __forceinline__ void finalizeNode32(Fields& F, long i, int li, const 
   F.f[F_XSPHDV_Z][i] = a.xdz;
   const NodeListParams L = hp.lists[li];
   const float m0 = cbrtf(fmaxf(0.0f, a.m0));
-  F.f[F_M0][i] = m0;
-  F.f[F_M1_X][i] = a.m1x;
-  F.f[F_M1_Y][i] = a.m1y;
-  F.f[F_M1_Z][i] = a.m1z;
+  if (!(TENSOR && hp.asphEnd)) {
+    F.f[F_M0][i] = m0;
+    F.f[F_M1_X][i] = a.m1x;
+    F.f[F_M1_Y][i] = a.m1y;
+    F.f[F_M1_Z][i] = a.m1z;
+  }
   if (TENSOR) {
     const SymT<float> Hi{a.h0.x, a.h0.y, a.h0.z, a.h0.w, a.h1.x, a.h1.y};
     storeSym(F, F_DHDTT_XX, i, smoothingScaleDerivative(Hi, D));
+    if (hp.asphEnd) return;   // ASPHSmoothingScale: the ideal H comes at the end of the step
     const SymT<float> M2{a.m2[0], a.m2[1], a.m2[2], a.m2[3], a.m2[4], a.m2[5]};
     storeSym(F, F_M2_XX, i, M2);
     const float nPerh = (float)L.nPerh;

@@ -942,6 +942,73 @@ __global__ void radius0Kernel(Fields F, long n) {
   const double x = F.f[F_X][i], y = F.f[F_Y][i], z = F.f[F_Z][i];
   F.f[F_RAD0][i] = sqrt(x * x + y * y + z * z);
 }
+// ASPHSmoothingScale::finalize (src/SmoothingScale/ASPHSmoothingScale.cc:157-380)
+// in its fixShape and radialOnly forms, gathered: the zeroth moment of the
+// end-of-step state over the step's neighbour lists (fweight_ij WSPH(|H_i r_ij|)),
+// the IdealH size ratio, H scaled (fixShape) or reshaped radially about the
+// origin (radialOnly), then the eigenvalue limits; with IntegrateH or FixedH
+// only the limits.  FP64 in both precision modes; in the mixed mode the FP32
+// extents and mirrors of the new H are written as the update writes them.
+__global__ void __launch_bounds__(128) asphEndKernel(Fields F, Fields32 P, const int* __restrict__ list, long n,
+                                                    Grid g, NeighborLists nl, TableDev t, HydroParams hp) {
+  extern __shared__ double smem[];   // dW/deta coefficients
+  const int ntab = 3 * (hp.tableN1 + 1);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) smem[k] = t.g[k];
+  __syncthreads();
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int li = list[i];
+  const NodeListParams L = hp.lists[li];
+  const Sym Hi = loadSym(F, F_HT_XX, i);
+  Sym Hn;
+  if (hp.hUpdate != 0) {
+    Hn = limitASPH(Hi, L.hminInv, L.hmaxInv, L.hminratio);
+  } else {
+    int hc[3];
+    unpackCell(nl.cell[i], hc);
+    const double* __restrict__ X = F.f[F_X];
+    const double* __restrict__ Y = F.f[F_Y];
+    const double* __restrict__ Z = F.f[F_Z];
+    const double xi = X[i], yi = Y[i], zi = Z[i];
+    const double mi = F.f[F_MASS][i], rhoi = F.f[F_RHO][i];
+    const bool multi = hp.numLists > 1;
+    double m0 = 0.0;
+    const int cnt = nl.count[i];
+    for (int q = 0; q < cnt; ++q) {
+      const uint32_t ent = nl.nbr[nbSlot(i, q, nl.cap)];
+      const int j = (int)(ent & kIndexMask), code = imageCode(g, hc, (int)(ent >> kIndexBits));
+      double xj = X[j], yj = Y[j], zj = Z[j];
+      imagePos(g, code, xj, yj, zj);
+      double ex, ey, ez;
+      symDot(Hi, xi - xj, yi - yj, zi - zj, ex, ey, ez);
+      const double eta = sqrt(ex * ex + ey * ey + ez * ez);
+      if (eta < hp.extent) {
+        const double wsph = fabs(tableEval(smem, tableIndex(eta, hp.tableN1, hp.tableXstep), eta));
+        const double fw = (multi && list[j] != li) ? F.f[F_MASS][j] * rhoi / (mi * F.f[F_RHO][j]) : 1.0;
+        m0 += fw * wsph;
+      }
+    }
+    const double mz = rootnu3T(fmax(0.0, m0));
+    F.f[F_M0][i] = mz;
+    const bool isolated = fabs(mz) <= 1.0e-15 * fmax(1.0, fabs(mz));
+    const double cur = isolated ? 0.5 * L.nPerh : fmax(0.0, hermiteLookup(t.herm, hp, mz));
+    const double s = fmin(4.0, fmax(0.25, L.nPerh / (cur + 1.0e-30)));
+    const double aa = s < 1.0 ? 0.4 * (1.0 + s * s) : 0.4 * (1.0 + 1.0 / (s * s * s));
+    const double f = 1.0 - aa + aa * s;
+    const Sym Hid = hp.fixShape ? symDiv(Hi, f) : radialEvolution(Hi, xi, yi, zi, f, F.f[F_RAD0][i]);
+    Hn = limitASPH(Hid, L.hminInv, L.hmaxInv, L.hminratio);
+    storeSym(F, F_HIDEALT_XX, i, Hn);
+  }
+  storeSym(F, F_HT_XX, i, Hn);
+  if (P.posh) {
+    storeExtent32(F, i, Hn);
+    P.posh[i].w = (float)F.f[F_HINV][i];
+    writeTensorMirror(F, P, i);
+  } else {
+    storeExtent(F, i, Hn);
+  }
+}
+
 __global__ void tensorExtentKernel(Fields F, long n) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -954,13 +1021,18 @@ __global__ void tensorExtentKernel(Fields F, long n) {
 // (IncrementBoundedState / ReplaceBoundedState with SymTensor min/max).
 // hUpdate: HEvolutionType -- 0 IdealH (the full update replaces H by Hideal),
 // 1 IntegrateH (both updates increment H by DHDt), 2 FixedH (H never changes).
+// asphEnd (ASPHSmoothingScale): both updates integrate H with
+// IncrementASPHHtensor (fixShape / radialOnly forms) unless FixedH.
 template <bool TENSOR>
 __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, const NodeListParams* __restrict__ lists,
                              double mult, int mid, int gravity, int epsIncrement, int hUpdate, int totalEnergy,
-                             int crk, Fields32 P, Grid g) {
+                             int crk, Fields32 P, Grid g, int asphEnd, int fixShape, int radialOnly) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const NodeListParams L = lists[list[i]];
+  // the position before this update (the radial direction of radialOnly:
+  // State::update applies the "H" policy before the "position" one)
+  const double xOld = F.f[F_X][i], yOld = F.f[F_Y][i], zOld = F.f[F_Z][i];
   // the half-step update first takes the beginning-of-step copy (state0)
   if (mid) {
     F.f[F_X0][i] = F.f[F_X][i]; F.f[F_Y0][i] = F.f[F_Y][i]; F.f[F_Z0][i] = F.f[F_Z][i];
@@ -1011,6 +1083,13 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
   double h;
   const bool increment = mid || hUpdate == 1;
   if (hUpdate == 2) {
+    h = F.f[F_HINV][i];
+  } else if (TENSOR && asphEnd) {
+    const Sym t = incrementASPHHtensor(loadSym(F, F_HT_XX, i), loadSym(F, F_DHDTT_XX, i), mult, xOld, yOld, zOld,
+                                       fixShape != 0, radialOnly != 0, hminInv, hmaxInv, L.hminratio);
+    storeSym(F, F_HT_XX, i, t);
+    if (P.posh) storeExtent32(F, i, t);
+    else storeExtent(F, i, t);
     h = F.f[F_HINV][i];
   } else if (TENSOR) {
     Sym t;
@@ -1400,10 +1479,17 @@ void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult
   if (mirror) P = *mirror;
   if (hp.asph)
     updateKernel<true><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0, epsInc,
-                                                       hp.hUpdate, hp.totalEnergy, 0, P, g);
+                                                       hp.hUpdate, hp.totalEnergy, 0, P, g, hp.asphEnd, hp.fixShape,
+                                                       hp.radialOnly);
   else
     updateKernel<false><<<gridFor(n, 256), 256, 0, s>>>(F, list, n, hp.lists, mult, mid ? 1 : 0, gravity ? 1 : 0,
-                                                        epsInc, hp.hUpdate, hp.totalEnergy, hp.crk, P, g);
+                                                        epsInc, hp.hUpdate, hp.totalEnergy, hp.crk, P, g, 0, 0, 0);
+  lc->add(1);
+}
+void launchASPHEnd(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                   HydroParams hp, cudaStream_t s, LaunchCounter* lc) {
+  const size_t smem = 3 * (size_t)(hp.tableN1 + 1) * sizeof(double);
+  asphEndKernel<<<gridFor(n, 128), 128, smem, s>>>(F, P, list, n, g, nl, t, hp);
   lc->add(1);
 }
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc) {

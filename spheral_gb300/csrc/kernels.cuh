@@ -123,6 +123,10 @@ void launchRadius0(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // also refresh the FP32 mirrors of the new state (mixed mode), cells of grid g.
 void launchUpdate(Fields F, const int* list, long n, HydroParams hp, double mult,
                   bool mid, bool gravity, const Fields32* mirror, const Grid& g, cudaStream_t s, LaunchCounter* lc);
+// ASPHSmoothingScale end of step: zeroth moment, IdealH and limits of H
+// (P.posh non-null: the mixed mode's FP32 extents and mirrors are refreshed).
+void launchASPHEnd(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
+                   HydroParams hp, cudaStream_t s, LaunchCounter* lc);
 // lists: device table of NodeListParams (HydroParams::lists).
 void launchEOS(Fields F, const int* list, long n, const NodeListParams* lists, cudaStream_t s, LaunchCounter* lc);
 void launchEnforce(Fields F, long n, Grid g, bool tensor, cudaStream_t s, LaunchCounter* lc);

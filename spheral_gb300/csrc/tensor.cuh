@@ -341,6 +341,48 @@ __device__ __forceinline__ SymT<T> asphClassicHideal(const SymT<T>& M2, bool m2P
   return symFromEigen(d, V);
 }
 
+// The eigenvalue limits of the ASPH smoothing scales: every eigenvalue of H
+// within [1/hmax, min(1/hmin, max(1/hmax, smallest)/hminratio)]
+// (constructSymTensorWithBoundedDiagonal + rotationalTransform,
+// IncrementASPHHtensor.cc:88-92, ASPHSmoothingScale.cc:355-359).
+__device__ __forceinline__ Sym limitASPH(const Sym& h, double hminInv, double hmaxInv, double hminratio) {
+  double ev[3], V[3][3], d[3];
+  symEigen(h, ev, V);
+  const double hminEffInv = fmin(hminInv, fmax(hmaxInv, fmin(ev[0], fmin(ev[1], ev[2]))) / hminratio);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = fmax(hmaxInv, fmin(hminEffInv, ev[k]));
+  return symFromEigen(d, V);
+}
+// IncrementASPHHtensor::update (src/SmoothingScale/IncrementASPHHtensor.cc:37-100)
+// for one node: fixShape scales H by the cube root of the determinant ratio
+// of the plain increment; radialOnly increments only the radial diagonal
+// element in the frame whose first axis is the radial direction of the
+// position (x, y, z) before this update; otherwise H += m DH/Dt; then the
+// limits.
+__device__ __forceinline__ Sym incrementASPHHtensor(const Sym& H, const Sym& D, double m, double x, double y,
+                                                    double z, bool fixShape, bool radialOnly, double hminInv,
+                                                    double hmaxInv, double hminratio) {
+  Sym h;
+  if (fixShape) {
+    const Sym hp{H.xx + m * D.xx, H.xy + m * D.xy, H.xz + m * D.xz, H.yy + m * D.yy, H.yz + m * D.yz,
+                 H.zz + m * D.zz};
+    h = symScale(H, rootnu3T(symDet(hp) / symDet(H)));
+  } else if (radialOnly) {
+    const double r = sqrt(x * x + y * y + z * z);
+    double ux = 1.0, uy = 0.0, uz = 0.0;   // GeomVector::unitVector
+    if (r > 1.0e-50) { ux = x / r; uy = y / r; uz = z / r; }
+    double R[3][3];
+    rotationMatrix3(ux, uy, uz, R);
+    h = symRotate(H, R, false);
+    const Sym dr = symRotate(D, R, false);
+    h.xx += m * dr.xx;
+    h = symRotate(h, R, true);
+  } else {
+    h = Sym{H.xx + m * D.xx, H.xy + m * D.xy, H.xz + m * D.xz, H.yy + m * D.yy, H.yz + m * D.yz, H.zz + m * D.zz};
+  }
+  return limitASPH(h, hminInv, hmaxInv, hminratio);
+}
+
 // FP32 mirror of tensor H for the FP32 sweeps and the neighbour pre-filter:
 // (xx xy xz yy) (yz zz det(H) lambda_max).
 __device__ __forceinline__ void writeTensorMirror(const Fields& F, const Fields32& P, long i) {

@@ -27,7 +27,7 @@ DT_REASONS = ["sound speed", "artificial viscosity", "velocity divergence", "acc
 
 VISCOSITY = {"monaghan_gingold": 0, "limited_monaghan_gingold": 1}
 # smoothing-scale package: SPHSmoothingScale or ASPHClassicSmoothingScale
-SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1}
+SMOOTHING_SCALE = {"sph": 0, "asph_classic": 1, "asph": 2}
 # HEvolutionType
 H_UPDATE = {"ideal": 0, "integrate": 1, "fixed": 2}
 # hydro package and the RK volume type of CRKSPH (RKVolumeType)

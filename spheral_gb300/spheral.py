@@ -89,13 +89,23 @@ class ASPHClassicSmoothingScale:
 
 
 class ASPHSmoothingScale:
-    """ASPHSmoothingScale shapes H from Voronoi cell moments (a tessellation
-    outside this path); with fixShape it reduces to scaling H, which the
-    classic form covers."""
+    """ASPHSmoothingScale(HUpdate, W, fixShape=False, radialOnly=False)
+    (src/SmoothingScale/ASPHSmoothingScale.cc): the tensor H is integrated
+    with DH/Dt during the step (IncrementASPHHtensor) and, with IdealH, reset
+    at the end of the step from the zeroth moment -- scaled (fixShape) or
+    reshaped along the radial direction about the origin (radialOnly).  Its
+    default form takes the shape of H from each node's Voronoi cell, a
+    tessellation outside this path, and is refused."""
 
-    def __init__(self, *args, **kwargs):
-        raise NotImplementedError("ASPHSmoothingScale needs Voronoi cells: use ASPH='CLASSIC' "
-                                  "(ASPHClassicSmoothingScale)")
+    def __init__(self, HUpdate=IdealH, W=None, fixShape=False, radialOnly=False):
+        if fixShape and radialOnly:   # ASPHSmoothingScale.cc:169
+            raise ValueError("fixShape and radialOnly cannot both be set")
+        if not (fixShape or radialOnly):
+            raise NotImplementedError("ASPHSmoothingScale without fixShape or radialOnly shapes H from Voronoi "
+                                      "cells, which are not on the GPU path: use fixShape=True, radialOnly=True "
+                                      "or ASPH='CLASSIC' (ASPHClassicSmoothingScale)")
+        self._cfg = dict(smoothing_scale="asph", fix_shape=bool(fixShape), radial_only=bool(radialOnly),
+                         h_update=_h_update(HUpdate))
 
 
 class BSplineKernel:
@@ -351,7 +361,8 @@ def SPH(W, WPi=None, WGrad=None, dataBase=None, Q=None, filter=0.0, cfl=0.25, us
                 smoothingScaleMethod = ASPHSmoothingScale(HUpdate, W)
         else:
             smoothingScaleMethod = SPHSmoothingScale(HUpdate, W)
-    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale, FixedSmoothingScale)):
+    elif not isinstance(smoothingScaleMethod, (SPHSmoothingScale, ASPHClassicSmoothingScale, ASPHSmoothingScale,
+                                               FixedSmoothingScale)):
         raise NotImplementedError("unknown smoothing-scale package")
     if (filter or 0.0) != 0.0:
         raise NotImplementedError("H filtering is not on the GPU path")

@@ -138,3 +138,18 @@ def test_nbspline_table_kernel_configures_the_package():
     assert c._cfg["Cl"] == 2.0 * 0.75 and c._cfg["Cq"] == 0.75 ** 2   # Cl = 2 (extent/4), Cq = (extent/4)^2
     with pytest.raises(NotImplementedError):
         S.NBSplineKernel(12)
+
+
+def test_asph_smoothing_scale_forms():
+    # ASPHSmoothingScale (ASPHSmoothingScale.cc): the fixShape and radialOnly
+    # forms are on the path, the Voronoi-shaped default form is refused
+    W = S.TableKernel(S.BSplineKernel(), 1000)
+    db = S.DataBase()
+    h = S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.ASPHSmoothingScale(S.IdealH, W, fixShape=True))
+    assert h._cfg["smoothing_scale"] == "asph" and h._cfg["fix_shape"] and not h._cfg["radial_only"]
+    r = S.SPH(W=W, dataBase=db, smoothingScaleMethod=S.ASPHSmoothingScale(S.IntegrateH, W, radialOnly=True))
+    assert r._cfg["radial_only"] and r._cfg["h_update"] == "integrate"
+    with pytest.raises(NotImplementedError):
+        S.ASPHSmoothingScale(S.IdealH, W)
+    with pytest.raises(ValueError):
+        S.ASPHSmoothingScale(S.IdealH, W, fixShape=True, radialOnly=True)
