@@ -328,6 +328,10 @@ int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
  * the first mixed-mode evaluation).  No reference counterpart (tuning only). */
 int sphgpu_set_pair_variant(sphgpu_handle h, int variant);
 int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
+/* Lanes per work group of the neighbour search (8, 16 or 32), picked by
+ * timing each width once per problem size (the lists are the same for every
+ * width).  No reference counterpart (tuning only). */
+int sphgpu_get_neighbor_width(sphgpu_handle h, int* width);
 
 /* Checkpoint and restart.  Replaces: SPHBase::dumpState / restoreState
  * (src/SPH/SPHBase.cc:711-768) with the integrator's time, last dt and cycle,

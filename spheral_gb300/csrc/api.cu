@@ -171,6 +171,8 @@ struct sphgpu_ctx {
   cudaEvent_t tA = nullptr, tB = nullptr;
   int itemWidth = 32;        // lanes per work item of the neighbour search
   int itemBound = 0;         // upper bound on the number of work items
+  int tunedWidth = 0;        // autotuned group width (0: not tuned yet)
+  long widthTunedN = 0;      // node count it was tuned at
   DBuf itemCount;            // device: number of work items
   bool capCheckPending = false, totalPending = false;
   double cachedBounds[kBoundsVals] = {};   // min h^-1, min x y z, max x y z, tensor extents of the current state
@@ -549,24 +551,28 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   c->nbrStart.ensure((n + 1) * sizeof(long long));
   c->scanWs.ensure(scanWorkspaceBytes(n) + 64);
   c->itemCount.ensure(sizeof(long long));
-  // work items: first node of every chunk of up to `width` nodes of a cell;
-  // the group width follows the mean occupancy of the cells so that few
-  // lanes of a group idle (a chunk rarely has fewer nodes than lanes).
+  // work items: first node of every chunk of up to `width` nodes of a cell.
+  // The first guess of the group width follows the mean occupancy of the
+  // cells so that few lanes of a group idle; the autotuner below then times
+  // the widths once per problem size.
   const double cellsTotal = (double)g.nc[0] * g.nc[1] * g.nc[2];
   const double occupancy = (double)n / cellsTotal;
-  c->itemWidth = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
-  // every non-empty cell adds at most one partial chunk
-  c->itemBound = (int)std::min<double>((double)n, (double)(n / c->itemWidth) + cellsTotal);
+  const int guess = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
+  const bool tuned = c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8;
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
-  {
+  auto makeItems = [&](int width) {
+    c->itemWidth = width;
+    // every non-empty cell adds at most one partial chunk
+    c->itemBound = (int)std::min<double>((double)n, (double)(n / width) + cellsTotal);
     Scope sc(c->prof, "neighbor_items");
     long long* pos = c->nbrStart.as<long long>();
-    launchItemFlags(k, n, c->cellStart.as<int>(), c->itemWidth, c->itemFlag.as<int>(), c->stream, &c->lc);
+    launchItemFlags(k, n, c->cellStart.as<int>(), width, c->itemFlag.as<int>(), c->stream, &c->lc);
     scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, c->itemCount.as<long long>(), c->stream, &c->lc);
     launchItemFill(c->itemFlag.as<int>(), pos, n, c->items.as<int>(), c->stream, &c->lc);
-  }
-  c->check();
+    c->check();
+  };
+  makeItems(tuned ? c->tunedWidth : guess);
   if (c->nbCapNext > 0) {   // adopt a smaller capacity decided at the previous build
     c->nbCap = c->nbCapNext;
     c->nbCapNext = 0;
@@ -580,6 +586,31 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
                         nullptr, 0, c->hp.extent * c->hp.extent, c->hp.asph != 0, c->stream, &c->lc);
     c->check();
     c->nbCap = capFor(readMaxCount(c));
+  }
+  if (!tuned) {
+    // Autotuner: the lists do not depend on the group width (the candidate
+    // order is the cell order in every width), so each width writes them
+    // once, timed, and the fastest is kept for this problem size.
+    cudaEvent_t e0, e1;
+    CUDA_OK(cudaEventCreate(&e0));
+    CUDA_OK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestW = guess;
+    for (const int w : {8, 16, 32}) {
+      if (w != c->itemWidth) makeItems(w);
+      CUDA_OK(cudaEventRecord(e0, c->stream));
+      writeLists(c);
+      CUDA_OK(cudaEventRecord(e1, c->stream));
+      CUDA_OK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) { best = ms; bestW = w; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->tunedWidth = bestW;
+    c->widthTunedN = n;
+    if (bestW != c->itemWidth) makeItems(bestW);
   }
   writeLists(c);
   if (deferCheck) {
@@ -1542,6 +1573,13 @@ int sphgpu_set_pair_variant(sphgpu_handle c, int variant) {
   if (variant < -1 || variant >= kPairVariants) throw Error(SPHGPU_E_ARG, "pair variant out of range");
   c->pairVariant = variant;
   c->pinnedVariant = variant >= 0;
+  API_END(c)
+}
+
+int sphgpu_get_neighbor_width(sphgpu_handle c, int* width) {
+  API_BEGIN(c)
+  if (!width) throw Error(SPHGPU_E_ARG, "null width");
+  *width = c->itemWidth;
   API_END(c)
 }
 

@@ -179,6 +179,12 @@ class Engine:
         self._chk(self.L.sphgpu_get_pair_variant(self.h, ctypes.byref(v), ctypes.byref(nv)))
         return v.value, nv.value
 
+    def neighbor_width(self):
+        """Lanes per work group of the neighbour search (autotuned)."""
+        w = ctypes.c_int()
+        self._chk(self.L.sphgpu_get_neighbor_width(self.h, ctypes.byref(w)))
+        return w.value
+
     def set_pair_variant(self, v):
         self._chk(self.L.sphgpu_set_pair_variant(self.h, v))
 

@@ -70,6 +70,7 @@ def test_neighbor_sets_exact_at_size(case):
     name, p, orc = case
     eng = Engine.from_problem(p)
     eng.initialize()
+    assert eng.neighbor_width() in (8, 16, 32)   # the autotuned search group width
     i, j, im = eng.pairs()
     got = np.sort(_pair_keys(i, j, im, p.n))
     assert np.all(np.diff(got) > 0), "duplicate neighbour entries"
