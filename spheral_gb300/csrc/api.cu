@@ -171,6 +171,8 @@ struct sphgpu_ctx {
   cudaEvent_t tA = nullptr, tB = nullptr;
   int itemWidth = 32;        // lanes per work item of the neighbour search
   int itemBound = 0;         // upper bound on the number of work items
+  int energyVariant = -1;    // autotuned batch depth of the FP32 energy sweep
+  long energyTunedN = 0;
   int tunedWidth = 0;        // autotuned group width (0: not tuned yet)
   long widthTunedN = 0;      // node count it was tuned at
   DBuf itemCount;            // device: number of work items
@@ -930,8 +932,33 @@ double step(sphgpu_ctx* c, double maxTime) {
     Scope sc(c->prof, "energy");
     if (c->fp32()) {
       c->v12.ensure(c->n * 2 * sizeof(float4));
+      if (c->energyVariant < 0 || std::labs(c->n - c->energyTunedN) > c->energyTunedN / 8) {
+        // Autotuner: time each batch depth once per problem size.  The trial
+        // launches take dt = 0, so they add nothing to the energies; the
+        // real launch below recomputes everything they wrote.
+        cudaEvent_t e0, e1;
+        CUDA_OK(cudaEventCreate(&e0));
+        CUDA_OK(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int bestV = 0;
+        for (int v = 0; v < kEnergyVariants; ++v) {
+          CUDA_OK(cudaEventRecord(e0, c->stream));
+          launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<float4>(),
+                                     c->v12.as<float4>() + c->n, 0.0, v, c->stream, &c->lc);
+          CUDA_OK(cudaEventRecord(e1, c->stream));
+          CUDA_OK(cudaEventSynchronize(e1));
+          c->check();
+          float ms = 0.f;
+          CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+          if (ms < best) { best = ms; bestV = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        c->energyVariant = bestV;
+        c->energyTunedN = c->n;
+      }
       launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<float4>(),
-                                 c->v12.as<float4>() + c->n, dt, c->stream, &c->lc);
+                                 c->v12.as<float4>() + c->n, dt, c->energyVariant, c->stream, &c->lc);
     }
     else
       launchCompatibleEnergy(c->F, c->n, c->grid, c->nl(), c->pacc.as<double>(), nullptr, dt, c->stream, &c->lc);

@@ -689,6 +689,9 @@ __global__ void halfStepVelocityKernel(Fields F, long n, double hdt, float4* __r
   vlo[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.0f);
 }
 
+// B: slots per batch (the gathers and pair-acceleration reads in flight per
+// thread); every B adds in the same slot order, so the result is the same.
+template <int B>
 __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, NeighborLists nl,
                                                       const float4* __restrict__ vhi, const float4* __restrict__ vlo,
                                                       const float* __restrict__ pacc, double dt) {
@@ -723,11 +726,9 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
     const float weightj = fmaxf(feps, hj.w * sg);
     kahanAdd(s, c, __fdividef(weighti, weighti + weightj) * du);
   };
-  // Batches of four slots: all their loads are issued before any is used,
-  // so four gathers and pair-acceleration reads are in flight together.
-  // The entries of the next batch are loaded while this batch's gathers
-  // are in flight.
-  constexpr int B = 4;
+  // Batches of B slots: all their loads are issued before any is used, so B
+  // gathers and pair-acceleration reads are in flight together.  The entries
+  // of the next batch are loaded while this batch's gathers are in flight.
   int q = 0;
   uint32_t en[B];
   if (B <= cnt) {
@@ -862,9 +863,11 @@ void launchDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Neigh
 }
 
 void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
-                                float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc) {
+                                float4* vlo, double dt, int variant, cudaStream_t s, LaunchCounter* lc) {
   halfStepVelocityKernel<<<gridFor(n, 256), 256, 0, s>>>(F, n, 0.5 * dt, vhi, vlo);
-  energyKernel32<<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
+  if (variant == 1) energyKernel32<8><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
+  else if (variant == 2) energyKernel32<2><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
+  else energyKernel32<4><<<gridFor(n, 128), 128, 0, s>>>(F, n, g, nl, vhi, vlo, pacc, dt);
   lc->add(2);
 }
 

@@ -86,8 +86,11 @@ void launchDt(Fields F, const int* list, long n, Grid g, NeighborLists nl, Hydro
               cudaStream_t s, LaunchCounter* lc);
 void launchCompatibleEnergy(Fields F, long n, Grid g, NeighborLists nl, const double* pacc, const float* pacc32,
                             double dt, cudaStream_t s, LaunchCounter* lc);
+// variant: slots per batch of the sweep, 0 -> 4, 1 -> 8, 2 -> 2 (the same
+// result for every variant; picked by the autotuner).
+constexpr int kEnergyVariants = 3;
 void launchCompatibleEnergyFP32(Fields F, long n, Grid g, NeighborLists nl, const float* pacc, float4* vhi,
-                                float4* vlo, double dt, cudaStream_t s, LaunchCounter* lc);
+                                float4* vlo, double dt, int variant, cudaStream_t s, LaunchCounter* lc);
 // state0 -> state (the copy is taken by the half-step update); tensor: also
 // the tensor H (ASPH)
 void launchRestoreState0(Fields F, long n, bool tensor, bool crk, cudaStream_t s, LaunchCounter* lc);
