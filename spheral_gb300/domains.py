@@ -31,8 +31,6 @@ are exact in float64).
 A `comm` object supplies rank, size, the all-reduces and the pairwise
 exchange; TorchComm wraps a torch.distributed process group.
 """
-import math
-
 import numpy as np
 
 from . import _native as N
@@ -333,9 +331,14 @@ class SlabDecomposition:
         return self.engine.time
 
     def owned(self, name):
-        """(global indices, values) of field `name` on this domain's nodes."""
-        f = self.engine.field(name)
-        return self.gid[:self.n_own], f[:self.n_own]
+        """(global indices, values) of field `name` on this domain's nodes.
+        Positions on a periodic decomposed axis are reported inside the box
+        (the domains wrap them when nodes migrate, between steps)."""
+        f = self.engine.field(name)[:self.n_own]
+        if name == "position" and self.periodic:
+            f = f.copy()
+            f[:, self.axis] = self.lo + np.mod(f[:, self.axis] - self.lo, self.length)
+        return self.gid[:self.n_own], f
 
     def conservation(self):
         """Totals of the whole run (all-reduced): mass, momentum (3),

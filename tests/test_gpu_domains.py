@@ -5,7 +5,8 @@ against the same run on one handle.
 FP64: the neighbour sets of the owned nodes are exactly those of the single
 run (across the cut and the periodic boundary), and after five steps every
 state field agrees to 1e-12 normwise (only the summation order of the
-neighbour sums differs), as do the dt sequence and the conserved totals.
+neighbour sums differs), as does the dt sequence; the conserved totals (host
+sums over the owned nodes) to 1e-11.
 Mixed mode: three steps within 5e-5 normwise (the FP32 sweeps see the same
 separations relative to different cell origins)."""
 import os
@@ -82,7 +83,9 @@ def test_two_slab_run_matches_single_run(native_lib, case, precision, nsteps, to
     for name in ("position", "velocity", "massDensity", "specificThermalEnergy", "H"):
         got = _gather(res, name, p.n)
         assert rel_err(got, eng.field(name)) <= tol, (name, rel_err(got, eng.field(name)))
+    # totals: host sums over owned nodes against the device tally (summation
+    # order differs)
     c = np.array(res[0]["conservation"])
     want_c = eng.conservation()
-    assert abs(c[7] - want_c[7]) <= 1e-12 * abs(want_c[7])
+    assert abs(c[7] - want_c[7]) <= 1e-11 * abs(want_c[7])
     assert abs(c[0] - want_c[0]) <= 1e-12 * abs(want_c[0])
