@@ -173,6 +173,7 @@ struct sphgpu_ctx {
   int itemBound = 0;         // upper bound on the number of work items
   int energyVariant = -1;    // autotuned batch depth of the FP32 energy sweep
   long energyTunedN = 0;
+  DBuf itemBox, chunkOf;     // bounding boxes of the search's work chunks, chunk of each chunk's first node
   int tunedWidth = 0;        // autotuned group width (0: not tuned yet)
   long widthTunedN = 0;      // node count it was tuned at
   DBuf itemCount;            // device: number of work items
@@ -472,7 +473,7 @@ void writeLists(sphgpu_ctx* c) {
   launchNeighborsWarp(c->F, c->f32(), c->n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
                       c->itemWidth, c->grid, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(),
                       maxCountPtr(c), c->nbr.as<uint32_t>(), c->nbCap, c->hp.extent * c->hp.extent, c->hp.asph != 0,
-                      c->stream, &c->lc);
+                      c->itemBox.as<float4>(), c->chunkOf.as<int>(), c->stream, &c->lc);
   c->check();
 }
 // CSR offsets of the lists (caller-order transfers) and their total, read
@@ -498,10 +499,13 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   const bool deferCheck = inStep;
   const long n = c->n;
   buildGrid(c);
-  const Grid& g = c->grid;
   int bitsAxis = 0;
-  while ((1 << bitsAxis) < std::max(g.nc[0], std::max(g.nc[1], g.nc[2]))) ++bitsAxis;
-  const int keyBits = std::max(1, 3 * bitsAxis);
+  while ((1 << bitsAxis) < std::max(c->grid.nc[0], std::max(c->grid.nc[1], c->grid.nc[2]))) ++bitsAxis;
+  // one sub-cell Morton level in the sort key while it fits 30 bits
+  c->grid.subShift = bitsAxis <= 9 ? 3 : 0;
+  const Grid& g = c->grid;
+  const int keyBits = std::max(1, 3 * bitsAxis);            // bits of the cell key
+  const int sortBits = keyBits + g.subShift;                // bits of the sort key
   c->keys.ensure(n * sizeof(uint32_t));
   c->keysAlt.ensure(n * sizeof(uint32_t));
   c->vals.ensure(n * sizeof(int));
@@ -517,7 +521,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   int* va = c->valsAlt.as<int>();
   {
     Scope sc(c->prof, "radix_sort");
-    radixSortPairs(k, v, ka, va, n, ((keyBits + 7) / 8) * 8, c->sortWs.p, c->stream, &c->lc);
+    radixSortPairs(k, v, ka, va, n, ((sortBits + 7) / 8) * 8, c->sortWs.p, c->stream, &c->lc);
   }
   c->check();
   {
@@ -543,7 +547,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   CUDA_OK(cudaMemsetAsync(c->cellEnd.p, 0, space * sizeof(int), c->stream));
   {
     Scope sc(c->prof, "cell_ranges");
-    launchCellRanges(k, n, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->stream, &c->lc);
+    launchCellRanges(k, n, g.subShift, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->stream, &c->lc);
   }
   {
     Scope sc(c->prof, "prepare_fp32");
@@ -563,15 +567,19 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   const bool tuned = c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8;
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
+  c->itemBox.ensure(2 * (size_t)n * sizeof(float4));
+  c->chunkOf.ensure(n * sizeof(int));
   auto makeItems = [&](int width) {
     c->itemWidth = width;
     // every non-empty cell adds at most one partial chunk
     c->itemBound = (int)std::min<double>((double)n, (double)(n / width) + cellsTotal);
     Scope sc(c->prof, "neighbor_items");
     long long* pos = c->nbrStart.as<long long>();
-    launchItemFlags(k, n, c->cellStart.as<int>(), width, c->itemFlag.as<int>(), c->stream, &c->lc);
+    launchItemFlags(k, n, g.subShift, c->cellStart.as<int>(), width, c->itemFlag.as<int>(), c->stream, &c->lc);
     scanExclusive<int>(c->itemFlag.as<int>(), pos, n, c->scanWs.p, c->itemCount.as<long long>(), c->stream, &c->lc);
     launchItemFill(c->itemFlag.as<int>(), pos, n, c->items.as<int>(), c->stream, &c->lc);
+    launchItemBoxes(c->items.as<int>(), c->itemCount.as<long long>(), c->itemBound, n, width, c->f32(),
+                    c->itemBox.as<float4>(), c->chunkOf.as<int>(), c->stream, &c->lc);
     c->check();
   };
   makeItems(tuned ? c->tunedWidth : guess);
@@ -585,7 +593,8 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     Scope sc(c->prof, "neighbor_count");
     launchNeighborsWarp(c->F, c->f32(), n, c->items.as<int>(), c->itemBound, c->itemCount.as<long long>(),
                         c->itemWidth, g, c->cellStart.as<int>(), c->cellEnd.as<int>(), c->counts.as<int>(), dMax,
-                        nullptr, 0, c->hp.extent * c->hp.extent, c->hp.asph != 0, c->stream, &c->lc);
+                        nullptr, 0, c->hp.extent * c->hp.extent, c->hp.asph != 0, c->itemBox.as<float4>(),
+                        c->chunkOf.as<int>(), c->stream, &c->lc);
     c->check();
     c->nbCap = capFor(readMaxCount(c));
   }
@@ -1239,8 +1248,8 @@ int sphgpu_destroy(sphgpu_handle c) {
   DBuf* bufs[] = {&c->dTable, &c->bankA, &c->bankB, &c->keys, &c->vals, &c->keysAlt, &c->valsAlt, &c->sortWs,
                   &c->cellStart, &c->cellEnd, &c->counts, &c->nbrStart, &c->nbr, &c->scanWs, &c->pacc,
                   &c->scratch, &c->small, &c->posh, &c->velm, &c->thermo, &c->hten, &c->stage, &c->v12, &c->itemFlag,
-                  &c->items,
-                  &c->dLists, &c->dvq};
+                  &c->items, &c->dLists, &c->dvq, &c->inv, &c->vol32, &c->rkc32, &c->xstage, &c->xidx,
+                  &c->itemBox, &c->chunkOf, &c->itemCount};
   for (auto* b : bufs) b->release();
   for (int k = 0; k < 2; ++k) { c->orig[k].release(); c->list[k].release(); c->cellc[k].release(); }
   if (c->grav) gravityDestroy(c->grav);

@@ -26,6 +26,7 @@ struct Grid {
   double wallHi[3];
   float cellf[3];      // cell edges rounded to FP32 (set on the host: no device conversions)
   float ext2f;         // kernel extent squared, FP32
+  int subShift;        // 3: sort keys carry one sub-cell Morton level below the cell key; 0: none
 };
 
 struct NodeListParams {

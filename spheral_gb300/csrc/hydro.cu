@@ -65,16 +65,24 @@ __global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ k
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double p[3] = {F.f[F_X][i], F.f[F_Y][i], F.f[F_Z][i]};
-  uint32_t c[3];
+  uint32_t c[3], f[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double q = floor((p[a] - g.lo[a]) / g.cell[a]);
+    const double u = (p[a] - g.lo[a]) / g.cell[a];
+    const double q = floor(u);
     long ci = (long)q;
     if (!(q == q)) ci = 0;
+    const bool clamped = ci < 0 || ci >= g.nc[a];
     ci = ci < 0 ? 0 : (ci >= g.nc[a] ? g.nc[a] - 1 : ci);
     c[a] = (uint32_t)ci;
+    // the half of the cell the node is in (order within the cell only)
+    f[a] = 2u * c[a] + ((!clamped && u - q >= 0.5) ? 1u : 0u);
   }
-  keys[i] = morton3(c[0], c[1], c[2]);
+  // With a sub-cell level the key is the Morton key of the half-cells, whose
+  // top bits are the cell's Morton key: nodes stay grouped by cell and within
+  // a cell they are ordered by octant, so consecutive nodes of a cell (a work
+  // chunk or a candidate batch of the neighbour search) sit close together.
+  keys[i] = g.subShift ? morton3(f[0], f[1], f[2]) : morton3(c[0], c[1], c[2]);
   vals[i] = (int)i;
   cellc[i] = c[0] | (c[1] << 10) | (c[2] << 20);
 }
@@ -94,13 +102,13 @@ __global__ void permuteKernel(Fields Fin, Fields Fout, const int* __restrict__ p
   cellOut[k] = cellIn[p];
 }
 
-__global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int* __restrict__ cellStart,
+__global__ void cellRangeKernel(const uint32_t* __restrict__ keys, long n, int shift, int* __restrict__ cellStart,
                                 int* __restrict__ cellEnd) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const uint32_t key = keys[k];
-  if (k == 0 || keys[k - 1] != key) cellStart[key] = (int)k;
-  if (k == n - 1 || keys[k + 1] != key) cellEnd[key] = (int)(k + 1);
+  const uint32_t key = keys[k] >> shift;
+  if (k == 0 || (keys[k - 1] >> shift) != key) cellStart[key] = (int)k;
+  if (k == n - 1 || (keys[k + 1] >> shift) != key) cellEnd[key] = (int)(k + 1);
 }
 
 // Pair criterion of ConnectivityMap::computeConnectivity
@@ -148,13 +156,23 @@ __device__ __noinline__ bool exactTensorCriterion(const Fields& F, const Grid& g
 // candidates; the rest take |H_i r|^2 and |H_j r|^2 in FP32 from the tensor
 // mirror with a per-node band (tensorBand), and only those inside a band
 // take the exact FP64 tensor test.
+//
+// Batch culling: every chunk of up to W consecutive nodes of a cell has a
+// bounding box (itemBoxKernel); a candidate batch whose box is farther from
+// the group's own box than the largest FP32 band edge of the group allows,
+// at the smaller of the two boxes' smallest h^-1, holds no neighbour of any
+// of the group's nodes and is skipped whole (a group-uniform decision).
+// With the sub-cell key order the chunks are compact, so the boxes are
+// small and the far batches of the 27 cells drop out.
 template <bool WRITE, int W, bool TENSOR>
 __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, long n, const int* __restrict__ items,
                                                           int nItems, Grid g, const int* __restrict__ cellStart,
                                                           const int* __restrict__ cellEnd, int* __restrict__ counts,
                                                           uint32_t* __restrict__ nbr, double ext2, float bandA,
                                                           float bandB, int cap, int* __restrict__ maxCount,
-                                                          const long long* __restrict__ dItems) {
+                                                          const long long* __restrict__ dItems,
+                                                          const float4* __restrict__ box,
+                                                          const int* __restrict__ chunkOf) {
   constexpr int G = 128 / W;             // groups per 128-thread block
   __shared__ float4 stage[G][W];         // one candidate batch per group
   constexpr int HW = TENSOR ? 2 * W : 1;
@@ -219,6 +237,13 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
     tHi = dI < 0.5f ? e2t * (1.0f + dI) : FLT_MAX;
   }
   int cnt = 0;
+  // the group's box and the culling threshold on gap^2 min(a)^2: the largest
+  // band edge of the group's nodes, widened against FP32 rounding; no
+  // culling where a band is wide open
+  const float4 gLo = box[2 * item], gHi = box[2 * item + 1];
+  const float delMax = __fmaf_rn(bandA, gHi.w, bandB);
+  const bool cull = delMax < 0.5f;
+  const float cullThr = e2t * (1.0f + delMax) * 1.0001f;
   // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
   uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;
   // first batch of the first non-empty cell, loaded ahead of use
@@ -255,6 +280,21 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         const bool ok = sn + lane < en;
         qn = ok ? P.posh[sn + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
         if (TENSOR && ok) { hn0 = P.hten[2 * (sn + lane)]; hn1 = P.hten[2 * (sn + lane) + 1]; }
+      }
+      if (cull) {
+        // the batch's box in the frame of the group's cell: a candidate at q
+        // (mirrored where the entry crosses a wall) sits at q - o there
+        const int cb = chunkOf[base];
+        const float4 bLo = box[2 * cb], bHi = box[2 * cb + 1];
+        float lx = bLo.x, hx = bHi.x, ly = bLo.y, hy = bHi.y, lz = bLo.z, hz = bHi.z;
+        if (mir & 3u) { lx = cx - bHi.x; hx = cx - bLo.x; }
+        if (mir & 12u) { ly = cy - bHi.y; hy = cy - bLo.y; }
+        if (mir & 48u) { lz = cz - bHi.z; hz = cz - bLo.z; }
+        const float gx = fmaxf(0.0f, fmaxf((lx - ox) - gHi.x, gLo.x - (hx - ox)));
+        const float gy = fmaxf(0.0f, fmaxf((ly - oy) - gHi.y, gLo.y - (hy - oy)));
+        const float gz = fmaxf(0.0f, fmaxf((lz - oz) - gHi.z, gLo.z - (hz - oz)));
+        const float am = fminf(gLo.w, bLo.w);
+        if ((am * am) * (gx * gx + gy * gy + gz * gz) > cullThr) continue;   // group-uniform
       }
       if (TENSOR) {   // band of node j, then H_j seen through the mirrors
         qh1.z = tensorBand(qh1.w, q.w, g);
@@ -417,11 +457,31 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
 
 // Items of the warp search: the first node of every chunk of up to 32 nodes
 // of a cell.  flag pass + scan + fill.
-__global__ void itemFlagKernel(const uint32_t* __restrict__ keys, long n, const int* __restrict__ cellStart,
-                               int width, int* __restrict__ flag) {
+__global__ void itemFlagKernel(const uint32_t* __restrict__ keys, long n, int shift,
+                               const int* __restrict__ cellStart, int width, int* __restrict__ flag) {
   const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  flag[k] = ((k - cellStart[keys[k]]) % width == 0) ? 1 : 0;
+  flag[k] = ((k - cellStart[keys[k] >> shift]) % width == 0) ? 1 : 0;
+}
+// Bounding box of every work chunk (up to `width` consecutive nodes of one
+// cell) in its cell's FP32 coordinates, with the smallest and largest h^-1:
+// box[2k] = (min x, min y, min z, min a), box[2k+1] = (max x, max y, max z,
+// max a).  chunkOf[first node of the chunk] = k.
+__global__ void itemBoxKernel(const int* __restrict__ items, const long long* __restrict__ dItems, long n,
+                              int width, Fields32 P, float4* __restrict__ box, int* __restrict__ chunkOf) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= *dItems) return;
+  const int s = items[k];
+  const uint32_t cell = P.cell[s];
+  float4 lo = P.posh[s], hi = lo;
+  for (int j = s + 1; j < s + width && j < n && P.cell[j] == cell; ++j) {
+    const float4 q = P.posh[j];
+    lo = make_float4(fminf(lo.x, q.x), fminf(lo.y, q.y), fminf(lo.z, q.z), fminf(lo.w, q.w));
+    hi = make_float4(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z), fmaxf(hi.w, q.w));
+  }
+  box[2 * k] = lo;
+  box[2 * k + 1] = hi;
+  chunkOf[s] = (int)k;
 }
 __global__ void itemFillKernel(const int* __restrict__ flag, const long long* __restrict__ pos, long n,
                                int* __restrict__ items) {
@@ -1389,9 +1449,14 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
                                                 sel);
   lc->add(1);
 }
-void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
+void launchCellRanges(const uint32_t* sortedKeys, long n, int shift, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc) {
-  cellRangeKernel<<<gridFor(n, 256), 256, 0, s>>>(sortedKeys, n, cellStart, cellEnd);
+  cellRangeKernel<<<gridFor(n, 256), 256, 0, s>>>(sortedKeys, n, shift, cellStart, cellEnd);
+  lc->add(1);
+}
+void launchItemBoxes(const int* items, const long long* dItems, int nItemsBound, long n, int width, Fields32 P,
+                     float4* box, int* chunkOf, cudaStream_t s, LaunchCounter* lc) {
+  itemBoxKernel<<<gridFor(std::max(1, nItemsBound), 256), 256, 0, s>>>(items, dItems, n, width, P, box, chunkOf);
   lc->add(1);
 }
 // Band of the FP32 pre-filter on e2 = min(a_i, a_j)^2 r^2 around ext^2
@@ -1558,9 +1623,9 @@ void launchCountsOut(const int* counts, const int* orig, double* stage, long n, 
   lc->add(1);
 }
 
-void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int width, int* flag, cudaStream_t s,
-                     LaunchCounter* lc) {
-  itemFlagKernel<<<gridFor(n, 256), 256, 0, s>>>(keys, n, cellStart, width, flag);
+void launchItemFlags(const uint32_t* keys, long n, int shift, const int* cellStart, int width, int* flag,
+                     cudaStream_t s, LaunchCounter* lc) {
+  itemFlagKernel<<<gridFor(n, 256), 256, 0, s>>>(keys, n, shift, cellStart, width, flag);
   lc->add(1);
 }
 void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc) {
@@ -1569,14 +1634,16 @@ void launchItemFill(const int* flag, const long long* pos, long n, int* items, c
 }
 void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
                          int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
-                         uint32_t* nbr, int cap, double ext2, bool tensor, cudaStream_t s, LaunchCounter* lc) {
+                         uint32_t* nbr, int cap, double ext2, bool tensor, const float4* box, const int* chunkOf,
+                         cudaStream_t s, LaunchCounter* lc) {
   float lo, hi;
   neighborBand(g, ext2, lo, hi);
   const long threads = (long)nItems * width;
   const unsigned gb = (unsigned)((threads + 127) / 128);
 #define SPH_NBR(WR, WD, TE)                                                                                        \
   neighborWarpKernel<WR, WD, TE><<<gb, 128, 0, s>>>(F, P, n, items, nItems, g, cellStart, cellEnd, counts,        \
-                                                    WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount, dItems)
+                                                    WR ? nbr : nullptr, ext2, lo, hi, WR ? cap : 0, maxCount, dItems, \
+                                                    box, chunkOf)
   if (tensor) {
     if (nbr) {
       if (width == 8) SPH_NBR(true, 8, true); else if (width == 16) SPH_NBR(true, 16, true); else SPH_NBR(true, 32, true);

@@ -42,19 +42,24 @@ void launchPermute(const Fields& Fin, Fields Fout, const int* perm, const int* o
 // The limited Q's DvDx <- the hydro DvDx; and its FP32 mirror (3 float4 per node).
 void launchCopyQGradient(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 void launchQGradient32(Fields F, float4* dvq, long n, cudaStream_t s, LaunchCounter* lc);
-void launchCellRanges(const uint32_t* sortedKeys, long n, int* cellStart, int* cellEnd, cudaStream_t s,
+// shift: sub-cell key bits below the cell key (Grid::subShift).
+void launchCellRanges(const uint32_t* sortedKeys, long n, int shift, int* cellStart, int* cellEnd, cudaStream_t s,
                       LaunchCounter* lc);
+// Bounding boxes of the work chunks (for the batch culling of the search).
+void launchItemBoxes(const int* items, const long long* dItems, int nItemsBound, long n, int width, Fields32 P,
+                     float4* box, int* chunkOf, cudaStream_t s, LaunchCounter* lc);
 // Group-cooperative neighbour search over items (first node of each chunk of
 // up to `width` nodes of a cell).
 // width: nodes per work item of the group-cooperative search (8, 16 or 32).
-void launchItemFlags(const uint32_t* keys, long n, const int* cellStart, int width, int* flag, cudaStream_t s,
-                     LaunchCounter* lc);
+void launchItemFlags(const uint32_t* keys, long n, int shift, const int* cellStart, int width, int* flag,
+                     cudaStream_t s, LaunchCounter* lc);
 void launchItemFill(const int* flag, const long long* pos, long n, int* items, cudaStream_t s, LaunchCounter* lc);
 // nItems: an upper bound on the item count (sizes the grid); *dItems (device)
 // holds the count itself.
 void launchNeighborsWarp(const Fields& F, Fields32 P, long n, const int* items, int nItems, const long long* dItems,
                          int width, Grid g, const int* cellStart, const int* cellEnd, int* counts, int* maxCount,
-                         uint32_t* nbr, int cap, double ext2, bool tensor, cudaStream_t s, LaunchCounter* lc);
+                         uint32_t* nbr, int cap, double ext2, bool tensor, const float4* box, const int* chunkOf,
+                         cudaStream_t s, LaunchCounter* lc);
 
 // Sweeps ---------------------------------------------------------------------
 void launchSumDensity(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
