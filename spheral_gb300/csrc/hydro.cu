@@ -331,33 +331,34 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         const bool own = dcode == 0 && base == k0;   // group-uniform: here candidate `lane` is node i
         bool amb = false;
         if (!WRITE || cnt + nval <= cap) {
-          // The candidates of the batch set bits of two masks (inside the
-          // band's lower edge: a neighbour; inside its upper edge: near);
-          // the neighbours are written after the batch in candidate order,
-          // so the loop body carries no store.
-          uint32_t hit = 0u, near = 0u;
+          uint32_t* o = WRITE ? out + (size_t)cnt * 32 : nullptr;
+          int c = 0;
+          if (!own) {
 #pragma unroll 4
-          for (int u = 0; u < nval; ++u) {
-            const float4 cq = stage[wib][u];
-            const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
-            const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
-            const uint32_t bit = 1u << u;
-            if (e2 < bandLo) hit |= bit;
-            if (e2 <= bandHi) near |= bit;
-          }
-          if (own) hit &= ~(1u << lane);   // node i itself (candidate `lane` of its own batch)
-          amb |= (near & ~hit & ~(own ? (1u << lane) : 0u)) != 0u;
-          if (WRITE) {
-            uint32_t* o = out + (size_t)cnt * 32;
-            uint32_t h = hit;
-            while (h) {
-              const int u = __ffs(h) - 1;
-              h &= h - 1u;
-              *o = ebase + (uint32_t)u;
-              o += 32;
+            for (int u = 0; u < nval; ++u) {
+              const float4 cq = stage[wib][u];
+              const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+              const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+              amb |= (e2 >= bandLo) & (e2 <= bandHi);
+              if (e2 < bandLo) {
+                if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
+                ++c;
+              }
+            }
+          } else {
+#pragma unroll 4
+            for (int u = 0; u < nval; ++u) {
+              const float4 cq = stage[wib][u];
+              const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
+              const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
+              amb |= (e2 >= bandLo) & (e2 <= bandHi);
+              if ((e2 < bandLo) & (u != lane)) {
+                if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
+                ++c;
+              }
             }
           }
-          cnt += __popc(hit);
+          cnt += c;
         } else {   // this batch may reach the capacity: count past it, store below it
           for (int u = 0; u < nval; ++u) {
             const float4 cq = stage[wib][u];

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _box(**kw):
-    p = problems.stretched_box(nx=14, ny=11, nz=9, seed=81)
+    p = problems.stretched_box(nx=18, ny=15, nz=12, seed=81)
     p.config.update(smoothing_scale="asph", **kw)
     return p
 
