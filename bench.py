@@ -426,6 +426,7 @@ def run_ours(args, ws, rank, local, dist):
     eng.profile(False)
     ms = max_over_ranks(dist, ms)
     pair_variant = eng.pair_variant()[0] if f32 else None
+    nb_width = eng.neighbor_width()   # lanes per group of the neighbour search (autotuned)
     e1 = eng.conservation()
     energy_err = abs(e1[7] - e0[7]) / abs(e0[7])
     p_scale = float(np.sum(prob.mass * np.linalg.norm(prob.vel, axis=1)))   # sum m |v| of the initial state
@@ -555,6 +556,7 @@ def run_ours(args, ws, rank, local, dist):
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
         "pair_variant": pair_variant,
+        "neighbor_width": nb_width,
         "roofline": {"bound": f"{pipe}_pipe", "achieved": tflops, "peak": pipe_peak, "unit": "TFLOP/s",
                      "frac": (tflops / pipe_peak) if tflops else None,
                      "traffic": (TRAFFIC_BYTES_PER_PAIR[pipe] * pairs_per_launch
