@@ -329,9 +329,18 @@ int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
 int sphgpu_set_pair_variant(sphgpu_handle h, int variant);
 int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
 /* Lanes per work group of the neighbour search (8, 16 or 32), picked by
- * timing each width once per problem size (the lists are the same for every
- * width).  No reference counterpart (tuning only). */
+ * timing each width once per problem size; sphgpu_set_neighbor_width pins
+ * one (taking effect at the next list build), or 0 to re-enable the
+ * autotuner.  The lists, entry order included, are the same for every
+ * width.  No reference counterpart (tuning only). */
+int sphgpu_set_neighbor_width(sphgpu_handle h, int width);
 int sphgpu_get_neighbor_width(sphgpu_handle h, int* width);
+/* Batch depth of the mixed-mode compatible-energy sweep (slots whose loads
+ * are issued together), autotuned like the pair variant; -1 re-enables the
+ * autotuner.  Every depth sums in slot order, so the energies are the same
+ * for every variant.  No reference counterpart (tuning only). */
+int sphgpu_set_energy_variant(sphgpu_handle h, int variant);
+int sphgpu_get_energy_variant(sphgpu_handle h, int* variant, int* nvariants);
 
 /* Checkpoint and restart.  Replaces: SPHBase::dumpState / restoreState
  * (src/SPH/SPHBase.cc:711-768) with the integrator's time, last dt and cycle,

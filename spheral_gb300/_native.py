@@ -109,6 +109,9 @@ SIGNATURES = {
     "sphgpu_restore": (_i, [_vp, _vp, ctypes.c_size_t]),
     "sphgpu_get_pair_variant": (_i, [_vp, _ip, _ip]),
     "sphgpu_get_neighbor_width": (_i, [_vp, _ip]),
+    "sphgpu_set_neighbor_width": (_i, [_vp, _i]),
+    "sphgpu_set_energy_variant": (_i, [_vp, _i]),
+    "sphgpu_get_energy_variant": (_i, [_vp, _ip, _ip]),
     "sphgpu_get_field": (_i, [_vp, _cp, _dp, _ip]),
     "sphgpu_set_field": (_i, [_vp, _cp, _dp]),
     "sphgpu_get_pairs": (_i, [_vp, _ip, _ip, _ip, _lp]),

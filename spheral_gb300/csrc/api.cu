@@ -173,8 +173,10 @@ struct sphgpu_ctx {
   int itemBound = 0;         // upper bound on the number of work items
   int energyVariant = -1;    // autotuned batch depth of the FP32 energy sweep
   long energyTunedN = 0;
+  bool energyPinned = false; // batch depth set by the caller
   DBuf itemBox, chunkOf;     // bounding boxes of the search's work chunks, chunk of each chunk's first node
   int tunedWidth = 0;        // autotuned group width (0: not tuned yet)
+  int pinnedWidth = 0;       // group width set by the caller (0: autotuned)
   long widthTunedN = 0;      // node count it was tuned at
   DBuf itemCount;            // device: number of work items
   bool capCheckPending = false, totalPending = false;
@@ -564,7 +566,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   const double cellsTotal = (double)g.nc[0] * g.nc[1] * g.nc[2];
   const double occupancy = (double)n / cellsTotal;
   const int guess = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
-  const bool tuned = c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8;
+  const bool tuned = c->pinnedWidth > 0 || (c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8);
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
   c->itemBox.ensure(2 * (size_t)n * sizeof(float4));
@@ -582,7 +584,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
                     c->itemBox.as<float4>(), c->chunkOf.as<int>(), c->stream, &c->lc);
     c->check();
   };
-  makeItems(tuned ? c->tunedWidth : guess);
+  makeItems(c->pinnedWidth > 0 ? c->pinnedWidth : (tuned ? c->tunedWidth : guess));
   if (c->nbCapNext > 0) {   // adopt a smaller capacity decided at the previous build
     c->nbCap = c->nbCapNext;
     c->nbCapNext = 0;
@@ -945,7 +947,7 @@ double step(sphgpu_ctx* c, double maxTime) {
     Scope sc(c->prof, "energy");
     if (c->fp32()) {
       c->v12.ensure(c->n * 2 * sizeof(float4));
-      if (c->energyVariant < 0 || std::labs(c->n - c->energyTunedN) > c->energyTunedN / 8) {
+      if (!c->energyPinned && (c->energyVariant < 0 || std::labs(c->n - c->energyTunedN) > c->energyTunedN / 8)) {
         // Autotuner: time each batch depth once per problem size.  The trial
         // launches take dt = 0, so they add nothing to the energies; the
         // real launch below recomputes everything they wrote.
@@ -1614,6 +1616,29 @@ int sphgpu_set_pair_variant(sphgpu_handle c, int variant) {
   if (variant < -1 || variant >= kPairVariants) throw Error(SPHGPU_E_ARG, "pair variant out of range");
   c->pairVariant = variant;
   c->pinnedVariant = variant >= 0;
+  API_END(c)
+}
+
+int sphgpu_set_neighbor_width(sphgpu_handle c, int width) {
+  API_BEGIN(c)
+  if (width != 0 && width != 8 && width != 16 && width != 32) throw Error(SPHGPU_E_ARG, "group width not 0, 8, 16 or 32");
+  c->pinnedWidth = width;
+  if (width == 0) c->tunedWidth = 0;   // time the widths again at the next build
+  API_END(c)
+}
+
+int sphgpu_set_energy_variant(sphgpu_handle c, int variant) {
+  API_BEGIN(c)
+  if (variant < -1 || variant >= kEnergyVariants) throw Error(SPHGPU_E_ARG, "energy variant out of range");
+  c->energyPinned = variant >= 0;
+  c->energyVariant = variant;
+  API_END(c)
+}
+
+int sphgpu_get_energy_variant(sphgpu_handle c, int* variant, int* nvariants) {
+  API_BEGIN(c)
+  if (variant) *variant = c->energyVariant;
+  if (nvariants) *nvariants = kEnergyVariants;
   API_END(c)
 }
 

@@ -322,13 +322,15 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         // Isotropic H.  The common path takes no branch per candidate: a
         // candidate below the band is a neighbour outright, one inside the
         // band only raises a flag, and the (rare) flagged batches are
-        // rescanned with the exact FP64 criterion afterwards, their
-        // neighbours appended behind the batch's others.  The capacity is
+        // written again in candidate order with the exact FP64 criterion
+        // for the band candidates, so a list is the same for every group
+        // width (and so are the rounding of its sums).  The capacity is
         // checked once per batch unless the batch could overflow it, and
         // the self test runs only in the group's own batch of the home cell.
         const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
         const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
         const bool own = dcode == 0 && base == k0;   // group-uniform: here candidate `lane` is node i
+        const int cnt0 = cnt;
         bool amb = false;
         if (!WRITE || cnt + nval <= cap) {
           uint32_t* o = WRITE ? out + (size_t)cnt * 32 : nullptr;
@@ -371,21 +373,25 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
             }
           }
         }
-        if (amb) {   // guard band: the exact FP64 criterion for the flagged candidates
+        if (amb) {   // guard band: the batch again, band candidates by the exact FP64 criterion
+          cnt = cnt0;
           for (int u = 0; u < nval; ++u) {
             const float4 cq = stage[wib][u];
             const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
             const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
-            if (e2 >= bandLo && e2 <= bandHi && u != self) {
+            if (e2 > bandHi || u == self) continue;
+            bool in = e2 < bandLo;
+            if (!in) {
               const int j = base + u;
               double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
               imagePos(g, imageCode(g, hc, dcode), xjd, yjd, zjd);
               const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
                            qz = __dsub_rn(F.f[F_Z][i], zjd);
-              if (eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2) {
-                if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
-                ++cnt;
-              }
+              in = eta2Exact(F.f[F_HINV][i], qx, qy, qz) <= ext2 || eta2Exact(F.f[F_HINV][j], qx, qy, qz) <= ext2;
+            }
+            if (in) {
+              if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
+              ++cnt;
             }
           }
         }
@@ -394,11 +400,12 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         // Tensor H: the scalar pre-filter (h^-1 the smallest eigenvalue)
         // rejects the far candidates, the rest take the FP32 tensor test on
         // each side with its own band; candidates inside a band only raise a
-        // flag, and flagged batches are rescanned with the exact FP64 tensor
-        // criterion afterwards (their neighbours appended behind the rest).
+        // flag, and flagged batches are written again in candidate order with
+        // the exact FP64 tensor criterion for the flagged candidates.
         const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
         // this node shifted by the cell offset: r = (x_i + o) - x_j
         const float px = __fadd_rn(pi.x, ox), py = __fadd_rn(pi.y, oy), pz = __fadd_rn(pi.z, oz);
+        const int cnt0 = cnt;
         bool amb = false;
 #pragma unroll 4
         for (int u = 0; u < nval; ++u) {
@@ -419,8 +426,9 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
             }
           }
         }
-        if (amb) {   // guard band: the exact FP64 tensor criterion for the flagged candidates
+        if (amb) {   // guard band: the batch again, flagged candidates by the exact FP64 tensor criterion
           const int code = imageCode(g, hc, dcode);
+          cnt = cnt0;
           for (int u = 0; u < nval; ++u) {
             const float4 cq = stage[wib][u];
             const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
@@ -431,13 +439,16 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
             const float e2j = eta2Sym32(h0, h1, rx, ry, rz);
             const float jLo = h1.z < 0.5f ? e2t * (1.0f - h1.z) : -1.0f;
             const float jHi = h1.z < 0.5f ? e2t * (1.0f + h1.z) : FLT_MAX;
-            if ((e2i <= tLo) | (e2j <= jLo) | ((e2i >= tHi) & (e2j >= jHi))) continue;   // settled in FP32
-            const int j = base + u;
-            double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
-            imagePos(g, code, xjd, yjd, zjd);
-            const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
-                         qz = __dsub_rn(F.f[F_Z][i], zjd);
-            if (exactTensorCriterion(F, g, i, j, code, qx, qy, qz, ext2)) {
+            bool in = (e2i <= tLo) | (e2j <= jLo);
+            if (!in && !((e2i >= tHi) & (e2j >= jHi))) {
+              const int j = base + u;
+              double xjd = F.f[F_X][j], yjd = F.f[F_Y][j], zjd = F.f[F_Z][j];
+              imagePos(g, code, xjd, yjd, zjd);
+              const double qx = __dsub_rn(F.f[F_X][i], xjd), qy = __dsub_rn(F.f[F_Y][i], yjd),
+                           qz = __dsub_rn(F.f[F_Z][i], zjd);
+              in = exactTensorCriterion(F, g, i, j, code, qx, qy, qz, ext2);
+            }
+            if (in) {
               if (WRITE && cnt < cap) out[(size_t)cnt * 32] = ebase + (uint32_t)u;
               ++cnt;
             }

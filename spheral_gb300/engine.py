@@ -188,6 +188,19 @@ class Engine:
     def set_pair_variant(self, v):
         self._chk(self.L.sphgpu_set_pair_variant(self.h, v))
 
+    def set_neighbor_width(self, w):
+        """Pin the search group width (8, 16 or 32) from the next list build; 0 re-enables the autotuner."""
+        self._chk(self.L.sphgpu_set_neighbor_width(self.h, w))
+
+    def energy_variant(self):
+        """(batch depth variant in use, number of variants) of the mixed-mode energy sweep."""
+        v, nv = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.L.sphgpu_get_energy_variant(self.h, ctypes.byref(v), ctypes.byref(nv)))
+        return v.value, nv.value
+
+    def set_energy_variant(self, v):
+        self._chk(self.L.sphgpu_set_energy_variant(self.h, v))
+
     @staticmethod
     def ensemble_advance(engines, nsteps, max_time=1.0e300, nthreads=0):
         """nsteps steps of every engine at once (sphgpu_ensemble_advance):
