@@ -177,6 +177,13 @@ struct sphgpu_ctx {
   DBuf itemBox, chunkOf;     // bounding boxes of the search's work chunks, chunk of each chunk's first node
   int tunedWidth = 0;        // autotuned group width (0: not tuned yet)
   int pinnedWidth = 0;       // group width set by the caller (0: autotuned)
+  // The autotuners time their options at the first use for a problem size
+  // and once more kRetuneAfter uses later, when the state has moved away
+  // from its initial conditions (ASPH H fields, for one, relax in the first
+  // steps and change which search width is fastest).
+  long listBuilds = 0, widthRetuneAt = -1;
+  long pairEvals = 0, pairRetuneAt = -1;
+  long energyEvals = 0, energyRetuneAt = -1;
   long widthTunedN = 0;      // node count it was tuned at
   DBuf itemCount;            // device: number of work items
   bool capCheckPending = false, totalPending = false;
@@ -566,7 +573,10 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
   const double cellsTotal = (double)g.nc[0] * g.nc[1] * g.nc[2];
   const double occupancy = (double)n / cellsTotal;
   const int guess = occupancy >= 24.0 ? 32 : (occupancy >= 12.0 ? 16 : 8);
-  const bool tuned = c->pinnedWidth > 0 || (c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8);
+  ++c->listBuilds;
+  const bool retuneWidth = c->widthRetuneAt >= 0 && c->listBuilds >= c->widthRetuneAt;
+  const bool tuned = c->pinnedWidth > 0 ||
+                     (!retuneWidth && c->tunedWidth > 0 && std::labs(n - c->widthTunedN) <= c->widthTunedN / 8);
   c->itemFlag.ensure(n * sizeof(int));
   c->items.ensure(n * sizeof(int));
   c->itemBox.ensure(2 * (size_t)n * sizeof(float4));
@@ -626,6 +636,7 @@ void buildNeighbors(sphgpu_ctx* c, bool inStep = false) {
     cudaEventDestroy(e1);
     c->tunedWidth = bestW;
     c->widthTunedN = n;
+    c->widthRetuneAt = retuneWidth ? -1 : c->listBuilds + kRetuneAfter;
     if (bestW != c->itemWidth) makeItems(bestW);
   }
   writeLists(c);
@@ -745,7 +756,9 @@ void evalDerivs(sphgpu_ctx* c) {
     // Autotuner: time each register/occupancy variant of the pair kernel once
     // per problem size (the kernel is a pure function of its inputs, so the
     // trial launches leave the same results) and keep the fastest.
-    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n)) {
+    ++c->pairEvals;
+    const bool retune = c->pairRetuneAt >= 0 && c->pairEvals >= c->pairRetuneAt;
+    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n || retune)) {
       cudaEvent_t e0, e1;
       CUDA_OK(cudaEventCreate(&e0));
       CUDA_OK(cudaEventCreate(&e1));
@@ -768,6 +781,7 @@ void evalDerivs(sphgpu_ctx* c) {
       cudaEventDestroy(e1);
       c->pairVariant = bestV;
       c->tunedN = c->n;
+      c->pairRetuneAt = retune ? -1 : c->pairEvals + kRetuneAfter;
     }
     Scope sc(c->prof, "pair_fp32");
     launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
@@ -947,7 +961,10 @@ double step(sphgpu_ctx* c, double maxTime) {
     Scope sc(c->prof, "energy");
     if (c->fp32()) {
       c->v12.ensure(c->n * 2 * sizeof(float4));
-      if (!c->energyPinned && (c->energyVariant < 0 || std::labs(c->n - c->energyTunedN) > c->energyTunedN / 8)) {
+      ++c->energyEvals;
+      const bool retune = c->energyRetuneAt >= 0 && c->energyEvals >= c->energyRetuneAt;
+      if (!c->energyPinned &&
+          (c->energyVariant < 0 || std::labs(c->n - c->energyTunedN) > c->energyTunedN / 8 || retune)) {
         // Autotuner: time each batch depth once per problem size.  The trial
         // launches take dt = 0, so they add nothing to the energies; the
         // real launch below recomputes everything they wrote.
@@ -972,6 +989,7 @@ double step(sphgpu_ctx* c, double maxTime) {
         cudaEventDestroy(e1);
         c->energyVariant = bestV;
         c->energyTunedN = c->n;
+        c->energyRetuneAt = retune ? -1 : c->energyEvals + kRetuneAfter;
       }
       launchCompatibleEnergyFP32(c->F, c->n, c->grid, c->nl(), c->pacc.as<float>(), c->v12.as<float4>(),
                                  c->v12.as<float4>() + c->n, dt, c->energyVariant, c->stream, &c->lc);

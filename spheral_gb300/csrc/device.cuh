@@ -24,6 +24,11 @@ __device__ __forceinline__ void sumAdd(float& s, float& c, float x, int plain) {
   else kahanAdd(s, c, x);
 }
 
+// eta from eta^2 in the FP32 sweeps: eta^2 times its reciprocal square root
+// (the hardware approximation; eta^2 = 0 gives 0).  The pair kernel forms
+// its eta_i and eta_j the same way.
+__device__ __forceinline__ float etaFromSq(float e2) { return __fmul_rn(e2, rsqrtf(fmaxf(e2, 1.0e-30f))); }
+
 // Velocity of a mirror image: the components along the mirrored axes flip
 // (mir: per-axis bits of the entry's cell-offset code that cross a wall).
 __device__ __forceinline__ void mirrorVel(uint32_t mir, float& vx, float& vy, float& vz) {

@@ -319,12 +319,13 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
       // the home cell's own batch contains node i itself
       const int self = (dcode == 0 && i >= base && i < base + nval) ? (int)(i - base) : -1;
       if (!TENSOR && active) {
-        // Isotropic H.  The common path takes no branch per candidate: a
-        // candidate below the band is a neighbour outright, one inside the
-        // band only raises a flag, and the (rare) flagged batches are
-        // written again in candidate order with the exact FP64 criterion
-        // for the band candidates, so a list is the same for every group
-        // width (and so are the rounding of its sums).  The capacity is
+        // Isotropic H.  The common path takes no branch per candidate: every
+        // candidate up to the top of the band is stored, and the largest
+        // stored e2 tells whether one of them sits inside the band; the
+        // (rare) batches that hold one are written again in candidate order
+        // with the exact FP64 criterion for the band candidates, so a list
+        // is the same for every group width (and so is the rounding of its
+        // sums).  The capacity is
         // checked once per batch unless the batch could overflow it, and
         // the self test runs only in the group's own batch of the home cell.
         const uint32_t ebase = (uint32_t)base | ((uint32_t)dcode << kIndexBits);
@@ -335,16 +336,17 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
         if (!WRITE || cnt + nval <= cap) {
           uint32_t* o = WRITE ? out + (size_t)cnt * 32 : nullptr;
           int c = 0;
+          float mx = -1.0f;   // largest e2 stored
           if (!own) {
 #pragma unroll 4
             for (int u = 0; u < nval; ++u) {
               const float4 cq = stage[wib][u];
               const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
               const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
-              amb |= (e2 >= bandLo) & (e2 <= bandHi);
-              if (e2 < bandLo) {
+              if (e2 <= bandHi) {
                 if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
                 ++c;
+                mx = fmaxf(mx, e2);
               }
             }
           } else {
@@ -353,13 +355,14 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
               const float4 cq = stage[wib][u];
               const float rx = __fsub_rn(px, cq.x), ry = __fsub_rn(py, cq.y), rz = __fsub_rn(pz, cq.z);
               const float e2 = fminf(ai2, cq.w) * (rx * rx + ry * ry + rz * rz);
-              amb |= (e2 >= bandLo) & (e2 <= bandHi);
-              if ((e2 < bandLo) & (u != lane)) {
+              if ((e2 <= bandHi) & (u != lane)) {
                 if (WRITE) o[(size_t)c * 32] = ebase + (uint32_t)u;
                 ++c;
+                mx = fmaxf(mx, e2);
               }
             }
           }
+          amb = mx >= bandLo;
           cnt += c;
         } else {   // this batch may reach the capacity: count past it, store below it
           for (int u = 0; u < nval; ++u) {

@@ -533,8 +533,10 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
                                                      TableDev t, HydroParams hp) {
   __shared__ float4 ta[kMaxTable / 3];
   __shared__ float2 tb[kMaxTable / 3];
+  __shared__ float4 sOff[64];
   const int nint = hp.tableN1 + 1;
   for (int k = threadIdx.x; k < nint; k += blockDim.x) { ta[k] = t.p32a[k]; tb[k] = t.p32b[k]; }
+  fillCellOffsets(sOff, g.cellf[0], g.cellf[1], g.cellf[2]);
   __syncthreads();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -568,8 +570,14 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
     if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
     const int dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
-    relSep(pi, pj, dcode, mm, cx, cy, cz, rx, ry, rz);
-    const float eta = TENSOR ? sqrtf(eta2Sym32(hi0, hi1, rx, ry, rz)) : ai * sqrtf(rx * rx + ry * ry + rz * rz);
+    relSepTab(pi, pj, dcode, mm, cx, cy, cz, sOff, rx, ry, rz);
+    float eta;
+    if (TENSOR) {
+      eta = etaFromSq(eta2Sym32(hi0, hi1, rx, ry, rz));
+    } else {
+      const float ex = ai * rx, ey = ai * ry, ez = ai * rz;
+      eta = etaFromSq(__fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex))));
+    }
     float w, gr;
     lookupPacked(ta, tb, N1, invStep, eta, extent, w, gr);
     sumAdd(ws, wc, w, hp.plainSums);

@@ -103,13 +103,20 @@ def sod(nx1=80, ny1=20, nPerh=1.51, cfl=0.25):
                    meta=dict(nx1=nx1, ny1=ny1, L=L))
 
 
-def kelvin_helmholtz(n1=112, n2=None, jitter=0.05, seed=1, nPerh=1.51):
+def kelvin_helmholtz(n1=112, n2=None, jitter=0.05, seed=1, nPerh=1.51, smooth=0.0):
     """Periodic unit-cube Kelvin-Helmholtz slab: |y - 0.5| < 0.25 has rho = 2,
     vx = +0.5 on a lattice of n2 per unit length; outside rho = 1, vx = -0.5
     on n1 per unit length; vy = 0.01 sin(4 pi x); P = 2.5.  n2 defaults to the
     even integer nearest n1 2^(1/3) (spacing ratio ~2^(-1/3), near-equal
     masses set so the densities are exact).  Positions get Gaussian jitter of
-    jitter x spacing (seed)."""
+    jitter x spacing (seed).
+
+    smooth > 0 tapers density and shear velocity across the two interfaces
+    as the reference's own 3-D test does
+    (tests/functional/Hydro/KelvinHelmholtz/KelvinHelmholtz-3d.py:246-270):
+    at distance d from the nearest interface the jump is relaxed by
+    exp(-d / smooth) from each side towards the mean (rho 1.5, vx 0), node
+    masses follow rho / rho_nominal and the energies keep P = 2.5."""
     if n2 is None:
         n2 = int(round(n1 * 2.0 ** (1.0 / 3.0) / 2.0)) * 2
     rng = np.random.default_rng(seed)
@@ -129,12 +136,20 @@ def kelvin_helmholtz(n1=112, n2=None, jitter=0.05, seed=1, nPerh=1.51):
     vel[:no, 0] = -0.5
     vel[no:, 0] = 0.5
     vel[:, 1] = 0.01 * np.sin(4.0 * math.pi * pos[:, 0])
+    if smooth > 0.0:
+        d = np.minimum(np.abs(pos[:, 1] - 0.25), np.abs(pos[:, 1] - 0.75))
+        f = 0.5 * np.exp(-d / smooth)
+        sign = np.concatenate([np.full(no, 1.0), np.full(ns, -1.0)])   # outer rises, slab falls
+        new = rho + sign * f
+        mass = mass * new / rho
+        rho = new
+        vel[:, 0] += sign * f
     eps = 2.5 / ((GAMMA - 1.0) * rho)
     cfg = dict(cfl=0.5, compatible_energy=True, gradh_correction=False, xsph=False, correct_velocity_gradient=True,
                Cl=1.0, Cq=1.0, dt_min=1.0e-8, dt_max=0.1, dt_growth=2.0, last_dt=1.0e-4)
     nls = [dict(nPerh=nPerh, hmin=1e-4, hmax=0.5, rhoMin=1e-10, rhoMax=1e10, gamma=GAMMA)]
     return Problem("kelvin_helmholtz", pos, vel, mass, rho, eps, h, None, nls, periodic_box_boundaries(), cfg,
-                   meta=dict(n1=n1, n2=n2, seed=seed))
+                   meta=dict(n1=n1, n2=n2, seed=seed, smooth=smooth))
 
 
 def evrard(n=1048576, seed=2, nPerh=1.51, G=1.0, softening=0.01, opening=0.5):
