@@ -453,6 +453,7 @@ void buildGrid(sphgpu_ctx* c) {
     g.lo[a] = lo;
     g.hi[a] = hi;
     g.cell[a] = cell;
+    g.inv2[a] = 2.0 / cell;
     g.cellf[a] = (float)cell;
     g.nc[a] = nc;
     if (g.kindLo[a] != AXIS_PERIODIC) {   // open sides: the grid origin follows the data

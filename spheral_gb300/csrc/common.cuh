@@ -19,6 +19,7 @@ struct Grid {
   double lo[3];        // grid origin per axis
   double hi[3];        // periodic / wall extents (hi of the domain)
   double cell[3];      // cell edge per axis
+  double inv2[3];      // 2 / cell edge (half-cells per unit length; set on the host)
   int nc[3];           // cells per axis
   int kindLo[3];       // AxisKind of the low side
   int kindHi[3];       // AxisKind of the high side

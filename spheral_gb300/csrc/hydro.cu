@@ -68,15 +68,19 @@ __global__ void cellKeyKernel(Fields F, long n, Grid g, uint32_t* __restrict__ k
   uint32_t c[3], f[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double u = (p[a] - g.lo[a]) / g.cell[a];
-    const double q = floor(u);
-    long ci = (long)q;
-    if (!(q == q)) ci = 0;
+    // position in half-cells, rounded down by the conversion itself: three
+    // FP64-pipe instructions per axis (no division; the FP64 pipe is the
+    // narrow one).  A node within rounding of a cell face may land in either
+    // cell: the cells exceed the kernel support by a relative 1e-9, far
+    // above that rounding.  NaN converts to the most negative value and is
+    // clamped into cell 0.
+    const long long hc = __double2ll_rd(__dmul_rn(__dsub_rn(p[a], g.lo[a]), g.inv2[a]));
+    long long ci = hc >> 1;
     const bool clamped = ci < 0 || ci >= g.nc[a];
     ci = ci < 0 ? 0 : (ci >= g.nc[a] ? g.nc[a] - 1 : ci);
     c[a] = (uint32_t)ci;
     // the half of the cell the node is in (order within the cell only)
-    f[a] = 2u * c[a] + ((!clamped && u - q >= 0.5) ? 1u : 0u);
+    f[a] = 2u * c[a] + ((!clamped && (hc & 1)) ? 1u : 0u);
   }
   // With a sub-cell level the key is the Morton key of the half-cells, whose
   // top bits are the cell's Morton key: nodes stay grouped by cell and within
@@ -1232,6 +1236,12 @@ __global__ void eosKernel(Fields F, const int* __restrict__ list, long n, const 
 // ReflectingBoundary.cc:465-473): nodes strictly outside a plane are mapped
 // back; reflecting walls also mirror the velocity.
 __device__ __forceinline__ bool fuzzyZero(double x) { return fabs(x) <= 1.0e-15 * fmax(1.0, fabs(x)); }
+// A signed integer with the order of the double x (for non-NaN x; -0 sorts
+// just below +0, which only sends a node at a wall to the exact test).
+__device__ __forceinline__ long long orderKey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
 // tensor: the H of a node mapped back through a reflecting wall is reflected
 // too (PlanarBoundary::updateViolationNodes -> enforceBoundary(Hfield),
 // (R H R).Symmetric()).
@@ -1250,6 +1260,10 @@ __global__ void enforceKernel(Fields F, long n, Grid g, int tensor) {
   for (int a = 0; a < 3; ++a) {
     const double lo = g.wallLo[a], hi = g.wallHi[a];
     double p = P[a][i];
+    // Integer pre-test on order-preserving keys of the bit patterns: a node
+    // strictly inside (lo, hi) needs nothing, and the FP64 tests below (the
+    // FP64 pipe is narrow) run only for the few on or beyond a wall.
+    if (orderKey(p) > orderKey(lo) && orderKey(p) < orderKey(hi)) continue;
     const double sdLo = p - lo, sdHi = hi - p;
     if (g.kindLo[a] == AXIS_PERIODIC) {
       if (sdLo < 0.0 && !fuzzyZero(sdLo)) p = imageCoord(p, 2, AXIS_PERIODIC, AXIS_PERIODIC, lo, hi);

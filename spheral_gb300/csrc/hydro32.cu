@@ -32,9 +32,11 @@ __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   P.posh[i] = make_float4((float)(F.f[F_X][i] - ox), (float)(F.f[F_Y][i] - oy), (float)(F.f[F_Z][i] - oz),
                           (float)F.f[F_HINV][i]);
   P.velm[i] = make_float4((float)F.f[F_VX][i], (float)F.f[F_VY][i], (float)F.f[F_VZ][i], (float)F.f[F_MASS][i]);
-  const double om = F.f[F_OMEGA][i];
+  // omega / (omega^2 + 1e-30) in FP32: an FP64 division here would cost
+  // more on the narrow FP64 pipe than the rest of the kernel
+  const float om = (float)F.f[F_OMEGA][i];
   P.thermo[i] = make_float4((float)F.f[F_RHO][i], (float)F.f[F_P][i], (float)F.f[F_CS][i],
-                            (float)(om / (om * om + 1.0e-30)));
+                            om / (om * om + 1.0e-30f));
   if (P.hten) writeTensorMirror(F, P, i);
   if (P.vol) P.vol[i] = (float)F.f[F_VOL][i];
 }
