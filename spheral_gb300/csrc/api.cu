@@ -354,6 +354,10 @@ void refreshParams(sphgpu_ctx* c) {
   if (c->haveTable) hp.WnPerh = tableW(c, 1.0 / c->lists[0].nPerh);
   // NodeList table in device memory, one per handle (handles on different
   // streams never share it).
+  for (auto& L : c->lists) {
+    L.gm1 = L.gamma - 1.0;
+    L.ggm1 = L.gamma * L.gm1;
+  }
   c->dLists.ensure(sizeof(c->lists));
   CUDA_OK(cudaMemcpyAsync(c->dLists.p, c->lists, sizeof(c->lists), cudaMemcpyHostToDevice, c->stream));
   hp.lists = c->dLists.as<NodeListParams>();

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "convert.cuh"
+
 namespace sph {
 
 // Neighbour entries: 26-bit sorted node index + 6-bit image code (2 bits per axis).
@@ -34,6 +36,7 @@ struct NodeListParams {
   double nPerh, hmin, hmax, rhoMin, rhoMax, gamma, minP, maxP;
   double hminInv, hmaxInv;   // 1/hmin, 1/hmax (computed on the host)
   double hminratio;          // NodeList::hminratio (ASPH eigenvalue floor)
+  double gm1, ggm1;          // gamma - 1 and gamma (gamma - 1) (computed on the host)
 };
 
 struct HydroParams {

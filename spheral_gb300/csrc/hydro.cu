@@ -1200,29 +1200,30 @@ __global__ void updateKernel(Fields F, const int* __restrict__ list, long n, con
     F.f[F_VOL][i] = fmax(volMin, fmin(volMax, F.f[F_VOL][i] + mult * dVdt));
   }
   if (P.posh) {
-    // Mixed mode: the sound speed feeds only FP32 sweeps (Q, dt vote), so it
-    // is evaluated in FP32 (an FP64 square root costs many cycles of GB300's
-    // thin FP64 pipe).
+    // Mixed mode.  The sound speed feeds only FP32 sweeps (Q, dt vote), so it
+    // is evaluated in FP32; the conversions between double and float take
+    // the integer pipe (convert.cuh) and the cell origins an integer-built
+    // index: GB300's FP64 pipe, which runs FP64 arithmetic and the
+    // conversion instructions at ~1/64 of the FP32 rate, bounds this kernel.
     const double eps = F.f[F_EPS][i];
-    double p = (L.gamma - 1.0) * rho * eps;
+    double p = L.gm1 * rho * eps;
     p = p < L.minP ? L.minP : (p > L.maxP ? L.maxP : p);
     F.f[F_P][i] = p;
-    F.f[F_CS][i] = (double)sqrtf(fmaxf(0.0f, (float)(L.gamma * (L.gamma - 1.0) * eps)));
-  } else {
-    eosNode(F, i, L);
-  }
-  if (P.posh) {
+    const float cs = sqrtf(fmaxf(0.0f, toFloatRN(L.ggm1 * eps)));
+    F.f[F_CS][i] = toDouble(cs);
     int c[3];
     unpackCell(P.cell[i], c);
-    const double ox = g.lo[0] + c[0] * g.cell[0];
-    const double oy = g.lo[1] + c[1] * g.cell[1];
-    const double oz = g.lo[2] + c[2] * g.cell[2];
-    P.posh[i] = make_float4((float)(x - ox), (float)(y - oy), (float)(z - oz), (float)h);
-    P.velm[i] = make_float4((float)vx, (float)vy, (float)vz, (float)F.f[F_MASS][i]);
-    const float om = (float)F.f[F_OMEGA][i];
-    P.thermo[i] = make_float4((float)rho, (float)F.f[F_P][i], (float)F.f[F_CS][i], om / (om * om + 1.0e-30f));
+    const double ox = g.lo[0] + smallIntToDouble(c[0]) * g.cell[0];
+    const double oy = g.lo[1] + smallIntToDouble(c[1]) * g.cell[1];
+    const double oz = g.lo[2] + smallIntToDouble(c[2]) * g.cell[2];
+    P.posh[i] = make_float4(toFloatRN(x - ox), toFloatRN(y - oy), toFloatRN(z - oz), toFloatRN(h));
+    P.velm[i] = make_float4(toFloatRN(vx), toFloatRN(vy), toFloatRN(vz), toFloatRN(F.f[F_MASS][i]));
+    const float om = toFloatRN(F.f[F_OMEGA][i]);
+    P.thermo[i] = make_float4(toFloatRN(rho), toFloatRN(p), cs, om / (om * om + 1.0e-30f));
     if (TENSOR) writeTensorMirror(F, P, i);
-    if (crk && P.vol) P.vol[i] = (float)F.f[F_VOL][i];
+    if (crk && P.vol) P.vol[i] = toFloatRN(F.f[F_VOL][i]);
+  } else {
+    eosNode(F, i, L);
   }
 }
 

@@ -24,21 +24,24 @@ using namespace dev;
 __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  // the same mirror values as the update kernel writes, by the same
+  // integer-pipe conversions (the FP64 pipe bounds this kernel otherwise)
   int c[3];
   unpackCell(P.cell[i], c);
-  const double ox = g.lo[0] + c[0] * g.cell[0];
-  const double oy = g.lo[1] + c[1] * g.cell[1];
-  const double oz = g.lo[2] + c[2] * g.cell[2];
-  P.posh[i] = make_float4((float)(F.f[F_X][i] - ox), (float)(F.f[F_Y][i] - oy), (float)(F.f[F_Z][i] - oz),
-                          (float)F.f[F_HINV][i]);
-  P.velm[i] = make_float4((float)F.f[F_VX][i], (float)F.f[F_VY][i], (float)F.f[F_VZ][i], (float)F.f[F_MASS][i]);
+  const double ox = g.lo[0] + smallIntToDouble(c[0]) * g.cell[0];
+  const double oy = g.lo[1] + smallIntToDouble(c[1]) * g.cell[1];
+  const double oz = g.lo[2] + smallIntToDouble(c[2]) * g.cell[2];
+  P.posh[i] = make_float4(toFloatRN(F.f[F_X][i] - ox), toFloatRN(F.f[F_Y][i] - oy), toFloatRN(F.f[F_Z][i] - oz),
+                          toFloatRN(F.f[F_HINV][i]));
+  P.velm[i] = make_float4(toFloatRN(F.f[F_VX][i]), toFloatRN(F.f[F_VY][i]), toFloatRN(F.f[F_VZ][i]),
+                          toFloatRN(F.f[F_MASS][i]));
   // omega / (omega^2 + 1e-30) in FP32: an FP64 division here would cost
   // more on the narrow FP64 pipe than the rest of the kernel
-  const float om = (float)F.f[F_OMEGA][i];
-  P.thermo[i] = make_float4((float)F.f[F_RHO][i], (float)F.f[F_P][i], (float)F.f[F_CS][i],
+  const float om = toFloatRN(F.f[F_OMEGA][i]);
+  P.thermo[i] = make_float4(toFloatRN(F.f[F_RHO][i]), toFloatRN(F.f[F_P][i]), toFloatRN(F.f[F_CS][i]),
                             om / (om * om + 1.0e-30f));
   if (P.hten) writeTensorMirror(F, P, i);
-  if (P.vol) P.vol[i] = (float)F.f[F_VOL][i];
+  if (P.vol) P.vol[i] = toFloatRN(F.f[F_VOL][i]);
 }
 
 __device__ __forceinline__ void lookup32(const float* __restrict__ tw, const float* __restrict__ tg, int N1,
@@ -734,7 +737,11 @@ __global__ void __launch_bounds__(128) energyKernel32(Fields F, long n, Grid g, 
     const float sg = du < 0.0f ? -1.0f : 1.0f;
     const float weighti = fmaxf(feps, d0i * sg);
     const float weightj = fmaxf(feps, hj.w * sg);
-    kahanAdd(s, c, __fdividef(weighti, weighti + weightj) * du);
+    // The split of du between i and j: both sides divide by the same sum with
+    // IEEE rounding, so the two shares add up to du with unbiased rounding
+    // errors.  (An approximate reciprocal here leaves a one-signed error on
+    // every pair, which accumulates into a steady energy drift.)
+    kahanAdd(s, c, __fmul_rn(__fdiv_rn(weighti, __fadd_rn(weighti, weightj)), du));
   };
   // Batches of B slots: all their loads are issued before any is used, so B
   // gathers and pair-acceleration reads are in flight together.  The entries
