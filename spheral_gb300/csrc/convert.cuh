@@ -66,6 +66,18 @@ __host__ __device__ __forceinline__ uint32_t bitsOfFloat(float x) {
 #endif
 }
 
+// The conversion instructions, kept out of line so that the compiler
+// branches around them instead of predicating them into every call.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ inline float castToFloat(double x) { return (float)x; }
+__device__ __noinline__ inline double castToDouble(float x) { return (double)x; }
+__device__ __noinline__ inline double castIntToDouble(int x) { return (double)x; }
+#else
+inline float castToFloat(double x) { return (float)x; }
+inline double castToDouble(float x) { return (double)x; }
+inline double castIntToDouble(int x) { return (double)x; }
+#endif
+
 // double -> float, round to nearest even.  Exponent field e of the double:
 // the float is normal before rounding when 897 <= e <= 1150 (float exponent
 // e - 896 in 1..254).  Dropping the 29 low mantissa bits with a rounding
@@ -75,7 +87,7 @@ __host__ __device__ __forceinline__ uint32_t bitsOfFloat(float x) {
 __host__ __device__ __forceinline__ float toFloatRN(double x) {
   const uint64_t b = bitsOfDouble(x);
   const uint64_t mag = b & 0x7fffffffffffffffULL;
-  if (mag - (897ULL << 52) >= ((1151ULL - 897ULL) << 52)) return (float)x;
+  if (mag - (897ULL << 52) >= ((1151ULL - 897ULL) << 52)) return castToFloat(x);
   const uint64_t r = (mag + 0x0fffffffULL + ((mag >> 29) & 1ULL)) >> 29;
   const uint32_t f = (uint32_t)(r - (896ULL << 23));
   return floatOfBits(f | ((uint32_t)(b >> 32) & 0x80000000u));
@@ -86,7 +98,7 @@ __host__ __device__ __forceinline__ float toFloatRN(double x) {
 __host__ __device__ __forceinline__ double toDouble(float x) {
   const uint32_t b = bitsOfFloat(x);
   const uint32_t mag = b & 0x7fffffffu;
-  if (mag - 0x00800000u >= 0x7f000000u) return (double)x;
+  if (mag - 0x00800000u >= 0x7f000000u) return castToDouble(x);
   const uint64_t d = ((uint64_t)mag << 29) + (896ULL << 52);
   return doubleOfBits(d | ((uint64_t)(b & 0x80000000u) << 32));
 }
@@ -94,7 +106,7 @@ __host__ __device__ __forceinline__ double toDouble(float x) {
 // Non-negative int -> double (exact): the top set bit gives the exponent,
 // the bits below it the mantissa.
 __host__ __device__ __forceinline__ double smallIntToDouble(int c) {
-  if (c <= 0) return c == 0 ? 0.0 : (double)c;
+  if (c <= 0) return c == 0 ? 0.0 : castIntToDouble(c);
 #ifdef __CUDA_ARCH__
   const int e = 31 - __clz(c);
 #else
