@@ -181,7 +181,13 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   __shared__ float4 stage[G][W];         // one candidate batch per group
   constexpr int HW = TENSOR ? 2 * W : 1;
   __shared__ float4 stageH[G][HW];       // TENSOR: the batch's H (xx xy xz yy | yz zz band .)
-  __shared__ int2 range[G][27];          // node ranges of the 27 candidate cells
+  __shared__ int4 cinfo[G][27];          // the 27 candidate cells: node range, first work chunk, cell-offset code
+  __shared__ float4 coff[G][27];         // the cell offset (ox, oy, oz) of each
+  // Isotropic H: each batch's culling box is loaded a batch ahead (in lanes
+  // 0 and 1) and passed through shared memory; the tensor path, heavier in
+  // registers already, loads it when its batch comes up.
+  constexpr bool BOXAHEAD = !TENSOR;
+  __shared__ float4 sbox[G][2];          // the current batch's box (lo, hi)
   const int item = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) / W);
   const int lane = threadIdx.x % W, wib = threadIdx.x / W;
   // lanes of this group within the warp
@@ -193,7 +199,9 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   int hc[3];
   unpackCell(cc, hc);
   // The 27 cell ranges are independent loads: fetch them lane-parallel so
-  // their latencies overlap.  Cell t is (dx, dy, dz) = (t%3, t/3%3, t/9) - 1.
+  // their latencies overlap, with each cell's first work chunk (its batches'
+  // boxes follow consecutively) and its offset code and offset.  Cell t is
+  // (dx, dy, dz) = (t%3, t/3%3, t/9) - 1.
   for (int t = lane; t < 27; t += W) {
     const int d[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
     int cell[3];
@@ -212,15 +220,23 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
       }
       cell[a] = nn;
     }
-    int2 r = make_int2(0, 0);
+    const int d0 = t % 3, d1 = (t / 3) % 3, d2 = t / 9;   // 0, 1, 2 for -1, 0, +1
+    const int dcode = (d0 == 0 ? 1 : (d0 == 2 ? 2 : 0)) | ((d1 == 0 ? 1 : (d1 == 2 ? 2 : 0)) << 2) |
+                      ((d2 == 0 ? 1 : (d2 == 2 ? 2 : 0)) << 4);
+    int4 r = make_int4(0, 0, 0, dcode);
     if (ok) {
       const uint32_t key = morton3((uint32_t)cell[0], (uint32_t)cell[1], (uint32_t)cell[2]);
-      r = make_int2(cellStart[key], cellEnd[key]);
+      r.x = cellStart[key];
+      r.y = cellEnd[key];
+      if (r.x < r.y) r.z = chunkOf[r.x];
     }
-    range[wib][t] = r;
+    cinfo[wib][t] = r;
+    coff[wib][t] = make_float4(d0 == 0 ? g.cellf[0] : (d0 == 2 ? -g.cellf[0] : 0.0f),
+                               d1 == 0 ? g.cellf[1] : (d1 == 2 ? -g.cellf[1] : 0.0f),
+                               d2 == 0 ? g.cellf[2] : (d2 == 2 ? -g.cellf[2] : 0.0f), 0.0f);
   }
   __syncwarp(gmask);
-  const int k1 = min(k0 + W, range[wib][13].y);   // cell 13 is the home cell
+  const int k1 = min(k0 + W, cinfo[wib][13].y);   // cell 13 is the home cell
   const long i = k0 + lane;
   const bool active = i < k1;
   const float4 pi = active ? P.posh[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -250,46 +266,56 @@ __global__ void __launch_bounds__(128) neighborWarpKernel(Fields F, Fields32 P, 
   const float cullThr = e2t * (1.0f + delMax) * 1.0001f;
   // slot 0 of node i in the warp-interleaved lists; slot q is 32 entries further per q
   uint32_t* out = WRITE ? nbr + nbSlot(i, 0, cap) : nullptr;
-  // first batch of the first non-empty cell, loaded ahead of use
+  // first batch of the first non-empty cell (and its box), loaded ahead of use
   int tn = 0;
-  while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
+  while (tn < 27 && cinfo[wib][tn].x >= cinfo[wib][tn].y) ++tn;
   float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 hn0 = qn, hn1 = qn;
-  if (tn < 27 && range[wib][tn].x + lane < range[wib][tn].y) {
-    qn = P.posh[range[wib][tn].x + lane];
-    if (TENSOR) { hn0 = P.hten[2 * (range[wib][tn].x + lane)]; hn1 = P.hten[2 * (range[wib][tn].x + lane) + 1]; }
+  float4 hn0 = qn, hn1 = qn, nbox = qn;
+  if (tn < 27) {
+    const int4 c0 = cinfo[wib][tn];
+    if (c0.x + lane < c0.y) {
+      qn = P.posh[c0.x + lane];
+      if (TENSOR) { hn0 = P.hten[2 * (c0.x + lane)]; hn1 = P.hten[2 * (c0.x + lane) + 1]; }
+    }
+    if (BOXAHEAD && cull && lane < 2) nbox = box[2 * c0.z + lane];
   }
   while (tn < 27) {
     const int t = tn;
-    const int s = range[wib][t].x, e = range[wib][t].y;
-    const int d0 = t % 3, d1 = (t / 3) % 3, d2 = t / 9;   // 0, 1, 2 for -1, 0, +1
-    const int dcode = (d0 == 0 ? 1 : (d0 == 2 ? 2 : 0)) | ((d1 == 0 ? 1 : (d1 == 2 ? 2 : 0)) << 2) |
-                      ((d2 == 0 ? 1 : (d2 == 2 ? 2 : 0)) << 4);
+    const int4 ct = cinfo[wib][t];
+    const int s = ct.x, e = ct.y, dcode = ct.w;
+    const float4 off = coff[wib][t];
     const uint32_t mir = (uint32_t)dcode & mm;
-    const float ox = d0 == 0 ? cx : (d0 == 2 ? -cx : 0.0f);
-    const float oy = d1 == 0 ? cy : (d1 == 2 ? -cy : 0.0f);
-    const float oz = d2 == 0 ? cz : (d2 == 2 ? -cz : 0.0f);
+    const float ox = off.x, oy = off.y, oz = off.z;
     // next non-empty cell
     ++tn;
-    while (tn < 27 && range[wib][tn].x >= range[wib][tn].y) ++tn;
-    for (int base = s; base < e; base += W) {
+    while (tn < 27 && cinfo[wib][tn].x >= cinfo[wib][tn].y) ++tn;
+    for (int base = s, cb = ct.z; base < e; base += W, ++cb) {
       float4 q = qn;
       float4 qh0 = hn0, qh1 = hn1;
+      if (BOXAHEAD && cull) {
+        if (lane < 2) sbox[wib][lane] = nbox;
+        __syncwarp(gmask);
+      }
+      // prefetch the next batch's candidates (and box: that of chunk cb + 1,
+      // or of the next cell's first chunk)
       if (base + W < e) {            // another batch of this cell follows
         const bool ok = base + W + lane < e;
         qn = ok ? P.posh[base + W + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
         if (TENSOR && ok) { hn0 = P.hten[2 * (base + W + lane)]; hn1 = P.hten[2 * (base + W + lane) + 1]; }
+        if (BOXAHEAD && cull && lane < 2) nbox = box[2 * (cb + 1) + lane];
       } else if (tn < 27) {          // last batch: prefetch the next cell's first batch
-        const int sn = range[wib][tn].x, en = range[wib][tn].y;
-        const bool ok = sn + lane < en;
-        qn = ok ? P.posh[sn + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (TENSOR && ok) { hn0 = P.hten[2 * (sn + lane)]; hn1 = P.hten[2 * (sn + lane) + 1]; }
+        const int4 cn = cinfo[wib][tn];
+        const bool ok = cn.x + lane < cn.y;
+        qn = ok ? P.posh[cn.x + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (TENSOR && ok) { hn0 = P.hten[2 * (cn.x + lane)]; hn1 = P.hten[2 * (cn.x + lane) + 1]; }
+        if (BOXAHEAD && cull && lane < 2) nbox = box[2 * cn.z + lane];
       }
       if (cull) {
+        float4 bLo, bHi;
+        if (BOXAHEAD) { bLo = sbox[wib][0]; bHi = sbox[wib][1]; }
+        else { bLo = box[2 * cb]; bHi = box[2 * cb + 1]; }
         // the batch's box in the frame of the group's cell: a candidate at q
         // (mirrored where the entry crosses a wall) sits at q - o there
-        const int cb = chunkOf[base];
-        const float4 bLo = box[2 * cb], bHi = box[2 * cb + 1];
         float lx = bLo.x, hx = bHi.x, ly = bLo.y, hy = bHi.y, lz = bLo.z, hz = bHi.z;
         if (mir & 3u) { lx = cx - bHi.x; hx = cx - bLo.x; }
         if (mir & 12u) { ly = cy - bHi.y; hy = cy - bLo.y; }
