@@ -25,8 +25,8 @@ __device__ __forceinline__ void sumAdd(float& s, float& c, float x, int plain) {
 }
 
 // eta from eta^2 in the FP32 sweeps: eta^2 times its reciprocal square root
-// (the hardware approximation; eta^2 = 0 gives 0).  The pair kernel forms
-// its eta_i and eta_j the same way.
+// (the hardware approximation; eta^2 = 0 gives 0), as the pair kernel forms
+// its eta_i and eta_j; the density/dt and grad-h sweeps use it too.
 __device__ __forceinline__ float etaFromSq(float e2) { return __fmul_rn(e2, rsqrtf(fmaxf(e2, 1.0e-30f))); }
 
 // Velocity of a mirror image: the components along the mirrored axes flip

@@ -462,12 +462,12 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
           h0.z *= sx * sz;
           h1.x *= sy * sz;
         }
-        eta = sqrtf(eta2Sym32(h0, h1, rx, ry, rz));
+        eta = etaFromSq(eta2Sym32(h0, h1, rx, ry, rz));
         Hdj = h1.z;
         lmaxj = h1.w;
       } else {
         const float aj = pj.w;
-        eta = aj * sqrtf(rx * rx + ry * ry + rz * rz);
+        eta = aj * etaFromSq(rx * rx + ry * ry + rz * rz);
         Hdj = aj * aj * aj;
         lmaxj = aj;
       }
