@@ -82,7 +82,14 @@ __device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, cons
 // grad W = gW H eta^, both in a fixed order so the pair force stays bitwise
 // antisymmetric), the second moment of ASPHClassicSmoothingScale and its
 // FP32 finalize.
-template <bool XSPH, bool COMPAT, bool MULTI, int MINB, bool PF, bool LIMQ, bool TENSOR>
+//
+// PF selects the neighbour loop: 0 one slot per iteration, 1 software-
+// pipelined (entry two slots ahead, node data one slot ahead), 2 or 4 that
+// many slots per iteration (their gathers issued together, the next
+// iteration's entries loaded ahead).  Every form evaluates the slots in list order, so all give
+// the same bits.  LEAN: compensated sums, no tensile correction and the
+// standard Q expansion fixed at compile time (no run-time flag in the loop).
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB, int PF, bool LIMQ, bool TENSOR, bool LEAN = false>
 __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
@@ -131,40 +138,10 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
   for (int k = 0; k < 6; ++k) m2[k] = 0.f;
 
   const int cnt = nl.count[i];
-  // PF: software pipeline over the neighbour list -- the entry two slots
-  // ahead and the node data one slot ahead are loaded while the current pair
-  // is evaluated, so the gathers overlap the arithmetic.
-  uint32_t entA = 0u, entB = 0u;
-  float4 pjA = make_float4(0.f, 0.f, 0.f, 0.f), vjA = pjA, thA = pjA, hA0 = pjA, hA1 = pjA;
-  if (PF) {
-    if (cnt > 0) {
-      entA = nl.nbr[nbSlot(i, 0, nl.cap)];
-      const int j0 = (int)(entA & kIndexMask);
-      pjA = P.posh[j0]; vjA = P.velm[j0]; thA = P.thermo[j0];
-      if (TENSOR) { hA0 = P.hten[2 * j0]; hA1 = P.hten[2 * j0 + 1]; }
-    }
-    if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
-  }
-  for (int q = 0; q < cnt; ++q) {
-    const long long k = nbSlot(i, q, nl.cap);
-    uint32_t ent;
-    float4 pj, vj4, thj, hj0 = make_float4(0.f, 0.f, 0.f, 0.f), hj1 = hj0;
-    if (PF) {
-      ent = entA; pj = pjA; vj4 = vjA; thj = thA;
-      if (TENSOR) { hj0 = hA0; hj1 = hA1; }
-      if (q + 1 < cnt) {
-        const int jn = (int)(entB & kIndexMask);
-        pjA = P.posh[jn]; vjA = P.velm[jn]; thA = P.thermo[jn];
-        if (TENSOR) { hA0 = P.hten[2 * jn]; hA1 = P.hten[2 * jn + 1]; }
-        entA = entB;
-      }
-      if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
-    } else {
-      ent = nl.nbr[k];
-      const int jj = (int)(ent & kIndexMask);
-      pj = P.posh[jj]; vj4 = P.velm[jj]; thj = P.thermo[jj];
-      if (TENSOR) { hj0 = P.hten[2 * jj]; hj1 = P.hten[2 * jj + 1]; }
-    }
+  // One neighbour slot: the pair's contributions to node i's sums (and the
+  // pair acceleration of the compatible-energy sweep at list slot k).
+  auto slot = [&](uint32_t ent, const float4& pj, const float4& vj4, const float4& thj, float4 hj0, float4 hj1,
+                  long long k) {
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     float rx, ry, rz;
     relSepTab(pi, pj, dcode, mm, cx, cy, cz, sOff, rx, ry, rz);
@@ -264,10 +241,10 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     const float mui = __fdividef(__fmaf_rn(vqz, eiz, __fmaf_rn(vqy, eiy, __fmul_rn(vqx, eix))), __fadd_rn(e2i, eps2));
     const float muj = __fdividef(__fmaf_rn(vqz, ejz, __fmaf_rn(vqy, ejy, __fmul_rn(vqx, ejx))), __fadd_rn(e2j, eps2));
     const float mni = fminf(0.f, mui), mnj = fminf(0.f, muj);
-    const float li_ = hp.linearInExpansion ? mui : mni;
-    const float lj_ = hp.linearInExpansion ? muj : mnj;
-    const float qi_ = hp.quadraticInExpansion ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : mni * mni;
-    const float qj_ = hp.quadraticInExpansion ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : mnj * mnj;
+    const float li_ = (!LEAN && hp.linearInExpansion) ? mui : mni;
+    const float lj_ = (!LEAN && hp.linearInExpansion) ? muj : mnj;
+    const float qi_ = (!LEAN && hp.quadraticInExpansion) ? -(mui < 0.f ? -1.f : 1.f) * mui * mui : mni * mni;
+    const float qj_ = (!LEAN && hp.quadraticInExpansion) ? -(muj < 0.f ? -1.f : 1.f) * muj * muj : mnj * mnj;
     const float ei = __fmaf_rn(Cq, qi_, __fmul_rn(mClci, li_));
     const float ej = __fmaf_rn(Cq, qj_, __fmul_rn(__fmul_rn(-Cl, csj), lj_));
     const float qai = __fmul_rn(0.5f, __fmul_rn(ei, iri)), qaj = __fmul_rn(0.5f, __fmul_rn(ej, irj));
@@ -275,7 +252,7 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     maxQ = fmaxf(maxQ, Qi);
     effQ += mj * Qi * Wi * irj;
     float Prhoi = Prhoi0, Prhoj = __fmul_rn(__fmul_rn(__fmul_rn(sOj, Pj), irj), irj);
-    if (epsT != 0.f) {
+    if (!LEAN && epsT != 0.f) {
       const float ti = Wi / (Hdeti * WnPerh), tj = Wj / (Hdetj * WnPerh);
       Prhoi = __fmul_rn(__fmul_rn(__fmul_rn(sOi, Pi + epsT * (ti * ti * ti * ti) * (Pi < 0.f ? -Pi : 0.f)), iri), iri);
       Prhoj = __fmul_rn(__fmul_rn(__fmul_rn(sOj, Pj + epsT * (tj * tj * tj * tj) * (Pj < 0.f ? -Pj : 0.f)), irj), irj);
@@ -286,16 +263,16 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     const float ddy = __fadd_rn(__fmul_rn(ci_, gwiy), __fmul_rn(cj_, gwjy));
     const float ddz = __fadd_rn(__fmul_rn(ci_, gwiz), __fmul_rn(cj_, gwjz));
     const float pax = __fmul_rn(-mj, ddx), pay = __fmul_rn(-mj, ddy), paz = __fmul_rn(-mj, ddz);
-    sumAdd(sdx, cdx, pax, hp.plainSums);
-    sumAdd(sdy, cdy, pay, hp.plainSums);
-    sumAdd(sdz, cdz, paz, hp.plainSums);
+    sumAdd(sdx, cdx, pax, LEAN ? 0 : hp.plainSums);
+    sumAdd(sdy, cdy, pay, LEAN ? 0 : hp.plainSums);
+    sumAdd(sdz, cdz, paz, LEAN ? 0 : hp.plainSums);
     if (COMPAT) {
       pacc[3 * k] = pax;
       pacc[3 * k + 1] = pay;
       pacc[3 * k + 2] = paz;
     }
     const float vg = vx * gwix + vy * gwiy + vz * gwiz;
-    sumAdd(se, ce, mj * (Prhoi + qai) * vg, hp.plainSums);
+    sumAdd(se, ce, mj * (Prhoi + qai) * vg, LEAN ? 0 : hp.plainSums);
     const float mvx = mj * vx, mvy = mj * vy, mvz = mj * vz;
     D[0] -= mvx * gwix; D[1] -= mvx * gwiy; D[2] -= mvx * gwiz;
     D[3] -= mvy * gwix; D[4] -= mvy * gwiy; D[5] -= mvy * gwiz;
@@ -321,6 +298,79 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
       const float w = fwW * WSPHi * (ir2 * ir2 * ir);
       m2[0] += w * (rx * rx); m2[1] += w * (rx * ry); m2[2] += w * (rx * rz);
       m2[3] += w * (ry * ry); m2[4] += w * (ry * rz); m2[5] += w * (rz * rz);
+    }
+  };
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (PF == 1) {
+    // software pipeline over the neighbour list: the entry two slots ahead
+    // and the node data one slot ahead are loaded while the current pair is
+    // evaluated, so the gathers overlap the arithmetic
+    uint32_t entA = 0u, entB = 0u;
+    float4 pjA = zero4, vjA = zero4, thA = zero4, hA0 = zero4, hA1 = zero4;
+    if (cnt > 0) {
+      entA = nl.nbr[nbSlot(i, 0, nl.cap)];
+      const int j0 = (int)(entA & kIndexMask);
+      pjA = P.posh[j0]; vjA = P.velm[j0]; thA = P.thermo[j0];
+      if (TENSOR) { hA0 = P.hten[2 * j0]; hA1 = P.hten[2 * j0 + 1]; }
+    }
+    if (cnt > 1) entB = nl.nbr[nbSlot(i, 1, nl.cap)];
+    for (int q = 0; q < cnt; ++q) {
+      const uint32_t ent = entA;
+      const float4 pj = pjA, vj4 = vjA, thj = thA;
+      const float4 hj0 = hA0, hj1 = hA1;
+      if (q + 1 < cnt) {
+        const int jn = (int)(entB & kIndexMask);
+        pjA = P.posh[jn]; vjA = P.velm[jn]; thA = P.thermo[jn];
+        if (TENSOR) { hA0 = P.hten[2 * jn]; hA1 = P.hten[2 * jn + 1]; }
+        entA = entB;
+      }
+      if (q + 2 < cnt) entB = nl.nbr[nbSlot(i, q + 2, nl.cap)];
+      slot(ent, pj, vj4, thj, hj0, hj1, nbSlot(i, q, nl.cap));
+    }
+  } else if (PF >= 2) {
+    // PF slots per iteration (slot q + 1 sits 32 entries after slot q): their
+    // gathers are issued together, the next iteration's entries meanwhile
+    constexpr int U = PF >= 2 ? PF : 2;
+    uint32_t nx[U];
+    if (U <= cnt) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) nx[u] = nl.nbr[nbSlot(i, u, nl.cap)];
+    }
+    int q = 0;
+    for (; q + U <= cnt; q += U) {
+      const long long k0 = nbSlot(i, q, nl.cap);
+      uint32_t e[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) e[u] = nx[u];
+      if (q + 2 * U <= cnt) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) nx[u] = nl.nbr[k0 + 32 * (U + u)];
+      }
+      float4 pp[U], vv[U], tt[U], aa[U], bb[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int jj = (int)(e[u] & kIndexMask);
+        pp[u] = P.posh[jj]; vv[u] = P.velm[jj]; tt[u] = P.thermo[jj];
+        aa[u] = zero4; bb[u] = zero4;
+        if (TENSOR) { aa[u] = P.hten[2 * jj]; bb[u] = P.hten[2 * jj + 1]; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) slot(e[u], pp[u], vv[u], tt[u], aa[u], bb[u], k0 + 32 * u);
+    }
+    for (; q < cnt; ++q) {
+      const long long k = nbSlot(i, q, nl.cap);
+      const uint32_t ent = nl.nbr[k];
+      const int jj = (int)(ent & kIndexMask);
+      slot(ent, P.posh[jj], P.velm[jj], P.thermo[jj], TENSOR ? P.hten[2 * jj] : zero4,
+           TENSOR ? P.hten[2 * jj + 1] : zero4, k);
+    }
+  } else {
+    for (int q = 0; q < cnt; ++q) {
+      const long long k = nbSlot(i, q, nl.cap);
+      const uint32_t ent = nl.nbr[k];
+      const int jj = (int)(ent & kIndexMask);
+      slot(ent, P.posh[jj], P.velm[jj], P.thermo[jj], TENSOR ? P.hten[2 * jj] : zero4,
+           TENSOR ? P.hten[2 * jj + 1] : zero4, k);
     }
   }
   NodeAcc32 a;
@@ -401,7 +451,7 @@ __global__ void __launch_bounds__(128) sumDensityKernel32(Fields F, Fields32 P, 
 // (GenericHydro.cc:113-381, pairwise velocity limit on the same neighbour
 // data, node limits with the new density) in one pass over the lists.
 //------------------------------------------------------------------------------
-template <bool TENSOR>
+template <bool TENSOR, bool LEAN>
 __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                          Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                          double maxNperh, double* __restrict__ part) {
@@ -421,7 +471,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
     const float cx = g.cellf[0], cy = g.cellf[1], cz = g.cellf[2];
     const float4 pi = P.posh[i], vi = P.velm[i];
     const float mi = vi.w;
-    const bool multi = hp.numLists > 1;
+    const bool multi = !LEAN && hp.numLists > 1;
     const int li = multi ? list[i] : 0;
     const float extent = (float)hp.extent, invStep = (float)(1.0 / hp.tableXstep);
     const int N1 = hp.tableN1;
@@ -474,7 +524,7 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
       if (eta < extent) {
         const int i0 = 3 * min(N1, (int)(eta * invStep));
         const float w = Hdj * (tw[i0] + (tw[i0 + 1] + tw[i0 + 2] * eta) * eta);
-        sumAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w, hp.plainSums);
+        sumAdd(s, c, ((multi ? list[j] == li : true) ? vj.w : mi) * w, LEAN ? 0 : hp.plainSums);
       }
       float vxj = vj.x, vyj = vj.y, vzj = vj.z;
       mirrorVel((uint32_t)dcode & mm, vxj, vyj, vzj);
@@ -793,17 +843,21 @@ void launchPrepareFP32(Fields F, Fields32 F32, long n, Grid g, cudaStream_t s, L
   lc->add(1);
 }
 
-// variant (common path: compatible energy, no XSPH, one NodeList): the
-// minimum resident blocks per SM requested from the compiler -- 4 (no
-// register cap below 128), 5 (<= 102 registers), 6 (<= 85 registers) -- for
-// variants 0-2 without and 3-5 with the software-pipelined neighbour loop.
-// Chosen at run time by the autotuner (kPairVariants).
+// variant (compatible energy, no XSPH, one NodeList): 0 the software-
+// pipelined loop at 4 blocks per SM (<= 128 registers), 1 the same at 5
+// (<= 102 registers), 2 two slots per iteration at 4, 3 four slots per
+// iteration at 3 (<= 168 registers); with the limited Q, 0-1 the pipelined
+// loop and 2-3 two slots per iteration.  Lean forms where the configuration
+// allows.  Chosen at run time by the autotuner (kPairVariants); every
+// variant gives the same bits.
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc) {
   const int b = 128;
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
+  // lean forms (no run-time flag in the loop) when the configuration allows
+  const bool lean = !hp.plainSums && hp.epsTensile == 0.0 && !hp.linearInExpansion && !hp.quadraticInExpansion;
 #define SPH_PAIR32(X, C, M, MB, PF, LQ) \
   pairKernelFP32<X, C, M, MB, PF, LQ, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
 #define SPH_PAIR32T(X, C, LQ)                                                                     \
@@ -821,9 +875,16 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
       if (hp.compatible) { if (hp.limitedQ) SPH_PAIR32T(false, true, true); else SPH_PAIR32T(false, true, false); }
       else { if (hp.limitedQ) SPH_PAIR32T(false, false, true); else SPH_PAIR32T(false, false, false); }
     }
-  } else if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity: one variant per path
-    if (!hp.xsph && hp.compatible && !multi) SPH_PAIR32(false, true, false, 4, true, true);
-    else if (hp.xsph) {
+  } else if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity
+    if (!hp.xsph && hp.compatible && !multi) {
+      if (lean) {
+        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, false, 4, 1, true, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+      } else {
+        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, false, 4, 1, true, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+      }
+    } else if (hp.xsph) {
       if (hp.compatible) SPH_PAIR32(true, true, true, 4, false, true);
       else SPH_PAIR32(true, false, true, 4, false, true);
     } else {
@@ -831,14 +892,18 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
       else SPH_PAIR32(false, false, true, 4, false, true);
     }
   } else if (!hp.xsph && hp.compatible && !multi) {
+#define SPH_PAIR32V(MB, PF) \
+  do {                                                                                                            \
+    if (lean) pairKernelFP32<false, true, false, MB, PF, false, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+    else pairKernelFP32<false, true, false, MB, PF, false, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+  } while (0)
     switch (variant) {
-      case 0: SPH_PAIR32(false, true, false, 4, false, false); break;
-      case 2: SPH_PAIR32(false, true, false, 6, false, false); break;
-      case 3: SPH_PAIR32(false, true, false, 4, true, false); break;
-      case 4: SPH_PAIR32(false, true, false, 5, true, false); break;
-      case 5: SPH_PAIR32(false, true, false, 6, true, false); break;
-      default: SPH_PAIR32(false, true, false, 5, false, false); break;
+      case 1: SPH_PAIR32V(5, 1); break;
+      case 2: SPH_PAIR32V(4, 2); break;
+      case 3: SPH_PAIR32V(3, 4); break;
+      default: SPH_PAIR32V(4, 1); break;
     }
+#undef SPH_PAIR32V
   } else if (hp.xsph) {
     if (hp.compatible) {
       if (multi) SPH_PAIR32(true, true, true, 5, false, false); else SPH_PAIR32(true, true, false, 5, false, false);
@@ -892,8 +957,11 @@ void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g
                          HydroParams hp, double maxNperh, double* dScratch,
                          double* dOut, cudaStream_t s, LaunchCounter* lc) {
   const int nb = (int)gridFor(n, 128);
-  if (hp.asph) densityDtKernel32<true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
-  else densityDtKernel32<false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  // lean: one NodeList and compensated sums fixed at compile time
+  const bool lean = hp.numLists == 1 && !hp.plainSums;
+  if (hp.asph) densityDtKernel32<true, false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  else if (lean) densityDtKernel32<false, true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  else densityDtKernel32<false, false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
 }

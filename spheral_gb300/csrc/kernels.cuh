@@ -68,7 +68,7 @@ void launchGradh(Fields F, long n, Grid g, NeighborLists nl, TableDev t, HydroPa
                  LaunchCounter* lc);
 void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                     double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
-constexpr int kPairVariants = 6;   // autotuned variants of launchPairFP32 (common path)
+constexpr int kPairVariants = 4;   // autotuned variants of launchPairFP32 (common path)
 constexpr int kRetuneAfter = 2;    // uses between an autotuner's first timing and its one retiming
 constexpr int kPairVariantsTensor = 2;   // of its tensor-H (ASPH) path
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,

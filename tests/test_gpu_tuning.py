@@ -1,8 +1,9 @@
 """The autotuned choices change speed only, never results.
 
 The mixed-mode step picks, by timing, the neighbour-search group width
-(8, 16 or 32 lanes), the pair-kernel variant (register budget and software
-pipelining) and the batch depth of the compatible-energy sweep.  With each
+(8, 16 or 32 lanes), the pair-kernel variant (register budget, software
+pipelining, one / two / four slots per loop iteration) and the batch depth
+of the compatible-energy sweep.  With each
 choice pinned in turn through the tuning entry points
 (sphgpu_set_neighbor_width, sphgpu_set_pair_variant,
 sphgpu_set_energy_variant), the neighbour lists -- entry order included,
@@ -10,8 +11,9 @@ guard-band candidates too -- and every state field after a few steps are
 bitwise the same: the search writes each list in candidate order whatever
 the width, and the sweeps sum in list order whatever their batching.
 
-Problems: the Kelvin-Helmholtz box (isotropic H, FP64 and mixed mode) and a
-stretched anisotropic box with reflecting walls (tensor H, mixed mode)."""
+Problems: the Kelvin-Helmholtz box (isotropic H, FP64 and mixed mode; the
+pair variants also with the limited Q) and a stretched anisotropic box with
+reflecting walls (tensor H, mixed mode)."""
 import numpy as np
 import pytest
 
@@ -62,9 +64,15 @@ def test_search_width_does_not_change_results(native_lib, case):
         _same(ref, _run(make, precision, 3, width=w), f"width {w}")
 
 
-def test_pair_variant_does_not_change_results(native_lib):
+def _kh_limited():
+    p = problems.kelvin_helmholtz(n1=24)
+    p.config.update(viscosity="limited_monaghan_gingold", Cl=2.0, Cq=2.0)
+    return p
+
+
+@pytest.mark.parametrize("make", [lambda: problems.kelvin_helmholtz(n1=24), _kh_limited], ids=["mg", "limited_q"])
+def test_pair_variant_does_not_change_results(native_lib, make):
     from spheral_gb300.engine import Engine
-    make = lambda: problems.kelvin_helmholtz(n1=24)
     _, nv = Engine.from_problem(make(), precision="fp32").pair_variant()
     ref = _run(make, "fp32", 3, width=32, pair=0)
     for v in range(1, nv):
