@@ -44,19 +44,6 @@ __global__ void prepareKernel(Fields F, Fields32 P, long n, Grid g) {
   if (P.vol) P.vol[i] = toFloatRN(F.f[F_VOL][i]);
 }
 
-__device__ __forceinline__ void lookup32(const float* __restrict__ tw, const float* __restrict__ tg, int N1,
-                                         float invStep, float eta, float extent, float& w, float& gr) {
-  if (eta < extent) {
-    const int k = min(N1, (int)(fmaxf(0.0f, eta) * invStep));
-    const int i0 = 3 * k;
-    w = __fmaf_rn(__fmaf_rn(tw[i0 + 2], eta, tw[i0 + 1]), eta, tw[i0]);
-    gr = __fmaf_rn(__fmaf_rn(tg[i0 + 2], eta, tg[i0 + 1]), eta, tg[i0]);
-  } else {
-    w = 0.0f;
-    gr = 0.0f;
-  }
-}
-
 //------------------------------------------------------------------------------
 // SPH pair loop (src/SPH/SPH.cc:294-470) + SPHSmoothingScale moments, FP32.
 // Every operation that enters the pair force is deterministic and appears in
@@ -86,10 +73,12 @@ __device__ __forceinline__ void lookupPacked(const float4* __restrict__ ta, cons
 // PF selects the neighbour loop: 0 one slot per iteration, 1 software-
 // pipelined (entry two slots ahead, node data one slot ahead), 2 or 4 that
 // many slots per iteration (their gathers issued together, the next
-// iteration's entries loaded ahead).  Every form evaluates the slots in list order, so all give
-// the same bits.  LEAN: compensated sums, no tensile correction and the
-// standard Q expansion fixed at compile time (no run-time flag in the loop).
-template <bool XSPH, bool COMPAT, bool MULTI, int MINB, int PF, bool LIMQ, bool TENSOR, bool LEAN = false>
+// iteration's entries loaded ahead).  Every form evaluates the slots in list
+// order, so all give the same bits.  LEAN (1: compensated sums, 2: plain
+// FP32 sums): the sum type, no tensile correction and the standard Q
+// expansion fixed at compile time (no run-time flag in the loop); 0 reads
+// them from hp.
+template <bool XSPH, bool COMPAT, bool MULTI, int MINB, int PF, bool LIMQ, bool TENSOR, int LEAN = 0>
 __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                       Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                       float* __restrict__ pacc) {
@@ -263,16 +252,16 @@ __global__ void __launch_bounds__(128, MINB) pairKernelFP32(Fields F, Fields32 P
     const float ddy = __fadd_rn(__fmul_rn(ci_, gwiy), __fmul_rn(cj_, gwjy));
     const float ddz = __fadd_rn(__fmul_rn(ci_, gwiz), __fmul_rn(cj_, gwjz));
     const float pax = __fmul_rn(-mj, ddx), pay = __fmul_rn(-mj, ddy), paz = __fmul_rn(-mj, ddz);
-    sumAdd(sdx, cdx, pax, LEAN ? 0 : hp.plainSums);
-    sumAdd(sdy, cdy, pay, LEAN ? 0 : hp.plainSums);
-    sumAdd(sdz, cdz, paz, LEAN ? 0 : hp.plainSums);
+    sumAdd(sdx, cdx, pax, LEAN == 2 ? 1 : (LEAN == 1 ? 0 : hp.plainSums));
+    sumAdd(sdy, cdy, pay, LEAN == 2 ? 1 : (LEAN == 1 ? 0 : hp.plainSums));
+    sumAdd(sdz, cdz, paz, LEAN == 2 ? 1 : (LEAN == 1 ? 0 : hp.plainSums));
     if (COMPAT) {
       pacc[3 * k] = pax;
       pacc[3 * k + 1] = pay;
       pacc[3 * k + 2] = paz;
     }
     const float vg = vx * gwix + vy * gwiy + vz * gwiz;
-    sumAdd(se, ce, mj * (Prhoi + qai) * vg, LEAN ? 0 : hp.plainSums);
+    sumAdd(se, ce, mj * (Prhoi + qai) * vg, LEAN == 2 ? 1 : (LEAN == 1 ? 0 : hp.plainSums));
     const float mvx = mj * vx, mvy = mj * vy, mvz = mj * vz;
     D[0] -= mvx * gwix; D[1] -= mvx * gwiy; D[2] -= mvx * gwiz;
     D[3] -= mvy * gwix; D[4] -= mvy * gwiy; D[5] -= mvy * gwiz;
@@ -856,8 +845,9 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
   const int b = 128;
   const unsigned gb = gridFor(n, b);
   const bool multi = hp.numLists > 1;
-  // lean forms (no run-time flag in the loop) when the configuration allows
-  const bool lean = !hp.plainSums && hp.epsTensile == 0.0 && !hp.linearInExpansion && !hp.quadraticInExpansion;
+  // lean forms (no run-time flag in the loop) when the configuration allows:
+  // 1 with compensated sums, 2 with plain ones
+  const int lean = (hp.epsTensile == 0.0 && !hp.linearInExpansion && !hp.quadraticInExpansion) ? (hp.plainSums ? 2 : 1) : 0;
 #define SPH_PAIR32(X, C, M, MB, PF, LQ) \
   pairKernelFP32<X, C, M, MB, PF, LQ, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc)
 #define SPH_PAIR32T(X, C, LQ)                                                                     \
@@ -877,12 +867,12 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
     }
   } else if (hp.limitedQ) {   // LimitedMonaghanGingoldViscosity
     if (!hp.xsph && hp.compatible && !multi) {
-      if (lean) {
-        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
-        else pairKernelFP32<false, true, false, 4, 1, true, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+      if (lean == 1) {
+        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, 1><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, false, 4, 1, true, false, 1><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
       } else {
-        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
-        else pairKernelFP32<false, true, false, 4, 1, true, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        if (variant >= 2) pairKernelFP32<false, true, false, 4, 2, true, false, 0><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, false, 4, 1, true, false, 0><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
       }
     } else if (hp.xsph) {
       if (hp.compatible) SPH_PAIR32(true, true, true, 4, false, true);
@@ -894,8 +884,9 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
   } else if (!hp.xsph && hp.compatible && !multi) {
 #define SPH_PAIR32V(MB, PF) \
   do {                                                                                                            \
-    if (lean) pairKernelFP32<false, true, false, MB, PF, false, false, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
-    else pairKernelFP32<false, true, false, MB, PF, false, false, false><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+    if (lean == 1) pairKernelFP32<false, true, false, MB, PF, false, false, 1><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+    else if (lean == 2) pairKernelFP32<false, true, false, MB, PF, false, false, 2><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
+    else pairKernelFP32<false, true, false, MB, PF, false, false, 0><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
   } while (0)
     switch (variant) {
       case 1: SPH_PAIR32V(5, 1); break;

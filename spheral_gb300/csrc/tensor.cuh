@@ -279,7 +279,7 @@ template <class T>
 __device__ __forceinline__ SymT<T> radialEvolution(const SymT<T>& Hi, T x, T y, T z, T s, T r0) {
   const T r1 = sqrt(x * x + y * y + z * z);
   T ux = T(1), uy = T(0), uz = T(0);   // GeomVector::unitVector
-  if (r1 > T(1.0e-50)) { ux = x / r1; uy = y / r1; uz = z / r1; }
+  if (r1 > T(sizeof(T) == 8 ? 1.0e-50 : 0.0)) { ux = x / r1; uy = y / r1; uz = z / r1; }   // 1e-50 is 0 in FP32
   T R[3][3];
   rotationMatrix3(ux, uy, uz, R);
   SymT<T> h = symRotate(Hi, R, false);
@@ -308,7 +308,7 @@ __device__ __forceinline__ SymT<T> asphClassicHideal(const SymT<T>& M2, bool m2P
                                                      bool fixShape, T hminInv, T hmaxInv, T hminratio,
                                                      bool radialOnly = false, T x = T(0), T y = T(0), T z = T(0),
                                                      T r0 = T(0)) {
-  const T tiny = T(1.0e-50);
+  const T tiny = T(sizeof(T) == 8 ? 1.0e-50 : 0.0);   // 1e-50 is 0 in FP32
   const T psiweight = fmax(T(0), fmin(T(1), T(2) / s - T(1)));
   SymT<T> Hid{T(1), T(0), T(0), T(1), T(0), T(1)};
   T ev[3], V[3][3], d[3];
