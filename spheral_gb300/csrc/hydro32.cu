@@ -855,10 +855,20 @@ void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, Nei
     if (variant & 1) pairKernelFP32<X, C, true, 4, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc); \
     else pairKernelFP32<X, C, true, 3, true, LQ, true><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);             \
   } while (0)
-  // ASPH (tensor H): pipelined, NodeList test at run time; odd variants cap
-  // the registers at 128 (4 blocks per SM, a few spills), even ones at 168
+  // ASPH (tensor H): NodeList test at run time; odd variants cap the
+  // registers at 128 (4 blocks per SM), even ones at 168 (3); variants 0-1
+  // the pipelined loop, 2-3 (compatible energy, no XSPH, standard Q) two
+  // slots per iteration
   if (hp.asph) {
-    if (hp.xsph) {
+    if (!hp.xsph && hp.compatible && !hp.limitedQ && variant >= 2) {
+      if (lean == 1) {
+        if (variant & 1) pairKernelFP32<false, true, true, 4, 2, false, true, 1><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, true, 3, 2, false, true, 1><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+      } else {
+        if (variant & 1) pairKernelFP32<false, true, true, 4, 2, false, true, 0><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+        else pairKernelFP32<false, true, true, 3, 2, false, true, 0><<<gb, b, 0, s>>>(F, F32, list, n, g, nl, t, hp, pacc);
+      }
+    } else if (hp.xsph) {
       if (hp.compatible) { if (hp.limitedQ) SPH_PAIR32T(true, true, true); else SPH_PAIR32T(true, true, false); }
       else { if (hp.limitedQ) SPH_PAIR32T(true, false, true); else SPH_PAIR32T(true, false, false); }
     } else {

@@ -70,7 +70,7 @@ void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl,
                     double* pacc, int blockSize, cudaStream_t s, LaunchCounter* lc);
 constexpr int kPairVariants = 4;   // autotuned variants of launchPairFP32 (common path)
 constexpr int kRetuneAfter = 2;    // uses between an autotuner's first timing and its one retiming
-constexpr int kPairVariantsTensor = 2;   // of its tensor-H (ASPH) path
+constexpr int kPairVariantsTensor = 4;   // of its tensor-H (ASPH) path
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);

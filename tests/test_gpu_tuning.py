@@ -13,7 +13,7 @@ the width, and the sweeps sum in list order whatever their batching.
 
 Problems: the Kelvin-Helmholtz box (isotropic H, FP64 and mixed mode; the
 pair variants also with the limited Q) and a stretched anisotropic box with
-reflecting walls (tensor H, mixed mode)."""
+reflecting walls (tensor H, mixed mode; search widths and pair variants)."""
 import numpy as np
 import pytest
 
@@ -70,7 +70,9 @@ def _kh_limited():
     return p
 
 
-@pytest.mark.parametrize("make", [lambda: problems.kelvin_helmholtz(n1=24), _kh_limited], ids=["mg", "limited_q"])
+@pytest.mark.parametrize("make", [lambda: problems.kelvin_helmholtz(n1=24), _kh_limited,
+                                  lambda: problems.stretched_box(seed=72, boundaries="reflecting")],
+                         ids=["mg", "limited_q", "asph_walls"])
 def test_pair_variant_does_not_change_results(native_lib, make):
     from spheral_gb300.engine import Engine
     _, nv = Engine.from_problem(make(), precision="fp32").pair_variant()
