@@ -748,49 +748,57 @@ void evalDerivs(sphgpu_ctx* c) {
     launchQGradient32(c->F, c->dvq.as<float4>(), c->n, c->stream, &c->lc);
     c->check();
   }
+  // Autotuner of the mixed pair kernels: time each variant (register budget,
+  // loop form) twice per problem size and again two uses later (the kernel
+  // is a pure function of its inputs and every variant gives the same bits,
+  // so the trial launches leave the results unchanged) and keep the fastest.
+  auto tunePair = [&](int nv, auto launch) {
+    ++c->pairEvals;
+    const bool retune = c->pairRetuneAt >= 0 && c->pairEvals >= c->pairRetuneAt;
+    if (c->pinnedVariant || !(c->pairVariant < 0 || c->tunedN != c->n || retune)) return;
+    cudaEvent_t e0, e1;
+    CUDA_OK(cudaEventCreate(&e0));
+    CUDA_OK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestV = 0;
+    for (int t = 0; t < 2 * nv; ++t) {   // two rounds, best time per variant
+      const int v = t % nv;
+      CUDA_OK(cudaEventRecord(e0, c->stream));
+      launch(v);
+      CUDA_OK(cudaEventRecord(e1, c->stream));
+      CUDA_OK(cudaEventSynchronize(e1));
+      c->check();
+      float ms = 0.f;
+      CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) { best = ms; bestV = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->pairVariant = bestV;
+    c->tunedN = c->n;
+    c->pairRetuneAt = retune ? -1 : c->pairEvals + kRetuneAfter;
+  };
   if (c->hp.crk && c->fp32()) {
     // RKCorrections::initialize, then CRKSPH::evaluateDerivatives, FP32 sweeps
     {
       Scope sc(c->prof, "rk_corrections");
       launchRKCorrectionsFP32(c->F, c->f32(), c->n, c->grid, c->nl(), c->tableDev(), c->hp, c->stream, &c->lc);
     }
+    auto crkPair = [&](int v) {
+      launchPairCRKFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
+                        c->pacc.as<float>(), v, c->stream, &c->lc);
+    };
+    tunePair(kPairVariantsCRK, crkPair);
     Scope sc(c->prof, "pair_crk");
-    launchPairCRKFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
-                      c->pacc.as<float>(), c->stream, &c->lc);
+    crkPair(c->pairVariant);
   } else if (c->fp32()) {
-    // Autotuner: time each register/occupancy variant of the pair kernel once
-    // per problem size (the kernel is a pure function of its inputs, so the
-    // trial launches leave the same results) and keep the fastest.
-    ++c->pairEvals;
-    const bool retune = c->pairRetuneAt >= 0 && c->pairEvals >= c->pairRetuneAt;
-    if (!c->pinnedVariant && (c->pairVariant < 0 || c->tunedN != c->n || retune)) {
-      cudaEvent_t e0, e1;
-      CUDA_OK(cudaEventCreate(&e0));
-      CUDA_OK(cudaEventCreate(&e1));
-      float best = 1e30f;
-      int bestV = 1;
-      const int nv = c->hp.asph ? kPairVariantsTensor : kPairVariants;
-      for (int t = 0; t < 2 * nv; ++t) {   // two rounds, best time per variant
-        const int v = t % nv;
-        CUDA_OK(cudaEventRecord(e0, c->stream));
-        launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
-                       c->pacc.as<float>(), v, c->stream, &c->lc);
-        CUDA_OK(cudaEventRecord(e1, c->stream));
-        CUDA_OK(cudaEventSynchronize(e1));
-        c->check();
-        float ms = 0.f;
-        CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) { best = ms; bestV = v; }
-      }
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      c->pairVariant = bestV;
-      c->tunedN = c->n;
-      c->pairRetuneAt = retune ? -1 : c->pairEvals + kRetuneAfter;
-    }
+    auto pair = [&](int v) {
+      launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
+                     c->pacc.as<float>(), v, c->stream, &c->lc);
+    };
+    tunePair(c->hp.asph ? kPairVariantsTensor : kPairVariants, pair);
     Scope sc(c->prof, "pair_fp32");
-    launchPairFP32(c->F, c->f32(), c->listp(), c->n, c->grid, c->nl(), c->tableDev(), c->hp,
-                   c->pacc.as<float>(), c->pairVariant, c->stream, &c->lc);
+    pair(c->pairVariant);
   } else if (c->hp.crk) {
     // RKCorrections::initialize (the integrator's initializeDerivatives) on
     // the state being evaluated, then CRKSPH::evaluateDerivatives
@@ -1675,7 +1683,10 @@ int sphgpu_get_neighbor_width(sphgpu_handle c, int* width) {
 int sphgpu_get_pair_variant(sphgpu_handle c, int* variant, int* nvariants) {
   API_BEGIN(c)
   if (variant) *variant = c->pairVariant;
-  if (nvariants) *nvariants = kPairVariants;
+  if (nvariants)
+    *nvariants = c->cfg.hydro == SPHGPU_HYDRO_CRKSPH
+                     ? kPairVariantsCRK
+                     : (c->cfg.smoothing_scale != SPHGPU_SMOOTHING_SPH ? kPairVariantsTensor : kPairVariants);
   API_END(c)
 }
 

@@ -351,7 +351,10 @@ __global__ void __launch_bounds__(128) rkCorrections32(Fields F, Fields32 P, lon
 //------------------------------------------------------------------------------
 // CRKSPH pair loop, FP32.
 //------------------------------------------------------------------------------
-template <bool XSPH, bool COMPAT, bool LIMQ>
+// U: neighbour slots per loop iteration (1, or 2 with both slots' gathers
+// issued together); the slots are evaluated in list order either way, so
+// both give the same bits.
+template <bool XSPH, bool COMPAT, bool LIMQ, int U = 1>
 __global__ void __launch_bounds__(128) pairKernelCRK32(Fields F, Fields32 P, const int* __restrict__ list, long n,
                                                        Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                                                        float* __restrict__ pacc) {
@@ -390,20 +393,18 @@ __global__ void __launch_bounds__(128) pairKernelCRK32(Fields F, Fields32 P, con
   for (int k = 0; k < 9; ++k) D[k] = 0.f;
 
   const int cnt = nl.count[i];
-  for (int q = 0; q < cnt; ++q) {
-    const long long slot = nbSlot(i, q, nl.cap);
-    const uint32_t ent = nl.nbr[slot];
+  // One neighbour slot (list slot `slot`, entry `ent`, node j's mirrors and
+  // corrections already gathered): its contributions to node i's sums.
+  auto pairSlot = [&](long long slot, uint32_t ent, const float4& pj, const float4& vj4, const float4& thj,
+                      float Vj, float* Cj) {
     const int j = (int)(ent & kIndexMask), dcode = (int)(ent >> kIndexBits);
     const uint32_t mq = (uint32_t)dcode & mm;
-    const float4 pj = P.posh[j], vj4 = P.velm[j], thj = P.thermo[j];
     float rx, ry, rz;
     relSepTab(pi, pj, dcode, mm, cx, cy, cz, sOff, rx, ry, rz);
     float vxj = vj4.x, vyj = vj4.y, vzj = vj4.z;
     mirrorVel(mq, vxj, vyj, vzj);
-    const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z, Vj = P.vol[j];
+    const float aj = pj.w, mj = vj4.w, rhoj = thj.x, Pj = thj.y, csj = thj.z;
     const bool same = multi ? (list[j] == li) : true;
-    float Cj[16];
-    loadRKC(P.rkc, j, Cj);
     mirrorRKC(mq, Cj);
 
     const float eix = ai * rx, eiy = ai * ry, eiz = ai * rz;
@@ -496,6 +497,30 @@ __global__ void __launch_bounds__(128) pairKernelCRK32(Fields F, Fields32 P, con
     const float fwW = fw * fabsf(Gi);
     m0 += fwW;
     m1x -= fwW * eix; m1y -= fwW * eiy; m1z -= fwW * eiz;
+  };
+  int q = 0;
+  if (U == 2) {
+    for (; q + 1 < cnt; q += 2) {
+      const long long s0 = nbSlot(i, q, nl.cap), s1 = s0 + 32;
+      const uint32_t e0 = nl.nbr[s0], e1 = nl.nbr[s1];
+      const int j0 = (int)(e0 & kIndexMask), j1 = (int)(e1 & kIndexMask);
+      const float4 p0 = P.posh[j0], v0 = P.velm[j0], t0 = P.thermo[j0];
+      const float4 p1 = P.posh[j1], v1 = P.velm[j1], t1 = P.thermo[j1];
+      const float V0 = P.vol[j0], V1 = P.vol[j1];
+      float C0[16], C1[16];
+      loadRKC(P.rkc, j0, C0);
+      loadRKC(P.rkc, j1, C1);
+      pairSlot(s0, e0, p0, v0, t0, V0, C0);
+      pairSlot(s1, e1, p1, v1, t1, V1, C1);
+    }
+  }
+  for (; q < cnt; ++q) {
+    const long long slot = nbSlot(i, q, nl.cap);
+    const uint32_t ent = nl.nbr[slot];
+    const int j = (int)(ent & kIndexMask);
+    float Cj[16];
+    loadRKC(P.rkc, j, Cj);
+    pairSlot(slot, ent, P.posh[j], P.velm[j], P.thermo[j], P.vol[j], Cj);
   }
   // node finalize: the sums leave as FP64 values, the per-node arithmetic is
   // FP32 (GB300's FP64 rate would make it visible next to the pair loop)
@@ -582,9 +607,16 @@ void launchRKCorrectionsFP32(Fields F, Fields32 P, long n, Grid g, NeighborLists
   lc->add(1);
 }
 void launchPairCRKFP32(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                       HydroParams hp, float* pacc, cudaStream_t s, LaunchCounter* lc) {
+                       HydroParams hp, float* pacc, int variant, cudaStream_t s, LaunchCounter* lc) {
   const unsigned gb = gridFor(n, 128);
 #define SPH_CRK32(X, C, Q) pairKernelCRK32<X, C, Q><<<gb, 128, 0, s>>>(F, P, list, n, g, nl, t, hp, pacc)
+  // variant 1: two slots per iteration (compatible energy, no XSPH)
+  if (variant == 1 && !hp.xsph && hp.compatible) {
+    if (hp.limitedQ) pairKernelCRK32<false, true, true, 2><<<gb, 128, 0, s>>>(F, P, list, n, g, nl, t, hp, pacc);
+    else pairKernelCRK32<false, true, false, 2><<<gb, 128, 0, s>>>(F, P, list, n, g, nl, t, hp, pacc);
+    lc->add(1);
+    return;
+  }
   if (hp.limitedQ) {
     if (hp.xsph) { if (hp.compatible) SPH_CRK32(true, true, true); else SPH_CRK32(true, false, true); }
     else { if (hp.compatible) SPH_CRK32(false, true, true); else SPH_CRK32(false, false, true); }

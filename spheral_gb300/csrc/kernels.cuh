@@ -71,6 +71,7 @@ void launchPairFP64(Fields F, const int* list, long n, Grid g, NeighborLists nl,
 constexpr int kPairVariants = 4;   // autotuned variants of launchPairFP32 (common path)
 constexpr int kRetuneAfter = 2;    // uses between an autotuner's first timing and its one retiming
 constexpr int kPairVariantsTensor = 4;   // of its tensor-H (ASPH) path
+constexpr int kPairVariantsCRK = 2;      // of the mixed CRKSPH pair kernel
 void launchPairFP32(Fields F, Fields32 F32, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
                     HydroParams hp, float* pacc, int variant, cudaStream_t s,
                     LaunchCounter* lc);
@@ -120,8 +121,10 @@ void launchCRKDensityFP32(Fields F, Fields32 P, const int* list, long n, Grid g,
                           HydroParams hp, cudaStream_t s, LaunchCounter* lc);
 void launchRKCorrectionsFP32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                              cudaStream_t s, LaunchCounter* lc);
+// variant: 0 one neighbour slot per loop iteration, 1 two (autotuned,
+// kPairVariantsCRK; the same bits either way)
 void launchPairCRKFP32(Fields F, Fields32 P, const int* list, long n, Grid g, NeighborLists nl, TableDev t,
-                       HydroParams hp, float* pacc, cudaStream_t s, LaunchCounter* lc);
+                       HydroParams hp, float* pacc, int variant, cudaStream_t s, LaunchCounter* lc);
 // ASPH: F_HINV / F_HLMAX <- smallest / largest eigenvalue of the tensor H
 void launchTensorExtent(Fields F, long n, cudaStream_t s, LaunchCounter* lc);
 // ASPH radialOnly: F_RAD0 <- |x|

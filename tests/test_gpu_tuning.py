@@ -12,8 +12,9 @@ bitwise the same: the search writes each list in candidate order whatever
 the width, and the sweeps sum in list order whatever their batching.
 
 Problems: the Kelvin-Helmholtz box (isotropic H, FP64 and mixed mode; the
-pair variants also with the limited Q) and a stretched anisotropic box with
-reflecting walls (tensor H, mixed mode; search widths and pair variants)."""
+pair variants also with the limited Q and under CRKSPH) and a stretched
+anisotropic box with reflecting walls (tensor H, mixed mode; search widths
+and pair variants)."""
 import numpy as np
 import pytest
 
@@ -70,9 +71,16 @@ def _kh_limited():
     return p
 
 
+def _kh_crksph():
+    p = problems.kelvin_helmholtz(n1=24, smooth=0.025)
+    p.config.update(hydro="crksph", rk_volume="sum", xsph=False, gradh_correction=False,
+                    viscosity="monaghan_gingold", Cl=1.0, Cq=1.0)
+    return p
+
+
 @pytest.mark.parametrize("make", [lambda: problems.kelvin_helmholtz(n1=24), _kh_limited,
-                                  lambda: problems.stretched_box(seed=72, boundaries="reflecting")],
-                         ids=["mg", "limited_q", "asph_walls"])
+                                  lambda: problems.stretched_box(seed=72, boundaries="reflecting"), _kh_crksph],
+                         ids=["mg", "limited_q", "asph_walls", "crksph"])
 def test_pair_variant_does_not_change_results(native_lib, make):
     from spheral_gb300.engine import Engine
     _, nv = Engine.from_problem(make(), precision="fp32").pair_variant()
