@@ -415,6 +415,8 @@ def run_ours(args, ws, rank, local, dist):
     eng = Engine.from_problem(prob, precision=args.precision, device=local)
     if args.search_width:
         eng.set_neighbor_width(args.search_width)
+    if args.pair_variant >= 0:
+        eng.set_pair_variant(args.pair_variant)
     eng.initialize()
     for _ in range(args.warmup):
         eng.step()
@@ -748,6 +750,8 @@ def main():
     ap.add_argument("--cpu1-steps", type=int, default=2)
     ap.add_argument("--search-width", type=int, default=0, choices=[0, 8, 16, 32],
                     help="pin the neighbour-search group width (0: autotuned)")
+    ap.add_argument("--pair-variant", type=int, default=-1,
+                    help="pin the mixed pair kernel's variant (-1: autotuned)")
     args = ap.parse_args()
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
