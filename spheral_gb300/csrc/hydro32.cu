@@ -572,7 +572,8 @@ __global__ void __launch_bounds__(128) densityDtKernel32(Fields F, Fields32 P, c
 //------------------------------------------------------------------------------
 // Grad-h correction, FP32 sums (computeSPHOmegaGradhCorrection.cc:15-116).
 //------------------------------------------------------------------------------
-template <bool TENSOR>
+// LEAN: compensated sums fixed at compile time.
+template <bool TENSOR, bool LEAN>
 __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long n, Grid g, NeighborLists nl,
                                                      TableDev t, HydroParams hp) {
   __shared__ float4 ta[kMaxTable / 3];
@@ -624,8 +625,8 @@ __global__ void __launch_bounds__(128) gradhKernel32(Fields F, Fields32 P, long 
     }
     float w, gr;
     lookupPacked(ta, tb, N1, invStep, eta, extent, w, gr);
-    sumAdd(ws, wc, w, hp.plainSums);
-    sumAdd(gs, gc, eta * gr, hp.plainSums);
+    sumAdd(ws, wc, w, LEAN ? 0 : hp.plainSums);
+    sumAdd(gs, gc, eta * gr, LEAN ? 0 : hp.plainSums);
   }
   // Omega = -sum eta dW/deta / (3 (sum W + W0)) (Hdet cancels), in FP32 from
   // the compensated sums
@@ -929,8 +930,13 @@ void launchSumDensityFP32(Fields F, Fields32 F32, const int* list, long n, Grid 
 
 void launchGradhFP32(Fields F, Fields32 F32, long n, Grid g, NeighborLists nl, TableDev t, HydroParams hp,
                      cudaStream_t s, LaunchCounter* lc) {
-  if (hp.asph) gradhKernel32<true><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
-  else gradhKernel32<false><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  if (hp.asph) {
+    if (hp.plainSums) gradhKernel32<true, false><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+    else gradhKernel32<true, true><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  } else {
+    if (hp.plainSums) gradhKernel32<false, false><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+    else gradhKernel32<false, true><<<gridFor(n, 128), 128, 0, s>>>(F, F32, n, g, nl, t, hp);
+  }
   lc->add(1);
 }
 
@@ -960,8 +966,10 @@ void launchDensityDtFP32(Fields F, Fields32 F32, const int* list, long n, Grid g
   const int nb = (int)gridFor(n, 128);
   // lean: one NodeList and compensated sums fixed at compile time
   const bool lean = hp.numLists == 1 && !hp.plainSums;
-  if (hp.asph) densityDtKernel32<true, false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
-  else if (lean) densityDtKernel32<false, true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  if (hp.asph) {
+    if (lean) densityDtKernel32<true, true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+    else densityDtKernel32<true, false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
+  } else if (lean) densityDtKernel32<false, true><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
   else densityDtKernel32<false, false><<<nb, 128, 0, s>>>(F, F32, list, n, g, nl, t, hp, maxNperh, dScratch);
   dtFinalKernel32<<<1, 256, 0, s>>>(dScratch, nb, dOut);
   lc->add(2);
