@@ -320,12 +320,15 @@ int sphgpu_timer_start(sphgpu_handle h);
 int sphgpu_timer_stop(sphgpu_handle h, double* ms);
 /* Ordered neighbour entries of the current lists (2x the unordered pairs). */
 int sphgpu_neighbor_count(sphgpu_handle h, long* entries);
-/* Mixed-mode pair kernel variant (register budget / software pipelining of
- * the neighbour loop).  By default (-1) the fastest of the variants is picked
- * by timing each once per problem size; sphgpu_set_pair_variant pins one
+/* Mixed-mode pair kernel variant (register budget and loop form: software
+ * pipelined, or two / four neighbour slots per iteration; the count depends
+ * on the configured hydro and smoothing scale).  By default (-1) the fastest
+ * is picked by timing each at the first evaluation for a problem size and
+ * again two evaluations later; sphgpu_set_pair_variant pins one
  * (0 .. *nvariants-1 from sphgpu_get_pair_variant), or -1 to re-enable the
- * autotuner.  sphgpu_get_pair_variant returns the variant in use (-1 before
- * the first mixed-mode evaluation).  No reference counterpart (tuning only). */
+ * autotuner.  Every variant gives the same bits.  sphgpu_get_pair_variant
+ * returns the variant in use (-1 before the first mixed-mode evaluation).
+ * No reference counterpart (tuning only). */
 int sphgpu_set_pair_variant(sphgpu_handle h, int variant);
 int sphgpu_get_pair_variant(sphgpu_handle h, int* variant, int* nvariants);
 /* Lanes per work group of the neighbour search (8, 16 or 32), picked by
